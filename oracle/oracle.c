@@ -1,0 +1,1212 @@
+/*
+ * oracle.c -- CPU restatement of uavs3e's mode-decision kernels (8-bit luma).
+ *
+ * TEST INFRASTRUCTURE ONLY (see oracle.h).  Each function cites the reference function whose
+ * algorithm it restates; file:line are relative to the uavs3e source tree.  The code is
+ * written for clarity, not speed, except where a batched workload would otherwise not
+ * finish in seconds (those loops use OpenMP).
+ */
+#include "oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MIN(a, b) ((a) < (b) ? (a) : (b))
+#define MAX(a, b) ((a) > (b) ? (a) : (b))
+#define CLIP3(lo, hi, v) MAX((lo), MIN((hi), (v)))
+#define ABSI(a) ((a) < 0 ? -(a) : (a))
+
+static int ilog2(int v) { int r = 0; while ((1 << (r + 1)) <= v) r++; return r; }
+
+/* =============================================================================== tables */
+
+/* 8-tap luma / 4-tap chroma quarter/eighth-sample filters, src/com_tables.c:149-154,191-200 */
+static const s8 MC_L[4][8] = {
+    { 0, 0, 0, 64, 0, 0, 0, 0 },
+    { -1, 4, -10, 57, 19, -7, 3, -1 },
+    { -1, 4, -11, 40, 40, -11, 4, -1 },
+    { -1, 3, -7, 19, 57, -10, 4, -1 },
+};
+static const s8 MC_C[8][4] = {
+    { 0, 64, 0, 0 }, { -4, 62, 6, 0 }, { -6, 56, 15, -1 }, { -5, 47, 25, -3 },
+    { -4, 36, 36, -4 }, { -3, 25, 47, -5 }, { -1, 15, 56, -6 }, { 0, 6, 62, -4 },
+};
+
+/* intra angle steps {multiplier, shift}: [0] along x for row offsets, [1] along y for column
+ * offsets; src/com_tables.c:402-423 */
+static const s8 DIR_DXDY[2][33][2] = {
+    { {0,0},{0,0},{0,0},{11,2},{2,0},{11,3},{1,0},{93,7},{1,1},{93,8},{1,2},{1,3},{0,0},{1,3},{1,2},
+      {93,8},{1,1},{93,7},{1,0},{11,3},{2,0},{11,2},{4,0},{8,0},{0,0},{8,0},{4,0},{11,2},{2,0},{11,3},
+      {1,0},{93,7},{1,1} },
+    { {0,0},{0,0},{0,0},{93,8},{1,1},{93,7},{1,0},{11,3},{2,0},{11,2},{4,0},{8,0},{0,0},{8,0},{4,0},
+      {11,2},{2,0},{11,3},{1,0},{93,7},{1,1},{93,8},{1,2},{1,3},{0,0},{1,3},{1,2},{93,8},{1,1},{93,7},
+      {1,0},{11,3},{2,0} },
+};
+
+/* intra prediction filter weights per block-size class, src/com_ipred.c:607-613 */
+static const u8 IPF_PARAM[5][10] = {
+    { 24, 6, 2, 0, 0, 0, 0, 0, 0, 0 },
+    { 44, 25, 14, 8, 4, 2, 1, 1, 0, 0 },
+    { 40, 27, 19, 13, 9, 6, 4, 3, 2, 1 },
+    { 36, 27, 21, 16, 12, 9, 7, 5, 4, 3 },
+    { 52, 44, 37, 31, 26, 22, 18, 15, 13, 11 },
+};
+
+/* quantiser scale per QP, src/quant.c:56-67 */
+static const u16 Q_SCALE[80] = {
+    16302, 15024, 13777, 12634, 11626, 10624, 9742, 8958, 8192, 7512, 6889, 6305, 5793, 5303, 4878, 4467,
+    4091, 3756, 3444, 3161, 2894, 2654, 2435, 2235, 2048, 1878, 1722, 1579, 1449, 1329, 1218, 1117,
+    1024, 939, 861, 790, 724, 664, 609, 558, 512, 470, 430, 395, 362, 332, 304, 279,
+    256, 235, 215, 197, 181, 166, 152, 140, 128, 116, 108, 99, 91, 83, 76, 69,
+    64, 59, 54, 49, 45, 41, 38, 35, 32, 30, 27, 25, 23, 21, 19, 18,
+};
+/* dequantiser scale and shift per QP, src/com_itdq.c:770-793 */
+static const u32 DQ_SCALE[80] = {
+    32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424, 32932, 35734, 38968, 42495, 46177, 50535, 55109, 59933,
+    65535, 35734, 38968, 42577, 46341, 50617, 55027, 60097, 32809, 35734, 38968, 42454, 46382, 50576, 55109, 60056,
+    65535, 35734, 38968, 42495, 46320, 50515, 55109, 60076, 65535, 35744, 38968, 42495, 46341, 50535, 55099, 60087,
+    65535, 35734, 38973, 42500, 46341, 50535, 55109, 60097, 32771, 35734, 38965, 42497, 46341, 50535, 55109, 60099,
+    32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424, 32932, 35734, 38968, 42495, 46177, 50535, 55109, 59933,
+};
+static const u8 DQ_SHIFT[80] = {
+    14, 14, 14, 14, 14, 14, 14, 14, 13, 13, 13, 13, 13, 13, 13, 13, 13, 12, 12, 12, 12, 12, 12, 12,
+    11, 11, 11, 11, 11, 11, 11, 11, 11, 10, 10, 10, 10, 10, 10, 10, 10, 9, 9, 9, 9, 9, 9, 9,
+    9, 8, 8, 8, 8, 8, 8, 8, 7, 7, 7, 7, 7, 7, 7, 7, 6, 6, 6, 6, 6, 6, 6, 6, 5, 5, 5, 5, 5, 5, 5, 5,
+};
+/* 4x4 alternative transform and 8x8 secondary transform kernels, src/com_tables.c:98-110 */
+static const s8 C4_TRANS[4][4] = { { 34, 58, 72, 81 }, { 77, 69, -7, -75 }, { 79, -33, -75, 58 }, { 55, -84, 73, -28 } };
+static const s8 C8_TRANS[4][4] = { { 123, -35, -8, -3 }, { -32, -120, 30, 10 }, { 14, 25, 123, -22 }, { 8, 13, 19, 126 } };
+
+static s8   DCT_TM[7][3 * 64 * 64];     /* [log2n][type][k][n] */
+static int  DCT2_FOLD[7][64 * 64];       /* effective DCT2 matrix of the partial butterflies */
+static int  DCT87_EFF[2][7][64 * 64];    /* effective DCT8 / DST7 matrices */
+static u16 *SCAN[7][7];
+static s32  RDOQ_ERR_SCALE[80][6];
+static double TBL_SQRT[2];
+static int  g_init = 0;
+
+/* DCT2 / DCT8 / DST7 integer matrices: s = sqrt(N)*32 times the orthonormal basis, rounded
+ * half away from zero; src/com_tables.c:222-278 */
+static void build_dct_tables(void)
+{
+    const double PI = 3.14159265358979323846;
+    for (int L = 1; L <= 6; L++) {
+        int c = 1 << L;
+        double s = sqrt((double)c) * 32;
+        s8 *T = DCT_TM[L];
+        for (int k = 0; k < c; k++) {
+            for (int n = 0; n < c; n++) {
+                double w0 = k == 0 ? sqrt(0.5) : 1;
+                double v = cos(PI * (n + 0.5) * k / c) * w0 * sqrt(2.0 / c);
+                T[0 * c * c + k * c + n] = (s8)(s * v + (v > 0 ? 0.5 : -0.5));
+                v = cos(PI * (k + 0.5) * (n + 0.5) / (c + 0.5)) * sqrt(2.0 / (c + 0.5));
+                T[1 * c * c + k * c + n] = (s8)(s * v + (v > 0 ? 0.5 : -0.5));
+                v = sin(PI * (k + 0.5) * (n + 1) / (c + 0.5)) * sqrt(2.0 / (c + 0.5));
+                T[2 * c * c + k * c + n] = (s8)(s * v + (v > 0 ? 0.5 : -0.5));
+            }
+        }
+    }
+    TBL_SQRT[0] = sqrt(4.0 * 8.0);
+    TBL_SQRT[1] = sqrt(16.0 * 8.0);
+}
+
+/*
+ * The reference's DCT2 butterflies (src/transform.c:57-251 forward, src/com_itdq.c:47-262
+ * inverse) read only the first N/2^(l+1) entries of each matrix row and rebuild the rest from
+ * the even/odd symmetry.  This computes the matrix they effectively apply, by running the
+ * even/odd decomposition on unit vectors: row k uses the difference vector of level ctz(k)+1,
+ * rows 0 and N/2 the final 2-entry sum vector.  With exact integer arithmetic (and mod-2^32
+ * wrap-around) the matrix form gives the butterfly's results bit for bit.
+ */
+static void build_dct2_fold(void)
+{
+    for (int L = 2; L <= 6; L++) {
+        int N = 1 << L;
+        const s8 *tm = DCT_TM[L];
+        int *F = DCT2_FOLD[L];
+        for (int n = 0; n < N; n++) {
+            int S[7][64], D[7][64];
+            for (int i = 0; i < N; i++) S[0][i] = i == n;
+            for (int l = 1; l < L; l++) {
+                int len = N >> (l - 1);
+                for (int i = 0; i < len / 2; i++) {
+                    S[l][i] = S[l - 1][i] + S[l - 1][len - 1 - i];
+                    D[l][i] = S[l - 1][i] - S[l - 1][len - 1 - i];
+                }
+            }
+            for (int k = 0; k < N; k++) {
+                const int *V; int len;
+                if (k == 0 || k == N / 2) { V = S[L - 1]; len = 2; }
+                else { int j = __builtin_ctz(k); V = D[j + 1]; len = N >> (j + 1); }
+                int acc = 0;
+                for (int i = 0; i < len; i++) acc += tm[k * N + i] * V[i];
+                F[k * N + n] = acc;
+            }
+        }
+    }
+}
+
+/* effective DCT8 (t=0) / DST7 (t=1) matrices: the 4-point kernels use fast forms built from
+ * row 0 of the table (src/transform.c:416-432, 545-562; inverse src/com_itdq.c:428-452,
+ * 543-566); larger sizes use the table as is. */
+static void build_dct87(void)
+{
+    for (int L = 2; L <= 6; L++) {
+        int N = 1 << L;
+        for (int t = 0; t < 2; t++) {
+            const s8 *tab = DCT_TM[L] + (t == 0 ? 1 : 2) * N * N;
+            int *M = DCT87_EFF[t][L];
+            if (N == 4) {
+                int a = tab[0], b = tab[1], c = tab[2], d = tab[3];
+                if (t == 0) {       /* DCT8 fast form uses b, c, d of row 0 */
+                    int r[4][4] = { { c + d, b, c, d }, { b, 0, -b, -b }, { c, -b, -d, c + d }, { d, -b, c + d, -c } };
+                    memcpy(M, r, sizeof(r));
+                } else {            /* DST7 fast form uses a, b, c of row 0 */
+                    int r[4][4] = { { a, b, c, a + b }, { c, c, 0, -c }, { a + b, -a, -c, b }, { b, -(a + b), c, -a } };
+                    memcpy(M, r, sizeof(r));
+                }
+            } else {
+                for (int i = 0; i < N * N; i++) M[i] = tab[i];
+            }
+        }
+    }
+}
+
+/* zig-zag scan, src/com_util.c:1220-1268 */
+static void build_scan(void)
+{
+    for (int ly = 1; ly <= 6; ly++) {
+        for (int lx = 1; lx <= 6; lx++) {
+            int sx = 1 << lx, sy = 1 << ly;
+            u16 *s = (u16 *)malloc(sizeof(u16) * sx * sy);
+            int pos = 0;
+            s[pos++] = 0;
+            for (int l = 1; l < sx + sy - 1; l++) {
+                if (l & 1) {
+                    int x = MIN(l, sx - 1), y = MAX(0, l - (sx - 1));
+                    for (; x >= 0 && y < sy; x--, y++) s[pos++] = (u16)(y * sx + x);
+                } else {
+                    int y = MIN(l, sy - 1), x = MAX(0, l - (sy - 1));
+                    for (; y >= 0 && x < sx; x++, y--) s[pos++] = (u16)(y * sx + x);
+                }
+            }
+            SCAN[lx][ly] = s;
+        }
+    }
+}
+
+/* RDOQ error scale, src/quant.c:69-83 (8-bit) */
+static void build_rdoq(void)
+{
+    for (int qp = 0; qp < 80; qp++) {
+        for (int i = 0; i < 6; i++) {
+            int tr_shift = 15 - 8 - (i + 1);
+            double e = pow(2.0, 15 - tr_shift);
+            e = e / Q_SCALE[qp] / 1;
+            RDOQ_ERR_SCALE[qp][i] = (s32)(e * (double)(1 << 20));
+        }
+    }
+}
+
+void orc_init(void)
+{
+    if (g_init) return;
+    build_dct_tables();
+    build_dct2_fold();
+    build_dct87();
+    build_scan();
+    build_rdoq();
+    g_init = 1;
+}
+
+const s8 *orc_dct_table(int log2n) { orc_init(); return DCT_TM[log2n]; }
+const u16 *orc_scan(int log2w, int log2h) { orc_init(); return SCAN[log2w][log2h]; }
+const s8 *orc_mc_luma_coef(void) { return &MC_L[0][0]; }
+const s8 *orc_mc_chroma_coef(void) { return &MC_C[0][0]; }
+u16 orc_quant_scale(int qp) { return Q_SCALE[qp]; }
+u32 orc_dq_scale(int qp) { return DQ_SCALE[qp]; }
+u32 orc_dq_shift(int qp) { return DQ_SHIFT[qp]; }
+s32 orc_rdoq_err_scale(int qp, int i) { orc_init(); return RDOQ_ERR_SCALE[qp][i]; }
+double orc_tbl_sqrt(int i) { orc_init(); return TBL_SQRT[i]; }
+
+/* MV-bits table (exp-Golomb-like lengths): tab[0]=1, |v| in [2^(e-1)-1, 2^e-2] -> 2e bits;
+ * src/inter.c:2029-2057.  tab points at 2*offset+1 entries; the centre is tab[offset]. */
+void orc_mvbits_table(u8 *tab, int offset)
+{
+    u8 *c = tab + offset;
+    memset(tab, 0, (size_t)(2 * offset + 1));
+    c[0] = 1;
+    c[-1] = c[1] = 2;
+    c[-2] = c[2] = 3;
+    for (int e = 2;; e++) {
+        int imax = MIN((1 << e) - 1, offset), imin = (1 << (e - 1)) - 1;
+        for (int i = imin; i < imax; i++) c[-i] = c[i] = (u8)(e << 1);
+        if (imax == offset) break;
+    }
+}
+
+/* ================================================================================ costs */
+
+/* DEFINE_SAD / DEFINE_SSD, src/com_cost.c:40-58, 117-137 */
+u32 orc_sad(int w, int h, const pel *o, int io, const pel *p, int ip)
+{
+    u32 s = 0;
+    for (int y = 0; y < h; y++, o += io, p += ip)
+        for (int x = 0; x < w; x++) s += (u32)ABSI(o[x] - p[x]);
+    return s;
+}
+
+u64 orc_ssd(int w, int h, const pel *o, int io, const pel *p, int ip)
+{
+    u64 s = 0;
+    for (int y = 0; y < h; y++, o += io, p += ip)
+        for (int x = 0; x < w; x++) { int d = o[x] - p[x]; s += (u64)(d * d); }
+    return s;
+}
+
+/* in-place Walsh-Hadamard transform of n values with the given stride */
+static void wht(int *v, int n, int stride)
+{
+    for (int h = 1; h < n; h <<= 1)
+        for (int i = 0; i < n; i += h << 1)
+            for (int j = i; j < i + h; j++) {
+                int a = v[j * stride], b = v[(j + h) * stride];
+                v[j * stride] = a + b;
+                v[(j + h) * stride] = a - b;
+            }
+}
+
+/*
+ * Hadamard SATD of one tw x th tile, com_had_4x4/8x8/16x8/8x16/8x4/4x8
+ * (src/com_cost.c:176-710).  Those functions apply complete 2-D Walsh-Hadamard transforms
+ * whose butterfly order only permutes and negates outputs, so the sum of magnitudes equals
+ * that of any WHT ordering.  Normalisation: 4x4 (s+1)>>1, 8x8 (s+2)>>2, 16x8/8x16 and
+ * 8x4/4x8 (int)(s / sqrt(tw*th) * 2.0) in double.
+ */
+u32 orc_satd_tile(int tw, int th, const pel *o, int io, const pel *p, int ip)
+{
+    orc_init();
+    int d[128];
+    for (int y = 0; y < th; y++)
+        for (int x = 0; x < tw; x++) d[y * tw + x] = o[y * io + x] - p[y * ip + x];
+    for (int y = 0; y < th; y++) wht(d + y * tw, tw, 1);
+    for (int x = 0; x < tw; x++) wht(d + x, th, tw);
+    int s = 0;
+    for (int i = 0; i < tw * th; i++) s += ABSI(d[i]);
+    if (tw == 4 && th == 4) return (u32)((s + 1) >> 1);
+    if (tw == 8 && th == 8) return (u32)((s + 2) >> 2);
+    if (tw * th == 128) return (u32)(int)(s / TBL_SQRT[1] * 2.0);
+    return (u32)(int)(s / TBL_SQRT[0] * 2.0);
+}
+
+/* com_had tiling by block shape, src/com_cost.c:712-812 */
+u32 orc_had(int w, int h, const pel *o, int io, const pel *p, int ip, int bd)
+{
+    int shift = bd - 8, tw, th;
+    if (w == h) {
+        if (w == 4) return orc_satd_tile(4, 4, o, io, p, ip) >> shift;
+        tw = 8; th = 8;
+    } else if (w > h) {
+        if (h == 4 || (h & 7)) { tw = 8; th = 4; }
+        else { tw = 16; th = 8; }
+    } else {
+        if (w == 4 || (w & 7)) { tw = 4; th = 8; }
+        else { tw = 8; th = 16; }
+    }
+    /* 12-wide blocks (w & 7, w != 4) use three 4x8 columns per 8 rows: covered by the
+     * generic tiling below since 12 = 3 * 4 */
+    int sum = 0;
+    for (int y = 0; y < h; y += th)
+        for (int x = 0; x < w; x += tw)
+            sum += (int)orc_satd_tile(tw, th, o + y * io + x, io, p + y * ip + x, ip);
+    return (u32)(sum >> shift);
+}
+
+/* calc_satd_intra, src/util.c:200-229: power-of-two sides go to com_had, 12/24/48 sides are
+ * split into three equal segments */
+u32 orc_satd_intra(int w, int h, const pel *o, const pel *p, int io, int ip, int bd)
+{
+    int sw = w, sh = h, nw = 1, nh = 1;
+    if (w & (w - 1)) { nw = 3; sw = w / 3; }
+    if (h & (h - 1)) { nh = 3; sh = h / 3; }
+    if (nw == 1 && nh == 1) return orc_had(w, h, o, io, p, ip, bd);
+    u32 c = 0;
+    for (int j = 0; j < nh; j++)
+        for (int i = 0; i < nw; i++)
+            c += orc_had(sw, sh, o + sw * i + sh * j * io, io, p + sw * i + sh * j * ip, ip, bd);
+    return c;
+}
+
+/* ==================================================================================== MC */
+
+/* mc_if_cpy, src/com_mc.c:645-654 */
+void orc_ipcpy(const pel *s, int is, pel *d, int id, int w, int h)
+{
+    for (int y = 0; y < h; y++, s += is, d += id) memcpy(d, s, (size_t)w);
+}
+
+/* separable one-dimensional filters: type 0 = 8-tap horizontal, 1 = 4-tap horizontal,
+ * 2 = 8-tap vertical, 3 = 4-tap vertical; (sum + 32) >> 6 clipped to [0, max_val].
+ * mc_if_hor_luma / mc_if_ver_luma / mc_if_hor_chroma / mc_if_ver_chroma,
+ * src/com_mc.c:461-491, 553-583 */
+void orc_ipflt(int type, const pel *s, int is, pel *d, int id, int w, int h, const s8 *c, int max_val)
+{
+    int taps = (type == 0 || type == 2) ? 8 : 4;
+    int step = (type >= 2) ? is : 1;
+    int back = taps / 2 - 1;
+    for (int y = 0; y < h; y++, s += is, d += id)
+        for (int x = 0; x < w; x++) {
+            int sum = 0;
+            for (int t = 0; t < taps; t++) sum += s[x + (t - back) * step] * c[t];
+            d[x] = (pel)CLIP3(0, max_val, (sum + 32) >> 6);
+        }
+}
+
+/* two-pass filters: horizontal into s16 rows (8-bit: no rounding shift), then vertical with
+ * (sum + 2048) >> 12; type 0 = 8-tap luma, 1 = 4-tap chroma.  mc_if_hor_ver_luma /
+ * mc_if_hor_ver_chroma, src/com_mc.c:493-551, 585-643 */
+void orc_ipflt_ext(int type, const pel *s, int is, pel *d, int id, int w, int h, const s8 *cx, const s8 *cy, int max_val)
+{
+    int taps = type == 0 ? 8 : 4, back = taps / 2 - 1;
+    int shift1 = max_val == 255 ? 0 : 2, shift2 = max_val == 255 ? 12 : 10;
+    int add1 = (1 << shift1) >> 1, add2 = 1 << (shift2 - 1);
+    int rows = h + taps - 1;
+    s16 *tmp = (s16 *)malloc(sizeof(s16) * (size_t)rows * w);
+    const pel *sp = s - back * is;
+    for (int r = 0; r < rows; r++, sp += is)
+        for (int x = 0; x < w; x++) {
+            int sum = 0;
+            for (int t = 0; t < taps; t++) sum += sp[x + t - back] * cx[t];
+            tmp[r * w + x] = (s16)(shift1 ? (sum + add1) >> shift1 : sum);
+        }
+    for (int y = 0; y < h; y++, d += id)
+        for (int x = 0; x < w; x++) {
+            int sum = 0;
+            for (int t = 0; t < taps; t++) sum += tmp[(y + t) * w + x] * cy[t];
+            d[x] = (pel)CLIP3(0, max_val, (sum + add2) >> shift2);
+        }
+    free(tmp);
+}
+
+/* com_img_padding(img, 1, 4) on one plane, src/com_util.c:103-160: the region
+ * [-4, W+4) x [-4, H+4) is replicated outward to the full padding */
+static void pad_plane4(pel *p0, int width, int height, int pad, int stride)
+{
+    int ext = pad - 4, rw = width + 8, rh = height + 8;
+    pel *a = p0 - 4 * stride - 4;
+    for (int y = 0; y < rh; y++) {
+        pel *row = a + y * stride;
+        memset(row - ext, row[0], (size_t)ext);
+        memset(row + rw, row[rw - 1], (size_t)ext);
+    }
+    for (int y = 1; y <= ext; y++) memcpy(a - ext - y * stride, a - ext, (size_t)stride);
+    for (int y = 1; y <= ext; y++) memcpy(a + (rh - 1 + y) * stride - ext, a + (rh - 1) * stride - ext, (size_t)stride);
+}
+
+/*
+ * com_if_luma_frame, src/com_mc.c:760-800 (8-bit):
+ *   horizontal phases (0,dx) over [-8, W+8) x [-8, H+8): clip((t + 32) >> 6), t kept as s16;
+ *   vertical phases (dy,0) from the integer plane over [-4, W+4) x [-4, H+4);
+ *   diagonal phases (dy,dx) from the s16 rows: clip((sum + 2048) >> 12);
+ *   then every fractional plane is edge-padded from its [-4, W+4) x [-4, H+4) region.
+ */
+void orc_if_luma_frame(pel *plane0, pel **planes15, int width, int height, int pad, int stride)
+{
+    int tw = width + 16, th = height + 16;
+    s16 *tmp[3];
+    for (int i = 0; i < 3; i++) tmp[i] = (s16 *)malloc(sizeof(s16) * (size_t)tw * th);
+    for (int y = -8; y < height + 8; y++) {
+        const pel *s = plane0 + y * stride;
+        for (int x = -8; x < width + 8; x++)
+            for (int f = 1; f <= 3; f++) {
+                int t = 0;
+                for (int k = 0; k < 8; k++) t += s[x + k - 3] * MC_L[f][k];
+                tmp[f - 1][(y + 8) * tw + x + 8] = (s16)t;
+                planes15[f - 1][y * stride + x] = (pel)CLIP3(0, 255, (t + 32) >> 6);
+            }
+    }
+    for (int y = -4; y < height + 4; y++)
+        for (int x = -4; x < width + 4; x++)
+            for (int f = 1; f <= 3; f++) {
+                int t = 0;
+                for (int k = 0; k < 8; k++) t += plane0[(y + k - 3) * stride + x] * MC_L[f][k];
+                planes15[f * 4 - 1][y * stride + x] = (pel)CLIP3(0, 255, (t + 32) >> 6);
+            }
+    for (int dx = 1; dx <= 3; dx++)
+        for (int y = -4; y < height + 4; y++)
+            for (int x = -4; x < width + 4; x++)
+                for (int dy = 1; dy <= 3; dy++) {
+                    int t = 0;
+                    for (int k = 0; k < 8; k++) t += tmp[dx - 1][(y + k - 3 + 8) * tw + x + 8] * MC_L[dy][k];
+                    planes15[dy * 4 + dx - 1][y * stride + x] = (pel)CLIP3(0, 255, (t + 2048) >> 12);
+                }
+    for (int i = 0; i < 15; i++) pad_plane4(planes15[i], width, height, pad, stride);
+    for (int i = 0; i < 3; i++) free(tmp[i]);
+}
+
+/* ================================================================================ pel ops */
+
+/* DEFINE_DIFF / DEFINE_AVRG / com_recon, src/com_util.c:3068-3129 */
+void orc_pel_diff(int w, int h, const pel *o, int io, const pel *p, int ip, s16 *r, int ir)
+{
+    for (int y = 0; y < h; y++, o += io, p += ip, r += ir)
+        for (int x = 0; x < w; x++) r[x] = (s16)(o[x] - p[x]);
+}
+
+void orc_pel_avrg(int w, int h, pel *d, int id, const pel *s1, const pel *s2)
+{
+    for (int y = 0; y < h; y++, d += id, s1 += w, s2 += w)
+        for (int x = 0; x < w; x++) d[x] = (pel)((s1[x] + s2[x] + 1) >> 1);
+}
+
+void orc_recon(const s16 *resi, const pel *pred, int ipred, int w, int h, pel *rec, int irec, int cbf, int bd)
+{
+    int mx = (1 << bd) - 1;
+    for (int y = 0; y < h; y++, pred += ipred, rec += irec)
+        for (int x = 0; x < w; x++) rec[x] = cbf ? (pel)CLIP3(0, mx, resi[y * w + x] + pred[x]) : pred[x];
+}
+
+/* ================================================================================= intra */
+
+/* com_intra_get_nbr (luma), src/com_ipred.c:40-112.  nb_out[ORC_NEIB_MID] is the corner,
+ * +1.. the top row (then the top-right run), -1.. the left column (then bottom-left run);
+ * extensions stop at the first SCU whose "coded" flag is clear and are padded with the last
+ * sample; unavailable sides take 1 << (bd-1). */
+void orc_intra_get_nbr(int x, int y, int w, int h, const pel *src, int s_src, const pel *top, int lcu_size, int avail,
+                       pel *nb_out, int scup, const u8 *coded, int i_scu, int bd)
+{
+    int wsc = w >> 2, hsc = h >> 2, unit = 4, i;
+    const pel *srcT = (y % lcu_size == 0) ? top : src - s_src;
+    const pel *srcTL = srcT - 1, *srcL = src - 1;
+    pel *dst = nb_out + ORC_NEIB_MID;
+    int def = 1 << (bd - 1);
+    int range = MAX(w, h) * 4 + 4;
+    (void)x;
+    if (avail & 1) {                                   /* AVAIL_UP */
+        pel *up = dst + 1;
+        const pel *t = srcT;
+        memcpy(up, t, (size_t)w);
+        up += w; t += w;
+        const u8 *m = coded + scup - i_scu + wsc;
+        for (i = 0; i < wsc; i++, up += unit, t += unit) {
+            if (!m[i]) break;
+            memcpy(up, t, (size_t)unit);
+        }
+        memset(up, up[-1], (size_t)(range - (w + i * unit)));
+    } else {
+        memset(dst + 1, def, (size_t)range);
+    }
+    if (avail & 2) {                                   /* AVAIL_LE */
+        pel *left = dst - 1;
+        const pel *s = srcL;
+        for (i = 0; i < h; i++, s += s_src) *left-- = *s;
+        const u8 *m = coded + scup - 1 + hsc * i_scu;
+        for (i = 0; i < hsc; i++) {
+            if (!m[i * i_scu]) break;
+            for (int j = 0; j < unit; j++, s += s_src) *left-- = *s;
+        }
+        int pads = range - h - i * unit;
+        memset(left - pads + 1, left[1], (size_t)pads);
+    } else {
+        memset(dst - range, def, (size_t)range);
+    }
+    if (avail & 4) dst[0] = srcTL[0];                   /* AVAIL_UP_LE */
+    else if (avail & 1) dst[0] = srcTL[1];
+    else if (avail & 2) dst[0] = srcL[0];
+    else dst[0] = (pel)def;
+}
+
+static int ang_ctx(int mode, int xy, int d, int *off)
+{
+    int mult = DIR_DXDY[xy][mode][0], sh = DIR_DXDY[xy][mode][1];
+    int dn = d * mult >> sh;
+    *off = ((d * mult * 32) >> sh) - dn * 32;
+    return dn;
+}
+
+static inline int f4(int p0, int p1, int p2, int p3, int off)
+{
+    return (p0 * (32 - off) + p1 * (64 - off) + p2 * (32 + off) + p3 * off + 64) >> 7;
+}
+
+/*
+ * Angular prediction as installed in the C kernel table (src/com_ipred.c:1647-1693):
+ *   modes 3..11: ipred_ang_x (:844), whose row reads stop at 2w (the specialisations for
+ *     4/6/8 match it; mode 10's ipred_ang_x_10 does not clamp);
+ *   modes 12..23: ipred_ang_xy (:1138) (the specialisations 13..23 match it);
+ *   modes 24..32: xPredIntraAngAdi_Y (:1003), whose column reads stop at -2h (mode 26's
+ *     specialisation does not clamp; mode 32 follows xPredIntraAngAdi_Y_32 (:1103) which
+ *     pads its two filtered lines after min(h/2+w-1, h) entries).
+ * s points at the neighbour-array centre.
+ */
+static void ang_core(const pel *s, pel *dst, int i_dst, int mode, int w, int h)
+{
+    if (mode < 12) {
+        for (int j = 0; j < h; j++, dst += i_dst) {
+            int off, idx = ang_ctx(mode, 0, j + 1, &off);
+            int pw = mode == 10 ? w : MIN(w, 2 * w - idx + 1);
+            int i;
+            for (i = 0; i < pw; i++) {
+                const pel *p = s + idx + i;
+                dst[i] = (pel)f4(p[0], p[1], p[2], p[3], off);
+            }
+            if (pw <= 0) {
+                dst[0] = (pel)f4(s[2 * w], s[2 * w + 1], s[2 * w + 2], s[2 * w + 3], off);
+                pw = 1;
+            }
+            for (; i < w; i++) dst[i] = dst[pw - 1];
+        }
+    } else if (mode < 24) {
+        for (int j = 0; j < h; j++, dst += i_dst) {
+            int ox, ix = ang_ctx(mode, 0, j + 1, &ox);
+            for (int i = 0; i < w; i++) {
+                int oy, xs = ang_ctx(mode, 1, i + 1, &oy);
+                int yy = j - xs;
+                if (yy <= -1) {
+                    const pel *px = s - ix + i;
+                    dst[i] = (pel)((px[2] * (32 - ox) + px[1] * (64 - ox) + px[0] * (32 + ox) + px[-1] * ox + 64) >> 7);
+                } else {
+                    dst[i] = (pel)((s[-yy - 2] * (32 - oy) + s[-yy - 1] * (64 - oy) + s[-yy] * (32 + oy) + s[-yy + 1] * oy + 64) >> 7);
+                }
+            }
+        }
+    } else if (mode == 32) {
+        int rs = MIN(h / 2 + w - 1, h);
+        int padv = (s[-1 - 2 * rs] + 2 * s[-2 - 2 * rs] + s[-3 - 2 * rs] + 2) >> 2;
+        for (int j = 0; j < h; j++, dst += i_dst)
+            for (int i = 0; i < w; i++) {
+                int n = (j >> 1) + i;
+                if (n >= rs) { dst[i] = (pel)padv; continue; }
+                int b = (j & 1) ? -3 - 2 * n : -2 - 2 * n;
+                dst[i] = (pel)((s[b] + 2 * s[b - 1] + s[b - 2] + 2) >> 2);
+            }
+    } else {
+        for (int j = 0; j < h; j++, dst += i_dst)
+            for (int i = 0; i < w; i++) {
+                int off, xs = ang_ctx(mode, 1, i + 1, &off);
+                int idx = -j - xs;
+                if (mode != 26) idx = MAX(-2 * h, idx);
+                dst[i] = (pel)f4(s[idx], s[idx - 1], s[idx - 2], s[idx - 3], off);
+            }
+    }
+}
+
+void orc_ipred_ang(const pel *nb, pel *dst, int i_dst, int mode, int w, int h)
+{
+    ang_core(nb + ORC_NEIB_MID, dst, i_dst, mode, w, h);
+}
+
+/* ipred_dc, src/com_ipred.c:130-162 */
+void orc_ipred_dc(const pel *nb, pel *dst, int i_dst, int w, int h, int avail, int bd)
+{
+    const pel *s = nb + ORC_NEIB_MID;
+    int dc = 0;
+    if (avail & 2) {
+        for (int i = 0; i < h; i++) dc += s[-i - 1];
+        if (avail & 1) {
+            for (int j = 0; j < w; j++) dc += s[j + 1];
+            dc = (dc + ((w + h) >> 1)) * (4096 / (w + h)) >> 12;
+        } else {
+            dc = (dc + (h >> 1)) >> ilog2(h);
+        }
+    } else if (avail & 1) {
+        for (int j = 0; j < w; j++) dc += s[j + 1];
+        dc = (dc + (w >> 1)) >> ilog2(w);
+    } else {
+        dc = 1 << (bd - 1);
+    }
+    for (int y = 0; y < h; y++, dst += i_dst) memset(dst, dc, (size_t)w);
+}
+
+/* plane prediction parameters, ipred_plane / ipred_plane_ipf, src/com_ipred.c:164-254 */
+static void plane_params(const pel *s, int w, int h, int *pb, int *pc, int *ptemp)
+{
+    static const int mult[5] = { 13, 17, 5, 11, 23 }, shf[5] = { 7, 10, 11, 15, 19 };
+    int w2 = w >> 1, h2 = h >> 1, iw = ilog2(w) - 2, ih = ilog2(h) - 2;
+    int ch = 0, cv = 0;
+    for (int x = 1; x <= w2; x++) ch += x * (s[w2 + x] - s[w2 - x]);
+    for (int y = 1; y <= h2; y++) cv += y * (s[-h2 - y] - s[-h2 + y]);
+    int a = (s[-h] + s[w]) << 4;
+    int b = ((ch << 5) * mult[iw] + (1 << (shf[iw] - 1))) >> shf[iw];
+    int c = ((cv << 5) * mult[ih] + (1 << (shf[ih] - 1))) >> shf[ih];
+    *pb = b; *pc = c;
+    *ptemp = a - (h2 - 1) * c - (w2 - 1) * b + 16;
+}
+
+void orc_ipred_plane(const pel *nb, pel *dst, int i_dst, int w, int h, int bd)
+{
+    int b, c, t, mx = (1 << bd) - 1;
+    plane_params(nb + ORC_NEIB_MID, w, h, &b, &c, &t);
+    for (int y = 0; y < h; y++, t += c, dst += i_dst) {
+        int t2 = t;
+        for (int x = 0; x < w; x++, t2 += b) dst[x] = (pel)CLIP3(0, mx, t2 >> 5);
+    }
+}
+
+void orc_ipred_plane_ipf(const pel *nb, s16 *dst, int w, int h)
+{
+    int b, c, t;
+    plane_params(nb + ORC_NEIB_MID, w, h, &b, &c, &t);
+    for (int y = 0; y < h; y++, t += c, dst += w) {
+        int t2 = t;
+        for (int x = 0; x < w; x++, t2 += b) dst[x] = (s16)(t2 >> 5);
+    }
+}
+
+/* bilinear prediction, ipred_bi / ipred_bi_ipf, src/com_ipred.c:256-368.  Written per
+ * sample: the running sums of the reference reduce to
+ *   predx  = (ref_le[y] << lw) + (x+1)*(a - ref_le[y])
+ *   ref_up = (ref_up[x] << lh) + (y+1)*(b - ref_up[x])
+ *   wxy    = x * y * wt   (the inner loop adds wy[y] = y*wt after each sample) */
+static int bi_sample(const pel *s, int w, int h, int x, int y)
+{
+    static const int tbl_wc[6] = { -1, 21, 13, 7, 4, 2 };
+    int lw = ilog2(w), lh = ilog2(h), ish = MIN(lw, lh), lxy = lw + lh + 1;
+    int off = 1 << (lw + lh);
+    int wc = tbl_wc[lw > lh ? lw - lh : lh - lw];
+    int a = s[w], b = s[-h];
+    int c = (w == h) ? (a + b + 1) >> 1 : (((a << lw) + (b << lh)) * wc + (1 << (ish + 5))) >> (ish + 6);
+    int wt = (c << 1) - a - b;
+    int up = s[x + 1], le = s[-y - 1];
+    int predx = (le << lw) + (x + 1) * (a - le);
+    int refup = (up << lh) + (y + 1) * (b - up);
+    int wxy = x * y * wt;
+    return ((predx << lh) + (refup << lw) + wxy + off) >> lxy;
+}
+
+void orc_ipred_bi(const pel *nb, pel *dst, int i_dst, int w, int h, int bd)
+{
+    int mx = (1 << bd) - 1;
+    for (int y = 0; y < h; y++, dst += i_dst)
+        for (int x = 0; x < w; x++) dst[x] = (pel)CLIP3(0, mx, bi_sample(nb + ORC_NEIB_MID, w, h, x, y));
+}
+
+void orc_ipred_bi_ipf(const pel *nb, s16 *dst, int w, int h)
+{
+    for (int y = 0; y < h; y++, dst += w)
+        for (int x = 0; x < w; x++) dst[x] = (s16)bi_sample(nb + ORC_NEIB_MID, w, h, x, y);
+}
+
+/* intra prediction filter ranges, ipf_core / ipf_core_s16, src/com_ipred.c:615-731 */
+static void ipf_ranges(int ipm, int w, int h, int *hr, int *vr, const u8 **hp, const u8 **vp)
+{
+    int ih = ilog2(w) - 2, iv = ilog2(h) - 2;
+    int vrange = MIN(h, 10), hrange = MIN(w, 10);
+    if (ih > 4) { ih = 4; hrange = 0; }
+    if (iv > 4) { iv = 4; vrange = 0; }
+    if (ipm >= 3 && ipm <= 18) vrange = 0;   /* IPD_DIA_L .. IPD_DIA_R */
+    if (ipm > 18) hrange = 0;
+    *hr = hrange; *vr = vrange;
+    *hp = IPF_PARAM[ih]; *vp = IPF_PARAM[iv];
+}
+
+void orc_ipf_core(const pel *nb, pel *dst, int i_dst, int ipm, int w, int h, int bd)
+{
+    const pel *s = nb + ORC_NEIB_MID, *top = s + 1;
+    int hr, vr; const u8 *hp, *vp;
+    (void)bd;
+    ipf_ranges(ipm, w, h, &hr, &vr, &hp, &vp);
+    for (int r = 0; r < h; r++, dst += i_dst) {
+        if (r < vr) {
+            int ct = vp[r];
+            for (int c = 0; c < w; c++) {
+                int cl = c < hr ? hp[c] : 0;
+                int cur = 64 - cl - ct;
+                dst[c] = (pel)((cl * s[-r - 1] + ct * top[c] + cur * dst[c] + 32) >> 6);
+            }
+        } else {
+            for (int c = 0; c < hr; c++) {
+                int cl = hp[c];
+                dst[c] = (pel)((cl * s[-r - 1] + (64 - cl) * dst[c] + 32) >> 6);
+            }
+        }
+    }
+}
+
+void orc_ipf_core_s16(const pel *nb, pel *dst, int i_dst, const s16 *pred, int ipm, int w, int h, int bd)
+{
+    const pel *s = nb + ORC_NEIB_MID, *top = s + 1;
+    int hr, vr, mx = (1 << bd) - 1; const u8 *hp, *vp;
+    ipf_ranges(ipm, w, h, &hr, &vr, &hp, &vp);
+    for (int r = 0; r < h; r++, dst += i_dst, pred += w) {
+        for (int c = 0; c < w; c++) {
+            int cl = (c < hr) ? hp[c] : 0;
+            int ct = (r < vr) ? vp[r] : 0;
+            int v;
+            if (r < vr || c < hr) v = (cl * s[-r - 1] + ct * top[c] + (64 - cl - ct) * pred[c] + 32) >> 6;
+            else v = pred[c];
+            dst[c] = (pel)CLIP3(0, mx, v);
+        }
+    }
+}
+
+/* com_intra_pred, src/com_ipred.c:733-779 (dst stride = w) */
+void orc_intra_pred(const pel *nb, pel *dst, int ipm, int w, int h, int bd, int avail, int ipf)
+{
+    const pel *s = nb + ORC_NEIB_MID;
+    if (ipm != 1 && ipm != 2) {
+        if (ipm == 12) {
+            for (int y = 0; y < h; y++) memcpy(dst + y * w, s + 1, (size_t)w);
+        } else if (ipm == 24) {
+            for (int y = 0; y < h; y++) memset(dst + y * w, s[-1 - y], (size_t)w);
+        } else if (ipm == 0) {
+            orc_ipred_dc(nb, dst, w, w, h, avail, bd);
+        } else {
+            ang_core(s, dst, w, ipm, w, h);
+        }
+        if (ipf) orc_ipf_core(nb, dst, w, ipm, w, h, bd);
+    } else if (ipf) {
+        s16 tmp[64 * 64];
+        if (ipm == 1) orc_ipred_plane_ipf(nb, tmp, w, h);
+        else orc_ipred_bi_ipf(nb, tmp, w, h);
+        orc_ipf_core_s16(nb, dst, w, tmp, ipm, w, h, bd);
+    } else {
+        if (ipm == 1) orc_ipred_plane(nb, dst, w, w, h, bd);
+        else orc_ipred_bi(nb, dst, w, w, h, bd);
+    }
+}
+
+/* ============================================================================ transforms */
+
+static inline int rnd_of(int shift) { return shift > 0 ? 1 << (shift - 1) : 0; }
+
+/*
+ * Forward DCT2 of a w x h residual (trans_dct2_wXhY, src/transform.c:253-412):
+ * rows with shift log2w + bd - 10, then columns with shift log2h + 5, each pass rounded and
+ * truncated to s16.  64-point passes produce only the first 32 outputs, so for w or h = 64
+ * only the top-left 32-wide / 32-high part of dst is written (the rest is left untouched).
+ */
+void orc_trans_dct2(int log2w, int log2h, const s16 *src, s16 *dst, int bd)
+{
+    orc_init();
+    int w = 1 << log2w, h = 1 << log2h;
+    int kw = MIN(w, 32), kh = MIN(h, 32);
+    int sh1 = log2w + bd - 10, sh2 = log2h + 5;
+    const int *FW = DCT2_FOLD[log2w], *FH = DCT2_FOLD[log2h];
+    s16 *t = (s16 *)malloc(sizeof(s16) * (size_t)w * h);   /* t[u*h + y] */
+    for (int y = 0; y < h; y++)
+        for (int u = 0; u < kw; u++) {
+            int acc = 0;
+            for (int x = 0; x < w; x++) acc += FW[u * w + x] * src[y * w + x];
+            t[u * h + y] = (s16)((acc + rnd_of(sh1)) >> sh1);
+        }
+    for (int u = 0; u < kw; u++)
+        for (int v = 0; v < kh; v++) {
+            int acc = 0;
+            for (int y = 0; y < h; y++) acc += FH[v * h + y] * t[u * h + y];
+            dst[v * w + u] = (s16)((acc + rnd_of(sh2)) >> sh2);
+        }
+    free(t);
+}
+
+/* forward DCT8 (type 0) / DST7 (type 1) pass, tx_dct8_pbN / tx_dst7_pbN,
+ * src/transform.c:416-671: input rows of N, output transposed with stride `line` */
+void orc_trans_dct8_dst7(int type, int log2n, const s16 *src, s16 *dst, int shift, int line)
+{
+    orc_init();
+    int N = 1 << log2n;
+    const int *M = DCT87_EFF[type][log2n];
+    for (int i = 0; i < line; i++, src += N)
+        for (int k = 0; k < N; k++) {
+            int acc = 0;
+            for (int n = 0; n < N; n++) acc += M[k * N + n] * src[n];
+            dst[k * line + i] = (s16)((acc + rnd_of(shift)) >> shift);
+        }
+}
+
+/* 4x4 alternative transform passes and 8x8-corner secondary transform,
+ * xCTr_4_1d_Hor/Vert, xTr2nd_8_1d_Hor/Vert, src/transform.c:674-764 */
+static void c4_fwd(const s16 *src, s16 *dst, int shift, int vert)
+{
+    int t[4][4], rnd = rnd_of(shift);
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) t[i][j] = src[i * 4 + j];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            int sum = rnd;
+            for (int k = 0; k < 4; k++) sum += C4_TRANS[i][k] * (vert ? t[k][j] : t[j][k]);
+            sum = CLIP3(-32768, 32767, sum >> shift);
+            if (vert) dst[i * 4 + j] = (s16)sum; else dst[j * 4 + i] = (s16)sum;
+        }
+}
+
+static void sec_fwd(s16 *src, int stride, int vert)
+{
+    int t[4][4];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) t[i][j] = src[i * stride + j];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            int sum = 64;
+            for (int k = 0; k < 4; k++) sum += C8_TRANS[i][k] * (vert ? t[k][j] : t[j][k]);
+            sum = CLIP3(-32768, 32767, sum >> 7);
+            if (vert) src[i * stride + j] = (s16)sum; else src[j * stride + i] = (s16)sum;
+        }
+}
+
+/* transform(), src/transform.c:772-797 (luma TB) */
+void orc_transform(int tb_nxn, int blk_idx, s16 *coef, const s16 *resi, int log2w, int log2h, int bd, int sec, int alt4)
+{
+    orc_init();
+    int sh1 = log2w + bd - 10, sh2 = log2h + 5;
+    if (alt4 && log2w == 2 && log2h == 2) {
+        s16 t[16];
+        c4_fwd(resi, t, sh1 + 1, 0);
+        c4_fwd(t, coef, sh2 + 1, 1);
+        return;
+    }
+    if (tb_nxn) {
+        s16 t[64 * 64];
+        orc_trans_dct8_dst7(blk_idx & 1, log2w, resi, t, sh1, 1 << log2h);
+        orc_trans_dct8_dst7(blk_idx >> 1, log2h, t, coef, sh2, 1 << log2w);
+    } else {
+        orc_trans_dct2(log2w, log2h, resi, coef, bd);
+    }
+    if (sec >> 1) sec_fwd(coef, 1 << log2w, 1);
+    if (sec & 1) sec_fwd(coef, 1 << log2w, 0);
+}
+
+/*
+ * Inverse DCT2 (itrans_dct2_hH_wW, src/com_itdq.c:264-423): columns with shift 5 clipped to
+ * s16, then rows with shift 20 - bd clipped to [-2^bd, 2^bd - 1].  64-point passes read only
+ * the first 32 coefficients.
+ */
+void orc_itrans_dct2(int log2h, int log2w, const s16 *coef, s16 *resi, int bd)
+{
+    orc_init();
+    int w = 1 << log2w, h = 1 << log2h;
+    int kw = MIN(w, 32), kh = MIN(h, 32);
+    int sh2 = 20 - bd, mx = (1 << bd) - 1, mn = -(1 << bd);
+    const int *FW = DCT2_FOLD[log2w], *FH = DCT2_FOLD[log2h];
+    s16 *t = (s16 *)malloc(sizeof(s16) * (size_t)w * h);   /* t[y*w + u] */
+    for (int u = 0; u < kw; u++)
+        for (int y = 0; y < h; y++) {
+            int acc = 0;
+            for (int v = 0; v < kh; v++) acc += FH[v * h + y] * coef[v * w + u];
+            t[y * w + u] = (s16)CLIP3(-32768, 32767, (acc + 16) >> 5);
+        }
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            int acc = 0;
+            for (int u = 0; u < kw; u++) acc += FW[u * w + x] * t[y * w + u];
+            resi[y * w + x] = (s16)CLIP3(mn, mx, (acc + (1 << (sh2 - 1))) >> sh2);
+        }
+    free(t);
+}
+
+/* inverse DCT8 / DST7 pass, itx_dct8_pbN / itx_dst7_pbN, src/com_itdq.c:428-653: input
+ * column i (stride `line`) -> output row i of N samples */
+void orc_itrans_dct8_dst7(int type, int log2n, const s16 *coef, s16 *blk, int shift, int line, int max_v, int min_v)
+{
+    orc_init();
+    int N = 1 << log2n;
+    const int *M = DCT87_EFF[type][log2n];
+    for (int i = 0; i < line; i++, blk += N)
+        for (int j = 0; j < N; j++) {
+            int acc = 0;
+            for (int k = 0; k < N; k++) acc += coef[k * line + i] * M[k * N + j];
+            blk[j] = (s16)CLIP3(min_v, max_v, (acc + rnd_of(shift)) >> shift);
+        }
+}
+
+static void c4_inv(const s16 *src, s16 *dst, int shift, int vert, int bd)
+{
+    int t[4][4], rnd = rnd_of(shift);
+    int lo = vert ? -32768 : -(1 << bd), hi = vert ? 32767 : (1 << bd) - 1;
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) t[i][j] = src[i * 4 + j];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            int sum = rnd;
+            for (int k = 0; k < 4; k++) sum += C4_TRANS[k][i] * (vert ? t[k][j] : t[j][k]);
+            sum = CLIP3(lo, hi, sum >> shift);
+            if (vert) dst[i * 4 + j] = (s16)sum; else dst[j * 4 + i] = (s16)sum;
+        }
+}
+
+static void sec_inv(s16 *src, int stride, int vert)
+{
+    int t[4][4];
+    for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) t[i][j] = src[i * stride + j];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            int sum = 64;
+            for (int k = 0; k < 4; k++) sum += C8_TRANS[k][i] * (vert ? t[k][j] : t[j][k]);
+            sum = CLIP3(-32768, 32767, sum >> 7);
+            if (vert) src[i * stride + j] = (s16)sum; else src[j * stride + i] = (s16)sum;
+        }
+}
+
+/* com_dquant / com_dquant_wq, src/com_itdq.c:807-871 */
+void orc_dquant(int flat, const s16 *coef, s16 *out, const u8 *wq4, const u8 *wq8, int log2w, int log2h, int scale, int shift, int bd)
+{
+    int w = 1 << log2w, h = 1 << log2h;
+    int off = shift == 0 ? 0 : 1 << (shift - 1);
+    int refix = (log2w + log2h) & 1;
+    (void)bd;
+    if (flat) {
+        int n = MIN(h, 32) * w;
+        for (int i = 0; i < n; i++) {
+            int lev = (coef[i] * scale + off) >> shift;
+            lev = CLIP3(-32768, 32767, lev);
+            out[i] = (s16)(refix ? (lev * 181 + 128) >> 8 : lev);
+        }
+        return;
+    }
+    const u8 *wq; int ish, istep, ww;
+    if (log2w == 2 && log2h == 2) { wq = wq4; ish = 0; istep = 1; ww = 4; }
+    else { wq = wq8; ish = MAX(log2w, log2h) - 3; istep = 1 << ish; ww = 8; }
+    for (int i = 0; i < h; i++) {
+        for (int j = 0; j < w; j++) {
+            int weight = ((i | j) & 0xE0) ? 0 : wq[j >> ish];
+            int lev = (int)(((((s64)((coef[i * w + j] * weight) >> 2)) * scale) >> 4) + off) >> shift;
+            lev = CLIP3(-32768, 32767, lev);
+            if (refix) lev = (lev * 181 + 128) >> 8;
+            out[i * w + j] = (s16)lev;
+        }
+        if ((i + 1) % istep == 0) wq += ww;
+    }
+}
+
+/* com_invqt -> com_inv_trans, src/com_itdq.c:747-881 (luma TB) */
+void orc_invqt(int tb_nxn, int blk_idx, const s16 *coef, s16 *resi, const u8 *wq4, const u8 *wq8, int log2w, int log2h, int qp, int bd, int sec, int alt4)
+{
+    orc_init();
+    s16 dq[64 * 64];
+    int log2_size = (log2w + log2h) >> 1;
+    int scale = (int)DQ_SCALE[qp];
+    int shift = (int)DQ_SHIFT[qp] - (15 - bd - log2_size) + 1;
+    orc_dquant(wq4 == NULL, coef, dq, wq4, wq8, log2w, log2h, scale, shift, bd);
+    if (alt4 && log2w == 2 && log2h == 2) {
+        s16 t[16];
+        c4_inv(dq, t, 5, 1, bd);
+        c4_inv(t, resi, 20 - bd + 2, 0, bd);
+        return;
+    }
+    int stride = 1 << log2w;
+    if (sec & 1) sec_inv(dq, stride, 0);
+    if (sec >> 1) sec_inv(dq, stride, 1);
+    if (tb_nxn) {
+        s16 t[64 * 64];
+        orc_itrans_dct8_dst7(blk_idx >> 1, log2h, dq, t, 5, 1 << log2w, 32767, -32768);
+        orc_itrans_dct8_dst7(blk_idx & 1, log2w, t, resi, 20 - bd, 1 << log2h, (1 << bd) - 1, -(1 << bd));
+    } else {
+        orc_itrans_dct2(log2h, log2w, dq, resi, bd);
+    }
+}
+
+/* quant_check / quant_rdoq (first RDOQ pass), src/com_itdq.c:910-954 */
+int orc_quant_check(const s16 *coef, int num, int threshold)
+{
+    for (int i = 0; i < (num >> 2) * 4; i++)
+        if (coef[i] > threshold || coef[i] < -threshold) return 0;
+    return 1;
+}
+
+int orc_quant_rdoq(const s16 *coef, int num, int q_value, int q_bits, s32 err_scale, int precision_bits,
+                   u32 *abs_coef, s16 *abs_level, s64 *uncoded_err)
+{
+    s32 add = 1 << (q_bits - 1);
+    int last = -1;
+    int thr = ((1 << (q_bits - 1)) - 1) / q_value + 1;
+    for (int i = 0; i < num; i++) {
+        int a = ABSI((int)coef[i]);
+        if (a < thr) { abs_level[i] = 0; continue; }
+        u32 ld = (u32)a * (u32)q_value;
+        s64 err = ((s64)ld * err_scale) >> precision_bits;
+        abs_level[i] = (s16)(u32)(((u64)ld + (u64)add) >> q_bits);
+        abs_coef[i] = ld;
+        uncoded_err[i] = err * err;
+        last = i;
+    }
+    return last;
+}
+
+/* ===================================================================== batched: motion */
+
+typedef struct { int minx, maxx, miny, maxy; } mvrange_t;
+
+/* get_max_search_range with is_padding = 1, mvr 0, mvp 0 (src/me.c:502-527) clipped to the
+ * [-range, range] full-search window */
+static mvrange_t me_range(int x, int y, int W, int H, int range)
+{
+    int mto = MAX(W, H);                        /* ((((max(W,H) << 2) + 3) << 0) >> 2) */
+    mvrange_t r;
+    r.minx = MAX(-range, MAX(-128 + 1 - x, -mto + 4));
+    r.miny = MAX(-range, MAX(-128 + 1 - y, -mto + 4));
+    r.maxx = MIN(range, MIN(W - 1 - x, mto - 4));
+    r.maxy = MIN(range, MIN(H - 1 - y, mto - 4));
+    return r;
+}
+
+/* com_mc_blk_luma_pointer, src/com_mc.c:89-101 */
+static const pel *mc_pointer(const pel *const *planes, int i_ref, int qx, int qy, int maxx, int maxy)
+{
+    int dx = qx & 3, dy = qy & 3;
+    int x = CLIP3(-128 - 4, maxx, qx >> 2), y = CLIP3(-128 - 4, maxy, qy >> 2);
+    return planes[dy * 4 + dx] + y * i_ref + x;
+}
+
+/*
+ * Batched motion search for one block and one reference:
+ *   integer full search of cost = (SAD << 16) + (bits(4dx) + bits(4dy)) * lambda_mv, strict
+ *   '<' in raster order (dy outer, dx inner) so the first minimum wins
+ *   (cost_sad + GET_MVBITS_IPEL_*, src/me.c:103-197);
+ *   then me_sub_pel_search with SATD cost (subpel_cost_type 0, src/me.c:366-500): centre,
+ *   8 half-sample points around the integer winner, 8 quarter-sample points around the
+ *   half-sample winner, cost = bits * lambda_mv + (satd << 16).
+ */
+static void me_one(const pel *org, int i_org, const pel *const *pl, int i_ref, int W, int H,
+                   const orc_me_block_t *b, int range, u32 lambda, const u8 *bits, orc_me_result_t *o)
+{
+    static const s8 HP[8][2] = { { -2, 0 }, { -2, 2 }, { 0, 2 }, { 2, 2 }, { 2, 0 }, { 2, -2 }, { 0, -2 }, { -2, -2 } };
+    static const s8 QP[8][2] = { { -1, 0 }, { 0, 1 }, { 1, 0 }, { 0, -1 }, { -1, 1 }, { 1, 1 }, { -1, -1 }, { 1, -1 } };
+    int x = b->x, y = b->y, w = b->w, h = b->h;
+    const pel *o0 = org + y * i_org + x;
+    const pel *ref = pl[0] + y * i_ref + x;
+    mvrange_t r = me_range(x, y, W, H, range);
+    u64 best = ~(u64)0; int bx = 0, by = 0; u32 bsad = 0;
+    for (int dy = r.miny; dy <= r.maxy; dy++)
+        for (int dx = r.minx; dx <= r.maxx; dx++) {
+            u32 sad = orc_sad(w, h, o0, i_org, ref + dy * i_ref + dx, i_ref);
+            u64 c = ((u64)sad << 16) + (u64)(bits[4 * dx] + bits[4 * dy]) * lambda;
+            if (c < best) { best = c; bx = dx; by = dy; bsad = sad; }
+        }
+    o->mv_int[0] = (s16)bx; o->mv_int[1] = (s16)by; o->sad_int = bsad; o->cost_int = best;
+
+    int maxx = W + 4, maxy = H + 4;
+    int cx = bx * 4, cy = by * 4;
+    u32 satd = orc_had(w, h, o0, i_org, ref + by * i_ref + bx, i_ref, 8);
+    u64 cbest = (u64)((u32)(bits[cx] + bits[cy]) * lambda) + ((u64)satd << 16);
+    int mx = cx, my = cy; u32 bsatd = satd;
+    for (int i = 0; i < 8; i++) {
+        int vx = cx + HP[i][0], vy = cy + HP[i][1];
+        const pel *p = mc_pointer(pl, i_ref, vx + (x << 2), vy + (y << 2), maxx, maxy);
+        u32 s = orc_had(w, h, o0, i_org, p, i_ref, 8);
+        u64 c = (u64)((u32)(bits[vx] + bits[vy]) * lambda) + ((u64)s << 16);
+        if (c < cbest) { cbest = c; mx = vx; my = vy; bsatd = s; }
+    }
+    cx = mx; cy = my;
+    for (int i = 0; i < 8; i++) {
+        int vx = cx + QP[i][0], vy = cy + QP[i][1];
+        const pel *p = mc_pointer(pl, i_ref, vx + (x << 2), vy + (y << 2), maxx, maxy);
+        u32 s = orc_had(w, h, o0, i_org, p, i_ref, 8);
+        u64 c = (u64)((u32)(bits[vx] + bits[vy]) * lambda) + ((u64)s << 16);
+        if (c < cbest) { cbest = c; mx = vx; my = vy; bsatd = s; }
+    }
+    o->mv_sub[0] = (s16)mx; o->mv_sub[1] = (s16)my; o->satd_sub = bsatd; o->cost_sub = cbest;
+}
+
+void orc_me_frame(const pel *org, int i_org, const pel *const *planes, int i_ref, int width, int height,
+                  int n_refs, const orc_me_block_t *blocks, int n_blocks, int range, u32 lambda_mv,
+                  orc_me_result_t *out, int threads)
+{
+    orc_init();
+    int off = (MAX(width, height) << 2) + 3;
+    u8 *tab = (u8 *)malloc((size_t)(2 * off + 1));
+    orc_mvbits_table(tab, off);
+    const u8 *bits = tab + off;
+#ifdef _OPENMP
+    if (threads < 1) threads = 1;
+    #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+#endif
+    for (int i = 0; i < n_blocks * n_refs; i++) {
+        int b = i / n_refs, r = i % n_refs;
+        me_one(org, i_org, planes + r * 16, i_ref, width, height, &blocks[b], range, lambda_mv, bits, &out[i]);
+    }
+    (void)threads;
+    free(tab);
+}
+
+/* ===================================================================== batched: intra */
+
+u32 orc_level_hash(const s16 *lev, int n)
+{
+    u32 hsh = 2166136261u;
+    for (int i = 0; i < n; i++) {
+        u16 v = (u16)lev[i];
+        hsh = (hsh ^ (v & 0xFF)) * 16777619u;
+        hsh = (hsh ^ (v >> 8)) * 16777619u;
+    }
+    return hsh;
+}
+
+/* quantisation of the lattice: rdoq_quant_block's quant_check early-out and its first pass
+ * (src/quant.c:196-231), with levels kept (no second RDOQ pass). Returns the signed levels. */
+static void lattice_quant(const s16 *coef, s16 *lev, int log2w, int log2h, int qp, int is_intra, orc_lat_q_t *q)
+{
+    int w = 1 << log2w, h = 1 << log2h, n = w * h;
+    int odd = (log2w + log2h) & 1;
+    int ns_shift = odd ? 7 : 0, ns_scale = odd ? 181 : 1, ns_off = odd ? 64 : 0;
+    int log2_size = (log2w + log2h) >> 1;
+    int tr_shift = 15 - 8 - log2_size;
+    int q_bits = 14 + tr_shift;
+    int q_value = (Q_SCALE[qp] * ns_scale + ns_off) >> ns_shift;
+    int used = 1 << (log2w + MIN(5, log2h));
+    int offset = (is_intra ? 201 : 153) << (q_bits - 9);
+    int nz_thr = ((((1 << q_bits) - offset) << 10) / q_value - 1) >> 10;
+    memset(lev, 0, sizeof(s16) * (size_t)n);
+    q->num_nz = 0; q->last_nz = -1; q->sum_abs = 0;
+    if (orc_quant_check(coef, used, nz_thr)) { q->coef_hash = orc_level_hash(lev, n); return; }
+    const u16 *scan = SCAN[log2w][log2h];
+    int thr = ((1 << (q_bits - 1)) - 1) / q_value + 1;
+    for (int i = 0; i < n; i++) {
+        int pos = scan[i];
+        int a = ABSI((int)coef[pos]);
+        if (a < thr) continue;
+        u32 ld = (u32)a * (u32)q_value;
+        int l = (int)(s16)(u32)(((u64)ld + (u64)(1u << (q_bits - 1))) >> q_bits);
+        if (!l) continue;
+        lev[pos] = (s16)(coef[pos] < 0 ? -l : l);
+        q->num_nz++; q->last_nz = (s16)i; q->sum_abs += (u32)l;
+    }
+    q->coef_hash = orc_level_hash(lev, n);
+}
+
+void orc_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, int width, int height,
+                       const orc_cu_t *cus, int n_cus, int ipf, const int *qps, int n_qp, int is_intra_slice,
+                       u32 *satd_out, orc_lat_q_t *q_out, int threads)
+{
+    orc_init();
+    int i_scu = (width >> 2) + 2, h_scu = (height >> 2) + 2;
+    u8 *coded = (u8 *)calloc((size_t)i_scu * h_scu, 1);
+    for (int y = 1; y <= (height >> 2); y++)
+        for (int x = 1; x <= (width >> 2); x++) coded[y * i_scu + x] = 1;
+#ifdef _OPENMP
+    if (threads < 1) threads = 1;
+    #pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
+#endif
+    for (int c = 0; c < n_cus; c++) {
+        const orc_cu_t *cu = &cus[c];
+        int x = cu->x, y = cu->y, w = cu->w, h = cu->h;
+        int lw = ilog2(w), lh = ilog2(h);
+        int avail = (y > 0 ? 1 : 0) | (x > 0 ? 2 : 0) | ((x > 0 && y > 0) ? 4 : 0);
+        pel nb[ORC_NEIB_SIZE];
+        int scup = (y >> 2) * i_scu + (x >> 2) + i_scu + 1;   /* map origin offset by the border */
+        const pel *src = rec + y * i_rec + x;
+        orc_intra_get_nbr(x, y, w, h, src, i_rec, src - i_rec, 1 << 30, avail, nb, scup, coded, i_scu, 8);
+        const pel *o = org + y * i_org + x;
+        pel pred[64 * 64], recon[64 * 64];
+        s16 resi[64 * 64], coef[64 * 64], lev[64 * 64], rr[64 * 64];
+        for (int m = 0; m < 33; m++) {
+            orc_intra_pred(nb, pred, m, w, h, 8, avail, ipf);
+            satd_out[c * 33 + m] = orc_satd_intra(w, h, o, pred, i_org, w, 8);
+            orc_pel_diff(w, h, o, i_org, pred, w, resi, w);
+            memset(coef, 0, sizeof(coef));
+            orc_trans_dct2(lw, lh, resi, coef, 8);
+            for (int q = 0; q < n_qp; q++) {
+                orc_lat_q_t *qo = &q_out[((size_t)c * 33 + m) * n_qp + q];
+                lattice_quant(coef, lev, lw, lh, qps[q], is_intra_slice, qo);
+                if (qo->num_nz) {
+                    orc_invqt(0, 0, lev, rr, NULL, NULL, lw, lh, qps[q], 8, 0, 0);
+                    orc_recon(rr, pred, w, w, h, recon, w, 1, 8);
+                } else {
+                    orc_recon(rr, pred, w, w, h, recon, w, 0, 8);
+                }
+                qo->ssd = (u32)orc_ssd(w, h, o, i_org, recon, w);
+            }
+        }
+    }
+    (void)threads;
+    free(coded);
+}

@@ -1,0 +1,146 @@
+/*
+ * oracle.h -- CPU restatement of uavs3e's mode-decision kernels (8-bit luma).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU path: the parity tests,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg call it; the product library
+ * (libuavs3e_cuda) never links, loads or falls back to it.
+ *
+ * Every function restates the algorithm of the reference function cited beside it
+ * (paths relative to the uavs3e source tree).  The restatement is pinned against the
+ * reference compiled from its own sources (oracle/Makefile "ref") by
+ * tests/golden/make_golden.py, whose vectors are committed under tests/golden/.
+ */
+#ifndef UAVS3E_ORACLE_H
+#define UAVS3E_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef uint8_t  pel;
+typedef int8_t   s8;
+typedef int16_t  s16;
+typedef int32_t  s32;
+typedef int64_t  s64;
+typedef uint8_t  u8;
+typedef uint16_t u16;
+typedef uint32_t u32;
+typedef uint64_t u64;
+
+#define ORC_NEIB_SIZE 576           /* INTRA_NEIB_SIZE, inc/com_define.h:277 */
+#define ORC_NEIB_MID  288
+
+void orc_init(void);
+
+/* tables */
+const s8  *orc_dct_table(int log2n);                 /* [3][N][N]: DCT2, DCT8, DST7 */
+const u16 *orc_scan(int log2w, int log2h);           /* zig-zag scan, src/com_util.c:1220 */
+const s8  *orc_mc_luma_coef(void);                   /* [4][8] */
+const s8  *orc_mc_chroma_coef(void);                 /* [8][4] */
+u16        orc_quant_scale(int qp);
+u32        orc_dq_scale(int qp);
+u32        orc_dq_shift(int qp);
+s32        orc_rdoq_err_scale(int qp, int log2_size_minus1);
+double     orc_tbl_sqrt(int i);
+void       orc_mvbits_table(u8 *tab, int offset);    /* fills tab[0 .. 2*offset], centre at tab[offset] */
+
+/* costs, src/com_cost.c */
+u32  orc_sad(int w, int h, const pel *o, int io, const pel *p, int ip);
+u64  orc_ssd(int w, int h, const pel *o, int io, const pel *p, int ip);
+u32  orc_satd_tile(int tw, int th, const pel *o, int io, const pel *p, int ip);  /* cost_satd[][] */
+u32  orc_had(int w, int h, const pel *o, int io, const pel *p, int ip, int bd);  /* com_had */
+u32  orc_satd_intra(int w, int h, const pel *o, const pel *p, int io, int ip, int bd);
+
+/* motion compensation, src/com_mc.c */
+void orc_ipcpy(const pel *s, int is, pel *d, int id, int w, int h);
+void orc_ipflt(int type, const pel *s, int is, pel *d, int id, int w, int h, const s8 *c, int max_val);
+void orc_ipflt_ext(int type, const pel *s, int is, pel *d, int id, int w, int h, const s8 *cx, const s8 *cy, int max_val);
+void orc_if_luma_frame(pel *plane0, pel **planes15, int width, int height, int pad, int stride);
+
+/* pel ops, src/com_util.c */
+void orc_pel_diff(int w, int h, const pel *o, int io, const pel *p, int ip, s16 *r, int ir);
+void orc_pel_avrg(int w, int h, pel *d, int id, const pel *s1, const pel *s2);
+void orc_recon(const s16 *resi, const pel *pred, int ipred, int w, int h, pel *rec, int irec, int cbf, int bd);
+
+/* intra, src/com_ipred.c */
+void orc_intra_get_nbr(int x, int y, int w, int h, const pel *src, int s_src, const pel *top, int lcu_size, int avail,
+                       pel *nb_out, int scup, const u8 *coded, int i_scu, int bd);
+void orc_intra_pred(const pel *nb, pel *dst, int ipm, int w, int h, int bd, int avail, int ipf);
+void orc_ipred_ang(const pel *nb, pel *dst, int i_dst, int mode, int w, int h);     /* intra_pred_ang[mode] */
+void orc_ipred_dc(const pel *nb, pel *dst, int i_dst, int w, int h, int avail, int bd);
+void orc_ipred_plane(const pel *nb, pel *dst, int i_dst, int w, int h, int bd);
+void orc_ipred_bi(const pel *nb, pel *dst, int i_dst, int w, int h, int bd);
+void orc_ipred_plane_ipf(const pel *nb, s16 *dst, int w, int h);
+void orc_ipred_bi_ipf(const pel *nb, s16 *dst, int w, int h);
+void orc_ipf_core(const pel *nb, pel *dst, int i_dst, int ipm, int w, int h, int bd);
+void orc_ipf_core_s16(const pel *nb, pel *dst, int i_dst, const s16 *pred, int ipm, int w, int h, int bd);
+
+/* transforms and quantisation, src/transform.c, src/com_itdq.c */
+void orc_trans_dct2(int log2w, int log2h, const s16 *src, s16 *dst, int bd);
+void orc_trans_dct8_dst7(int type, int log2n, const s16 *src, s16 *dst, int shift, int line);
+void orc_transform(int tb_nxn, int blk_idx, s16 *coef, const s16 *resi, int log2w, int log2h, int bd, int sec, int alt4);
+void orc_itrans_dct2(int log2h, int log2w, const s16 *coef, s16 *resi, int bd);
+void orc_itrans_dct8_dst7(int type, int log2n, const s16 *coef, s16 *blk, int shift, int line, int max_v, int min_v);
+void orc_dquant(int flat, const s16 *coef, s16 *out, const u8 *wq4, const u8 *wq8, int log2w, int log2h, int scale, int shift, int bd);
+void orc_invqt(int tb_nxn, int blk_idx, const s16 *coef, s16 *resi, const u8 *wq4, const u8 *wq8, int log2w, int log2h, int qp, int bd, int sec, int alt4);
+int  orc_quant_check(const s16 *coef, int num, int threshold);
+int  orc_quant_rdoq(const s16 *coef, int num, int q_value, int q_bits, s32 err_scale, int precision_bits,
+                    u32 *abs_coef, s16 *abs_level, s64 *uncoded_err);
+
+/* ---------------- batched workloads (the GPU path's batch definitions) ---------------- */
+
+/* one motion-search block: position and size in luma samples */
+typedef struct { s16 x, y; u8 w, h; u16 pad; } orc_me_block_t;
+
+/* per (block, reference) result of the batched motion search */
+typedef struct {
+    s16 mv_int[2];      /* best integer MV, integer-sample units            */
+    s16 mv_sub[2];      /* best quarter-sample MV after hpel+qpel refinement  */
+    u32 sad_int;        /* SAD at mv_int                                     */
+    u32 satd_sub;       /* SATD (com_had) at mv_sub                          */
+    u64 cost_int;       /* (SAD << 16) + mvbits * lambda_mv at mv_int        */
+    u64 cost_sub;       /* (SATD << 16) + mvbits * lambda_mv at mv_sub       */
+} orc_me_result_t;
+
+/*
+ * Full-search integer ME over [-range, range]^2 (clipped to the encoder's MV limits), then
+ * hpel and qpel SATD refinement on the 15 fractional planes, for every block and reference.
+ * planes[r*16 + dy*4 + dx] is the (dy,dx) quarter-sample plane of reference r (index 0 =
+ * the integer plane), all with stride i_ref and a padding of at least 144 samples.
+ * Results are written to out[b * n_refs + r].  Uses OpenMP over blocks when threads > 1.
+ */
+void orc_me_frame(const pel *org, int i_org, const pel *const *planes, int i_ref, int width, int height,
+                  int n_refs, const orc_me_block_t *blocks, int n_blocks, int range, u32 lambda_mv,
+                  orc_me_result_t *out, int threads);
+
+/* one intra lattice CU */
+typedef struct { s16 x, y; u8 w, h; u16 pad; } orc_cu_t;
+
+/* per (CU, mode, QP) result of the intra lattice */
+typedef struct {
+    u32 ssd;            /* SSD(org, recon)                        */
+    u32 coef_hash;      /* hash of the quantised levels (raster)  */
+    u16 num_nz;         /* non-zero quantised levels              */
+    s16 last_nz;        /* last non-zero position in scan order   */
+    u32 sum_abs;        /* sum of |level|                         */
+} orc_lat_q_t;
+
+/*
+ * Intra lattice: for each CU and each of the 33 luma modes: neighbours from `rec` (every
+ * in-picture sample outside the CU counts as reconstructed), prediction (com_intra_pred,
+ * ipf flag as given), SATD against org, residual, forward DCT2, then for each QP: first-pass
+ * quantisation (quant_check + quant_rdoq level), dequantisation, inverse DCT2,
+ * reconstruction and SSD.  satd_out[cu*33 + m]; q_out[(cu*33 + m)*n_qp + q].
+ */
+void orc_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, int width, int height,
+                       const orc_cu_t *cus, int n_cus, int ipf, const int *qps, int n_qp, int is_intra_slice,
+                       u32 *satd_out, orc_lat_q_t *q_out, int threads);
+
+/* level hash used by the lattice (FNV-1a over the raster s16 levels) */
+u32 orc_level_hash(const s16 *lev, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,298 @@
+"""ctypes bindings of the CPU checkers (test infrastructure only).
+
+``Oracle``  wraps ``_build/liboracle.so`` (the C restatement, oracle.c); it builds on any host.
+``RefLib``  wraps ``_ref/libuavs3e_ref.so`` (the reference encoder compiled from its own sources
+            by ``make -C oracle ref``); it exists only where the reference sources are present.
+
+Both expose the same Python methods with numpy arguments, so a parity test can run one case
+through either checker and through the GPU library.  Nothing in the product imports this.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libuavs3e_ref.so")
+NEIB = 576
+
+P = C.c_void_p
+I = C.c_int
+
+
+def ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def build_oracle():
+    subprocess.run(["make", "-C", HERE, "-s"], check=True)
+
+
+def build_ref(ref_dir="/root/reference"):
+    if not os.path.isdir(ref_dir):
+        return False
+    subprocess.run(["make", "-C", HERE, "-s", "-j8", "ref", "REF=" + ref_dir], check=True)
+    return True
+
+
+class _Common:
+    """Methods with identical argument meaning on both libraries."""
+
+    def sad(self, w, h, o, io, p, ip):
+        raise NotImplementedError
+
+    # helpers shared by both bindings -------------------------------------------------
+    @staticmethod
+    def _u8(a):
+        return np.ascontiguousarray(a, dtype=np.uint8)
+
+
+class Oracle(_Common):
+    def __init__(self, path=ORACLE_SO):
+        if not os.path.exists(path):
+            build_oracle()
+        L = C.CDLL(path)
+        self.L = L
+        L.orc_init()
+        L.orc_sad.restype = C.c_uint32
+        L.orc_ssd.restype = C.c_uint64
+        L.orc_satd_tile.restype = C.c_uint32
+        L.orc_had.restype = C.c_uint32
+        L.orc_satd_intra.restype = C.c_uint32
+        L.orc_quant_check.restype = I
+        L.orc_quant_rdoq.restype = I
+        L.orc_dct_table.restype = C.POINTER(C.c_int8)
+        L.orc_scan.restype = C.POINTER(C.c_uint16)
+        L.orc_rdoq_err_scale.restype = C.c_int32
+        L.orc_dq_scale.restype = C.c_uint32
+        L.orc_dq_shift.restype = C.c_uint32
+        L.orc_quant_scale.restype = C.c_uint16
+        L.orc_tbl_sqrt.restype = C.c_double
+        L.orc_level_hash.restype = C.c_uint32
+
+    # costs
+    def sad(self, w, h, o, io, p, ip):
+        return self.L.orc_sad(w, h, P(o), io, P(p), ip)
+
+    def ssd(self, w, h, o, io, p, ip):
+        return self.L.orc_ssd(w, h, P(o), io, P(p), ip)
+
+    def satd_tile(self, tw, th, o, io, p, ip):
+        return self.L.orc_satd_tile(tw, th, P(o), io, P(p), ip)
+
+    def had(self, w, h, o, io, p, ip, bd=8):
+        return self.L.orc_had(w, h, P(o), io, P(p), ip, bd)
+
+    def satd_intra(self, w, h, o, p, io, ip, bd=8):
+        return self.L.orc_satd_intra(w, h, P(o), P(p), io, ip, bd)
+
+    # mc
+    def ipflt(self, t, s, is_, d, id_, w, h, c, mx=255):
+        self.L.orc_ipflt(t, P(s), is_, P(d), id_, w, h, ptr(c), mx)
+
+    def ipflt_ext(self, t, s, is_, d, id_, w, h, cx, cy, mx=255):
+        self.L.orc_ipflt_ext(t, P(s), is_, P(d), id_, w, h, ptr(cx), ptr(cy), mx)
+
+    def ipcpy(self, s, is_, d, id_, w, h):
+        self.L.orc_ipcpy(P(s), is_, P(d), id_, w, h)
+
+    def if_luma_frame(self, plane0_ptr, plane_ptrs, W, H, pad, stride):
+        arr = (C.c_void_p * 15)(*plane_ptrs)
+        self.L.orc_if_luma_frame(P(plane0_ptr), arr, W, H, pad, stride)
+
+    # pel
+    def pel_diff(self, w, h, o, io, p, ip, r, ir):
+        self.L.orc_pel_diff(w, h, P(o), io, P(p), ip, P(r), ir)
+
+    def pel_avrg(self, w, h, d, id_, s1, s2):
+        self.L.orc_pel_avrg(w, h, P(d), id_, P(s1), P(s2))
+
+    def recon(self, resi, pred, ipred, w, h, rec, irec, cbf, bd=8):
+        self.L.orc_recon(P(resi), P(pred), ipred, w, h, P(rec), irec, cbf, bd)
+
+    # intra
+    def intra_get_nbr(self, x, y, w, h, src, s_src, top, lcu, avail, nb, scup, coded, n_scu, i_scu, bd=8):
+        self.L.orc_intra_get_nbr(x, y, w, h, P(src), s_src, P(top), lcu, avail, ptr(nb), scup, ptr(coded), i_scu, bd)
+
+    def intra_pred(self, nb, dst, ipm, w, h, avail, ipf, bd=8):
+        self.L.orc_intra_pred(ptr(nb), ptr(dst), ipm, w, h, bd, avail, ipf)
+
+    def ipred_ang(self, nb, dst, i_dst, mode, w, h):
+        self.L.orc_ipred_ang(ptr(nb), ptr(dst), i_dst, mode, w, h)
+
+    # transforms
+    def trans_dct2(self, lw, lh, src, dst, bd=8):
+        self.L.orc_trans_dct2(lw, lh, ptr(src), ptr(dst), bd)
+
+    def trans_dct8_dst7(self, t, ln, src, dst, shift, line):
+        self.L.orc_trans_dct8_dst7(t, ln, ptr(src), ptr(dst), shift, line)
+
+    def transform(self, nxn, blk, coef, resi, lw, lh, bd=8, sec=0, alt4=0):
+        self.L.orc_transform(nxn, blk, ptr(coef), ptr(resi), lw, lh, bd, sec, alt4)
+
+    def itrans_dct2(self, lh, lw, coef, resi, bd=8):
+        self.L.orc_itrans_dct2(lh, lw, ptr(coef), ptr(resi), bd)
+
+    def itrans_dct8_dst7(self, t, ln, coef, blk, shift, line, mx, mn):
+        self.L.orc_itrans_dct8_dst7(t, ln, ptr(coef), ptr(blk), shift, line, mx, mn)
+
+    def dquant(self, flat, coef, out, wq4, wq8, lw, lh, scale, shift, bd=8):
+        self.L.orc_dquant(flat, ptr(coef), ptr(out), ptr(wq4), ptr(wq8), lw, lh, scale, shift, bd)
+
+    def invqt(self, nxn, blk, coef, resi, wq4, wq8, lw, lh, qp, bd=8, sec=0, alt4=0):
+        w4 = None if wq4 is None else ptr(wq4)
+        w8 = None if wq8 is None else ptr(wq8)
+        self.L.orc_invqt(nxn, blk, ptr(coef), ptr(resi), w4, w8, lw, lh, qp, bd, sec, alt4)
+
+    def quant_check(self, coef, num, thr):
+        return self.L.orc_quant_check(ptr(coef), num, thr)
+
+    def quant_rdoq(self, coef, num, qv, qb, es, pb, abs_coef, abs_level, err):
+        return self.L.orc_quant_rdoq(ptr(coef), num, qv, qb, es, pb, ptr(abs_coef), ptr(abs_level), ptr(err))
+
+    # tables
+    def dct_table(self, ln):
+        n = 1 << ln
+        return np.ctypeslib.as_array(self.L.orc_dct_table(ln), shape=(3, n, n)).copy()
+
+    def scan(self, lw, lh):
+        return np.ctypeslib.as_array(self.L.orc_scan(lw, lh), shape=(1 << (lw + lh),)).copy()
+
+    # batched workloads
+    def me_frame(self, org, i_org, plane_ptrs, i_ref, W, H, n_refs, blocks, rng, lambda_mv, threads=1):
+        """blocks: structured array of ME_BLOCK; returns structured array of ME_RESULT."""
+        out = np.zeros(len(blocks) * n_refs, dtype=ME_RESULT)
+        arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
+        self.L.orc_me_frame(P(org), i_org, arr, i_ref, W, H, n_refs, ptr(blocks), len(blocks), rng,
+                            C.c_uint32(lambda_mv), ptr(out), threads)
+        return out
+
+    def intra_lattice(self, org, i_org, rec, i_rec, W, H, cus, ipf, qps, is_intra=1, threads=1):
+        qps = np.ascontiguousarray(qps, dtype=np.int32)
+        satd = np.zeros(len(cus) * 33, dtype=np.uint32)
+        q = np.zeros(len(cus) * 33 * len(qps), dtype=LAT_Q)
+        self.L.orc_intra_lattice(P(org), i_org, P(rec), i_rec, W, H, ptr(cus), len(cus), ipf, ptr(qps),
+                                 len(qps), is_intra, ptr(satd), ptr(q), threads)
+        return satd, q
+
+
+class RefLib(_Common):
+    """The reference's own C kernels (through oracle/ref_glue.c)."""
+
+    def __init__(self, path=REF_SO):
+        L = C.CDLL(path)
+        self.L = L
+        L.refk_init()
+        for n in ("refk_sad", "refk_satd", "refk_had", "refk_satd_intra"):
+            getattr(L, n).restype = C.c_uint32
+        L.refk_ssd.restype = C.c_uint64
+        L.refk_quant_check.restype = I
+        L.refk_quant_rdoq.restype = I
+        L.refk_dct_table.restype = C.POINTER(C.c_int8)
+        L.refk_scan.restype = C.POINTER(C.c_uint16)
+        L.refk_tbl_sqrt.restype = C.c_double
+
+    @staticmethod
+    def widx(w):
+        return int(w).bit_length() - 3
+
+    def sad(self, w, h, o, io, p, ip):
+        return self.L.refk_sad(self.widx(w), P(o), io, P(p), ip, h)
+
+    def ssd(self, w, h, o, io, p, ip):
+        return self.L.refk_ssd(self.widx(w), P(o), io, P(p), ip, h)
+
+    def satd_tile(self, tw, th, o, io, p, ip):
+        return self.L.refk_satd(tw.bit_length() - 3, th.bit_length() - 3, P(o), io, P(p), ip)
+
+    def had(self, w, h, o, io, p, ip, bd=8):
+        return self.L.refk_had(w, h, P(o), io, P(p), ip, bd)
+
+    def satd_intra(self, w, h, o, p, io, ip, bd=8):
+        return self.L.refk_satd_intra(w, h, P(o), P(p), io, ip, bd)
+
+    def ipflt(self, t, s, is_, d, id_, w, h, c, mx=255):
+        self.L.refk_ipflt(t, self.widx(w), P(s), is_, P(d), id_, w, h, ptr(c), mx)
+
+    def ipflt_ext(self, t, s, is_, d, id_, w, h, cx, cy, mx=255):
+        self.L.refk_ipflt_ext(t, self.widx(w), P(s), is_, P(d), id_, w, h, ptr(cx), ptr(cy), mx)
+
+    def ipcpy(self, s, is_, d, id_, w, h):
+        self.L.refk_ipcpy(self.widx(w), P(s), is_, P(d), id_, w, h)
+
+    def if_luma_frame(self, plane0_ptr, plane_ptrs, W, H, pad, stride):
+        arr = (C.c_void_p * 15)(*plane_ptrs)
+        self.L.refk_if_luma_frame(P(plane0_ptr), arr, W, H, pad, stride)
+
+    def pel_diff(self, w, h, o, io, p, ip, r, ir):
+        self.L.refk_pel_diff(self.widx(w), P(o), io, P(p), ip, P(r), ir, h)
+
+    def pel_avrg(self, w, h, d, id_, s1, s2):
+        self.L.refk_pel_avrg(self.widx(w), P(d), id_, P(s1), P(s2), h)
+
+    def recon(self, resi, pred, ipred, w, h, rec, irec, cbf, bd=8):
+        self.L.refk_recon(self.widx(w), P(resi), P(pred), ipred, w, h, P(rec), irec, cbf, bd)
+
+    def intra_get_nbr(self, x, y, w, h, src, s_src, top, lcu, avail, nb, scup, coded, n_scu, i_scu, bd=8):
+        self.L.refk_intra_get_nbr(x, y, w, h, P(src), s_src, P(top), lcu, avail, ptr(nb), scup, ptr(coded),
+                                  n_scu, i_scu, bd)
+
+    def intra_pred(self, nb, dst, ipm, w, h, avail, ipf, bd=8):
+        self.L.refk_intra_pred(ptr(nb), ptr(dst), ipm, w, h, bd, avail, ipf)
+
+    def ipred_ang(self, nb, dst, i_dst, mode, w, h):
+        self.L.refk_intra_ang_entry(mode, ptr(nb), ptr(dst), i_dst, mode, w, h)
+
+    def trans_dct2(self, lw, lh, src, dst, bd=8):
+        self.L.refk_trans_dct2(lw, lh, ptr(src), ptr(dst), bd)
+
+    def trans_dct8_dst7(self, t, ln, src, dst, shift, line):
+        self.L.refk_trans_dct8_dst7(t, ln, ptr(src), ptr(dst), shift, line)
+
+    def transform(self, nxn, blk, coef, resi, lw, lh, bd=8, sec=0, alt4=0):
+        self.L.refk_transform(nxn, blk, ptr(coef), ptr(resi), lw, lh, bd, sec, alt4)
+
+    def itrans_dct2(self, lh, lw, coef, resi, bd=8):
+        self.L.refk_itrans_dct2(lh, lw, ptr(coef), ptr(resi), bd)
+
+    def itrans_dct8_dst7(self, t, ln, coef, blk, shift, line, mx, mn):
+        self.L.refk_itrans_dct8_dst7(t, ln, ptr(coef), ptr(blk), shift, line, mx, mn)
+
+    def dquant(self, flat, coef, out, wq4, wq8, lw, lh, scale, shift, bd=8):
+        self.L.refk_dquant(flat, ptr(coef), ptr(out), ptr(wq4), ptr(wq8), lw, lh, scale, shift, bd)
+
+    def invqt(self, nxn, blk, coef, resi, wq4, wq8, lw, lh, qp, bd=8, sec=0, alt4=0):
+        w4 = None if wq4 is None else ptr(wq4)
+        w8 = None if wq8 is None else ptr(wq8)
+        self.L.refk_invqt(nxn, blk, ptr(coef), ptr(resi), w4, w8, lw, lh, qp, bd, sec, alt4)
+
+    def quant_check(self, coef, num, thr):
+        return self.L.refk_quant_check(ptr(coef), num, thr)
+
+    def quant_rdoq(self, coef, num, qv, qb, es, pb, abs_coef, abs_level, err):
+        return self.L.refk_quant_rdoq(ptr(coef), num, qv, qb, es, pb, ptr(abs_coef), ptr(abs_level), ptr(err))
+
+    def dct_table(self, ln):
+        n = 1 << ln
+        return np.ctypeslib.as_array(self.L.refk_dct_table(ln), shape=(3, n, n)).copy()
+
+    def scan(self, lw, lh):
+        return np.ctypeslib.as_array(self.L.refk_scan(lw, lh), shape=(1 << (lw + lh),)).copy()
+
+
+ME_BLOCK = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
+ME_RESULT = np.dtype([("mv_int", "<i2", (2,)), ("mv_sub", "<i2", (2,)), ("sad_int", "<u4"), ("satd_sub", "<u4"),
+                      ("cost_int", "<u8"), ("cost_sub", "<u8")])
+CU = ME_BLOCK
+LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
+
+MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],
+                    [-1, 3, -7, 19, 57, -10, 4, -1]], dtype=np.int8)
+MC_CHROMA = np.array([[0, 64, 0, 0], [-4, 62, 6, 0], [-6, 56, 15, -1], [-5, 47, 25, -3], [-4, 36, 36, -4],
+                      [-3, 25, 47, -5], [-1, 15, 56, -6], [0, 6, 62, -4]], dtype=np.int8)
+
+
+def has_ref():
+    return os.path.exists(REF_SO)

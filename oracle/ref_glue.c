@@ -1,0 +1,148 @@
+/*
+ * ref_glue.c -- checker-side glue compiled together with the reference encoder's own C
+ * sources (oracle/Makefile, target "ref").  TEST INFRASTRUCTURE ONLY: nothing in the
+ * product library links or loads this.
+ *
+ * It does two things:
+ *   1. supplies empty x86 SIMD initialisers, so uavs3e_create() (src/uavs3e.c:1332-1339)
+ *      keeps the plain-C kernel table that uavs3e_funs_init_c() installs
+ *      (src/com_util.c:3131); the C table and the SIMD table encode identical bitstreams;
+ *   2. exports flat "refk_*" wrappers that call the reference's kernel-table entries
+ *      (funs_handle_t, inc/com_util.h:278-341) and exported helpers with plain pointers,
+ *      so the Python golden-vector generator and the CPU parity tests can call them
+ *      through ctypes.
+ */
+#include "define.h"
+#include "util.h"
+
+/* ---- 1. SIMD initialisers left empty (their real bodies live in src/sse, src/avx2) ---- */
+void uavs3e_funs_init_sse(void) {}
+void uavs3e_funs_init_avx2(void) {}
+int  uavs3e_simd_avx_level(int *phwavx) { if (phwavx) *phwavx = 0; return 0; }
+
+/* ---- 2. flat wrappers ---------------------------------------------------------------- */
+static int g_inited = 0;
+
+void refk_init(void)
+{
+    if (g_inited) return;
+    uavs3e_funs_init_c();           /* src/com_util.c:3131 */
+    com_scan_tbl_init();            /* src/com_util.c:1254 */
+    com_dct_coef_create();          /* src/com_tables.c:222 */
+    rdoq_init_err_scale(8);         /* src/quant.c:69 */
+    rdoq_init_prob_2_bits();        /* src/quant.c:85 */
+    g_inited = 1;
+}
+
+#define H (&uavs3e_funs_handle)
+
+u32  refk_sad(int widx, pel *o, int io, pel *p, int ip, int h) { return H->cost_sad[widx](o, io, p, ip, h); }
+void refk_sad_x3(int widx, pel *o, int io, pel *p0, pel *p1, pel *p2, int ip, u32 *s, int h) { H->cost_sad_x3[widx](o, io, p0, p1, p2, ip, s, h); }
+void refk_sad_x4(int widx, pel *o, int io, pel *p0, pel *p1, pel *p2, pel *p3, int ip, u32 *s, int h) { H->cost_sad_x4[widx](o, io, p0, p1, p2, p3, ip, s, h); }
+u64  refk_ssd(int widx, pel *o, int io, pel *p, int ip, int h) { return H->cost_ssd[widx](o, io, p, ip, h); }
+u32  refk_satd(int wi, int hi, pel *o, int io, pel *p, int ip) { return H->cost_satd[wi][hi](o, io, p, ip); }
+u32  refk_had(int w, int h, pel *o, int io, pel *p, int ip, int bd) { return com_had(w, h, o, io, p, ip, bd); }
+u32  refk_satd_intra(int w, int h, pel *o, pel *p, int io, int ip, int bd) { return calc_satd_intra(w, h, o, p, io, ip, bd); }
+
+void refk_ipcpy(int widx, const pel *s, int is, pel *d, int id, int w, int h) { H->ipcpy[widx](s, is, d, id, w, h); }
+void refk_ipflt(int t, int widx, const pel *s, int is, pel *d, int id, int w, int h, const s8 *c, int mx) { H->ipflt[t][widx](s, is, d, id, w, h, c, mx); }
+void refk_ipflt_ext(int t, int widx, const pel *s, int is, pel *d, int id, int w, int h, const s8 *cx, const s8 *cy, int mx) { H->ipflt_ext[t][widx](s, is, d, id, w, h, cx, cy, mx); }
+
+/* com_if_luma_frame (src/com_mc.c:760) on caller buffers: plane0 is the padded integer
+ * plane, planes[15] the 15 fractional planes in [dy*4+dx-1] order, all width x height
+ * with the same pad and stride (pels). */
+void refk_if_luma_frame(pel *plane0, pel **planes, int width, int height, int pad, int stride)
+{
+    com_img_t imgs[16];
+    com_img_t *list[4][4];
+    s16 *tmp[3];
+    int tmp_stride = width + 16;
+    for (int i = 0; i < 16; i++) {
+        memset(&imgs[i], 0, sizeof(com_img_t));
+        imgs[i].num_planes = 1;
+        imgs[i].width[0] = width;
+        imgs[i].height[0] = height;
+        imgs[i].stride[0] = stride * (int)sizeof(pel);
+        imgs[i].pad[0] = pad;
+        imgs[i].planes[0] = i == 0 ? plane0 : planes[i - 1];
+        list[i >> 2][i & 3] = &imgs[i];
+    }
+    for (int i = 0; i < 3; i++) tmp[i] = (s16 *)malloc(sizeof(s16) * (size_t)tmp_stride * (height + 16));
+    com_if_luma_frame(list, tmp, 8);
+    for (int i = 0; i < 3; i++) free(tmp[i]);
+}
+
+void refk_pel_diff(int widx, pel *o, int io, pel *p, int ip, s16 *r, int ir, int h) { H->pel_diff[widx](o, io, p, ip, r, ir, h); }
+void refk_pel_avrg(int widx, pel *d, int id, pel *s1, pel *s2, int h) { H->pel_avrg[widx](d, id, s1, s2, h); }
+void refk_recon(int widx, s16 *resi, pel *pred, int ipred, int w, int h, pel *rec, int irec, int cbf, int bd) { H->recon[widx](resi, pred, ipred, w, h, rec, irec, cbf, bd); }
+
+/* com_intra_get_nbr (src/com_ipred.c:40) with a plain byte map of "coded" flags of the
+ * i_scu-wide SCU grid; scup indexes that grid.  nb_out receives INTRA_NEIB_SIZE pels. */
+void refk_intra_get_nbr(int x, int y, int w, int h, pel *src, int s_src, pel *top, int lcu_size, int avail,
+                        pel *nb_out, int scup, const u8 *coded, int n_scu, int i_scu, int bd)
+{
+    static pel nb[N_C][INTRA_NEIB_SIZE];
+    com_scu_t *map = (com_scu_t *)calloc((size_t)n_scu, sizeof(com_scu_t));
+    for (int i = 0; i < n_scu; i++) map[i].coded = coded[i] ? 1 : 0;
+    memset(nb, 0, sizeof(nb));
+    com_intra_get_nbr(x, y, w, h, src, s_src, top, lcu_size, (u16)avail, nb, scup, map, i_scu, bd, Y_C);
+    memcpy(nb_out, nb[Y_C], sizeof(pel) * INTRA_NEIB_SIZE);
+    free(map);
+}
+
+/* com_intra_pred (src/com_ipred.c:733); nb points at a full INTRA_NEIB_SIZE array */
+void refk_intra_pred(pel *nb, pel *dst, int ipm, int w, int h, int bd, int avail, int ipf)
+{
+    com_intra_pred(nb + INTRA_NEIB_MID, dst, ipm, w, h, bd, (u16)avail, (u8)ipf);
+}
+
+/* one angular table entry called directly: lets the checker compare the specialised
+ * entries (e.g. intra_pred_ang[4]) with the generic ones called for the same mode */
+void refk_intra_ang_entry(int entry, pel *nb, pel *dst, int i_dst, int mode, int w, int h)
+{
+    H->intra_pred_ang[entry](nb + INTRA_NEIB_MID, dst, i_dst, mode, w, h);
+}
+
+void refk_trans_dct2(int log2w, int log2h, s16 *src, s16 *dst, int bd) { H->trans_dct2[log2w - 1][log2h - 1](src, dst, bd); }
+void refk_trans_dct8_dst7(int t, int log2n, s16 *src, s16 *dst, int shift, int line) { H->trans_dct8_dst7[t][log2n - 1](src, dst, shift, line); }
+void refk_itrans_dct2(int log2h, int log2w, s16 *coef, s16 *resi, int bd) { H->itrans_dct2[log2h - 1][log2w - 1](coef, resi, bd); }
+void refk_itrans_dct8_dst7(int t, int log2n, s16 *coef, s16 *blk, int shift, int line, int mx, int mn) { H->itrans_dct8_dst7[t][log2n - 1](coef, blk, shift, line, mx, mn); }
+void refk_dquant(int flat, s16 *coef, s16 *out, u8 *wq4, u8 *wq8, int log2w, int log2h, int scale, int shift, int bd)
+{
+    u8 *wq[2] = { wq4, wq8 };
+    H->dquant[flat ? 1 : 0](coef, out, wq, log2w, log2h, scale, shift, bd);
+}
+int refk_quant_check(s16 *coef, int num, int thr) { return H->quant_check(coef, num, thr); }
+int refk_quant_rdoq(s16 *coef, int num, int qv, int qb, int es, int pb, u32 *abs_coef, s16 *abs_level, s64 *err)
+{
+    return H->quant_rdoq(coef, num, qv, qb, es, pb, abs_coef, abs_level, err);
+}
+
+/* transform() (src/transform.c:772) and com_invqt() (src/com_itdq.c:873) for a luma TB */
+void refk_transform(int tb_nxn, int blk_idx, s16 *coef, s16 *resi, int log2w, int log2h, int bd, int sec, int alt4)
+{
+    static com_mode_t mode;
+    mode.tb_part = tb_nxn ? SIZE_NxN : SIZE_2Nx2N;
+    transform(&mode, Y_C, blk_idx, coef, resi, log2w, log2h, bd, sec, alt4);
+}
+void refk_invqt(int tb_nxn, int blk_idx, s16 *coef, s16 *resi, u8 *wq4, u8 *wq8, int log2w, int log2h, int qp, int bd, int sec, int alt4)
+{
+    static com_mode_t mode;
+    u8 *wq[2] = { wq4, wq8 };
+    mode.tb_part = tb_nxn ? SIZE_NxN : SIZE_2Nx2N;
+    com_invqt(&mode, Y_C, blk_idx, coef, resi, wq, log2w, log2h, qp, bd, sec, alt4);
+}
+
+const u16 *refk_scan(int log2w, int log2h) { return com_tbl_scan[log2w - 1][log2h - 1]; }
+const s8 *refk_dct_table(int log2n)
+{
+    switch (log2n) {
+    case 1: return &com_tbl_tm2[0][0][0];
+    case 2: return &com_tbl_tm4[0][0][0];
+    case 3: return &com_tbl_tm8[0][0][0];
+    case 4: return &com_tbl_tm16[0][0][0];
+    case 5: return &com_tbl_tm32[0][0][0];
+    default: return &com_tbl_tm64[0][0][0];
+    }
+}
+double refk_tbl_sqrt(int i) { return com_tbl_sqrt[i]; }
