@@ -1,0 +1,333 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched motion search on 1080p frames (the hot path's headline workload).
+
+One step = one 1080p frame through the GPU path: the newest reconstructed picture becomes a
+reference (device padding + 15-plane quarter-sample interpolation), then the integer full
+search (+-64, 129^2 candidates) and the half/quarter-sample SATD refinement of every block of
+the ten shapes 8x8..64x64 against 2 references.  Inputs are seeded synthetic 1080p frames
+(the external sequence is unavailable).
+
+  python bench.py [--gpus N --steps K --warmup W]         GPU path (one JSON line on rank 0)
+  python bench.py --impl reference [...]                  the CPU restatement of the same path
+
+Under torchrun each rank runs an independent replica on its own GPU (the path has no exchange
+step); value is the sum of frames over all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, N_REFS, RANGE, QP, PAD = 1920, 1080, 2, 64, 32, 144
+RING = 8                      # distinct frames cycled through (working set > L2)
+CPU_SAMPLE_ROWS = 2           # CTU rows of one frame timed for the CPU baseline
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload_config():
+    from uavs3e_gb300.synth import lambda_mv_for_qp
+    ctus = ((W + 63) // 64) * ((H + 63) // 64)
+    return {
+        "workload": "batched integer (+-64 full search) + quarter-sample SATD motion search, 1920x1080 8-bit luma, "
+                    "2 references, blocks 8x8..64x64 incl. 2:1 on the 64x64 CTU grid",
+        "width": W, "height": H, "refs": N_REFS, "search_range": RANGE, "qp": QP,
+        "lambda_mv": lambda_mv_for_qp(QP), "ctus": ctus, "blocks_per_ctu": 169,
+        "int_candidates_per_block": (2 * RANGE + 1) ** 2, "subpel_candidates_per_block": 17,
+        "parallelism": "replicas",
+    }
+
+
+def frames_ring(seed=0):
+    from uavs3e_gb300.synth import motion_sequence
+    return motion_sequence(W, H, RING, seed=seed)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region"""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.p = None
+        self.index = index
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sms, mx, reasons = [], 0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
+
+
+class CpuSearch:
+    """The oracle (C restatement, OpenMP over blocks) on the bench workload: reference planes are
+    interpolated once; time_rows() times the search of `rows` CTU rows of one frame."""
+
+    def __init__(self, frames, lam, threads=None):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import numpy as np
+        import pyoracle
+        from gpu_util import padded
+        import uavs3e_gb300 as u
+        self.np, self.pyoracle = np, pyoracle
+        self.oracle = pyoracle.Oracle()
+        self.threads = threads or os.cpu_count() or 1
+        self.lam = lam
+        self.stride = ((W + 2 * PAD) + 15) & ~15
+        self.keep, self.ptrs = [], []
+        for f in (frames[1], frames[0]):
+            p0 = padded(f, PAD, self.stride)
+            planes = [np.zeros_like(p0) for _ in range(15)]
+            base = PAD * self.stride + PAD
+            self.oracle.if_luma_frame(p0.ctypes.data + base, [p.ctypes.data + base for p in planes], W, H, PAD, self.stride)
+            self.keep += [p0] + planes
+            self.ptrs += [p0.ctypes.data + base] + [p.ctypes.data + base for p in planes]
+        self.bl = u.me_blocks(W, H)
+        self.org = np.ascontiguousarray(frames[2])
+
+    def time_rows(self, rows, first_row=4):
+        np, bl = self.np, self.bl
+        sel = ((bl[:, 1] >= first_row * 64) & (bl[:, 1] < (first_row + rows) * 64) &
+               (bl[:, 0] + bl[:, 2] <= W) & (bl[:, 1] + bl[:, 3] <= H))
+        blocks = np.zeros(int(sel.sum()), dtype=self.pyoracle.ME_BLOCK)
+        blocks["x"], blocks["y"], blocks["w"], blocks["h"] = bl[sel, 0], bl[sel, 1], bl[sel, 2], bl[sel, 3]
+        t0 = time.perf_counter()
+        self.oracle.me_frame(self.org.ctypes.data, W, self.ptrs, self.stride, W, H, N_REFS, blocks, RANGE, self.lam,
+                             threads=self.threads)
+        return time.perf_counter() - t0, len(blocks)
+
+
+def cpu_baseline(frames, lam, rows=CPU_SAMPLE_ROWS):
+    cs = CpuSearch(frames, lam)
+    dt, nb = cs.time_rows(rows)
+    ctu_rows = (H + 63) // 64
+    return {"value": (rows / ctu_rows) / dt, "unit": "frames/s", "cores": cs.threads, "kind": "port",
+            "sample": f"{rows} of {ctu_rows} CTU rows of one 1080p frame ({nb} blocks x {N_REFS} refs, integer search "
+                      f"+ refinement; reference interpolation not timed), {dt:.2f} s.  The oracle restatement is timed: "
+                      f"the reference's own sources are not present on this host"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from uavs3e_gb300.synth import lambda_mv_for_qp
+    frames = frames_ring()
+    lam = lambda_mv_for_qp(QP)
+    cs = CpuSearch(frames, lam)
+    ctu_rows = (H + 63) // 64
+    for k in range(args.warmup):
+        cs.time_rows(1, first_row=k % ctu_rows)
+    tot = 0.0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        tot += cs.time_rows(1, first_row=k % ctu_rows)[0]
+    wall = time.perf_counter() - t0
+    v = args.steps * (1.0 / ctu_rows) / tot
+    cb = {"value": v, "unit": "frames/s", "cores": cs.threads, "kind": "port",
+          "sample": f"each step: the search of 1 of {ctu_rows} CTU rows of a 1080p frame (2 refs), oracle restatement "
+                    f"on all host cores; frames/s = rows searched / {ctu_rows} / time"}
+    out = {"impl": "reference", "metric": "1080p ME frames/s", "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+           "config": workload_config(), "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import uavs3e_gb300 as u
+    from uavs3e_gb300.synth import lambda_mv_for_qp
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    u.build()
+    u.init(local)
+    lam = lambda_mv_for_qp(QP)
+    frames = frames_ring(seed=rank)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    d_frames = [torch.from_numpy(f).cuda() for f in frames]
+    ms = u.MotionSearch(W, H, n_refs=N_REFS, search_range=RANGE, pad=PAD)
+    d_out = torch.empty(ms.n_results * 32, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ms.set_ref_device(0, d_frames[0].data_ptr(), W, sp)
+
+    def step(t):
+        ms.set_ref_device((t - 1) % N_REFS, d_frames[(t - 1) % RING].data_ptr(), W, sp)
+        ms.run_device(d_frames[t % RING].data_ptr(), W, lam, d_out.data_ptr(), sp)
+
+    t = 2
+    for _ in range(max(3, args.warmup)):
+        step(t)
+        t += 1
+    torch.cuda.synchronize()
+
+    # ---- kernel path: inputs resident in HBM, L2 flushed (256 MiB write) before every step
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    u.profile_collect()
+    u.profile_enable(True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    launches0 = u.launch_count()
+    for k in range(args.steps):
+        flush.zero_()
+        evs[k][0].record(stream)
+        step(t)
+        evs[k][1].record(stream)
+        t += 1
+    torch.cuda.synchronize()
+    launches = u.launch_count() - launches0
+    clk = clocks.stop()
+    u.profile_enable(False)
+    prof = u.profile_collect()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_s = sum(step_ms) / 1000.0
+    if world > 1:
+        tt = torch.tensor([total_s], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(tt.item())
+        torch.distributed.barrier()
+    value = world * args.steps / total_s
+
+    # ---- end to end through the C ABI with host buffers (pinned), copies inside the region
+    pin = [torch.from_numpy(f).pin_memory() for f in frames]
+    h_out = torch.empty(ms.n_results * 32, dtype=torch.uint8).pin_memory()
+    torch.cuda.synchronize()
+    e2e_steps = max(5, args.steps // 2)
+    lib = u.lib()
+
+    def e2e_step(t):
+        u.check(lib.uavs3e_cuda_me_set_ref(ms.h, (t - 1) % N_REFS, pin[(t - 1) % RING].data_ptr(), W), "me_set_ref")
+        ms.run_ptr(pin[t % RING].data_ptr(), W, lam, h_out.data_ptr())
+
+    for k in range(2):
+        e2e_step(2 + k)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        e2e_step(4 + k)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    cfg = workload_config()
+    n_cand = cfg["int_candidates_per_block"]
+    gcand = N_REFS * cfg["ctus"] * 169 * n_cand  # per frame, integer candidates over all blocks
+    # roofline of the dominant kernel (integer search): SAD on the integer pipe, 4 samples per
+    # vabsdiff4; algorithmic ops = refs * picture samples * candidates / 4 per frame
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    int_peak = sm_count * 128 * sm_mhz * 1e6 / 1e9            # Gop/s, INT32 lanes x max clock
+    ms_int, n_int = prof["me_int"]
+    avg_int_ms = ms_int / max(1, args.steps)                   # both integer-search launches of a step
+    alg_ops = N_REFS * W * H * n_cand / 4.0
+    achieved = alg_ops / (avg_int_ms / 1000.0) / 1e9
+    roofline = {"bound": "int", "kernel": "k_me_int (integer full search, both launches of a frame)",
+                "achieved": achieved, "peak": int_peak, "unit": "Gop/s", "frac": achieved / int_peak,
+                "traffic": None,
+                "peak_source": f"{sm_count} SMs x 128 INT32 lanes x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); "
+                               "MEASURED_PEAKS.json has no integer peak",
+                "ops_per_launch": alg_ops, "avg_launch_ms": avg_int_ms,
+                "kernel_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in prof.items()}}
+    h2d = 2 * W * H
+    d2h = ms.n_results * 32
+    out = {
+        "metric": "1080p ME frames/s (bit-exact batched integer+quarter-sample motion search, 2 refs)",
+        "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": dict(cfg, l2="flushed (256 MiB write) before every timed step; per-step CUDA events"),
+        "gcandidates_per_s": gcand * value / 1e9,
+        "e2e": {"value": world * e2e_steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "uavs3e_cuda_me_set_ref + uavs3e_cuda_me_run with pinned host buffers"},
+        "gpu_launches": launches,
+        "gpu_launches_per_step": launches / args.steps,
+        "roofline": roofline,
+        "clocks": clk,
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(frames, lam)
+    print(json.dumps(out))
+    ms.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

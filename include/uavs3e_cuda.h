@@ -1,0 +1,150 @@
+/*
+ * uavs3e_cuda.h -- C ABI of libuavs3e_cuda, the GB300 (sm_103a) implementation of uavs3e's
+ * mode-decision hot path (8-bit luma).
+ *
+ * Two layers:
+ *   1. Batched entry points (this file): one call per frame does the work the encoder's
+ *      search loops would otherwise ask for one block at a time -- frame interpolation,
+ *      the full motion-search cost table, the intra/transform lattice.  Inputs and outputs
+ *      are plain pointers and sizes; "d_" pointers are device memory, others host memory.
+ *   2. Kernel-table entries (uavs3e_cuda_table.h): functions with the exact C signatures of
+ *      the reference's function-pointer table funs_handle_t (inc/com_util.h:278-341), and an
+ *      installer that writes them into a caller's table.
+ *
+ * Types: the reference's pel/s16/u32/u64 (inc/com_api.h:48, inc/com_system.h) are written
+ * here as uint8_t/int16_t/uint32_t/uint64_t, which is the same ABI for an 8-bit build.
+ *
+ * Errors: every int-returning call returns 0 or a negative UAVS3E_CUDA_ERR_* code, and the
+ * first failure is also kept as a sticky status (uavs3e_cuda_status).  The library never
+ * computes on the CPU: without a usable GPU the calls fail.
+ */
+#ifndef UAVS3E_CUDA_H
+#define UAVS3E_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define UAVS3E_CUDA_API __declspec(dllexport)
+#else
+#define UAVS3E_CUDA_API __attribute__((visibility("default")))
+#endif
+
+#define UAVS3E_CUDA_OK                 0
+#define UAVS3E_CUDA_ERR_ARG         (-101)   /* mirrors COM_ERR_INVALID_ARGUMENT, inc/com_api.h:61 */
+#define UAVS3E_CUDA_ERR_MEMORY      (-102)   /* mirrors COM_ERR_OUT_OF_MEMORY */
+#define UAVS3E_CUDA_ERR_UNSUPPORTED (-103)   /* mirrors COM_ERR_UNSUPPORTED */
+#define UAVS3E_CUDA_ERR_CUDA        (-110)   /* a CUDA runtime call failed */
+#define UAVS3E_CUDA_ERR_NOT_INIT    (-111)   /* no device selected / no GPU */
+#define UAVS3E_CUDA_ERR_TIMEOUT     (-112)   /* a bounded device wait gave up */
+
+/* ------------------------------------------------------------------ library state */
+
+/* Select the CUDA device used by this process and upload constant tables.  Must be called
+ * before the first other call (kernel-table entries call it lazily with device 0). */
+UAVS3E_CUDA_API int uavs3e_cuda_init(int device);
+
+/* First error since the last clear (0 if none), its text, and reset. */
+UAVS3E_CUDA_API int uavs3e_cuda_status(void);
+UAVS3E_CUDA_API const char *uavs3e_cuda_status_string(void);
+UAVS3E_CUDA_API void uavs3e_cuda_clear_status(void);
+
+/* Library version string. */
+UAVS3E_CUDA_API const char *uavs3e_cuda_version(void);
+
+/* Kernel timing (observability; the reference has none): while enabled, every launch of the
+ * batched kernels is bracketed by CUDA events on its stream.  collect() waits for them and
+ * returns, per kernel id (0 pad, 1 frame interpolation, 2 integer search, 3 fractional
+ * refinement), the summed milliseconds and launch counts, then forgets them. */
+UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
+/* Number of kernels this library has launched in this process. */
+UAVS3E_CUDA_API unsigned long long uavs3e_cuda_launch_count(void);
+UAVS3E_CUDA_API int uavs3e_cuda_profile_collect(double ms[], int counts[], int n);
+
+/* ------------------------------------------------------------ frame interpolation */
+
+/*
+ * The 15 quarter-sample luma planes of a padded reference picture, identical to
+ * com_if_luma_frame (src/com_mc.c:760-800) followed by its padding of each plane
+ * (com_img_padding(img, 1, 4), src/com_util.c:148).  Replaces the per-frame call of the
+ * ip_flt_y_hor / ip_flt_y_ver / ip_flt_y_ver_ext entries (inc/com_util.h:304-306).
+ *   d_plane0   : device pointer to sample (0,0) of the integer plane, padded by >= pad
+ *                (pad >= 8) with its edges replicated (com_img_padding(img, 3, 0));
+ *   d_planes   : 15 device pointers to sample (0,0) of the output planes, index
+ *                dy*4 + dx - 1 for quarter-sample phase (dx, dy); every sample of the padded
+ *                plane [-pad, width+pad) x [-pad, height+pad) is written;
+ *   stride     : samples per row of all 16 planes;
+ *   stream     : cudaStream_t (NULL = legacy default stream); the call does not synchronise.
+ */
+UAVS3E_CUDA_API int uavs3e_cuda_subpel_planes(const uint8_t *d_plane0, uint8_t *const d_planes[15], int width,
+                                              int height, int pad, int stride, void *stream);
+
+/* Replicate the edge samples of a picture into its padding (com_img_padding with ext 0,
+ * src/com_util.c:148, one luma plane). */
+UAVS3E_CUDA_API int uavs3e_cuda_pad_plane(uint8_t *d_plane0, int width, int height, int pad, int stride, void *stream);
+
+/* ------------------------------------------------------------ batched motion search */
+
+/*
+ * A motion-search session holds, resident in HBM, the reference pictures (integer plane plus
+ * the 15 fractional planes each) and the search tables of one picture size.  One call per
+ * frame computes, for every block of the ten shapes 8x8, 16x8, 8x16, 16x16, 32x16, 16x32,
+ * 32x32, 64x32, 32x64, 64x64 on the 64x64 CTU grid and every reference:
+ *   - the integer full search over [-range, range]^2 (range <= 64; clipped as
+ *     get_max_search_range, src/me.c:502-527, with is_padding = 1), cost
+ *     (SAD << 16) + (mvbits(4dx) + mvbits(4dy)) * lambda_mv, predictor (0,0), first minimum
+ *     in raster order (dy outer, dx inner) -- the costs the encoder's search_raster /
+ *     search_diamond (src/me.c:103-355) evaluate with cost_sad;
+ *   - the quarter-sample refinement of me_sub_pel_search (src/me.c:366-500) with the SATD
+ *     cost (com_had): centre, 8 half-sample, then 8 quarter-sample neighbours.
+ * Results are indexed [ctu][block][ref], ctu in raster order of the CTU grid, block as
+ * uavs3e_cuda_me_block_table; blocks that do not fit inside the picture have cost fields
+ * set to UINT64_MAX.
+ */
+typedef struct uavs3e_cuda_me uavs3e_cuda_me;
+
+typedef struct {
+    int16_t  mv_int[2];   /* best integer MV (integer samples)                    */
+    int16_t  mv_sub[2];   /* best MV after refinement (quarter samples)           */
+    uint32_t sad_int;     /* SAD at mv_int                                        */
+    uint32_t satd_sub;    /* com_had SATD at mv_sub                               */
+    uint64_t cost_int;    /* (sad_int << 16) + mvbits * lambda_mv                 */
+    uint64_t cost_sub;    /* (satd_sub << 16) + mvbits * lambda_mv                */
+} uavs3e_cuda_me_result_t;
+
+/* (x, y, w, h) inside the CTU of the 169 blocks, in result order */
+UAVS3E_CUDA_API int uavs3e_cuda_me_block_table(int out[169][4]);
+
+/* pad: reference padding in samples (>= 144, the encoder's PIC_PAD_SIZE_L); n_refs <= 4 */
+UAVS3E_CUDA_API uavs3e_cuda_me *uavs3e_cuda_me_open(int width, int height, int n_refs, int range, int pad);
+UAVS3E_CUDA_API void uavs3e_cuda_me_close(uavs3e_cuda_me *me);
+UAVS3E_CUDA_API int uavs3e_cuda_me_num_results(const uavs3e_cuda_me *me);
+
+/* Make picture `plane` (host, width x height, row stride in samples) reference `slot`:
+ * upload, pad and interpolate it on the GPU.  The hook point in the encoder is the
+ * per-reference com_if_luma_frame call (src/uavs3e.c:1088). */
+UAVS3E_CUDA_API int uavs3e_cuda_me_set_ref(uavs3e_cuda_me *me, int slot, const uint8_t *plane, int stride);
+/* same from a device picture, enqueued on `stream` */
+UAVS3E_CUDA_API int uavs3e_cuda_me_set_ref_device(uavs3e_cuda_me *me, int slot, const uint8_t *d_plane, int stride,
+                                                  void *stream);
+
+/* Search one frame: host org in, host results out (num_results records); synchronous. */
+UAVS3E_CUDA_API int uavs3e_cuda_me_run(uavs3e_cuda_me *me, const uint8_t *org, int i_org, uint32_t lambda_mv,
+                                       uavs3e_cuda_me_result_t *out);
+/* Search one frame from device org into device results, enqueued on `stream`. */
+UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *me, const uint8_t *d_org, int i_org,
+                                              uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);
+
+/* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
+ * session's plane stride; for inspection by tests. */
+UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *me, int slot, int phase);
+UAVS3E_CUDA_API int uavs3e_cuda_me_plane_stride(const uavs3e_cuda_me *me);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,63 @@
+// Internal declarations shared between the .cu translation units of libuavs3e_cuda.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "common.cuh"
+
+namespace uc {
+
+struct PlaneSet15 { pel *p[15]; };
+
+constexpr int ME_MAX_REFS = 4;
+constexpr int ME_CTU = 64;
+constexpr int ME_BLOCKS_PER_CTU = 169;
+constexpr int ME_GROUPS = 16;          // lane groups (half-warps) per search CTA
+constexpr int ME_RANK_BITS = 11;
+constexpr int ME_MAX_GROUP = 1 << ME_RANK_BITS;
+
+// canonical per-CTU block list: shapes 8x8, 16x8, 8x16, 16x16, 32x16, 16x32, 32x32, 64x32,
+// 32x64, 64x64, each in raster order of its positions inside the 64x64 CTU
+struct CtuBlock { u8 x, y, w, h; };
+void ctu_block_table(CtuBlock out[ME_BLOCKS_PER_CTU]);
+
+// result record of one (block, reference), same layout as uavs3e_cuda_me_result_t
+struct MeResult {
+    s16 mv_int[2];
+    s16 mv_sub[2];
+    u32 sad_int;
+    u32 satd_sub;
+    u64 cost_int;
+    u64 cost_sub;
+};
+
+// optional per-kernel timing with CUDA events on the launching stream
+enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_N = 8 };
+void prof_begin(int k, cudaStream_t st);
+void prof_end(int k, cudaStream_t st);
+void count_launch(int n);
+
+int launch_subpel_planes(const pel *src, int stride, int W, int H, int pad, const PlaneSet15 &out, cudaStream_t st);
+
+// integer search + quarter-sample refinement over every CTU block of the frame
+struct MeFrameArgs {
+    const pel *org; int i_org;
+    const pel *planes[ME_MAX_REFS][16]; int i_ref, pad;
+    int W, H, n_refs, range;
+    u32 lambda_mv;
+    MeResult *out;                      // [n_ctu][169][n_refs]
+    // device copies of the host-built search tables (me_build_tables)
+    const u32 *q2tab; const u16 *rank2mv;
+};
+
+struct MeTables {
+    int lo_x, hi_x, lo_y, hi_y, ndx, ndy, nchunk, n_items, ndy_per_item;
+    u32 lambda_mv;
+};
+// builds the packed (q << 11 | rank) table and the rank -> raster map on the host
+int me_build_tables(int W, int H, int range, u32 lambda_mv, int ndy_per_item, MeTables *t,
+                    u32 *q2tab, u16 *rank2mv, size_t q2cap);
+size_t me_q2_entries(int range, int ndy_per_item);
+size_t me_key_scratch_bytes(int W, int H, int n_refs);
+int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStream_t st);
+
+}  // namespace uc
