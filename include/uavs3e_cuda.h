@@ -144,6 +144,41 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *me, const uint8_t 
 UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *me, int slot, int phase);
 UAVS3E_CUDA_API int uavs3e_cuda_me_plane_stride(const uavs3e_cuda_me *me);
 
+/* ------------------------------------------------------------ batched intra lattice */
+
+/*
+ * Intra mode decision lattice.  For every CU and every luma intra mode 0..32 this computes what
+ * the encoder's intra search evaluates per candidate: the neighbour array of the CU read from
+ * `rec` (com_intra_get_nbr, src/com_ipred.c:40, with every in-picture sample outside the CU
+ * treated as reconstructed), the prediction (com_intra_pred, :733, IPF on or off), its SATD
+ * (calc_satd_intra, src/util.c:200), the forward DCT2 of the residual (trans_dct2,
+ * src/transform.c:253-412) and, for each QP, the first RDOQ pass (quant_check + quant_rdoq,
+ * src/com_itdq.c:910-954, parameters of rdoq_quant_block src/quant.c:196-231; the context-
+ * dependent second pass stays with the CPU), dequantisation (com_dquant :807), inverse DCT2
+ * (itrans_dct2 :264-423) and reconstruction (com_recon src/com_util.c:3107).
+ *   satd[cu*33 + mode]; q[(cu*33 + mode)*n_qp + qp_index]  (n_qp <= 4)
+ * CU sides are powers of two in 4..64 inside the picture (others yield zeroed records).
+ */
+typedef struct { int16_t x, y; uint8_t w, h; uint16_t pad; } uavs3e_cuda_cu_t;
+
+typedef struct {
+    uint32_t ssd;         /* SSD(org, reconstruction)                                  */
+    uint32_t coef_hash;   /* sum over non-zero levels of fmix32(pos << 16 | (u16)level) */
+    uint16_t num_nz;      /* non-zero levels                                           */
+    int16_t  last_nz;     /* last non-zero level in zig-zag scan order, -1 if none     */
+    uint32_t sum_abs;     /* sum of |level|                                            */
+} uavs3e_cuda_lat_q_t;
+
+/* The 23-shape lattice (w, h in 4..64, aspect <= 8, largest first) of a picture: writes up to
+ * cap records to out (may be NULL) and returns the total count. */
+UAVS3E_CUDA_API int uavs3e_cuda_lattice_cus(int width, int height, uavs3e_cuda_cu_t *out, int cap);
+
+/* device buffers in and out, enqueued on `stream`; qps is a host array */
+UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i_org, const uint8_t *d_rec, int i_rec,
+                                                     int width, int height, const uavs3e_cuda_cu_t *d_cus, int n_cus,
+                                                     int ipf, const int *qps, int n_qp, int is_intra_slice,
+                                                     uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1120,14 +1120,20 @@ void orc_me_frame(const pel *org, int i_org, const pel *const *planes, int i_ref
 
 /* ===================================================================== batched: intra */
 
+/* MurmurHash3's 32-bit finaliser */
+static u32 fmix32(u32 h)
+{
+    h ^= h >> 16; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16;
+    return h;
+}
+
+/* order-independent hash of a level block: sum over non-zero levels of
+ * fmix32(raster_position << 16 | (u16)level) */
 u32 orc_level_hash(const s16 *lev, int n)
 {
-    u32 hsh = 2166136261u;
-    for (int i = 0; i < n; i++) {
-        u16 v = (u16)lev[i];
-        hsh = (hsh ^ (v & 0xFF)) * 16777619u;
-        hsh = (hsh ^ (v >> 8)) * 16777619u;
-    }
+    u32 hsh = 0;
+    for (int i = 0; i < n; i++)
+        if (lev[i]) hsh += fmix32(((u32)i << 16) | (u16)lev[i]);
     return hsh;
 }
 

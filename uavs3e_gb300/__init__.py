@@ -53,6 +53,8 @@ def _declare(L):
     L.uavs3e_cuda_me_plane.restype = P
     L.uavs3e_cuda_me_plane.argtypes = [P, I, I]
     L.uavs3e_cuda_me_plane_stride.argtypes = [P]
+    L.uavs3e_cuda_lattice_cus.argtypes = [I, I, P, I]
+    L.uavs3e_cuda_intra_lattice_device.argtypes = [P, I, P, I, I, I, P, I, I, P, I, I, P, P, P]
     L.uavs3e_cuda_profile_enable.argtypes = [I]
     L.uavs3e_cuda_launch_count.restype = C.c_ulonglong
     L.uavs3e_cuda_profile_collect.argtypes = [P, P, I]
@@ -71,7 +73,38 @@ def init(device=0):
     check(lib().uavs3e_cuda_init(device), "uavs3e_cuda_init")
 
 
-PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub")
+PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice")
+
+CU = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
+LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
+
+
+def lattice_cus(width, height):
+    """the 23-shape CU lattice of a picture (largest shapes first)"""
+    n = lib().uavs3e_cuda_lattice_cus(width, height, None, 0)
+    out = np.zeros(n, dtype=CU)
+    lib().uavs3e_cuda_lattice_cus(width, height, out.ctypes.data, n)
+    return out
+
+
+def intra_lattice(org, rec, cus, qps=(27, 32, 37, 42), ipf=0, is_intra=1, stream=None):
+    """Intra lattice on the GPU from host arrays; returns (satd[n_cus*33], q[n_cus*33*n_qp])."""
+    import torch
+    H, W = org.shape
+    d_org = torch.from_numpy(np.ascontiguousarray(org)).cuda()
+    d_rec = torch.from_numpy(np.ascontiguousarray(rec)).cuda()
+    d_cus = torch.from_numpy(np.ascontiguousarray(cus).view(np.uint8)).cuda()
+    n = len(cus)
+    q = np.ascontiguousarray(qps, dtype=np.int32)
+    d_satd = torch.zeros(max(1, n * 33), dtype=torch.int32, device="cuda")
+    d_q = torch.zeros(max(1, n * 33 * len(q) * LAT_Q.itemsize), dtype=torch.uint8, device="cuda")
+    sp = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_intra_lattice_device(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H, d_cus.data_ptr(), n,
+                                                 ipf, q.ctypes.data, len(q), is_intra, d_satd.data_ptr(),
+                                                 d_q.data_ptr(), sp), "intra_lattice")
+    torch.cuda.synchronize()
+    return (d_satd.cpu().numpy().view(np.uint32)[:n * 33].copy(),
+            d_q.cpu().numpy().view(LAT_Q)[:n * 33 * len(q)].copy())
 
 
 def profile_enable(on=True):

@@ -214,6 +214,7 @@ struct uavs3e_cuda_me {
     pel *org_buf = nullptr;           // W x H for host runs
     MeResult *out_buf = nullptr;      // device results for host runs
     u64 *keys = nullptr;              // per-block integer winners
+    u32 *sub = nullptr;               // per-candidate SATD sums of the refinement
     u32 *q2 = nullptr;                // device search tables
     u16 *r2m = nullptr;
     MeTables tab;
@@ -269,6 +270,7 @@ UAVS3E_CUDA_API uavs3e_cuda_me *uavs3e_cuda_me_open(int width, int height, int n
               cudaMalloc(&m->org_buf, (size_t)width * height) == cudaSuccess &&
               cudaMalloc(&m->out_buf, nres * sizeof(MeResult)) == cudaSuccess &&
               cudaMalloc(&m->keys, me_key_scratch_bytes(width, height, n_refs)) == cudaSuccess &&
+              cudaMalloc(&m->sub, me_sub_scratch_bytes(width, height, n_refs)) == cudaSuccess &&
               cudaMalloc(&m->q2, me_q2_entries(range, kNdy) * sizeof(u32)) == cudaSuccess &&
               cudaMalloc(&m->r2m, (size_t)ME_GROUPS * ME_MAX_GROUP * sizeof(u16)) == cudaSuccess &&
               cudaMemset(m->planes_buf, 0, m->plane_bytes * 16 * n_refs) == cudaSuccess;
@@ -285,7 +287,7 @@ UAVS3E_CUDA_API void uavs3e_cuda_me_close(uavs3e_cuda_me *m)
     if (!m) return;
     if (m->st) cudaStreamSynchronize(m->st);
     cudaFree(m->planes_buf); cudaFree(m->org_buf); cudaFree(m->out_buf);
-    cudaFree(m->keys); cudaFree(m->q2); cudaFree(m->r2m);
+    cudaFree(m->keys); cudaFree(m->sub); cudaFree(m->q2); cudaFree(m->r2m);
     if (m->st) cudaStreamDestroy(m->st);
     delete m;
 }
@@ -337,7 +339,7 @@ static int me_launch(uavs3e_cuda_me *m, const pel *d_org, int i_org, u32 lambda,
         for (int q = 0; q < 16; q++) a.planes[s][q] = me_plane_ptr(m, s, q);
     a.i_ref = m->stride; a.pad = m->pad;
     a.W = m->W; a.H = m->H; a.n_refs = m->n_refs; a.range = m->range; a.lambda_mv = lambda;
-    a.out = d_out; a.q2tab = m->q2; a.rank2mv = m->r2m;
+    a.out = d_out; a.q2tab = m->q2; a.rank2mv = m->r2m; a.sub_scratch = m->sub;
     return launch_me_frame(a, m->tab, m->keys, st);
 }
 

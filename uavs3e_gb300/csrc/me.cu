@@ -58,6 +58,12 @@ size_t me_q2_entries(int range, int ndy_per_item)
     return (size_t)nd * nchunk * ndy_per_item;
 }
 
+size_t me_sub_scratch_bytes(int W, int H, int n_refs)
+{
+    size_t nctu = (size_t)((W + 63) / 64) * ((H + 63) / 64);
+    return nctu * n_refs * ME_BLOCKS_PER_CTU * 17 * sizeof(u32);
+}
+
 size_t me_key_scratch_bytes(int W, int H, int n_refs)
 {
     size_t nctu = (size_t)((W + 63) / 64) * ((H + 63) / 64);
@@ -115,7 +121,8 @@ struct MeIntParams {
     const u32 *q2tab; const u16 *rank2mv;
     u64 *keys;             // [ctu][ref][169]
     int n_refs;
-    int win_h, win_ww;     // window rows, words per row
+    int win_h, win_ww;     // window rows, words per stored row (incl. skew room)
+    int win_cols;          // window data bytes per row
     int pad;               // reference padding (samples)
     int edge, nx_int, ny_int, ctus_h;   // CTU subset of this launch (see ctu_of)
 };
@@ -132,9 +139,17 @@ __device__ __forceinline__ void ctu_of(const MeIntParams &P, int i, int *col, in
     *col = i % P.nx_int; *row = P.ny_int + i / P.nx_int;
 }
 
-__device__ __forceinline__ void upd(u32 &b, u32 sad, u32 q2, bool ok)
+// word skew of window row r: rows 16 apart (the four sub-block rows of a half-warp) land on
+// bank offsets 0, 16, 2, 18, which with the 4-word column steps of the sub-block columns
+// gives 16 distinct even banks per half-warp
+__device__ __forceinline__ int win_skew(int r)
 {
-    u32 v = (sad << ME_RANK_BITS) + q2;
+    int t = (r >> 4) & 3;
+    return ((t & 1) << 4) | ((t >> 1) << 1);
+}
+
+__device__ __forceinline__ void upd(u32 &b, u32 v, bool ok)
+{
     if (ok) b = min(b, v);
 }
 
@@ -152,15 +167,17 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
     const int tid = threadIdx.x;
     const pel *rp = P.ref[ref];
 
-    // ---- stage the search window: rows cy+lo_y .., columns from a 16-byte boundary
+    // ---- stage the search window: rows cy+lo_y .., columns from a 16-byte boundary.
+    // Row r is stored at word r*win_ww + skew(r): the 16 lanes of a half-warp read rows 16
+    // apart, and the skew spreads them over distinct banks.
     const pel *g0 = rp + (long long)(cy + P.lo_y) * P.i_ref + (cx + P.lo_x);
     const int off = (int)(((uintptr_t)g0) & 15);
     const pel *gw = g0 - off;
-    const int wbytes = P.win_ww * 4;
+    const int wwords = P.win_cols >> 2;                 // words of window data per row
     // columns past the right padding are never read by a valid candidate: filled with 0
-    const int gcol0 = cx + P.lo_x - off, gcol_end = P.W + P.pad;   // first column, bound
+    const int gcol0 = cx + P.lo_x - off, gcol_end = P.W + P.pad;
     if ((P.i_ref & 15) == 0) {
-        const int nv = wbytes >> 4;
+        const int nv = wwords >> 2;
         for (int i = tid; i < P.win_h * nv; i += blockDim.x) {
             int r = i / nv, c = i % nv;
             uint4 v;
@@ -177,13 +194,18 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
                 }
                 v = make_uint4(wv[0], wv[1], wv[2], wv[3]);
             }
-            reinterpret_cast<uint4 *>(win)[r * nv + c] = v;
+            u32 *d = win + r * P.win_ww + win_skew(r) + 4 * c;
+            d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
         }
     } else {
-        pel *wb = reinterpret_cast<pel *>(win);
-        for (int i = tid; i < P.win_h * wbytes; i += blockDim.x) {
-            int r = i / wbytes, c = i % wbytes;
-            wb[r * wbytes + c] = gcol0 + c < gcol_end ? gw[(long long)r * P.i_ref + c] : (pel)0;
+        for (int i = tid; i < P.win_h * wwords; i += blockDim.x) {
+            int r = i / wwords, c = i % wwords;
+            u32 v = 0;
+            for (int b = 0; b < 4; b++) {
+                int col = 4 * c + b;
+                if (gcol0 + col < gcol_end) v |= (u32)gw[(long long)r * P.i_ref + col] << (8 * b);
+            }
+            win[r * P.win_ww + win_skew(r) + c] = v;
         }
     }
     for (int i = tid; i < ME_BLOCKS_PER_CTU; i += blockDim.x) skey[i] = ~0ull;
@@ -227,7 +249,8 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
         const int dx = P.lo_x + dxi, dy0 = P.lo_y + dyc * NDY;
         const int bx = off + 16 * sx + dxi;
         const int sh = bx & 3;
-        const u32 *wrow = win + (16 * sy + dyc * NDY) * P.win_ww + (bx >> 2);
+        const int row0 = 16 * sy + dyc * NDY;
+        const u32 *wrow = win + row0 * P.win_ww + (bx >> 2);
 
         u32 acc[NDY][4];
 #pragma unroll
@@ -237,7 +260,7 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
 
 #pragma unroll
         for (int rr = 0; rr < 16 + NDY - 1; rr++) {
-            const u32 *wp = wrow + rr * P.win_ww;
+            const u32 *wp = wrow + rr * P.win_ww + win_skew(row0 + rr);
             const u32 w0 = wp[0], w1 = wp[1], w2 = wp[2], w3 = wp[3], w4 = wp[4];
             const u32 a0 = align4(w0, w1, sh), a1 = align4(w1, w2, sh);
             const u32 a2 = align4(w2, w3, sh), a3 = align4(w3, w4, sh);
@@ -262,29 +285,34 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
             bool vx0 = true, vx1 = true, vy0 = true, vy1 = true;
             if (EDGE) { vx0 = dx <= lim_x0; vx1 = dx <= lim_x1; vy0 = dy <= lim_y0; vy1 = dy <= lim_y1; }
             const u32 t00 = acc[j][0], t01 = acc[j][1], t10 = acc[j][2], t11 = acc[j][3];
-            upd(best[0], t00, q2, ok && vx0 && vy0);
-            upd(best[1], t01, q2, ok && vx1 && vy0);
-            upd(best[2], t10, q2, ok && vx0 && vy1);
-            upd(best[3], t11, q2, ok && vx1 && vy1);
-            upd(best[4], t00 + t01, q2, ok && vx0 && vy0);      // 16x8 top
-            upd(best[5], t10 + t11, q2, ok && vx0 && vy1);      // 16x8 bottom
-            upd(best[6], t00 + t10, q2, ok && vx0 && vy0);      // 8x16 left
-            upd(best[7], t01 + t11, q2, ok && vx1 && vy0);      // 8x16 right
-            const u32 s16 = t00 + t01 + t10 + t11;
-            const bool v00 = ok && vx0 && vy0;
-            upd(best[8], s16, q2, v00);
-            const u32 s32x16 = s16 + __shfl_xor_sync(0xFFFFFFFFu, s16, 1);
-            const u32 s16x32 = s16 + __shfl_xor_sync(0xFFFFFFFFu, s16, 4);
-            const u32 s32 = s32x16 + __shfl_xor_sync(0xFFFFFFFFu, s32x16, 4);
-            const u32 s64x32 = s32 + __shfl_xor_sync(0xFFFFFFFFu, s32, 2);
-            const u32 s32x64 = s32 + __shfl_xor_sync(0xFFFFFFFFu, s32, 8);
-            const u32 s64 = s64x32 + __shfl_xor_sync(0xFFFFFFFFu, s64x32, 8);
-            upd(best[9], s32x16, q2, v00);
-            upd(best[10], s16x32, q2, v00);
-            upd(best[11], s32, q2, v00);
-            upd(best[12], s64x32, q2, v00);
-            upd(best[13], s32x64, q2, v00);
-            upd(best[14], s64, q2, v00);
+            // keys (sad << 11) + q2, sums of keys formed as a + b - q2 (exact modulo 2^32)
+            const u32 v00 = (t00 << ME_RANK_BITS) + q2, v01 = (t01 << ME_RANK_BITS) + q2;
+            const u32 v10 = (t10 << ME_RANK_BITS) + q2, v11 = (t11 << ME_RANK_BITS) + q2;
+            const u32 vt = v00 + (t01 << ME_RANK_BITS), vb = v10 + (t11 << ME_RANK_BITS);
+            const u32 vl = v00 + (t10 << ME_RANK_BITS), vr = v01 + (t11 << ME_RANK_BITS);
+            const u32 v16 = vt + vb - q2;
+            const bool v00ok = ok && vx0 && vy0;
+            upd(best[0], v00, v00ok);
+            upd(best[1], v01, ok && vx1 && vy0);
+            upd(best[2], v10, ok && vx0 && vy1);
+            upd(best[3], v11, ok && vx1 && vy1);
+            upd(best[4], vt, v00ok);                  // 16x8 top
+            upd(best[5], vb, ok && vx0 && vy1);       // 16x8 bottom
+            upd(best[6], vl, v00ok);                  // 8x16 left
+            upd(best[7], vr, ok && vx1 && vy0);       // 8x16 right
+            upd(best[8], v16, v00ok);
+            const u32 v32x16 = v16 + __shfl_xor_sync(0xFFFFFFFFu, v16, 1) - q2;
+            const u32 v16x32 = v16 + __shfl_xor_sync(0xFFFFFFFFu, v16, 4) - q2;
+            const u32 v32 = v32x16 + __shfl_xor_sync(0xFFFFFFFFu, v32x16, 4) - q2;
+            const u32 v64x32 = v32 + __shfl_xor_sync(0xFFFFFFFFu, v32, 2) - q2;
+            const u32 v32x64 = v32 + __shfl_xor_sync(0xFFFFFFFFu, v32, 8) - q2;
+            const u32 v64 = v64x32 + __shfl_xor_sync(0xFFFFFFFFu, v64x32, 8) - q2;
+            upd(best[9], v32x16, v00ok);
+            upd(best[10], v16x32, v00ok);
+            upd(best[11], v32, v00ok);
+            upd(best[12], v64x32, v00ok);
+            upd(best[13], v32x64, v00ok);
+            upd(best[14], v64, v00ok);
         }
     }
 
@@ -324,6 +352,13 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
 }
 
 // ---------------------------------------------------------------- fractional refinement
+//
+// Task grid: one thread per (block, reference, candidate, com_had tile).  Stage 1 evaluates
+// the centre and the 8 half-sample points, stage 2 the 8 quarter-sample points around the
+// stage-1 winner (each stage-2 thread re-derives that winner from the stage-1 sums), and a
+// final pass picks the stage-2 winner.  Tile SATDs are summed per (block, reference,
+// candidate) with global atomics; candidate order and the strict '<' of me_sub_pel_search
+// are applied in the selection.
 
 struct MeSubParams {
     const pel *org; int i_org;
@@ -333,12 +368,19 @@ struct MeSubParams {
     u32 lambda_mv;
     double sq32, sq128;
     const u64 *keys;
+    u32 *satd1;          // [item][9]
+    u32 *satd2;          // [item][8]
     MeResult *out;
+    long long task_base[11];   // prefix of tasks per shape class
 };
 
 __constant__ s8 kHalfPat[8][2] = { { -2, 0 }, { -2, 2 }, { 0, 2 }, { 2, 2 }, { 2, 0 }, { 2, -2 }, { 0, -2 }, { -2, -2 } };
 __constant__ s8 kQuarPat[8][2] = { { -1, 0 }, { 0, 1 }, { 1, 0 }, { 0, -1 }, { -1, 1 }, { 1, 1 }, { -1, -1 }, { 1, -1 } };
 __constant__ CtuBlock kCtuBlocks[ME_BLOCKS_PER_CTU];
+// shape classes of the CTU block table: first block index, count, width, height
+__constant__ int kShapeFirst[11] = { 0, 64, 96, 128, 144, 152, 160, 164, 166, 168, 169 };
+__constant__ u8 kShapeWH[10][2] = { { 8, 8 }, { 16, 8 }, { 8, 16 }, { 16, 16 }, { 32, 16 }, { 16, 32 }, { 32, 32 },
+                                   { 64, 32 }, { 32, 64 }, { 64, 64 } };
 
 // com_mc_blk_luma_pointer (src/com_mc.c:89-101) for a block at (x, y) with qpel MV (mvx, mvy)
 __device__ __forceinline__ const pel *mc_ptr(const MeSubParams &P, int ref, int x, int y, int mvx, int mvy)
@@ -348,92 +390,199 @@ __device__ __forceinline__ const pel *mc_ptr(const MeSubParams &P, int ref, int 
     return P.planes[ref][(qy & 3) * 4 + (qx & 3)] + (long long)py * P.i_ref + px;
 }
 
-// one warp per (CTU block, reference)
-__global__ void __launch_bounds__(128) k_me_sub(MeSubParams P)
+// 8 samples at p (any alignment) as two little-endian words; reads only words that hold
+// requested samples
+__device__ __forceinline__ void load8(const pel *p, u32 &lo, u32 &hi)
 {
-    __shared__ u32 s_satd[4][9];
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long item = (long long)blockIdx.x * 4 + wib;
-    const long long total = (long long)P.n_ctu * ME_BLOCKS_PER_CTU * P.n_refs;
-    if (item >= total) return;
-    const int ref = (int)(item % P.n_refs);
-    const int lb = (int)((item / P.n_refs) % ME_BLOCKS_PER_CTU);
-    const int ctu = (int)(item / P.n_refs / ME_BLOCKS_PER_CTU);
-    const CtuBlock cb = kCtuBlocks[lb];
-    const int x = (ctu % P.ctus_w) * ME_CTU + cb.x, y = (ctu / P.ctus_w) * ME_CTU + cb.y;
-    const int w = cb.w, h = cb.h;
-    MeResult *o = P.out + item;
-    const u64 key = P.keys[((size_t)ctu * P.n_refs + ref) * ME_BLOCKS_PER_CTU + lb];
-    if (x + w > P.W || y + h > P.H || key == ~0ull) {
-        if (lane == 0) {
-            MeResult r = {};
-            r.cost_int = ~0ull; r.cost_sub = ~0ull;
-            *o = r;
-        }
-        return;
-    }
-    const u32 raster = (u32)(key & 0x7FFF);
-    const u64 cost_int = key >> 15;
-    const int dx = P.lo_x + (int)(raster % P.ndx), dy = P.lo_y + (int)(raster / P.ndx);
-    const u32 mvc_int = (mvbits(4 * dx) + mvbits(4 * dy)) * P.lambda_mv;
+    const uintptr_t a = (uintptr_t)p;
+    const u32 *q = (const u32 *)(a & ~(uintptr_t)3);
+    const u32 sh = (u32)(a & 3) * 8;
+    const u32 w0 = __ldg(q), w1 = __ldg(q + 1);
+    const u32 w2 = sh ? __ldg(q + 2) : 0u;
+    lo = __funnelshift_r(w0, w1, sh);
+    hi = __funnelshift_r(w1, w2, sh);
+}
 
+// magnitude sum of the 2-D WHT of the 8x8 difference org - pred; with o2/p2 the second 8x8
+// half of a 16x8 / 8x16 tile is folded in as first + sgn * second (the first stage of the
+// 16-point transform).  Rows are transformed as they are loaded.
+__device__ __noinline__ int satd8x8_raw(const pel *o, int io, const pel *p, int ip, const pel *o2, const pel *p2,
+                                           int sgn)
+{
+    int d[64];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        u32 ol, oh, pl, ph;
+        load8(o + r * io, ol, oh);
+        load8(p + r * ip, pl, ph);
+        int v[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const u32 ow = c < 4 ? ol : oh, pw = c < 4 ? pl : ph;
+            v[c] = (int)((ow >> (8 * (c & 3))) & 255) - (int)((pw >> (8 * (c & 3))) & 255);
+        }
+        if (o2) {
+            load8(o2 + r * io, ol, oh);
+            load8(p2 + r * ip, pl, ph);
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const u32 ow = c < 4 ? ol : oh, pw = c < 4 ? pl : ph;
+                v[c] += sgn * ((int)((ow >> (8 * (c & 3))) & 255) - (int)((pw >> (8 * (c & 3))) & 255));
+            }
+        }
+        wht<8>(v);
+#pragma unroll
+        for (int c = 0; c < 8; c++) d[r * 8 + c] = v[c];
+    }
+    int s = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        int col[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) col[r] = d[r * 8 + c];
+        wht<8>(col);
+#pragma unroll
+        for (int r = 0; r < 8; r++) s += abs(col[r]);
+    }
+    return s;
+}
+
+// com_had tile SATD for the ME tile shapes 8x8 / 16x8 / 8x16.  For 16x8 (8x16) the 16-point
+// transform's first stage forms left+right and left-right (top+bottom, top-bottom); the
+// magnitude sum is the sum of the two 8x8 transforms of those.
+__device__ __forceinline__ u32 me_tile_satd(int tw, int th, const pel *o, int io, const pel *p, int ip, double sq128)
+{
+    if (tw == 8 && th == 8) return (u32)((satd8x8_raw(o, io, p, ip, nullptr, nullptr, 0) + 2) >> 2);
+    const int bo = tw == 16 ? 8 : 8 * io, bp = tw == 16 ? 8 : 8 * ip;
+    int s = satd8x8_raw(o, io, p, ip, o + bo, p + bp, 1);
+    s += satd8x8_raw(o, io, p, ip, o + bo, p + bp, -1);
+    return (u32)(int)((double)s / sq128 * 2.0);
+}
+
+struct SubTask { int item, ctu, b, ref, cand, tile, x, y, w, h, tw, th; };
+
+__device__ __forceinline__ bool decode_task(const MeSubParams &P, long long t, int ncand, SubTask &k)
+{
+    int s = 0;
+    while (s < 9 && t >= P.task_base[s + 1]) s++;
+    long long l = t - P.task_base[s];
+    const int w = kShapeWH[s][0], h = kShapeWH[s][1];
     int tw, th;
     had_tile_shape(w, h, &tw, &th);
-    const int ntx = w / tw, ntiles = ntx * (h / th);
-    const pel *ob = P.org + (long long)y * P.i_org + x;
+    const int ntiles = (w * h) / (tw * th);
+    const int cnt = kShapeFirst[s + 1] - kShapeFirst[s];
+    k.tile = (int)(l % ntiles); l /= ntiles;
+    k.cand = (int)(l % ncand); l /= ncand;
+    k.ref = (int)(l % P.n_refs); l /= P.n_refs;
+    k.b = kShapeFirst[s] + (int)(l % cnt);
+    k.ctu = (int)(l / cnt);
+    k.item = (k.ctu * ME_BLOCKS_PER_CTU + k.b) * P.n_refs + k.ref;
+    const CtuBlock cb = kCtuBlocks[k.b];
+    k.x = (k.ctu % P.ctus_w) * ME_CTU + cb.x;
+    k.y = (k.ctu / P.ctus_w) * ME_CTU + cb.y;
+    k.w = w; k.h = h; k.tw = tw; k.th = th;
+    return k.x + w <= P.W && k.y + h <= P.H;
+}
 
-    int cx = dx * 4, cy = dy * 4;
-    u64 cbest = 0;
-    u32 bsatd = 0;
-    int mx = cx, my = cy;
-    for (int stage = 0; stage < 2; stage++) {
-        const int ncand = stage == 0 ? 9 : 8;
-        if (lane < 9) s_satd[wib][lane] = 0;
-        __syncwarp();
-        for (int task = lane; task < ncand * ntiles; task += 32) {
-            const int c = task / ntiles, t = task % ntiles;
-            int vx, vy;
-            const pel *pb;
-            if (stage == 0 && c == 0) {
-                vx = cx; vy = cy;
-                pb = P.planes[ref][0] + (long long)(y + dy) * P.i_ref + (x + dx);
-            } else {
-                const int k = stage == 0 ? c - 1 : c;
-                vx = cx + (stage == 0 ? kHalfPat[k][0] : kQuarPat[k][0]);
-                vy = cy + (stage == 0 ? kHalfPat[k][1] : kQuarPat[k][1]);
-                pb = mc_ptr(P, ref, x, y, vx, vy);
-            }
-            const int tx = (t % ntx) * tw, ty = (t / ntx) * th;
-            const u32 v = satd_tile(tw, th, ob + (long long)ty * P.i_org + tx, P.i_org,
-                                    pb + (long long)ty * P.i_ref + tx, P.i_ref, P.sq32, P.sq128);
-            atomicAdd(&s_satd[wib][c], v);
-        }
-        __syncwarp();
-        // candidate order and strict '<' as me_sub_pel_search
-        for (int c = 0; c < ncand; c++) {
-            int vx, vy;
-            if (stage == 0 && c == 0) { vx = cx; vy = cy; }
-            else {
-                const int k = stage == 0 ? c - 1 : c;
-                vx = cx + (stage == 0 ? kHalfPat[k][0] : kQuarPat[k][0]);
-                vy = cy + (stage == 0 ? kHalfPat[k][1] : kQuarPat[k][1]);
-            }
-            const u32 sd = s_satd[wib][c];
-            const u64 cost = (u64)((mvbits(vx) + mvbits(vy)) * P.lambda_mv) + ((u64)sd << 16);
-            if ((stage == 0 && c == 0) || cost < cbest) { cbest = cost; mx = vx; my = vy; bsatd = sd; }
-        }
-        __syncwarp();
-        cx = mx; cy = my;
+__device__ __forceinline__ void int_winner(const MeSubParams &P, int ctu, int b, int ref, int &dx, int &dy, u64 &key)
+{
+    key = P.keys[((size_t)ctu * P.n_refs + ref) * ME_BLOCKS_PER_CTU + b];
+    const u32 raster = (u32)(key & 0x7FFF);
+    dx = P.lo_x + (int)(raster % P.ndx);
+    dy = P.lo_y + (int)(raster / P.ndx);
+}
+
+__device__ __forceinline__ u64 sub_cost(const MeSubParams &P, int vx, int vy, u32 satd)
+{
+    return (u64)((mvbits(vx) + mvbits(vy)) * P.lambda_mv) + ((u64)satd << 16);
+}
+
+// stage-1 winner (centre first, then the half-sample pattern, strict '<')
+__device__ __forceinline__ void hpel_winner(const MeSubParams &P, int item, int cx, int cy, int &mx, int &my,
+                                            u64 &cbest, u32 &bsatd)
+{
+    const u32 *s1 = P.satd1 + (size_t)item * 9;
+    mx = cx; my = cy; bsatd = s1[0];
+    cbest = sub_cost(P, cx, cy, bsatd);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const int vx = cx + kHalfPat[c][0], vy = cy + kHalfPat[c][1];
+        const u32 sd = s1[c + 1];
+        const u64 cost = sub_cost(P, vx, vy, sd);
+        if (cost < cbest) { cbest = cost; mx = vx; my = vy; bsatd = sd; }
     }
-    if (lane == 0) {
-        MeResult r;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256, 2) k_me_sub_eval(MeSubParams P, long long n_tasks)
+{
+    const int ncand = STAGE == 1 ? 9 : 8;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n_tasks;
+         t += (long long)gridDim.x * blockDim.x) {
+        SubTask k;
+        if (!decode_task(P, t, ncand, k)) continue;
+        int dx, dy;
+        u64 key;
+        int_winner(P, k.ctu, k.b, k.ref, dx, dy, key);
+        int cx = dx * 4, cy = dy * 4;
+        const pel *pb;
+        if (STAGE == 1) {
+            if (k.cand == 0) {
+                pb = P.planes[k.ref][0] + (long long)(k.y + dy) * P.i_ref + (k.x + dx);
+            } else {
+                pb = mc_ptr(P, k.ref, k.x, k.y, cx + kHalfPat[k.cand - 1][0], cy + kHalfPat[k.cand - 1][1]);
+            }
+        } else {
+            int mx, my; u64 cb; u32 bs;
+            hpel_winner(P, k.item, cx, cy, mx, my, cb, bs);
+            pb = mc_ptr(P, k.ref, k.x, k.y, mx + kQuarPat[k.cand][0], my + kQuarPat[k.cand][1]);
+        }
+        const int ntx = k.w / k.tw;
+        const int tx = (k.tile % ntx) * k.tw, ty = (k.tile / ntx) * k.th;
+        const pel *ob = P.org + (long long)(k.y + ty) * P.i_org + k.x + tx;
+        const u32 v = me_tile_satd(k.tw, k.th, ob, P.i_org, pb + (long long)ty * P.i_ref + tx, P.i_ref, P.sq128);
+        atomicAdd((STAGE == 1 ? P.satd1 + (size_t)k.item * 9 : P.satd2 + (size_t)k.item * 8) + k.cand, v);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_me_sub_final(MeSubParams P)
+{
+    const long long total = (long long)P.n_ctu * ME_BLOCKS_PER_CTU * P.n_refs;
+    for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < total;
+         item += (long long)gridDim.x * blockDim.x) {
+        const int ref = (int)(item % P.n_refs);
+        const int b = (int)((item / P.n_refs) % ME_BLOCKS_PER_CTU);
+        const int ctu = (int)(item / P.n_refs / ME_BLOCKS_PER_CTU);
+        const CtuBlock cb = kCtuBlocks[b];
+        const int x = (ctu % P.ctus_w) * ME_CTU + cb.x, y = (ctu / P.ctus_w) * ME_CTU + cb.y;
+        MeResult r = {};
+        if (x + cb.w > P.W || y + cb.h > P.H) {
+            r.cost_int = ~0ull; r.cost_sub = ~0ull;
+            P.out[item] = r;
+            continue;
+        }
+        int dx, dy;
+        u64 key;
+        int_winner(P, ctu, b, ref, dx, dy, key);
+        const u64 cost_int = key >> 15;
+        const u32 mvc = (mvbits(4 * dx) + mvbits(4 * dy)) * P.lambda_mv;
+        int mx, my; u64 cbest; u32 bsatd;
+        hpel_winner(P, (int)item, dx * 4, dy * 4, mx, my, cbest, bsatd);
+        const u32 *s2 = P.satd2 + (size_t)item * 8;
+        const int hx = mx, hy = my;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const int vx = hx + kQuarPat[c][0], vy = hy + kQuarPat[c][1];
+            const u64 cost = sub_cost(P, vx, vy, s2[c]);
+            if (cost < cbest) { cbest = cost; mx = vx; my = vy; bsatd = s2[c]; }
+        }
         r.mv_int[0] = (s16)dx; r.mv_int[1] = (s16)dy;
         r.mv_sub[0] = (s16)mx; r.mv_sub[1] = (s16)my;
-        r.sad_int = (u32)((cost_int - mvc_int) >> 16);
+        r.sad_int = (u32)((cost_int - mvc) >> 16);
         r.satd_sub = bsatd;
         r.cost_int = cost_int;
         r.cost_sub = cbest;
-        *o = r;
+        P.out[item] = r;
     }
 }
 
@@ -460,7 +609,8 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     constexpr int NDY = 4;
     if (t.ndy_per_item != NDY) return set_status(UC_ERR_ARG, "me: table built for another NDY");
     P.win_h = 64 + t.nchunk * NDY - 1 + 1;
-    P.win_ww = ((15 + 64 + t.ndx + 4 + 15) / 16) * 4;
+    P.win_cols = ((15 + 64 + t.ndx + 4 + 15) / 16) * 16;
+    P.win_ww = (P.win_cols >> 2) + 18 + 2;    // even, room for the largest skew
     const size_t smem = (size_t)P.win_h * P.win_ww * 4;
     static bool attr_set[64];
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
@@ -499,10 +649,31 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     S.sq32 = sqrt(32.0); S.sq128 = sqrt(128.0);
     S.keys = keys; S.out = a.out;
     const long long items = (long long)S.n_ctu * ME_BLOCKS_PER_CTU * a.n_refs;
+    S.satd1 = a.sub_scratch;
+    S.satd2 = a.sub_scratch + items * 9;
+    CtuBlock tab[ME_BLOCKS_PER_CTU];
+    ctu_block_table(tab);
+    static const int first[11] = { 0, 64, 96, 128, 144, 152, 160, 164, 166, 168, 169 };
+    long long tb1[11], tb2[11];
+    tb1[0] = tb2[0] = 0;
+    for (int s = 0; s < 10; s++) {
+        int w = tab[first[s]].w, h = tab[first[s]].h, tw, th;
+        had_tile_shape(w, h, &tw, &th);
+        long long n = (long long)S.n_ctu * (first[s + 1] - first[s]) * a.n_refs * ((w * h) / (tw * th));
+        tb1[s + 1] = tb1[s] + n * 9;
+        tb2[s + 1] = tb2[s] + n * 8;
+    }
+    UC_CHECK(cudaMemsetAsync(a.sub_scratch, 0, (size_t)items * 17 * sizeof(u32), st));
     prof_begin(PROF_ME_SUB, st);
-    k_me_sub<<<(unsigned)((items + 3) / 4), 128, 0, st>>>(S);
+    for (int s = 0; s < 11; s++) S.task_base[s] = tb1[s];
+    k_me_sub_eval<1><<<(unsigned)std::min<long long>((tb1[10] + 255) / 256, 152 * 64), 256, 0, st>>>(S, tb1[10]);
     UC_CHECK(cudaGetLastError());
-    count_launch(1);
+    for (int s = 0; s < 11; s++) S.task_base[s] = tb2[s];
+    k_me_sub_eval<2><<<(unsigned)std::min<long long>((tb2[10] + 255) / 256, 152 * 64), 256, 0, st>>>(S, tb2[10]);
+    UC_CHECK(cudaGetLastError());
+    k_me_sub_final<<<(unsigned)std::min<long long>((items + 255) / 256, 152 * 16), 256, 0, st>>>(S);
+    UC_CHECK(cudaGetLastError());
+    count_launch(3);
     prof_end(PROF_ME_SUB, st);
     return UC_OK;
 }

@@ -31,7 +31,8 @@ struct MeResult {
 };
 
 // optional per-kernel timing with CUDA events on the launching stream
-enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_N = 8 };
+enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_N = 8 };
+int ensure_init();   // selects the library's device (initialising device 0 on first use)
 void prof_begin(int k, cudaStream_t st);
 void prof_end(int k, cudaStream_t st);
 void count_launch(int n);
@@ -47,7 +48,9 @@ struct MeFrameArgs {
     MeResult *out;                      // [n_ctu][169][n_refs]
     // device copies of the host-built search tables (me_build_tables)
     const u32 *q2tab; const u16 *rank2mv;
+    u32 *sub_scratch;                   // me_sub_scratch_bytes(): per-candidate SATD sums
 };
+size_t me_sub_scratch_bytes(int W, int H, int n_refs);
 
 struct MeTables {
     int lo_x, hi_x, lo_y, hi_y, ndx, ndy, nchunk, n_items, ndy_per_item;
