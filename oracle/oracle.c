@@ -302,12 +302,14 @@ u32 orc_satd_tile(int tw, int th, const pel *o, int io, const pel *p, int ip)
     return (u32)(int)(s / TBL_SQRT[0] * 2.0);
 }
 
-/* com_had tiling by block shape, src/com_cost.c:712-812 */
+/* com_had tiling by block shape, src/com_cost.c:712-812.  Square blocks whose side is not a
+ * multiple of 8 (resp. 16) take a single 4x4 (resp. 8x8) tile at the top-left. */
 u32 orc_had(int w, int h, const pel *o, int io, const pel *p, int ip, int bd)
 {
     int shift = bd - 8, tw, th;
     if (w == h) {
-        if (w == 4) return orc_satd_tile(4, 4, o, io, p, ip) >> shift;
+        if (w & 7) return orc_satd_tile(4, 4, o, io, p, ip) >> shift;
+        if (w & 15) return orc_satd_tile(8, 8, o, io, p, ip) >> shift;
         tw = 8; th = 8;
     } else if (w > h) {
         if (h == 4 || (h & 7)) { tw = 8; th = 4; }
@@ -316,8 +318,6 @@ u32 orc_had(int w, int h, const pel *o, int io, const pel *p, int ip, int bd)
         if (w == 4 || (w & 7)) { tw = 4; th = 8; }
         else { tw = 8; th = 16; }
     }
-    /* 12-wide blocks (w & 7, w != 4) use three 4x8 columns per 8 rows: covered by the
-     * generic tiling below since 12 = 3 * 4 */
     int sum = 0;
     for (int y = 0; y < h; y += th)
         for (int x = 0; x < w; x += tw)

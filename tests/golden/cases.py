@@ -1,0 +1,354 @@
+"""Seeded parity cases shared by the golden-vector generator and the tests.
+
+Each case is (kernel, params, seed).  Inputs are regenerated from the seed with numpy's PCG64
+(identical on every platform), run through a backend object with the pyoracle method set
+(pyoracle.RefLib = the reference's own C, pyoracle.Oracle = the restatement, or the GPU
+table-entry adapter), and the outputs are reduced to an md5 digest.  golden.json stores the
+digests the reference produced (make_golden.py).
+"""
+import hashlib
+
+import numpy as np
+
+NEIB = 576
+MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],
+                    [-1, 3, -7, 19, 57, -10, 4, -1]], dtype=np.int8)
+MC_CHROMA = np.array([[0, 64, 0, 0], [-4, 62, 6, 0], [-6, 56, 15, -1], [-5, 47, 25, -3], [-4, 36, 36, -4],
+                      [-3, 25, 47, -5], [-1, 15, 56, -6], [0, 6, 62, -4]], dtype=np.int8)
+SIZES = [4, 8, 16, 32, 64]
+
+
+def digest(*arrays):
+    h = hashlib.md5()
+    for a in arrays:
+        if isinstance(a, (int, np.integer)):
+            a = np.array([a], dtype=np.int64)
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def pic(rng, h, w, kind):
+    """test content: uniform noise, binary extremes, or smooth"""
+    if kind == 0:
+        return rng.integers(0, 256, (h, w), dtype=np.uint8)
+    if kind == 1:
+        return (rng.integers(0, 2, (h, w)) * 255).astype(np.uint8)
+    y, x = np.mgrid[0:h, 0:w]
+    return np.clip(128 + 60 * np.sin(x / 5.0 + rng.uniform(0, 6)) + 30 * np.cos(y / 7.0) +
+                   rng.integers(-3, 4, (h, w)), 0, 255).astype(np.uint8)
+
+
+# ------------------------------------------------------------------------------ runners
+def run_sad(B, p, seed):
+    rng = np.random.default_rng(seed)
+    w, h, kind = p["w"], p["h"], p["kind"]
+    o = pic(rng, h, w + 9, kind)
+    r = pic(rng, h, w + 13, kind)
+    return digest(B.sad(w, h, o.ctypes.data, w + 9, r.ctypes.data, w + 13),
+                  B.ssd(w, h, o.ctypes.data, w + 9, r.ctypes.data, w + 13))
+
+
+def run_satd_tile(B, p, seed):
+    rng = np.random.default_rng(seed)
+    tw, th = p["tw"], p["th"]
+    out = []
+    for k in range(8):
+        o = pic(rng, 16, 24, k % 3)
+        r = pic(rng, 16, 24, (k + 1) % 3)
+        out.append(B.satd_tile(tw, th, o.ctypes.data, 24, r.ctypes.data, 24))
+    return digest(np.array(out, np.int64))
+
+
+def run_had(B, p, seed):
+    rng = np.random.default_rng(seed)
+    w, h = p["w"], p["h"]
+    o = pic(rng, 64, 72, p["kind"])
+    r = pic(rng, 64, 72, (p["kind"] + 1) % 3)
+    return digest(B.had(w, h, o.ctypes.data, 72, r.ctypes.data, 72), B.satd_intra(w, h, o.ctypes.data, r.ctypes.data, 72, 72))
+
+
+def run_ipflt(B, p, seed):
+    rng = np.random.default_rng(seed)
+    t, w, h = p["t"], p["w"], p["h"]
+    src = pic(rng, h + 16, w + 24, p["kind"])
+    s0 = src.ctypes.data + 8 * (w + 24) + 8
+    taps = MC_LUMA if t in (0, 2) else MC_CHROMA
+    c = taps[p["phase"]].copy()
+    d = np.zeros((h, w + 5), np.uint8)
+    B.ipflt(t, s0, w + 24, d.ctypes.data, w + 5, w, h, c)
+    return digest(d)
+
+
+def run_ipflt_ext(B, p, seed):
+    rng = np.random.default_rng(seed)
+    t, w, h = p["t"], p["w"], p["h"]
+    src = pic(rng, h + 16, w + 24, p["kind"])
+    s0 = src.ctypes.data + 8 * (w + 24) + 8
+    taps = MC_LUMA if t == 0 else MC_CHROMA
+    cx, cy = taps[p["px"]].copy(), taps[p["py"]].copy()
+    d = np.zeros((h, w), np.uint8)
+    B.ipflt_ext(t, s0, w + 24, d.ctypes.data, w, w, h, cx, cy)
+    return digest(d)
+
+
+def run_ipcpy(B, p, seed):
+    rng = np.random.default_rng(seed)
+    w, h = p["w"], p["h"]
+    src = pic(rng, h, w + 7, 0)
+    d = np.zeros((h, w + 3), np.uint8)
+    B.ipcpy(src.ctypes.data, w + 7, d.ctypes.data, w + 3, w, h)
+    return digest(d)
+
+
+def padded_plane(img, pad, stride):
+    h, w = img.shape
+    buf = np.zeros((h + 2 * pad, stride), np.uint8)
+    buf[pad:pad + h, pad:pad + w] = img
+    buf[pad:pad + h, :pad] = img[:, :1]
+    buf[pad:pad + h, pad + w:pad + w + pad] = img[:, -1:]
+    buf[:pad] = buf[pad]
+    buf[pad + h:] = buf[pad + h - 1]
+    return buf
+
+
+def run_if_luma_frame(B, p, seed):
+    rng = np.random.default_rng(seed)
+    w, h, pad = p["w"], p["h"], p["pad"]
+    stride = w + 2 * pad
+    p0 = padded_plane(pic(rng, h, w, p["kind"]), pad, stride).reshape(-1)
+    planes = [np.zeros_like(p0) for _ in range(15)]
+    base = pad * stride + pad
+    B.if_luma_frame(p0.ctypes.data + base, [q.ctypes.data + base for q in planes], w, h, pad, stride)
+    return digest(*planes)
+
+
+def run_pel(B, p, seed):
+    rng = np.random.default_rng(seed)
+    w, h = p["w"], p["h"]
+    o = pic(rng, h, w + 5, 0)
+    r = pic(rng, h, w + 3, 0)
+    res = np.zeros((h, w + 2), np.int16)
+    B.pel_diff(w, h, o.ctypes.data, w + 5, r.ctypes.data, w + 3, res.ctypes.data, w + 2)
+    s1 = pic(rng, h, w, 0)
+    s2 = pic(rng, h, w, 1)
+    av = np.zeros((h, w + 4), np.uint8)
+    B.pel_avrg(w, h, av.ctypes.data, w + 4, s1.ctypes.data, s2.ctypes.data)
+    resi = rng.integers(-300, 300, (h, w)).astype(np.int16)
+    rec = np.zeros((2, h, w + 6), np.uint8)
+    for cbf in (0, 1):
+        B.recon(resi.ctypes.data, r.ctypes.data, w + 3, w, h, rec[cbf].ctypes.data, w + 6, cbf)
+    return digest(res, av, rec)
+
+
+def nb_array(rng, kind):
+    if kind == 0:
+        return rng.integers(0, 256, NEIB, dtype=np.uint8)
+    if kind == 1:
+        return (rng.integers(0, 2, NEIB) * 255).astype(np.uint8)
+    return np.clip(128 + 50 * np.sin(np.arange(NEIB) / 9.0) + rng.integers(-4, 5, NEIB), 0, 255).astype(np.uint8)
+
+
+def run_intra(B, p, seed):
+    rng = np.random.default_rng(seed)
+    w, h = p["w"], p["h"]
+    outs = []
+    for ipm in range(33):
+        for avail in (0, 1, 2, 3, 7):
+            for ipf in (0, 1):
+                nb = nb_array(rng, (ipm + avail) % 3)
+                d = np.zeros(w * h, np.uint8)
+                B.intra_pred(nb, d, ipm, w, h, avail, ipf)
+                outs.append(d)
+    return digest(*outs)
+
+
+def run_ang_entry(B, p, seed):
+    rng = np.random.default_rng(seed)
+    w, h = p["w"], p["h"]
+    outs = []
+    for mode in [m for m in range(3, 33) if m != 24]:
+        nb = nb_array(rng, mode % 3)
+        d = np.zeros((h, w + 6), np.uint8)
+        B.ipred_ang(nb, d, w + 6, mode, w, h)
+        outs.append(d)
+    return digest(*outs)
+
+
+def run_nbr(B, p, seed):
+    rng = np.random.default_rng(seed)
+    W, H = 128, 96
+    img = pic(rng, H, W, p["kind"])
+    i_scu = W // 4 + 2
+    n_scu = i_scu * (H // 4 + 2)
+    outs = []
+    for t in range(40):
+        w, h = int(rng.choice(SIZES)), int(rng.choice(SIZES))
+        x = int(rng.integers(0, (W - w) // 4 + 1)) * 4
+        y = int(rng.integers(0, (H - h) // 4 + 1)) * 4
+        coded = (rng.random(n_scu) < 0.75).astype(np.uint8).reshape(H // 4 + 2, i_scu)
+        coded[0, :] = coded[-1, :] = 0
+        coded[:, 0] = coded[:, -1] = 0
+        coded = coded.ravel().copy()
+        avail = int(rng.integers(0, 8))
+        if y == 0:
+            avail &= ~(1 | 4)
+        if x == 0:
+            avail &= ~(2 | 4)
+        scup = (y // 4 + 1) * i_scu + x // 4 + 1
+        nb = np.zeros(NEIB, np.uint8)
+        src = img.ctypes.data + y * W + x
+        B.intra_get_nbr(x, y, w, h, src, W, src - W, p["lcu"], avail, nb, scup, coded, n_scu, i_scu)
+        outs.append(nb)
+    return digest(*outs)
+
+
+def run_fdct2(B, p, seed):
+    rng = np.random.default_rng(seed)
+    lw, lh = p["lw"], p["lh"]
+    n = (1 << lw) * (1 << lh)
+    resi = rng.integers(-255, 256, n).astype(np.int16) if p["kind"] == 0 else \
+        rng.integers(-32768, 32768, n).astype(np.int16)
+    c = np.full(4096, 7, np.int16)
+    B.trans_dct2(lw, lh, resi, c)
+    coef = rng.integers(-2000, 2000, 4096).astype(np.int16) if p["kind"] == 0 else \
+        rng.integers(-32768, 32768, 4096).astype(np.int16)
+    r = np.zeros(4096, np.int16)
+    B.itrans_dct2(lh, lw, coef, r)
+    return digest(c, r)
+
+
+def run_dct87(B, p, seed):
+    rng = np.random.default_rng(seed)
+    t, ln = p["t"], p["ln"]
+    src = rng.integers(-255, 256, (1 << ln) * 8).astype(np.int16)
+    outs = []
+    for sh in (0, 1, 5, 8):
+        d = np.zeros(4096, np.int16)
+        B.trans_dct8_dst7(t, ln, src, d, sh, 8)
+        outs.append(d)
+    coef = rng.integers(-3000, 3000, (1 << ln) * 8).astype(np.int16)
+    d = np.zeros(4096, np.int16)
+    B.itrans_dct8_dst7(t, ln, coef, d, 5, 8, 32767, -32768)
+    outs.append(d)
+    d = np.zeros(4096, np.int16)
+    B.itrans_dct8_dst7(t, ln, coef, d, 12, 8, 255, -256)
+    outs.append(d)
+    return digest(*outs)
+
+
+def run_xform(B, p, seed):
+    rng = np.random.default_rng(seed)
+    lw, lh = p["lw"], p["lh"]
+    n = (1 << lw) * (1 << lh)
+    outs = []
+    for nxn in (0, 1):
+        for blk in range(4):
+            for sec in range(4):
+                for alt in (0, 1):
+                    resi = rng.integers(-255, 256, n).astype(np.int16)
+                    c = np.zeros(4096, np.int16)
+                    B.transform(nxn, blk, c, resi, lw, lh, 8, sec, alt)
+                    coef = (rng.integers(-60, 60, n) * (rng.random(n) < 0.3)).astype(np.int16)
+                    qp = int(rng.integers(0, 64))
+                    r = np.zeros(4096, np.int16)
+                    B.invqt(nxn, blk, coef, r, None, None, lw, lh, qp, 8, sec, alt)
+                    wq4 = rng.integers(16, 128, 16).astype(np.uint8)
+                    wq8 = rng.integers(16, 128, 64).astype(np.uint8)
+                    r2 = np.zeros(4096, np.int16)
+                    B.invqt(nxn, blk, coef, r2, wq4, wq8, lw, lh, qp, 8, sec, alt)
+                    outs += [c, r, r2]
+    return digest(*outs)
+
+
+def run_quant(B, p, seed):
+    rng = np.random.default_rng(seed)
+    outs = []
+    for t in range(40):
+        n = int(rng.choice([16, 64, 256, 1024, 4096]))
+        coef = (rng.integers(-3000, 3000, n) * (rng.random(n) < 0.5)).astype(np.int16)
+        thr = int(rng.integers(0, 100))
+        outs.append(np.array([B.quant_check(coef, n, thr)], np.int64))
+        qv = int(rng.integers(18, 16302))
+        qb = int(rng.integers(14, 22))
+        es = int(rng.integers(1, 100000))
+        a = np.zeros(n, np.uint32)
+        lv = np.zeros(n, np.int16)
+        e = np.zeros(n, np.int64)
+        last = B.quant_rdoq(coef, n, qv, qb, es, 20, a, lv, e)
+        outs += [np.array([last], np.int64), a, lv, e]
+    return digest(*outs)
+
+
+def run_tables(B, p, seed):
+    outs = [B.dct_table(ln) for ln in range(1, 7)]
+    outs += [B.scan(lw, lh) for lw in range(1, 7) for lh in range(1, 7)]
+    return digest(*outs)
+
+
+RUNNERS = {
+    "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
+    "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
+    "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
+    "quant": run_quant, "tables": run_tables,
+}
+
+
+def all_cases():
+    cases = []
+    s = 1000
+
+    def add(kernel, **p):
+        nonlocal s
+        s += 1
+        cases.append({"kernel": kernel, "params": p, "seed": s})
+
+    for w in (4, 8, 16, 32, 64, 128):
+        for h in (4, 8, 16, 32, 64):
+            add("sad", w=w, h=h, kind=(w + h) % 3)
+    for tw, th in ((4, 4), (8, 8), (16, 8), (8, 16), (8, 4), (4, 8)):
+        add("satd_tile", tw=tw, th=th)
+    for w in SIZES + [12, 24, 48]:
+        for h in SIZES + [12, 24, 48]:
+            if (w & (w - 1)) and (h & (h - 1)) and w != h:
+                pass
+            add("had", w=w, h=h, kind=(w * h) % 3)
+    for t in range(4):
+        for w in (4, 8, 16, 32, 64, 128):
+            add("ipflt", t=t, w=w, h=[4, 8, 16, 32, 64][(w + t) % 5], phase=1 + (w + t) % 3, kind=t % 3)
+    for t in range(2):
+        for w in SIZES:
+            add("ipflt_ext", t=t, w=w, h=[4, 8, 16, 32, 64][(w // 4 + t) % 5], px=1 + w % 3, py=1 + (w // 4) % 3,
+                kind=w % 3)
+    for w in (4, 8, 16, 32, 64, 128):
+        add("ipcpy", w=w, h=8 + w % 5)
+    add("if_luma_frame", w=32, h=16, pad=16, kind=0)
+    add("if_luma_frame", w=40, h=24, pad=20, kind=2)
+    for w in SIZES:
+        add("pel", w=w, h=[4, 8, 16][w % 3])
+    for w in SIZES:
+        for h in SIZES:
+            if (w, h) == (64, 4):
+                continue   # the reference's mode-23 kernel writes past a 64x4 block (not a size it predicts)
+            add("intra", w=w, h=h)
+            add("ang_entry", w=w, h=h)
+    for k in range(3):
+        add("nbr", kind=k, lcu=64 if k < 2 else 1 << 20)
+    for lw in range(2, 7):
+        for lh in range(2, 7):
+            if (lw, lh) in ((6, 2), (2, 6)):
+                continue
+            add("fdct2", lw=lw, lh=lh, kind=0)
+            add("fdct2", lw=lw, lh=lh, kind=1)
+    for t in (0, 1):
+        for ln in range(2, 7):
+            add("dct87", t=t, ln=ln)
+    for lw in range(2, 6):
+        for lh in range(2, 6):
+            add("xform", lw=lw, lh=lh)
+    add("quant")
+    add("tables")
+    return cases
+
+
+def run_case(B, case):
+    return RUNNERS[case["kernel"]](B, case["params"], case["seed"])
