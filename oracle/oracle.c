@@ -959,7 +959,7 @@ void orc_dquant(int flat, const s16 *coef, s16 *out, const u8 *wq4, const u8 *wq
     for (int i = 0; i < h; i++) {
         for (int j = 0; j < w; j++) {
             int weight = ((i | j) & 0xE0) ? 0 : wq[j >> ish];
-            int lev = (int)(((((s64)((coef[i * w + j] * weight) >> 2)) * scale) >> 4) + off) >> shift;
+            int lev = (int)((((((s64)((coef[i * w + j] * weight) >> 2)) * scale) >> 4) + off) >> shift);
             lev = CLIP3(-32768, 32767, lev);
             if (refix) lev = (lev * 181 + 128) >> 8;
             out[i * w + j] = (s16)lev;

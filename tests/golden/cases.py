@@ -279,6 +279,26 @@ def run_quant(B, p, seed):
     return digest(*outs)
 
 
+def run_dquant(B, p, seed):
+    rng = np.random.default_rng(seed)
+    lw, lh = p["lw"], p["lh"]
+    w, h = 1 << lw, 1 << lh
+    outs = []
+    for k in range(6):
+        coef = (rng.integers(-400, 400, w * h) * (rng.random(w * h) < 0.4)).astype(np.int16)
+        if k == 5:
+            coef[:4] = [32767, -32768, 20000, -20000]
+        scale = int(rng.choice([32768, 36061, 46341, 60424, 65535]))
+        shift = int(rng.integers(0, 14))
+        wq4 = rng.integers(16, 128, 16).astype(np.uint8)
+        wq8 = rng.integers(16, 128, 64).astype(np.uint8)
+        for flat in (1, 0):
+            out = np.full(w * h, 99, np.int16)
+            B.dquant(flat, coef, out, wq4, wq8, lw, lh, scale, shift)
+            outs.append(out)
+    return digest(*outs)
+
+
 def run_tables(B, p, seed):
     outs = [B.dct_table(ln) for ln in range(1, 7)]
     outs += [B.scan(lw, lh) for lw in range(1, 7) for lh in range(1, 7)]
@@ -289,7 +309,7 @@ RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "tables": run_tables,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables,
 }
 
 
@@ -346,6 +366,9 @@ def all_cases():
         for lh in range(2, 6):
             add("xform", lw=lw, lh=lh)
     add("quant")
+    for lw in range(2, 7):
+        for lh in range(2, 7):
+            add("dquant", lw=lw, lh=lh)
     add("tables")
     return cases
 

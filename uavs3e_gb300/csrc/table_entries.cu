@@ -390,7 +390,7 @@ __global__ void k_e_dquant(int flat, const s16 *coef, s16 *out, const u8 *wq4, c
                 int ish = max(lw, lh) - 3;
                 weight = ((r | c) & 0xE0) ? 0 : wq8[(r >> ish) * 8 + (c >> ish)];
             }
-            lev = (int)(((((s64)((coef[i] * weight) >> 2)) * scale) >> 4) + off) >> shift;
+            lev = (int)((((((s64)((coef[i] * weight) >> 2)) * scale) >> 4) + off) >> shift);   // 64-bit, then truncated
             lev = min(32767, max(-32768, lev));
             if (refix) lev = (lev * 181 + 128) >> 8;
             out[i] = (s16)lev;
