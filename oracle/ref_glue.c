@@ -14,6 +14,25 @@
  */
 #include "define.h"
 #include "util.h"
+#include <stddef.h>
+#include "../include/uavs3e_cuda_table.h"
+
+/* ---- 0. the GPU library's table twin must have funs_handle_t's layout, member by member ---- */
+#define SAME_OFFSET(m) _Static_assert(offsetof(funs_handle_t, m) == offsetof(uavs3e_cuda_funs_t, m), #m)
+SAME_OFFSET(intra_pred_dc); SAME_OFFSET(intra_pred_plane); SAME_OFFSET(intra_pred_bi);
+SAME_OFFSET(intra_pred_plane_ipf); SAME_OFFSET(intra_pred_bi_ipf); SAME_OFFSET(intra_pred_ver);
+SAME_OFFSET(intra_pred_hor); SAME_OFFSET(intra_pred_ang); SAME_OFFSET(intra_pred_ipf_core);
+SAME_OFFSET(intra_pred_ipf_core_s16); SAME_OFFSET(deblock_luma); SAME_OFFSET(deblock_chroma); SAME_OFFSET(sao);
+SAME_OFFSET(sao_stat); SAME_OFFSET(alf); SAME_OFFSET(alf_fix); SAME_OFFSET(alf_calc); SAME_OFFSET(ipcpy);
+SAME_OFFSET(ipflt); SAME_OFFSET(ipflt_ext); SAME_OFFSET(ip_flt_y_hor); SAME_OFFSET(ip_flt_y_ver);
+SAME_OFFSET(ip_flt_y_ver_ext); SAME_OFFSET(recon); SAME_OFFSET(dquant); SAME_OFFSET(itrans_dct2);
+SAME_OFFSET(itrans_dct8_dst7); SAME_OFFSET(trans_dct2); SAME_OFFSET(trans_dct8_dst7); SAME_OFFSET(cost_sad);
+SAME_OFFSET(cost_sad_x3); SAME_OFFSET(cost_sad_x4); SAME_OFFSET(cost_ssd); SAME_OFFSET(cost_satd);
+SAME_OFFSET(cost_var); SAME_OFFSET(ssim_4x4x2_core); SAME_OFFSET(ssim_end4); SAME_OFFSET(pel_diff);
+SAME_OFFSET(pel_avrg); SAME_OFFSET(affine_sobel_flt_hor); SAME_OFFSET(affine_sobel_flt_ver);
+SAME_OFFSET(affine_coef_computer); SAME_OFFSET(quant_rdoq); SAME_OFFSET(quant_check); SAME_OFFSET(sobel_cost);
+_Static_assert(sizeof(funs_handle_t) == sizeof(uavs3e_cuda_funs_t), "table size");
+size_t refk_table_size(void) { return sizeof(funs_handle_t); }
 
 /* ---- 1. SIMD initialisers left empty (their real bodies live in src/sse, src/avx2) ---- */
 void uavs3e_funs_init_sse(void) {}

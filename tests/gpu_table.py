@@ -64,7 +64,7 @@ class GpuTable:
             self.L.uavs3e_cuda_ip_flt_y_ver_ext(P(tmp[dx - 1].ctypes.data + 2 * (4 * ts + 4)), ts, d, stride, W + 8,
                                                 H + 8, _p(coef), 8)
         # the edge padding of each fractional plane (com_img_padding(img, 1, 4)) on the host view
-        rows, ext = H + 2 * pad, pad - 4
+        rows = H + 2 * pad
         for q in plane_ptrs:
             buf = np.ctypeslib.as_array((C.c_uint8 * (rows * stride)).from_address(q - pad * stride - pad))
             img = buf.reshape(rows, stride)
@@ -73,7 +73,6 @@ class GpuTable:
             img[r0:r1, c1:] = img[r0:r1, c1 - 1:c1]
             img[:r0] = img[r0]
             img[r1:] = img[r1 - 1]
-            del ext
 
     def pel_diff(self, w, h, o, io, p, ip, r, ir):
         getattr(self.L, f"uavs3e_cuda_pel_diff_{w}")(P(o), io, P(p), ip, P(r), ir, h)
