@@ -139,6 +139,33 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_run(uavs3e_cuda_me *me, const uint8_t *org, i
 UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *me, const uint8_t *d_org, int i_org,
                                               uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);
 
+/*
+ * The same search without any allocation -- no cudaMalloc/cudaFree, no allocating library call,
+ * no host heap.  It has no counterpart in the reference; it exists for callers that cannot
+ * allocate when they search a frame (an encoder thread working inside a fixed memory budget set
+ * up at start-up, or code that must not call cudaMalloc/cudaFree because they synchronise the
+ * device).  The caller passes every buffer: d_org (W x H, row stride i_org), d_planes
+ * (n_refs * 16 device pointers to sample (0,0) of each reference's planes, index
+ * ref*16 + dy*4 + dx, 0 = integer plane; padded by `pad` >= 144 with stride i_ref, e.g. filled
+ * by uavs3e_cuda_pad_plane + uavs3e_cuda_subpel_planes) and d_out (uavs3e_cuda_me_block_table
+ * order, (W+63)/64 * (H+63)/64 * 169 * n_refs records).  The scratch lives in one static device
+ * array of UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits; frames beyond UAVS3E_CUDA_NOALLOC_MAX_CTUS CTUs (1920x1088), more than
+ * UAVS3E_CUDA_NOALLOC_MAX_REFS references or a range above UAVS3E_CUDA_NOALLOC_MAX_RANGE are
+ * rejected with UAVS3E_CUDA_ERR_ARG.  The first call on a device looks up the array's device
+ * address (and every call with a new size or lambda uploads search tables and waits for that
+ * upload), so make the first call on each device before any stream capture.  All calls share
+ * the one array and the call leaves its contents behind: calls whose GPU work overlaps (other
+ * streams, other host threads) race and must be serialised by the caller.
+ */
+#define UAVS3E_CUDA_NOALLOC_MAX_CTUS      510
+#define UAVS3E_CUDA_NOALLOC_MAX_REFS      2
+#define UAVS3E_CUDA_NOALLOC_MAX_RANGE     64
+#define UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES 13234944u
+UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_org, int i_org, const uint8_t *const *d_planes,
+                                                  int i_ref, int pad, int width, int height, int n_refs, int range,
+                                                  uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);
+
 /* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
  * session's plane stride; for inspection by tests. */
 UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *me, int slot, int phase);

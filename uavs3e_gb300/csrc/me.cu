@@ -51,6 +51,8 @@ __host__ __device__ __forceinline__ u32 mvbits(int v)
 #endif
 }
 
+u32 me_mvbits(int v) { return mvbits(v); }
+
 size_t me_q2_entries(int range, int ndy_per_item)
 {
     int nd = 2 * range + 1;

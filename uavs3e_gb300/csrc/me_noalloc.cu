@@ -1,0 +1,161 @@
+// Batched motion search that allocates nothing (uavs3e_cuda_me_search_noalloc).
+//
+// Some callers cannot allocate device memory when they search a frame: an encoder thread that
+// runs inside a fixed memory budget set up at start-up, code that must not call cudaMalloc /
+// cudaFree because those synchronise the device and would stall other streams, or a host that
+// hands this library only the buffers it owns.  This variant takes every input and output from
+// the caller (original picture, the 16 planes of each reference -- e.g. from
+// uavs3e_cuda_pad_plane + uavs3e_cuda_subpel_planes -- and the result array) and keeps its
+// scratch -- the per-block integer winners, the per-candidate SATD sums of the refinement and
+// the per-lambda search tables -- in one file-scope device array of fixed size, which every GPU
+// that loads the library holds until the process exits.  The host-side search tables are built
+// in static host arrays, so no heap allocation happens either.
+#include "common.cuh"
+#include "uavs3e_cuda_internal.h"
+#include "../../include/uavs3e_cuda.h"
+
+#include <algorithm>
+#include <string.h>
+
+namespace uc {
+
+// limits of the static scratch: a 1920x1088 frame (510 CTUs of 64x64), 2 references,
+// search range 64 (4 vertically adjacent candidates per search item)
+constexpr int NA_MAX_CTUS = UAVS3E_CUDA_NOALLOC_MAX_CTUS;
+constexpr int NA_MAX_REFS = UAVS3E_CUDA_NOALLOC_MAX_REFS;
+constexpr int NA_MAX_RANGE = UAVS3E_CUDA_NOALLOC_MAX_RANGE;
+constexpr int NA_NDY = 4;
+constexpr size_t NA_KEYS = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * sizeof(u64);
+constexpr size_t NA_SUB = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * 17 * sizeof(u32);
+constexpr size_t NA_Q2_ENTRIES = (size_t)(2 * NA_MAX_RANGE + 1) * (((2 * NA_MAX_RANGE + 1) + NA_NDY - 1) / NA_NDY) * NA_NDY;
+constexpr size_t NA_Q2 = NA_Q2_ENTRIES * sizeof(u32);
+constexpr size_t NA_R2M = (size_t)ME_GROUPS * ME_MAX_GROUP * sizeof(u16);
+constexpr size_t na_up(size_t v) { return (v + 255) & ~(size_t)255; }
+constexpr size_t NA_OFF_SUB = na_up(NA_KEYS);
+constexpr size_t NA_OFF_Q2 = na_up(NA_OFF_SUB + NA_SUB);
+constexpr size_t NA_OFF_R2M = na_up(NA_OFF_Q2 + NA_Q2);
+constexpr size_t NA_BYTES = NA_OFF_R2M + NA_R2M;
+static_assert(NA_BYTES == UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES, "scratch size in the header");
+static_assert(NA_OFF_SUB % 256 == 0 && NA_OFF_Q2 % 16 == 0 && NA_OFF_R2M % 16 == 0, "scratch alignment");
+
+// the scratch every call of this entry point uses
+static __device__ __align__(256) unsigned char g_me_scratch[NA_BYTES];
+
+// per device: the scratch's device address (set-up on the first call with that device current)
+// and the parameters of the search tables it currently holds
+struct NaDevice {
+    unsigned char *scratch = nullptr;
+    bool tables = false;
+    int W = 0, H = 0, range = 0;
+    u32 lambda = 0;
+    MeTables tab;
+};
+static NaDevice g_na[64];
+
+// static host buffers for the table build (no heap use)
+static u32 g_h_q2[NA_Q2_ENTRIES];
+static u16 g_h_r2m[ME_GROUPS * ME_MAX_GROUP];
+struct NaCand { u32 r, raster, pos; };
+static NaCand g_cand[ME_MAX_GROUP];
+
+// the search tables of me_build_tables (csrc/me.cu), built into the static buffers
+static int na_build_tables(int W, int H, int range, u32 lambda, MeTables *t)
+{
+    const int M = std::max(W, H);
+    t->lo_x = t->lo_y = std::max(-range, -M + 4);
+    t->hi_x = t->hi_y = std::min(range, M - 4);
+    t->ndx = t->hi_x - t->lo_x + 1;
+    t->ndy = t->hi_y - t->lo_y + 1;
+    t->ndy_per_item = NA_NDY;
+    t->nchunk = (t->ndy + NA_NDY - 1) / NA_NDY;
+    t->n_items = t->ndx * t->nchunk;
+    t->lambda_mv = lambda;
+    if (t->ndx <= 0 || (size_t)t->n_items * NA_NDY > NA_Q2_ENTRIES) return UC_ERR_ARG;
+    for (int g = 0; g < ME_GROUPS; g++) {
+        int n = 0;
+        for (int it = g; it < t->n_items; it += ME_GROUPS) {
+            const int dx = t->lo_x + it % t->ndx, dy0 = t->lo_y + (it / t->ndx) * NA_NDY;
+            for (int j = 0; j < NA_NDY; j++) {
+                const int dy = dy0 + j;
+                const u32 pos = (u32)(it * NA_NDY + j);
+                if (dy > t->hi_y) { g_h_q2[pos] = 0xFFFFFFFFu; continue; }
+                if (n >= ME_MAX_GROUP) return UC_ERR_ARG;
+                const u32 mvc = (me_mvbits(4 * dx) + me_mvbits(4 * dy)) * lambda;
+                g_cand[n++] = NaCand{ mvc & 0xFFFFu, (u32)((dy - t->lo_y) * t->ndx + (dx - t->lo_x)), pos };
+            }
+        }
+        std::sort(g_cand, g_cand + n, [](const NaCand &a, const NaCand &b) {
+            return a.r != b.r ? a.r < b.r : a.raster < b.raster;
+        });
+        for (int k = 0; k < n; k++) {
+            const u32 pos = g_cand[k].pos;
+            const int it = (int)(pos / NA_NDY), j = (int)(pos % NA_NDY);
+            const int dx = t->lo_x + it % t->ndx, dy = t->lo_y + (it / t->ndx) * NA_NDY + j;
+            const u32 mvc = (me_mvbits(4 * dx) + me_mvbits(4 * dy)) * lambda;
+            g_h_q2[pos] = ((mvc >> 16) << ME_RANK_BITS) | (u32)k;
+            g_h_r2m[g * ME_MAX_GROUP + k] = (u16)g_cand[k].raster;
+        }
+    }
+    return UC_OK;
+}
+
+}  // namespace uc
+
+using namespace uc;
+
+extern "C" UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_org, int i_org,
+                                                             const uint8_t *const *d_planes, int i_ref, int pad,
+                                                             int width, int height, int n_refs, int range,
+                                                             uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out,
+                                                             void *stream)
+{
+    // size limits of the static scratch first: a larger request is an argument error
+    const long long n_ctu = (long long)((width + 63) / 64) * ((height + 63) / 64);
+    if (width < 64 || height < 64 || n_ctu > NA_MAX_CTUS || n_refs < 1 || n_refs > NA_MAX_REFS || range < 1 ||
+        range > NA_MAX_RANGE)
+        return set_status(UC_ERR_ARG, "me_search_noalloc: frame, reference count or range exceeds the static scratch "
+                                      "(at most 510 CTUs of 64x64, 2 references, range 64)");
+    if (!d_org || !d_planes || !d_out || i_org < width || pad < 144 || i_ref < width + 2 * pad)
+        return set_status(UC_ERR_ARG, "me_search_noalloc: bad pointer or geometry");
+    if ((uint64_t)lambda_mv * 36u >= (1ull << 32)) return set_status(UC_ERR_ARG, "me_search_noalloc: lambda_mv too large");
+    for (int i = 0; i < n_refs * 16; i++)
+        if (!d_planes[i]) return set_status(UC_ERR_ARG, "me_search_noalloc: null plane");
+    int r = ensure_init();
+    if (r) return r;
+    int dev = 0;
+    UC_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "me_search_noalloc: device index");
+    NaDevice &D = g_na[dev];
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!D.scratch) {
+        // once per device, with that device current: the array's device address (host code may
+        // not use the symbol itself)
+        void *p = nullptr;
+        UC_CHECK(cudaGetSymbolAddress(&p, g_me_scratch));
+        D.scratch = (unsigned char *)p;
+    }
+    if (!D.tables || D.W != width || D.H != height || D.range != range || D.lambda != lambda_mv) {
+        if (na_build_tables(width, height, range, lambda_mv, &D.tab))
+            return set_status(UC_ERR_ARG, "me_search_noalloc: cannot build search tables");
+        D.tables = false;
+        UC_CHECK(cudaMemcpyAsync(D.scratch + NA_OFF_Q2, g_h_q2, (size_t)D.tab.n_items * NA_NDY * sizeof(u32),
+                                 cudaMemcpyHostToDevice, st));
+        UC_CHECK(cudaMemcpyAsync(D.scratch + NA_OFF_R2M, g_h_r2m, NA_R2M, cudaMemcpyHostToDevice, st));
+        // the host buffers are reused by the next build: wait until the copies have read them
+        UC_CHECK(cudaStreamSynchronize(st));
+        D.tables = true;
+        D.W = width; D.H = height; D.range = range; D.lambda = lambda_mv;
+    }
+    MeFrameArgs a;
+    memset(&a, 0, sizeof(a));
+    a.org = d_org; a.i_org = i_org;
+    for (int s = 0; s < n_refs; s++)
+        for (int q = 0; q < 16; q++) a.planes[s][q] = d_planes[s * 16 + q];
+    a.i_ref = i_ref; a.pad = pad;
+    a.W = width; a.H = height; a.n_refs = n_refs; a.range = range; a.lambda_mv = lambda_mv;
+    a.out = (MeResult *)d_out;
+    a.q2tab = (const u32 *)(D.scratch + NA_OFF_Q2);
+    a.rank2mv = (const u16 *)(D.scratch + NA_OFF_R2M);
+    a.sub_scratch = (u32 *)(D.scratch + NA_OFF_SUB);      // zeroed by launch_me_frame before use
+    return launch_me_frame(a, D.tab, (u64 *)D.scratch, st);
+}

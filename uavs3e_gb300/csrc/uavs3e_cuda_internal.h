@@ -61,6 +61,7 @@ int me_build_tables(int W, int H, int range, u32 lambda_mv, int ndy_per_item, Me
                     u32 *q2tab, u16 *rank2mv, size_t q2cap);
 size_t me_q2_entries(int range, int ndy_per_item);
 size_t me_key_scratch_bytes(int W, int H, int n_refs);
+u32 me_mvbits(int v);   // MV bits of one quarter-sample component (host)
 int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStream_t st);
 
 }  // namespace uc
