@@ -225,7 +225,7 @@ struct uavs3e_cuda_me {
     std::vector<u16> h_r2m;
 };
 
-static const int kNdy = 4;
+static const int kNdy = ME_NDY;
 static_assert(sizeof(MeResult) == sizeof(uavs3e_cuda_me_result_t), "result record layout");
 
 static pel *me_plane_ptr(uavs3e_cuda_me *m, int slot, int phase)

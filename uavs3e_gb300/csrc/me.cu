@@ -251,8 +251,12 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
         const int dx = P.lo_x + dxi, dy0 = P.lo_y + dyc * NDY;
         const int bx = off + 16 * sx + dxi;
         const int sh = bx & 3;
-        const int row0 = 16 * sy + dyc * NDY;
-        const u32 *wrow = win + row0 * P.win_ww + (bx >> 2);
+        // rows R0 .. R0+15+NDY-1 of the window; the skew changes once, at the same row for
+        // every lane (16*sy is a multiple of 16), so two base pointers cover the item
+        const int R0 = 16 * sy + dyc * NDY;
+        const int rr_c = 16 - (R0 & 15);
+        const u32 *p0 = win + R0 * P.win_ww + win_skew(R0) + (bx >> 2);
+        const u32 *p1 = p0 + (win_skew(R0 + 16) - win_skew(R0));
 
         u32 acc[NDY][4];
 #pragma unroll
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
 
 #pragma unroll
         for (int rr = 0; rr < 16 + NDY - 1; rr++) {
-            const u32 *wp = wrow + rr * P.win_ww + win_skew(row0 + rr);
+            const u32 *wp = (rr < rr_c ? p0 : p1) + rr * P.win_ww;
             const u32 w0 = wp[0], w1 = wp[1], w2 = wp[2], w3 = wp[3], w4 = wp[4];
             const u32 a0 = align4(w0, w1, sh), a1 = align4(w1, w2, sh);
             const u32 a2 = align4(w2, w3, sh), a3 = align4(w3, w4, sh);
@@ -608,7 +612,7 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     P.lo_x = t.lo_x; P.hi_x = t.hi_x; P.lo_y = t.lo_y; P.hi_y = t.hi_y;
     P.ndx = t.ndx; P.nchunk = t.nchunk; P.n_items = t.n_items; P.lambda_mv = a.lambda_mv;
     P.q2tab = a.q2tab; P.rank2mv = a.rank2mv; P.keys = keys; P.n_refs = a.n_refs;
-    constexpr int NDY = 4;
+    constexpr int NDY = ME_NDY;
     if (t.ndy_per_item != NDY) return set_status(UC_ERR_ARG, "me: table built for another NDY");
     P.win_h = 64 + t.nchunk * NDY - 1 + 1;
     P.win_cols = ((15 + 64 + t.ndx + 4 + 15) / 16) * 16;

@@ -20,11 +20,11 @@
 namespace uc {
 
 // limits of the static scratch: a 1920x1088 frame (510 CTUs of 64x64), 2 references,
-// search range 64 (4 vertically adjacent candidates per search item)
+// search range 64
 constexpr int NA_MAX_CTUS = UAVS3E_CUDA_NOALLOC_MAX_CTUS;
 constexpr int NA_MAX_REFS = UAVS3E_CUDA_NOALLOC_MAX_REFS;
 constexpr int NA_MAX_RANGE = UAVS3E_CUDA_NOALLOC_MAX_RANGE;
-constexpr int NA_NDY = 4;
+constexpr int NA_NDY = ME_NDY;
 constexpr size_t NA_KEYS = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * sizeof(u64);
 constexpr size_t NA_SUB = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * 17 * sizeof(u32);
 constexpr size_t NA_Q2_ENTRIES = (size_t)(2 * NA_MAX_RANGE + 1) * (((2 * NA_MAX_RANGE + 1) + NA_NDY - 1) / NA_NDY) * NA_NDY;

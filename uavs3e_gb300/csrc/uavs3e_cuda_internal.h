@@ -13,6 +13,7 @@ constexpr int ME_CTU = 64;
 constexpr int ME_BLOCKS_PER_CTU = 169;
 constexpr int ME_GROUPS = 16;          // lane groups (half-warps) per search CTA
 constexpr int ME_RANK_BITS = 11;
+constexpr int ME_NDY = 8;              // vertically adjacent candidates per search item
 constexpr int ME_MAX_GROUP = 1 << ME_RANK_BITS;
 
 // canonical per-CTU block list: shapes 8x8, 16x8, 8x16, 16x16, 32x16, 16x32, 32x32, 64x32,
