@@ -61,6 +61,11 @@ UAVS3E_CUDA_API const char *uavs3e_cuda_version(void);
  * returns, per kernel id (0 pad, 1 frame interpolation, 2 integer search, 3 fractional
  * refinement), the summed milliseconds and launch counts, then forgets them. */
 UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
+/* Measured issue rate of the 4-sample SAD instruction (vabsdiff4 with accumulate) on the current
+ * device: operations per second and per clock per SM.  The integer motion search's roofline
+ * denominator (about 1.3 ms of GPU time). */
+UAVS3E_CUDA_API int uavs3e_cuda_measure_sad4_rate(double *ops_per_s, double *ops_per_clk_sm);
+
 /* Number of kernels this library has launched in this process. */
 UAVS3E_CUDA_API unsigned long long uavs3e_cuda_launch_count(void);
 UAVS3E_CUDA_API int uavs3e_cuda_profile_collect(double ms[], int counts[], int n);

@@ -111,6 +111,13 @@ def profile_enable(on=True):
     lib().uavs3e_cuda_profile_enable(1 if on else 0)
 
 
+def measure_sad4_rate():
+    """(ops/s, ops per clock per SM) of vabsdiff4-with-accumulate on the current device"""
+    a, b = C.c_double(), C.c_double()
+    check(lib().uavs3e_cuda_measure_sad4_rate(C.byref(a), C.byref(b)), "measure_sad4_rate")
+    return a.value, b.value
+
+
 def launch_count():
     return int(lib().uavs3e_cuda_launch_count())
 
