@@ -52,7 +52,10 @@ def run_oracle_me(oracle, org, refs, W, H, rng, lam, pad=144, threads=8):
     return valid, res.reshape(len(vb), len(refs))
 
 
-@pytest.mark.parametrize("W,H,rng,qp", [(192, 128, 64, 32), (200, 136, 24, 27), (128, 64, 16, 45), (320, 200, 8, 37)])
+# search ranges cover every split of the dy range into 8-row items plus leftover rows:
+# 2r+1 = 129, 49, 33, 17 (one row left), 13 (five), 21 (five), 7 and 5 (no full item)
+@pytest.mark.parametrize("W,H,rng,qp", [(192, 128, 64, 32), (200, 136, 24, 27), (128, 64, 16, 45), (320, 200, 8, 37),
+                                        (256, 128, 6, 32), (136, 72, 10, 40), (192, 128, 3, 30), (160, 96, 2, 22)])
 def test_me_frame_matches_oracle(gpu, oracle, W, H, rng, qp):
     frames = motion_sequence(W, H, 3, seed=W + H, n_rects=3)
     lam = lambda_mv_for_qp(qp)

@@ -238,8 +238,10 @@ static int me_prepare_tables(uavs3e_cuda_me *m, u32 lambda, cudaStream_t st)
     if (m->tab_ok && m->tab.lambda_mv == lambda) return UC_OK;
     size_t cap = me_q2_entries(m->range, kNdy);
     m->h_q2.assign(cap, 0xFFFFFFFFu);
-    m->h_r2m.assign((size_t)ME_GROUPS * ME_MAX_GROUP, 0);
-    if (me_build_tables(m->W, m->H, m->range, lambda, kNdy, &m->tab, m->h_q2.data(), m->h_r2m.data(), cap))
+    m->h_r2m.assign((size_t)ME_R2M_ENTRIES, 0);
+    std::vector<MeCand> cand(ME_MAX_GROUP);
+    if (me_build_tables(m->W, m->H, m->range, lambda, kNdy, &m->tab, m->h_q2.data(), m->h_r2m.data(), cap,
+                        cand.data()))
         return set_status(UC_ERR_ARG, "me: cannot build search tables for this size/range");
     // synchronous upload: tables change only with lambda (per slice QP)
     UC_CHECK(cudaStreamSynchronize(st));
@@ -272,7 +274,7 @@ UAVS3E_CUDA_API uavs3e_cuda_me *uavs3e_cuda_me_open(int width, int height, int n
               cudaMalloc(&m->keys, me_key_scratch_bytes(width, height, n_refs)) == cudaSuccess &&
               cudaMalloc(&m->sub, me_sub_scratch_bytes(width, height, n_refs)) == cudaSuccess &&
               cudaMalloc(&m->q2, me_q2_entries(range, kNdy) * sizeof(u32)) == cudaSuccess &&
-              cudaMalloc(&m->r2m, (size_t)ME_GROUPS * ME_MAX_GROUP * sizeof(u16)) == cudaSuccess &&
+              cudaMalloc(&m->r2m, (size_t)ME_R2M_ENTRIES * sizeof(u16)) == cudaSuccess &&
               cudaMemset(m->planes_buf, 0, m->plane_bytes * 16 * n_refs) == cudaSuccess;
     if (!ok) {
         set_status(UC_ERR_MEMORY, "me_open: device allocation failed");

@@ -7,20 +7,21 @@
 //   fractional stage: me_sub_pel_search with SATD cost (src/me.c:366-500): centre, 8
 //     half-sample and 8 quarter-sample neighbours, com_had on the interpolated planes.
 //
-// Integer stage layout: one CTA per (CTU, reference).  Its search window is staged once into
-// shared memory.  A half-warp covers the CTU as a 4x4 grid of 16x16 sub-blocks (one lane
-// each, org samples in registers) and sweeps NDY vertically adjacent candidates at one dx,
-// so every byte-aligned reference word is reused by up to NDY rows of the block.  The four
-// 8x8 tile SADs of a lane give the 8x8/16x8/8x16/16x16 blocks; warp shuffles give the
-// 32x16 .. 64x64 ones.  Each block keeps a 32-bit running minimum of
+// Integer stage layout: one CTA per (CTU, reference, class of dx mod 4).  Its search window
+// is staged once into shared memory, pre-shifted so that the class's reference words are
+// word-aligned.  A half-warp covers the CTU as a 4x4 grid of 16x16 sub-blocks (one lane each,
+// org samples in registers) and sweeps NDY vertically adjacent candidates at one dx, so every
+// reference word is reused by up to NDY rows of the block.  The four 8x8 tile SADs of a lane
+// give the 8x8/16x8/8x16/16x16 blocks; warp shuffles give the 32x16 .. 64x64 ones.  Each
+// block keeps a 32-bit running minimum of
 //     ((SAD + q) << 11) | rank,   q = mvcost >> 16,
 // where rank orders this lane group's candidates by (mvcost & 0xffff, raster index): the
-// minimum is then exactly the (cost, raster) minimum, so a block update is one LEA + one
-// IMNMX.  Per-group winners are merged into a 64-bit (cost << 15 | raster) key.
+// minimum is then exactly the (cost, raster) minimum, so a block update is one IMAD + one
+// IMNMX.  Per-group winners are merged into a 64-bit (cost << 15 | raster) key, first in
+// shared memory, then across the four class CTAs with global atomics.
 #include "common.cuh"
 #include "uavs3e_cuda_internal.h"
 #include <algorithm>
-#include <vector>
 
 namespace uc {
 
@@ -53,13 +54,6 @@ __host__ __device__ __forceinline__ u32 mvbits(int v)
 
 u32 me_mvbits(int v) { return mvbits(v); }
 
-size_t me_q2_entries(int range, int ndy_per_item)
-{
-    int nd = 2 * range + 1;
-    int nchunk = (nd + ndy_per_item - 1) / ndy_per_item;
-    return (size_t)nd * nchunk * ndy_per_item;
-}
-
 size_t me_sub_scratch_bytes(int W, int H, int n_refs)
 {
     size_t nctu = (size_t)((W + 63) / 64) * ((H + 63) / 64);
@@ -72,45 +66,87 @@ size_t me_key_scratch_bytes(int W, int H, int n_refs)
     return nctu * n_refs * ME_BLOCKS_PER_CTU * sizeof(u64);
 }
 
+// Search items.  Candidates of one alignment class c (dx index = c mod 4) are cut into main
+// items of ME_NDY vertically adjacent candidates (rows 8k .. 8k+7 of the dy range) and, for
+// the ndy % 8 rows left at the bottom, tail items of one candidate.  Each list is padded to a
+// multiple of ME_GROUPS items with repeats of its first items, so every lane group has work
+// and needs no validity test; a repeated candidate only repeats a key.  Lane group g takes
+// items g, g + 16, ...; its candidates are ranked by (mvcost & 0xffff, raster).
+//
+// Buffer layout (u32): per class [main q2: 8 per item][tail q2: 1 per item], then per class
+// [main descriptors][tail descriptors]; a descriptor is dx_k | dy_row << 16 for the dx index
+// c + 4 dx_k and the dy index dy_row (of the item's first candidate).
 int me_build_tables(int W, int H, int range, u32 lambda_mv, int ndy, MeTables *t, u32 *q2tab, u16 *rank2mv,
-                    size_t q2cap)
+                    size_t q2cap, MeCand *cand)
 {
+    if (ndy != ME_NDY) return UC_ERR_ARG;
     int M = std::max(W, H);
     t->lo_x = t->lo_y = std::max(-range, -M + 4);
     t->hi_x = t->hi_y = std::min(range, M - 4);
     t->ndx = t->hi_x - t->lo_x + 1;
     t->ndy = t->hi_y - t->lo_y + 1;
     t->ndy_per_item = ndy;
-    t->nchunk = (t->ndy + ndy - 1) / ndy;
-    t->n_items = t->ndx * t->nchunk;
+    t->nfull = t->ndy / ndy;
+    t->rem = t->ndy % ndy;
     t->lambda_mv = lambda_mv;
-    if (t->ndx <= 0 || (size_t)t->n_items * ndy > q2cap || t->ndx * t->ndy > (1 << 15)) return UC_ERR_ARG;
-    // per lane group: its candidates sorted by (mvcost & 0xffff, raster)
-    for (int g = 0; g < ME_GROUPS; g++) {
-        std::vector<std::pair<u32, u32>> c;   // (r, raster) -> position in the table
-        std::vector<std::pair<std::pair<u32, u32>, size_t>> v;
-        for (int it = g; it < t->n_items; it += ME_GROUPS) {
-            int dx = t->lo_x + it % t->ndx, dy0 = t->lo_y + (it / t->ndx) * ndy;
-            for (int j = 0; j < ndy; j++) {
-                int dy = dy0 + j;
-                size_t pos = (size_t)it * ndy + j;
-                if (dy > t->hi_y) { q2tab[pos] = 0xFFFFFFFFu; continue; }
-                u32 mvc = (mvbits(4 * dx) + mvbits(4 * dy)) * lambda_mv;
-                u32 raster = (u32)((dy - t->lo_y) * t->ndx + (dx - t->lo_x));
-                v.push_back({ { mvc & 0xFFFFu, raster }, pos });
-            }
+    if (t->ndx <= 0 || t->ndx * t->ndy > (1 << 15)) return UC_ERR_ARG;
+    const auto up16 = [](int n) { return (n + ME_GROUPS - 1) / ME_GROUPS * ME_GROUPS; };
+    size_t pos = 0;
+    int nm_real[ME_CLASSES], nt_real[ME_CLASSES];
+    for (int c = 0; c < ME_CLASSES; c++) {
+        t->n_dx[c] = t->ndx > c ? (t->ndx - c + ME_CLASSES - 1) / ME_CLASSES : 0;
+        nm_real[c] = t->n_dx[c] * t->nfull;
+        nt_real[c] = t->n_dx[c] * t->rem;
+        t->n_main[c] = up16(nm_real[c]);
+        t->n_tail[c] = up16(nt_real[c]);
+        t->q2_main[c] = (int)pos; pos += (size_t)t->n_main[c] * ndy;
+        t->q2_tail[c] = (int)pos; pos += (size_t)t->n_tail[c];
+    }
+    for (int c = 0; c < ME_CLASSES; c++) {
+        t->d_main[c] = (int)pos; pos += (size_t)t->n_main[c];
+        t->d_tail[c] = (int)pos; pos += (size_t)t->n_tail[c];
+    }
+    if (pos > q2cap) return UC_ERR_ARG;
+    t->n_entries = (int)pos;
+    for (int c = 0; c < ME_CLASSES; c++) {
+        for (int it = 0; it < t->n_main[c]; it++) {
+            const int ri = it % nm_real[c];
+            q2tab[t->d_main[c] + it] = (u32)(ri % t->n_dx[c]) | (u32)(ndy * (ri / t->n_dx[c])) << 16;
         }
-        if (v.size() > (size_t)ME_MAX_GROUP) return UC_ERR_ARG;
-        std::sort(v.begin(), v.end());
-        for (size_t k = 0; k < v.size(); k++) {
-            size_t pos = v[k].second;
-            int it = (int)(pos / ndy), j = (int)(pos % ndy);
-            int dx = t->lo_x + it % t->ndx, dy = t->lo_y + (it / t->ndx) * ndy + j;
-            u32 mvc = (mvbits(4 * dx) + mvbits(4 * dy)) * lambda_mv;
-            q2tab[pos] = ((mvc >> 16) << ME_RANK_BITS) | (u32)k;
-            rank2mv[g * ME_MAX_GROUP + k] = (u16)v[k].first.second;
+        for (int it = 0; it < t->n_tail[c]; it++) {
+            const int ri = it % nt_real[c];
+            q2tab[t->d_tail[c] + it] = (u32)(ri % t->n_dx[c]) | (u32)(ndy * t->nfull + ri / t->n_dx[c]) << 16;
         }
     }
+    for (int c = 0; c < ME_CLASSES; c++)
+        for (int g = 0; g < ME_GROUPS; g++) {
+            int n = 0;
+            const auto add = [&](u32 desc, int j, u32 at) {
+                const int dxi = c + ME_CLASSES * (int)(desc & 0xFFFFu), dyi = (int)(desc >> 16) + j;
+                const int dx = t->lo_x + dxi, dy = t->lo_y + dyi;
+                const u32 mvc = (mvbits(4 * dx) + mvbits(4 * dy)) * lambda_mv;
+                cand[n++] = MeCand{ mvc & 0xFFFFu, (u32)(dyi * t->ndx + dxi), at };
+            };
+            for (int it = g; it < t->n_main[c]; it += ME_GROUPS)
+                for (int j = 0; j < ndy; j++) {
+                    if (n >= ME_MAX_GROUP) return UC_ERR_ARG;
+                    add(q2tab[t->d_main[c] + it], j, (u32)(t->q2_main[c] + it * ndy + j));
+                }
+            for (int it = g; it < t->n_tail[c]; it += ME_GROUPS) {
+                if (n >= ME_MAX_GROUP) return UC_ERR_ARG;
+                add(q2tab[t->d_tail[c] + it], 0, (u32)(t->q2_tail[c] + it));
+            }
+            std::sort(cand, cand + n, [](const MeCand &x, const MeCand &y) {
+                return x.r != y.r ? x.r < y.r : x.raster < y.raster;
+            });
+            for (int k = 0; k < n; k++) {
+                const int dx = t->lo_x + (int)(cand[k].raster % t->ndx);
+                const int dy = t->lo_y + (int)(cand[k].raster / t->ndx);
+                const u32 mvc = (mvbits(4 * dx) + mvbits(4 * dy)) * lambda_mv;
+                q2tab[cand[k].pos] = ((mvc >> 16) << ME_RANK_BITS) | (u32)k;
+                rank2mv[(c * ME_GROUPS + g) * ME_MAX_GROUP + k] = (u16)cand[k].raster;
+            }
+        }
     return UC_OK;
 }
 
@@ -118,8 +154,12 @@ struct MeIntParams {
     const pel *org; int i_org;
     const pel *ref[ME_MAX_REFS]; int i_ref;
     int W, H, ctus_w;
-    int lo_x, hi_x, lo_y, hi_y, ndx, nchunk, n_items;
+    int lo_x, hi_x, lo_y, hi_y, ndx;
+    int n_main[ME_CLASSES], n_tail[ME_CLASSES];     // items per class (multiples of ME_GROUPS)
+    int q2_main[ME_CLASSES], q2_tail[ME_CLASSES];   // offsets into q2tab
+    int d_main[ME_CLASSES], d_tail[ME_CLASSES];
     u32 lambda_mv;
+    u32 mul, one, minus1;  // 2^11, 1, 2^32-1 as run-time values: key arithmetic stays on IMAD
     const u32 *q2tab; const u16 *rank2mv;
     u64 *keys;             // [ctu][ref][169]
     int n_refs;
@@ -155,7 +195,150 @@ __device__ __forceinline__ void upd(u32 &b, u32 v, bool ok)
     if (ok) b = min(b, v);
 }
 
+// per-lane constants of the integer search
+struct MeLane {
+    int sx, sy;
+    u32 b0, b1, b2, b3, nb0, nb1, nb2, nb3;   // bits of the lane's sub-block index and complements
+    // largest valid dx / dy of a block whose top-left corner is the lane's 16x16 sub-block (0),
+    // its right or lower 8x8 half (1), the 32-aligned pair it belongs to (p), the CTU (c)
+    int X0, X1, Xp, Xc, Y0, Y1, Yp, Yc;
+};
+
+// One search item of a lane: NDY vertically adjacent candidates at one dx against the lane's
+// 16x16 sub-block, folded into the running minima of the 15 blocks the lane keeps.
 template <int NDY, bool EDGE>
+__device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, const u32 (&o)[16][4],
+                                        u32 (&best)[15], u32 desc, const u32 *q2p, int cls, int off,
+                                        const MeLane &L)
+{
+    const int dxi = cls + ME_CLASSES * (int)(desc & 0xFFFFu);
+    const int dyi0 = (int)(desc >> 16);
+    const int dx = P.lo_x + dxi, dy0 = P.lo_y + dyi0;
+    const int bx = off + 16 * L.sx + dxi;             // == the window's shift (mod 4)
+    // rows R0 .. R0+15+NDY-1 of the window; the skew changes once, at the same row for every
+    // lane of the half-warp (16*sy is a multiple of 16), so two base pointers cover the item
+    const int R0 = 16 * L.sy + dyi0;
+    const u32 *p0 = win + R0 * P.win_ww + win_skew(R0) + (bx >> 2);
+    const u32 *p1 = p0 + (win_skew(R0 + 16) - win_skew(R0));
+    // main items start on a multiple of 8 rows: rows 0-7 are before the change, rows 16..
+    // after it, rows 8-15 on the side R0 & 8 selects
+    const u32 *pm = (R0 & 8) ? p1 : p0;
+    const int rr_c = 16 - (R0 & 15);
+
+    u32 acc[NDY][4];
+#pragma unroll
+    for (int j = 0; j < NDY; j++)
+#pragma unroll
+        for (int t = 0; t < 4; t++) acc[j][t] = 0;
+
+#pragma unroll
+    for (int rr = 0; rr < 16 + NDY - 1; rr++) {
+        const u32 *wp;
+        if (NDY == 8) wp = (rr < 8 ? p0 : rr < 16 ? pm : p1) + rr * P.win_ww;
+        else wp = (rr < rr_c ? p0 : p1) + rr * P.win_ww;
+        const u32 a0 = wp[0], a1 = wp[1], a2 = wp[2], a3 = wp[3];
+#pragma unroll
+        for (int j = 0; j < NDY; j++) {
+            const int r = rr - j;
+            if (r < 0 || r >= 16) continue;
+            const int t = (r >> 3) * 2;
+            acc[j][t] = sad4(o[r][0], a0, acc[j][t]);
+            acc[j][t] = sad4(o[r][1], a1, acc[j][t]);
+            acc[j][t + 1] = sad4(o[r][2], a2, acc[j][t + 1]);
+            acc[j][t + 1] = sad4(o[r][3], a3, acc[j][t + 1]);
+        }
+    }
+
+    // keys (sad << 11) + q2 and the SAD sums of larger blocks are IMADs with run-time
+    // multipliers (mul = 2^11, one = 1, m1 = -1, lane bits as selectors): they issue on the FMA
+    // pipe and leave the integer ALU pipe to the vabsdiff4s and the running minima
+    const u32 mul = P.mul, one = P.one, m1 = P.minus1;
+    const bool xa = dx <= L.X0, xb = dx <= L.X1, xp = dx <= L.Xp, xc = dx <= L.Xc;
+    u32 s16[NDY], q2s[NDY];
+#pragma unroll
+    for (int j = 0; j < NDY; j++) {
+        const u32 q2 = __ldg(q2p + j);
+        q2s[j] = q2;
+        const int dy = dy0 + j;
+        const bool ya = dy <= L.Y0, yb = dy <= L.Y1;
+        const u32 t00 = acc[j][0], t01 = acc[j][1], t10 = acc[j][2], t11 = acc[j][3];
+        const u32 v00 = t00 * mul + q2, v01 = t01 * mul + q2;
+        const u32 v10 = t10 * mul + q2, v11 = t11 * mul + q2;
+        const u32 vl = t10 * mul + v00, vr = t11 * mul + v01;
+        const u32 st = t00 * one + t01, sb = t10 * one + t11;
+        const u32 vt = st * mul + q2, vb = sb * mul + q2;
+        s16[j] = st * one + sb;
+        const u32 v16 = s16[j] * mul + q2;
+        upd(best[0], v00, !EDGE || (xa && ya));
+        upd(best[1], v01, !EDGE || (xb && ya));
+        upd(best[2], v10, !EDGE || (xa && yb));
+        upd(best[3], v11, !EDGE || (xb && yb));
+        upd(best[4], vt, !EDGE || (xa && ya));     // 16x8 top
+        upd(best[5], vb, !EDGE || (xa && yb));     // 16x8 bottom
+        upd(best[6], vl, !EDGE || (xa && ya));     // 8x16 left
+        upd(best[7], vr, !EDGE || (xb && ya));     // 8x16 right
+        upd(best[8], v16, !EDGE || (xa && ya));
+    }
+
+    if constexpr (NDY == 1) {
+        // one candidate: every lane of a block's group forms the block's full sum
+        const u32 q2 = q2s[0];
+        const int dy = dy0;
+        const bool ya = dy <= L.Y0, yp = dy <= L.Yp, yc = dy <= L.Yc;
+        const u32 s32x16 = __shfl_xor_sync(0xFFFFFFFFu, s16[0], 1) * one + s16[0];
+        const u32 s16x32 = __shfl_xor_sync(0xFFFFFFFFu, s16[0], 4) * one + s16[0];
+        const u32 s32 = __shfl_xor_sync(0xFFFFFFFFu, s32x16, 4) * one + s32x16;
+        const u32 s64x32 = __shfl_xor_sync(0xFFFFFFFFu, s32, 2) * one + s32;
+        const u32 s32x64 = __shfl_xor_sync(0xFFFFFFFFu, s32, 8) * one + s32;
+        const u32 s64 = __shfl_xor_sync(0xFFFFFFFFu, s64x32, 8) * one + s64x32;
+        upd(best[9], s32x16 * mul + q2, !EDGE || (xp && ya));
+        upd(best[10], s16x32 * mul + q2, !EDGE || (xa && yp));
+        upd(best[11], s32 * mul + q2, !EDGE || (xp && yp));
+        upd(best[12], s64x32 * mul + q2, !EDGE || (xc && yp));
+        upd(best[13], s32x64 * mul + q2, !EDGE || (xp && yc));
+        upd(best[14], s64 * mul + q2, !EDGE || (xc && yc));
+    } else {
+        // eight candidates: the lanes that share a larger block split the candidates between
+        // them at each merge step (a lane keeps the half its bit selects and sends the other
+        // half to its partner), so each lane folds only its share into the block's minimum
+        static_assert(NDY == 8, "split merge of eight candidates");
+        u32 h[4], v[4];   // 32x16 sums for j = 4*b0 + i, 16x32 sums for j = 4*b2 + i
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const u32 d = s16[i] * m1 + s16[i + 4];
+            h[i] = __shfl_xor_sync(0xFFFFFFFFu, d * L.nb0 + s16[i], 1) * one + (d * L.b0 + s16[i]);
+            v[i] = __shfl_xor_sync(0xFFFFFFFFu, d * L.nb2 + s16[i], 4) * one + (d * L.b2 + s16[i]);
+        }
+        const int jb = 4 * (int)L.b0 + 2 * (int)L.b2;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int jh = 4 * (int)L.b0 + i, jv = 4 * (int)L.b2 + i;
+            upd(best[9], h[i] * mul + __ldg(q2p + jh), !EDGE || (xp && dy0 + jh <= L.Y0));
+            upd(best[10], v[i] * mul + __ldg(q2p + jv), !EDGE || (xa && dy0 + jv <= L.Yp));
+        }
+        // 32x32 from the 32x16 sums of the pair below/above (same candidates), split on b2
+        u32 q[2];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const u32 d = h[i] * m1 + h[i + 2];
+            q[i] = __shfl_xor_sync(0xFFFFFFFFu, d * L.nb2 + h[i], 4) * one + (d * L.b2 + h[i]);
+            upd(best[11], q[i] * mul + __ldg(q2p + jb + i), !EDGE || (xp && dy0 + jb + i <= L.Yp));
+        }
+        // 64x32 (partner 32 samples to the side, split on b1), 32x64 (partner 32 rows away,
+        // split on b3), 64x64 from the 64x32 sums (no split left)
+        const u32 dq = q[0] * m1 + q[1];
+        const u32 e = __shfl_xor_sync(0xFFFFFFFFu, dq * L.nb1 + q[0], 2) * one + (dq * L.b1 + q[0]);
+        const u32 f = __shfl_xor_sync(0xFFFFFFFFu, dq * L.nb3 + q[0], 8) * one + (dq * L.b3 + q[0]);
+        const u32 z = __shfl_xor_sync(0xFFFFFFFFu, e, 8) * one + e;
+        const int je = jb + (int)L.b1, jf = jb + (int)L.b3;
+        const u32 qe = __ldg(q2p + je);
+        upd(best[12], e * mul + qe, !EDGE || (xc && dy0 + je <= L.Yp));
+        upd(best[13], f * mul + __ldg(q2p + jf), !EDGE || (xp && dy0 + jf <= L.Yc));
+        upd(best[14], z * mul + qe, !EDGE || (xc && dy0 + je <= L.Yc));
+    }
+}
+
+template <bool EDGE>
 __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
 {
     extern __shared__ __align__(16) u32 win[];
@@ -170,56 +353,61 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
     const pel *rp = P.ref[ref];
 
     // ---- stage the search window: rows cy+lo_y .., columns from a 16-byte boundary.
-    // Row r is stored at word r*win_ww + skew(r): the 16 lanes of a half-warp read rows 16
-    // apart, and the skew spreads them over distinct banks.
+    // This CTA only searches horizontal offsets of one residue class mod 4, so every lane's
+    // reference words start at the same byte offset `sh` within a word: the window is stored
+    // pre-shifted by sh bytes and the search reads whole words.  Row r is stored at word
+    // r*win_ww + skew(r): the 16 lanes of a half-warp read rows 16 apart, and the skew spreads
+    // them over distinct banks.
+    const int cls = blockIdx.z;
     const pel *g0 = rp + (long long)(cy + P.lo_y) * P.i_ref + (cx + P.lo_x);
     const int off = (int)(((uintptr_t)g0) & 15);
     const pel *gw = g0 - off;
+    const int sh = (off + cls) & 3;
     const int wwords = P.win_cols >> 2;                 // words of window data per row
     // columns past the right padding are never read by a valid candidate: filled with 0
     const int gcol0 = cx + P.lo_x - off, gcol_end = P.W + P.pad;
-    if ((P.i_ref & 15) == 0) {
-        const int nv = wwords >> 2;
+    {
+        const int nv = wwords >> 2;                     // 16-byte chunks per row
         for (int i = tid; i < P.win_h * nv; i += blockDim.x) {
-            int r = i / nv, c = i % nv;
-            uint4 v;
-            if (gcol0 + c * 16 + 15 < gcol_end) {
-                v = __ldg(reinterpret_cast<const uint4 *>(gw + (long long)r * P.i_ref) + c);
+            const int r = i / nv, c = i % nv;
+            const pel *grow = gw + (long long)r * P.i_ref;
+            u32 wv[5];
+            if ((P.i_ref & 15) == 0 && gcol0 + c * 16 + 19 < gcol_end) {
+                const uint4 v = __ldg(reinterpret_cast<const uint4 *>(grow) + c);
+                wv[0] = v.x; wv[1] = v.y; wv[2] = v.z; wv[3] = v.w;
+                wv[4] = __ldg(reinterpret_cast<const u32 *>(grow) + 4 * c + 4);
             } else {
-                u32 wv[4];
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < 5; q++) {
                     wv[q] = 0;
                     for (int b = 0; b < 4; b++) {
-                        int col = c * 16 + q * 4 + b;
-                        if (gcol0 + col < gcol_end) wv[q] |= (u32)gw[(long long)r * P.i_ref + col] << (8 * b);
+                        const int col = c * 16 + q * 4 + b;
+                        if (gcol0 + col < gcol_end) wv[q] |= (u32)grow[col] << (8 * b);
                     }
                 }
-                v = make_uint4(wv[0], wv[1], wv[2], wv[3]);
             }
             u32 *d = win + r * P.win_ww + win_skew(r) + 4 * c;
-            d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
-        }
-    } else {
-        for (int i = tid; i < P.win_h * wwords; i += blockDim.x) {
-            int r = i / wwords, c = i % wwords;
-            u32 v = 0;
-            for (int b = 0; b < 4; b++) {
-                int col = 4 * c + b;
-                if (gcol0 + col < gcol_end) v |= (u32)gw[(long long)r * P.i_ref + col] << (8 * b);
-            }
-            win[r * P.win_ww + win_skew(r) + c] = v;
+#pragma unroll
+            for (int q = 0; q < 4; q++) d[q] = __funnelshift_r(wv[q], wv[q + 1], 8 * sh);
         }
     }
     for (int i = tid; i < ME_BLOCKS_PER_CTU; i += blockDim.x) skey[i] = ~0ull;
 
     const int lane = tid & 31, warp = tid >> 5;
     const int s = lane & 15, g = warp * 2 + (lane >> 4);
-    const int sx = s & 3, sy = s >> 2;
+    MeLane L;
+    L.sx = s & 3; L.sy = s >> 2;
+    L.b0 = s & 1; L.b1 = (s >> 1) & 1; L.b2 = (s >> 2) & 1; L.b3 = (s >> 3) & 1;
+    L.nb0 = 1 - L.b0; L.nb1 = 1 - L.b1; L.nb2 = 1 - L.b2; L.nb3 = 1 - L.b3;
+    // block-validity limits at the right/bottom picture edge (max_mv = pic - 1 - pos)
+    L.X0 = P.W - 1 - (cx + 16 * L.sx); L.X1 = L.X0 - 8;
+    L.Xp = P.W - 1 - (cx + 16 * (L.sx & 2)); L.Xc = P.W - 1 - cx;
+    L.Y0 = P.H - 1 - (cy + 16 * L.sy); L.Y1 = L.Y0 - 8;
+    L.Yp = P.H - 1 - (cy + 16 * (L.sy & 2)); L.Yc = P.H - 1 - cy;
 
     // ---- org 16x16 sub-block in registers (reads clamped to the picture)
     u32 o[16][4];
     {
-        const int ox = cx + 16 * sx, oy = cy + 16 * sy;
+        const int ox = cx + 16 * L.sx, oy = cy + 16 * L.sy;
 #pragma unroll
         for (int r = 0; r < 16; r++) {
             const pel *orow = P.org + (long long)min(oy + r, P.H - 1) * P.i_org;
@@ -234,96 +422,26 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
     }
     __syncthreads();
 
-    // block-validity limits at the right/bottom picture edge (max_mv = pic - 1 - pos)
-    const int lim_x0 = P.W - 1 - (cx + 16 * sx), lim_x1 = lim_x0 - 8;
-    const int lim_y0 = P.H - 1 - (cy + 16 * sy), lim_y1 = lim_y0 - 8;
-
     u32 best[15];
 #pragma unroll
     for (int i = 0; i < 15; i++) best[i] = 0xFFFFFFFFu;
 
-    const int n_iter = (P.n_items + ME_GROUPS - 1) / ME_GROUPS;   // warp-uniform trip count
-    for (int k = 0; k < n_iter; k++) {
-        const int it = g + k * ME_GROUPS;
-        const bool item_ok = it < P.n_items;
-        const int iti = item_ok ? it : 0;
-        const int dxi = iti % P.ndx, dyc = iti / P.ndx;
-        const int dx = P.lo_x + dxi, dy0 = P.lo_y + dyc * NDY;
-        const int bx = off + 16 * sx + dxi;
-        const int sh = bx & 3;
-        // rows R0 .. R0+15+NDY-1 of the window; the skew changes once, at the same row for
-        // every lane (16*sy is a multiple of 16), so two base pointers cover the item
-        const int R0 = 16 * sy + dyc * NDY;
-        const int rr_c = 16 - (R0 & 15);
-        const u32 *p0 = win + R0 * P.win_ww + win_skew(R0) + (bx >> 2);
-        const u32 *p1 = p0 + (win_skew(R0 + 16) - win_skew(R0));
-
-        u32 acc[NDY][4];
-#pragma unroll
-        for (int j = 0; j < NDY; j++)
-#pragma unroll
-            for (int t = 0; t < 4; t++) acc[j][t] = 0;
-
-#pragma unroll
-        for (int rr = 0; rr < 16 + NDY - 1; rr++) {
-            const u32 *wp = (rr < rr_c ? p0 : p1) + rr * P.win_ww;
-            const u32 w0 = wp[0], w1 = wp[1], w2 = wp[2], w3 = wp[3], w4 = wp[4];
-            const u32 a0 = align4(w0, w1, sh), a1 = align4(w1, w2, sh);
-            const u32 a2 = align4(w2, w3, sh), a3 = align4(w3, w4, sh);
-#pragma unroll
-            for (int j = 0; j < NDY; j++) {
-                const int r = rr - j;
-                if (r < 0 || r >= 16) continue;
-                const int t = (r >> 3) * 2;
-                acc[j][t] = sad4(o[r][0], a0, acc[j][t]);
-                acc[j][t] = sad4(o[r][1], a1, acc[j][t]);
-                acc[j][t + 1] = sad4(o[r][2], a2, acc[j][t + 1]);
-                acc[j][t + 1] = sad4(o[r][3], a3, acc[j][t + 1]);
-            }
-        }
-
-        const u32 *q2p = P.q2tab + (size_t)iti * NDY;
-#pragma unroll
-        for (int j = 0; j < NDY; j++) {
-            const int dy = dy0 + j;
-            const u32 q2 = __ldg(q2p + j);
-            const bool ok = item_ok && q2 != 0xFFFFFFFFu;
-            bool vx0 = true, vx1 = true, vy0 = true, vy1 = true;
-            if (EDGE) { vx0 = dx <= lim_x0; vx1 = dx <= lim_x1; vy0 = dy <= lim_y0; vy1 = dy <= lim_y1; }
-            const u32 t00 = acc[j][0], t01 = acc[j][1], t10 = acc[j][2], t11 = acc[j][3];
-            // keys (sad << 11) + q2, sums of keys formed as a + b - q2 (exact modulo 2^32)
-            const u32 v00 = (t00 << ME_RANK_BITS) + q2, v01 = (t01 << ME_RANK_BITS) + q2;
-            const u32 v10 = (t10 << ME_RANK_BITS) + q2, v11 = (t11 << ME_RANK_BITS) + q2;
-            const u32 vt = v00 + (t01 << ME_RANK_BITS), vb = v10 + (t11 << ME_RANK_BITS);
-            const u32 vl = v00 + (t10 << ME_RANK_BITS), vr = v01 + (t11 << ME_RANK_BITS);
-            const u32 v16 = vt + vb - q2;
-            const bool v00ok = ok && vx0 && vy0;
-            upd(best[0], v00, v00ok);
-            upd(best[1], v01, ok && vx1 && vy0);
-            upd(best[2], v10, ok && vx0 && vy1);
-            upd(best[3], v11, ok && vx1 && vy1);
-            upd(best[4], vt, v00ok);                  // 16x8 top
-            upd(best[5], vb, ok && vx0 && vy1);       // 16x8 bottom
-            upd(best[6], vl, v00ok);                  // 8x16 left
-            upd(best[7], vr, ok && vx1 && vy0);       // 8x16 right
-            upd(best[8], v16, v00ok);
-            const u32 v32x16 = v16 + __shfl_xor_sync(0xFFFFFFFFu, v16, 1) - q2;
-            const u32 v16x32 = v16 + __shfl_xor_sync(0xFFFFFFFFu, v16, 4) - q2;
-            const u32 v32 = v32x16 + __shfl_xor_sync(0xFFFFFFFFu, v32x16, 4) - q2;
-            const u32 v64x32 = v32 + __shfl_xor_sync(0xFFFFFFFFu, v32, 2) - q2;
-            const u32 v32x64 = v32 + __shfl_xor_sync(0xFFFFFFFFu, v32, 8) - q2;
-            const u32 v64 = v64x32 + __shfl_xor_sync(0xFFFFFFFFu, v64x32, 8) - q2;
-            upd(best[9], v32x16, v00ok);
-            upd(best[10], v16x32, v00ok);
-            upd(best[11], v32, v00ok);
-            upd(best[12], v64x32, v00ok);
-            upd(best[13], v32x64, v00ok);
-            upd(best[14], v64, v00ok);
-        }
+    // item counts are multiples of ME_GROUPS: the trip counts are warp-uniform
+    {
+        const u32 *dsc = P.q2tab + P.d_main[cls], *q2b = P.q2tab + P.q2_main[cls];
+        for (int it = g; it < P.n_main[cls]; it += ME_GROUPS)
+            me_item<ME_NDY, EDGE>(P, win, o, best, __ldg(dsc + it), q2b + it * ME_NDY, cls, off, L);
+    }
+    {
+        const u32 *dsc = P.q2tab + P.d_tail[cls], *q2b = P.q2tab + P.q2_tail[cls];
+        for (int it = g; it < P.n_tail[cls]; it += ME_GROUPS)
+            me_item<1, EDGE>(P, win, o, best, __ldg(dsc + it), q2b + it, cls, off, L);
     }
 
-    // ---- decode the lane group's winners and merge into the CTU's 64-bit keys
+    // ---- decode the lane's winners and merge into the CTU's 64-bit keys.  The lanes that
+    // share a block hold minima over disjoint (or repeated) candidates of the same lane group.
     {
+        const int sx = L.sx, sy = L.sy;
         int ids[15];
 #pragma unroll
         for (int i = 0; i < 2; i++)
@@ -334,17 +452,17 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
         ids[6] = 96 + sy * 8 + 2 * sx;
         ids[7] = 96 + sy * 8 + 2 * sx + 1;
         ids[8] = 128 + sy * 4 + sx;
-        ids[9] = (sx & 1) ? -1 : 144 + sy * 2 + (sx >> 1);
-        ids[10] = (sy & 1) ? -1 : 152 + (sy >> 1) * 4 + sx;
-        ids[11] = ((sx | sy) & 1) ? -1 : 160 + (sy >> 1) * 2 + (sx >> 1);
-        ids[12] = (sx == 0 && !(sy & 1)) ? 164 + (sy >> 1) : -1;
-        ids[13] = (sy == 0 && !(sx & 1)) ? 166 + (sx >> 1) : -1;
-        ids[14] = (sx == 0 && sy == 0) ? 168 : -1;
-        const u16 *r2m = P.rank2mv + g * ME_MAX_GROUP;
+        ids[9] = 144 + sy * 2 + (sx >> 1);
+        ids[10] = 152 + (sy >> 1) * 4 + sx;
+        ids[11] = 160 + (sy >> 1) * 2 + (sx >> 1);
+        ids[12] = 164 + (sy >> 1);
+        ids[13] = 166 + (sx >> 1);
+        ids[14] = 168;
+        const u16 *r2m = P.rank2mv + (cls * ME_GROUPS + g) * ME_MAX_GROUP;
 #pragma unroll
         for (int i = 0; i < 15; i++) {
             const u32 b = best[i];
-            if (ids[i] < 0 || b == 0xFFFFFFFFu) continue;
+            if (b == 0xFFFFFFFFu) continue;
             const u32 raster = r2m[b & (ME_MAX_GROUP - 1)];
             const int dx = P.lo_x + (int)(raster % P.ndx), dy = P.lo_y + (int)(raster / P.ndx);
             const u32 mvc = (mvbits(4 * dx) + mvbits(4 * dy)) * P.lambda_mv;
@@ -353,8 +471,10 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
         }
     }
     __syncthreads();
+    // the four alignment-class CTAs of this (CTU, reference) merge into keys preset to ~0
     u64 *dst = P.keys + ((size_t)ctu * P.n_refs + ref) * ME_BLOCKS_PER_CTU;
-    for (int i = tid; i < ME_BLOCKS_PER_CTU; i += blockDim.x) dst[i] = skey[i];
+    for (int i = tid; i < ME_BLOCKS_PER_CTU; i += blockDim.x)
+        if (skey[i] != ~0ull) atomicMin(reinterpret_cast<unsigned long long *>(dst + i), skey[i]);
 }
 
 // ---------------------------------------------------------------- fractional refinement
@@ -610,18 +730,24 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     for (int r = 0; r < ME_MAX_REFS; r++) P.ref[r] = r < a.n_refs ? a.planes[r][0] : nullptr;
     P.i_ref = a.i_ref; P.W = a.W; P.H = a.H; P.ctus_w = ctus_w;
     P.lo_x = t.lo_x; P.hi_x = t.hi_x; P.lo_y = t.lo_y; P.hi_y = t.hi_y;
-    P.ndx = t.ndx; P.nchunk = t.nchunk; P.n_items = t.n_items; P.lambda_mv = a.lambda_mv;
+    P.ndx = t.ndx; P.lambda_mv = a.lambda_mv;
+    for (int c = 0; c < ME_CLASSES; c++) {
+        P.n_main[c] = t.n_main[c]; P.n_tail[c] = t.n_tail[c];
+        P.q2_main[c] = t.q2_main[c]; P.q2_tail[c] = t.q2_tail[c];
+        P.d_main[c] = t.d_main[c]; P.d_tail[c] = t.d_tail[c];
+    }
+    P.mul = 1u << ME_RANK_BITS; P.one = 1u; P.minus1 = 0xFFFFFFFFu;
     P.q2tab = a.q2tab; P.rank2mv = a.rank2mv; P.keys = keys; P.n_refs = a.n_refs;
-    constexpr int NDY = ME_NDY;
-    if (t.ndy_per_item != NDY) return set_status(UC_ERR_ARG, "me: table built for another NDY");
-    P.win_h = 64 + t.nchunk * NDY - 1 + 1;
+    if (t.ndy_per_item != ME_NDY) return set_status(UC_ERR_ARG, "me: table built for another NDY");
+    // rows read: main items up to 48 + 8 (nfull - 1) + 22, tail items up to 48 + ndy - 1 + 15
+    P.win_h = t.ndy + 63;
     P.win_cols = ((15 + 64 + t.ndx + 4 + 15) / 16) * 16;
     P.win_ww = (P.win_cols >> 2) + 18 + 2;    // even, room for the largest skew
     const size_t smem = (size_t)P.win_h * P.win_ww * 4;
     static bool attr_set[64];
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        UC_CHECK(cudaFuncSetAttribute(k_me_int<NDY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-        UC_CHECK(cudaFuncSetAttribute(k_me_int<NDY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        UC_CHECK(cudaFuncSetAttribute(k_me_int<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        UC_CHECK(cudaFuncSetAttribute(k_me_int<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set[dev] = true;
     }
     if (smem > 100 * 1024) return set_status(UC_ERR_ARG, "me: window too large");
@@ -629,18 +755,20 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     int nx = a.W - 57 - t.hi_x >= 0 ? (a.W - 57 - t.hi_x) / 64 + 1 : 0;
     int ny = a.H - 57 - t.hi_y >= 0 ? (a.H - 57 - t.hi_y) / 64 + 1 : 0;
     nx = std::min(nx, ctus_w); ny = std::min(ny, ctus_h);
+    if (t.nfull == 0) nx = ny = 0;   // the interior kernel has no row limit: short ranges go to the edge kernel
     P.pad = a.pad; P.ctus_h = ctus_h; P.nx_int = nx; P.ny_int = ny;
     prof_begin(PROF_ME_INT, st);
+    UC_CHECK(cudaMemsetAsync(keys, 0xFF, (size_t)ctus_w * ctus_h * a.n_refs * ME_BLOCKS_PER_CTU * sizeof(u64), st));
     if (nx * ny > 0) {
         P.edge = 0;
-        k_me_int<NDY, false><<<dim3(nx * ny, a.n_refs), 256, smem, st>>>(P);
+        k_me_int<false><<<dim3(nx * ny, a.n_refs, ME_CLASSES), 256, smem, st>>>(P);
         UC_CHECK(cudaGetLastError());
         count_launch(1);
     }
     const int n_edge = ctus_w * ctus_h - nx * ny;
     if (n_edge > 0) {
         P.edge = 1;
-        k_me_int<NDY, true><<<dim3(n_edge, a.n_refs), 256, smem, st>>>(P);
+        k_me_int<true><<<dim3(n_edge, a.n_refs, ME_CLASSES), 256, smem, st>>>(P);
         UC_CHECK(cudaGetLastError());
         count_launch(1);
     }

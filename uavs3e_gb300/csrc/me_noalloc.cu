@@ -27,9 +27,9 @@ constexpr int NA_MAX_RANGE = UAVS3E_CUDA_NOALLOC_MAX_RANGE;
 constexpr int NA_NDY = ME_NDY;
 constexpr size_t NA_KEYS = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * sizeof(u64);
 constexpr size_t NA_SUB = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * 17 * sizeof(u32);
-constexpr size_t NA_Q2_ENTRIES = (size_t)(2 * NA_MAX_RANGE + 1) * (((2 * NA_MAX_RANGE + 1) + NA_NDY - 1) / NA_NDY) * NA_NDY;
+constexpr size_t NA_Q2_ENTRIES = me_q2_entries(NA_MAX_RANGE, NA_NDY);
 constexpr size_t NA_Q2 = NA_Q2_ENTRIES * sizeof(u32);
-constexpr size_t NA_R2M = (size_t)ME_GROUPS * ME_MAX_GROUP * sizeof(u16);
+constexpr size_t NA_R2M = (size_t)ME_R2M_ENTRIES * sizeof(u16);
 constexpr size_t na_up(size_t v) { return (v + 255) & ~(size_t)255; }
 constexpr size_t NA_OFF_SUB = na_up(NA_KEYS);
 constexpr size_t NA_OFF_Q2 = na_up(NA_OFF_SUB + NA_SUB);
@@ -54,50 +54,8 @@ static NaDevice g_na[64];
 
 // static host buffers for the table build (no heap use)
 static u32 g_h_q2[NA_Q2_ENTRIES];
-static u16 g_h_r2m[ME_GROUPS * ME_MAX_GROUP];
-struct NaCand { u32 r, raster, pos; };
-static NaCand g_cand[ME_MAX_GROUP];
-
-// the search tables of me_build_tables (csrc/me.cu), built into the static buffers
-static int na_build_tables(int W, int H, int range, u32 lambda, MeTables *t)
-{
-    const int M = std::max(W, H);
-    t->lo_x = t->lo_y = std::max(-range, -M + 4);
-    t->hi_x = t->hi_y = std::min(range, M - 4);
-    t->ndx = t->hi_x - t->lo_x + 1;
-    t->ndy = t->hi_y - t->lo_y + 1;
-    t->ndy_per_item = NA_NDY;
-    t->nchunk = (t->ndy + NA_NDY - 1) / NA_NDY;
-    t->n_items = t->ndx * t->nchunk;
-    t->lambda_mv = lambda;
-    if (t->ndx <= 0 || (size_t)t->n_items * NA_NDY > NA_Q2_ENTRIES) return UC_ERR_ARG;
-    for (int g = 0; g < ME_GROUPS; g++) {
-        int n = 0;
-        for (int it = g; it < t->n_items; it += ME_GROUPS) {
-            const int dx = t->lo_x + it % t->ndx, dy0 = t->lo_y + (it / t->ndx) * NA_NDY;
-            for (int j = 0; j < NA_NDY; j++) {
-                const int dy = dy0 + j;
-                const u32 pos = (u32)(it * NA_NDY + j);
-                if (dy > t->hi_y) { g_h_q2[pos] = 0xFFFFFFFFu; continue; }
-                if (n >= ME_MAX_GROUP) return UC_ERR_ARG;
-                const u32 mvc = (me_mvbits(4 * dx) + me_mvbits(4 * dy)) * lambda;
-                g_cand[n++] = NaCand{ mvc & 0xFFFFu, (u32)((dy - t->lo_y) * t->ndx + (dx - t->lo_x)), pos };
-            }
-        }
-        std::sort(g_cand, g_cand + n, [](const NaCand &a, const NaCand &b) {
-            return a.r != b.r ? a.r < b.r : a.raster < b.raster;
-        });
-        for (int k = 0; k < n; k++) {
-            const u32 pos = g_cand[k].pos;
-            const int it = (int)(pos / NA_NDY), j = (int)(pos % NA_NDY);
-            const int dx = t->lo_x + it % t->ndx, dy = t->lo_y + (it / t->ndx) * NA_NDY + j;
-            const u32 mvc = (me_mvbits(4 * dx) + me_mvbits(4 * dy)) * lambda;
-            g_h_q2[pos] = ((mvc >> 16) << ME_RANK_BITS) | (u32)k;
-            g_h_r2m[g * ME_MAX_GROUP + k] = (u16)g_cand[k].raster;
-        }
-    }
-    return UC_OK;
-}
+static u16 g_h_r2m[ME_R2M_ENTRIES];
+static MeCand g_cand[ME_MAX_GROUP];
 
 }  // namespace uc
 
@@ -135,10 +93,10 @@ extern "C" UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_or
         D.scratch = (unsigned char *)p;
     }
     if (!D.tables || D.W != width || D.H != height || D.range != range || D.lambda != lambda_mv) {
-        if (na_build_tables(width, height, range, lambda_mv, &D.tab))
+        if (me_build_tables(width, height, range, lambda_mv, NA_NDY, &D.tab, g_h_q2, g_h_r2m, NA_Q2_ENTRIES, g_cand))
             return set_status(UC_ERR_ARG, "me_search_noalloc: cannot build search tables");
         D.tables = false;
-        UC_CHECK(cudaMemcpyAsync(D.scratch + NA_OFF_Q2, g_h_q2, (size_t)D.tab.n_items * NA_NDY * sizeof(u32),
+        UC_CHECK(cudaMemcpyAsync(D.scratch + NA_OFF_Q2, g_h_q2, (size_t)D.tab.n_entries * sizeof(u32),
                                  cudaMemcpyHostToDevice, st));
         UC_CHECK(cudaMemcpyAsync(D.scratch + NA_OFF_R2M, g_h_r2m, NA_R2M, cudaMemcpyHostToDevice, st));
         // the host buffers are reused by the next build: wait until the copies have read them

@@ -14,6 +14,7 @@ constexpr int ME_BLOCKS_PER_CTU = 169;
 constexpr int ME_GROUPS = 16;          // lane groups (half-warps) per search CTA
 constexpr int ME_RANK_BITS = 11;
 constexpr int ME_NDY = 8;              // vertically adjacent candidates per search item
+constexpr int ME_CLASSES = 4;          // horizontal offsets are split by residue mod 4 (one per CTA)
 constexpr int ME_MAX_GROUP = 1 << ME_RANK_BITS;
 
 // canonical per-CTU block list: shapes 8x8, 16x8, 8x16, 16x16, 32x16, 16x32, 32x32, 64x32,
@@ -54,13 +55,31 @@ struct MeFrameArgs {
 size_t me_sub_scratch_bytes(int W, int H, int n_refs);
 
 struct MeTables {
-    int lo_x, hi_x, lo_y, hi_y, ndx, ndy, nchunk, n_items, ndy_per_item;
+    int lo_x, hi_x, lo_y, hi_y, ndx, ndy, ndy_per_item;
+    int nfull, rem;                     // full ndy_per_item-row chunks, rows left over
+    int n_entries;                      // u32 entries of the table buffer in use
+    // per alignment class (dx index mod 4): offsets, main and tail item counts, table offsets
+    int n_dx[ME_CLASSES], n_main[ME_CLASSES], n_tail[ME_CLASSES];
+    int q2_main[ME_CLASSES], q2_tail[ME_CLASSES], d_main[ME_CLASSES], d_tail[ME_CLASSES];
     u32 lambda_mv;
 };
-// builds the packed (q << 11 | rank) table and the rank -> raster map on the host
+// one candidate of a lane group while its ranks are built
+struct MeCand { u32 r, raster, pos; };
+constexpr int ME_R2M_ENTRIES = ME_CLASSES * ME_GROUPS * ME_MAX_GROUP;   // rank -> raster map
+// builds the packed (q << 11 | rank) table (me_q2_entries) and the rank -> raster map
+// (ME_R2M_ENTRIES) on the host; cand is ME_MAX_GROUP entries of work space
 int me_build_tables(int W, int H, int range, u32 lambda_mv, int ndy_per_item, MeTables *t,
-                    u32 *q2tab, u16 *rank2mv, size_t q2cap);
-size_t me_q2_entries(int range, int ndy_per_item);
+                    u32 *q2tab, u16 *rank2mv, size_t q2cap, MeCand *cand);
+// u32 entries of the search-table buffer (q2 entries, then item descriptors) for a search
+// range: per class at most ceil(nd/4) horizontal offsets, ceil(nd/8) main chunks and 7 tail
+// rows, each list padded to a multiple of ME_GROUPS items
+constexpr size_t me_q2_entries(int range, int ndy_per_item)
+{
+    return ME_CLASSES * ((ndy_per_item + 1) * (((2 * (size_t)range + 1 + ME_CLASSES - 1) / ME_CLASSES) *
+                                                   ((2 * (size_t)range + 1 + ndy_per_item - 1) / ndy_per_item) +
+                                               ME_GROUPS) +
+                         2 * (((2 * (size_t)range + 1 + ME_CLASSES - 1) / ME_CLASSES) * (ndy_per_item - 1) + ME_GROUPS));
+}
 size_t me_key_scratch_bytes(int W, int H, int n_refs);
 u32 me_mvbits(int v);   // MV bits of one quarter-sample component (host)
 int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStream_t st);
