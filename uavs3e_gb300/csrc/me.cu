@@ -150,6 +150,11 @@ int me_build_tables(int W, int H, int range, u32 lambda_mv, int ndy, MeTables *t
     return UC_OK;
 }
 
+// words per stored window row: data (at most 56 words at range 64), the largest skew (18)
+// and 2 spare; a multiple of 4, so rows 16 apart start on the same bank before the skew, and a
+// compile-time constant, so every row address of an item is an immediate offset
+constexpr int ME_WIN_WW = 76;
+
 struct MeIntParams {
     const pel *org; int i_org;
     const pel *ref[ME_MAX_REFS]; int i_ref;
@@ -163,7 +168,7 @@ struct MeIntParams {
     const u32 *q2tab; const u16 *rank2mv;
     u64 *keys;             // [ctu][ref][169]
     int n_refs;
-    int win_h, win_ww;     // window rows, words per stored row (incl. skew room)
+    int win_h;             // window rows (row pitch: ME_WIN_WW words)
     int win_cols;          // window data bytes per row
     int pad;               // reference padding (samples)
     int edge, nx_int, ny_int, ctus_h;   // CTU subset of this launch (see ctu_of)
@@ -218,7 +223,7 @@ __device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, co
     // rows R0 .. R0+15+NDY-1 of the window; the skew changes once, at the same row for every
     // lane of the half-warp (16*sy is a multiple of 16), so two base pointers cover the item
     const int R0 = 16 * L.sy + dyi0;
-    const u32 *p0 = win + R0 * P.win_ww + win_skew(R0) + (bx >> 2);
+    const u32 *p0 = win + R0 * ME_WIN_WW + win_skew(R0) + (bx >> 2);
     const u32 *p1 = p0 + (win_skew(R0 + 16) - win_skew(R0));
     // main items start on a multiple of 8 rows: rows 0-7 are before the change, rows 16..
     // after it, rows 8-15 on the side R0 & 8 selects
@@ -234,8 +239,8 @@ __device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, co
 #pragma unroll
     for (int rr = 0; rr < 16 + NDY - 1; rr++) {
         const u32 *wp;
-        if (NDY == 8) wp = (rr < 8 ? p0 : rr < 16 ? pm : p1) + rr * P.win_ww;
-        else wp = (rr < rr_c ? p0 : p1) + rr * P.win_ww;
+        if (NDY == 8) wp = (rr < 8 ? p0 : rr < 16 ? pm : p1) + rr * ME_WIN_WW;
+        else wp = (rr < rr_c ? p0 : p1) + rr * ME_WIN_WW;
         const u32 a0 = wp[0], a1 = wp[1], a2 = wp[2], a3 = wp[3];
 #pragma unroll
         for (int j = 0; j < NDY; j++) {
@@ -356,7 +361,7 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
     // This CTA only searches horizontal offsets of one residue class mod 4, so every lane's
     // reference words start at the same byte offset `sh` within a word: the window is stored
     // pre-shifted by sh bytes and the search reads whole words.  Row r is stored at word
-    // r*win_ww + skew(r): the 16 lanes of a half-warp read rows 16 apart, and the skew spreads
+    // r*ME_WIN_WW + skew(r): the 16 lanes of a half-warp read rows 16 apart, and the skew spreads
     // them over distinct banks.
     const int cls = blockIdx.z;
     const pel *g0 = rp + (long long)(cy + P.lo_y) * P.i_ref + (cx + P.lo_x);
@@ -385,7 +390,7 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
                     }
                 }
             }
-            u32 *d = win + r * P.win_ww + win_skew(r) + 4 * c;
+            u32 *d = win + r * ME_WIN_WW + win_skew(r) + 4 * c;
 #pragma unroll
             for (int q = 0; q < 4; q++) d[q] = __funnelshift_r(wv[q], wv[q + 1], 8 * sh);
         }
@@ -396,8 +401,10 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
     const int s = lane & 15, g = warp * 2 + (lane >> 4);
     MeLane L;
     L.sx = s & 3; L.sy = s >> 2;
-    L.b0 = s & 1; L.b1 = (s >> 1) & 1; L.b2 = (s >> 2) & 1; L.b3 = (s >> 3) & 1;
-    L.nb0 = 1 - L.b0; L.nb1 = 1 - L.b1; L.nb2 = 1 - L.b2; L.nb3 = 1 - L.b3;
+    // multiplied by the run-time 1, the selectors stay opaque: d * b + x remains one IMAD
+    L.b0 = (s & 1) * P.one; L.b1 = ((s >> 1) & 1) * P.one; L.b2 = ((s >> 2) & 1) * P.one; L.b3 = ((s >> 3) & 1) * P.one;
+    L.nb0 = (1 - (s & 1)) * P.one; L.nb1 = (1 - ((s >> 1) & 1)) * P.one;
+    L.nb2 = (1 - ((s >> 2) & 1)) * P.one; L.nb3 = (1 - ((s >> 3) & 1)) * P.one;
     // block-validity limits at the right/bottom picture edge (max_mv = pic - 1 - pos)
     L.X0 = P.W - 1 - (cx + 16 * L.sx); L.X1 = L.X0 - 8;
     L.Xp = P.W - 1 - (cx + 16 * (L.sx & 2)); L.Xc = P.W - 1 - cx;
@@ -742,8 +749,8 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     // rows read: main items up to 48 + 8 (nfull - 1) + 22, tail items up to 48 + ndy - 1 + 15
     P.win_h = t.ndy + 63;
     P.win_cols = ((15 + 64 + t.ndx + 4 + 15) / 16) * 16;
-    P.win_ww = (P.win_cols >> 2) + 18 + 2;    // even, room for the largest skew
-    const size_t smem = (size_t)P.win_h * P.win_ww * 4;
+    if ((P.win_cols >> 2) + 18 + 2 > ME_WIN_WW) return set_status(UC_ERR_ARG, "me: window too wide");
+    const size_t smem = (size_t)P.win_h * ME_WIN_WW * 4;
     static bool attr_set[64];
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
         UC_CHECK(cudaFuncSetAttribute(k_me_int<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
