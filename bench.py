@@ -294,13 +294,30 @@ def run_ours(args):
     avg_int_ms = ms_int / max(1, args.steps)                   # both integer-search launches of a step
     alg_ops = N_REFS * W * H * n_cand / 4.0
     achieved = alg_ops / (avg_int_ms / 1000.0) / 1e9
+    # DRAM traffic of the two integer-search launches of one frame (interior 7.87 MB + edge
+    # 2.55 MB read, nothing written back), from the ncu capture summarised in
+    # profiles/me_kernels_1080p_full.md
+    traffic = 7.87e6 + 2.55e6
     roofline = {"bound": "int", "kernel": "k_me_int (integer full search, both launches of a frame)",
                 "achieved": achieved, "peak": int_peak, "unit": "Gop/s", "frac": achieved / int_peak,
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_note": "DRAM bytes per frame (both launches) from ncu; algorithmic ops, not bytes, bind",
                 "peak_source": f"vabsdiff4.add issue rate max(measured {per_clk_sm:.1f}, 64) ops/clk/SM x {sm_count} "
                                f"SMs x {sm_mhz:.0f} MHz max SM clock (MEASURED_PEAKS.json has no integer peak)",
                 "ops_per_launch": alg_ops, "avg_launch_ms": avg_int_ms,
                 "kernel_ms_per_step": {k: v[0] / max(1, args.steps) for k, v in prof.items()}}
+    # the HBM-side kernel of the frame: 15 quarter-sample planes of the newest reference written,
+    # its padded integer plane read (16 padded planes of stride x rows bytes)
+    stride = ((W + 2 * PAD) + 15) & ~15
+    sub_bytes = 16.0 * stride * (H + 2 * PAD)
+    sub_ms = prof["subpel_planes"][0] / max(1, args.steps)
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    roofline_hbm = {"bound": "hbm", "kernel": "k_subpel_planes (15 quarter-sample planes of one reference)",
+                    "achieved": sub_bytes / (sub_ms / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": sub_bytes / (sub_ms / 1000.0) / 1e9 / hbm_peak, "traffic": 2.26e6 + 0.20e6,
+                    "bytes_per_launch": sub_bytes,
+                    "peak_source": "hbm_gbs of MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+                    "traffic_note": "ncu DRAM bytes per launch: the written planes stay in the 129 MB L2"}
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -316,6 +333,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "gpu_launches_per_step": launches / args.steps,
         "roofline": roofline,
+        "roofline_hbm": roofline_hbm,
         "clocks": clk,
     }
     if not args.no_cpu:
