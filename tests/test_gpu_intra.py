@@ -45,3 +45,29 @@ def test_intra_lattice_edge_cases(gpu, oracle):
         satd_o, q_o = oracle_lattice(oracle, org, rec, cus, 1, [5], is_intra)
         assert np.array_equal(satd, satd_o)
         assert np.array_equal(q, q_o)
+
+
+def test_intra_lattice_unsorted_and_invalid_cus(gpu, oracle):
+    # CUs in random order with unsupported entries mixed in: outputs go by CU index, the
+    # unsupported ones (outside the picture, sides not a power of two) come back zeroed
+    W, H = 96, 64
+    org = intra_frame(W, H, seed=5)
+    rec = np.clip(org.astype(int) + np.random.default_rng(5).integers(-4, 5, org.shape), 0, 255).astype(np.uint8)
+    cus = gpu.lattice_cus(W, H)
+    rng = np.random.default_rng(7)
+    cus = cus[rng.permutation(len(cus))]
+    bad = np.zeros(3, dtype=cus.dtype)
+    bad[0] = (80, 48, 32, 32, 0)      # crosses the right and bottom edges
+    bad[1] = (0, 0, 12, 16, 0)        # width not a power of two
+    bad[2] = (0, 0, 128, 8, 0)        # side above 64
+    allc = np.concatenate([cus[:40], bad[:1], cus[40:90], bad[1:], cus[90:]])
+    qps = [22, 37]
+    satd, q = gpu.intra_lattice(org, rec, allc, qps, ipf=0)
+    valid = np.ones(len(allc), bool)
+    valid[[40, 91, 92]] = False
+    satd = satd.reshape(len(allc), 33)
+    q = q.reshape(len(allc), 33, len(qps))
+    assert not satd[~valid].any() and not q[~valid].view(np.uint8).any()
+    satd_o, q_o = oracle_lattice(oracle, org, rec, allc[valid], 0, qps)
+    assert np.array_equal(satd[valid].ravel(), satd_o)
+    assert np.array_equal(q[valid].ravel(), q_o)

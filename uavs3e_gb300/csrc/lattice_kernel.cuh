@@ -1,0 +1,546 @@
+// Device side of the batched intra lattice (one kernel instance per CU shape); the launcher,
+// the shape grouping and the C ABI are in lattice.cu, the instances in lattice_w*.cu.
+#pragma once
+#include "common.cuh"
+#include "intra.cuh"
+#include "tables.h"
+#include "uavs3e_cuda_internal.h"
+
+namespace uc {
+
+__device__ __constant__ static const u16 kQScale[80] = {
+    16302, 15024, 13777, 12634, 11626, 10624, 9742, 8958, 8192, 7512, 6889, 6305, 5793, 5303, 4878, 4467,
+    4091, 3756, 3444, 3161, 2894, 2654, 2435, 2235, 2048, 1878, 1722, 1579, 1449, 1329, 1218, 1117,
+    1024, 939, 861, 790, 724, 664, 609, 558, 512, 470, 430, 395, 362, 332, 304, 279,
+    256, 235, 215, 197, 181, 166, 152, 140, 128, 116, 108, 99, 91, 83, 76, 69,
+    64, 59, 54, 49, 45, 41, 38, 35, 32, 30, 27, 25, 23, 21, 19, 18,
+};
+__device__ __constant__ static const u32 kDqScale[80] = {
+    32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424, 32932, 35734, 38968, 42495, 46177, 50535, 55109, 59933,
+    65535, 35734, 38968, 42577, 46341, 50617, 55027, 60097, 32809, 35734, 38968, 42454, 46382, 50576, 55109, 60056,
+    65535, 35734, 38968, 42495, 46320, 50515, 55109, 60076, 65535, 35744, 38968, 42495, 46341, 50535, 55099, 60087,
+    65535, 35734, 38973, 42500, 46341, 50535, 55109, 60097, 32771, 35734, 38965, 42497, 46341, 50535, 55109, 60099,
+    32768, 36061, 38968, 42495, 46341, 50535, 55437, 60424, 32932, 35734, 38968, 42495, 46177, 50535, 55109, 59933,
+};
+__device__ __constant__ static const u8 kDqShift[80] = {
+    14, 14, 14, 14, 14, 14, 14, 14, 13, 13, 13, 13, 13, 13, 13, 13, 13, 12, 12, 12, 12, 12, 12, 12,
+    11, 11, 11, 11, 11, 11, 11, 11, 11, 10, 10, 10, 10, 10, 10, 10, 10, 9, 9, 9, 9, 9, 9, 9,
+    9, 8, 8, 8, 8, 8, 8, 8, 7, 7, 7, 7, 7, 7, 7, 7, 6, 6, 6, 6, 6, 6, 6, 6, 5, 5, 5, 5, 5, 5, 5, 5,
+};
+
+__device__ __forceinline__ u32 fmix32(u32 h)
+{
+    h ^= h >> 16; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16;
+    return h;
+}
+
+// sum of 4 (unsigned byte of a) x (signed byte of b) products + c
+__device__ __forceinline__ int dp4a_us(u32 a, u32 b, int c)
+{
+    int d;
+    asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+// sum of the 2 signed halfwords of a times signed bytes 0,1 (lo) or 2,3 (hi) of b, + c
+__device__ __forceinline__ int dp2a_lo(u32 a, u32 b, int c)
+{
+    int d;
+    asm("dp2a.lo.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+__device__ __forceinline__ int dp2a_hi(u32 a, u32 b, int c)
+{
+    int d;
+    asm("dp2a.hi.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+struct LatCu { s16 x, y; u8 w, h; u16 pad; };
+struct LatQ { u32 ssd; u32 coef_hash; u16 num_nz; s16 last_nz; u32 sum_abs; };
+
+constexpr int LAT_THREADS = 256;
+constexpr int LAT_BUDGET = 48 * 1024;   // dynamic shared bytes per CTA (4 CTAs per SM with the static part)
+constexpr int LAT_MAX_QP = 4;
+constexpr int LAT_MAX_G = 8;            // CUs per CTA
+constexpr int LAT_MAX_JOBS = 33 * LAT_MAX_G;
+constexpr int LAT_NB = 592;             // neighbour buffer per CU (INTRA_NEIB_SIZE + pad)
+constexpr int LAT_SHAPES = 25;          // log2 sides 2..6
+
+// shared-memory layout of one shape's CTAs (host and device compute it the same way)
+struct LatLayout {
+    int w, h, lw, lh, kw, kh, lkw, lkh;
+    int ps;            // prediction / org row stride (bytes): w + 4
+    int ts;            // forward row-pass output row stride (s16): h + 2
+    int ds;            // transposed dequantised row stride (s16): kh + 2
+    int fw_ws, fh_ws, fht_ws, fwt_ws;   // table row strides in words
+    int o_fw, o_fh, o_fht, o_fwt;       // table offsets
+    int o_cu, cu_bytes;                 // per-CU blocks: org, neighbours, org row-pass sums
+    int c_org, c_nb, c_torg;
+    int o_job, job_bytes;               // per-job blocks: prediction, T, C, DQ^T, T2
+    int j_pred, j_t, j_c, j_dqt, j_t2;
+    int G, MC, nchunk;                  // CUs per CTA, modes per CTA, mode chunks per CU
+    int smem;
+};
+
+__host__ __device__ __forceinline__ int lat_up16(int v) { return (v + 15) & ~15; }
+
+__host__ __device__ inline void lat_layout(int lw, int lh, LatLayout &L)
+{
+    L.lw = lw; L.lh = lh; L.w = 1 << lw; L.h = 1 << lh;
+    L.kw = L.w < 32 ? L.w : 32; L.kh = L.h < 32 ? L.h : 32;
+    L.lkw = lw < 5 ? lw : 5; L.lkh = lh < 5 ? lh : 5;
+    L.ps = L.w + 4; L.ts = L.h + 2; L.ds = L.kh + 2;
+    L.fw_ws = L.w / 4 + 1; L.fh_ws = L.h / 4 + 1; L.fht_ws = L.kh / 4 + 1; L.fwt_ws = L.kw / 4 + 1;
+    int o = 0;
+    L.o_fw = o; o += lat_up16(L.kw * L.fw_ws * 4);
+    L.o_fh = o; o += lat_up16(L.kh * L.fh_ws * 4);
+    L.o_fht = o; o += lat_up16(L.h * L.fht_ws * 4);
+    L.o_fwt = o; o += lat_up16(L.w * L.fwt_ws * 4);
+    int c = 0;
+    L.c_org = c; c += lat_up16(L.h * L.ps);
+    L.c_nb = c; c += lat_up16(LAT_NB);
+    L.c_torg = c; c += lat_up16(L.kw * L.h * 4);
+    L.cu_bytes = c;
+    int j = 0;
+    L.j_pred = j; j += lat_up16(L.h * L.ps);
+    L.j_t = j; j += lat_up16(L.kw * L.ts * 2);
+    L.j_c = j; j += lat_up16(L.kh * L.kw * 2);
+    L.j_dqt = j; j += lat_up16(L.kw * L.ds * 2);
+    L.j_t2 = j; j += lat_up16(L.h * L.kw * 2);
+    L.job_bytes = j;
+    const int avail = LAT_BUDGET - o;
+    // several whole CUs when 33 jobs of the shape fit, else one CU and a chunk of its modes
+    int G = avail / (33 * L.job_bytes + L.cu_bytes);
+    if (G >= 1) {
+        L.G = G < LAT_MAX_G ? G : LAT_MAX_G;
+        L.MC = 33; L.nchunk = 1;
+    } else {
+        int J = (avail - L.cu_bytes) / L.job_bytes;
+        J = J < 1 ? 1 : J;
+        L.G = 1;
+        L.nchunk = (33 + J - 1) / J;
+        L.MC = (33 + L.nchunk - 1) / L.nchunk;
+    }
+    L.o_cu = o; o += L.G * L.cu_bytes;
+    L.o_job = o; o += L.G * L.MC * L.job_bytes;
+    L.smem = o;
+}
+
+struct LatParams {
+    const pel *org; int i_org;
+    const pel *rec; int i_rec;
+    int W, H;
+    const LatCu *cus;
+    const int *perm;          // CU indices of this shape
+    int n_shape;              // CUs of this shape
+    int ipf, n_qp, is_intra;
+    int qp[LAT_MAX_QP];
+    u32 *satd_out; LatQ *q_out;
+    const s8 *fold_w, *fold_h;
+    const u16 *scanpos;
+    double sq32, sq128;
+};
+
+// lanes [k*seg, (k+1)*seg) of a warp hold one job's elements (seg = 16 or 32): the sum, max
+// or or over the lane's segment, with the warp-wide reduction instructions
+__device__ __forceinline__ u32 seg_sum(u32 v, int seg, int lane)
+{
+    if (seg == 32) return __reduce_add_sync(0xFFFFFFFFu, v);
+    const u32 lo = __reduce_add_sync(0xFFFFFFFFu, lane < 16 ? v : 0u);
+    const u32 hi = __reduce_add_sync(0xFFFFFFFFu, lane < 16 ? 0u : v);
+    return lane < 16 ? lo : hi;
+}
+__device__ __forceinline__ int seg_max(int v, int seg, int lane)
+{
+    if (seg == 32) return __reduce_max_sync(0xFFFFFFFFu, v);
+    const int lo = __reduce_max_sync(0xFFFFFFFFu, lane < 16 ? v : -1);
+    const int hi = __reduce_max_sync(0xFFFFFFFFu, lane < 16 ? -1 : v);
+    return lane < 16 ? lo : hi;
+}
+__device__ __forceinline__ u32 seg_or(u32 v, int seg, int lane)
+{
+    if (seg == 32) return __reduce_or_sync(0xFFFFFFFFu, v);
+    const u32 lo = __reduce_or_sync(0xFFFFFFFFu, lane < 16 ? v : 0u);
+    const u32 hi = __reduce_or_sync(0xFFFFFFFFu, lane < 16 ? 0u : v);
+    return lane < 16 ? lo : hi;
+}
+
+// com_had tile of a (2^LW) x (2^LH) block (src/com_cost.c:712-812), as constants
+constexpr int lat_tw(int w, int h)
+{
+    return w == h ? (w == 4 ? 4 : 8) : w > h ? (h == 4 ? 8 : 16) : (w == 4 ? 4 : 8);
+}
+constexpr int lat_th(int w, int h)
+{
+    return w == h ? (w == 4 ? 4 : 8) : w > h ? (h == 4 ? 4 : 8) : (w == 4 ? 8 : 16);
+}
+
+// SATD of every (job, tile) by groups of R lanes (R = 4 or 8, the transform size): lane k of a
+// group holds row k of the tile's difference (of both halves for the 16x8 / 8x16 / 8x4 / 4x8
+// tiles, which combine two R x R transforms), transforms it in registers, and the column
+// transform runs across the group's lanes with shuffles.  Same coefficients, sums and
+// normalisation as satd_tile.
+template <int TW, int TH>
+__device__ __forceinline__ void lat_satd_tiles(int n_tiles, int lnt, int ntx, const u8 *cub, int cu_bytes, int c_org,
+                                               const u8 *jobb, int job_bytes, int j_pred, int ps, int MCv,
+                                               u32 *s_satd, double sq32, double sq128)
+{
+    constexpr int R = (TW == 4 || TH == 4) ? 4 : 8;
+    constexpr bool PAIR = TW != TH, SIDE = TW > TH;
+    constexpr int GPW = 32 / R;                       // groups per warp
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k = lane % R, grp = lane / R;
+    for (int base = warp * GPW; base < n_tiles; base += (LAT_THREADS / 32) * GPW) {
+        const int ti = base + grp;
+        const bool act = ti < n_tiles;
+        const int tt = act ? ti : base;
+        const int j = tt >> lnt, t = tt & ((1 << lnt) - 1);
+        const int ox = (t % ntx) * TW, oy = (t / ntx) * TH;
+        const u8 *o = cub + (j / MCv) * cu_bytes + c_org + (oy + k) * ps + ox;
+        const u8 *p = jobb + j * job_bytes + j_pred + (oy + k) * ps + ox;
+        int a[R], b[R];
+#pragma unroll
+        for (int c = 0; c < R; c++) a[c] = (int)o[c] - (int)p[c];
+        if (PAIR) {
+            const int bo = SIDE ? R : R * ps;
+#pragma unroll
+            for (int c = 0; c < R; c++) b[c] = (int)o[bo + c] - (int)p[bo + c];
+        }
+        wht<R>(a);
+        if (PAIR) wht<R>(b);
+#pragma unroll
+        for (int d = 1; d < R; d <<= 1) {
+#pragma unroll
+            for (int c = 0; c < R; c++) {
+                const int x = __shfl_xor_sync(0xFFFFFFFFu, a[c], d);
+                a[c] = (k & d) ? x - a[c] : a[c] + x;
+                if (PAIR) {
+                    const int y = __shfl_xor_sync(0xFFFFFFFFu, b[c], d);
+                    b[c] = (k & d) ? y - b[c] : b[c] + y;
+                }
+            }
+        }
+        int sum = 0;
+#pragma unroll
+        for (int c = 0; c < R; c++) sum += PAIR ? 2 * max(abs(a[c]), abs(b[c])) : abs(a[c]);
+#pragma unroll
+        for (int d = 1; d < R; d <<= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, d);
+        if (act && k == 0) {
+            u32 v;
+            if (!PAIR) v = R == 8 ? (u32)((sum + 2) >> 2) : (u32)((sum + 1) >> 1);
+            else v = (u32)(int)((double)sum / (R == 8 ? sq128 : sq32) * 2.0);
+            atomicAdd(&s_satd[j], v);
+        }
+    }
+}
+
+template <int LW, int LH>
+__global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
+{
+    extern __shared__ __align__(16) u8 sm[];
+    __shared__ IpredBlock sB[LAT_MAX_G];
+    __shared__ int s_cu[LAT_MAX_G];
+    __shared__ u32 s_satd[LAT_MAX_JOBS], s_flag[LAT_MAX_JOBS];
+    __shared__ u32 s_nz[LAT_MAX_JOBS], s_sum[LAT_MAX_JOBS], s_hash[LAT_MAX_JOBS], s_ssd[LAT_MAX_JOBS];
+    __shared__ int s_last[LAT_MAX_JOBS];
+
+    LatLayout L;
+    lat_layout(LW, LH, L);      // compile-time shape: every index and trip count below is a constant
+    const int w = L.w, h = L.h, lw = L.lw, lh = L.lh, kw = L.kw, kh = L.kh, lkw = L.lkw, lkh = L.lkh;
+    const int N = w * h, lN = lw + lh;
+    const int tid = threadIdx.x, lane = tid & 31, wbase = tid & ~31;
+
+    // this CTA's CUs and modes
+    const int grp = blockIdx.x / L.nchunk, chunk = blockIdx.x % L.nchunk;
+    const int cu0 = grp * L.G;
+    const int Gv = min(L.G, P.n_shape - cu0);
+    const int m0 = chunk * L.MC;
+    const int MCv = min(L.MC, 33 - m0);
+    const int J = Gv * MCv;
+    if (Gv <= 0 || MCv <= 0) return;
+
+    u32 *fw = (u32 *)(sm + L.o_fw), *fh = (u32 *)(sm + L.o_fh);
+    u32 *fht = (u32 *)(sm + L.o_fht), *fwt = (u32 *)(sm + L.o_fwt);
+    u8 *cub = sm + L.o_cu, *jobb = sm + L.o_job;
+
+    // ---- matrices: rows packed 4 bytes to a word
+    for (int i = tid; i < kw * w; i += LAT_THREADS) {
+        const int u = i >> lw, x = i & (w - 1);
+        const u8 v = (u8)P.fold_w[u * w + x];
+        ((u8 *)fw)[u * L.fw_ws * 4 + x] = v;        // Fw[u][x]
+        ((u8 *)fwt)[x * L.fwt_ws * 4 + u] = v;      // Fw^T[x][u]
+    }
+    for (int i = tid; i < kh * h; i += LAT_THREADS) {
+        const int v = i >> lh, y = i & (h - 1);
+        const u8 c = (u8)P.fold_h[v * h + y];
+        ((u8 *)fh)[v * L.fh_ws * 4 + y] = c;        // Fh[v][y]
+        ((u8 *)fht)[y * L.fht_ws * 4 + v] = c;      // Fh^T[y][v]
+    }
+    if (tid < Gv) s_cu[tid] = P.perm[cu0 + tid];
+    for (int j = tid; j < J; j += LAT_THREADS) {
+        s_satd[j] = 0; s_flag[j] = 0; s_nz[j] = 0; s_sum[j] = 0; s_hash[j] = 0; s_ssd[j] = 0; s_last[j] = -1;
+    }
+    __syncthreads();
+
+    // ---- per CU: org block, neighbours (com_intra_get_nbr with every in-picture sample
+    // reconstructed)
+    for (int i = tid; i < Gv * N; i += LAT_THREADS) {
+        const int g = i >> lN, p = i & (N - 1);
+        const LatCu cu = P.cus[s_cu[g]];
+        (cub + g * L.cu_bytes + L.c_org)[(p >> lw) * L.ps + (p & (w - 1))] =
+            P.org[(long long)(cu.y + (p >> lw)) * P.i_org + cu.x + (p & (w - 1))];
+    }
+    const int range = max(w, h) * 4 + 4;
+    for (int i = tid; i < Gv * range; i += LAT_THREADS) {
+        const int g = i / range, k = i - g * range;
+        const LatCu cu = P.cus[s_cu[g]];
+        const int x = cu.x, y = cu.y;
+        const int avail = (y > 0 ? 1 : 0) | (x > 0 ? 2 : 0);
+        const int up_cnt = (y > 0) ? min(w >> 2, max(0, (P.W - (x + w)) >> 2)) : 0;
+        const int le_cnt = (x > 0) ? min(h >> 2, max(0, (P.H - (y + h)) >> 2)) : 0;
+        pel *nbm = cub + g * L.cu_bytes + L.c_nb + 288;
+        nbm[1 + k] = (avail & 1) ? P.rec[(long long)(y - 1) * P.i_rec + x + min(k, w + 4 * up_cnt - 1)] : (pel)128;
+        nbm[-1 - k] = (avail & 2) ? P.rec[(long long)(y + min(k, h + 4 * le_cnt - 1)) * P.i_rec + x - 1] : (pel)128;
+        if (k == 0) {
+            pel c;
+            if (x > 0 && y > 0) c = P.rec[(long long)(y - 1) * P.i_rec + x - 1];
+            else if (y > 0) c = P.rec[(long long)(y - 1) * P.i_rec + x];
+            else if (x > 0) c = P.rec[(long long)y * P.i_rec + x - 1];
+            else c = 128;
+            nbm[0] = c;
+        }
+    }
+    __syncthreads();
+    if (tid < Gv) {
+        const LatCu cu = P.cus[s_cu[tid]];
+        const int avail = (cu.y > 0 ? 1 : 0) | (cu.x > 0 ? 2 : 0) | ((cu.x > 0 && cu.y > 0) ? 4 : 0);
+        ipred_block_setup(cub + tid * L.cu_bytes + L.c_nb + 288, w, h, avail, 8, sB[tid]);
+    }
+    // org part of the forward row pass: Torg[u][y] = sum_x Fw[u][x] org[y][x]
+    for (int i = tid; i < Gv * kw * h; i += LAT_THREADS) {
+        const int u = i & (kw - 1), y = (i >> lkw) & (h - 1), g = i >> (lkw + lh);
+        const u8 *c = cub + g * L.cu_bytes;
+        const u32 *o = (const u32 *)(c + L.c_org + y * L.ps), *f = fw + u * L.fw_ws;
+        int acc = 0;
+        #pragma unroll
+        for (int k = 0; k < (w >> 2); k++) acc = dp4a_us(o[k], f[k], acc);
+        ((int *)(c + L.c_torg))[u * h + y] = acc;
+    }
+    __syncthreads();
+
+    // job j -> (CU g, mode m): j = g * MCv + (m - m0)
+#define JG(j) ((j) / MCv)
+#define JPRED(j) (jobb + (j) * L.job_bytes + L.j_pred)
+#define JT(j) ((s16 *)(jobb + (j) * L.job_bytes + L.j_t))
+#define JC(j) ((s16 *)(jobb + (j) * L.job_bytes + L.j_c))
+#define JDQT(j) ((s16 *)(jobb + (j) * L.job_bytes + L.j_dqt))
+#define JT2(j) ((s16 *)(jobb + (j) * L.job_bytes + L.j_t2))
+#define CORG(g) (cub + (g) * L.cu_bytes + L.c_org)
+
+    // ---- prediction
+    for (int i = tid; i < (J << lN); i += LAT_THREADS) {
+        const int j = i >> lN, p = i & (N - 1);
+        const int g = JG(j), m = m0 + (j - g * MCv);
+        const int x = p & (w - 1), y = p >> lw;
+        JPRED(j)[y * L.ps + x] = (pel)ipred_sample(cub + g * L.cu_bytes + L.c_nb + 288, sB[g], m, P.ipf, x, y);
+    }
+    __syncthreads();
+
+    // ---- SATD (com_had tiling) and forward row pass T[u][y] = (Torg - sum_x Fw pred + rnd) >> sh1
+    {
+        constexpr int TW = lat_tw(1 << LW, 1 << LH), TH = lat_th(1 << LW, 1 << LH);
+        constexpr int lnt = LW + LH - (TW == 16 ? 4 : TW == 8 ? 3 : 2) - (TH == 16 ? 4 : TH == 8 ? 3 : 2);
+        lat_satd_tiles<TW, TH>(J << lnt, lnt, (1 << LW) / TW, cub, L.cu_bytes, L.c_org, jobb, L.job_bytes, L.j_pred, L.ps,
+                               MCv, s_satd, P.sq32, P.sq128);
+    }
+    {
+        const int sh1 = lw - 2, rnd1 = sh1 > 0 ? 1 << (sh1 - 1) : 0;
+        for (int i = tid; i < J * kw * h; i += LAT_THREADS) {
+            const int u = i & (kw - 1), y = (i >> lkw) & (h - 1), j = i >> (lkw + lh);
+            const int g = JG(j);
+            const u32 *pr = (const u32 *)(JPRED(j) + y * L.ps), *f = fw + u * L.fw_ws;
+            int s = 0;
+            #pragma unroll
+            for (int k = 0; k < (w >> 2); k++) s = dp4a_us(pr[k], f[k], s);
+            const int acc = ((const int *)(cub + g * L.cu_bytes + L.c_torg))[u * h + y] - s;
+            JT(j)[u * L.ts + y] = (s16)((acc + rnd1) >> sh1);
+        }
+    }
+    __syncthreads();
+
+    // quantisation parameters per QP
+    const int odd = lN & 1, log2_size = lN >> 1;
+    const int q_bits = 14 + (15 - 8 - log2_size);
+    const int offset = (P.is_intra ? 201 : 153) << (q_bits - 9);
+    const u32 qadd = 1u << (q_bits - 1);
+
+    // ---- forward column pass C[v][u] = (sum_y Fh[v][y] T[u][y] + rnd2) >> sh2, and the
+    // quant_check flags of every QP (bit q: some |C| above that QP's all-zero threshold)
+    {
+        int nz_thr[LAT_MAX_QP];
+#pragma unroll
+        for (int q = 0; q < LAT_MAX_QP; q++) {
+            const int qp = P.qp[q];
+            const int q_value = ((int)kQScale[qp] * (odd ? 181 : 1) + (odd ? 64 : 0)) >> (odd ? 7 : 0);
+            nz_thr[q] = ((((1 << q_bits) - offset) << 10) / q_value - 1) >> 10;
+        }
+        const int sh2 = lh + 5, rnd2 = 1 << (sh2 - 1);
+        const int E = kw * kh, lE = lkw + lkh, seg = E < 32 ? E : 32;
+        for (int base = wbase; base < (J << lE); base += LAT_THREADS) {
+            const int i = base + lane;
+            const bool act = i < (J << lE);
+            const int ii = act ? i : base;
+            const int u = ii & (kw - 1), v = (ii >> lkw) & (kh - 1), j = ii >> lE;
+            const u32 *t = (const u32 *)(JT(j) + u * L.ts), *f = fh + v * L.fh_ws;
+            int acc = 0;
+            #pragma unroll
+            for (int k = 0; k < (h >> 2); k++) {
+                const u32 fwd = f[k];
+                acc = dp2a_lo(t[2 * k], fwd, acc);
+                acc = dp2a_hi(t[2 * k + 1], fwd, acc);
+            }
+            const int c = (acc + rnd2) >> sh2;
+            u32 fl = 0;
+            if (act) {
+                JC(j)[v * kw + u] = (s16)c;
+                const int a = c < 0 ? -(int)(s16)c : (int)(s16)c;
+#pragma unroll
+                for (int q = 0; q < LAT_MAX_QP; q++)
+                    if (q < P.n_qp && a > nz_thr[q]) fl |= 1u << q;
+            }
+            fl = seg_or(fl, seg, lane);
+            if (act && (lane & (seg - 1)) == 0 && fl) atomicOr(&s_flag[j], fl);
+        }
+    }
+    __syncthreads();
+    for (int j = tid; j < J; j += LAT_THREADS)
+        P.satd_out[(size_t)s_cu[JG(j)] * 33 + m0 + (j - JG(j) * MCv)] = s_satd[j];
+
+    const u16 *scanpos = P.scanpos;
+    for (int q = 0; q < P.n_qp; q++) {
+        const int qp = P.qp[q];
+        const int q_value = ((int)kQScale[qp] * (odd ? 181 : 1) + (odd ? 64 : 0)) >> (odd ? 7 : 0);
+        const int thr = ((1 << (q_bits - 1)) - 1) / q_value + 1;
+        const int dq_scale = (int)kDqScale[qp];
+        const int dq_shift = (int)kDqShift[qp] - (15 - 8 - log2_size) + 1;
+        const int dq_off = dq_shift == 0 ? 0 : 1 << (dq_shift - 1);
+        // first-pass levels, statistics, dequantisation (stored transposed, DQ^T[u][v])
+        {
+            const int E = kw * kh, lE = lkw + lkh, seg = E < 32 ? E : 32;
+            for (int base = wbase; base < (J << lE); base += LAT_THREADS) {
+                const int i = base + lane;
+                const bool act = i < (J << lE);
+                const int ii = act ? i : base;
+                const int r = ii & (E - 1), j = ii >> lE;
+                const int u = r & (kw - 1), v = r >> lkw;
+                int lev = 0;
+                if (act && (s_flag[j] >> q & 1)) {
+                    const int c = JC(j)[r];
+                    const int a = c < 0 ? -c : c;
+                    if (a >= thr) {
+                        const u32 ld = (u32)a * (u32)q_value;
+                        const int l = (int)(s16)(u32)(((u64)ld + qadd) >> q_bits);
+                        lev = c < 0 ? -l : l;
+                    }
+                }
+                int dq = 0;
+                u32 nz = 0, sa = 0, hs = 0;
+                int last = -1;
+                if (lev) {
+                    const int pos = v * w + u;
+                    nz = 1;
+                    sa = (u32)(lev < 0 ? -lev : lev);
+                    hs = fmix32(((u32)pos << 16) | (u16)(s16)lev);
+                    last = (int)scanpos[pos];
+                    int d = (lev * dq_scale + dq_off) >> dq_shift;
+                    d = min(32767, max(-32768, d));
+                    dq = odd ? (d * 181 + 128) >> 8 : d;
+                }
+                if (act) JDQT(j)[u * L.ds + v] = (s16)dq;
+                nz = seg_sum(nz, seg, lane);
+                if (__any_sync(0xFFFFFFFFu, nz != 0)) {
+                    sa = seg_sum(sa, seg, lane);
+                    hs = seg_sum(hs, seg, lane);
+                    last = seg_max(last, seg, lane);
+                    if (act && (lane & (seg - 1)) == 0 && nz) {
+                        atomicAdd(&s_nz[j], nz);
+                        atomicAdd(&s_sum[j], sa);
+                        atomicAdd(&s_hash[j], hs);
+                        atomicMax(&s_last[j], last);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // inverse column pass T2[y][u] = clip16((sum_v Fh[v][y] DQ[v][u] + 16) >> 5), only
+        // for jobs with coded levels
+        for (int i = tid; i < J * h * kw; i += LAT_THREADS) {
+            const int u = i & (kw - 1), y = (i >> lkw) & (h - 1), j = i >> (lkw + lh);
+            if (!s_nz[j]) continue;
+            const u32 *d = (const u32 *)(JDQT(j) + u * L.ds), *f = fht + y * L.fht_ws;
+            int acc = 0;
+            #pragma unroll
+            for (int k = 0; k < (kh >> 2); k++) {
+                const u32 fwd = f[k];
+                acc = dp2a_lo(d[2 * k], fwd, acc);
+                acc = dp2a_hi(d[2 * k + 1], fwd, acc);
+            }
+            JT2(j)[y * kw + u] = (s16)min(32767, max(-32768, (acc + 16) >> 5));
+        }
+        __syncthreads();
+        // inverse row pass, reconstruction, SSD
+        {
+            const int seg = N < 32 ? N : 32;
+            for (int base = wbase; base < (J << lN); base += LAT_THREADS) {
+                const int i = base + lane;
+                const bool act = i < (J << lN);
+                const int ii = act ? i : base;
+                const int p = ii & (N - 1), j = ii >> lN;
+                const int x = p & (w - 1), y = p >> lw;
+                int rv = JPRED(j)[y * L.ps + x];
+                if (s_nz[j]) {
+                    const u32 *t = (const u32 *)(JT2(j) + y * kw), *f = fwt + x * L.fwt_ws;
+                    int acc = 0;
+                    #pragma unroll
+                    for (int k = 0; k < (kw >> 2); k++) {
+                        const u32 fwd = f[k];
+                        acc = dp2a_lo(t[2 * k], fwd, acc);
+                        acc = dp2a_hi(t[2 * k + 1], fwd, acc);
+                    }
+                    const int r = min(255, max(-256, (acc + 2048) >> 12));
+                    rv = min(255, max(0, rv + r));
+                }
+                const int d = (int)CORG(JG(j))[y * L.ps + x] - rv;
+                u32 e = act ? (u32)(d * d) : 0u;
+                e = seg_sum(e, seg, lane);
+                if (act && (lane & (seg - 1)) == 0) atomicAdd(&s_ssd[j], e);
+            }
+        }
+        __syncthreads();
+        for (int j = tid; j < J; j += LAT_THREADS) {
+            const int g = JG(j);
+            LatQ o;
+            o.ssd = s_ssd[j];
+            o.coef_hash = s_hash[j];
+            o.num_nz = (u16)s_nz[j];
+            o.last_nz = (s16)s_last[j];
+            o.sum_abs = s_sum[j];
+            P.q_out[((size_t)s_cu[g] * 33 + m0 + (j - g * MCv)) * P.n_qp + q] = o;
+            s_ssd[j] = 0; s_hash[j] = 0; s_nz[j] = 0; s_last[j] = -1; s_sum[j] = 0;
+        }
+        __syncthreads();
+    }
+#undef JG
+#undef JPRED
+#undef JT
+#undef JC
+#undef JDQT
+#undef JT2
+#undef CORG
+}
+
+// launches the instance for (2^LW) x (2^lh) CUs (lattice_w*.cu)
+template <int LW>
+int lat_launch_w(int lh, unsigned grid, int smem, cudaStream_t st, const LatParams &P);
+
+}  // namespace uc

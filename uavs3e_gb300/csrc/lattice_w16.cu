@@ -1,0 +1,31 @@
+// Intra lattice kernel instances for CUs 16 samples wide (heights 4..64).
+#include "lattice_kernel.cuh"
+
+namespace uc {
+
+template <>
+int lat_launch_w<4>(int lh, unsigned grid, int smem, cudaStream_t st, const LatParams &P)
+{
+    static bool attr[64][7];
+    int dev = 0;
+    UC_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "intra_lattice: device index");
+    void (*k)(LatParams) = nullptr;
+    switch (lh) {
+    case 2: k = k_intra_lattice<4, 2>; break;
+    case 3: k = k_intra_lattice<4, 3>; break;
+    case 4: k = k_intra_lattice<4, 4>; break;
+    case 5: k = k_intra_lattice<4, 5>; break;
+    case 6: k = k_intra_lattice<4, 6>; break;
+    default: return set_status(UC_ERR_ARG, "intra_lattice: CU height");
+    }
+    if (!attr[dev][lh]) {
+        UC_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr[dev][lh] = true;
+    }
+    k<<<grid, LAT_THREADS, smem, st>>>(P);
+    UC_CHECK(cudaGetLastError());
+    return UC_OK;
+}
+
+}  // namespace uc
