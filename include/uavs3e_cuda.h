@@ -166,7 +166,7 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *me, const uint8_t 
 #define UAVS3E_CUDA_NOALLOC_MAX_CTUS      510
 #define UAVS3E_CUDA_NOALLOC_MAX_REFS      2
 #define UAVS3E_CUDA_NOALLOC_MAX_RANGE     64
-#define UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES 13454336u
+#define UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES 14143744u
 UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_org, int i_org, const uint8_t *const *d_planes,
                                                   int i_ref, int pad, int width, int height, int n_refs, int range,
                                                   uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);

@@ -57,7 +57,7 @@ u32 me_mvbits(int v) { return mvbits(v); }
 size_t me_sub_scratch_bytes(int W, int H, int n_refs)
 {
     size_t nctu = (size_t)((W + 63) / 64) * ((H + 63) / 64);
-    return nctu * n_refs * ME_BLOCKS_PER_CTU * 17 * sizeof(u32);
+    return nctu * n_refs * ME_BLOCKS_PER_CTU * 18 * sizeof(u32);
 }
 
 size_t me_key_scratch_bytes(int W, int H, int n_refs)
@@ -503,8 +503,9 @@ struct MeSubParams {
     const u64 *keys;
     u32 *satd1;          // [item][9]
     u32 *satd2;          // [item][8]
+    u32 *hpel;           // [item]: stage-1 winner (mx, my)
+    int cls_base[4], cls_nx[3];   // refinement items per tile class (per reference), tiles per row
     MeResult *out;
-    long long task_base[11];   // prefix of tasks per shape class
 };
 
 __constant__ s8 kHalfPat[8][2] = { { -2, 0 }, { -2, 2 }, { 0, 2 }, { 2, 2 }, { 2, 0 }, { 2, -2 }, { 0, -2 }, { -2, -2 } };
@@ -534,6 +535,35 @@ __device__ __forceinline__ void load8(const pel *p, u32 &lo, u32 &hi)
     const u32 w2 = sh ? __ldg(q + 2) : 0u;
     lo = __funnelshift_r(w0, w1, sh);
     hi = __funnelshift_r(w1, w2, sh);
+}
+
+__device__ __forceinline__ void int_winner(const MeSubParams &P, int ctu, int b, int ref, int &dx, int &dy, u64 &key)
+{
+    key = P.keys[((size_t)ctu * P.n_refs + ref) * ME_BLOCKS_PER_CTU + b];
+    const u32 raster = (u32)(key & 0x7FFF);
+    dx = P.lo_x + (int)(raster % P.ndx);
+    dy = P.lo_y + (int)(raster / P.ndx);
+}
+
+__device__ __forceinline__ u64 sub_cost(const MeSubParams &P, int vx, int vy, u32 satd)
+{
+    return (u64)((mvbits(vx) + mvbits(vy)) * P.lambda_mv) + ((u64)satd << 16);
+}
+
+// stage-1 winner (centre first, then the half-sample pattern, strict '<')
+__device__ __forceinline__ void hpel_winner(const MeSubParams &P, int item, int cx, int cy, int &mx, int &my,
+                                            u64 &cbest, u32 &bsatd)
+{
+    const u32 *s1 = P.satd1 + (size_t)item * 9;
+    mx = cx; my = cy; bsatd = s1[0];
+    cbest = sub_cost(P, cx, cy, bsatd);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const int vx = cx + kHalfPat[c][0], vy = cy + kHalfPat[c][1];
+        const u32 sd = s1[c + 1];
+        const u64 cost = sub_cost(P, vx, vy, sd);
+        if (cost < cbest) { cbest = cost; mx = vx; my = vy; bsatd = sd; }
+    }
 }
 
 // magnitude sum of the 2-D WHT of the 8x8 difference org - pred; with o2/p2 the second 8x8
@@ -592,89 +622,119 @@ __device__ __forceinline__ u32 me_tile_satd(int tw, int th, const pel *o, int io
     return (u32)(int)((double)s / sq128 * 2.0);
 }
 
-struct SubTask { int item, ctu, b, ref, cand, tile, x, y, w, h, tw, th; };
+// Refinement work items: one per (reference, com_had tile position, tile class).  The tile
+// classes are 8x8 (tiles of the square blocks 8x8 .. 64x64), 16x8 (16x8, 32x16, 64x32) and 8x16
+// (8x16, 16x32, 32x64); a tile of a class lies in exactly one block of each of the class's
+// shapes (4 or 3 nested blocks).  A thread takes one (item, candidate): it forms the candidate's
+// prediction pointer for every nested block, evaluates the tile SATD once per distinct
+// pointer (nested blocks that share the integer or half-sample winner share the prediction)
+// and adds it to each block's sum for that candidate.
+__constant__ s8 kClassShapes[3][4] = { { 0, 3, 6, 9 }, { 1, 4, 7, -1 }, { 2, 5, 8, -1 } };
 
-__device__ __forceinline__ bool decode_task(const MeSubParams &P, long long t, int ncand, SubTask &k)
-{
-    int s = 0;
-    while (s < 9 && t >= P.task_base[s + 1]) s++;
-    long long l = t - P.task_base[s];
-    const int w = kShapeWH[s][0], h = kShapeWH[s][1];
-    int tw, th;
-    had_tile_shape(w, h, &tw, &th);
-    const int ntiles = (w * h) / (tw * th);
-    const int cnt = kShapeFirst[s + 1] - kShapeFirst[s];
-    k.tile = (int)(l % ntiles); l /= ntiles;
-    k.cand = (int)(l % ncand); l /= ncand;
-    k.ref = (int)(l % P.n_refs); l /= P.n_refs;
-    k.b = kShapeFirst[s] + (int)(l % cnt);
-    k.ctu = (int)(l / cnt);
-    k.item = (k.ctu * ME_BLOCKS_PER_CTU + k.b) * P.n_refs + k.ref;
-    const CtuBlock cb = kCtuBlocks[k.b];
-    k.x = (k.ctu % P.ctus_w) * ME_CTU + cb.x;
-    k.y = (k.ctu / P.ctus_w) * ME_CTU + cb.y;
-    k.w = w; k.h = h; k.tw = tw; k.th = th;
-    return k.x + w <= P.W && k.y + h <= P.H;
-}
+struct SubItem {
+    int ref, cls, px, py, tw, th, nb;
+    int bx[4], by[4], ctu[4], b[4], item[4];
+    bool ok[4];
+};
 
-__device__ __forceinline__ void int_winner(const MeSubParams &P, int ctu, int b, int ref, int &dx, int &dy, u64 &key)
+__device__ __forceinline__ void decode_sub_item(const MeSubParams &P, int it, SubItem &I)
 {
-    key = P.keys[((size_t)ctu * P.n_refs + ref) * ME_BLOCKS_PER_CTU + b];
-    const u32 raster = (u32)(key & 0x7FFF);
-    dx = P.lo_x + (int)(raster % P.ndx);
-    dy = P.lo_y + (int)(raster / P.ndx);
-}
-
-__device__ __forceinline__ u64 sub_cost(const MeSubParams &P, int vx, int vy, u32 satd)
-{
-    return (u64)((mvbits(vx) + mvbits(vy)) * P.lambda_mv) + ((u64)satd << 16);
-}
-
-// stage-1 winner (centre first, then the half-sample pattern, strict '<')
-__device__ __forceinline__ void hpel_winner(const MeSubParams &P, int item, int cx, int cy, int &mx, int &my,
-                                            u64 &cbest, u32 &bsatd)
-{
-    const u32 *s1 = P.satd1 + (size_t)item * 9;
-    mx = cx; my = cy; bsatd = s1[0];
-    cbest = sub_cost(P, cx, cy, bsatd);
+    I.ref = it % P.n_refs;
+    int rest = it / P.n_refs;
+    int c = 0;
+    while (c < 2 && rest >= P.cls_base[c + 1]) c++;
+    rest -= P.cls_base[c];
+    I.cls = c;
+    I.tw = c == 1 ? 16 : 8; I.th = c == 2 ? 16 : 8;
+    const int nx = P.cls_nx[c];
+    I.px = (rest % nx) * I.tw; I.py = (rest / nx) * I.th;
+    I.nb = c == 0 ? 4 : 3;
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-        const int vx = cx + kHalfPat[c][0], vy = cy + kHalfPat[c][1];
-        const u32 sd = s1[c + 1];
-        const u64 cost = sub_cost(P, vx, vy, sd);
-        if (cost < cbest) { cbest = cost; mx = vx; my = vy; bsatd = sd; }
+    for (int j = 0; j < 4; j++) {
+        I.ok[j] = false; I.item[j] = 0; I.bx[j] = 0; I.by[j] = 0; I.ctu[j] = 0; I.b[j] = 0;
+        if (j >= I.nb) continue;
+        const int sh = kClassShapes[c][j];
+        const int w = kShapeWH[sh][0], h = kShapeWH[sh][1];
+        const int bx = I.px & ~(w - 1), by = I.py & ~(h - 1);
+        const int ctu = (by >> 6) * P.ctus_w + (bx >> 6);
+        const int b = kShapeFirst[sh] + ((by & 63) / h) * (ME_CTU / w) + ((bx & 63) / w);
+        I.bx[j] = bx; I.by[j] = by; I.ctu[j] = ctu; I.b[j] = b;
+        I.item[j] = (ctu * ME_BLOCKS_PER_CTU + b) * P.n_refs + I.ref;
+        I.ok[j] = bx + w <= P.W && by + h <= P.H;
     }
 }
 
-template <int STAGE>
-__global__ void __launch_bounds__(256, 2) k_me_sub_eval(MeSubParams P, long long n_tasks)
+__device__ __forceinline__ u32 sub_tile_satd(const MeSubParams &P, const SubItem &I, const pel *pb)
 {
-    const int ncand = STAGE == 1 ? 9 : 8;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n_tasks;
-         t += (long long)gridDim.x * blockDim.x) {
-        SubTask k;
-        if (!decode_task(P, t, ncand, k)) continue;
+    const pel *ob = P.org + (long long)I.py * P.i_org + I.px;
+    if (I.cls == 0) return (u32)((satd8x8_raw(ob, P.i_org, pb, P.i_ref, nullptr, nullptr, 0) + 2) >> 2);
+    const int bo = I.cls == 1 ? 8 : 8 * P.i_org, bp = I.cls == 1 ? 8 : 8 * P.i_ref;
+    int s = satd8x8_raw(ob, P.i_org, pb, P.i_ref, ob + bo, pb + bp, 1);
+    s += satd8x8_raw(ob, P.i_org, pb, P.i_ref, ob + bo, pb + bp, -1);
+    return (u32)(int)((double)s / P.sq128 * 2.0);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256, 2) k_me_sub_eval(MeSubParams P, int n_threads)
+{
+    constexpr int NC = STAGE == 1 ? 9 : 8;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_threads; t += gridDim.x * blockDim.x) {
+        const int it = t / NC, c = t - it * NC;
+        SubItem I;
+        decode_sub_item(P, it, I);
+        const pel *ptr[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            ptr[j] = nullptr;
+            if (!I.ok[j]) continue;
+            const long long toff = (long long)(I.py - I.by[j]) * P.i_ref + (I.px - I.bx[j]);
+            if (STAGE == 1) {
+                int dx, dy;
+                u64 key;
+                int_winner(P, I.ctu[j], I.b[j], I.ref, dx, dy, key);
+                if (c == 0) ptr[j] = P.planes[I.ref][0] + (long long)(I.by[j] + dy) * P.i_ref + (I.bx[j] + dx) + toff;
+                else ptr[j] = mc_ptr(P, I.ref, I.bx[j], I.by[j], 4 * dx + kHalfPat[c - 1][0], 4 * dy + kHalfPat[c - 1][1]) + toff;
+            } else {
+                const u32 hp = P.hpel[I.item[j]];
+                const int mx = (int)(s16)(hp & 0xFFFF), my = (int)(s16)(hp >> 16);
+                ptr[j] = mc_ptr(P, I.ref, I.bx[j], I.by[j], mx + kQuarPat[c][0], my + kQuarPat[c][1]) + toff;
+            }
+        }
+        u32 val[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            val[j] = 0;
+            if (!I.ok[j]) continue;
+            int same = -1;
+#pragma unroll
+            for (int i = 0; i < j; i++)
+                if (same < 0 && I.ok[i] && ptr[i] == ptr[j]) same = i;
+            u32 v = 0;
+#pragma unroll
+            for (int i = 0; i < j; i++)
+                if (i == same) v = val[i];
+            if (same < 0) v = sub_tile_satd(P, I, ptr[j]);
+            val[j] = v;
+            atomicAdd((STAGE == 1 ? P.satd1 + (size_t)I.item[j] * 9 : P.satd2 + (size_t)I.item[j] * 8) + c, v);
+        }
+    }
+}
+
+// stage-1 winner of every (block, reference): (mx, my) packed as two s16
+__global__ void __launch_bounds__(256) k_me_sub_pick(MeSubParams P)
+{
+    const long long total = (long long)P.n_ctu * ME_BLOCKS_PER_CTU * P.n_refs;
+    for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < total;
+         item += (long long)gridDim.x * blockDim.x) {
+        const int ref = (int)(item % P.n_refs);
+        const int b = (int)((item / P.n_refs) % ME_BLOCKS_PER_CTU);
+        const int ctu = (int)(item / P.n_refs / ME_BLOCKS_PER_CTU);
         int dx, dy;
         u64 key;
-        int_winner(P, k.ctu, k.b, k.ref, dx, dy, key);
-        int cx = dx * 4, cy = dy * 4;
-        const pel *pb;
-        if (STAGE == 1) {
-            if (k.cand == 0) {
-                pb = P.planes[k.ref][0] + (long long)(k.y + dy) * P.i_ref + (k.x + dx);
-            } else {
-                pb = mc_ptr(P, k.ref, k.x, k.y, cx + kHalfPat[k.cand - 1][0], cy + kHalfPat[k.cand - 1][1]);
-            }
-        } else {
-            int mx, my; u64 cb; u32 bs;
-            hpel_winner(P, k.item, cx, cy, mx, my, cb, bs);
-            pb = mc_ptr(P, k.ref, k.x, k.y, mx + kQuarPat[k.cand][0], my + kQuarPat[k.cand][1]);
-        }
-        const int ntx = k.w / k.tw;
-        const int tx = (k.tile % ntx) * k.tw, ty = (k.tile / ntx) * k.th;
-        const pel *ob = P.org + (long long)(k.y + ty) * P.i_org + k.x + tx;
-        const u32 v = me_tile_satd(k.tw, k.th, ob, P.i_org, pb + (long long)ty * P.i_ref + tx, P.i_ref, P.sq128);
-        atomicAdd((STAGE == 1 ? P.satd1 + (size_t)k.item * 9 : P.satd2 + (size_t)k.item * 8) + k.cand, v);
+        int_winner(P, ctu, b, ref, dx, dy, key);
+        int mx, my; u64 cb; u32 bs;
+        hpel_winner(P, (int)item, dx * 4, dy * 4, mx, my, cb, bs);
+        P.hpel[item] = ((u32)(u16)(s16)my << 16) | (u16)(s16)mx;
     }
 }
 
@@ -792,29 +852,26 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     const long long items = (long long)S.n_ctu * ME_BLOCKS_PER_CTU * a.n_refs;
     S.satd1 = a.sub_scratch;
     S.satd2 = a.sub_scratch + items * 9;
-    CtuBlock tab[ME_BLOCKS_PER_CTU];
-    ctu_block_table(tab);
-    static const int first[11] = { 0, 64, 96, 128, 144, 152, 160, 164, 166, 168, 169 };
-    long long tb1[11], tb2[11];
-    tb1[0] = tb2[0] = 0;
-    for (int s = 0; s < 10; s++) {
-        int w = tab[first[s]].w, h = tab[first[s]].h, tw, th;
-        had_tile_shape(w, h, &tw, &th);
-        long long n = (long long)S.n_ctu * (first[s + 1] - first[s]) * a.n_refs * ((w * h) / (tw * th));
-        tb1[s + 1] = tb1[s] + n * 9;
-        tb2[s + 1] = tb2[s] + n * 8;
-    }
+    // refinement items: per reference, every tile position of the three tile classes
+    const int cnx[3] = { (a.W + 7) / 8, (a.W + 15) / 16, (a.W + 7) / 8 };
+    const int cny[3] = { (a.H + 7) / 8, (a.H + 7) / 8, (a.H + 15) / 16 };
+    S.cls_base[0] = 0;
+    for (int c = 0; c < 3; c++) { S.cls_nx[c] = cnx[c]; S.cls_base[c + 1] = S.cls_base[c] + cnx[c] * cny[c]; }
+    const long long n_items = (long long)S.cls_base[3] * a.n_refs;
+    if (n_items * 9 >= (1ll << 31)) return set_status(UC_ERR_ARG, "me: frame too large for the refinement grid");
+    S.hpel = a.sub_scratch + items * 17;
     UC_CHECK(cudaMemsetAsync(a.sub_scratch, 0, (size_t)items * 17 * sizeof(u32), st));
     prof_begin(PROF_ME_SUB, st);
-    for (int s = 0; s < 11; s++) S.task_base[s] = tb1[s];
-    k_me_sub_eval<1><<<(unsigned)std::min<long long>((tb1[10] + 255) / 256, 152 * 64), 256, 0, st>>>(S, tb1[10]);
+    const int n1 = (int)(n_items * 9), n2 = (int)(n_items * 8);
+    k_me_sub_eval<1><<<(unsigned)std::min<long long>((n1 + 255) / 256, 152 * 32), 256, 0, st>>>(S, n1);
     UC_CHECK(cudaGetLastError());
-    for (int s = 0; s < 11; s++) S.task_base[s] = tb2[s];
-    k_me_sub_eval<2><<<(unsigned)std::min<long long>((tb2[10] + 255) / 256, 152 * 64), 256, 0, st>>>(S, tb2[10]);
+    k_me_sub_pick<<<(unsigned)std::min<long long>((items + 255) / 256, 152 * 16), 256, 0, st>>>(S);
+    UC_CHECK(cudaGetLastError());
+    k_me_sub_eval<2><<<(unsigned)std::min<long long>((n2 + 255) / 256, 152 * 32), 256, 0, st>>>(S, n2);
     UC_CHECK(cudaGetLastError());
     k_me_sub_final<<<(unsigned)std::min<long long>((items + 255) / 256, 152 * 16), 256, 0, st>>>(S);
     UC_CHECK(cudaGetLastError());
-    count_launch(3);
+    count_launch(4);
     prof_end(PROF_ME_SUB, st);
     return UC_OK;
 }

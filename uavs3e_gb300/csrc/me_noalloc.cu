@@ -26,7 +26,7 @@ constexpr int NA_MAX_REFS = UAVS3E_CUDA_NOALLOC_MAX_REFS;
 constexpr int NA_MAX_RANGE = UAVS3E_CUDA_NOALLOC_MAX_RANGE;
 constexpr int NA_NDY = ME_NDY;
 constexpr size_t NA_KEYS = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * sizeof(u64);
-constexpr size_t NA_SUB = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * 17 * sizeof(u32);
+constexpr size_t NA_SUB = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * 18 * sizeof(u32);
 constexpr size_t NA_Q2_ENTRIES = me_q2_entries(NA_MAX_RANGE, NA_NDY);
 constexpr size_t NA_Q2 = NA_Q2_ENTRIES * sizeof(u32);
 constexpr size_t NA_R2M = (size_t)ME_R2M_ENTRIES * sizeof(u16);
