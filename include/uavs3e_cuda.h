@@ -65,6 +65,9 @@ UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
  * device: operations per second and per clock per SM.  The integer motion search's roofline
  * denominator (about 1.3 ms of GPU time). */
 UAVS3E_CUDA_API int uavs3e_cuda_measure_sad4_rate(double *ops_per_s, double *ops_per_clk_sm);
+/* The same for the 2-way halfword-by-byte dot product (dp2a), which carries the intra lattice's
+ * transforms (2 multiply-adds per instruction). */
+UAVS3E_CUDA_API int uavs3e_cuda_measure_dp2a_rate(double *ops_per_s, double *ops_per_clk_sm);
 
 /* Number of kernels this library has launched in this process. */
 UAVS3E_CUDA_API unsigned long long uavs3e_cuda_launch_count(void);

@@ -118,6 +118,13 @@ def measure_sad4_rate():
     return a.value, b.value
 
 
+def measure_dp2a_rate():
+    """(ops/s, ops per clock per SM) of dp2a (2 multiply-adds each) on the current device"""
+    a, b = C.c_double(), C.c_double()
+    check(lib().uavs3e_cuda_measure_dp2a_rate(C.byref(a), C.byref(b)), "measure_dp2a_rate")
+    return a.value, b.value
+
+
 def launch_count():
     return int(lib().uavs3e_cuda_launch_count())
 
