@@ -74,6 +74,7 @@ struct LatLayout {
     int ds;            // transposed dequantised row stride (s16): kh + 2
     int fw_ws, fh_ws, fht_ws, fwt_ws;   // table row strides in words
     int o_fw, o_fh, o_fht, o_fwt;       // table offsets
+    int o_scan;                         // scan index of each kept coefficient, [v][u] (u16)
     int o_cu, cu_bytes;                 // per-CU blocks: org, neighbours, org row-pass sums
     int c_org, c_nb, c_torg;
     int o_job, job_bytes;               // per-job blocks: prediction, T, C, DQ^T, T2
@@ -96,6 +97,7 @@ __host__ __device__ inline void lat_layout(int lw, int lh, LatLayout &L)
     L.o_fh = o; o += lat_up16(L.kh * L.fh_ws * 4);
     L.o_fht = o; o += lat_up16(L.h * L.fht_ws * 4);
     L.o_fwt = o; o += lat_up16(L.w * L.fwt_ws * 4);
+    L.o_scan = o; o += lat_up16(L.kw * L.kh * 2);
     int c = 0;
     L.c_org = c; c += lat_up16(L.h * L.ps);
     L.c_nb = c; c += lat_up16(LAT_NB);
@@ -276,6 +278,8 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
         ((u8 *)fh)[v * L.fh_ws * 4 + y] = c;        // Fh[v][y]
         ((u8 *)fht)[y * L.fht_ws * 4 + v] = c;      // Fh^T[y][v]
     }
+    u16 *s_scan = (u16 *)(sm + L.o_scan);
+    for (int i = tid; i < kw * kh; i += LAT_THREADS) s_scan[i] = P.scanpos[(i >> lkw) * w + (i & (kw - 1))];
     if (tid < Gv) s_cu[tid] = P.perm[cu0 + tid];
     for (int j = tid; j < J; j += LAT_THREADS) {
         s_satd[j] = 0; s_flag[j] = 0; s_nz[j] = 0; s_sum[j] = 0; s_hash[j] = 0; s_ssd[j] = 0; s_last[j] = -1;
@@ -416,15 +420,16 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     for (int j = tid; j < J; j += LAT_THREADS)
         P.satd_out[(size_t)s_cu[JG(j)] * 33 + m0 + (j - JG(j) * MCv)] = s_satd[j];
 
-    const u16 *scanpos = P.scanpos;
     for (int q = 0; q < P.n_qp; q++) {
         const int qp = P.qp[q];
-        const int q_value = ((int)kQScale[qp] * (odd ? 181 : 1) + (odd ? 64 : 0)) >> (odd ? 7 : 0);
-        const int thr = ((1 << (q_bits - 1)) - 1) / q_value + 1;
+        const u32 q_value = (u32)(((int)kQScale[qp] * (odd ? 181 : 1) + (odd ? 64 : 0)) >> (odd ? 7 : 0));
+        const int thr = ((1 << (q_bits - 1)) - 1) / (int)q_value + 1;
         const int dq_scale = (int)kDqScale[qp];
         const int dq_shift = (int)kDqShift[qp] - (15 - 8 - log2_size) + 1;
         const int dq_off = dq_shift == 0 ? 0 : 1 << (dq_shift - 1);
-        // first-pass levels, statistics, dequantisation (stored transposed, DQ^T[u][v])
+        // first-pass levels, statistics, dequantisation (stored transposed, DQ^T[u][v]).  The
+        // level (|c| q_value + 2^(q_bits-1)) >> q_bits is exact in 32 bits: |c| <= 2^15 and
+        // q_value < 2^15.
         {
             const int E = kw * kh, lE = lkw + lkh, seg = E < 32 ? E : 32;
             for (int base = wbase; base < (J << lE); base += LAT_THREADS) {
@@ -438,8 +443,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
                     const int c = JC(j)[r];
                     const int a = c < 0 ? -c : c;
                     if (a >= thr) {
-                        const u32 ld = (u32)a * (u32)q_value;
-                        const int l = (int)(s16)(u32)(((u64)ld + qadd) >> q_bits);
+                        const int l = (int)(s16)(((u32)a * q_value + qadd) >> q_bits);
                         lev = c < 0 ? -l : l;
                     }
                 }
@@ -451,7 +455,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
                     nz = 1;
                     sa = (u32)(lev < 0 ? -lev : lev);
                     hs = fmix32(((u32)pos << 16) | (u16)(s16)lev);
-                    last = (int)scanpos[pos];
+                    last = (int)s_scan[r];
                     int d = (lev * dq_scale + dq_off) >> dq_shift;
                     d = min(32767, max(-32768, d));
                     dq = odd ? (d * 181 + 128) >> 8 : d;
