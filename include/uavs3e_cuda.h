@@ -214,6 +214,37 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i
                                                      int ipf, const int *qps, int n_qp, int is_intra_slice,
                                                      uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Learned CU-partition / intra-mode pruning network (no counterpart in the reference: the
+ * learned part stands beside the bit-exact path and never changes it).  bf16 tensor-core
+ * implicit-GEMM convolutions with FP32 accumulation; all pointers are device memory.
+ * Activations NHWC bf16; weights [Cout][Kp] bf16 (k = (ky * ks + kx) * Cin + ci, Kp = ks*ks*Cin
+ * rounded up to 16); biases, gradients and Adam state FP32.  Shapes: Cin even, Cout a multiple
+ * of 8 (16 for wgrad), batch x output pixels a multiple of 16, ks 1 or 3 (padding ks/2). */
+
+/* y = act(conv(x, w) + bias): y bf16, or FP32 when y_f32; relu 0/1. */
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int y_f32,
+                                             int batch, int hin, int win, int cin, int cout, int ks, int stride,
+                                             int kp, int relu, void *stream);
+/* dx = (x > 0) * conv^T(dy, w): the gradient at the previous layer's pre-activation, bf16;
+ * wt_scratch holds cin * ks * ks * cout bf16. */
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_dgrad(const void *dy, const void *w, const void *x, void *dx, void *wt_scratch,
+                                               int batch, int hin, int win, int cin, int cout, int ks, int stride,
+                                               int kp, void *stream);
+/* dw = dy^T x_col [cout][kp], db = sum dy (both overwritten). */
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_wgrad(const void *dy, const void *x, float *dw, float *db, int batch, int hin,
+                                               int win, int cin, int cout, int ks, int stride, int kp, void *stream);
+/* Network input of n CTUs at (ctu_xy[2i], ctu_xy[2i+1]) of a picture: [n][64][64][2] bf16. */
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_input(const uint8_t *d_pic, int stride, int width, int height,
+                                          const int *d_ctu_xy, int n, int qp, void *x0, void *stream);
+/* Head losses (BCE on the split flags, cross-entropy on the modes) of [batch][16][48] logits
+ * against [batch][40] labels; dlogits bf16 scaled by 1/batch, loss[4] = per-part means. */
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_head_loss(const float *logits, const uint8_t *labels, int batch, void *dlogits,
+                                              float *loss, void *stream);
+/* One Adam step (step >= 1) on n FP32 weights; refreshes the bf16 copy when w_bf16 != NULL. */
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_adam(float *w, float *m, float *v, const float *g, void *w_bf16, int n, float lr,
+                                         float b1, float b2, float eps, int step, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

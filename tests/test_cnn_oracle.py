@@ -1,0 +1,83 @@
+"""CPU: the pruning network's numpy restatement (the GPU kernels' checker) and the plain-path
+decision labels."""
+import numpy as np
+
+import cnn_ref
+from uavs3e_gb300 import cnn
+
+
+def tiny_net(seed=0, B=2):
+    rng = np.random.default_rng(seed)
+    params = cnn.init_params(seed)
+    params = [(w.astype(np.float64), rng.normal(0, 0.1, b.shape)) for w, b in params]
+    x0 = rng.normal(0, 1, (B, 64, 64, 2))
+    labels = np.zeros((B, 40), np.uint8)
+    labels[:, :21] = rng.integers(0, 2, (B, 21))
+    labels[:, 21:37] = rng.integers(0, 33, (B, 16))
+    return params, x0, labels
+
+
+def total_loss(params, x0, labels):
+    acts, logits = cnn_ref.forward(x0, params, cnn.LAYERS, cnn.HEAD)
+    loss, _ = cnn_ref.head_loss(logits, labels)
+    return loss.sum()
+
+
+def test_backward_matches_finite_differences():
+    cnn_ref.EXACT = True
+    try:
+        params, x0, labels = tiny_net()
+        acts, logits = cnn_ref.forward(x0, params, cnn.LAYERS, cnn.HEAD)
+        _, grads = cnn_ref.backward(acts, logits, labels, params, cnn.LAYERS, cnn.HEAD)
+        rng = np.random.default_rng(3)
+        eps = 1e-5
+        for li in range(len(params)):
+            w, b = params[li]
+            K = cnn.LAYERS[li][2] ** 2 * cnn.LAYERS[li][0] if li < 4 else cnn.HEAD[0]
+            for _ in range(3):
+                o, k = rng.integers(0, w.shape[0]), rng.integers(0, K)
+                w[o, k] += eps
+                up = total_loss(params, x0, labels)
+                w[o, k] -= 2 * eps
+                dn = total_loss(params, x0, labels)
+                w[o, k] += eps
+                num = (up - dn) / (2 * eps)
+                assert abs(num - grads[li][0][o, k]) <= 1e-6 + 1e-4 * abs(num), (li, o, k, num, grads[li][0][o, k])
+            o = rng.integers(0, b.shape[0])
+            b[o] += eps
+            up = total_loss(params, x0, labels)
+            b[o] -= 2 * eps
+            dn = total_loss(params, x0, labels)
+            b[o] += eps
+            num = (up - dn) / (2 * eps)
+            assert abs(num - grads[li][1][o]) <= 1e-6 + 1e-4 * abs(num)
+    finally:
+        cnn_ref.EXACT = False
+
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.00390625, 1.005859375, 1.0078125, -3.14159, 0.0], np.float32)
+    r = cnn_ref.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125 and r[3] == 1.0078125
+    assert abs(r[4] + 3.140625) < 1e-7 and r[5] == 0.0
+
+
+def test_plain_decisions_quad_tree():
+    W, H = 128, 64
+    cus = cnn.square_cus(W, H)
+    J = np.full((len(cus), 33), 1e6)
+    # CTU 0: cheap 8x8 CUs everywhere (split to 8); CTU 1: cheap 64x64 with mode 7 (no split)
+    for i, c in enumerate(cus):
+        if c["x"] < 64:
+            if c["w"] == 8:
+                J[i, 3] = 10.0
+        else:
+            if c["w"] == 64:
+                J[i, 7] = 10.0
+            if c["w"] == 16:
+                J[i, 5] = 1e5
+    labels, xy = cnn.plain_decisions(J, cus, W, H)
+    assert xy.tolist() == [[0, 0], [64, 0]]
+    assert labels[0, 0] == 1 and labels[0, 1:5].all() and labels[0, 5:21].all()
+    assert labels[1, 0] == 0
+    assert (labels[1, 21:37] == 5).all()
