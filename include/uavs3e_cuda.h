@@ -213,6 +213,15 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i
                                                      int width, int height, const uavs3e_cuda_cu_t *d_cus, int n_cus,
                                                      int ipf, const int *qps, int n_qp, int is_intra_slice,
                                                      uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream);
+/* The same over a subset of modes: d_modes holds n_modes mode indices (0..32) per CU
+ * ([n_cus][n_modes], device); only those (CU, mode) records are written.  Used by the pruned
+ * search, which evaluates a shortlist of modes per CU. */
+UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_modes_device(const uint8_t *d_org, int i_org, const uint8_t *d_rec,
+                                                           int i_rec, int width, int height,
+                                                           const uavs3e_cuda_cu_t *d_cus, int n_cus,
+                                                           const uint8_t *d_modes, int n_modes, int ipf,
+                                                           const int *qps, int n_qp, int is_intra_slice,
+                                                           uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream);
 
 /* ---------------------------------------------------------------------------------------
  * Learned CU-partition / intra-mode pruning network (no counterpart in the reference: the

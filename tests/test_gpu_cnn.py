@@ -117,3 +117,17 @@ def test_training_learns_a_learnable_target(gpu):
     top8 = np.argsort(-logits[:, :, 3:36], axis=2)[:, :, :cnn.SHORTLIST]
     recall = (top8 == labels[:, 21:37, None]).any(2).mean()
     assert recall > 0.9
+
+
+def test_pruning_beats_the_method_without_the_network(gpu):
+    # trained on the plain path's decisions (lattice costs) of a few frames, evaluated on a
+    # held-out frame: better mode shortlist than the prior and a cheaper pruned search
+    from uavs3e_gb300 import cnn
+    r = cnn.experiment(train_seeds=range(200, 203), test_seeds=(950,), steps=500, batch=64, taus=(0.9,),
+                       width=640, height=384)
+    assert r["loss_last"] < 0.6 * r["loss_first"]
+    assert r["net"]["mode_top8_recall"] > r["prior"]["mode_top8_recall"] + 0.2
+    net, prior = r["net"]["tau0.9"], r["prior"]["tau0.9"]
+    assert net["rd_cost_increase"] < prior["rd_cost_increase"]
+    assert net["work_fraction"] < 0.5
+    assert r["pruned_lattice_tau0.9"]["speedup"] > 1.5

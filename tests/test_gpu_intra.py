@@ -71,3 +71,42 @@ def test_intra_lattice_unsorted_and_invalid_cus(gpu, oracle):
     satd_o, q_o = oracle_lattice(oracle, org, rec, allc[valid], 0, qps)
     assert np.array_equal(satd[valid].ravel(), satd_o)
     assert np.array_equal(q[valid].ravel(), q_o)
+
+
+def test_intra_lattice_mode_subset(gpu):
+    # a shortlist of modes per CU writes exactly those records, equal to the full lattice's
+    import ctypes as C
+    import torch
+    W, H = 96, 64
+    org = intra_frame(W, H, seed=8)
+    rec = np.clip(org.astype(int) + np.random.default_rng(8).integers(-4, 5, org.shape), 0, 255).astype(np.uint8)
+    cus = gpu.lattice_cus(W, H)
+    qps = [27, 37]
+    satd_all, q_all = gpu.intra_lattice(org, rec, cus, qps, ipf=1)
+    rng = np.random.default_rng(9)
+    K = 8
+    modes = np.stack([rng.permutation(33)[:K] for _ in range(len(cus))]).astype(np.uint8)
+    L = gpu.lib()
+    P, I = C.c_void_p, C.c_int
+    L.uavs3e_cuda_intra_lattice_modes_device.argtypes = [P, I, P, I, I, I, P, I, P, I, I, P, I, I, P, P, P]
+    d_org = torch.from_numpy(org).cuda()
+    d_rec = torch.from_numpy(rec).cuda()
+    d_cus = torch.from_numpy(cus.view(np.uint8).copy()).cuda()
+    d_modes = torch.from_numpy(modes).cuda()
+    n = len(cus)
+    d_satd = torch.full((n * 33,), -1, dtype=torch.int32, device="cuda")
+    d_q = torch.full((n * 33 * len(qps) * 16,), 0xAB, dtype=torch.uint8, device="cuda")
+    q = np.array(qps, np.int32)
+    rc = L.uavs3e_cuda_intra_lattice_modes_device(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H, d_cus.data_ptr(), n,
+                                                  d_modes.data_ptr(), K, 1, q.ctypes.data, len(qps), 1,
+                                                  d_satd.data_ptr(), d_q.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0
+    torch.cuda.synchronize()
+    satd = d_satd.cpu().numpy().view(np.uint32).reshape(n, 33)
+    qq = d_q.cpu().numpy().view(gpu.LAT_Q).reshape(n, 33, len(qps))
+    sel = np.zeros((n, 33), bool)
+    np.put_along_axis(sel, modes.astype(int), True, 1)
+    assert np.array_equal(satd[sel], satd_all.reshape(n, 33)[sel])
+    assert np.array_equal(qq[sel], q_all.reshape(n, 33, len(qps))[sel])
+    assert (satd[~sel] == 0xFFFFFFFF).all()
+    assert (qq[~sel].view(np.uint8) == 0xAB).all()

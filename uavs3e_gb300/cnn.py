@@ -24,7 +24,8 @@ LAYERS = [(2, 16, 3, 2), (16, 32, 3, 2), (32, 32, 3, 2), (32, 64, 3, 2)]
 HEAD = (64, 48, 1, 1)
 N_MODES = 33
 SHORTLIST = 8
-LAMBDA_QP = lambda qp: 0.57 * 2.0 ** ((qp - 12) / 3.0)  # noqa: E731
+# the encoder's rate-distortion lambda for an 8-bit QP (src/uavs3e.c:834)
+LAMBDA_QP = lambda qp: 1.43631 * 2.0 ** ((qp - 16) / 4.0)  # noqa: E731
 
 
 def kpad(cin, ks):
@@ -198,3 +199,281 @@ def plain_decisions(J, cus, W, H):
                 labels[b, 5 + c] = node(x, y, 16)[1]
                 labels[b, 21 + c] = arg[idx[(x, y, 16)]]
     return labels, xy
+
+
+# ----------------------------------------------------------------------------- data, training
+
+def frame_dataset(frame, qp=32):
+    """labels of the plain path for every full CTU of a frame (GPU lattice on the square CUs,
+    org as the reconstructed neighbours) -> (ctus [n][64][64] u8, labels, xy, J, cus)"""
+    from . import intra_lattice
+    H, W = frame.shape
+    cus = square_cus(W, H)
+    _, q = intra_lattice(frame, frame, cus, qps=(qp,), ipf=0)
+    J = rd_costs(q, cus, qp)
+    labels, xy = plain_decisions(J, cus, W, H)
+    ctus = np.stack([frame[y:y + 64, x:x + 64] for x, y in xy])
+    return ctus, labels, xy, J, cus
+
+
+def host_input(ctus, qp):
+    """network input of CTUs (host): [n][64][64][2] float32, rounded to bf16 on upload"""
+    x = np.empty(ctus.shape + (2,), np.float32)
+    x[..., 0] = (ctus.astype(np.float32) - 128.0) / 64.0
+    x[..., 1] = (qp - 32.0) / 8.0
+    return x
+
+
+def train(net, ctus, labels, qp=32, steps=300, lr=2e-3, seed=0):
+    """Adam on random batches of net.B CTUs; returns the loss (sum of the 4 parts) per step"""
+    import torch
+    rng = np.random.default_rng(seed)
+    hist = []
+    d_lab = torch.empty((net.B, 40), dtype=torch.uint8, device="cuda")
+    for _ in range(steps):
+        idx = rng.integers(0, len(ctus), net.B)
+        net.acts[0].copy_(torch.from_numpy(host_input(ctus[idx], qp)).to(torch.bfloat16))
+        d_lab.copy_(torch.from_numpy(labels[idx]))
+        net.forward()
+        hist.append(net.backward(d_lab).sum())
+        net.adam(lr=lr)
+    return [float(h) for h in torch.stack(hist).cpu()]
+
+
+def predict(net, ctus, qp=32):
+    """(split probabilities p64 [n], p32 [n][4], p16 [n][16], mode shortlist [n][16][8]) of CTUs"""
+    import torch
+    n = len(ctus)
+    p64, p32, p16, top = [], [], [], []
+    for s in range(0, n, net.B):
+        part = ctus[s:s + net.B]
+        x = np.zeros((net.B, 64, 64), np.uint8)
+        x[:len(part)] = part
+        net.acts[0].copy_(torch.from_numpy(host_input(x, qp)).to(torch.bfloat16))
+        lg = net.forward().cpu().numpy()[:len(part)]
+        sig = lambda v: 1.0 / (1.0 + np.exp(-v))  # noqa: E731
+        p64.append(sig(lg[:, :, 2].mean(1)))
+        cell = np.arange(16)
+        quad = (cell // 8) * 2 + (cell % 4) // 2
+        p32.append(sig(np.stack([lg[:, quad == qd, 1].mean(1) for qd in range(4)], 1)))
+        p16.append(sig(lg[:, :, 0]))
+        top.append(np.argsort(-lg[:, :, 3:36], axis=2)[:, :, :SHORTLIST])
+    return np.concatenate(p64), np.concatenate(p32), np.concatenate(p16), np.concatenate(top)
+
+
+def pruned_search(J, cus, xy, pred, tau, shortlist=True):
+    """RD cost of the quad-tree search over the candidates the predictions keep, against the
+    full search: a level is decided by the prediction only when its split probability is beyond
+    tau (or below 1 - tau); 16x16 and 8x8 CUs try only their cell's shortlist.  Returns
+    (relative RD-cost increase, fraction of the lattice's work (CU samples x modes) searched)."""
+    p64, p32, p16, top = pred
+    idx = {(int(c["x"]), int(c["y"]), int(c["w"])): i for i, c in enumerate(cus)}
+    split_bits = LAMBDA_QP(32) * 1.0
+    work = [0.0]
+
+    def own(x, y, s, modes):
+        row = J[idx[(x, y, s)]]
+        work[0] += s * s * (len(modes) if modes is not None else N_MODES)
+        return (row.min() if modes is None else row[modes].min()) + split_bits
+
+    def full(x, y, s):
+        o = J[idx[(x, y, s)]].min() + split_bits
+        if s == 8:
+            return o
+        h = s // 2
+        return min(o, sum(full(x + dx, y + dy, h) for dy in (0, h) for dx in (0, h)) + split_bits)
+
+    def node(x, y, s, b, x0, y0):
+        if s == 64:
+            p = p64[b]
+        elif s == 32:
+            p = p32[b][((y - y0) // 32) * 2 + (x - x0) // 32]
+        elif s == 16:
+            p = p16[b][((y - y0) // 16) * 4 + (x - x0) // 16]
+        else:
+            p = 0.0
+        cell = ((y - y0) // 16) * 4 + (x - x0) // 16
+        modes = top[b][cell] if (shortlist and s <= 16) else None
+        best = np.inf
+        if not p > tau:
+            best = own(x, y, s, modes)
+        if s > 8 and not p < 1 - tau:
+            h = s // 2
+            best = min(best, sum(node(x + dx, y + dy, h, b, x0, y0) for dy in (0, h) for dx in (0, h)) + split_bits)
+        return best
+
+    jp = jf = 0.0
+    for b, (x0, y0) in enumerate(xy):
+        jp += node(int(x0), int(y0), 64, b, int(x0), int(y0))
+        jf += full(int(x0), int(y0), 64)
+    all_work = len(xy) * 4 * 64 * 64 * N_MODES
+    return (jp - jf) / jf, work[0] / all_work
+
+
+def prior_predictions(labels, n):
+    """the method without the network: constant split probabilities (training label rates) and
+    the 8 most frequent training modes as every cell's shortlist"""
+    p64 = np.full(n, labels[:, 0].mean())
+    p32 = np.full((n, 4), labels[:, 1:5].mean())
+    p16 = np.full((n, 16), labels[:, 5:21].mean())
+    freq = np.bincount(labels[:, 21:37].ravel(), minlength=N_MODES)
+    top = np.tile(np.argsort(-freq)[:SHORTLIST], (n, 16, 1))
+    return p64, p32, p16, top
+
+
+def kept_cus(cus, xy, pred, tau):
+    """the square CUs the pruned search evaluates (any of their modes)"""
+    p64, p32, p16, _ = pred
+    keep = []
+    idx = {(int(c["x"]), int(c["y"]), int(c["w"])): i for i, c in enumerate(cus)}
+
+    def node(x, y, s, b, x0, y0):
+        p = (p64[b] if s == 64 else p32[b][((y - y0) // 32) * 2 + (x - x0) // 32] if s == 32
+             else p16[b][((y - y0) // 16) * 4 + (x - x0) // 16] if s == 16 else 0.0)
+        if not p > tau:
+            keep.append(idx[(x, y, s)])
+        if s > 8 and not p < 1 - tau:
+            h = s // 2
+            for dy in (0, h):
+                for dx in (0, h):
+                    node(x + dx, y + dy, h, b, x0, y0)
+
+    for b, (x0, y0) in enumerate(xy):
+        node(int(x0), int(y0), 64, b, int(x0), int(y0))
+    return cus[np.array(sorted(keep), dtype=np.int64)]
+
+
+def lattice_ms(frame, cus, qp=32, reps=3, modes=None):
+    """GPU time of the intra lattice over a CU list (one QP; all 33 modes, or the per-CU mode
+    lists [n][K] when given), CUDA events"""
+    import torch
+    from . import LAT_Q, lib
+    H, W = frame.shape
+    L = lib()
+    L.uavs3e_cuda_intra_lattice_modes_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                                          C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                                          C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                          C.c_void_p]
+    if len(cus) == 0:
+        return 0.0
+    d = torch.from_numpy(np.ascontiguousarray(frame)).cuda()
+    d_cus = torch.from_numpy(np.ascontiguousarray(cus).view(np.uint8)).cuda()
+    n = len(cus)
+    d_modes = None if modes is None else torch.from_numpy(np.ascontiguousarray(modes, dtype=np.uint8)).cuda()
+    K = 33 if modes is None else modes.shape[1]
+    d_satd = torch.empty(n * 33, dtype=torch.int32, device="cuda")
+    d_q = torch.empty(n * 33 * LAT_Q.itemsize, dtype=torch.uint8, device="cuda")
+    qps = np.array([qp], np.int32)
+    st = torch.cuda.current_stream()
+
+    def run():
+        check(L.uavs3e_cuda_intra_lattice_modes_device(d.data_ptr(), W, d.data_ptr(), W, W, H, d_cus.data_ptr(), n,
+                                                       None if d_modes is None else d_modes.data_ptr(), K, 0,
+                                                       qps.ctypes.data, 1, 1, d_satd.data_ptr(), d_q.data_ptr(),
+                                                       st.cuda_stream), "intra_lattice")
+
+    run()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def pruned_lattice_ms(frame, cus, xy, pred, tau, qp=32):
+    """GPU time of the pruned search's lattice work: the kept 64x64 / 32x32 CUs with all modes,
+    the kept 16x16 / 8x8 CUs with their cell's shortlist"""
+    kept = kept_cus(cus, xy, pred, tau)
+    big = kept[kept["w"] >= 32]
+    small = kept[kept["w"] <= 16]
+    top = pred[3]
+    origin = {(int(x), int(y)): b for b, (x, y) in enumerate(xy)}
+    modes = np.zeros((len(small), SHORTLIST), np.uint8)
+    for i, c in enumerate(small):
+        x, y = int(c["x"]), int(c["y"])
+        b = origin[(x & ~63, y & ~63)]
+        modes[i] = top[b][((y & 63) // 16) * 4 + (x & 63) // 16]
+    return lattice_ms(frame, big, qp) + lattice_ms(frame, small, qp, modes=modes), len(kept)
+
+
+def experiment(train_seeds=range(100, 104), test_seeds=(900,), qp=32, steps=1500, batch=128, taus=(0.8, 0.9),
+               seed=0, width=1920, height=1080):
+    """train on the plain path's decisions over synthetic 1080p I-frames, evaluate on held-out
+    frames against the method without the network; one dict of results"""
+    import time
+    import torch
+    from .synth import intra_frame
+    t0 = time.perf_counter()
+    tr = [frame_dataset(intra_frame(width, height, seed=s), qp) for s in train_seeds]
+    te_frames = [intra_frame(width, height, seed=s) for s in test_seeds]
+    te = [frame_dataset(f, qp) for f in te_frames]
+    t_label = time.perf_counter() - t0
+    ctus = np.concatenate([d[0] for d in tr])
+    labels = np.concatenate([d[1] for d in tr])
+    net = PruneNet(batch, seed=seed)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    hist = train(net, ctus, labels, qp=qp, steps=steps, seed=seed)
+    e1.record()
+    torch.cuda.synchronize()
+    train_ms = e0.elapsed_time(e1) / steps
+    out = {"train_ctus": int(len(ctus)), "test_ctus": int(sum(len(d[0]) for d in te)), "steps": steps, "batch": batch,
+           "label_rates": {"split64": float(labels[:, 0].mean()), "split32": float(labels[:, 1:5].mean()),
+                           "split16": float(labels[:, 5:21].mean()),
+                           "mode_top8_share": float(np.sort(np.bincount(labels[:, 21:37].ravel(), minlength=N_MODES))[::-1][:SHORTLIST].sum() / labels[:, 21:37].size)},
+           "train_ms_per_step": train_ms, "label_s": t_label, "loss_first": hist[0], "loss_last": float(np.mean(hist[-20:]))}
+    # accuracy against the held-out plain decisions
+    te_ctus = np.concatenate([d[0] for d in te])
+    te_labels = np.concatenate([d[1] for d in te])
+    pred = predict(net, te_ctus, qp)
+    prior = prior_predictions(labels, len(te_ctus))
+    for name, p in (("net", pred), ("prior", prior)):
+        p64, p32, p16, top = p
+        out[name] = {
+            "split64_acc": float(((p64 > 0.5) == te_labels[:, 0].astype(bool)).mean()),
+            "split32_acc": float(((p32 > 0.5) == te_labels[:, 1:5].astype(bool)).mean()),
+            "split16_acc": float(((p16 > 0.5) == te_labels[:, 5:21].astype(bool)).mean()),
+            "mode_top8_recall": float((top == te_labels[:, 21:37, None]).any(2).mean()),
+        }
+    # pruned search on the held-out frames: RD-cost increase and work kept, per threshold
+    for tau in taus:
+        for name, p in (("net", pred), ("prior", prior)):
+            dj, wk, off = [], [], 0
+            for d in te:
+                n = len(d[0])
+                sub = tuple(a[off:off + n] for a in p)
+                r = pruned_search(d[3], d[4], d[2], sub, tau)
+                dj.append(r[0]); wk.append(r[1])
+                off += n
+            out[name][f"tau{tau}"] = {"rd_cost_increase": float(np.mean(dj)), "work_fraction": float(np.mean(wk))}
+    # GPU time: inference of a frame's CTUs, and the lattice over all square CUs vs the kept ones
+    f0, d0 = te_frames[0], te[0]
+    infer = PruneNet(len(d0[0]), params=net.params())
+    x = torch.from_numpy(host_input(d0[0], qp)).to(torch.bfloat16).cuda()
+    infer.acts[0].copy_(x)
+    infer.forward()
+    e0.record()
+    for _ in range(5):
+        infer.forward()
+    e1.record()
+    torch.cuda.synchronize()
+    out["inference_ms_per_frame"] = e0.elapsed_time(e1) / 5
+    full_ms = lattice_ms(f0, d0[4], qp)
+    n0 = len(d0[0])
+    out["lattice_square_cus_ms"] = full_ms
+    out["square_cus"] = int(len(d0[4]))
+    for tau in taus:
+        ms, nk = pruned_lattice_ms(f0, d0[4], d0[2], tuple(a[:n0] for a in pred), tau, qp)
+        out[f"pruned_lattice_tau{tau}"] = {"ms": ms, "kept_cus": int(nk), "speedup": full_ms / ms if ms else None}
+    return out
+
+
+if __name__ == "__main__":
+    import json
+    from . import build, init
+    build()
+    init(0)
+    print(json.dumps(experiment()))

@@ -62,13 +62,13 @@ __global__ void k_lat_scatter(const LatCu *cus, int n, int W, int H, const int *
     perm[offsets[c] + atomicAdd(&cursor[c], 1)] = i;
 }
 
-size_t lattice_smem_bytes(int w, int h)
+size_t lattice_smem_bytes(int w, int h, int nm)
 {
     int lw = 0, lh = 0;
     while ((1 << lw) < w) lw++;
     while ((1 << lh) < h) lh++;
     LatLayout L;
-    lat_layout(lw, lh, L);
+    lat_layout(lw, lh, nm, L);
     return (size_t)L.smem;
 }
 
@@ -82,8 +82,8 @@ struct LatScratch {
 static LatScratch g_lat[64];
 
 int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, int W, int H, const LatCu *cus,
-                         int n_cus, int ipf, const int *qps, int n_qp, int is_intra, u32 *satd_out, LatQ *q_out,
-                         cudaStream_t st)
+                         int n_cus, const u8 *modes, int n_modes, int ipf, const int *qps, int n_qp, int is_intra,
+                         u32 *satd_out, LatQ *q_out, cudaStream_t st)
 {
     int dev = 0;
     UC_CHECK(cudaGetDevice(&dev));
@@ -91,6 +91,8 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     const DevTables *tab = device_tables(dev);
     if (!tab) return set_status(UC_ERR_MEMORY, "intra_lattice: table upload failed");
     if (n_qp < 1 || n_qp > LAT_MAX_QP || n_cus < 0) return set_status(UC_ERR_ARG, "intra_lattice: bad qp count");
+    if (n_modes < 1 || n_modes > 33 || (!modes && n_modes != 33))
+        return set_status(UC_ERR_ARG, "intra_lattice: mode list");
     for (int i = 0; i < n_qp; i++)
         if (qps[i] < 0 || qps[i] > 63) return set_status(UC_ERR_ARG, "intra_lattice: qp out of range");
     if (n_cus == 0) return UC_OK;
@@ -124,6 +126,7 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     P.cus = cus; P.ipf = ipf; P.n_qp = n_qp; P.is_intra = is_intra;
     for (int i = 0; i < LAT_MAX_QP; i++) P.qp[i] = i < n_qp ? qps[i] : 0;
     P.satd_out = satd_out; P.q_out = q_out;
+    P.modes = modes; P.n_modes = n_modes;
     P.sq32 = sqrt(32.0); P.sq128 = sqrt(128.0);
     // largest shapes first: their CTAs are the longest
     for (int lw = 6; lw >= 2; lw--)
@@ -132,7 +135,7 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
             const int n = S.h_counts[c];
             if (!n) continue;
             LatLayout L;
-            lat_layout(lw, lh, L);
+            lat_layout(lw, lh, n_modes, L);
             P.perm = S.perm + offs[c];
             P.n_shape = n;
             P.fold_w = tab->fold[lw]; P.fold_h = tab->fold[lh];
@@ -181,17 +184,28 @@ UAVS3E_CUDA_API int uavs3e_cuda_lattice_cus(int width, int height, uavs3e_cuda_c
     return n;
 }
 
-UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i_org, const uint8_t *d_rec, int i_rec,
-                                                     int width, int height, const uavs3e_cuda_cu_t *d_cus, int n_cus,
-                                                     int ipf, const int *qps, int n_qp, int is_intra_slice,
-                                                     uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream)
+UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_modes_device(const uint8_t *d_org, int i_org, const uint8_t *d_rec,
+                                                           int i_rec, int width, int height,
+                                                           const uavs3e_cuda_cu_t *d_cus, int n_cus,
+                                                           const uint8_t *d_modes, int n_modes, int ipf, const int *qps,
+                                                           int n_qp, int is_intra_slice, uint32_t *d_satd,
+                                                           uavs3e_cuda_lat_q_t *d_q, void *stream)
 {
     int r = ensure_init();
     if (r) return r;
     if (!d_org || !d_rec || !d_cus || !d_satd || !d_q || !qps) return set_status(UC_ERR_ARG, "intra_lattice: null pointer");
     if (width % 4 || height % 4) return set_status(UC_ERR_ARG, "intra_lattice: picture size must be a multiple of 4");
-    return launch_intra_lattice(d_org, i_org, d_rec, i_rec, width, height, (const LatCu *)d_cus, n_cus, ipf, qps, n_qp,
-                                is_intra_slice, d_satd, (LatQ *)d_q, (cudaStream_t)stream);
+    return launch_intra_lattice(d_org, i_org, d_rec, i_rec, width, height, (const LatCu *)d_cus, n_cus, d_modes, n_modes,
+                                ipf, qps, n_qp, is_intra_slice, d_satd, (LatQ *)d_q, (cudaStream_t)stream);
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i_org, const uint8_t *d_rec, int i_rec,
+                                                     int width, int height, const uavs3e_cuda_cu_t *d_cus, int n_cus,
+                                                     int ipf, const int *qps, int n_qp, int is_intra_slice,
+                                                     uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream)
+{
+    return uavs3e_cuda_intra_lattice_modes_device(d_org, i_org, d_rec, i_rec, width, height, d_cus, n_cus, nullptr, 33,
+                                                  ipf, qps, n_qp, is_intra_slice, d_satd, d_q, stream);
 }
 
 }  // extern "C"

@@ -61,6 +61,7 @@ struct LatQ { u32 ssd; u32 coef_hash; u16 num_nz; s16 last_nz; u32 sum_abs; };
 constexpr int LAT_THREADS = 256;
 constexpr int LAT_BUDGET = 48 * 1024;   // dynamic shared bytes per CTA (4 CTAs per SM with the static part)
 constexpr int LAT_MAX_QP = 4;
+constexpr int LAT_SMEM_MAX = 96 * 1024;   // dynamic shared memory admitted by the kernel attribute
 constexpr int LAT_MAX_G = 8;            // CUs per CTA
 constexpr int LAT_MAX_JOBS = 33 * LAT_MAX_G;
 constexpr int LAT_NB = 592;             // neighbour buffer per CU (INTRA_NEIB_SIZE + pad)
@@ -85,7 +86,7 @@ struct LatLayout {
 
 __host__ __device__ __forceinline__ int lat_up16(int v) { return (v + 15) & ~15; }
 
-__host__ __device__ inline void lat_layout(int lw, int lh, LatLayout &L)
+__host__ __device__ inline void lat_layout(int lw, int lh, int nm, LatLayout &L)
 {
     L.lw = lw; L.lh = lh; L.w = 1 << lw; L.h = 1 << lh;
     L.kw = L.w < 32 ? L.w : 32; L.kh = L.h < 32 ? L.h : 32;
@@ -111,17 +112,17 @@ __host__ __device__ inline void lat_layout(int lw, int lh, LatLayout &L)
     L.j_t2 = j; j += lat_up16(L.h * L.kw * 2);
     L.job_bytes = j;
     const int avail = LAT_BUDGET - o;
-    // several whole CUs when 33 jobs of the shape fit, else one CU and a chunk of its modes
-    int G = avail / (33 * L.job_bytes + L.cu_bytes);
+    // several whole CUs when nm jobs of the shape fit, else one CU and a chunk of its modes
+    int G = avail / (nm * L.job_bytes + L.cu_bytes);
     if (G >= 1) {
         L.G = G < LAT_MAX_G ? G : LAT_MAX_G;
-        L.MC = 33; L.nchunk = 1;
+        L.MC = nm; L.nchunk = 1;
     } else {
         int J = (avail - L.cu_bytes) / L.job_bytes;
         J = J < 1 ? 1 : J;
         L.G = 1;
-        L.nchunk = (33 + J - 1) / J;
-        L.MC = (33 + L.nchunk - 1) / L.nchunk;
+        L.nchunk = (nm + J - 1) / J;
+        L.MC = (nm + L.nchunk - 1) / L.nchunk;
     }
     L.o_cu = o; o += L.G * L.cu_bytes;
     L.o_job = o; o += L.G * L.MC * L.job_bytes;
@@ -140,6 +141,8 @@ struct LatParams {
     u32 *satd_out; LatQ *q_out;
     const s8 *fold_w, *fold_h;
     const u16 *scanpos;
+    const u8 *modes;          // [CU][n_modes] modes to evaluate, or null for all 33 in order
+    int n_modes;
     double sq32, sq128;
 };
 
@@ -242,12 +245,13 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     extern __shared__ __align__(16) u8 sm[];
     __shared__ IpredBlock sB[LAT_MAX_G];
     __shared__ int s_cu[LAT_MAX_G];
+    __shared__ u8 s_mode[LAT_MAX_JOBS];
     __shared__ u32 s_satd[LAT_MAX_JOBS], s_flag[LAT_MAX_JOBS];
     __shared__ u32 s_nz[LAT_MAX_JOBS], s_sum[LAT_MAX_JOBS], s_hash[LAT_MAX_JOBS], s_ssd[LAT_MAX_JOBS];
     __shared__ int s_last[LAT_MAX_JOBS];
 
     LatLayout L;
-    lat_layout(LW, LH, L);      // compile-time shape: every index and trip count below is a constant
+    lat_layout(LW, LH, P.n_modes, L);   // compile-time shape: the indices and trip counts below are constants
     const int w = L.w, h = L.h, lw = L.lw, lh = L.lh, kw = L.kw, kh = L.kh, lkw = L.lkw, lkh = L.lkh;
     const int N = w * h, lN = lw + lh;
     const int tid = threadIdx.x, lane = tid & 31, wbase = tid & ~31;
@@ -257,7 +261,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     const int cu0 = grp * L.G;
     const int Gv = min(L.G, P.n_shape - cu0);
     const int m0 = chunk * L.MC;
-    const int MCv = min(L.MC, 33 - m0);
+    const int MCv = min(L.MC, P.n_modes - m0);
     const int J = Gv * MCv;
     if (Gv <= 0 || MCv <= 0) return;
 
@@ -282,6 +286,8 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     for (int i = tid; i < kw * kh; i += LAT_THREADS) s_scan[i] = P.scanpos[(i >> lkw) * w + (i & (kw - 1))];
     if (tid < Gv) s_cu[tid] = P.perm[cu0 + tid];
     for (int j = tid; j < J; j += LAT_THREADS) {
+        const int g = j / MCv, mi = m0 + (j - g * MCv);
+        s_mode[j] = P.modes ? P.modes[(size_t)P.perm[cu0 + g] * P.n_modes + mi] : (u8)mi;
         s_satd[j] = 0; s_flag[j] = 0; s_nz[j] = 0; s_sum[j] = 0; s_hash[j] = 0; s_ssd[j] = 0; s_last[j] = -1;
     }
     __syncthreads();
@@ -344,7 +350,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     // ---- prediction
     for (int i = tid; i < (J << lN); i += LAT_THREADS) {
         const int j = i >> lN, p = i & (N - 1);
-        const int g = JG(j), m = m0 + (j - g * MCv);
+        const int g = JG(j), m = s_mode[j];
         const int x = p & (w - 1), y = p >> lw;
         JPRED(j)[y * L.ps + x] = (pel)ipred_sample(cub + g * L.cu_bytes + L.c_nb + 288, sB[g], m, P.ipf, x, y);
     }
@@ -418,7 +424,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     }
     __syncthreads();
     for (int j = tid; j < J; j += LAT_THREADS)
-        P.satd_out[(size_t)s_cu[JG(j)] * 33 + m0 + (j - JG(j) * MCv)] = s_satd[j];
+        P.satd_out[(size_t)s_cu[JG(j)] * 33 + s_mode[j]] = s_satd[j];
 
     for (int q = 0; q < P.n_qp; q++) {
         const int qp = P.qp[q];
@@ -529,7 +535,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
             o.num_nz = (u16)s_nz[j];
             o.last_nz = (s16)s_last[j];
             o.sum_abs = s_sum[j];
-            P.q_out[((size_t)s_cu[g] * 33 + m0 + (j - g * MCv)) * P.n_qp + q] = o;
+            P.q_out[((size_t)s_cu[g] * 33 + s_mode[j]) * P.n_qp + q] = o;
             s_ssd[j] = 0; s_hash[j] = 0; s_nz[j] = 0; s_last[j] = -1; s_sum[j] = 0;
         }
         __syncthreads();

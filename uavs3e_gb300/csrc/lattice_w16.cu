@@ -19,10 +19,13 @@ int lat_launch_w<4>(int lh, unsigned grid, int smem, cudaStream_t st, const LatP
     case 6: k = k_intra_lattice<4, 6>; break;
     default: return set_status(UC_ERR_ARG, "intra_lattice: CU height");
     }
+    // the launch's own size decides the occupancy; the attribute only has to admit every
+    // layout (mode counts change it)
     if (!attr[dev][lh]) {
-        UC_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        UC_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, LAT_SMEM_MAX));
         attr[dev][lh] = true;
     }
+    if (smem > LAT_SMEM_MAX) return set_status(UC_ERR_ARG, "intra_lattice: shared memory layout");
     k<<<grid, LAT_THREADS, smem, st>>>(P);
     UC_CHECK(cudaGetLastError());
     return UC_OK;
