@@ -284,6 +284,17 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
     return out
 
 
+def pruning_leg():
+    """the learned CU pruning beside the lattice: trained on the plain path's decisions over 4
+    synthetic 1080p I-frames, evaluated on a held-out frame (RD-cost increase of the pruned
+    search, share of the lattice's work it searches, GPU time of the pruned lattice)"""
+    from uavs3e_gb300 import cnn
+    r = cnn.experiment()
+    r["workload"] = ("CNN 2 -> 16/32/32/64 ch (3x3, stride 2) + 1x1 head, bf16 tensor cores (mma.sync), FP32 "
+                     "accumulation; labels: quad-tree + mode decisions from the lattice's RD costs at QP 32")
+    return r
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -422,6 +433,7 @@ def run_ours(args):
                     "peak_source": "hbm_gbs of MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
                     "traffic_note": "ncu DRAM bytes per launch: the written planes stay in the 129 MB L2"}
     lattice = lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, not args.no_cpu)
+    pruning = pruning_leg()
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -439,6 +451,7 @@ def run_ours(args):
         "roofline": roofline,
         "roofline_hbm": roofline_hbm,
         "lattice": lattice,
+        "pruning": pruning,
         "clocks": clk,
     }
     if not args.no_cpu:
