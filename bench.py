@@ -37,6 +37,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--legs", default="me,lattice,pruning",
+                    help="comma list of legs: me (the headline line), lattice, pruning")
+    ap.add_argument("--pruning-steps", type=int, default=1500, help="training steps of the pruning leg")
     return ap.parse_args()
 
 
@@ -284,12 +287,12 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
     return out
 
 
-def pruning_leg():
+def pruning_leg(steps=1500):
     """the learned CU pruning beside the lattice: trained on the plain path's decisions over 4
     synthetic 1080p I-frames, evaluated on a held-out frame (RD-cost increase of the pruned
     search, share of the lattice's work it searches, GPU time of the pruned lattice)"""
     from uavs3e_gb300 import cnn
-    r = cnn.experiment()
+    r = cnn.experiment(steps=steps)
     r["workload"] = ("CNN 2 -> 16/32/32/64 ch (3x3, stride 2) + 1x1 head, bf16 tensor cores (mma.sync), FP32 "
                      "accumulation; labels: quad-tree + mode decisions from the lattice's RD costs at QP 32")
     return r
@@ -432,8 +435,9 @@ def run_ours(args):
                     "bytes_per_launch": sub_bytes,
                     "peak_source": "hbm_gbs of MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
                     "traffic_note": "ncu DRAM bytes per launch: the written planes stay in the 129 MB L2"}
-    lattice = lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, not args.no_cpu)
-    pruning = pruning_leg()
+    legs = set(args.legs.split(","))
+    lattice = lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, not args.no_cpu) if "lattice" in legs else None
+    pruning = pruning_leg(args.pruning_steps) if "pruning" in legs else None
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -462,10 +466,36 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_legs(args):
+    """the lattice and / or pruning legs alone (profiling runs of those kernels)"""
+    import torch
+    import uavs3e_gb300 as u
+    legs = set(args.legs.split(","))
+    u.build()
+    u.init(0)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    sm_count = torch.cuda.get_device_properties(0).multi_processor_count
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {}
+    if "lattice" in legs:
+        out["lattice"] = lattice_leg(u, torch, torch.cuda.current_stream(), flush, peaks, sm_count, sm_mhz,
+                                     not args.no_cpu)
+    if "pruning" in legs:
+        out["pruning"] = pruning_leg(args.pruning_steps)
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif "me" not in args.legs.split(","):
+        run_legs(args)
     else:
         run_ours(args)
 

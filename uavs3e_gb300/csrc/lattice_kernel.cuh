@@ -70,9 +70,11 @@ constexpr int LAT_SHAPES = 25;          // log2 sides 2..6
 // shared-memory layout of one shape's CTAs (host and device compute it the same way)
 struct LatLayout {
     int w, h, lw, lh, kw, kh, lkw, lkh;
-    int ps;            // prediction / org row stride (bytes): w + 4
-    int ts;            // forward row-pass output row stride (s16): h + 2
-    int ds;            // transposed dequantised row stride (s16): kh + 2
+    int ps;            // prediction / org row stride (bytes): 16-byte aligned rows
+    int ts;            // forward row-pass output row stride (s16): 16-byte aligned rows
+    int cs;            // coefficient row stride (s16): kw + 2
+    int ds;            // transposed dequantised row stride (s16): 16-byte aligned rows
+    int t2s;           // inverse column-pass output row stride (s16): 16-byte aligned rows
     int fw_ws, fh_ws, fht_ws, fwt_ws;   // table row strides in words
     int o_fw, o_fh, o_fht, o_fwt;       // table offsets
     int o_scan;                         // scan index of each kept coefficient, [v][u] (u16)
@@ -91,7 +93,14 @@ __host__ __device__ inline void lat_layout(int lw, int lh, int nm, LatLayout &L)
     L.lw = lw; L.lh = lh; L.w = 1 << lw; L.h = 1 << lh;
     L.kw = L.w < 32 ? L.w : 32; L.kh = L.h < 32 ? L.h : 32;
     L.lkw = lw < 5 ? lw : 5; L.lkh = lh < 5 ? lh : 5;
-    L.ps = L.w + 4; L.ts = L.h + 2; L.ds = L.kh + 2;
+    // rows that are read whole by every lane of a warp (broadcast) start on 16 bytes; the
+    // strides also keep the rows 8 lanes read at once on distinct banks
+    L.ps = L.w <= 8 ? 16 : L.w <= 32 ? 48 : 80;
+    L.ts = L.h >= 8 ? L.h + 8 : 8;
+    L.cs = L.kw + 2;
+    L.ds = L.kh >= 8 ? L.kh + 8 : 8;
+    L.t2s = L.kw >= 8 ? L.kw + 8 : 8;
+    // matrix rows are read one per lane: strides of an odd number of words
     L.fw_ws = L.w / 4 + 1; L.fh_ws = L.h / 4 + 1; L.fht_ws = L.kh / 4 + 1; L.fwt_ws = L.kw / 4 + 1;
     int o = 0;
     L.o_fw = o; o += lat_up16(L.kw * L.fw_ws * 4);
@@ -107,9 +116,9 @@ __host__ __device__ inline void lat_layout(int lw, int lh, int nm, LatLayout &L)
     int j = 0;
     L.j_pred = j; j += lat_up16(L.h * L.ps);
     L.j_t = j; j += lat_up16(L.kw * L.ts * 2);
-    L.j_c = j; j += lat_up16(L.kh * L.kw * 2);
+    L.j_c = j; j += lat_up16(L.kh * L.cs * 2);
     L.j_dqt = j; j += lat_up16(L.kw * L.ds * 2);
-    L.j_t2 = j; j += lat_up16(L.h * L.kw * 2);
+    L.j_t2 = j; j += lat_up16(L.h * L.t2s * 2);
     L.job_bytes = j;
     const int avail = LAT_BUDGET - o;
     // several whole CUs when nm jobs of the shape fit, else one CU and a chunk of its modes
@@ -168,6 +177,37 @@ __device__ __forceinline__ u32 seg_or(u32 v, int seg, int lane)
     const u32 lo = __reduce_or_sync(0xFFFFFFFFu, lane < 16 ? v : 0u);
     const u32 hi = __reduce_or_sync(0xFFFFFFFFu, lane < 16 ? 0u : v);
     return lane < 16 ? lo : hi;
+}
+
+// NW words of a row that every lane of a warp reads (16-byte aligned): vector loads
+template <int NW>
+__device__ __forceinline__ void lat_row(const void *p, u32 (&r)[NW])
+{
+    if constexpr (NW >= 4) {
+#pragma unroll
+        for (int k = 0; k < NW / 4; k++) {
+            const uint4 v = reinterpret_cast<const uint4 *>(p)[k];
+            r[4 * k] = v.x; r[4 * k + 1] = v.y; r[4 * k + 2] = v.z; r[4 * k + 3] = v.w;
+        }
+    } else if constexpr (NW == 2) {
+        const uint2 v = *reinterpret_cast<const uint2 *>(p);
+        r[0] = v.x; r[1] = v.y;
+    } else {
+        r[0] = *reinterpret_cast<const u32 *>(p);
+    }
+}
+
+// sum over aligned groups of SEG lanes (SEG a power of two <= 32)
+template <int SEG>
+__device__ __forceinline__ u32 lat_seg_sum(u32 v, int lane)
+{
+    if constexpr (SEG >= 16) {
+        return seg_sum(v, SEG, lane);
+    } else {
+#pragma unroll
+        for (int d = 1; d < SEG; d <<= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
+        return v;
+    }
 }
 
 // com_had tile of a (2^LW) x (2^LH) block (src/com_cost.c:712-812), as constants
@@ -254,6 +294,13 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     lat_layout(LW, LH, P.n_modes, L);   // compile-time shape: the indices and trip counts below are constants
     const int w = L.w, h = L.h, lw = L.lw, lh = L.lh, kw = L.kw, kh = L.kh, lkw = L.lkw, lkh = L.lkh;
     const int N = w * h, lN = lw + lh;
+    constexpr int W_ = 1 << LW, H_ = 1 << LH, KW_ = W_ < 32 ? W_ : 32, KH_ = H_ < 32 ? H_ : 32;
+    constexpr int LKW_ = LW < 5 ? LW : 5, LKH_ = LH < 5 ? LH : 5;
+    // row passes: a task is one matrix row (in registers) against RY data rows; column passes:
+    // against RU data columns.  Lanes of a warp take consecutive matrix rows, so the data row
+    // they read is the same (one broadcast load).
+    constexpr int RY = H_ < 8 ? H_ : 8, NYC = H_ / RY;
+    constexpr int RU = KW_ < 8 ? KW_ : 8, NUC = KW_ / RU;
     const int tid = threadIdx.x, lane = tid & 31, wbase = tid & ~31;
 
     // this CTA's CUs and modes
@@ -326,7 +373,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
         const int avail = (cu.y > 0 ? 1 : 0) | (cu.x > 0 ? 2 : 0) | ((cu.x > 0 && cu.y > 0) ? 4 : 0);
         ipred_block_setup(cub + tid * L.cu_bytes + L.c_nb + 288, w, h, avail, 8, sB[tid]);
     }
-    // org part of the forward row pass: Torg[u][y] = sum_x Fw[u][x] org[y][x]
+    // org part of the forward row pass: Torg[y][u] = sum_x Fw[u][x] org[y][x]
     for (int i = tid; i < Gv * kw * h; i += LAT_THREADS) {
         const int u = i & (kw - 1), y = (i >> lkw) & (h - 1), g = i >> (lkw + lh);
         const u8 *c = cub + g * L.cu_bytes;
@@ -334,7 +381,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
         int acc = 0;
         #pragma unroll
         for (int k = 0; k < (w >> 2); k++) acc = dp4a_us(o[k], f[k], acc);
-        ((int *)(c + L.c_torg))[u * h + y] = acc;
+        ((int *)(c + L.c_torg))[y * kw + u] = acc;
     }
     __syncthreads();
 
@@ -365,15 +412,23 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     }
     {
         const int sh1 = lw - 2, rnd1 = sh1 > 0 ? 1 << (sh1 - 1) : 0;
-        for (int i = tid; i < J * kw * h; i += LAT_THREADS) {
-            const int u = i & (kw - 1), y = (i >> lkw) & (h - 1), j = i >> (lkw + lh);
-            const int g = JG(j);
-            const u32 *pr = (const u32 *)(JPRED(j) + y * L.ps), *f = fw + u * L.fw_ws;
-            int s = 0;
-            #pragma unroll
-            for (int k = 0; k < (w >> 2); k++) s = dp4a_us(pr[k], f[k], s);
-            const int acc = ((const int *)(cub + g * L.cu_bytes + L.c_torg))[u * h + y] - s;
-            JT(j)[u * L.ts + y] = (s16)((acc + rnd1) >> sh1);
+        for (int i = tid; i < J * NYC * KW_; i += LAT_THREADS) {
+            const int u = i & (KW_ - 1), yc = (i >> LKW_) % NYC, j = i / (KW_ * NYC);
+            u32 f[W_ / 4];
+#pragma unroll
+            for (int k = 0; k < W_ / 4; k++) f[k] = fw[u * L.fw_ws + k];
+            const int *torg = (const int *)(cub + JG(j) * L.cu_bytes + L.c_torg);
+            s16 *T = JT(j);
+#pragma unroll
+            for (int r = 0; r < RY; r++) {
+                const int y = yc * RY + r;
+                u32 pw[W_ / 4];
+                lat_row<W_ / 4>(JPRED(j) + y * L.ps, pw);
+                int sacc = 0;
+#pragma unroll
+                for (int k = 0; k < W_ / 4; k++) sacc = dp4a_us(pw[k], f[k], sacc);
+                T[u * L.ts + y] = (s16)((torg[y * KW_ + u] - sacc + rnd1) >> sh1);
+            }
         }
     }
     __syncthreads();
@@ -395,31 +450,31 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
             nz_thr[q] = ((((1 << q_bits) - offset) << 10) / q_value - 1) >> 10;
         }
         const int sh2 = lh + 5, rnd2 = 1 << (sh2 - 1);
-        const int E = kw * kh, lE = lkw + lkh, seg = E < 32 ? E : 32;
-        for (int base = wbase; base < (J << lE); base += LAT_THREADS) {
-            const int i = base + lane;
-            const bool act = i < (J << lE);
-            const int ii = act ? i : base;
-            const int u = ii & (kw - 1), v = (ii >> lkw) & (kh - 1), j = ii >> lE;
-            const u32 *t = (const u32 *)(JT(j) + u * L.ts), *f = fh + v * L.fh_ws;
-            int acc = 0;
-            #pragma unroll
-            for (int k = 0; k < (h >> 2); k++) {
-                const u32 fwd = f[k];
-                acc = dp2a_lo(t[2 * k], fwd, acc);
-                acc = dp2a_hi(t[2 * k + 1], fwd, acc);
-            }
-            const int c = (acc + rnd2) >> sh2;
+        for (int i = tid; i < J * NUC * KH_; i += LAT_THREADS) {
+            const int v = i & (KH_ - 1), uc = (i >> LKH_) % NUC, j = i / (KH_ * NUC);
+            u32 f[H_ / 4];
+#pragma unroll
+            for (int k = 0; k < H_ / 4; k++) f[k] = fh[v * L.fh_ws + k];
             u32 fl = 0;
-            if (act) {
-                JC(j)[v * kw + u] = (s16)c;
+#pragma unroll
+            for (int r = 0; r < RU; r++) {
+                const int u = uc * RU + r;
+                u32 tw[H_ / 2];
+                lat_row<H_ / 2>(JT(j) + u * L.ts, tw);
+                int acc = 0;
+#pragma unroll
+                for (int k = 0; k < H_ / 4; k++) {
+                    acc = dp2a_lo(tw[2 * k], f[k], acc);
+                    acc = dp2a_hi(tw[2 * k + 1], f[k], acc);
+                }
+                const int c = (acc + rnd2) >> sh2;
+                JC(j)[v * L.cs + u] = (s16)c;
                 const int a = c < 0 ? -(int)(s16)c : (int)(s16)c;
 #pragma unroll
                 for (int q = 0; q < LAT_MAX_QP; q++)
                     if (q < P.n_qp && a > nz_thr[q]) fl |= 1u << q;
             }
-            fl = seg_or(fl, seg, lane);
-            if (act && (lane & (seg - 1)) == 0 && fl) atomicOr(&s_flag[j], fl);
+            if (fl) atomicOr(&s_flag[j], fl);
         }
     }
     __syncthreads();
@@ -443,10 +498,10 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
                 const bool act = i < (J << lE);
                 const int ii = act ? i : base;
                 const int r = ii & (E - 1), j = ii >> lE;
-                const int u = r & (kw - 1), v = r >> lkw;
+                const int v = r & (KH_ - 1), u = r >> LKH_;
                 int lev = 0;
                 if (act && (s_flag[j] >> q & 1)) {
-                    const int c = JC(j)[r];
+                    const int c = JC(j)[v * L.cs + u];
                     const int a = c < 0 ? -c : c;
                     if (a >= thr) {
                         const int l = (int)(s16)(((u32)a * q_value + qadd) >> q_bits);
@@ -461,7 +516,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
                     nz = 1;
                     sa = (u32)(lev < 0 ? -lev : lev);
                     hs = fmix32(((u32)pos << 16) | (u16)(s16)lev);
-                    last = (int)s_scan[r];
+                    last = (int)s_scan[v * KW_ + u];
                     int d = (lev * dq_scale + dq_off) >> dq_shift;
                     d = min(32767, max(-32768, d));
                     dq = odd ? (d * 181 + 128) >> 8 : d;
@@ -484,46 +539,63 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
         __syncthreads();
         // inverse column pass T2[y][u] = clip16((sum_v Fh[v][y] DQ[v][u] + 16) >> 5), only
         // for jobs with coded levels
-        for (int i = tid; i < J * h * kw; i += LAT_THREADS) {
-            const int u = i & (kw - 1), y = (i >> lkw) & (h - 1), j = i >> (lkw + lh);
+        for (int i = tid; i < J * NUC * H_; i += LAT_THREADS) {
+            const int y = i & (H_ - 1), uc = (i >> LH) % NUC, j = i / (H_ * NUC);
             if (!s_nz[j]) continue;
-            const u32 *d = (const u32 *)(JDQT(j) + u * L.ds), *f = fht + y * L.fht_ws;
-            int acc = 0;
-            #pragma unroll
-            for (int k = 0; k < (kh >> 2); k++) {
-                const u32 fwd = f[k];
-                acc = dp2a_lo(d[2 * k], fwd, acc);
-                acc = dp2a_hi(d[2 * k + 1], fwd, acc);
+            u32 f[KH_ / 4];
+#pragma unroll
+            for (int k = 0; k < KH_ / 4; k++) f[k] = fht[y * L.fht_ws + k];
+#pragma unroll
+            for (int r = 0; r < RU; r++) {
+                const int u = uc * RU + r;
+                u32 dw[KH_ / 2];
+                lat_row<KH_ / 2>(JDQT(j) + u * L.ds, dw);
+                int acc = 0;
+#pragma unroll
+                for (int k = 0; k < KH_ / 4; k++) {
+                    acc = dp2a_lo(dw[2 * k], f[k], acc);
+                    acc = dp2a_hi(dw[2 * k + 1], f[k], acc);
+                }
+                JT2(j)[y * L.t2s + u] = (s16)min(32767, max(-32768, (acc + 16) >> 5));
             }
-            JT2(j)[y * kw + u] = (s16)min(32767, max(-32768, (acc + 16) >> 5));
         }
         __syncthreads();
-        // inverse row pass, reconstruction, SSD
+        // inverse row pass, reconstruction, SSD: a task is one column x over RY rows
         {
-            const int seg = N < 32 ? N : 32;
-            for (int base = wbase; base < (J << lN); base += LAT_THREADS) {
+            constexpr int TPJ = W_ * NYC, SEG = TPJ < 32 ? TPJ : 32;
+            for (int base = wbase; base < J * TPJ; base += LAT_THREADS) {
                 const int i = base + lane;
-                const bool act = i < (J << lN);
+                const bool act = i < J * TPJ;
                 const int ii = act ? i : base;
-                const int p = ii & (N - 1), j = ii >> lN;
-                const int x = p & (w - 1), y = p >> lw;
-                int rv = JPRED(j)[y * L.ps + x];
-                if (s_nz[j]) {
-                    const u32 *t = (const u32 *)(JT2(j) + y * kw), *f = fwt + x * L.fwt_ws;
-                    int acc = 0;
-                    #pragma unroll
-                    for (int k = 0; k < (kw >> 2); k++) {
-                        const u32 fwd = f[k];
-                        acc = dp2a_lo(t[2 * k], fwd, acc);
-                        acc = dp2a_hi(t[2 * k + 1], fwd, acc);
+                const int x = ii & (W_ - 1), yc = (ii >> LW) % NYC, j = ii / TPJ;
+                const bool coded = s_nz[j] != 0;
+                u32 f[KW_ / 4];
+#pragma unroll
+                for (int k = 0; k < KW_ / 4; k++) f[k] = fwt[x * L.fwt_ws + k];
+                const pel *po = CORG(JG(j));
+                u32 e = 0;
+#pragma unroll
+                for (int r = 0; r < RY; r++) {
+                    const int y = yc * RY + r;
+                    int rv = JPRED(j)[y * L.ps + x];
+                    if (coded) {
+                        u32 tw[KW_ / 2];
+                        lat_row<KW_ / 2>(JT2(j) + y * L.t2s, tw);
+                        int acc = 0;
+#pragma unroll
+                        for (int k = 0; k < KW_ / 4; k++) {
+                            acc = dp2a_lo(tw[2 * k], f[k], acc);
+                            acc = dp2a_hi(tw[2 * k + 1], f[k], acc);
+                        }
+                        const int res = min(255, max(-256, (acc + 2048) >> 12));
+                        rv = min(255, max(0, rv + res));
                     }
-                    const int r = min(255, max(-256, (acc + 2048) >> 12));
-                    rv = min(255, max(0, rv + r));
+                    const int d = (int)po[y * L.ps + x] - rv;
+                    e += (u32)(d * d);
                 }
-                const int d = (int)CORG(JG(j))[y * L.ps + x] - rv;
-                u32 e = act ? (u32)(d * d) : 0u;
-                e = seg_sum(e, seg, lane);
-                if (act && (lane & (seg - 1)) == 0) atomicAdd(&s_ssd[j], e);
+                if (!act) e = 0;
+                e = lat_seg_sum<SEG>(e, lane);
+                if (act && (lane & (SEG - 1)) == 0) atomicAdd(&s_ssd[j], e);
             }
         }
         __syncthreads();
