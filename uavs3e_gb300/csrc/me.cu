@@ -566,48 +566,61 @@ __device__ __forceinline__ void hpel_winner(const MeSubParams &P, int item, int 
     }
 }
 
+// one row of 8 differences o - p (+ sgn * (o2 - p2) when o2), unpacked
+__device__ __forceinline__ void diff_row8(const pel *o, const pel *p, const pel *o2, const pel *p2, int sgn, int (&v)[8])
+{
+    u32 ol, oh, pl, ph;
+    load8(o, ol, oh);
+    load8(p, pl, ph);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        v[c] = (int)__byte_perm(ol, 0u, 0x4440 + c) - (int)__byte_perm(pl, 0u, 0x4440 + c);
+        v[c + 4] = (int)__byte_perm(oh, 0u, 0x4440 + c) - (int)__byte_perm(ph, 0u, 0x4440 + c);
+    }
+    if (o2) {
+        load8(o2, ol, oh);
+        load8(p2, pl, ph);
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            v[c] += sgn * ((int)__byte_perm(ol, 0u, 0x4440 + c) - (int)__byte_perm(pl, 0u, 0x4440 + c));
+            v[c + 4] += sgn * ((int)__byte_perm(oh, 0u, 0x4440 + c) - (int)__byte_perm(ph, 0u, 0x4440 + c));
+        }
+    }
+}
+
 // magnitude sum of the 2-D WHT of the 8x8 difference org - pred; with o2/p2 the second 8x8
 // half of a 16x8 / 8x16 tile is folded in as first + sgn * second (the first stage of the
-// 16-point transform).  Rows are transformed as they are loaded.
+// 16-point transform).  Rows r and r + 4 travel packed in one register as d[r+4] * 2^16 + d[r]
+// (integer adds and subtracts keep both halves exact: every value stays below 2^15 in
+// magnitude), so the row transforms and the first two column stages run on packed pairs; the
+// last column stage pairs the two halves, where |lo + hi| + |lo - hi| = 2 max(|lo|, |hi|).
 __device__ __noinline__ int satd8x8_raw(const pel *o, int io, const pel *p, int ip, const pel *o2, const pel *p2,
                                            int sgn)
 {
-    int d[64];
+    int P[4][8];
 #pragma unroll
-    for (int r = 0; r < 8; r++) {
-        u32 ol, oh, pl, ph;
-        load8(o + r * io, ol, oh);
-        load8(p + r * ip, pl, ph);
-        int v[8];
+    for (int r = 0; r < 4; r++) {
+        int lo[8], hi[8];
+        diff_row8(o + r * io, p + r * ip, o2 ? o2 + r * io : nullptr, p2 ? p2 + r * ip : nullptr, sgn, lo);
+        diff_row8(o + (r + 4) * io, p + (r + 4) * ip, o2 ? o2 + (r + 4) * io : nullptr,
+                  p2 ? p2 + (r + 4) * ip : nullptr, sgn, hi);
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-            const u32 ow = c < 4 ? ol : oh, pw = c < 4 ? pl : ph;
-            v[c] = (int)((ow >> (8 * (c & 3))) & 255) - (int)((pw >> (8 * (c & 3))) & 255);
-        }
-        if (o2) {
-            load8(o2 + r * io, ol, oh);
-            load8(p2 + r * ip, pl, ph);
-#pragma unroll
-            for (int c = 0; c < 8; c++) {
-                const u32 ow = c < 4 ? ol : oh, pw = c < 4 ? pl : ph;
-                v[c] += sgn * ((int)((ow >> (8 * (c & 3))) & 255) - (int)((pw >> (8 * (c & 3))) & 255));
-            }
-        }
-        wht<8>(v);
-#pragma unroll
-        for (int c = 0; c < 8; c++) d[r * 8 + c] = v[c];
+        for (int c = 0; c < 8; c++) P[r][c] = hi[c] * 65536 + lo[c];
+        wht<8>(P[r]);
     }
     int s = 0;
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-        int col[8];
+        const int b0 = P[0][c] + P[1][c], b1 = P[0][c] - P[1][c];
+        const int b2 = P[2][c] + P[3][c], b3 = P[2][c] - P[3][c];
+        const int q[4] = { b0 + b2, b1 + b3, b0 - b2, b1 - b3 };
 #pragma unroll
-        for (int r = 0; r < 8; r++) col[r] = d[r * 8 + c];
-        wht<8>(col);
-#pragma unroll
-        for (int r = 0; r < 8; r++) s += abs(col[r]);
+        for (int k = 0; k < 4; k++) {
+            const int lo = (int)(short)(q[k] & 0xFFFF), hi = (q[k] - lo) >> 16;
+            s += max(abs(lo), abs(hi));
+        }
     }
-    return s;
+    return 2 * s;
 }
 
 // com_had tile SATD for the ME tile shapes 8x8 / 16x8 / 8x16.  For 16x8 (8x16) the 16-point
@@ -675,7 +688,7 @@ __device__ __forceinline__ u32 sub_tile_satd(const MeSubParams &P, const SubItem
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(256, 2) k_me_sub_eval(MeSubParams P, int n_threads)
+__global__ void __launch_bounds__(256, 3) k_me_sub_eval(MeSubParams P, int n_threads)
 {
     constexpr int NC = STAGE == 1 ? 9 : 8;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_threads; t += gridDim.x * blockDim.x) {
