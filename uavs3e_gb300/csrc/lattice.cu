@@ -36,30 +36,58 @@ __device__ __forceinline__ int lat_class(const LatCu &cu, int W, int H)
     return (ilog2d(w) - 2) * 5 + (ilog2d(h) - 2);
 }
 
+// CUs per thread in the shape-grouping kernels; blocks of 256 threads count in shared memory
+// and touch each global counter once
+constexpr int LAT_GROUP_K = 4;
+
 // counts CUs per shape; a CU outside the supported set gets zeroed outputs here
-__global__ void k_lat_count(const LatCu *cus, int n, int W, int H, int n_qp, int *counts, u32 *satd_out, LatQ *q_out)
+__global__ void __launch_bounds__(256) k_lat_count(const LatCu *cus, int n, int W, int H, int n_qp, int *counts,
+                                                   u32 *satd_out, LatQ *q_out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int c = lat_class(cus[i], W, H);
-    if (c >= 0) {
-        atomicAdd(&counts[c], 1);
-        return;
+    __shared__ int s_cnt[32];
+    if (threadIdx.x < 32) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int k = 0; k < LAT_GROUP_K; k++) {
+        const int i = (blockIdx.x * LAT_GROUP_K + k) * blockDim.x + threadIdx.x;
+        if (i >= n) break;
+        const int c = lat_class(cus[i], W, H);
+        if (c >= 0) {
+            atomicAdd(&s_cnt[c], 1);
+            continue;
+        }
+        for (int m = 0; m < 33; m++) {
+            satd_out[(size_t)i * 33 + m] = 0;
+            for (int q = 0; q < n_qp; q++) q_out[((size_t)i * 33 + m) * n_qp + q] = LatQ{};
+        }
     }
-    for (int m = 0; m < 33; m++) {
-        satd_out[(size_t)i * 33 + m] = 0;
-        for (int q = 0; q < n_qp; q++) q_out[((size_t)i * 33 + m) * n_qp + q] = LatQ{};
-    }
+    __syncthreads();
+    if (threadIdx.x < LAT_SHAPES && s_cnt[threadIdx.x]) atomicAdd(&counts[threadIdx.x], s_cnt[threadIdx.x]);
 }
 
-// lists the CUs of each shape (order within a shape is irrelevant: outputs go by CU index)
-__global__ void k_lat_scatter(const LatCu *cus, int n, int W, int H, const int *offsets, int *cursor, int *perm)
+// lists the CUs of each shape (order within a shape is irrelevant: outputs go by CU index):
+// a block reserves one range per shape, its threads fill it
+__global__ void __launch_bounds__(256) k_lat_scatter(const LatCu *cus, int n, int W, int H, const int *offsets,
+                                                     int *cursor, int *perm)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int c = lat_class(cus[i], W, H);
-    if (c < 0) return;
-    perm[offsets[c] + atomicAdd(&cursor[c], 1)] = i;
+    __shared__ int s_cnt[32], s_base[32];
+    if (threadIdx.x < 32) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    int cls[LAT_GROUP_K], rank[LAT_GROUP_K];
+#pragma unroll
+    for (int k = 0; k < LAT_GROUP_K; k++) {
+        const int i = (blockIdx.x * LAT_GROUP_K + k) * blockDim.x + threadIdx.x;
+        cls[k] = i < n ? lat_class(cus[i], W, H) : -1;
+        rank[k] = cls[k] >= 0 ? atomicAdd(&s_cnt[cls[k]], 1) : 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < LAT_SHAPES && s_cnt[threadIdx.x])
+        s_base[threadIdx.x] = offsets[threadIdx.x] + atomicAdd(&cursor[threadIdx.x], s_cnt[threadIdx.x]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < LAT_GROUP_K; k++) {
+        const int i = (blockIdx.x * LAT_GROUP_K + k) * blockDim.x + threadIdx.x;
+        if (cls[k] >= 0) perm[s_base[cls[k]] + rank[k]] = i;
+    }
 }
 
 size_t lattice_smem_bytes(int w, int h, int nm)
@@ -109,7 +137,7 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     }
     prof_begin(PROF_LATTICE, st);
     UC_CHECK(cudaMemsetAsync(S.counters, 0, 96 * sizeof(int), st));
-    const int nb = (n_cus + 255) / 256;
+    const int nb = (n_cus + 256 * LAT_GROUP_K - 1) / (256 * LAT_GROUP_K);
     k_lat_count<<<nb, 256, 0, st>>>(cus, n_cus, W, H, n_qp, S.counters, satd_out, q_out);
     UC_CHECK(cudaGetLastError());
     UC_CHECK(cudaMemcpyAsync(S.h_counts, S.counters, 32 * sizeof(int), cudaMemcpyDeviceToHost, st));
