@@ -39,7 +39,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--legs", default="me,lattice,pruning",
                     help="comma list of legs: me (the headline line), lattice, pruning")
-    ap.add_argument("--pruning-steps", type=int, default=1500, help="training steps of the pruning leg")
+    ap.add_argument("--pruning-steps", type=int, default=3000, help="training steps of the pruning leg")
     return ap.parse_args()
 
 
@@ -287,8 +287,8 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
     return out
 
 
-def pruning_leg(steps=1500):
-    """the learned CU pruning beside the lattice: trained on the plain path's decisions over 4
+def pruning_leg(steps=3000):
+    """the learned CU pruning beside the lattice: trained on the plain path's decisions over 16
     synthetic 1080p I-frames, evaluated on a held-out frame (RD-cost increase of the pruned
     search, share of the lattice's work it searches, GPU time of the pruned lattice)"""
     from uavs3e_gb300 import cnn

@@ -399,7 +399,7 @@ def pruned_lattice_ms(frame, cus, xy, pred, tau, qp=32):
     return lattice_ms(frame, big, qp) + lattice_ms(frame, small, qp, modes=modes), len(kept)
 
 
-def experiment(train_seeds=range(100, 104), test_seeds=(900,), qp=32, steps=1500, batch=128, taus=(0.8, 0.9),
+def experiment(train_seeds=range(100, 116), test_seeds=(900,), qp=32, steps=3000, batch=128, taus=(0.8, 0.9),
                seed=0, width=1920, height=1080):
     """train on the plain path's decisions over synthetic 1080p I-frames, evaluate on held-out
     frames against the method without the network; one dict of results"""
