@@ -210,6 +210,19 @@ __device__ __forceinline__ u32 lat_seg_sum(u32 v, int lane)
     }
 }
 
+// maximum over aligned groups of SEG lanes
+template <int SEG>
+__device__ __forceinline__ int lat_seg_max(int v, int lane)
+{
+    if constexpr (SEG >= 16) {
+        return seg_max(v, SEG, lane);
+    } else {
+#pragma unroll
+        for (int d = 1; d < SEG; d <<= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, d));
+        return v;
+    }
+}
+
 // com_had tile of a (2^LW) x (2^LH) block (src/com_cost.c:712-812), as constants
 constexpr int lat_tw(int w, int h)
 {
@@ -491,43 +504,48 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
         // first-pass levels, statistics, dequantisation (stored transposed, DQ^T[u][v]).  The
         // level (|c| q_value + 2^(q_bits-1)) >> q_bits is exact in 32 bits: |c| <= 2^15 and
         // q_value < 2^15.
+        // A task is one coefficient row v of a job over RU columns (lanes take consecutive v):
+        // the statistics are summed in registers and reduced once per task.
         {
-            const int E = kw * kh, lE = lkw + lkh, seg = E < 32 ? E : 32;
-            for (int base = wbase; base < (J << lE); base += LAT_THREADS) {
+            constexpr int TPJ = KH_ * NUC, SEG = TPJ < 32 ? TPJ : 32;
+            for (int base = wbase; base < J * TPJ; base += LAT_THREADS) {
                 const int i = base + lane;
-                const bool act = i < (J << lE);
+                const bool act = i < J * TPJ;
                 const int ii = act ? i : base;
-                const int r = ii & (E - 1), j = ii >> lE;
-                const int v = r & (KH_ - 1), u = r >> LKH_;
-                int lev = 0;
-                if (act && (s_flag[j] >> q & 1)) {
-                    const int c = JC(j)[v * L.cs + u];
-                    const int a = c < 0 ? -c : c;
-                    if (a >= thr) {
-                        const int l = (int)(s16)(((u32)a * q_value + qadd) >> q_bits);
-                        lev = c < 0 ? -l : l;
-                    }
-                }
-                int dq = 0;
+                const int v = ii & (KH_ - 1), uc = (ii >> LKH_) % NUC, j = ii / TPJ;
+                const bool coded = act && (s_flag[j] >> q & 1);
                 u32 nz = 0, sa = 0, hs = 0;
                 int last = -1;
-                if (lev) {
-                    const int pos = v * w + u;
-                    nz = 1;
-                    sa = (u32)(lev < 0 ? -lev : lev);
-                    hs = fmix32(((u32)pos << 16) | (u16)(s16)lev);
-                    last = (int)s_scan[v * KW_ + u];
-                    int d = (lev * dq_scale + dq_off) >> dq_shift;
-                    d = min(32767, max(-32768, d));
-                    dq = odd ? (d * 181 + 128) >> 8 : d;
+#pragma unroll
+                for (int r = 0; r < RU; r++) {
+                    const int u = uc * RU + r;
+                    int lev = 0;
+                    if (coded) {
+                        const int c = JC(j)[v * L.cs + u];
+                        const int a = c < 0 ? -c : c;
+                        if (a >= thr) {
+                            const int l = (int)(s16)(((u32)a * q_value + qadd) >> q_bits);
+                            lev = c < 0 ? -l : l;
+                        }
+                    }
+                    int dq = 0;
+                    if (lev) {
+                        nz++;
+                        sa += (u32)(lev < 0 ? -lev : lev);
+                        hs += fmix32(((u32)(v * w + u) << 16) | (u16)(s16)lev);
+                        last = max(last, (int)s_scan[v * KW_ + u]);
+                        int d = (lev * dq_scale + dq_off) >> dq_shift;
+                        d = min(32767, max(-32768, d));
+                        dq = odd ? (d * 181 + 128) >> 8 : d;
+                    }
+                    if (act) JDQT(j)[u * L.ds + v] = (s16)dq;
                 }
-                if (act) JDQT(j)[u * L.ds + v] = (s16)dq;
-                nz = seg_sum(nz, seg, lane);
                 if (__any_sync(0xFFFFFFFFu, nz != 0)) {
-                    sa = seg_sum(sa, seg, lane);
-                    hs = seg_sum(hs, seg, lane);
-                    last = seg_max(last, seg, lane);
-                    if (act && (lane & (seg - 1)) == 0 && nz) {
+                    nz = lat_seg_sum<SEG>(nz, lane);
+                    sa = lat_seg_sum<SEG>(sa, lane);
+                    hs = lat_seg_sum<SEG>(hs, lane);
+                    last = lat_seg_max<SEG>(last, lane);
+                    if (act && (lane & (SEG - 1)) == 0 && nz) {
                         atomicAdd(&s_nz[j], nz);
                         atomicAdd(&s_sum[j], sa);
                         atomicAdd(&s_hash[j], hs);
