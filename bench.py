@@ -47,6 +47,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(value, world, device):
+    """the largest of every rank's value (replicas: the job's time is its slowest rank's)"""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank):
+    """each replica searches its own synthetic sequence"""
+    return 1000 * rank
+
+
 def workload_config():
     from uavs3e_gb300.synth import lambda_mv_for_qp
     ctus = ((W + 63) // 64) * ((H + 63) // 64)
@@ -312,7 +328,7 @@ def run_ours(args):
     u.build()
     u.init(local)
     lam = lambda_mv_for_qp(QP)
-    frames = frames_ring(seed=rank)
+    frames = frames_ring(seed=replica_seed(rank))
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     d_frames = [torch.from_numpy(f).cuda() for f in frames]
@@ -353,10 +369,8 @@ def run_ours(args):
     prof = u.profile_collect()
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_s = sum(step_ms) / 1000.0
+    total_s = max_over_ranks(total_s, world, "cuda")
     if world > 1:
-        tt = torch.tensor([total_s], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(tt.item())
         torch.distributed.barrier()
     value = world * args.steps / total_s
 
@@ -378,11 +392,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     for k in range(e2e_steps):
         e2e_step(4 + k)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
 
     if rank != 0:
         if world > 1:
