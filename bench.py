@@ -37,8 +37,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="me,lattice,pruning",
-                    help="comma list of legs: me (the headline line), lattice, pruning")
+    ap.add_argument("--legs", default="me,lattice,pruning,lookahead",
+                    help="comma list of legs: me (the headline line), lattice, pruning, lookahead")
     ap.add_argument("--pruning-steps", type=int, default=3000, help="training steps of the pruning leg")
     return ap.parse_args()
 
@@ -303,6 +303,131 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
     return out
 
 
+LOKA_PAD = 144
+
+
+def loka_pictures(seed=21):
+    """the lookahead leg's pictures: POC 0, 7, 8, 16 of the 1080p motion sequence (pan
+    (+3.25, -1.5) per frame), chroma = 2x-downsampled luma offset by +16 / -16"""
+    import numpy as np
+    from uavs3e_gb300.synth import motion_sequence
+    seq = motion_sequence(W, H, 17, seed=seed)
+    pics = {}
+    for t in (0, 7, 8, 16):
+        y = seq[t]
+        c = y.reshape(H // 2, 2, W // 2, 2).astype(np.int32).mean((1, 3)).astype(np.int32)
+        pics[t] = (y, np.clip(c + 16, 0, 255).astype(np.uint8), np.clip(c - 16, 0, 255).astype(np.uint8))
+    return pics
+
+
+def loka_padded(y):
+    import numpy as np
+    s = W + 2 * LOKA_PAD
+    return np.pad(y, LOKA_PAD, mode="edge").reshape(H + 2 * LOKA_PAD, s)
+
+
+def lookahead_leg(u, torch, stream, flush, sm_count, sm_mhz, with_cpu, reps=20):
+    """loka_estimate_coding_cost of a 1080p picture: the encoder's picture-level estimate of
+    POC 8 in a random-access GOP of 16 (references POC 0 in list 0 and POC 16 in list 1, padded,
+    search range 384) and the lookahead's scene-cut estimate of POC 8 against POC 7 (no padding,
+    search range 64).  Device path timed with CUDA events (L2 flushed before each call), the
+    host-buffer entry point end to end."""
+    import numpy as np
+    pics = loka_pictures()
+    lib = u.lib()
+    n_units = (W // 16) * (H // 16)
+    sp = stream.cuda_stream
+    confs = {
+        "encoder_ra_bi": (u.loka_cfg(W, H, 1, 384, 16, 8, [0], [16]), [0], [16]),
+        "scenecut": (u.loka_cfg(W, H, 0, 64, 16, 8, [7], []), [7], []),
+    }
+    y, cu, cv = pics[8]
+    d_y, d_u, d_v = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (y, cu, cv))
+    d_units = torch.empty(n_units * u.LOKA_UNIT.itemsize, dtype=torch.uint8, device="cuda")
+    d_energy = torch.empty(n_units, dtype=torch.int64, device="cuda")
+    d_tot = torch.empty(5, dtype=torch.int64, device="cuda")
+    _, sad_clk = u.measure_sad4_rate()
+    int_peak = max(sad_clk, 64.0) * sm_count * sm_mhz * 1e6 / 1e9
+    out = {"workload": "lookahead cost estimation (loka_estimate_coding_cost) of a 1080p 4:2:0 picture: "
+                       f"{n_units} 16x16 units, integer TZ search per reference + uni/bi SATD + 11 intra modes + "
+                       "chroma SATD + dQP energy", "units": n_units}
+    for name, (cfg, l0, l1) in confs.items():
+        padded = {t: loka_padded(pics[t][0]) for t in l0 + l1}
+        d_ref = {t: torch.from_numpy(padded[t]).cuda() for t in padded}
+        off = LOKA_PAD * (W + 2 * LOKA_PAD) + LOKA_PAD
+        i_ref = W + 2 * LOKA_PAD
+
+        def run():
+            u.loka_units_device(cfg, d_y.data_ptr(), W, d_u.data_ptr(), d_v.data_ptr(), W // 2,
+                                [d_ref[t].data_ptr() + off for t in l0], [d_ref[t].data_ptr() + off for t in l1],
+                                i_ref, LOKA_PAD, d_units.data_ptr(), d_energy.data_ptr(), d_tot.data_ptr(), sp)
+
+        for _ in range(3):
+            run()
+        torch.cuda.synchronize()
+        l0c = u.launch_count()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            run()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        launches = (u.launch_count() - l0c) / reps
+        ms = sum(a.elapsed_time(b) for a, b in evs) / reps
+        sads = int(d_tot.cpu().numpy().view(np.uint64)[4])
+        # end to end: host planes (pinned) in, the reference's outputs back
+        pin_y, pin_u, pin_v = (torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (y, cu, cv))
+        pin_r = {t: torch.from_numpy(padded[t]).pin_memory() for t in padded}
+        cfg_c = np.ascontiguousarray(cfg)
+        import ctypes as C
+        a0 = (C.c_void_p * 4)(*([pin_r[t].data_ptr() + off for t in l0] + [None] * (4 - len(l0))))
+        a1 = (C.c_void_p * 4)(*([pin_r[t].data_ptr() + off for t in l1] + [None] * (4 - len(l1))))
+        cost, icost = C.c_double(), C.c_double()
+        uv = (C.c_double * 2)()
+        dqp = np.zeros(n_units, np.float32)
+
+        def e2e():
+            u.check(lib.uavs3e_cuda_loka_estimate(cfg_c.ctypes.data, pin_y.data_ptr(), W, pin_u.data_ptr(),
+                                                  pin_v.data_ptr(), W // 2, a0, a1, i_ref, LOKA_PAD, C.byref(cost),
+                                                  C.byref(icost), uv, dqp.ctypes.data, None), "loka_estimate")
+
+        for _ in range(3):
+            e2e()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            e2e()
+        e2e_ms = (time.perf_counter() - t0) * 1000.0 / reps
+        ops = sads * 64.0                     # 16x16 SAD = 64 four-sample vabsdiff4 operations
+        # the padded search copies each reference with its padding, the other one the picture only
+        ref_bytes = (W + 2 * LOKA_PAD) * (H + 2 * LOKA_PAD) if cfg["is_padding"][0] else W * H
+        r = {"ms_per_picture": ms, "pictures_per_s": 1000.0 / ms, "units_per_s": n_units / (ms / 1000.0),
+             "gpu_launches_per_picture": launches, "sad16_evaluations": sads,
+             "e2e": {"ms_per_picture": e2e_ms, "pictures_per_s": 1000.0 / e2e_ms,
+                     "h2d_bytes": int(W * H * 3 // 2 + len(padded) * ref_bytes),
+                     "d2h_bytes": int(5 * 8 + n_units * 8),
+                     "path": "uavs3e_cuda_loka_estimate on pinned host planes (cost, icost, icost_uv, map_dqp)"},
+             "picture_cost": cost.value, "icost": icost.value,
+             "roofline": {"bound": "int", "kernel": "k_loka_search + k_loka_unit (SAD work of the searches only)",
+                          "achieved": ops / (ms / 1000.0) / 1e9, "peak": int_peak, "unit": "Gop/s",
+                          "frac": ops / (ms / 1000.0) / 1e9 / int_peak,
+                          "peak_source": f"vabsdiff4.add rate max(measured {sad_clk:.1f}, 64)/clk/SM x {sm_count} "
+                                         f"SMs x {sm_mhz:.0f} MHz"}}
+        if with_cpu:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import pyoracle
+            o = pyoracle.Oracle()
+            threads = os.cpu_count() or 1
+            refs_addr = [[padded[t].ctypes.data + off for t in lst] for lst in (l0, l1)]
+            t0 = time.perf_counter()
+            o.loka_units(cfg, y, W, cu, cv, W // 2, refs_addr[0], refs_addr[1], i_ref, threads)
+            dt = time.perf_counter() - t0
+            r["cpu_baseline"] = {"value": 1.0 / dt, "unit": "pictures/s", "cores": threads, "kind": "port",
+                                 "sample": f"the whole picture through the oracle restatement, {dt:.2f} s"}
+        out[name] = r
+    return out
+
+
 def pruning_leg(steps=3000):
     """the learned CU pruning beside the lattice: trained on the plain path's decisions over 16
     synthetic 1080p I-frames, evaluated on a held-out frame (RD-cost increase of the pruned
@@ -448,6 +573,8 @@ def run_ours(args):
     legs = set(args.legs.split(","))
     lattice = lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, not args.no_cpu) if "lattice" in legs else None
     pruning = pruning_leg(args.pruning_steps) if "pruning" in legs else None
+    lookahead = (lookahead_leg(u, torch, stream, flush, sm_count, sm_mhz, not args.no_cpu)
+                 if "lookahead" in legs else None)
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -466,6 +593,7 @@ def run_ours(args):
         "roofline_hbm": roofline_hbm,
         "lattice": lattice,
         "pruning": pruning,
+        "lookahead": lookahead,
         "clocks": clk,
     }
     if not args.no_cpu:
@@ -497,6 +625,9 @@ def run_legs(args):
                                      not args.no_cpu)
     if "pruning" in legs:
         out["pruning"] = pruning_leg(args.pruning_steps)
+    if "lookahead" in legs:
+        out["lookahead"] = lookahead_leg(u, torch, torch.cuda.current_stream(), flush, sm_count, sm_mhz,
+                                         not args.no_cpu)
     print(json.dumps(out))
 
 

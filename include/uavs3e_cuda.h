@@ -223,6 +223,80 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_modes_device(const uint8_t *d_org,
                                                            const int *qps, int n_qp, int is_intra_slice,
                                                            uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream);
 
+/* ------------------------------------------------------------ lookahead cost estimation */
+
+/*
+ * loka_estimate_coding_cost (src/lookahead.c:82-293, declared inc/lookahead.h:51) for a whole
+ * picture: for every 16x16 unit (raster order over (width/16) x (height/16)) and every
+ * reference, the integer search of me_search_tz (src/me.c:529-568) with the estimate's
+ * settings (integer resolution, predictor (0,0), lambda of QP 32, no bi-prediction search),
+ * the com_had SATD of the block it finds, the SATD of the two bi-prediction averages, the 11
+ * intra modes predicted from the original picture (get_ipred_neighbor, src/lookahead.c:40),
+ * the chroma SATD with the best intra mode and the unit's cost_var energy.
+ *   cfg        : what the reference reads from inter_search_t and the pictures: size,
+ *                is_padding (1 = the encoder's picture-level search, src/uavs3e.c:185/929, whose
+ *                references are padded by PIC_PAD_SIZE_L = 144; 0 = the lookahead's scene-cut
+ *                estimate, src/uavs3e.c:1326/1257, whose MVs keep the unit inside the picture),
+ *                max_search_range (SEARCH_RANGE_IPEL_LD 64 or _RA 384), gop_size, the reference
+ *                counts per list (<= 4) and the POCs of the picture and its references;
+ *   org planes : the picture's Y (W x H) and U, V (W/2 x H/2) planes;
+ *   references : luma planes, pointers to sample (0,0), stride i_ref (a multiple of 4), readable
+ *                ref_pad samples around the picture (>= 144 when is_padding, else >= 4).
+ */
+#define UAVS3E_CUDA_LOKA_MAX_REFS 4
+
+typedef struct {
+    int     width, height;
+    int     is_padding;
+    int     max_search_range;
+    int     gop_size;
+    int     num_ref[2];
+    int64_t ptr;
+    int64_t ref_ptr[2][UAVS3E_CUDA_LOKA_MAX_REFS];
+} uavs3e_cuda_loka_cfg_t;
+
+typedef struct {
+    int16_t  mv[2][UAVS3E_CUDA_LOKA_MAX_REFS][2];   /* integer MV per list / reference      */
+    uint32_t satd[2][UAVS3E_CUDA_LOKA_MAX_REFS];    /* com_had at that MV                   */
+    uint32_t bi_satd;     /* average of the two list winners (pictures with both lists)       */
+    uint32_t zero_satd;   /* average of the (0,0) blocks of ref_l0[0] and ref_l1[0]           */
+    uint32_t min_cost;    /* smallest inter or intra cost: the unit's share of picture_satd   */
+    uint32_t min_icost;   /* smallest intra cost                                              */
+    uint32_t icost_u, icost_v;
+    uint64_t energy;      /* cost_var of Y 16x16 + U 8x8 + V 8x8                              */
+    uint8_t  best_mode, pad[7];
+} uavs3e_cuda_loka_unit_t;
+
+/* The whole call on host buffers, synchronous.  Writes the return value of
+ * loka_estimate_coding_cost to *cost and, where the pointers are not NULL, icost, icost_uv[2],
+ * map_dqp[units] (the reference's outputs) and the unit records. */
+UAVS3E_CUDA_API int uavs3e_cuda_loka_estimate(const uavs3e_cuda_loka_cfg_t *cfg, const uint8_t *org_y, int i_org,
+                                              const uint8_t *org_u, const uint8_t *org_v, int i_org_c,
+                                              const uint8_t *const *ref_l0, const uint8_t *const *ref_l1, int i_ref,
+                                              int ref_pad, double *cost, double *icost, double icost_uv[2],
+                                              float *map_dqp, uavs3e_cuda_loka_unit_t *units);
+/* loka_get_sc_ratio (src/lookahead.c:378-386): the estimate against the previous picture
+ * alone, P cost / intra cost. */
+UAVS3E_CUDA_API int uavs3e_cuda_loka_sc_ratio(int width, int height, int is_padding, int max_search_range,
+                                              int gop_size, int64_t ptr, const uint8_t *org_y, int i_org,
+                                              const uint8_t *org_u, const uint8_t *org_v, int i_org_c,
+                                              const uint8_t *last_y, int64_t last_ptr, int i_last, int last_pad,
+                                              double *ratio);
+/* Device buffers in and out, enqueued on `stream`: d_units[units], d_energy[units] (the energies
+ * again, contiguous), d_totals[5] = sums of min_cost, min_icost, icost_u, icost_v and the number
+ * of 16x16 SADs the searches evaluated.  ref pointer arrays are host arrays of device pointers. */
+UAVS3E_CUDA_API int uavs3e_cuda_loka_units_device(const uavs3e_cuda_loka_cfg_t *cfg, const uint8_t *d_org_y,
+                                                  int i_org, const uint8_t *d_org_u, const uint8_t *d_org_v,
+                                                  int i_org_c, const uint8_t *const *d_ref_l0,
+                                                  const uint8_t *const *d_ref_l1, int i_ref, int ref_pad,
+                                                  uavs3e_cuda_loka_unit_t *d_units, uint64_t *d_energy,
+                                                  uint64_t *d_totals, void *stream);
+/* The reference's picture-level results from the totals (host copy) and, for map_dqp, the
+ * energies (host copy): returns the picture cost. */
+UAVS3E_CUDA_API double uavs3e_cuda_loka_finish(const uavs3e_cuda_loka_cfg_t *cfg, const uint64_t totals[4],
+                                               const uint64_t *energy, double *icost, double icost_uv[2],
+                                               float *map_dqp);
+
 /* ---------------------------------------------------------------------------------------
  * Learned CU-partition / intra-mode pruning network (no counterpart in the reference: the
  * learned part stands beside the bit-exact path and never changes it).  bf16 tensor-core

@@ -1216,3 +1216,260 @@ void orc_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, int
     (void)threads;
     free(coded);
 }
+
+/* ============================================================ batched: lookahead cost */
+
+/* One motion search of loka_estimate_coding_cost: me_search_tz (src/me.c:529-568) on a 16x16
+ * unit at integer resolution (curr_mvr 2), predictor (0,0), no bi-prediction, so the MV-bits
+ * lookup GET_MVBITS_IPEL_* (inc/util.h:43-44) indexes the table with the integer MV itself. */
+typedef struct {
+    const pel *org; int i_org;          /* unit origin in the current picture            */
+    const pel *ref; int i_ref;          /* co-located sample of the reference plane      */
+    int minx, maxx, miny, maxy;         /* get_max_search_range, src/me.c:502-527        */
+    u32 lambda;                         /* lambda_mv                                     */
+    const u8 *bits;                     /* MV-bits table centre                          */
+    u64 best; int mvx, mvy;             /* running best cost and MV                      */
+} tz_ctx_t;
+
+static u64 tz_cost(const tz_ctx_t *c, int mx, int my)
+{
+    u32 sad = orc_sad(16, 16, c->org, c->i_org, c->ref + my * c->i_ref + mx, c->i_ref);
+    return ((u64)sad << 16) + (u64)((u32)(c->bits[mx] + c->bits[my]) * c->lambda);
+}
+
+static void tz_try(tz_ctx_t *c, int mx, int my, int *improved)
+{
+    u64 cost = tz_cost(c, mx, my);
+    if (cost < c->best) { c->best = cost; c->mvx = mx; c->mvy = my; if (improved) *improved = 1; }
+}
+
+/* search_diamond with bi = 0 (src/me.c:199-334): the centre, the 5x5 core square (its edges
+ * kept strictly inside the MV range, :240-243), then diamond rings of step 4, 8, 16 below
+ * max_step (4 points at step 4, 8 at step 8, 16 at step 16, :307-331).  Returns the step of the
+ * last ring point that improved the cost, else 2 if the core square moved the MV, else 0. */
+static int tz_diamond(tz_ctx_t *c, int max_step)
+{
+    static const s8 RING_A[8][2] = { { -2, 0 }, { -1, 1 }, { 0, 2 }, { 1, 1 },
+                                     { 2, 0 }, { 1, -1 }, { 0, -2 }, { -1, -1 } };
+    static const s8 RING_B[16][2] = { { -4, 0 }, { -3, 1 }, { -2, 2 }, { -1, 3 }, { 0, 4 }, { 1, 3 },
+                                      { 2, 2 }, { 3, 1 }, { 4, 0 }, { 3, -1 }, { 2, -2 }, { 1, -3 },
+                                      { 0, -4 }, { -1, -3 }, { -2, -2 }, { -3, -1 } };
+    const int cx = c->mvx, cy = c->mvy;
+    int best_step = 0;
+    tz_try(c, cx, cy, NULL);
+    int x0 = MAX(cx - 2, c->minx + 1), x1 = MIN(cx + 2, c->maxx - 1);
+    int y0 = MAX(cy - 2, c->miny + 1), y1 = MIN(cy + 2, c->maxy - 1);
+    for (int my = y0; my <= y1; my++)
+        for (int mx = x0; mx <= x1; mx++) tz_try(c, mx, my, NULL);
+    if (c->mvx != cx || c->mvy != cy) best_step = 2;
+    for (int step = 4, round = 0; step < max_step; step <<= 1, round++) {
+        const s8(*ring)[2] = round < 2 ? RING_A : RING_B;
+        int n = round < 2 ? 8 : 16, inc = round == 0 ? 2 : 1;
+        int scale = round < 2 ? step >> 1 : step >> 2;
+        for (int i = 0; i < n; i += inc) {
+            int mx = cx + scale * ring[i][0], my = cy + scale * ring[i][1];
+            if (mx < c->minx || mx > c->maxx || my < c->miny || my > c->maxy) continue;
+            int imp = 0;
+            tz_try(c, mx, my, &imp);
+            if (imp) best_step = step;
+        }
+    }
+    return best_step;
+}
+
+/* search_raster with adaptive_raster_range 0 (src/me.c:103-197, get_raster_range :65-100):
+ * a grid of step 8 * (refi + 1) over [mv - range, mv + range] (clipped), then grids of the
+ * halved step over [mv - step, mv + step] around the running best until the step is 1.
+ * Each grid starts at its clipped lower corner. */
+static void tz_raster(tz_ctx_t *c, int refi, int range)
+{
+    int step = MAX(5, 16 >> 1) * (refi + 1);
+    int x0 = CLIP3(c->minx, c->maxx, c->mvx - range), x1 = CLIP3(c->minx, c->maxx, c->mvx + range);
+    int y0 = CLIP3(c->miny, c->maxy, c->mvy - range), y1 = CLIP3(c->miny, c->maxy, c->mvy + range);
+    for (int round = 0; step >= 1; round++, step >>= 1) {
+        if (round) {
+            x0 = MAX(c->mvx - step, c->minx); x1 = MIN(c->mvx + step, c->maxx);
+            y0 = MAX(c->mvy - step, c->miny); y1 = MIN(c->mvy + step, c->maxy);
+        }
+        for (int my = y0; my <= y1; my += step)
+            for (int mx = x0; mx <= x1; mx += step) tz_try(c, mx, my, NULL);
+    }
+}
+
+/* get_ipred_neighbor, src/lookahead.c:40-80: neighbours of a w x h block taken from the
+ * ORIGINAL picture -- 2w above and 2h to the left (cut at the picture edge, then the last
+ * sample repeated up to 4 * max(w, h) + 4), the corner, 1 << (bd - 1) where unavailable */
+static void loka_nbr(pel *nb, int x, int y, int w, int h, int W, int H, const pel *src, int s)
+{
+    pel *c = nb + ORC_NEIB_MID;
+    int range = MAX(w, h) * 4 + 4, dflt = 128;
+    if (y) {
+        int n = MIN(2 * w, W - x);
+        for (int i = 0; i < range; i++) c[1 + i] = src[-s + MIN(i, n - 1)];
+    } else {
+        for (int i = 0; i < range; i++) c[1 + i] = (pel)dflt;
+    }
+    if (x) {
+        int n = MIN(2 * h, H - y);
+        for (int i = 0; i < range; i++) c[-1 - i] = src[MIN(i, n - 1) * s - 1];
+    } else {
+        for (int i = 0; i < range; i++) c[-1 - i] = (pel)dflt;
+    }
+    c[0] = (x && y) ? src[-s - 1] : y ? src[-s] : x ? src[-1] : (pel)dflt;
+}
+
+/* cost_var (DEFINE_VAR, src/com_cost.c:139-151): sum of squares - (sum^2 >> 2 log2 n) */
+static u64 loka_var(const pel *p, int s, int n)
+{
+    u64 sum = 0, sq = 0;
+    for (int y = 0; y < n; y++, p += s)
+        for (int x = 0; x < n; x++) { sum += p[x]; sq += (u64)(p[x] * p[x]); }
+    return sq - ((sum * sum) >> (2 * ilog2(n)));
+}
+
+static void loka_unit(const orc_loka_cfg_t *cfg, const pel *org_y, int i_org, const pel *org_u, const pel *org_v,
+                      int i_org_c, const pel *const *refs[2], int i_ref, const u8 *bits, u32 lambda,
+                      int ux, int uy, orc_loka_unit_t *u)
+{
+    static const u8 IPM[11] = { 0, 1, 2, 4, 8, 12, 16, 20, 24, 28, 32 };   /* src/lookahead.c:213 */
+    const int W = cfg->width, H = cfg->height, x = ux * 16, y = uy * 16;
+    const int is_bi = cfg->num_ref[0] && cfg->num_ref[1];
+    const pel *org = org_y + y * i_org + x;
+    pel pred[256], best_pred[2][256];
+    memset(u, 0, sizeof(*u));
+
+    /* get_max_search_range (src/me.c:502-527) for mvp 0, mvr 2 */
+    int mto = (MAX(W, H) << 2) + 3;
+    tz_ctx_t c;
+    c.org = org; c.i_org = i_org; c.i_ref = i_ref; c.lambda = lambda; c.bits = bits;
+    if (cfg->is_padding) {
+        c.minx = MAX(-128 + 1 - x, -mto + 4); c.miny = MAX(-128 + 1 - y, -mto + 4);
+        c.maxx = MIN(W - 1 - x, mto - 4);     c.maxy = MIN(H - 1 - y, mto - 4);
+    } else {
+        c.minx = MAX(-x, -mto + 4);           c.miny = MAX(-y, -mto + 4);
+        c.maxx = MIN(W - 1 - x - 16, mto - 4); c.maxy = MIN(H - 1 - y - 16, mto - 4);
+    }
+    int max_sr = cfg->max_search_range >> 1;
+
+    u64 min_cost = ~(u64)0;
+    for (int l = 0; l < 2; l++) {
+        u64 min_dir = ~(u64)0;
+        for (int r = 0; r < cfg->num_ref[l]; r++) {
+            int dist = (int)(cfg->ptr - cfg->ref_ptr[l][r]);
+            dist = ABSI(dist);
+            int range = CLIP3(max_sr >> 2, max_sr, (max_sr * dist + (cfg->gop_size >> 1)) / cfg->gop_size);
+            c.ref = refs[l][r] + y * i_ref + x;
+            c.best = ~(u64)0;
+            c.mvx = CLIP3(c.minx, c.maxx, 0); c.mvy = CLIP3(c.miny, c.maxy, 0);
+            int bs = tz_diamond(&c, 32);
+            if (c.mvx || c.mvy) {
+                if (bs > 5) tz_raster(&c, r, range);
+                tz_diamond(&c, 8);
+            }
+            u->mv[l][r][0] = (s16)c.mvx; u->mv[l][r][1] = (s16)c.mvy;
+            /* com_mc_blk_luma at an integer MV inside [-MAX_CU_SIZE-4, max_coord]: a copy */
+            const pel *blk = c.ref + c.mvy * i_ref + c.mvx;
+            u32 cost = orc_had(16, 16, org, i_org, blk, i_ref, 8);
+            u->satd[l][r] = cost;
+            if (cost < min_dir) {
+                min_dir = cost;
+                if (cost < min_cost) min_cost = cost;
+                if (is_bi) orc_ipcpy(blk, i_ref, best_pred[l], 16, 16, 16);
+            }
+        }
+    }
+    if (is_bi) {
+        orc_pel_avrg(16, 16, pred, 16, best_pred[0], best_pred[1]);
+        u->bi_satd = orc_had(16, 16, org, i_org, pred, 16, 8);
+        if (u->bi_satd < min_cost) min_cost = u->bi_satd;
+        const pel *z0 = refs[0][0] + y * i_ref + x, *z1 = refs[1][0] + y * i_ref + x;
+        pel a[256], b[256];
+        orc_ipcpy(z0, i_ref, a, 16, 16, 16);
+        orc_ipcpy(z1, i_ref, b, 16, 16, 16);
+        orc_pel_avrg(16, 16, pred, 16, a, b);
+        u->zero_satd = orc_had(16, 16, org, i_org, pred, 16, 8);
+        if (u->zero_satd < min_cost) min_cost = u->zero_satd;
+    }
+
+    /* intra: 11 modes predicted from the original picture's neighbours (:208-230) */
+    pel nb[ORC_NEIB_SIZE];
+    loka_nbr(nb, x, y, 16, 16, W, H, org, i_org);
+    int avail = (x ? 2 : 0) | (y ? 1 : 0) | ((x && y) ? 4 : 0);
+    u32 min_icost = 0xFFFFFFFFu;
+    int best_mode = 0;
+    for (int i = 0; i < 11; i++) {
+        orc_intra_pred(nb, pred, IPM[i], 16, 16, 8, avail, 0);
+        u32 cost = orc_had(16, 16, org, i_org, pred, 16, 8);
+        if (cost < min_cost) min_cost = cost;
+        if (cost < min_icost) { min_icost = cost; best_mode = IPM[i]; }
+    }
+    u->min_cost = (u32)min_cost;
+    u->min_icost = min_icost;
+    u->best_mode = (u8)best_mode;
+
+    /* chroma with the best luma mode (:231-243) and the energy of the dQP map (:248-262) */
+    int xc = x >> 1, yc = y >> 1;
+    const pel *ou = org_u + yc * i_org_c + xc, *ov = org_v + yc * i_org_c + xc;
+    loka_nbr(nb, xc, yc, 8, 8, W / 2, H / 2, ou, i_org_c);
+    orc_intra_pred(nb, pred, best_mode, 8, 8, 8, avail, 0);
+    u->icost_u = orc_had(8, 8, ou, i_org_c, pred, 8, 8);
+    loka_nbr(nb, xc, yc, 8, 8, W / 2, H / 2, ov, i_org_c);
+    orc_intra_pred(nb, pred, best_mode, 8, 8, 8, avail, 0);
+    u->icost_v = orc_had(8, 8, ov, i_org_c, pred, 8, 8);
+    u->energy = loka_var(org, i_org, 16) + loka_var(ou, i_org_c, 8) + loka_var(ov, i_org_c, 8);
+}
+
+/* lambda_mv of the estimation: base QP 32 (src/lookahead.c:85-106) */
+static u32 loka_lambda(void)
+{
+    double base_lambda = 1.43631 * pow(2.0, (32 - 16.0) / 4.0);
+    return (u32)floor(65536.0 * sqrt(base_lambda));
+}
+
+void orc_loka_units(const orc_loka_cfg_t *cfg, const pel *org_y, int i_org, const pel *org_u, const pel *org_v,
+                    int i_org_c, const pel *const *ref_l0, const pel *const *ref_l1, int i_ref,
+                    orc_loka_unit_t *units, int threads)
+{
+    int nux = cfg->width / 16, nuy = cfg->height / 16;
+    int off = (MAX(cfg->width, cfg->height) << 2) + 3;
+    u8 *tab = (u8 *)malloc((size_t)(2 * off + 1));
+    orc_mvbits_table(tab, off);
+    const pel *const *refs[2] = { ref_l0, ref_l1 };
+    u32 lambda = loka_lambda();
+#ifdef _OPENMP
+    if (threads < 1) threads = 1;
+    #pragma omp parallel for schedule(dynamic, 8) num_threads(threads)
+#endif
+    for (int i = 0; i < nux * nuy; i++)
+        loka_unit(cfg, org_y, i_org, org_u, org_v, i_org_c, refs, i_ref, tab + off, lambda, i % nux, i / nux,
+                  &units[i]);
+    (void)threads;
+    free(tab);
+}
+
+/* src/lookahead.c:201-292: totals accumulated in double in raster order, averages per sample,
+ * the dQP map as 0.8 log2(energy) minus its mean */
+double orc_loka_finish(const orc_loka_cfg_t *cfg, const orc_loka_unit_t *units, double *icost, double *icost_uv,
+                       float *map_dqp)
+{
+    int n = (cfg->width / 16) * (cfg->height / 16);
+    double tc = 0, ti = 0, tu = 0, tv = 0, tvar = 0;
+    for (int i = 0; i < n; i++) {
+        tc += units[i].min_cost;
+        ti += units[i].min_icost;
+        tu += units[i].icost_u;
+        tv += units[i].icost_v;
+        if (map_dqp) {
+            u64 e = units[i].energy;
+            map_dqp[i] = (float)(0.8 * log2((double)MAX(e, 1)));
+            tvar += map_dqp[i];
+        }
+    }
+    if (icost) *icost = ti / n / 16 / 16;
+    if (icost_uv) { icost_uv[0] = tu / n / 8 / 8; icost_uv[1] = tv / n / 8 / 8; }
+    if (map_dqp) {
+        float avg = (float)(tvar / n);
+        for (int i = 0; i < n; i++) map_dqp[i] -= avg;
+    }
+    return tc / n / 16 / 16;
+}

@@ -140,6 +140,46 @@ void orc_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, int
 /* level hash used by the lattice: sum over non-zero levels of fmix32(pos << 16 | (u16)level) */
 u32 orc_level_hash(const s16 *lev, int n);
 
+/* ------------- lookahead cost estimation (loka_estimate_coding_cost, src/lookahead.c:82) ------------- */
+
+#define ORC_LOKA_MAX_REFS 4             /* MAX_NUM_ACTIVE_REF_FRAME, inc/com_define.h:297 */
+
+/* the picture-level inputs of one call: the inter_search_t fields its search reads
+ * (inter_search_init, src/inter.c:2015) and the POCs that set the raster range */
+typedef struct {
+    int width, height;                  /* luma picture size                                   */
+    int is_padding;                     /* 1: references padded by >= 144 samples (encoder);  */
+                                        /* 0: MVs keep the unit inside the picture (lookahead) */
+    int max_search_range;               /* 64 (low delay) or 384 (random access)               */
+    int gop_size;
+    int num_ref[2];                     /* references per list (<= ORC_LOKA_MAX_REFS)         */
+    s64 ptr;                            /* POC of the current picture                          */
+    s64 ref_ptr[2][ORC_LOKA_MAX_REFS];  /* POC of each reference                               */
+} orc_loka_cfg_t;
+
+/* per 16x16 unit (raster order over (width/16) x (height/16)) */
+typedef struct {
+    s16 mv[2][ORC_LOKA_MAX_REFS][2];    /* integer MV found by me_search_tz per list/ref       */
+    u32 satd[2][ORC_LOKA_MAX_REFS];     /* com_had of the block at that MV                     */
+    u32 bi_satd;                        /* average of the two list winners (bi pictures)       */
+    u32 zero_satd;                      /* average of the (0,0) blocks of ref_l0[0], ref_l1[0] */
+    u32 min_cost;                       /* min over the inter and intra costs                  */
+    u32 min_icost;                      /* min over the 11 intra modes                         */
+    u32 icost_u, icost_v;               /* 8x8 chroma SATD with the best luma mode             */
+    u64 energy;                         /* cost_var of Y 16x16 + U 8x8 + V 8x8                 */
+    u8  best_mode, pad[7];
+} orc_loka_unit_t;
+
+/* every unit's record; ref_l0/ref_l1 point at sample (0,0) of each reference luma plane
+ * (stride i_ref).  Uses OpenMP over units when threads > 1. */
+void orc_loka_units(const orc_loka_cfg_t *cfg, const pel *org_y, int i_org, const pel *org_u, const pel *org_v,
+                    int i_org_c, const pel *const *ref_l0, const pel *const *ref_l1, int i_ref,
+                    orc_loka_unit_t *units, int threads);
+/* the picture-level results from the records (src/lookahead.c:255-292): returns the picture
+ * SATD cost; icost, icost_uv[2], map_dqp[units] are filled when non-NULL */
+double orc_loka_finish(const orc_loka_cfg_t *cfg, const orc_loka_unit_t *units, double *icost, double *icost_uv,
+                       float *map_dqp);
+
 #ifdef __cplusplus
 }
 #endif

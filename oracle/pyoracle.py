@@ -177,6 +177,34 @@ class Oracle(_Common):
                                  len(qps), is_intra, ptr(satd), ptr(q), threads)
         return satd, q
 
+    def loka_units(self, cfg, org_y, i_org, org_u, org_v, i_org_c, ref_l0, ref_l1, i_ref, threads=1):
+        """cfg: LOKA_CFG record; ref_l0/ref_l1: lists of sample-(0,0) addresses; returns LOKA_UNIT array"""
+        cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
+        n = (int(cfg["width"][0]) // 16) * (int(cfg["height"][0]) // 16)
+        out = np.zeros(n, dtype=LOKA_UNIT)
+        a0 = (C.c_void_p * 4)(*(list(ref_l0) + [None] * (4 - len(ref_l0))))
+        a1 = (C.c_void_p * 4)(*(list(ref_l1) + [None] * (4 - len(ref_l1))))
+        self.L.orc_loka_units(ptr(cfg), ptr(org_y), i_org, ptr(org_u), ptr(org_v), i_org_c, a0, a1, i_ref, ptr(out),
+                              threads)
+        return out
+
+    def loka_estimate(self, cfg, org_y, i_org, org_u, org_v, i_org_c, ref_l0, ref_l1, i_ref, want_uv=True,
+                      want_dqp=True, threads=1):
+        """the same tuple as RefLib.loka_estimate, from loka_units + loka_finish"""
+        units = self.loka_units(cfg, org_y, i_org, org_u, org_v, i_org_c, ref_l0, ref_l1, i_ref, threads)
+        cost, icost, icost_uv, dqp = self.loka_finish(cfg, units)
+        return cost, icost, icost_uv if want_uv else None, dqp if want_dqp else None
+
+    def loka_finish(self, cfg, units):
+        """(picture cost, icost, icost_uv[2], map_dqp) from the unit records"""
+        cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
+        icost = C.c_double()
+        icost_uv = (C.c_double * 2)()
+        dqp = np.zeros(len(units), dtype=np.float32)
+        self.L.orc_loka_finish.restype = C.c_double
+        cost = self.L.orc_loka_finish(ptr(cfg), ptr(units), C.byref(icost), icost_uv, ptr(dqp))
+        return cost, icost.value, (icost_uv[0], icost_uv[1]), dqp
+
 
 class RefLib(_Common):
     """The reference's own C kernels (through oracle/ref_glue.c)."""
@@ -281,11 +309,48 @@ class RefLib(_Common):
     def scan(self, lw, lh):
         return np.ctypeslib.as_array(self.L.refk_scan(lw, lh), shape=(1 << (lw + lh),)).copy()
 
+    def loka_estimate(self, cfg, org_y, i_org, org_u, org_v, i_org_c, ref_l0, ref_l1, i_ref, want_uv=True,
+                      want_dqp=True):
+        """loka_estimate_coding_cost itself: (picture cost, icost, icost_uv or None, map_dqp or None)"""
+        c = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)[0]
+        W, H = int(c["width"]), int(c["height"])
+        n0, n1 = int(c["num_ref"][0]), int(c["num_ref"][1])
+        r0 = (C.c_void_p * 4)(*(list(ref_l0) + [None] * (4 - len(ref_l0))))
+        r1 = (C.c_void_p * 4)(*(list(ref_l1) + [None] * (4 - len(ref_l1))))
+        p0 = (C.c_longlong * 4)(*[int(v) for v in c["ref_ptr"][0]])
+        p1 = (C.c_longlong * 4)(*[int(v) for v in c["ref_ptr"][1]])
+        icost = C.c_double()
+        icost_uv = (C.c_double * 2)()
+        dqp = np.zeros((W // 16) * (H // 16), dtype=np.float32)
+        self.L.refk_loka_estimate.restype = C.c_double
+        cost = self.L.refk_loka_estimate(W, H, int(c["is_padding"]), int(c["max_search_range"]), int(c["gop_size"]),
+                                         C.c_longlong(int(c["ptr"])), ptr(org_y), i_org, ptr(org_u), ptr(org_v), i_org_c,
+                                         n0, r0, p0, n1, r1, p1, i_ref, C.byref(icost),
+                                         icost_uv if want_uv else None, ptr(dqp) if want_dqp else None)
+        return (cost, icost.value, (icost_uv[0], icost_uv[1]) if want_uv else None, dqp if want_dqp else None)
+
+    def loka_search(self, cfg, org_y, i_org, ref, i_ref, ref_ptr, refi, num_refp, x, y):
+        """me_search_tz of one 16x16 unit with the lookahead's settings: (mv_x, mv_y, cost)"""
+        c = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)[0]
+        mv = (C.c_short * 2)()
+        self.L.refk_loka_search.restype = C.c_ulonglong
+        cost = self.L.refk_loka_search(int(c["width"]), int(c["height"]), int(c["is_padding"]),
+                                       int(c["max_search_range"]), int(c["gop_size"]), C.c_longlong(int(c["ptr"])),
+                                       ptr(org_y), i_org, P(ref), i_ref, C.c_longlong(int(ref_ptr)), refi, num_refp,
+                                       x, y, mv)
+        return mv[0], mv[1], cost
+
 
 ME_BLOCK = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
 ME_RESULT = np.dtype([("mv_int", "<i2", (2,)), ("mv_sub", "<i2", (2,)), ("sad_int", "<u4"), ("satd_sub", "<u4"),
                       ("cost_int", "<u8"), ("cost_sub", "<u8")])
 CU = ME_BLOCK
+LOKA_CFG = np.dtype([("width", "<i4"), ("height", "<i4"), ("is_padding", "<i4"), ("max_search_range", "<i4"),
+                     ("gop_size", "<i4"), ("num_ref", "<i4", (2,)), ("ptr", "<i8"), ("ref_ptr", "<i8", (2, 4))],
+                    align=True)
+LOKA_UNIT = np.dtype([("mv", "<i2", (2, 4, 2)), ("satd", "<u4", (2, 4)), ("bi_satd", "<u4"), ("zero_satd", "<u4"),
+                      ("min_cost", "<u4"), ("min_icost", "<u4"), ("icost_u", "<u4"), ("icost_v", "<u4"),
+                      ("energy", "<u8"), ("best_mode", "u1"), ("pad", "u1", (7,))])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
 
 MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],

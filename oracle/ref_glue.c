@@ -15,6 +15,7 @@
 #include "define.h"
 #include "util.h"
 #include <stddef.h>
+#include <math.h>
 #include "../include/uavs3e_cuda_table.h"
 
 /* ---- 0. the GPU library's table twin must have funs_handle_t's layout, member by member ---- */
@@ -165,3 +166,98 @@ const s8 *refk_dct_table(int log2n)
     }
 }
 double refk_tbl_sqrt(int i) { return com_tbl_sqrt[i]; }
+
+#undef H   /* the table shorthand of section 2 */
+
+/* ---- 3. lookahead cost estimation -------------------------------------------------------
+ * loka_estimate_coding_cost (src/lookahead.c:82) on caller planes.  The search context is set
+ * up as inter_search_create/inter_search_init do (src/inter.c:2015-2057) for a picture of
+ * W x H, with the low-delay search range when max_search_range is 64. */
+static void loka_setup(com_info_t *info, inter_search_t *pi, int W, int H, int is_padding, int max_search_range,
+                       int gop_size)
+{
+    memset(info, 0, sizeof(*info));
+    info->pic_width = W;
+    info->pic_height = H;
+    info->bit_depth_internal = 8;
+    info->gop_size = gop_size;
+    info->sqh.low_delay = max_search_range == SEARCH_RANGE_IPEL_LD;
+    inter_search_create(&info->tab_mvbits, info);
+    memset(pi, 0, sizeof(*pi));
+    inter_search_init(pi, info, is_padding);
+}
+
+static void loka_img(com_img_t *img, int W, int H, long long ptr, pel *y, int iy, pel *u, pel *v, int ic)
+{
+    memset(img, 0, sizeof(*img));
+    img->num_planes = u ? 3 : 1;
+    img->ptr = ptr;
+    img->width[0] = W; img->height[0] = H; img->stride[0] = iy * (int)sizeof(pel); img->planes[0] = y;
+    for (int i = 1; i < 3 && u; i++) {
+        img->width[i] = W / 2; img->height[i] = H / 2; img->stride[i] = ic * (int)sizeof(pel);
+        img->planes[i] = i == 1 ? u : v;
+    }
+}
+
+double refk_loka_estimate(int W, int H, int is_padding, int max_search_range, int gop_size, long long ptr,
+                          pel *org_y, int i_org, pel *org_u, pel *org_v, int i_org_c,
+                          int n0, pel **ref0, long long *ptr0, int n1, pel **ref1, long long *ptr1, int i_ref,
+                          double *icost, double *icost_uv, float *map_dqp)
+{
+    refk_init();
+    static com_info_t info;
+    inter_search_t *pi = (inter_search_t *)calloc(1, sizeof(inter_search_t));
+    loka_setup(&info, pi, W, H, is_padding, max_search_range, gop_size);
+    com_img_t org, r0[4], r1[4];
+    com_img_t *l0[4], *l1[4];
+    loka_img(&org, W, H, ptr, org_y, i_org, org_u, org_v, i_org_c);
+    for (int i = 0; i < n0; i++) { loka_img(&r0[i], W, H, ptr0[i], ref0[i], i_ref, NULL, NULL, 0); l0[i] = &r0[i]; }
+    for (int i = 0; i < n1; i++) { loka_img(&r1[i], W, H, ptr1[i], ref1[i], i_ref, NULL, NULL, 0); l1[i] = &r1[i]; }
+    int num_ref[2] = { n0, n1 };
+    double cost = loka_estimate_coding_cost(pi, &org, l0, l1, num_ref, 8, icost, icost_uv, map_dqp);
+    inter_search_free(info.tab_mvbits, pi->tab_mvbits_offset);
+    free(pi);
+    return cost;
+}
+
+/* me_search_tz (src/me.c:529) for the 16x16 unit at (x, y) with the lookahead's settings
+ * (src/lookahead.c:104-111): integer resolution, predictor (0,0), no bi-prediction.
+ * Writes the integer MV; returns the search's cost. */
+unsigned long long refk_loka_search(int W, int H, int is_padding, int max_search_range, int gop_size, long long ptr,
+                                    pel *org_y, int i_org, pel *ref, int i_ref, long long ref_ptr, int refi, int num_refp,
+                                    int x, int y, short *mv_out)
+{
+    refk_init();
+    static com_info_t info;
+    inter_search_t *pi = (inter_search_t *)calloc(1, sizeof(inter_search_t));
+    loka_setup(&info, pi, W, H, is_padding, max_search_range, gop_size);
+    com_img_t rimg;
+    loka_img(&rimg, W, H, ref_ptr, ref, i_ref, NULL, NULL, 0);
+    com_pic_t pic;
+    com_subpel_t subpel;
+    memset(&pic, 0, sizeof(pic));
+    memset(&subpel, 0, sizeof(subpel));
+    pic.subpel = &subpel;
+    pic.ptr = ref_ptr;
+    pic.img = &rimg;
+    pic.stride_luma = i_ref;
+    pic.y = ref;
+    subpel.imgs[0][0] = &rimg;
+    double base_lambda = 1.43631 * pow(2.0, (32 - 16.0) / 4.0);
+    pi->ptr = ptr;
+    pi->curr_mvr = 2;
+    pi->lambda_mv = (u32)floor(65536.0 * sqrt(base_lambda));
+    pi->i_org = i_org;
+    pi->adaptive_raster_range = 0;
+    pi->subpel_cost_type = 0;
+    pi->org = org_y + y * i_org + x;
+    pi->num_refp = (u8)num_refp;
+    pi->ref_pic = &pic;
+    s16 mv[2], mvp[2] = { 0, 0 };
+    u64 cost = me_search_tz(pi, x, y, 16, 16, W, H, (s8)refi, 0, mvp, mv, 0);
+    mv_out[0] = (short)(mv[0] >> 2);
+    mv_out[1] = (short)(mv[1] >> 2);
+    inter_search_free(info.tab_mvbits, pi->tab_mvbits_offset);
+    free(pi);
+    return cost;
+}

@@ -305,12 +305,85 @@ def run_tables(B, p, seed):
     return digest(*outs)
 
 
+# ------------------------------------------------------------------ lookahead estimation
+def loka_frames(rng, W, H, pocs, vel, n_rect=6):
+    """4:2:0 frames of a panning scene: the frame at POC t is the W x H window of a larger
+    canvas (smooth pattern + textured squares) at offset t * vel, plus per-frame noise in
+    [-3, 3]; chroma = 2x-downsampled luma offset by +16 / -16 (clipped)"""
+    margin = int(max(abs(vel[0]), abs(vel[1])) * max(abs(t) for t in pocs)) + 8
+    CH, CW = H + 2 * margin, W + 2 * margin
+    yy, xx = np.mgrid[0:CH, 0:CW]
+    canvas = 128 + 45 * np.sin(xx / 9.0 + rng.uniform(0, 6)) * np.cos(yy / 13.0) + 20 * np.sin((xx + yy) / 5.0)
+    for _ in range(n_rect):
+        s = int(rng.integers(8, 40))
+        y0, x0 = int(rng.integers(0, CH - s)), int(rng.integers(0, CW - s))
+        canvas[y0:y0 + s, x0:x0 + s] = rng.integers(0, 256, (s, s))
+    frames = {}
+    for t in pocs:
+        ox, oy = margin + int(round(t * vel[0])), margin + int(round(t * vel[1]))
+        y = np.clip(canvas[oy:oy + H, ox:ox + W] + rng.integers(-3, 4, (H, W)), 0, 255).astype(np.uint8)
+        c = y.reshape(H // 2, 2, W // 2, 2).astype(np.int32).mean((1, 3)).astype(np.int32)
+        frames[t] = (y, np.clip(c + 16, 0, 255).astype(np.uint8), np.clip(c - 16, 0, 255).astype(np.uint8))
+    return frames
+
+
+LOKA_PAD = 144
+
+
+def loka_inputs(p, seed):
+    """(cfg record, org planes, padded reference planes) of one lookahead case"""
+    import pyoracle
+    rng = np.random.default_rng(seed)
+    W, H, ptr = p["w"], p["h"], p.get("ptr", 8)
+    l0, l1 = p["l0"], p["l1"]
+    frames = loka_frames(rng, W, H, [ptr] + l0 + l1, p["vel"])
+    cfg = np.zeros(1, dtype=pyoracle.LOKA_CFG)
+    cfg["width"], cfg["height"], cfg["is_padding"] = W, H, p["pad"]
+    cfg["max_search_range"], cfg["gop_size"], cfg["ptr"] = p["range"], p["gop"], ptr
+    cfg["num_ref"][0] = [len(l0), len(l1)]
+    for li, lst in enumerate((l0, l1)):
+        for r, t in enumerate(lst):
+            cfg["ref_ptr"][0, li, r] = t
+    stride = W + 2 * LOKA_PAD
+    refs = [[padded_plane(frames[t][0], LOKA_PAD, stride) for t in lst] for lst in (l0, l1)]
+    return cfg, frames[ptr], refs, stride
+
+
+def loka_ref_addrs(refs, stride):
+    return [[r.ctypes.data + LOKA_PAD * stride + LOKA_PAD for r in lst] for lst in refs]
+
+
+def run_loka(B, p, seed):
+    cfg, (y, u, v), refs, stride = loka_inputs(p, seed)
+    a0, a1 = loka_ref_addrs(refs, stride)
+    W = p["w"]
+    cost, icost, icost_uv, dqp = B.loka_estimate(cfg, y, W, u, v, W // 2, a0, a1, stride, want_uv=p["uv"],
+                                                 want_dqp=p["dqp"])
+    outs = [np.array([cost, icost], dtype=np.float64)]
+    if icost_uv is not None:
+        outs.append(np.array(icost_uv, dtype=np.float64))
+    if dqp is not None:
+        outs.append(dqp)
+    return digest(*outs)
+
+
 RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka,
 }
+
+# lookahead cases: encoder picture level (padded references, random access with both lists or
+# low delay with 4 references) and the scene-cut estimate (1 reference, no padding)
+LOKA_CASES = [
+    dict(w=128, h=96, pad=1, range=384, gop=16, l0=[0, 4], l1=[16, 12], vel=(1.5, -0.75), uv=True, dqp=True),
+    dict(w=144, h=80, pad=1, range=384, gop=16, l0=[0], l1=[16], vel=(5.0, 3.0), uv=True, dqp=True),
+    dict(w=128, h=64, pad=1, range=64, gop=4, l0=[7, 6, 5, 4], l1=[], vel=(2.5, 1.25), uv=True, dqp=True),
+    dict(w=136, h=72, pad=0, range=384, gop=16, l0=[7], l1=[], vel=(3.0, -2.0), uv=False, dqp=False),
+    dict(w=160, h=96, pad=0, range=64, gop=4, l0=[6], l1=[], vel=(-6.0, 4.0), uv=False, dqp=False),
+    dict(w=48, h=32, pad=1, range=384, gop=16, l0=[0], l1=[16], vel=(2.0, 1.0), uv=True, dqp=True),
+]
 
 
 def all_cases():
@@ -370,6 +443,8 @@ def all_cases():
         for lh in range(2, 7):
             add("dquant", lw=lw, lh=lh)
     add("tables")
+    for p in LOKA_CASES:
+        add("loka", **p)
     return cases
 
 

@@ -58,6 +58,11 @@ def _declare(L):
     L.uavs3e_cuda_profile_enable.argtypes = [I]
     L.uavs3e_cuda_launch_count.restype = C.c_ulonglong
     L.uavs3e_cuda_profile_collect.argtypes = [P, P, I]
+    L.uavs3e_cuda_loka_estimate.argtypes = [P, P, I, P, P, I, P, P, I, I, P, P, P, P, P]
+    L.uavs3e_cuda_loka_units_device.argtypes = [P, P, I, P, P, I, P, P, I, I, P, P, P, P]
+    L.uavs3e_cuda_loka_finish.argtypes = [P, P, P, P, P, P]
+    L.uavs3e_cuda_loka_finish.restype = C.c_double
+    L.uavs3e_cuda_loka_sc_ratio.argtypes = [I, I, I, I, I, C.c_int64, P, I, P, P, I, P, C.c_int64, I, I, P]
 
 
 def check(rc, what="uavs3e_cuda"):
@@ -73,7 +78,7 @@ def init(device=0):
     check(lib().uavs3e_cuda_init(device), "uavs3e_cuda_init")
 
 
-PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice")
+PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka")
 
 CU = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
@@ -105,6 +110,100 @@ def intra_lattice(org, rec, cus, qps=(27, 32, 37, 42), ipf=0, is_intra=1, stream
     torch.cuda.synchronize()
     return (d_satd.cpu().numpy().view(np.uint32)[:n * 33].copy(),
             d_q.cpu().numpy().view(LAT_Q)[:n * 33 * len(q)].copy())
+
+
+# ------------------------------------------------------------------ lookahead cost estimation
+LOKA_CFG = np.dtype([("width", "<i4"), ("height", "<i4"), ("is_padding", "<i4"), ("max_search_range", "<i4"),
+                     ("gop_size", "<i4"), ("num_ref", "<i4", (2,)), ("ptr", "<i8"), ("ref_ptr", "<i8", (2, 4))],
+                    align=True)
+LOKA_UNIT = np.dtype([("mv", "<i2", (2, 4, 2)), ("satd", "<u4", (2, 4)), ("bi_satd", "<u4"), ("zero_satd", "<u4"),
+                      ("min_cost", "<u4"), ("min_icost", "<u4"), ("icost_u", "<u4"), ("icost_v", "<u4"),
+                      ("energy", "<u8"), ("best_mode", "u1"), ("pad", "u1", (7,))])
+
+
+def loka_cfg(width, height, is_padding, max_search_range, gop_size, ptr, ref_ptr_l0=(), ref_ptr_l1=()):
+    """the uavs3e_cuda_loka_cfg_t record of one picture"""
+    c = np.zeros(1, dtype=LOKA_CFG)
+    c["width"], c["height"], c["is_padding"] = width, height, is_padding
+    c["max_search_range"], c["gop_size"], c["ptr"] = max_search_range, gop_size, ptr
+    c["num_ref"][0] = [len(ref_ptr_l0), len(ref_ptr_l1)]
+    for li, lst in enumerate((ref_ptr_l0, ref_ptr_l1)):
+        for r, t in enumerate(lst):
+            c["ref_ptr"][0, li, r] = t
+    return c
+
+
+def _addrs(planes, pad):
+    """sample-(0,0) addresses of padded 2-D planes"""
+    arr = (C.c_void_p * 4)()
+    for i, p in enumerate(planes):
+        arr[i] = p.ctypes.data + pad * p.strides[0] + pad
+    return arr
+
+
+def loka_estimate(cfg, org_y, org_u, org_v, refs_l0, refs_l1, ref_pad, units=False):
+    """loka_estimate_coding_cost on host planes: refs are 2-D uint8 planes padded by ref_pad.
+    Returns dict(cost, icost, icost_uv, map_dqp[, units])."""
+    cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
+    W, H = int(cfg["width"][0]), int(cfg["height"][0])
+    n = (W // 16) * (H // 16)
+    refs = [np.ascontiguousarray(r) for r in refs_l0] + [np.ascontiguousarray(r) for r in refs_l1]
+    i_ref = refs[0].strides[0] if refs else 0
+    a0, a1 = _addrs(refs[:len(refs_l0)], ref_pad), _addrs(refs[len(refs_l0):], ref_pad)
+    cost, icost = C.c_double(), C.c_double()
+    icost_uv = (C.c_double * 2)()
+    dqp = np.zeros(max(1, n), dtype=np.float32)
+    out = np.zeros(max(1, n), dtype=LOKA_UNIT) if units else None
+    check(lib().uavs3e_cuda_loka_estimate(cfg.ctypes.data, org_y.ctypes.data, org_y.strides[0], org_u.ctypes.data,
+                                          org_v.ctypes.data, org_u.strides[0], a0, a1, i_ref, ref_pad,
+                                          C.byref(cost), C.byref(icost), icost_uv, dqp.ctypes.data,
+                                          out.ctypes.data if units else None), "loka_estimate")
+    r = dict(cost=cost.value, icost=icost.value, icost_uv=(icost_uv[0], icost_uv[1]), map_dqp=dqp[:n])
+    if units:
+        r["units"] = out[:n]
+    return r
+
+
+def loka_sc_ratio(width, height, is_padding, max_search_range, gop_size, ptr, org_y, org_u, org_v, last_y, last_ptr,
+                  last_pad):
+    """loka_get_sc_ratio: last_y is the previous picture's luma plane padded by last_pad"""
+    ratio = C.c_double()
+    addr = last_y.ctypes.data + last_pad * last_y.strides[0] + last_pad
+    check(lib().uavs3e_cuda_loka_sc_ratio(width, height, is_padding, max_search_range, gop_size, ptr,
+                                          org_y.ctypes.data, org_y.strides[0], org_u.ctypes.data, org_v.ctypes.data,
+                                          org_u.strides[0], addr, last_ptr, last_y.strides[0], last_pad,
+                                          C.byref(ratio)), "loka_sc_ratio")
+    return ratio.value
+
+
+def loka_units_device(cfg, d_org_y, i_org, d_org_u, d_org_v, i_org_c, d_refs_l0, d_refs_l1, i_ref, ref_pad, d_units,
+                      d_energy, d_totals, stream=None):
+    """device-buffer entry (addresses as ints), enqueued on `stream` (default: torch's current)"""
+    cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
+    a0 = (C.c_void_p * 4)(*(list(d_refs_l0) + [None] * (4 - len(d_refs_l0))))
+    a1 = (C.c_void_p * 4)(*(list(d_refs_l1) + [None] * (4 - len(d_refs_l1))))
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_loka_units_device(cfg.ctypes.data, d_org_y, i_org, d_org_u, d_org_v, i_org_c, a0, a1,
+                                              i_ref, ref_pad, d_units, d_energy, d_totals, stream),
+          "loka_units_device")
+
+
+def loka_finish(cfg, totals, energy=None):
+    """(cost, icost, icost_uv, map_dqp or None) from host totals[>=4] and energies"""
+    cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
+    t = np.ascontiguousarray(totals, dtype=np.uint64)
+    icost = C.c_double()
+    icost_uv = (C.c_double * 2)()
+    dqp = None
+    if energy is not None:
+        energy = np.ascontiguousarray(energy, dtype=np.uint64)
+        dqp = np.zeros(len(energy), dtype=np.float32)
+    cost = lib().uavs3e_cuda_loka_finish(cfg.ctypes.data, t.ctypes.data,
+                                         energy.ctypes.data if energy is not None else None, C.byref(icost),
+                                         icost_uv, dqp.ctypes.data if dqp is not None else None)
+    return cost, icost.value, (icost_uv[0], icost_uv[1]), dqp
 
 
 def profile_enable(on=True):

@@ -33,7 +33,7 @@ struct MeResult {
 };
 
 // optional per-kernel timing with CUDA events on the launching stream
-enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_N = 8 };
+enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_LOKA = 5, PROF_N = 8 };
 int ensure_init();   // selects the library's device (initialising device 0 on first use)
 void prof_begin(int k, cudaStream_t st);
 void prof_end(int k, cudaStream_t st);
