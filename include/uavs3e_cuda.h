@@ -5,7 +5,8 @@
  * Two layers:
  *   1. Batched entry points (this file): one call per frame does the work the encoder's
  *      search loops would otherwise ask for one block at a time -- frame interpolation,
- *      the full motion-search cost table, the intra/transform lattice.  Inputs and outputs
+ *      the full motion-search cost table, the intra/transform lattice, the lookahead's
+ *      per-picture cost estimate.  Inputs and outputs
  *      are plain pointers and sizes; "d_" pointers are device memory, others host memory.
  *   2. Kernel-table entries (uavs3e_cuda_table.h): functions with the exact C signatures of
  *      the reference's function-pointer table funs_handle_t (inc/com_util.h:278-341), and an
@@ -59,7 +60,8 @@ UAVS3E_CUDA_API const char *uavs3e_cuda_version(void);
 /* Kernel timing (observability; the reference has none): while enabled, every launch of the
  * batched kernels is bracketed by CUDA events on its stream.  collect() waits for them and
  * returns, per kernel id (0 pad, 1 frame interpolation, 2 integer search, 3 fractional
- * refinement), the summed milliseconds and launch counts, then forgets them. */
+ * refinement, 4 intra lattice, 5 lookahead estimate), the summed milliseconds and launch counts,
+ * then forgets them. */
 UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
 /* Measured issue rate of the 4-sample SAD instruction (vabsdiff4 with accumulate) on the current
  * device: operations per second and per clock per SM.  The integer motion search's roofline
@@ -240,8 +242,10 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_modes_device(const uint8_t *d_org,
  *                max_search_range (SEARCH_RANGE_IPEL_LD 64 or _RA 384), gop_size, the reference
  *                counts per list (<= 4) and the POCs of the picture and its references;
  *   org planes : the picture's Y (W x H) and U, V (W/2 x H/2) planes;
- *   references : luma planes, pointers to sample (0,0), stride i_ref (a multiple of 4), readable
- *                ref_pad samples around the picture (>= 144 when is_padding, else >= 4).
+ *   references : luma planes, pointers to sample (0,0), stride i_ref, padded by ref_pad samples
+ *                (>= 144 when is_padding; the host entry reads no padding otherwise, the device
+ *                entry wants >= 4 readable samples around the picture and a stride that is a
+ *                multiple of 4).
  */
 #define UAVS3E_CUDA_LOKA_MAX_REFS 4
 

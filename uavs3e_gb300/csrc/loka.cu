@@ -12,7 +12,9 @@
 //   The SATD (com_had) of the winner closes the search.
 // k_loka_unit: one warp per unit picks each list's winner, builds the two bi-prediction
 //   averages, predicts the 11 intra modes from the original picture's neighbours, the chroma
-//   blocks with the best mode, the unit's energy, and sums the picture totals.
+//   blocks with the best mode, the unit's energy, and sums the picture totals.  Every 16x16
+//   prediction is spread over the warp (8 samples a lane, one mode at a time) and its SATD is a
+//   warp Hadamard (rows in registers, columns through shuffles).
 #include "common.cuh"
 #include "intra.cuh"
 #include "uavs3e_cuda_internal.h"
@@ -181,13 +183,61 @@ __device__ void lk_grid(LkSearch &S, int x0, int x1, int y0, int y1, int s, int 
     }
 }
 
+// A grid of step 8 with the lanes along one grid row: the 16 samples of lane l's candidate are
+// the words w[2l .. 2l+4] of the row (from the common aligned base), so each lane loads its own
+// two words and takes the next three from lanes l+1 and l+2.  30 candidates per pass; the two
+// lanes after the last candidate only load, and only the words of the last candidate's span.
+__device__ void lk_grid8(LkSearch &S, int x0, int x1, int y0, int y1, int lane)
+{
+    const int nx = (x1 - x0) / 8 + 1, ny = (y1 - y0) / 8 + 1;
+    const u32 sh = (u32)(((uintptr_t)(S.ref + x0)) & 3) * 8;       // the same for every row and lane
+    const int ws = S.stride >> 2;
+    u64 kmin = ~0ull;
+    for (int gy = 0; gy < ny; gy++) {
+        const int my = y0 + 8 * gy;
+        for (int c0 = 0; c0 < nx; c0 += 30) {
+            const int nc = min(30, nx - c0);
+            const bool ld = lane < nc + 2;
+            const int mx = x0 + 8 * (c0 + lane);
+            const u32 *q = (const u32 *)(((uintptr_t)(S.ref + my * S.stride + mx)) & ~(uintptr_t)3);
+            u32 sad = 0;
+#pragma unroll 4
+            for (int r = 0; r < 16; r++, q += ws) {
+                const u32 w0 = ld ? __ldg(q) : 0u, w1 = lane < nc + 1 ? __ldg(q + 1) : 0u;
+                const u32 w2 = __shfl_down_sync(0xffffffffu, w0, 1), w3 = __shfl_down_sync(0xffffffffu, w1, 1);
+                const u32 w4 = __shfl_down_sync(0xffffffffu, w0, 2);
+                const uint4 o = *(const uint4 *)(S.so + r * 4);
+                sad = sad4(o.x, __funnelshift_r(w0, w1, sh), sad);
+                sad = sad4(o.y, __funnelshift_r(w1, w2, sh), sad);
+                sad = sad4(o.z, __funnelshift_r(w2, w3, sh), sad);
+                sad = sad4(o.w, __funnelshift_r(w3, w4, sh), sad);
+            }
+            if (lane < nc) {
+                S.evals++;
+                const u64 cost = ((u64)sad << 16) + (u64)((lk_bits(mx) + lk_bits(my)) * S.lambda);
+                const u64 key = (cost << LK_LIST_BITS) | (u64)(gy * nx + c0 + lane);
+                kmin = key < kmin ? key : kmin;
+            }
+        }
+    }
+    kmin = warp_min_u64(kmin);
+    if ((kmin >> LK_LIST_BITS) < S.best) {
+        const int k = (int)(kmin & ((1u << LK_LIST_BITS) - 1));
+        S.best = kmin >> LK_LIST_BITS;
+        S.mvx = x0 + (k % nx) * 8;
+        S.mvy = y0 + (k / nx) * 8;
+    }
+}
+
 // search_raster with adaptive_raster_range 0: the full-range grid of step 8 (refi + 1), then
 // grids of the halved step around the running best until the step is 1
 __device__ void lk_raster(LkSearch &S, int refi, int range, int lane)
 {
     int s = 8 * (refi + 1);
-    lk_grid(S, min(max(S.mvx - range, S.minx), S.maxx), min(max(S.mvx + range, S.minx), S.maxx),
-            min(max(S.mvy - range, S.miny), S.maxy), min(max(S.mvy + range, S.miny), S.maxy), s, lane);
+    const int gx0 = min(max(S.mvx - range, S.minx), S.maxx), gx1 = min(max(S.mvx + range, S.minx), S.maxx);
+    const int gy0 = min(max(S.mvy - range, S.miny), S.maxy), gy1 = min(max(S.mvy + range, S.miny), S.maxy);
+    if (s == 8) lk_grid8(S, gx0, gx1, gy0, gy1, lane);
+    else lk_grid(S, gx0, gx1, gy0, gy1, s, lane);
     for (s >>= 1; s >= 1; s >>= 1)
         lk_grid(S, max(S.mvx - s, S.minx), min(S.mvx + s, S.maxx), max(S.mvy - s, S.miny), min(S.mvy + s, S.maxy), s,
                 lane);
@@ -202,17 +252,66 @@ __device__ __forceinline__ void lk_load_org(u32 *so, const pel *org, int i_org, 
     so[r * 4 + (c >> 2) + 1] = (u32)p[4] | (u32)p[5] << 8 | (u32)p[6] << 16 | (u32)p[7] << 24;
 }
 
-// com_had of the 16x16 block: 4 lanes each transform one 8x8 tile; the sum lands in lane 0
-__device__ __forceinline__ u32 lk_had16(const pel *o, int io, const pel *p, int ip, int lane)
+// com_had of a 16x16 difference block held by the warp: lane l has row l >> 1, columns
+// (l & 1) * 8 .. +7.  Rows of each 8x8 tile are transformed in registers, columns across the
+// lanes whose bits 1..3 differ (butterflies on lane ^ 2, ^ 4, ^ 8); each tile's sum of magnitudes
+// is rounded as com_had_8x8 does ((s + 2) >> 2) and the four tiles are added.  Every lane
+// returns the total.
+__device__ __forceinline__ u32 warp_had16(int *d, int lane)
 {
-    u32 t = 0;
-    if (lane < 4) {
-        const int oy = (lane >> 1) * 8, ox = (lane & 1) * 8;
-        t = satd_tile(8, 8, o + oy * io + ox, io, p + oy * ip + ox, ip, 0.0, 0.0);
+    wht<8>(d);
+#pragma unroll
+    for (int b = 2; b <= 8; b <<= 1) {
+        const bool hi = lane & b;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int p = __shfl_xor_sync(0xffffffffu, d[i], b);
+            d[i] = hi ? p - d[i] : d[i] + p;
+        }
     }
-    t += __shfl_down_sync(0xffffffffu, t, 2);
-    t += __shfl_down_sync(0xffffffffu, t, 1);
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += abs(d[i]);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    s += __shfl_xor_sync(0xffffffffu, s, 4);
+    s += __shfl_xor_sync(0xffffffffu, s, 8);
+    u32 t = (u32)((s + 2) >> 2);
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
+    t += __shfl_xor_sync(0xffffffffu, t, 16);
     return t;
+}
+
+// com_had of two 8x8 difference blocks: lane l has row l & 7 of block (l >> 3) & 1 (lanes 16..31
+// repeat 0..15); columns are transformed across lane ^ 1, ^ 2, ^ 4.  Returns the block's SATD.
+__device__ __forceinline__ u32 warp_had8x2(int *d, int lane)
+{
+    wht<8>(d);
+#pragma unroll
+    for (int b = 1; b <= 4; b <<= 1) {
+        const bool hi = lane & b;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int p = __shfl_xor_sync(0xffffffffu, d[i], b);
+            d[i] = hi ? p - d[i] : d[i] + p;
+        }
+    }
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += abs(d[i]);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    s += __shfl_xor_sync(0xffffffffu, s, 4);
+    return (u32)((s + 2) >> 2);
+}
+
+// the 16x16 SATD of the org block (smem bytes, stride 16) against p
+__device__ __forceinline__ u32 lk_had16(const pel *o, const pel *p, int ip, int lane)
+{
+    const int j = lane >> 1, i0 = (lane & 1) * 8;
+    int d[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) d[k] = (int)o[j * 16 + i0 + k] - (int)p[j * ip + i0 + k];
+    return warp_had16(d, lane);
 }
 
 __global__ void __launch_bounds__(32 * LK_WARPS) k_loka_search(const LokaParams P)
@@ -253,7 +352,7 @@ __global__ void __launch_bounds__(32 * LK_WARPS) k_loka_search(const LokaParams 
             lk_diamond(S, 4, lane);
         }
         const pel *blk = S.ref + S.mvy * P.i_ref + S.mvx;
-        const u32 satd = lk_had16((const pel *)s_org[warp], 16, blk, P.i_ref, lane);
+        const u32 satd = lk_had16((const pel *)s_org[warp], blk, P.i_ref, lane);
         if (lane == 0) {
             LokaUnit &U = P.units[u];
             U.mv[l][r][0] = (s16)S.mvx;
@@ -280,23 +379,6 @@ __device__ __forceinline__ void lk_nbr(pel *c, int x, int y, int w, int h, int W
         c[-1 - i] = x ? src[min(i, nl - 1) * s - 1] : (pel)128;
     }
     if (lane == 0) c[0] = (x && y) ? src[-s - 1] : y ? src[-s] : x ? src[-1] : (pel)128;
-}
-
-// Hadamard 8x8 of org - prediction(mode) over the tile at (tx, ty) of a block with neighbours c
-__device__ __forceinline__ u32 lk_intra_tile(const pel *o, int io, const pel *c, const IpredBlock &B, int mode,
-                                             int tx, int ty)
-{
-    int d[64];
-#pragma unroll
-    for (int j = 0; j < 8; j++)
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-            d[j * 8 + i] = (int)o[(ty + j) * io + tx + i] - ipred_sample(c, B, mode, 0, tx + i, ty + j);
-    wht2d<8>(d);
-    int s = 0;
-#pragma unroll
-    for (int i = 0; i < 64; i++) s += abs(d[i]);
-    return (u32)((s + 2) >> 2);
 }
 
 __device__ __forceinline__ u64 lk_var_sums(const pel *p, int s, int n, int lane, u64 *sq_out)
@@ -327,9 +409,7 @@ __device__ __forceinline__ u64 lk_var(const pel *p, int s, int n, int log2n, int
 __global__ void __launch_bounds__(32 * LK_WARPS) k_loka_unit(const LokaParams P)
 {
     __shared__ __align__(16) pel s_org[LK_WARPS][256];
-    __shared__ __align__(16) pel s_pred[LK_WARPS][2][256];
     __shared__ pel s_nb[LK_WARPS][3][144];
-    __shared__ u32 s_tile[LK_WARPS][44];
     __shared__ unsigned long long s_tot[4];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int u = blockIdx.x * LK_WARPS + warp;
@@ -339,11 +419,10 @@ __global__ void __launch_bounds__(32 * LK_WARPS) k_loka_unit(const LokaParams P)
         const int x = (u % P.nux) * 16, y = (u / P.nux) * 16;
         const pel *org = P.org + y * P.i_org + x;
         pel *so = s_org[warp];
-        {
-            const int rr = lane >> 1, cc = (lane & 1) * 8;
+        // lane l covers row j, columns i0 .. i0 + 7 of the unit in every 16x16 pass below
+        const int j = lane >> 1, i0 = (lane & 1) * 8;
 #pragma unroll
-            for (int i = 0; i < 8; i++) so[rr * 16 + cc + i] = org[rr * P.i_org + cc + i];
-        }
+        for (int k = 0; k < 8; k++) so[j * 16 + i0 + k] = org[j * P.i_org + i0 + k];
         LokaUnit &U = P.units[u];
         // per list: the first reference with the smallest SATD (src/lookahead.c:131-175)
         u64 min_cost = ~0ull;
@@ -356,68 +435,63 @@ __global__ void __launch_bounds__(32 * LK_WARPS) k_loka_unit(const LokaParams P)
             }
         }
         u32 bi_satd = 0, zero_satd = 0;
-        const bool is_bi = P.n_ref[0] && P.n_ref[1];
-        if (is_bi) {
-            // averages (pel_avrg) of the two list winners and of the (0,0) blocks of the first refs
+        if (P.n_ref[0] && P.n_ref[1]) {
+            // pel_avrg of the two list winners, then of the (0,0) blocks of the first references
             const int r0 = best_ref[0], r1 = best_ref[1];
-            const pel *a = P.ref[0][r0] + (y + U.mv[0][r0][1]) * P.i_ref + x + U.mv[0][r0][0];
-            const pel *b = P.ref[1][r1] + (y + U.mv[1][r1][1]) * P.i_ref + x + U.mv[1][r1][0];
-            const pel *za = P.ref[0][0] + y * P.i_ref + x, *zb = P.ref[1][0] + y * P.i_ref + x;
-            const int rr = lane >> 1, cc = (lane & 1) * 8;
+            const pel *a = P.ref[0][r0] + (y + U.mv[0][r0][1] + j) * P.i_ref + x + U.mv[0][r0][0] + i0;
+            const pel *b = P.ref[1][r1] + (y + U.mv[1][r1][1] + j) * P.i_ref + x + U.mv[1][r1][0] + i0;
+            const pel *za = P.ref[0][0] + (y + j) * P.i_ref + x + i0, *zb = P.ref[1][0] + (y + j) * P.i_ref + x + i0;
+            int d[8];
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const int o = rr * P.i_ref + cc + i;
-                s_pred[warp][0][rr * 16 + cc + i] = (pel)((a[o] + b[o] + 1) >> 1);
-                s_pred[warp][1][rr * 16 + cc + i] = (pel)((za[o] + zb[o] + 1) >> 1);
-            }
-            __syncwarp();
-            u32 t = 0;
-            if (lane < 8) {
-                const int k = lane & 3, oy = (k >> 1) * 8, ox = (k & 1) * 8;
-                t = satd_tile(8, 8, so + oy * 16 + ox, 16, s_pred[warp][lane >> 2] + oy * 16 + ox, 16, 0.0, 0.0);
-            }
-            t += __shfl_down_sync(0xffffffffu, t, 2);
-            t += __shfl_down_sync(0xffffffffu, t, 1);
-            bi_satd = __shfl_sync(0xffffffffu, t, 0);
-            zero_satd = __shfl_sync(0xffffffffu, t, 4);
+            for (int k = 0; k < 8; k++) d[k] = (int)so[j * 16 + i0 + k] - ((a[k] + b[k] + 1) >> 1);
+            bi_satd = warp_had16(d, lane);
+#pragma unroll
+            for (int k = 0; k < 8; k++) d[k] = (int)so[j * 16 + i0 + k] - ((za[k] + zb[k] + 1) >> 1);
+            zero_satd = warp_had16(d, lane);
             if (bi_satd < min_cost) min_cost = bi_satd;
             if (zero_satd < min_cost) min_cost = zero_satd;
         }
-        // intra: 11 modes x 4 tiles, neighbours from the original picture (src/lookahead.c:204-230)
+        // intra: the 11 modes one after another over the whole warp, neighbours from the original
+        // picture (src/lookahead.c:204-230)
         pel *c = s_nb[warp][0] + 70;
         lk_nbr(c, x, y, 16, 16, P.W, P.H, org, P.i_org, lane);
         __syncwarp();
         const int avail = (x ? 2 : 0) | (y ? 1 : 0) | ((x && y) ? 4 : 0);
+        u32 min_icost = 0xFFFFFFFFu;
+        int best_mode = 0;
         {
             IpredBlock B;
             ipred_block_setup(c, 16, 16, avail, 8, B);
-            for (int t = lane; t < 44; t += 32)
-                s_tile[warp][t] = lk_intra_tile(so, 16, c, B, kLokaModes[t >> 2], (t & 1) * 8, ((t >> 1) & 1) * 8);
+            for (int m = 0; m < 11; m++) {
+                const int mode = kLokaModes[m];
+                int d[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) d[k] = (int)so[j * 16 + i0 + k] - ipred_sample(c, B, mode, 0, i0 + k, j);
+                const u32 cost = warp_had16(d, lane);
+                if (cost < min_cost) min_cost = cost;
+                if (cost < min_icost) { min_icost = cost; best_mode = mode; }
+            }
         }
-        __syncwarp();
-        u32 min_icost = 0xFFFFFFFFu;
-        int best_mode = 0;
-        for (int m = 0; m < 11; m++) {
-            const u32 cost = s_tile[warp][4 * m] + s_tile[warp][4 * m + 1] + s_tile[warp][4 * m + 2] +
-                             s_tile[warp][4 * m + 3];
-            if (cost < min_cost) min_cost = cost;
-            if (cost < min_icost) { min_icost = cost; best_mode = kLokaModes[m]; }
-        }
-        // chroma 8x8 with the luma winner (src/lookahead.c:231-243)
+        // chroma 8x8 blocks with the luma winner (src/lookahead.c:231-243): lanes 0..7 U, 8..15 V
         const int xc = x >> 1, yc = y >> 1;
         const pel *ou = P.org_u + yc * P.i_org_c + xc, *ov = P.org_v + yc * P.i_org_c + xc;
         pel *cu = s_nb[warp][1] + 40, *cv = s_nb[warp][2] + 40;
         lk_nbr(cu, xc, yc, 8, 8, P.W >> 1, P.H >> 1, ou, P.i_org_c, lane);
         lk_nbr(cv, xc, yc, 8, 8, P.W >> 1, P.H >> 1, ov, P.i_org_c, lane);
         __syncwarp();
-        u32 tc = 0;
-        if (lane < 2) {
-            const pel *cc = lane ? cv : cu;
+        u32 icost_u, icost_v;
+        {
+            const int plane = (lane >> 3) & 1, row = lane & 7;
+            const pel *cc = plane ? cv : cu, *oc = (plane ? ov : ou) + row * P.i_org_c;
             IpredBlock B;
             ipred_block_setup(cc, 8, 8, avail, 8, B);
-            tc = lk_intra_tile(lane ? ov : ou, P.i_org_c, cc, B, best_mode, 0, 0);
+            int d[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) d[k] = (int)oc[k] - ipred_sample(cc, B, best_mode, 0, k, row);
+            const u32 t = warp_had8x2(d, lane);
+            icost_u = __shfl_sync(0xffffffffu, t, 0);
+            icost_v = __shfl_sync(0xffffffffu, t, 8);
         }
-        const u32 icost_u = __shfl_sync(0xffffffffu, tc, 0), icost_v = __shfl_sync(0xffffffffu, tc, 1);
         // energy of the dQP map (src/lookahead.c:248-262)
         const u64 energy = lk_var(org, P.i_org, 16, 4, lane) + lk_var(ou, P.i_org_c, 8, 3, lane) +
                            lk_var(ov, P.i_org_c, 8, 3, lane);
@@ -624,8 +698,11 @@ UAVS3E_CUDA_API int uavs3e_cuda_loka_estimate(const uavs3e_cuda_loka_cfg_t *cfg,
     const int n_search = cfg->num_ref[0] + cfg->num_ref[1];
     // device copies: org planes at stride W (16-aligned), references with `pad` samples around
     const int so = (W + 15) & ~15, soc = (Wc + 15) & ~15;
+    // the device copies carry `pad` samples around the picture; the caller's planes need
+    // padding only when the search may leave the picture (only then is the padding copied)
     const int pad = cfg->is_padding ? 144 : 4;
-    if (n_search && ref_pad < pad) return set_status(UC_ERR_ARG, "loka_estimate: reference padding");
+    if (n_search && cfg->is_padding && ref_pad < 144)
+        return set_status(UC_ERR_ARG, "loka_estimate: reference padding");
     const int sr = (W + 2 * pad + 15) & ~15;
     const size_t plane = (size_t)sr * (H + 2 * pad);
     rc = grow(&S.org, &S.org_cap, (size_t)so * H + 2 * (size_t)soc * Hc);
