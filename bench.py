@@ -37,8 +37,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="me,lattice,pruning,lookahead",
-                    help="comma list of legs: me (the headline line), lattice, pruning, lookahead")
+    ap.add_argument("--legs", default="me,lattice,pruning,lookahead,tz",
+                    help="comma list of legs: me (the headline line), lattice, pruning, lookahead, tz")
     ap.add_argument("--pruning-steps", type=int, default=3000, help="training steps of the pruning leg")
     return ap.parse_args()
 
@@ -428,6 +428,77 @@ def lookahead_leg(u, torch, stream, flush, sm_count, sm_mhz, with_cpu, reps=20):
     return out
 
 
+def tz_leg(u, torch, stream, flush, with_cpu, reps=10):
+    """per-call TZ motion searches (me_search_tz) of a 1080p frame: every block of the ten shapes
+    on the CTU grid against 2 references, each at a random AMVR resolution with a random
+    predictor, 30 % of them bi calls against the other reference's prediction"""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cases
+    from uavs3e_gb300.synth import motion_sequence
+    seq = motion_sequence(W, H, 3, seed=31)
+    ms = u.MotionSearch(W, H, n_refs=2, search_range=RANGE, pad=PAD)
+    sp = stream.cuda_stream
+    d_seq = [torch.from_numpy(f).cuda() for f in seq]
+    ms.set_ref_device(0, d_seq[1].data_ptr(), W, sp)
+    ms.set_ref_device(1, d_seq[0].data_ptr(), W, sp)
+    rng = np.random.default_rng(17)
+    b = u.me_blocks(W, H)
+    blocks = b[(b[:, 0] + b[:, 2] <= W) & (b[:, 1] + b[:, 3] <= H)]
+    reqs = cases.tz_requests(rng, W, H, 2 * len(blocks), [1, 2])
+    for i, f in enumerate(("x", "y", "w", "h")):
+        reqs[f] = np.repeat(blocks[:, i], 2)
+    reqs["ref_slot"] = np.tile([0, 1], len(blocks))
+    reqs["other_slot"] = 1 - reqs["ref_slot"]
+    reqs["dist"] = reqs["ref_slot"] + 1
+    n = len(reqs)
+    planes = [ms.plane_ptr(s, ph) for s in range(2) for ph in range(16)]
+    pic = (W, H, 1, 384, 16)
+    d_req = torch.from_numpy(reqs.view(np.uint8).copy()).cuda()
+    d_out = torch.empty(n * u.TZ_OUT.itemsize, dtype=torch.uint8, device="cuda")
+
+    def run():
+        u.me_tz_device(pic, d_seq[2].data_ptr(), W, planes, ms.stride, PAD, d_req.data_ptr(), n, d_out.data_ptr(), sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms_gpu = sum(a.elapsed_time(b) for a, b in evs) / reps
+    # end to end: host org + requests in, results out, through the session entry
+    org_pin = torch.from_numpy(seq[2]).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        got = ms.tz(pic, org_pin.numpy(), reqs)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / reps
+    out = {"workload": f"me_search_tz calls of a 1080p frame: {len(blocks)} blocks (10 shapes 8x8..64x64 on the CTU "
+                       "grid) x 2 references, AMVR resolutions 0..4, 30 % bi, SATD/SAD refinement mixed",
+           "calls": n, "ms_per_batch": ms_gpu, "calls_per_s": n / (ms_gpu / 1000.0),
+           "bi_calls": int(reqs["bi"].sum()),
+           "e2e": {"ms_per_batch": e2e_ms, "calls_per_s": n / (e2e_ms / 1000.0),
+                   "h2d_bytes": int(W * H + reqs.nbytes), "d2h_bytes": int(got.nbytes),
+                   "path": "uavs3e_cuda_me_tz (host org and requests, session references)"}}
+    if with_cpu:
+        import pyoracle
+        o = pyoracle.Oracle()
+        keep, addrs, stride = cases.tz_planes(o, {t: (seq[t],) for t in range(3)}, [1, 0], W, H)
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        o.me_tz(pic, seq[2], W, addrs, stride, reqs, threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "calls/s", "cores": threads, "kind": "port",
+                               "sample": f"the whole batch through the oracle restatement, {dt:.2f} s"}
+    ms.close()
+    return out
+
+
 def pruning_leg(steps=3000):
     """the learned CU pruning beside the lattice: trained on the plain path's decisions over 16
     synthetic 1080p I-frames, evaluated on a held-out frame (RD-cost increase of the pruned
@@ -575,6 +646,7 @@ def run_ours(args):
     pruning = pruning_leg(args.pruning_steps) if "pruning" in legs else None
     lookahead = (lookahead_leg(u, torch, stream, flush, sm_count, sm_mhz, not args.no_cpu)
                  if "lookahead" in legs else None)
+    tz = tz_leg(u, torch, stream, flush, not args.no_cpu) if "tz" in legs else None
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -594,6 +666,7 @@ def run_ours(args):
         "lattice": lattice,
         "pruning": pruning,
         "lookahead": lookahead,
+        "tz": tz,
         "clocks": clk,
     }
     if not args.no_cpu:
@@ -628,6 +701,8 @@ def run_legs(args):
     if "lookahead" in legs:
         out["lookahead"] = lookahead_leg(u, torch, torch.cuda.current_stream(), flush, sm_count, sm_mhz,
                                          not args.no_cpu)
+    if "tz" in legs:
+        out["tz"] = tz_leg(u, torch, torch.cuda.current_stream(), flush, not args.no_cpu)
     print(json.dumps(out))
 
 

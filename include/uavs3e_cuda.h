@@ -60,7 +60,7 @@ UAVS3E_CUDA_API const char *uavs3e_cuda_version(void);
 /* Kernel timing (observability; the reference has none): while enabled, every launch of the
  * batched kernels is bracketed by CUDA events on its stream.  collect() waits for them and
  * returns, per kernel id (0 pad, 1 frame interpolation, 2 integer search, 3 fractional
- * refinement, 4 intra lattice, 5 lookahead estimate), the summed milliseconds and launch counts,
+ * refinement, 4 intra lattice, 5 lookahead estimate, 6 TZ requests), the summed milliseconds and launch counts,
  * then forgets them. */
 UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
 /* Measured issue rate of the 4-sample SAD instruction (vabsdiff4 with accumulate) on the current
@@ -175,6 +175,64 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *me, const uint8_t 
 UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_org, int i_org, const uint8_t *const *d_planes,
                                                   int i_ref, int pad, int width, int height, int n_refs, int range,
                                                   uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);
+
+/* ------------------------------------------------------------ per-call TZ motion search */
+
+/*
+ * me_search_tz (src/me.c:529-568, declared inc/analyze.h:60) for a list of independent calls,
+ * each with the inter_search_t state it reads: integer search (search_diamond :199, and for
+ * uni-prediction search_raster :103 + a refinement diamond), the fractional refinement of
+ * me_sub_pel_search (:366) at quarter/half resolution, every AMVR resolution (curr_mvr 0..4),
+ * bi-prediction (the org replaced by 2 org - the other list's prediction, create_bi_org
+ * src/inter.c:55).  Each result equals that call of the reference: the MV it writes, the integer
+ * MV it stores in pi->mv_ipel (uni), and its return value.
+ */
+#define UAVS3E_CUDA_TZ_SAD             1   /* flags: pi->subpel_cost_type = 1 (SAD refinement) */
+#define UAVS3E_CUDA_TZ_ADAPTIVE_RANGE  2   /* flags: pi->adaptive_raster_range                 */
+#define UAVS3E_CUDA_TZ_MAX_SLOTS       8
+
+typedef struct {
+    int16_t  x, y;            /* block position (luma samples)                                 */
+    uint8_t  w, h;            /* block size, 4..64 (powers of two)                             */
+    uint8_t  ref_slot;        /* planes of pi->ref_pic                                         */
+    int8_t   refi;            /* reference index in its list (raster step, reference bits)     */
+    uint8_t  num_refp;        /* pi->num_refp                                                  */
+    uint8_t  mvr;             /* pi->curr_mvr 0..4                                             */
+    uint8_t  bi;              /* the bi argument                                               */
+    uint8_t  flags;           /* UAVS3E_CUDA_TZ_*                                              */
+    int16_t  mvp[2];          /* predictor, quarter samples, a multiple of 1 << mvr            */
+    int16_t  mv[2];           /* bi: start MV (pi->mv_scale), quarter samples, same grid        */
+    int16_t  mv_ipel[2];      /* pi->mv_ipel[lidx][refi] (adaptive raster range), samples      */
+    int16_t  other_mv[2];     /* bi: the other list's MV, quarter samples                      */
+    uint8_t  other_slot;      /* bi: planes of the other list's reference                      */
+    uint8_t  pad0[3];
+    int32_t  mot_bits_other;  /* bi: pi->mot_bits of the other list                            */
+    uint32_t lambda_mv;       /* pi->lambda_mv                                                 */
+    int32_t  dist;            /* |pi->ptr - ref_pic->ptr|                                      */
+    int32_t  pad1;
+} uavs3e_cuda_tz_req_t;
+
+typedef struct {
+    int16_t  mv[2];           /* the MV the call writes (quarter samples)                      */
+    int16_t  mv_ipel[2];      /* pi->mv_ipel[lidx][refi] after the call                        */
+    uint64_t cost;            /* return value; UINT64_MAX when the MV range is empty or the    */
+                              /* request is outside the supported domain (MVs left unchanged)  */
+} uavs3e_cuda_tz_out_t;
+
+/* picture-level inter_search_t fields (inter_search_init, src/inter.c:2015) */
+typedef struct { int width, height, is_padding, max_search_range, gop_size; } uavs3e_cuda_tz_pic_t;
+
+/* Requests against a motion-search session's references (slot = session slot), host buffers,
+ * synchronous: org is the current picture (row stride i_org). */
+UAVS3E_CUDA_API int uavs3e_cuda_me_tz(uavs3e_cuda_me *me, const uavs3e_cuda_tz_pic_t *pic, const uint8_t *org,
+                                      int i_org, const uavs3e_cuda_tz_req_t *reqs, int n, uavs3e_cuda_tz_out_t *out);
+/* Device form: d_planes is a host array of n_slots * 16 device pointers (slot-major, phase
+ * dy*4 + dx, 0 = integer plane) to sample (0,0) of planes padded by pad >= 144 with stride i_ref
+ * (a multiple of 4); max_search_range <= 1024. */
+UAVS3E_CUDA_API int uavs3e_cuda_me_tz_device(const uavs3e_cuda_tz_pic_t *pic, const uint8_t *d_org, int i_org,
+                                             const uint8_t *const *d_planes, int n_slots, int i_ref, int pad,
+                                             const uavs3e_cuda_tz_req_t *d_reqs, int n, uavs3e_cuda_tz_out_t *d_out,
+                                             void *stream);
 
 /* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
  * session's plane stride; for inspection by tests. */

@@ -1473,3 +1473,216 @@ double orc_loka_finish(const orc_loka_cfg_t *cfg, const orc_loka_unit_t *units, 
     }
     return tc / n / 16 / 16;
 }
+
+/* ======================================================= per-call TZ motion search */
+
+/* tbl_refi_bits (src/tables.c:52): truncated unary code of refi among num_refp references */
+static int refi_bits(int num_refp, int refi)
+{
+    return num_refp <= 1 ? 0 : MIN(refi + 1, num_refp - 1);
+}
+
+/* the state of one me_search_tz call (inter_search_t fields it reads, src/me.c:529) */
+typedef struct {
+    const pel *org; int i_org;          /* block origin of org (or of 2 org - pred for bi)  */
+    const pel *ref; int i_ref;          /* integer plane at the block origin                */
+    const pel *const *planes;           /* the reference's 16 planes                        */
+    int x, y, w, h;
+    int minx, maxx, miny, maxy;         /* integer-sample MV range                          */
+    int mvr;
+    u32 lambda;
+    const u8 *bx, *by;                  /* MV-bits tables offset by the predictor           */
+    int shift;                          /* 16 - bi                                          */
+    u64 best; int mvx, mvy;
+} tzg_t;
+
+static u64 tzg_cost(const tzg_t *c, int mx, int my)
+{
+    u32 sad = orc_sad(c->w, c->h, c->org, c->i_org, c->ref + my * c->i_ref + mx, c->i_ref);
+    u32 bits = (u32)(c->bx[(mx * 4) >> c->mvr] + c->by[(my * 4) >> c->mvr]);
+    return ((u64)sad << c->shift) + (u64)(bits * c->lambda);
+}
+
+static int tzg_try(tzg_t *c, int mx, int my)
+{
+    u64 cost = tzg_cost(c, mx, my);
+    if (cost < c->best) { c->best = cost; c->mvx = mx; c->mvy = my; return 1; }
+    return 0;
+}
+
+/* search_diamond (src/me.c:199-334) for any MV resolution, bi or not */
+static int tzg_diamond(tzg_t *c, int max_step, int bi, const s16 *mvp)
+{
+    static const s8 RING_A[8][2] = { { -2, 0 }, { -1, 1 }, { 0, 2 }, { 1, 1 },
+                                     { 2, 0 }, { 1, -1 }, { 0, -2 }, { -1, -1 } };
+    static const s8 RING_B[16][2] = { { -4, 0 }, { -3, 1 }, { -2, 2 }, { -1, 3 }, { 0, 4 }, { 1, 3 },
+                                      { 2, 2 }, { 3, 1 }, { 4, 0 }, { 3, -1 }, { 2, -2 }, { 1, -3 },
+                                      { 0, -4 }, { -1, -3 }, { -2, -2 }, { -3, -1 } };
+    const int cx = c->mvx, cy = c->mvy;
+    int core = bi ? 5 : 2, cstep = 1, best_step = 0;
+    if (bi) {
+        if (c->mvr > 2) core++;
+        int ix = (mvp[0] + 2) >> 2, iy = (mvp[1] + 2) >> 2;
+        int diff = MAX(ABSI(ix - cx), ABSI(iy - cy)) >> MAX(0, c->mvr - 2);
+        core = CLIP3(2, core, diff);
+    }
+    if (c->mvr > 2) { core <<= c->mvr - 2; cstep <<= c->mvr - 2; }
+    int x0 = cx - core, y0 = cy - core, x1 = cx + core, y1 = cy + core;
+    while (x0 <= c->minx) x0 += cstep;
+    while (y0 <= c->miny) y0 += cstep;
+    while (x1 >= c->maxx) x1 -= cstep;
+    while (y1 >= c->maxy) y1 -= cstep;
+    tzg_try(c, cx, cy);
+    if (max_step)
+        for (int my = y0; my <= y1; my += cstep)
+            for (int mx = x0; mx <= x1; mx += cstep) tzg_try(c, mx, my);
+    if (c->mvx != cx || c->mvy != cy) best_step = 2;
+    if (bi) return best_step;
+    int mvr_scale = MAX(c->mvr - 2, 0);
+    for (int step = 4, round = 0; step < max_step; step <<= 1, round++) {
+        int scale = (step << mvr_scale) >> 1;
+        const s8(*ring)[2] = round < 2 ? RING_A : RING_B;
+        int n = round < 2 ? 8 : 16, inc = round < 1 ? 2 : 1, sh = round < 2 ? 0 : 1;
+        for (int i = 0; i < n; i += inc) {
+            int mx = cx + (scale >> sh) * ring[i][0], my = cy + (scale >> sh) * ring[i][1];
+            if (mx <= c->maxx && mx >= c->minx && my <= c->maxy && my >= c->miny && tzg_try(c, mx, my))
+                best_step = step;
+        }
+    }
+    return best_step;
+}
+
+/* search_raster with get_raster_range (src/me.c:65-197) for any MV resolution */
+static void tzg_raster(tzg_t *c, const orc_tz_req_t *rq, const orc_tz_pic_t *pic)
+{
+    static const int BASE[5] = { 5, 5, 5, 6, 8 }, SMIN[5] = { 1, 1, 1, 2, 4 };
+    const int mvr = c->mvr;
+    int step = MAX(BASE[mvr], MIN(c->w >> 1, c->h >> 1)) * (rq->refi + 1);
+    int max_sr = pic->max_search_range >> MAX(3 - mvr, 0);
+    int rxy = CLIP3(max_sr >> 2, max_sr, (max_sr * rq->dist + (pic->gop_size >> 1)) / pic->gop_size);
+    int rx = rxy, ry = rxy;
+    if (mvr && (rq->flags & 2)) {
+        rx = ABSI(rq->mv_ipel[0] - c->mvx) * 4;
+        ry = ABSI(rq->mv_ipel[1] - c->mvy) * 2;
+        rx = MIN(MAX(MAX(rx, max_sr >> 2), step * 8), rxy);
+        ry = MIN(MAX(MAX(ry, max_sr >> 2), step * 4), rxy);
+    }
+    if (mvr > 2) { rx = (rx >> (mvr - 2)) << (mvr - 2); ry = (ry >> (mvr - 2)) << (mvr - 2); }
+    int x0 = CLIP3(c->minx, c->maxx, c->mvx - rx), x1 = CLIP3(c->minx, c->maxx, c->mvx + rx);
+    int y0 = CLIP3(c->miny, c->maxy, c->mvy - ry), y1 = CLIP3(c->miny, c->maxy, c->mvy + ry);
+    for (int round = 0; step >= SMIN[mvr]; round++) {
+        if (round) {
+            x0 = MAX(c->mvx - step, c->minx); x1 = MIN(c->mvx + step, c->maxx);
+            y0 = MAX(c->mvy - step, c->miny); y1 = MIN(c->mvy + step, c->maxy);
+        }
+        for (int my = y0; my <= y1; my += step)
+            for (int mx = x0; mx <= x1; mx += step) tzg_try(c, mx, my);
+        step >>= 1;
+        if (mvr > 2) step = (step >> (mvr - 2)) << (mvr - 2);
+    }
+}
+
+/* me_sub_pel_search (src/me.c:366-500): centre, 8 half-sample points, then (quarter-sample
+ * resolution) 8 quarter-sample points; SATD cost, or SAD with the SATD recomputed at the end */
+static u64 tzg_subpel(tzg_t *c, int *qx, int *qy, int bi, int cost_type, int W, int H)
+{
+    static const s8 HP[8][2] = { { -2, 0 }, { -2, 2 }, { 0, 2 }, { 2, 2 }, { 2, 0 }, { 2, -2 }, { 0, -2 }, { -2, -2 } };
+    static const s8 QP[8][2] = { { -1, 0 }, { 0, 1 }, { 1, 0 }, { 0, -1 }, { -1, 1 }, { 1, 1 }, { -1, -1 }, { 1, -1 } };
+    const int maxx = W + 4, maxy = H + 4, shift = 16 - bi, mvr = c->mvr;
+    int cx = *qx, cy = *qy;
+    const pel *p0 = c->ref + (cx >> 2) + (cy >> 2) * c->i_ref;
+    u32 d = cost_type ? orc_sad(c->w, c->h, c->org, c->i_org, p0, c->i_ref)
+                      : orc_had(c->w, c->h, c->org, c->i_org, p0, c->i_ref, 8);
+    u64 best = (u64)(c->lambda * (u32)(c->bx[cx >> mvr] + c->by[cy >> mvr])) + ((u64)d << shift);
+    for (int pass = 0; pass < (mvr == 0 ? 2 : 1); pass++) {
+        const s8(*pat)[2] = pass ? QP : HP;
+        cx = *qx; cy = *qy;
+        for (int i = 0; i < 8; i++) {
+            int vx = cx + pat[i][0], vy = cy + pat[i][1];
+            const pel *p = mc_pointer(c->planes, c->i_ref, vx + (c->x << 2), vy + (c->y << 2), maxx, maxy);
+            d = cost_type ? orc_sad(c->w, c->h, c->org, c->i_org, p, c->i_ref)
+                          : orc_had(c->w, c->h, c->org, c->i_org, p, c->i_ref, 8);
+            u64 cost = (u64)(c->lambda * (u32)(c->bx[vx >> mvr] + c->by[vy >> mvr])) + ((u64)d << shift);
+            if (cost < best) { best = cost; *qx = vx; *qy = vy; }
+        }
+    }
+    if (cost_type) {
+        const pel *p = mc_pointer(c->planes, c->i_ref, *qx + (c->x << 2), *qy + (c->y << 2), maxx, maxy);
+        d = orc_had(c->w, c->h, c->org, c->i_org, p, c->i_ref, 8);
+        best = (u64)(c->lambda * (u32)(c->bx[*qx >> mvr] + c->by[*qy >> mvr])) + ((u64)d << (16 - bi));
+    }
+    return best;
+}
+
+static void tz_one(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *const *planes, int i_ref,
+                   const u8 *bits, int mto, const orc_tz_req_t *rq, orc_tz_out_t *o)
+{
+    const int x = rq->x, y = rq->y, w = rq->w, h = rq->h, mvr = rq->mvr, bi = rq->bi;
+    const int W = pic->width, H = pic->height;
+    tzg_t c;
+    pel org_bi[64 * 64];
+    o->mv[0] = rq->mv[0]; o->mv[1] = rq->mv[1];
+    o->mv_ipel[0] = rq->mv_ipel[0]; o->mv_ipel[1] = rq->mv_ipel[1];
+    /* get_max_search_range (src/me.c:502-527) */
+    int mt = (mto << mvr) >> 2, px = rq->mvp[0] >> 2, py = rq->mvp[1] >> 2;
+    if (pic->is_padding) {
+        c.minx = MAX(-128 + 1 - x, px - mt + 4); c.miny = MAX(-128 + 1 - y, py - mt + 4);
+        c.maxx = MIN(W - 1 - x, px + mt - 4);     c.maxy = MIN(H - 1 - y, py + mt - 4);
+    } else {
+        c.minx = MAX(-x, px - mt + 4);             c.miny = MAX(-y, py - mt + 4);
+        c.maxx = MIN(W - 1 - x - w, px + mt - 4);  c.maxy = MIN(H - 1 - y - h, py + mt - 4);
+    }
+    if (mvr > 2) {   /* com_ipel_range_rounding: towards zero to a multiple of 1 << (mvr - 2) */
+        int s = mvr - 2;
+        int *v[4] = { &c.minx, &c.miny, &c.maxx, &c.maxy };
+        for (int i = 0; i < 4; i++) *v[i] = *v[i] >= 0 ? ((*v[i] >> s) << s) : -(((-*v[i]) >> s) << s);
+    }
+    if (c.minx > c.maxx || c.miny > c.maxy) { o->cost = ~(u64)0; return; }
+    const pel *const *pl = planes + rq->ref_slot * 16;
+    c.planes = pl; c.i_ref = i_ref; c.ref = pl[0] + y * i_ref + x;
+    c.x = x; c.y = y; c.w = w; c.h = h; c.mvr = mvr; c.lambda = rq->lambda_mv; c.shift = 16 - bi;
+    c.bx = bits - (rq->mvp[0] >> mvr); c.by = bits - (rq->mvp[1] >> mvr);
+    if (bi) {
+        /* create_bi_org (src/inter.c:55) against com_mc_cu's prediction of the other list */
+        const pel *pr = mc_pointer(planes + rq->other_slot * 16, i_ref, (x << 2) + rq->other_mv[0],
+                                   (y << 2) + rq->other_mv[1], W + 4, H + 4);
+        const pel *og = org + y * i_org + x;
+        for (int j = 0; j < h; j++)
+            for (int i = 0; i < w; i++) org_bi[j * w + i] = (pel)CLIP3(0, 255, 2 * og[j * i_org + i] - pr[j * i_ref + i]);
+        c.org = org_bi; c.i_org = w;
+    } else {
+        c.org = org + y * i_org + x; c.i_org = i_org;
+    }
+    int mvx = bi ? rq->mv[0] : rq->mvp[0], mvy = bi ? rq->mv[1] : rq->mvp[1];
+    c.mvx = CLIP3(c.minx, c.maxx, (mvx + 2) >> 2);
+    c.mvy = CLIP3(c.miny, c.maxy, (mvy + 2) >> 2);
+    c.best = ~(u64)0;
+    int bs = tzg_diamond(&c, 32, bi, rq->mvp);
+    if (!bi && (ABSI(rq->mvp[0] - (c.mvx << 2)) > 2 || ABSI(rq->mvp[1] - (c.mvy << 2)) > 2)) {
+        if (bs > 5) tzg_raster(&c, rq, pic);
+        tzg_diamond(&c, 8, bi, rq->mvp);
+    }
+    if (!bi) { o->mv_ipel[0] = (s16)c.mvx; o->mv_ipel[1] = (s16)c.mvy; }
+    int qx = c.mvx << 2, qy = c.mvy << 2;
+    u64 cost = c.best;
+    if (mvr < 2) cost = tzg_subpel(&c, &qx, &qy, bi, rq->flags & 1, W, H);
+    int extra = refi_bits(rq->num_refp, rq->refi) + mvr + (mvr < 4) + (bi ? rq->mot_bits_other + 1 : 2);
+    cost += (u64)(rq->lambda_mv * (u32)extra);
+    o->mv[0] = (s16)qx; o->mv[1] = (s16)qy;
+    o->cost = (u32)((cost + (1 << 15)) >> 16);
+}
+
+void orc_me_tz(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *const *planes, int i_ref,
+               const orc_tz_req_t *reqs, int n, orc_tz_out_t *out, int threads)
+{
+    int off = (MAX(pic->width, pic->height) << 2) + 3;
+    u8 *tab = (u8 *)malloc((size_t)(2 * off + 1));
+    orc_mvbits_table(tab, off);
+#ifdef _OPENMP
+    if (threads < 1) threads = 1;
+    #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+#endif
+    for (int i = 0; i < n; i++) tz_one(pic, org, i_org, planes, i_ref, tab + off, off, &reqs[i], &out[i]);
+    (void)threads;
+    free(tab);
+}

@@ -175,6 +175,44 @@ typedef struct {
 void orc_loka_units(const orc_loka_cfg_t *cfg, const pel *org_y, int i_org, const pel *org_u, const pel *org_v,
                     int i_org_c, const pel *const *ref_l0, const pel *const *ref_l1, int i_ref,
                     orc_loka_unit_t *units, int threads);
+/* ----------------------- per-call TZ motion search (me_search_tz, src/me.c:529-568) ----------------------- */
+
+/* one call of me_search_tz: the block, the reference (a slot of the planes array), and the
+ * inter_search_t state the call reads */
+typedef struct {
+    s16 x, y;           /* block position (luma samples)                                  */
+    u8  w, h;           /* block size, 4..64                                             */
+    u8  ref_slot;       /* planes of pi->ref_pic: planes[ref_slot * 16 + phase]           */
+    s8  refi;           /* reference index in its list (raster step, reference bits)      */
+    u8  num_refp;       /* pi->num_refp                                                   */
+    u8  mvr;            /* pi->curr_mvr, 0 (quarter) .. 4 (4 samples)                     */
+    u8  bi;             /* 1: search against 2 org - the other list's prediction          */
+    u8  flags;          /* bit 0: subpel_cost_type (SAD), bit 1: adaptive_raster_range    */
+    s16 mvp[2];         /* predictor, quarter samples (a multiple of 1 << mvr)            */
+    s16 mv[2];          /* bi: start MV (quarter samples, a multiple of 1 << mvr)         */
+    s16 mv_ipel[2];     /* pi->mv_ipel[lidx][refi] (adaptive raster range), samples       */
+    s16 other_mv[2];    /* bi: MV of the other list (quarter samples)                     */
+    u8  other_slot;     /* bi: planes slot of the other list's reference                  */
+    u8  pad0[3];
+    s32 mot_bits_other; /* bi: pi->mot_bits of the other list                             */
+    u32 lambda_mv;
+    s32 dist;           /* |POC of the picture - POC of the reference|                    */
+    s32 pad1;
+} orc_tz_req_t;
+
+typedef struct {
+    s16 mv[2];          /* the MV me_search_tz writes (quarter samples)                   */
+    s16 mv_ipel[2];     /* the integer winner it stores in pi->mv_ipel (uni searches)     */
+    u64 cost;           /* its return value; UINT64_MAX when the MV range is empty        */
+} orc_tz_out_t;
+
+typedef struct { int width, height, is_padding, max_search_range, gop_size; } orc_tz_pic_t;
+
+/* planes[slot * 16 + dy * 4 + dx]: the quarter-sample planes of each reference (0 = integer),
+ * stride i_ref, padded by >= 144.  Uses OpenMP over requests when threads > 1. */
+void orc_me_tz(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *const *planes, int i_ref,
+               const orc_tz_req_t *reqs, int n, orc_tz_out_t *out, int threads);
+
 /* the picture-level results from the records (src/lookahead.c:255-292): returns the picture
  * SATD cost; icost, icost_uv[2], map_dqp[units] are filled when non-NULL */
 double orc_loka_finish(const orc_loka_cfg_t *cfg, const orc_loka_unit_t *units, double *icost, double *icost_uv,

@@ -195,6 +195,16 @@ class Oracle(_Common):
         cost, icost, icost_uv, dqp = self.loka_finish(cfg, units)
         return cost, icost, icost_uv if want_uv else None, dqp if want_dqp else None
 
+    def me_tz(self, pic, org, i_org, plane_ptrs, i_ref, reqs, threads=1):
+        """per-call TZ searches: pic = (W, H, is_padding, max_search_range, gop_size); plane_ptrs =
+        slot-major addresses of the 16 planes of each reference; reqs: TZ_REQ array -> TZ_OUT"""
+        p = (C.c_int * 5)(*pic)
+        arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
+        reqs = np.ascontiguousarray(reqs, dtype=TZ_REQ)
+        out = np.zeros(len(reqs), dtype=TZ_OUT)
+        self.L.orc_me_tz(p, ptr(org), i_org, arr, i_ref, ptr(reqs), len(reqs), ptr(out), threads)
+        return out
+
     def loka_finish(self, cfg, units):
         """(picture cost, icost, icost_uv[2], map_dqp) from the unit records"""
         cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
@@ -329,6 +339,17 @@ class RefLib(_Common):
                                          icost_uv if want_uv else None, ptr(dqp) if want_dqp else None)
         return (cost, icost.value, (icost_uv[0], icost_uv[1]) if want_uv else None, dqp if want_dqp else None)
 
+    def me_tz(self, pic, org, i_org, plane_ptrs, i_ref, reqs, threads=1):
+        """me_search_tz itself, one call per request (same arguments as Oracle.me_tz)"""
+        arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
+        reqs = np.ascontiguousarray(reqs, dtype=TZ_REQ)
+        out = np.zeros(len(reqs), dtype=TZ_OUT)
+        for i in range(len(reqs)):
+            self.L.refk_me_tz(pic[0], pic[1], pic[2], pic[3], pic[4], ptr(org), i_org, arr, i_ref,
+                              C.c_void_p(reqs.ctypes.data + i * TZ_REQ.itemsize),
+                              C.c_void_p(out.ctypes.data + i * TZ_OUT.itemsize))
+        return out
+
     def loka_search(self, cfg, org_y, i_org, ref, i_ref, ref_ptr, refi, num_refp, x, y):
         """me_search_tz of one 16x16 unit with the lookahead's settings: (mv_x, mv_y, cost)"""
         c = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)[0]
@@ -351,6 +372,12 @@ LOKA_CFG = np.dtype([("width", "<i4"), ("height", "<i4"), ("is_padding", "<i4"),
 LOKA_UNIT = np.dtype([("mv", "<i2", (2, 4, 2)), ("satd", "<u4", (2, 4)), ("bi_satd", "<u4"), ("zero_satd", "<u4"),
                       ("min_cost", "<u4"), ("min_icost", "<u4"), ("icost_u", "<u4"), ("icost_v", "<u4"),
                       ("energy", "<u8"), ("best_mode", "u1"), ("pad", "u1", (7,))])
+TZ_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("ref_slot", "u1"), ("refi", "i1"),
+                   ("num_refp", "u1"), ("mvr", "u1"), ("bi", "u1"), ("flags", "u1"), ("mvp", "<i2", (2,)),
+                   ("mv", "<i2", (2,)), ("mv_ipel", "<i2", (2,)), ("other_mv", "<i2", (2,)), ("other_slot", "u1"),
+                   ("pad0", "u1", (3,)), ("mot_bits_other", "<i4"), ("lambda_mv", "<u4"), ("dist", "<i4"),
+                   ("pad1", "<i4")])
+TZ_OUT = np.dtype([("mv", "<i2", (2,)), ("mv_ipel", "<i2", (2,)), ("cost", "<u8")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
 
 MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],

@@ -261,3 +261,82 @@ unsigned long long refk_loka_search(int W, int H, int is_padding, int max_search
     free(pi);
     return cost;
 }
+
+/* ---- 4. per-call TZ motion search ---------------------------------------------------------
+ * me_search_tz (src/me.c:529) for one request on caller planes: planes[slot * 16 + phase] are the
+ * quarter-sample planes of each reference (0 = integer plane; stride i_ref; padded).  The
+ * inter_search_t is set up as inter_search_init does, with the request's state; a bi request's
+ * org is 2 org - (the other list's prediction by com_mc_blk_luma), clipped, as create_bi_org
+ * (src/inter.c:55) forms it.  Layout of req/out: orc_tz_req_t / orc_tz_out_t (oracle.h). */
+typedef struct {
+    s16 x, y; u8 w, h; u8 ref_slot; s8 refi; u8 num_refp; u8 mvr; u8 bi; u8 flags;
+    s16 mvp[2]; s16 mv[2]; s16 mv_ipel[2]; s16 other_mv[2]; u8 other_slot; u8 pad0[3];
+    s32 mot_bits_other; u32 lambda_mv; s32 dist; s32 pad1;
+} glue_tz_req_t;
+typedef struct { s16 mv[2]; s16 mv_ipel[2]; u64 cost; } glue_tz_out_t;
+
+static void tz_pic(com_pic_t *pic, com_subpel_t *sp, com_img_t imgs[16], pel **planes, int slot, int W, int H,
+                   int i_ref, long long ptr)
+{
+    memset(pic, 0, sizeof(*pic));
+    memset(sp, 0, sizeof(*sp));
+    for (int i = 0; i < 16; i++) {
+        loka_img(&imgs[i], W, H, ptr, planes[slot * 16 + i], i_ref, NULL, NULL, 0);
+        sp->imgs[i >> 2][i & 3] = &imgs[i];
+    }
+    pic->subpel = sp;
+    pic->ptr = ptr;
+    pic->img = &imgs[0];
+    pic->stride_luma = i_ref;
+    pic->y = planes[slot * 16];
+    pic->width_luma = W;
+    pic->height_luma = H;
+}
+
+void refk_me_tz(int W, int H, int is_padding, int max_search_range, int gop_size, pel *org, int i_org,
+                pel **planes, int i_ref, const glue_tz_req_t *rq, glue_tz_out_t *out)
+{
+    refk_init();
+    static com_info_t info;
+    inter_search_t *pi = (inter_search_t *)calloc(1, sizeof(inter_search_t));
+    loka_setup(&info, pi, W, H, is_padding, max_search_range, gop_size);
+    static com_pic_t pic, pic_o;
+    static com_subpel_t sp, sp_o;
+    static com_img_t imgs[16], imgs_o[16];
+    tz_pic(&pic, &sp, imgs, planes, rq->ref_slot, W, H, i_ref, 0);
+    ALIGNED_32(pel org_bi[MAX_CU_DIM]);
+    const int x = rq->x, y = rq->y, w = rq->w, h = rq->h;
+    pi->ptr = rq->dist;
+    pi->curr_mvr = rq->mvr;
+    pi->lambda_mv = rq->lambda_mv;
+    pi->num_refp = rq->num_refp;
+    pi->subpel_cost_type = rq->flags & 1;
+    pi->adaptive_raster_range = (rq->flags >> 1) & 1;
+    pi->mv_ipel[REFP_0][rq->refi][0] = rq->mv_ipel[0];
+    pi->mv_ipel[REFP_0][rq->refi][1] = rq->mv_ipel[1];
+    pi->mot_bits[REFP_1] = rq->mot_bits_other;
+    pi->ref_pic = &pic;
+    if (rq->bi) {
+        ALIGNED_32(pel pred[MAX_CU_DIM]);
+        tz_pic(&pic_o, &sp_o, imgs_o, planes, rq->other_slot, W, H, i_ref, 0);
+        com_mc_blk_luma(&pic_o, pred, w, (x << 2) + rq->other_mv[0], (y << 2) + rq->other_mv[1], w, h,
+                        CONV_LOG2(w) - MIN_CU_LOG2, pi->max_coord[MV_X], pi->max_coord[MV_Y], 255, 0);
+        const pel *o = org + y * i_org + x;
+        for (int j = 0; j < h; j++)
+            for (int i = 0; i < w; i++) org_bi[j * w + i] = (pel)COM_CLIP3(0, 255, (o[j * i_org + i] << 1) - pred[j * w + i]);
+        pi->org = org_bi;
+        pi->i_org = w;
+    } else {
+        pi->org = org + y * i_org + x;
+        pi->i_org = i_org;
+    }
+    s16 mvp[2] = { rq->mvp[0], rq->mvp[1] };
+    s16 mv[2] = { rq->mv[0], rq->mv[1] };
+    out->cost = me_search_tz(pi, x, y, w, h, W, H, rq->refi, REFP_0, mvp, mv, rq->bi);
+    out->mv[0] = mv[0];
+    out->mv[1] = mv[1];
+    out->mv_ipel[0] = rq->bi ? rq->mv_ipel[0] : pi->mv_ipel[REFP_0][rq->refi][0];
+    out->mv_ipel[1] = rq->bi ? rq->mv_ipel[1] : pi->mv_ipel[REFP_0][rq->refi][1];
+    inter_search_free(info.tab_mvbits, pi->tab_mvbits_offset);
+    free(pi);
+}

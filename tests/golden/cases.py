@@ -367,12 +367,86 @@ def run_loka(B, p, seed):
     return digest(*outs)
 
 
+# ------------------------------------------------------------------ per-call TZ motion search
+TZ_PAD = 144
+TZ_SIZES = [(8, 8), (16, 16), (32, 32), (64, 64), (16, 8), (8, 16), (32, 16), (16, 32), (64, 32), (32, 64),
+            (8, 32), (32, 8), (16, 64), (64, 16), (4, 8), (8, 4), (4, 16), (16, 4)]
+
+
+def tz_planes(B, frames, pocs, W, H):
+    """slot-major 16 planes (integer + 15 quarter-sample, padded by TZ_PAD) of the pictures at
+    `pocs`, interpolated by the backend's own com_if_luma_frame; returns (arrays, addresses, stride)"""
+    stride = W + 2 * TZ_PAD
+    base = TZ_PAD * stride + TZ_PAD
+    keep = []
+    for t in pocs:
+        p0 = padded_plane(frames[t][0], TZ_PAD, stride).reshape(-1)
+        fr = [np.zeros_like(p0) for _ in range(15)]
+        B.if_luma_frame(p0.ctypes.data + base, [q.ctypes.data + base for q in fr], W, H, TZ_PAD, stride)
+        keep += [p0] + fr
+    return keep, [a.ctypes.data + base for a in keep], stride
+
+
+def tz_requests(rng, W, H, n, dists, bi_share=0.3):
+    """n me_search_tz calls with the encoder's ranges of state: any MV resolution, predictors and
+    bi start MVs on that resolution's grid, both cost types, adaptive raster ranges"""
+    import pyoracle
+    r = np.zeros(n, dtype=pyoracle.TZ_REQ)
+    for i in range(n):
+        w, h = TZ_SIZES[int(rng.integers(len(TZ_SIZES)))]
+        mvr = int(rng.integers(0, 5))
+        unit = 1 << mvr
+        q = int(rng.integers(22, 46))
+        r[i]["x"] = int(rng.integers(0, (W - w) // 4 + 1)) * 4
+        r[i]["y"] = int(rng.integers(0, (H - h) // 4 + 1)) * 4
+        r[i]["w"], r[i]["h"] = w, h
+        r[i]["ref_slot"] = int(rng.integers(0, len(dists)))
+        r[i]["num_refp"] = int(rng.integers(1, 5))
+        r[i]["refi"] = int(rng.integers(0, r[i]["num_refp"]))
+        r[i]["mvr"] = mvr
+        r[i]["bi"] = int(rng.random() < bi_share)
+        r[i]["flags"] = int(rng.integers(0, 4))
+        r[i]["mvp"] = (rng.integers(-200, 201, 2) // unit) * unit
+        r[i]["mv"] = ((r[i]["mvp"] + rng.integers(-48, 49, 2)) // unit) * unit
+        r[i]["mv_ipel"] = rng.integers(-40, 41, 2)
+        r[i]["other_mv"] = rng.integers(-120, 121, 2)
+        r[i]["other_slot"] = int(rng.integers(0, len(dists)))
+        r[i]["mot_bits_other"] = int(rng.integers(2, 24))
+        r[i]["lambda_mv"] = int(np.floor(65536.0 * np.sqrt(1.43631 * 2.0 ** ((q - 16) / 4.0))))
+        r[i]["dist"] = dists[r[i]["ref_slot"]]
+    return r
+
+
+def tz_inputs(B, p, seed):
+    rng = np.random.default_rng(seed)
+    W, H = p["w"], p["h"]
+    frames = loka_frames(rng, W, H, [0, 4, 8], p["vel"])
+    keep, addrs, stride = tz_planes(B, frames, [4, 0], W, H)
+    reqs = tz_requests(rng, W, H, p["n"], [4, 8])
+    pic = (W, H, p["pad"], p["range"], p["gop"])
+    return pic, frames[8][0], keep, addrs, stride, reqs
+
+
+def run_tz(B, p, seed):
+    pic, org, keep, addrs, stride, reqs = tz_inputs(B, p, seed)
+    out = B.me_tz(pic, org, p["w"], addrs, stride, reqs)
+    return digest(out.view(np.uint8))
+
+
 RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz,
 }
+
+# TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
+# and one without padding
+TZ_CASES = [
+    dict(w=192, h=128, pad=1, range=384, gop=16, vel=(2.5, -1.25), n=96),
+    dict(w=160, h=96, pad=1, range=64, gop=4, vel=(-4.0, 3.0), n=96),
+    dict(w=128, h=128, pad=0, range=384, gop=16, vel=(1.75, 2.5), n=64),
+]
 
 # lookahead cases: encoder picture level (padded references, random access with both lists or
 # low delay with 4 references) and the scene-cut estimate (1 reference, no padding)
@@ -445,6 +519,8 @@ def all_cases():
     add("tables")
     for p in LOKA_CASES:
         add("loka", **p)
+    for p in TZ_CASES:
+        add("tz", **p)
     return cases
 
 

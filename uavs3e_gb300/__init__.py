@@ -63,6 +63,8 @@ def _declare(L):
     L.uavs3e_cuda_loka_finish.argtypes = [P, P, P, P, P, P]
     L.uavs3e_cuda_loka_finish.restype = C.c_double
     L.uavs3e_cuda_loka_sc_ratio.argtypes = [I, I, I, I, I, C.c_int64, P, I, P, P, I, P, C.c_int64, I, I, P]
+    L.uavs3e_cuda_me_tz.argtypes = [P, P, P, I, P, I, P]
+    L.uavs3e_cuda_me_tz_device.argtypes = [P, P, I, P, I, I, I, P, I, P, P]
 
 
 def check(rc, what="uavs3e_cuda"):
@@ -78,7 +80,7 @@ def init(device=0):
     check(lib().uavs3e_cuda_init(device), "uavs3e_cuda_init")
 
 
-PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka")
+PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz")
 
 CU = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
@@ -300,3 +302,34 @@ class MotionSearch:
 
     def plane_ptr(self, slot, phase):
         return lib().uavs3e_cuda_me_plane(self.h, slot, phase)
+
+    def tz(self, pic, org, reqs):
+        """me_search_tz calls (TZ_REQ array) against the session's references; returns TZ_OUT"""
+        org = np.ascontiguousarray(org, dtype=np.uint8)
+        reqs = np.ascontiguousarray(reqs, dtype=TZ_REQ)
+        out = np.zeros(max(1, len(reqs)), dtype=TZ_OUT)
+        p = np.array(pic, dtype=np.int32)
+        check(lib().uavs3e_cuda_me_tz(self.h, p.ctypes.data, org.ctypes.data, org.strides[0], reqs.ctypes.data,
+                                      len(reqs), out.ctypes.data), "me_tz")
+        return out[:len(reqs)]
+
+
+# ------------------------------------------------------------------ per-call TZ motion search
+TZ_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("ref_slot", "u1"), ("refi", "i1"),
+                   ("num_refp", "u1"), ("mvr", "u1"), ("bi", "u1"), ("flags", "u1"), ("mvp", "<i2", (2,)),
+                   ("mv", "<i2", (2,)), ("mv_ipel", "<i2", (2,)), ("other_mv", "<i2", (2,)), ("other_slot", "u1"),
+                   ("pad0", "u1", (3,)), ("mot_bits_other", "<i4"), ("lambda_mv", "<u4"), ("dist", "<i4"),
+                   ("pad1", "<i4")])
+TZ_OUT = np.dtype([("mv", "<i2", (2,)), ("mv_ipel", "<i2", (2,)), ("cost", "<u8")])
+
+
+def me_tz_device(pic, d_org, i_org, d_planes, i_ref, pad, d_reqs, n, d_out, stream=None):
+    """device form: pic = (W, H, is_padding, max_search_range, gop_size); d_planes = slot-major
+    list of 16 device addresses per reference"""
+    p = np.array(pic, dtype=np.int32)
+    arr = (C.c_void_p * len(d_planes))(*d_planes)
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_me_tz_device(p.ctypes.data, d_org, i_org, arr, len(d_planes) // 16, i_ref, pad, d_reqs,
+                                         n, d_out, stream), "me_tz_device")

@@ -52,6 +52,17 @@ __device__ __forceinline__ u32 sad4(u32 a, u32 b, u32 c)
     return d;
 }
 
+// smallest value over the warp (every lane receives it)
+__device__ __forceinline__ u64 warp_min_u64(u64 v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        u64 t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t < v ? t : v;
+    }
+    return v;
+}
+
 // 4 bytes starting `sh` bytes (0..3) into the 8-byte little-endian pair (lo, hi)
 __device__ __forceinline__ u32 align4(u32 lo, u32 hi, u32 sh)
 {

@@ -75,16 +75,6 @@ __device__ __forceinline__ u32 lk_bits(int v)
     return v == 0 ? 1u : 2u * (32u - (u32)__clz(abs(v) + 1));
 }
 
-__device__ __forceinline__ u64 warp_min_u64(u64 v)
-{
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        u64 t = __shfl_xor_sync(0xffffffffu, v, o);
-        v = t < v ? t : v;
-    }
-    return v;
-}
-
 // 16x16 SAD of the org block (smem words, row-major 4 per row) against p (stride a multiple of 4)
 __device__ __forceinline__ u32 lk_sad16(const u32 *so, const pel *p, int stride)
 {
