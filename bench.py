@@ -428,7 +428,14 @@ def lookahead_leg(u, torch, stream, flush, sm_count, sm_mhz, with_cpu, reps=20):
     return out
 
 
-def tz_leg(u, torch, stream, flush, with_cpu, reps=10):
+def loka_chroma(y):
+    """chroma planes of a synthetic luma picture: 2x-downsampled luma offset by +16 / -16"""
+    import numpy as np
+    c = y.reshape(y.shape[0] // 2, 2, y.shape[1] // 2, 2).astype(np.int32).mean((1, 3)).astype(np.int32)
+    return np.clip(c + 16, 0, 255).astype(np.uint8), np.clip(c - 16, 0, 255).astype(np.uint8)
+
+
+def tz_leg(u, torch, stream, flush, with_cpu, hbm_peak, reps=10):
     """per-call TZ motion searches (me_search_tz) of a 1080p frame: every block of the ten shapes
     on the CTU grid against 2 references, each at a random AMVR resolution with a random
     predictor, 30 % of them bi calls against the other reference's prediction"""
@@ -472,6 +479,43 @@ def tz_leg(u, torch, stream, flush, with_cpu, reps=10):
         e1.record(stream)
     torch.cuda.synchronize()
     ms_gpu = sum(a.elapsed_time(b) for a, b in evs) / reps
+    # CU motion compensation of the same blocks at the MVs found: luma + chroma, one list, or
+    # both lists for the bi calls (the other list at its own MV)
+    tz_out = d_out.cpu().numpy().view(u.TZ_OUT)
+    mreq = np.zeros(n, dtype=u.MC_REQ)
+    for f in ("x", "y", "w", "h"):
+        mreq[f] = reqs[f]
+    mreq["slot"][:, 0] = reqs["ref_slot"]
+    mreq["slot"][:, 1] = np.where(reqs["bi"] == 1, reqs["other_slot"].astype(np.int8), np.int8(-1))
+    mreq["mv"][:, 0] = tz_out["mv"]
+    mreq["mv"][:, 1] = reqs["other_mv"]
+    sizes = mreq["w"].astype(np.int64) * mreq["h"] * 3 // 2
+    mreq["out_offset"] = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    mc_bytes = int(sizes.sum())
+    ms.set_ref_chroma(0, *[np.ascontiguousarray(c) for c in loka_chroma(seq[1])])
+    ms.set_ref_chroma(1, *[np.ascontiguousarray(c) for c in loka_chroma(seq[0])])
+    d_mreq = torch.from_numpy(mreq.view(np.uint8).copy()).cuda()
+    d_pred = torch.empty(mc_bytes, dtype=torch.uint8, device="cuda")
+    chroma_ptrs = [ms.chroma_plane_ptr(s, c) for s in range(2) for c in range(2)]
+
+    def mc_run():
+        u.mc_cu_device(W, H, planes, ms.stride, PAD, chroma_ptrs, ms.chroma_stride(), 72, d_mreq.data_ptr(), n,
+                       d_pred.data_ptr(), mc_bytes, sp)
+
+    for _ in range(3):
+        mc_run()
+    torch.cuda.synchronize()
+    mevs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in mevs:
+        flush.zero_()
+        e0.record(stream)
+        mc_run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    mc_ms = sum(a.elapsed_time(b) for a, b in mevs) / reps
+    # bytes: every prediction written once, each used list's reference block read once (chroma
+    # filter halo not counted)
+    mc_traffic = mc_bytes + int((sizes * ((mreq["slot"][:, 1] >= 0) + 1)).sum())
     # end to end: host org + requests in, results out, through the session entry
     org_pin = torch.from_numpy(seq[2]).pin_memory()
     t0 = time.perf_counter()
@@ -482,6 +526,12 @@ def tz_leg(u, torch, stream, flush, with_cpu, reps=10):
                        "grid) x 2 references, AMVR resolutions 0..4, 30 % bi, SATD/SAD refinement mixed",
            "calls": n, "ms_per_batch": ms_gpu, "calls_per_s": n / (ms_gpu / 1000.0),
            "bi_calls": int(reqs["bi"].sum()),
+           "mc": {"workload": "com_mc_cu of the same blocks at the MVs found (luma + 4-tap chroma, bi calls "
+                              "averaged with the other list)", "ms_per_batch": mc_ms,
+                  "bytes": mc_traffic, "gb_per_s": mc_traffic / (mc_ms / 1000.0) / 1e9,
+                  "roofline": {"bound": "hbm", "achieved": mc_traffic / (mc_ms / 1000.0) / 1e9, "peak": hbm_peak,
+                               "unit": "GB/s", "frac": mc_traffic / (mc_ms / 1000.0) / 1e9 / hbm_peak,
+                               "peak_source": "hbm_gbs of MEASURED_PEAKS.json"}},
            "e2e": {"ms_per_batch": e2e_ms, "calls_per_s": n / (e2e_ms / 1000.0),
                    "h2d_bytes": int(W * H + reqs.nbytes), "d2h_bytes": int(got.nbytes),
                    "path": "uavs3e_cuda_me_tz (host org and requests, session references)"}}
@@ -646,7 +696,7 @@ def run_ours(args):
     pruning = pruning_leg(args.pruning_steps) if "pruning" in legs else None
     lookahead = (lookahead_leg(u, torch, stream, flush, sm_count, sm_mhz, not args.no_cpu)
                  if "lookahead" in legs else None)
-    tz = tz_leg(u, torch, stream, flush, not args.no_cpu) if "tz" in legs else None
+    tz = tz_leg(u, torch, stream, flush, not args.no_cpu, hbm_peak) if "tz" in legs else None
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -702,7 +752,8 @@ def run_legs(args):
         out["lookahead"] = lookahead_leg(u, torch, torch.cuda.current_stream(), flush, sm_count, sm_mhz,
                                          not args.no_cpu)
     if "tz" in legs:
-        out["tz"] = tz_leg(u, torch, torch.cuda.current_stream(), flush, not args.no_cpu)
+        out["tz"] = tz_leg(u, torch, torch.cuda.current_stream(), flush, not args.no_cpu,
+                           float(peaks.get("hbm_gbs", 6800.0)))
     print(json.dumps(out))
 
 

@@ -60,7 +60,8 @@ UAVS3E_CUDA_API const char *uavs3e_cuda_version(void);
 /* Kernel timing (observability; the reference has none): while enabled, every launch of the
  * batched kernels is bracketed by CUDA events on its stream.  collect() waits for them and
  * returns, per kernel id (0 pad, 1 frame interpolation, 2 integer search, 3 fractional
- * refinement, 4 intra lattice, 5 lookahead estimate, 6 TZ requests), the summed milliseconds and launch counts,
+ * refinement, 4 intra lattice, 5 lookahead estimate, 6 TZ requests, 7 CU motion compensation), the summed
+ * milliseconds and launch counts,
  * then forgets them. */
 UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
 /* Measured issue rate of the 4-sample SAD instruction (vabsdiff4 with accumulate) on the current
@@ -234,10 +235,53 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_tz_device(const uavs3e_cuda_tz_pic_t *pic, co
                                              const uavs3e_cuda_tz_req_t *d_reqs, int n, uavs3e_cuda_tz_out_t *d_out,
                                              void *stream);
 
+/* ------------------------------------------------------------ CU motion compensation */
+
+/*
+ * com_mc_cu (src/com_mc.c:140-200, declared inc/com_modules.h:71) for a list of CUs: the luma
+ * prediction copied from the reference's quarter-sample plane (com_mc_blk_luma), the chroma
+ * predictions by the 4-tap filters at eighth-sample positions (com_mc_blk_chroma: ipcpy,
+ * ipflt H_4 / V_4, ipflt_ext EXT_4), the two lists averaged (pel_avrg).  Each CU's prediction
+ * is written at out + out_offset: Y (w x h) then U and V (w/2 x h/2), for the channels asked.
+ */
+#define UAVS3E_CUDA_MC_LUMA_CHROMA 0   /* channel_type_t CHANNEL_LC */
+#define UAVS3E_CUDA_MC_LUMA        1   /* CHANNEL_L */
+#define UAVS3E_CUDA_MC_CHROMA      2   /* CHANNEL_C */
+
+typedef struct {
+    int16_t  x, y;            /* CU position (luma samples), CU inside the picture             */
+    uint8_t  w, h;            /* 8..64, powers of two                                          */
+    int8_t   slot[2];         /* reference slot of list 0 / 1 (refi), -1 = list not used       */
+    int16_t  mv[2][2];        /* quarter-sample MVs                                            */
+    uint8_t  channel;         /* UAVS3E_CUDA_MC_*                                              */
+    uint8_t  pad[3];
+    uint32_t out_offset;      /* byte offset of this CU's prediction                           */
+} uavs3e_cuda_mc_req_t;
+
+/* Chroma planes of reference `slot` of a motion-search session (host, W/2 x H/2, stride in
+ * samples): uploaded and padded by 72 samples (PIC_PAD_SIZE_C) with the edges replicated. */
+UAVS3E_CUDA_API int uavs3e_cuda_me_set_ref_chroma(uavs3e_cuda_me *me, int slot, const uint8_t *u, const uint8_t *v,
+                                                  int stride);
+/* CU predictions from the session's references (luma planes and chroma planes), host buffers,
+ * synchronous; out holds out_bytes (CUs whose prediction would not fit are skipped). */
+UAVS3E_CUDA_API int uavs3e_cuda_mc_cu(uavs3e_cuda_me *me, const uavs3e_cuda_mc_req_t *reqs, int n, uint8_t *out,
+                                      size_t out_bytes);
+/* Device form: d_planes = n_slots * 16 luma plane pointers (as uavs3e_cuda_me_tz_device, padded by
+ * pad >= 144), d_chroma = n_slots * 2 pointers to sample (0,0) of U and V (stride i_c, padded by
+ * pad_c >= 72); host pointer arrays of device pointers. */
+UAVS3E_CUDA_API int uavs3e_cuda_mc_cu_device(int width, int height, const uint8_t *const *d_planes, int n_slots,
+                                             int i_ref, int pad, const uint8_t *const *d_chroma, int i_c, int pad_c,
+                                             const uavs3e_cuda_mc_req_t *d_reqs, int n, uint8_t *d_out,
+                                             size_t out_bytes, void *stream);
+
 /* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
  * session's plane stride; for inspection by tests. */
 UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *me, int slot, int phase);
 UAVS3E_CUDA_API int uavs3e_cuda_me_plane_stride(const uavs3e_cuda_me *me);
+/* Device pointer to sample (0,0) of chroma plane c (0 U, 1 V) of `slot` (NULL before the first
+ * uavs3e_cuda_me_set_ref_chroma), and the chroma stride (0 before it). */
+UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_chroma_plane(uavs3e_cuda_me *me, int slot, int c);
+UAVS3E_CUDA_API int uavs3e_cuda_me_chroma_stride(const uavs3e_cuda_me *me);
 
 /* ------------------------------------------------------------ batched intra lattice */
 

@@ -1686,3 +1686,56 @@ void orc_me_tz(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *co
     (void)threads;
     free(tab);
 }
+
+/* ============================================================ CU motion compensation */
+
+/* com_mc_blk_chroma with hp_flag 0 (src/com_mc.c:103-138): 1/8-sample position, clipped to
+ * [-(MAX_CU_SIZE/2) - 2, max_pos], copy or 4-tap filters (ipflt H_4 / V_4, ipflt_ext EXT_4) */
+static void mc_chroma_blk(const pel *plane, int i_c, pel *dst, int qx, int qy, int w, int h, int maxx, int maxy)
+{
+    const s8(*coef)[4] = (const s8(*)[4])orc_mc_chroma_coef();
+    int dx = qx & 7, dy = qy & 7;
+    int x = CLIP3(-64 - 2, maxx, qx >> 3), y = CLIP3(-64 - 2, maxy, qy >> 3);
+    const pel *src = plane + y * i_c + x;
+    if (!dx && !dy) orc_ipcpy(src, i_c, dst, w, w, h);
+    else if (!dy) orc_ipflt(1, src, i_c, dst, w, w, h, coef[dx], 255);
+    else if (!dx) orc_ipflt(3, src, i_c, dst, w, w, h, coef[dy], 255);
+    else orc_ipflt_ext(1, src, i_c, dst, w, w, h, coef[dx], coef[dy], 255);
+}
+
+/* com_mc_cu (src/com_mc.c:140-200): each used list's prediction, the two averaged (pel_avrg);
+ * identical motion on the same picture keeps the first, which the average equals */
+void orc_mc_cu(int width, int height, const pel *const *planes, int i_ref, const pel *const *chroma, int i_c,
+               const orc_mc_req_t *reqs, int n, pel *out)
+{
+    for (int i = 0; i < n; i++) {
+        const orc_mc_req_t *r = &reqs[i];
+        const int w = r->w, h = r->h, wc = w >> 1, hc = h >> 1;
+        pel pred[2][3][64 * 64];
+        int np = 0;
+        for (int l = 0; l < 2; l++) {
+            if (r->slot[l] < 0) continue;
+            int qx = (r->x << 2) + r->mv[l][0], qy = (r->y << 2) + r->mv[l][1];
+            if (r->channel != 2) {
+                const pel *p = mc_pointer(planes + r->slot[l] * 16, i_ref, qx, qy, width + 4, height + 4);
+                orc_ipcpy(p, i_ref, pred[np][0], w, w, h);
+            }
+            if (r->channel != 1)
+                for (int c = 0; c < 2; c++)
+                    mc_chroma_blk(chroma[r->slot[l] * 2 + c], i_c, pred[np][1 + c], qx, qy, wc, hc, (width + 4) >> 1,
+                                  (height + 4) >> 1);
+            np++;
+        }
+        pel *o = out + r->out_offset;
+        if (r->channel != 2) {
+            if (np == 2) orc_pel_avrg(w, h, o, w, pred[0][0], pred[1][0]);
+            else memcpy(o, pred[0][0], (size_t)w * h);
+            o += w * h;
+        }
+        if (r->channel != 1)
+            for (int c = 0; c < 2; c++, o += wc * hc) {
+                if (np == 2) orc_pel_avrg(wc, hc, o, wc, pred[0][1 + c], pred[1][1 + c]);
+                else memcpy(o, pred[0][1 + c], (size_t)wc * hc);
+            }
+    }
+}

@@ -208,6 +208,23 @@ typedef struct {
 
 typedef struct { int width, height, is_padding, max_search_range, gop_size; } orc_tz_pic_t;
 
+/* ------------------------- CU motion compensation (com_mc_cu, src/com_mc.c:140-200) ------------------------- */
+
+typedef struct {
+    s16 x, y;           /* CU position (luma samples)                                              */
+    u8  w, h;           /* CU size, 8..64 (powers of two)                                          */
+    s8  slot[2];        /* reference slot of list 0 / list 1, -1 when the list is unused           */
+    s16 mv[2][2];       /* quarter-sample MVs                                                      */
+    u8  channel;        /* channel_type_t: 0 luma and chroma, 1 luma, 2 chroma                     */
+    u8  pad[3];
+    u32 out_offset;     /* byte offset of the CU's prediction: Y (w x h), then U and V (w/2 x h/2) */
+} orc_mc_req_t;
+
+/* luma from the quarter-sample planes (planes[slot * 16 + phase], stride i_ref), chroma with the
+ * 4-tap filters from chroma[slot * 2 + (0 U, 1 V)] (stride i_c, padded by >= 72) */
+void orc_mc_cu(int width, int height, const pel *const *planes, int i_ref, const pel *const *chroma, int i_c,
+               const orc_mc_req_t *reqs, int n, pel *out);
+
 /* planes[slot * 16 + dy * 4 + dx]: the quarter-sample planes of each reference (0 = integer),
  * stride i_ref, padded by >= 144.  Uses OpenMP over requests when threads > 1. */
 void orc_me_tz(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *const *planes, int i_ref,

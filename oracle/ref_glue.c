@@ -340,3 +340,41 @@ void refk_me_tz(int W, int H, int is_padding, int max_search_range, int gop_size
     inter_search_free(info.tab_mvbits, pi->tab_mvbits_offset);
     free(pi);
 }
+
+/* ---- 5. CU motion compensation -------------------------------------------------------------
+ * com_mc_cu (src/com_mc.c:140) for one request: planes[slot * 16 + phase] are each reference's
+ * quarter-sample luma planes (stride i_ref), chroma[slot * 2 + (0 U, 1 V)] its chroma planes
+ * (stride i_c); reference index = slot in both lists, POC = slot.  Layout of req:
+ * orc_mc_req_t (oracle.h); the prediction goes to out as Y (w x h) then U, V (w/2 x h/2) for
+ * the channels asked. */
+typedef struct {
+    s16 x, y; u8 w, h; s8 slot[2]; s16 mv[2][2]; u8 channel; u8 pad[3]; u32 out_offset;
+} glue_mc_req_t;
+
+void refk_mc_cu(int W, int H, pel **planes, int n_slots, int i_ref, pel **chroma, int i_c, const glue_mc_req_t *rq,
+                pel *out)
+{
+    refk_init();
+    static com_pic_t pics[8];
+    static com_subpel_t sps[8];
+    static com_img_t imgs[8][16];
+    static com_ref_pic_t refp[8][REFP_NUM];
+    static pel pred[N_C][MAX_CU_DIM];
+    for (int s = 0; s < n_slots && s < 8; s++) {
+        tz_pic(&pics[s], &sps[s], imgs[s], planes, s, W, H, i_ref, s);
+        pics[s].u = chroma[s * 2];
+        pics[s].v = chroma[s * 2 + 1];
+        pics[s].stride_chroma = i_c;
+        for (int l = 0; l < REFP_NUM; l++) { refp[s][l].pic = &pics[s]; refp[s][l].ptr = s; }
+    }
+    s8 refi[REFP_NUM] = { rq->slot[0], rq->slot[1] };
+    s16 mv[REFP_NUM][MV_D] = { { rq->mv[0][0], rq->mv[0][1] }, { rq->mv[1][0], rq->mv[1][1] } };
+    com_mc_cu(rq->x, rq->y, W, H, rq->w, rq->h, refi, mv, refp, pred, rq->w, (channel_type_t)rq->channel, 8);
+    pel *o = out + rq->out_offset;
+    const int w = rq->w, h = rq->h;
+    if (rq->channel != CHANNEL_C) { memcpy(o, pred[Y_C], (size_t)w * h); o += w * h; }
+    if (rq->channel != CHANNEL_L) {
+        memcpy(o, pred[U_C], (size_t)w * h / 4);
+        memcpy(o + w * h / 4, pred[V_C], (size_t)w * h / 4);
+    }
+}

@@ -433,11 +433,56 @@ def run_tz(B, p, seed):
     return digest(out.view(np.uint8))
 
 
+# ------------------------------------------------------------------ CU motion compensation
+MC_PAD_C = 72
+
+
+def mc_requests(rng, W, H, n):
+    """com_mc_cu calls: CUs 8..64, one or both lists (sometimes the same picture and MV), MVs that
+    reach past the picture edges, every channel selection; returns (requests, output bytes)"""
+    import pyoracle
+    r = np.zeros(n, dtype=pyoracle.MC_REQ)
+    off = 0
+    for i in range(n):
+        w, h = (8, 16, 32, 64)[int(rng.integers(4))], (8, 16, 32, 64)[int(rng.integers(4))]
+        r[i]["x"] = int(rng.integers(0, (W - w) // 8 + 1)) * 8
+        r[i]["y"] = int(rng.integers(0, (H - h) // 8 + 1)) * 8
+        r[i]["w"], r[i]["h"] = w, h
+        use = int(rng.integers(1, 4))           # bit 0 list 0, bit 1 list 1
+        r[i]["slot"] = [int(rng.integers(0, 2)) if use & 1 else -1, int(rng.integers(0, 2)) if use & 2 else -1]
+        r[i]["mv"] = rng.integers(-260, 261, (2, 2))
+        if use == 3 and rng.random() < 0.15:    # identical motion on the same picture
+            r[i]["slot"][1] = r[i]["slot"][0]
+            r[i]["mv"][1] = r[i]["mv"][0]
+        ch = int(rng.integers(0, 3))
+        r[i]["channel"] = ch
+        r[i]["out_offset"] = off
+        off += (w * h if ch != 2 else 0) + (w * h // 2 if ch != 1 else 0)
+    return r, off
+
+
+def mc_inputs(B, p, seed):
+    rng = np.random.default_rng(seed)
+    W, H = p["w"], p["h"]
+    frames = loka_frames(rng, W, H, [0, 4, 8], p["vel"])
+    keep, addrs, stride = tz_planes(B, frames, [4, 0], W, H)
+    sc = W // 2 + 2 * MC_PAD_C
+    chroma = [padded_plane(frames[t][c], MC_PAD_C, sc).reshape(-1) for t in (4, 0) for c in (1, 2)]
+    caddrs = [a.ctypes.data + MC_PAD_C * sc + MC_PAD_C for a in chroma]
+    reqs, nbytes = mc_requests(rng, W, H, p["n"])
+    return (keep, addrs, stride), (chroma, caddrs, sc), reqs, nbytes
+
+
+def run_mc(B, p, seed):
+    (keep, addrs, stride), (chroma, caddrs, sc), reqs, nbytes = mc_inputs(B, p, seed)
+    return digest(B.mc_cu(p["w"], p["h"], addrs, stride, caddrs, sc, reqs, nbytes))
+
+
 RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -446,6 +491,12 @@ TZ_CASES = [
     dict(w=192, h=128, pad=1, range=384, gop=16, vel=(2.5, -1.25), n=96),
     dict(w=160, h=96, pad=1, range=64, gop=4, vel=(-4.0, 3.0), n=96),
     dict(w=128, h=128, pad=0, range=384, gop=16, vel=(1.75, 2.5), n=64),
+]
+
+# CU motion-compensation cases
+MC_CASES = [
+    dict(w=192, h=128, vel=(2.5, -1.25), n=160),
+    dict(w=96, h=64, vel=(-6.0, 3.5), n=96),
 ]
 
 # lookahead cases: encoder picture level (padded references, random access with both lists or
@@ -521,6 +572,8 @@ def all_cases():
         add("loka", **p)
     for p in TZ_CASES:
         add("tz", **p)
+    for p in MC_CASES:
+        add("mc", **p)
     return cases
 
 

@@ -65,6 +65,12 @@ def _declare(L):
     L.uavs3e_cuda_loka_sc_ratio.argtypes = [I, I, I, I, I, C.c_int64, P, I, P, P, I, P, C.c_int64, I, I, P]
     L.uavs3e_cuda_me_tz.argtypes = [P, P, P, I, P, I, P]
     L.uavs3e_cuda_me_tz_device.argtypes = [P, P, I, P, I, I, I, P, I, P, P]
+    L.uavs3e_cuda_me_set_ref_chroma.argtypes = [P, I, P, P, I]
+    L.uavs3e_cuda_me_chroma_plane.restype = P
+    L.uavs3e_cuda_me_chroma_plane.argtypes = [P, I, I]
+    L.uavs3e_cuda_me_chroma_stride.argtypes = [P]
+    L.uavs3e_cuda_mc_cu.argtypes = [P, P, I, P, C.c_size_t]
+    L.uavs3e_cuda_mc_cu_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
 
 
 def check(rc, what="uavs3e_cuda"):
@@ -80,7 +86,7 @@ def init(device=0):
     check(lib().uavs3e_cuda_init(device), "uavs3e_cuda_init")
 
 
-PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz")
+PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz", "mc")
 
 CU = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
@@ -312,6 +318,43 @@ class MotionSearch:
         check(lib().uavs3e_cuda_me_tz(self.h, p.ctypes.data, org.ctypes.data, org.strides[0], reqs.ctypes.data,
                                       len(reqs), out.ctypes.data), "me_tz")
         return out[:len(reqs)]
+
+
+    def set_ref_chroma(self, slot, u, v):
+        u = np.ascontiguousarray(u, dtype=np.uint8)
+        v = np.ascontiguousarray(v, dtype=np.uint8)
+        assert u.strides[0] == v.strides[0]
+        check(lib().uavs3e_cuda_me_set_ref_chroma(self.h, slot, u.ctypes.data, v.ctypes.data, u.strides[0]),
+              "me_set_ref_chroma")
+
+    def chroma_plane_ptr(self, slot, c):
+        return lib().uavs3e_cuda_me_chroma_plane(self.h, slot, c)
+
+    def chroma_stride(self):
+        return lib().uavs3e_cuda_me_chroma_stride(self.h)
+
+    def mc_cu(self, reqs, out_bytes):
+        """com_mc_cu for every MC_REQ against the session's references; returns the output bytes"""
+        reqs = np.ascontiguousarray(reqs, dtype=MC_REQ)
+        out = np.zeros(max(1, out_bytes), dtype=np.uint8)
+        check(lib().uavs3e_cuda_mc_cu(self.h, reqs.ctypes.data, len(reqs), out.ctypes.data, out_bytes), "mc_cu")
+        return out[:out_bytes]
+
+
+MC_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)),
+                   ("mv", "<i2", (2, 2)), ("channel", "u1"), ("pad", "u1", (3,)), ("out_offset", "<u4")])
+
+
+def mc_cu_device(width, height, d_planes, i_ref, pad, d_chroma, i_c, pad_c, d_reqs, n, d_out, out_bytes,
+                 stream=None):
+    """device form of com_mc_cu over a list of CUs (addresses as ints)"""
+    a = (C.c_void_p * len(d_planes))(*d_planes)
+    c = (C.c_void_p * len(d_chroma))(*d_chroma)
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_mc_cu_device(width, height, a, len(d_planes) // 16, i_ref, pad, c, i_c, pad_c, d_reqs, n,
+                                         d_out, out_bytes, stream), "mc_cu_device")
 
 
 # ------------------------------------------------------------------ per-call TZ motion search

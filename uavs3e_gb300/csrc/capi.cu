@@ -225,7 +225,18 @@ struct uavs3e_cuda_me {
     std::vector<u16> h_r2m;
     void *tz_buf = nullptr;           // TZ requests and results of host runs
     size_t tz_cap = 0;
+    pel *chroma_buf = nullptr;        // [n_refs][2][rows_c * stride_c], padded by 72
+    int stride_c = 0, rows_c = 0;
+    void *mc_buf = nullptr;           // CU MC requests and predictions of host runs
+    size_t mc_cap = 0;
 };
+
+static const int kPadC = 72;          // PIC_PAD_SIZE_C
+
+static pel *me_chroma_ptr(uavs3e_cuda_me *m, int slot, int c)
+{
+    return m->chroma_buf + ((size_t)slot * 2 + c) * m->stride_c * m->rows_c + (size_t)kPadC * m->stride_c + kPadC;
+}
 
 static const int kNdy = ME_NDY;
 static_assert(sizeof(MeResult) == sizeof(uavs3e_cuda_me_result_t), "result record layout");
@@ -292,6 +303,7 @@ UAVS3E_CUDA_API void uavs3e_cuda_me_close(uavs3e_cuda_me *m)
     if (m->st) cudaStreamSynchronize(m->st);
     cudaFree(m->planes_buf); cudaFree(m->org_buf); cudaFree(m->out_buf);
     cudaFree(m->keys); cudaFree(m->sub); cudaFree(m->q2); cudaFree(m->r2m); cudaFree(m->tz_buf);
+    cudaFree(m->chroma_buf); cudaFree(m->mc_buf);
     if (m->st) cudaStreamDestroy(m->st);
     delete m;
 }
@@ -371,6 +383,59 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *m, const uint8_t *
     return me_launch(m, d_org, i_org, lambda_mv, (MeResult *)d_out, (cudaStream_t)stream);
 }
 
+UAVS3E_CUDA_API int uavs3e_cuda_me_set_ref_chroma(uavs3e_cuda_me *m, int slot, const uint8_t *u, const uint8_t *v,
+                                                  int stride)
+{
+    if (!m || !u || !v || slot < 0 || slot >= m->n_refs || stride < m->W / 2)
+        return set_status(UC_ERR_ARG, "me_set_ref_chroma: bad argument");
+    if (ensure_init()) return uavs3e_cuda_status();
+    const int Wc = m->W / 2, Hc = m->H / 2;
+    if (!m->chroma_buf) {
+        m->stride_c = (Wc + 2 * kPadC + 15) & ~15;
+        m->rows_c = Hc + 2 * kPadC;
+        UC_CHECK(cudaMalloc(&m->chroma_buf, (size_t)m->n_refs * 2 * m->stride_c * m->rows_c));
+    }
+    for (int c = 0; c < 2; c++) {
+        pel *d = me_chroma_ptr(m, slot, c);
+        UC_CHECK(cudaMemcpy2DAsync(d, m->stride_c, c ? v : u, stride, Wc, Hc, cudaMemcpyHostToDevice, m->st));
+        int r = launch_pad_plane(d, Wc, Hc, kPadC, m->stride_c, m->st);
+        if (r) return r;
+    }
+    UC_CHECK(cudaStreamSynchronize(m->st));
+    return UC_OK;
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_mc_cu(uavs3e_cuda_me *m, const uavs3e_cuda_mc_req_t *reqs, int n, uint8_t *out,
+                                      size_t out_bytes)
+{
+    if (!m || n < 0 || (n > 0 && (!reqs || !out))) return set_status(UC_ERR_ARG, "mc_cu: bad argument");
+    if (!m->chroma_buf) return set_status(UC_ERR_ARG, "mc_cu: no chroma planes (uavs3e_cuda_me_set_ref_chroma)");
+    if (ensure_init()) return uavs3e_cuda_status();
+    if (n == 0) return UC_OK;
+    const size_t rb = ((size_t)n * sizeof(uavs3e_cuda_mc_req_t) + 255) & ~(size_t)255;
+    if (m->mc_cap < rb + out_bytes) {
+        if (m->mc_buf) UC_CHECK(cudaFree(m->mc_buf));
+        m->mc_buf = nullptr;
+        m->mc_cap = 0;
+        UC_CHECK(cudaMalloc(&m->mc_buf, rb + out_bytes));
+        m->mc_cap = rb + out_bytes;
+    }
+    const int slots = std::min(m->n_refs, UAVS3E_CUDA_TZ_MAX_SLOTS);
+    const pel *planes[UAVS3E_CUDA_TZ_MAX_SLOTS * 16], *chroma[UAVS3E_CUDA_TZ_MAX_SLOTS * 2];
+    for (int s = 0; s < slots; s++) {
+        for (int ph = 0; ph < 16; ph++) planes[s * 16 + ph] = me_plane_ptr(m, s, ph);
+        for (int c = 0; c < 2; c++) chroma[s * 2 + c] = me_chroma_ptr(m, s, c);
+    }
+    pel *d_out = (pel *)m->mc_buf + rb;
+    UC_CHECK(cudaMemcpyAsync(m->mc_buf, reqs, (size_t)n * sizeof(*reqs), cudaMemcpyHostToDevice, m->st));
+    int r = launch_mc_cu(m->W, m->H, planes, slots, m->stride, m->pad, chroma, m->stride_c, kPadC, m->mc_buf, n,
+                         d_out, (unsigned long long)out_bytes, m->st);
+    if (r) return r;
+    UC_CHECK(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, m->st));
+    UC_CHECK(cudaStreamSynchronize(m->st));
+    return UC_OK;
+}
+
 UAVS3E_CUDA_API int uavs3e_cuda_me_tz(uavs3e_cuda_me *m, const uavs3e_cuda_tz_pic_t *pic, const uint8_t *org,
                                       int i_org, const uavs3e_cuda_tz_req_t *reqs, int n, uavs3e_cuda_tz_out_t *out)
 {
@@ -412,5 +477,13 @@ UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *m, int slot,
 }
 
 UAVS3E_CUDA_API int uavs3e_cuda_me_plane_stride(const uavs3e_cuda_me *m) { return m ? m->stride : 0; }
+
+UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_chroma_plane(uavs3e_cuda_me *m, int slot, int c)
+{
+    if (!m || !m->chroma_buf || slot < 0 || slot >= m->n_refs || c < 0 || c > 1) return nullptr;
+    return me_chroma_ptr(m, slot, c);
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_me_chroma_stride(const uavs3e_cuda_me *m) { return m ? m->stride_c : 0; }
 
 }  // extern "C"

@@ -34,9 +34,13 @@ struct MeResult {
 };
 
 // optional per-kernel timing with CUDA events on the launching stream
-enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_LOKA = 5, PROF_TZ = 6, PROF_N = 8 };
+enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_LOKA = 5, PROF_TZ = 6, PROF_MC = 7, PROF_N = 8 };
 int ensure_init();   // selects the library's device (initialising device 0 on first use)
 // per-call TZ motion searches (tz.cu); planes: n_slots * 16 sample-(0,0) pointers
+// CU motion compensation (mc.cu); chroma: n_slots * 2 sample-(0,0) pointers (U, V)
+int launch_mc_cu(int W, int H, const uint8_t *const *planes, int n_slots, int i_ref, int pad,
+                 const uint8_t *const *chroma, int i_c, int pad_c, const void *reqs, int n, uint8_t *out,
+                 unsigned long long out_bytes, cudaStream_t st);
 int launch_me_tz(const uavs3e_cuda_tz_pic_t *pic, const uint8_t *org, int i_org, const uint8_t *const *planes,
                  int n_slots, int i_ref, int pad, const void *reqs, int n, void *out, cudaStream_t st);
 void prof_begin(int k, cudaStream_t st);
