@@ -516,6 +516,32 @@ def tz_leg(u, torch, stream, flush, with_cpu, hbm_peak, reps=10):
     # bytes: every prediction written once, each used list's reference block read once (chroma
     # filter halo not counted)
     mc_traffic = mc_bytes + int((sizes * ((mreq["slot"][:, 1] >= 0) + 1)).sum())
+    # affine predictions of every block of 16x16 and larger (random 2/3 control-point MVs)
+    big = blocks[(blocks[:, 2] >= 16) & (blocks[:, 3] >= 16)]
+    areq, a_bytes = cases.affine_requests(np.random.default_rng(23), W, H, len(big))
+    for i, f in enumerate(("x", "y", "w", "h")):
+        areq[f] = big[:, i]
+    asz = areq["w"].astype(np.int64) * areq["h"] * 3 // 2
+    areq["out_offset"] = np.concatenate([[0], np.cumsum(asz)[:-1]])
+    a_bytes = int(asz.sum())
+    d_areq = torch.from_numpy(areq.view(np.uint8).copy()).cuda()
+    d_apred = torch.empty(a_bytes, dtype=torch.uint8, device="cuda")
+
+    def aff_run():
+        u.mc_affine_device(W, H, planes, ms.stride, PAD, chroma_ptrs, ms.chroma_stride(), 72, d_areq.data_ptr(),
+                           len(areq), d_apred.data_ptr(), a_bytes, sp)
+
+    for _ in range(3):
+        aff_run()
+    torch.cuda.synchronize()
+    aevs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in aevs:
+        flush.zero_()
+        e0.record(stream)
+        aff_run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    aff_ms = sum(a.elapsed_time(b) for a, b in aevs) / reps
     # end to end: host org + requests in, results out, through the session entry
     org_pin = torch.from_numpy(seq[2]).pin_memory()
     t0 = time.perf_counter()
@@ -532,6 +558,10 @@ def tz_leg(u, torch, stream, flush, with_cpu, hbm_peak, reps=10):
                   "roofline": {"bound": "hbm", "achieved": mc_traffic / (mc_ms / 1000.0) / 1e9, "peak": hbm_peak,
                                "unit": "GB/s", "frac": mc_traffic / (mc_ms / 1000.0) / 1e9 / hbm_peak,
                                "peak_source": "hbm_gbs of MEASURED_PEAKS.json"}},
+           "affine": {"workload": f"com_mc_cu_affine of the {len(areq)} blocks of 16x16 and larger (2 or 3 "
+                                  "control points, one or two lists, luma 16-phase + chroma 32-phase filters)",
+                      "ms_per_batch": aff_ms, "cus_per_s": len(areq) / (aff_ms / 1000.0),
+                      "samples_per_s": a_bytes / (aff_ms / 1000.0)},
            "e2e": {"ms_per_batch": e2e_ms, "calls_per_s": n / (e2e_ms / 1000.0),
                    "h2d_bytes": int(W * H + reqs.nbytes), "d2h_bytes": int(got.nbytes),
                    "path": "uavs3e_cuda_me_tz (host org and requests, session references)"}}

@@ -274,6 +274,31 @@ UAVS3E_CUDA_API int uavs3e_cuda_mc_cu_device(int width, int height, const uint8_
                                              const uavs3e_cuda_mc_req_t *d_reqs, int n, uint8_t *d_out,
                                              size_t out_bytes, void *stream);
 
+/*
+ * Affine CUs: com_mc_cu_affine (src/com_mc.c:361-422, declared inc/com_modules.h:72): each list's
+ * sub-block MVs from its 2 or 3 control-point MVs (4x4 sub-blocks, 8x8 with
+ * affine_subblk_size_idx 1 or both lists), luma by the 16-phase 8-tap filters of the integer
+ * plane, chroma 4x4 blocks at the rounded mean MV of their four luma units by the 32-phase 4-tap
+ * filters, the lists averaged.  Output Y (w x h), U, V (w/2 x h/2) at out + out_offset.
+ */
+typedef struct {
+    int16_t  x, y;            /* CU position, CU inside the picture                            */
+    uint8_t  w, h;            /* 16..64, powers of two                                         */
+    int8_t   slot[2];         /* reference slot of list 0 / 1, -1 = unused                     */
+    uint8_t  cp_num;          /* 2 or 3 control points                                         */
+    uint8_t  sub8;            /* pichdr->affine_subblk_size_idx                                */
+    uint8_t  pad[2];
+    int32_t  cpmv[2][3][2];   /* control-point MVs per list, 1/16 samples                      */
+    uint32_t out_offset;
+} uavs3e_cuda_affine_req_t;
+
+UAVS3E_CUDA_API int uavs3e_cuda_mc_affine(uavs3e_cuda_me *me, const uavs3e_cuda_affine_req_t *reqs, int n,
+                                          uint8_t *out, size_t out_bytes);
+UAVS3E_CUDA_API int uavs3e_cuda_mc_affine_device(int width, int height, const uint8_t *const *d_planes, int n_slots,
+                                                 int i_ref, int pad, const uint8_t *const *d_chroma, int i_c,
+                                                 int pad_c, const uavs3e_cuda_affine_req_t *d_reqs, int n,
+                                                 uint8_t *d_out, size_t out_bytes, void *stream);
+
 /* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
  * session's plane stride; for inspection by tests. */
 UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *me, int slot, int phase);

@@ -1739,3 +1739,121 @@ void orc_mc_cu(int width, int height, const pel *const *planes, int i_ref, const
             }
     }
 }
+
+/* ============================================================ affine motion compensation */
+
+/* 1/16-sample luma and 1/32-sample chroma filters of affine prediction (com_tbl_mc_l_coeff_hp,
+ * com_tbl_mc_c_coeff_hp, src/com_tables.c:130-189) */
+static const s8 MC_L_HP[16][8] = {
+    { 0, 0, 0, 64, 0, 0, 0, 0 },      { 0, 1, -3, 63, 4, -2, 1, 0 },     { -1, 2, -5, 62, 8, -3, 1, 0 },
+    { -1, 3, -8, 60, 13, -4, 1, 0 },   { -1, 4, -10, 58, 17, -5, 1, 0 },  { -1, 4, -11, 52, 26, -8, 3, -1 },
+    { -1, 3, -9, 47, 31, -10, 4, -1 }, { -1, 4, -11, 45, 34, -10, 4, -1 }, { -1, 4, -11, 40, 40, -11, 4, -1 },
+    { -1, 4, -10, 34, 45, -11, 4, -1 }, { -1, 4, -10, 31, 47, -9, 3, -1 }, { -1, 3, -8, 26, 52, -11, 4, -1 },
+    { 0, 1, -5, 17, 58, -10, 4, -1 },  { 0, 1, -4, 13, 60, -8, 3, -1 },   { 0, 1, -3, 8, 62, -5, 2, -1 },
+    { 0, 1, -2, 4, 63, -3, 1, 0 },
+};
+static const s8 MC_C_HP[32][4] = {
+    { 0, 64, 0, 0 },    { -1, 63, 2, 0 },   { -2, 62, 4, 0 },   { -2, 60, 7, -1 },  { -2, 58, 10, -2 },
+    { -3, 57, 12, -2 }, { -4, 56, 14, -2 }, { -4, 55, 15, -2 }, { -4, 54, 16, -2 }, { -5, 53, 18, -2 },
+    { -6, 52, 20, -2 }, { -6, 49, 24, -3 }, { -6, 46, 28, -4 }, { -5, 44, 29, -4 }, { -4, 42, 30, -4 },
+    { -4, 39, 33, -4 }, { -4, 36, 36, -4 }, { -4, 33, 39, -4 }, { -4, 30, 42, -4 }, { -4, 29, 44, -5 },
+    { -4, 28, 46, -6 }, { -3, 24, 49, -6 }, { -2, 20, 52, -6 }, { -2, 18, 53, -5 }, { -2, 16, 54, -4 },
+    { -2, 15, 55, -4 }, { -2, 14, 56, -4 }, { -2, 12, 57, -3 }, { -2, 10, 58, -2 }, { -1, 7, 60, -2 },
+    { 0, 4, 62, -2 },   { 0, 2, 63, -1 },
+};
+
+/* com_mv_rounding_s32 (inc/com_util.h:189) with right shift 7, left shift 0: magnitude rounded */
+static s32 affine_round7(s32 v) { return v >= 0 ? (v + 64) >> 7 : -((-v + 64) >> 7); }
+
+/* com_mc_blk_luma with hp_flag 1 (src/com_mc.c:41-87): its plane shortcut never applies (its
+ * vertical test needs dy == 0 and dy == 8 at once), so every block is filtered from the integer
+ * plane with the 16-phase filters */
+static void affine_luma_blk(const pel *plane, int i_ref, pel *dst, int id, int qx, int qy, int w, int h, int maxx,
+                            int maxy)
+{
+    int dx = qx & 15, dy = qy & 15;
+    int x = CLIP3(-128 - 4, maxx, qx >> 4), y = CLIP3(-128 - 4, maxy, qy >> 4);
+    const pel *src = plane + y * i_ref + x;
+    if (!dx && !dy) orc_ipcpy(src, i_ref, dst, id, w, h);
+    else if (!dy) orc_ipflt(0, src, i_ref, dst, id, w, h, MC_L_HP[dx], 255);
+    else if (!dx) orc_ipflt(2, src, i_ref, dst, id, w, h, MC_L_HP[dy], 255);
+    else orc_ipflt_ext(0, src, i_ref, dst, id, w, h, MC_L_HP[dx], MC_L_HP[dy], 255);
+}
+
+/* com_mc_blk_chroma with hp_flag 1 (src/com_mc.c:103-138): 1/32-sample positions */
+static void affine_chroma_blk(const pel *plane, int i_c, pel *dst, int id, int qx, int qy, int w, int h, int maxx,
+                              int maxy)
+{
+    int dx = qx & 31, dy = qy & 31;
+    int x = CLIP3(-64 - 2, maxx, qx >> 5), y = CLIP3(-64 - 2, maxy, qy >> 5);
+    const pel *src = plane + y * i_c + x;
+    if (!dx && !dy) orc_ipcpy(src, i_c, dst, id, w, h);
+    else if (!dy) orc_ipflt(1, src, i_c, dst, id, w, h, MC_C_HP[dx], 255);
+    else if (!dx) orc_ipflt(3, src, i_c, dst, id, w, h, MC_C_HP[dy], 255);
+    else orc_ipflt_ext(1, src, i_c, dst, id, w, h, MC_C_HP[dx], MC_C_HP[dy], 255);
+}
+
+/* com_mc_blk_affine (src/com_mc.c:256-359): sub-block MVs from the control points at the
+ * sub-block centres (corner sub-blocks at the control points), rounded to 1/16 and clipped to
+ * 18 bits; chroma 4x4 blocks take the rounded mean of their four 4x4 luma MVs */
+static void affine_blk(int W, int H, int x, int y, int cw, int ch, const s32 (*ac)[2], int cp_num, int sub,
+                       const pel *plane, int i_ref, const pel *pu, const pel *pv, int i_c, pel *py, pel *ou, pel *ov)
+{
+    static s32 mvs[16][16][2];
+    const int lw = ilog2(cw), lh = ilog2(ch), half = sub >> 1;
+    const s32 dhx = ((ac[1][0] - ac[0][0]) * 128) >> lw, dhy = ((ac[1][1] - ac[0][1]) * 128) >> lw;
+    s32 dvx = -dhy, dvy = dhx;
+    if (cp_num == 3) { dvx = ((ac[2][0] - ac[0][0]) * 128) >> lh; dvy = ((ac[2][1] - ac[0][1]) * 128) >> lh; }
+    for (int h = 0; h < ch; h += sub)
+        for (int w = 0; w < cw; w += sub) {
+            int px = w + half, pyy = h + half;
+            if (w == 0 && h == 0) { px = 0; pyy = 0; }
+            else if (w + sub == cw && h == 0) { px = cw; pyy = 0; }
+            else if (w == 0 && h + sub == ch && cp_num == 3) { px = 0; pyy = ch; }
+            s32 mx = ac[0][0] * 128 + dhx * px + dvx * pyy, my = ac[0][1] * 128 + dhy * px + dvy * pyy;
+            mx = CLIP3(-131072, 131071, affine_round7(mx));
+            my = CLIP3(-131072, 131071, affine_round7(my));
+            for (int j = 0; j < sub / 4; j++)
+                for (int i = 0; i < sub / 4; i++) { mvs[(w >> 2) + i][(h >> 2) + j][0] = mx; mvs[(w >> 2) + i][(h >> 2) + j][1] = my; }
+            affine_luma_blk(plane, i_ref, py + h * cw + w, cw, ((x + w) << 4) + mx, ((y + h) << 4) + my, sub, sub,
+                            W + 4, H + 4);
+        }
+    for (int h = 0; h < ch; h += 8)
+        for (int w = 0; w < cw; w += 8) {
+            int ws = w >> 2, hs = h >> 2;
+            s32 mx = (mvs[ws][hs][0] + mvs[ws + 1][hs][0] + mvs[ws][hs + 1][0] + mvs[ws + 1][hs + 1][0] + 2) >> 2;
+            s32 my = (mvs[ws][hs][1] + mvs[ws + 1][hs][1] + mvs[ws][hs + 1][1] + mvs[ws + 1][hs + 1][1] + 2) >> 2;
+            int qx = ((x + w) << 4) + mx, qy = ((y + h) << 4) + my;
+            affine_chroma_blk(pu, i_c, ou + (h >> 1) * (cw >> 1) + (w >> 1), cw >> 1, qx, qy, 4, 4, (W + 4) >> 1,
+                              (H + 4) >> 1);
+            affine_chroma_blk(pv, i_c, ov + (h >> 1) * (cw >> 1) + (w >> 1), cw >> 1, qx, qy, 4, 4, (W + 4) >> 1,
+                              (H + 4) >> 1);
+        }
+}
+
+/* com_mc_cu_affine (src/com_mc.c:361-422): 4x4 sub-blocks, 8x8 with affine_subblk_size_idx 1 or
+ * with both lists; the two lists averaged */
+void orc_mc_affine(int width, int height, const pel *const *planes, int i_ref, const pel *const *chroma, int i_c,
+                   const orc_affine_req_t *reqs, int n, pel *out)
+{
+    static pel pr[2][3][64 * 64];
+    for (int i = 0; i < n; i++) {
+        const orc_affine_req_t *r = &reqs[i];
+        const int w = r->w, h = r->h, bi = r->slot[0] >= 0 && r->slot[1] >= 0;
+        const int sub = (r->sub8 == 1 || bi) ? 8 : 4;
+        int np = 0;
+        for (int l = 0; l < 2; l++) {
+            if (r->slot[l] < 0) continue;
+            int s = r->slot[l];
+            affine_blk(width, height, r->x, r->y, w, h, r->cpmv[l], r->cp_num, sub, planes[s * 16], i_ref,
+                       chroma[s * 2], chroma[s * 2 + 1], i_c, pr[np][0], pr[np][1], pr[np][2]);
+            np++;
+        }
+        pel *o = out + r->out_offset;
+        const int sizes[3] = { w * h, w * h / 4, w * h / 4 };
+        for (int c = 0; c < 3; c++, o += sizes[c - 1]) {
+            for (int k = 0; k < sizes[c]; k++)
+                o[k] = np == 2 ? (pel)((pr[0][c][k] + pr[1][c][k] + 1) >> 1) : pr[0][c][k];
+        }
+    }
+}

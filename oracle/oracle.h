@@ -220,6 +220,23 @@ typedef struct {
     u32 out_offset;     /* byte offset of the CU's prediction: Y (w x h), then U and V (w/2 x h/2) */
 } orc_mc_req_t;
 
+/* one affine CU (com_mc_cu_affine, src/com_mc.c:361-422) */
+typedef struct {
+    s16 x, y;           /* CU position                                                            */
+    u8  w, h;           /* CU size, 16..64 (powers of two)                                        */
+    s8  slot[2];        /* reference slot of list 0 / list 1, -1 when unused                      */
+    u8  cp_num;         /* control points, 2 or 3                                                 */
+    u8  sub8;           /* pichdr->affine_subblk_size_idx (1: 8x8 sub-blocks)                     */
+    u8  pad[2];
+    s32 cpmv[2][3][2];  /* control-point MVs per list, 1/16 samples                              */
+    u32 out_offset;     /* Y (w x h), then U and V (w/2 x h/2)                                    */
+} orc_affine_req_t;
+
+/* affine CU predictions: luma by the 16-phase 8-tap filters from the integer planes
+ * (planes[slot * 16]), chroma by the 32-phase 4-tap filters (chroma[slot * 2 + c]) */
+void orc_mc_affine(int width, int height, const pel *const *planes, int i_ref, const pel *const *chroma, int i_c,
+                   const orc_affine_req_t *reqs, int n, pel *out);
+
 /* luma from the quarter-sample planes (planes[slot * 16 + phase], stride i_ref), chroma with the
  * 4-tap filters from chroma[slot * 2 + (0 U, 1 V)] (stride i_c, padded by >= 72) */
 void orc_mc_cu(int width, int height, const pel *const *planes, int i_ref, const pel *const *chroma, int i_c,

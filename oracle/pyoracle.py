@@ -214,6 +214,15 @@ class Oracle(_Common):
         self.L.orc_mc_cu(W, H, arr, i_ref, carr, i_c, ptr(reqs), len(reqs), ptr(out))
         return out[:out_bytes]
 
+    def mc_affine(self, W, H, plane_ptrs, i_ref, chroma_ptrs, i_c, reqs, out_bytes):
+        """com_mc_cu_affine for every AFFINE_REQ; returns the output buffer"""
+        arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
+        carr = (C.c_void_p * len(chroma_ptrs))(*chroma_ptrs)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFINE_REQ)
+        out = np.zeros(max(1, out_bytes), dtype=np.uint8)
+        self.L.orc_mc_affine(W, H, arr, i_ref, carr, i_c, ptr(reqs), len(reqs), ptr(out))
+        return out[:out_bytes]
+
     def loka_finish(self, cfg, units):
         """(picture cost, icost, icost_uv[2], map_dqp) from the unit records"""
         cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
@@ -370,6 +379,17 @@ class RefLib(_Common):
                               C.c_void_p(reqs.ctypes.data + i * MC_REQ.itemsize), ptr(out))
         return out[:out_bytes]
 
+    def mc_affine(self, W, H, plane_ptrs, i_ref, chroma_ptrs, i_c, reqs, out_bytes):
+        """com_mc_cu_affine itself, one call per request (same arguments as Oracle.mc_affine)"""
+        arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
+        carr = (C.c_void_p * len(chroma_ptrs))(*chroma_ptrs)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFINE_REQ)
+        out = np.zeros(max(1, out_bytes), dtype=np.uint8)
+        for i in range(len(reqs)):
+            self.L.refk_mc_affine(W, H, arr, len(plane_ptrs) // 16, i_ref, carr, i_c,
+                                  C.c_void_p(reqs.ctypes.data + i * AFFINE_REQ.itemsize), ptr(out))
+        return out[:out_bytes]
+
     def loka_search(self, cfg, org_y, i_org, ref, i_ref, ref_ptr, refi, num_refp, x, y):
         """me_search_tz of one 16x16 unit with the lookahead's settings: (mv_x, mv_y, cost)"""
         c = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)[0]
@@ -400,6 +420,8 @@ TZ_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("ref_s
 TZ_OUT = np.dtype([("mv", "<i2", (2,)), ("mv_ipel", "<i2", (2,)), ("cost", "<u8")])
 MC_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)),
                    ("mv", "<i2", (2, 2)), ("channel", "u1"), ("pad", "u1", (3,)), ("out_offset", "<u4")])
+AFFINE_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)), ("cp_num", "u1"),
+                       ("sub8", "u1"), ("pad", "u1", (2,)), ("cpmv", "<i4", (2, 3, 2)), ("out_offset", "<u4")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
 
 MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],

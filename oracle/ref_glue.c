@@ -378,3 +378,41 @@ void refk_mc_cu(int W, int H, pel **planes, int n_slots, int i_ref, pel **chroma
         memcpy(o + w * h / 4, pred[V_C], (size_t)w * h / 4);
     }
 }
+
+/* ---- 6. affine CU motion compensation --------------------------------------------------------
+ * com_mc_cu_affine (src/com_mc.c:361) for one request (layout orc_affine_req_t, oracle.h);
+ * planes / chroma as in section 5.  The prediction goes to out as Y, then U, V. */
+typedef struct {
+    s16 x, y; u8 w, h; s8 slot[2]; u8 cp_num; u8 sub8; u8 pad[2]; s32 cpmv[2][3][2]; u32 out_offset;
+} glue_affine_req_t;
+
+void refk_mc_affine(int W, int H, pel **planes, int n_slots, int i_ref, pel **chroma, int i_c,
+                    const glue_affine_req_t *rq, pel *out)
+{
+    refk_init();
+    static com_pic_t pics[8];
+    static com_subpel_t sps[8];
+    static com_img_t imgs[8][16];
+    static com_ref_pic_t refp[8][REFP_NUM];
+    static pel pred[N_C][MAX_CU_DIM];
+    static com_pic_header_t sh;
+    for (int s = 0; s < n_slots && s < 8; s++) {
+        tz_pic(&pics[s], &sps[s], imgs[s], planes, s, W, H, i_ref, s);
+        pics[s].u = chroma[s * 2];
+        pics[s].v = chroma[s * 2 + 1];
+        pics[s].stride_chroma = i_c;
+        for (int l = 0; l < REFP_NUM; l++) { refp[s][l].pic = &pics[s]; refp[s][l].ptr = s; }
+    }
+    sh.affine_subblk_size_idx = rq->sub8;
+    s8 refi[REFP_NUM] = { rq->slot[0], rq->slot[1] };
+    CPMV mv[REFP_NUM][VER_NUM][MV_D];
+    memset(mv, 0, sizeof(mv));
+    for (int l = 0; l < 2; l++)
+        for (int v = 0; v < 3; v++) { mv[l][v][0] = rq->cpmv[l][v][0]; mv[l][v][1] = rq->cpmv[l][v][1]; }
+    com_mc_cu_affine(rq->x, rq->y, W, H, rq->w, rq->h, refi, mv, refp, pred, rq->cp_num, &sh, 8);
+    pel *o = out + rq->out_offset;
+    const int n = rq->w * rq->h;
+    memcpy(o, pred[Y_C], (size_t)n);
+    memcpy(o + n, pred[U_C], (size_t)n / 4);
+    memcpy(o + n + n / 4, pred[V_C], (size_t)n / 4);
+}

@@ -478,11 +478,44 @@ def run_mc(B, p, seed):
     return digest(B.mc_cu(p["w"], p["h"], addrs, stride, caddrs, sc, reqs, nbytes))
 
 
+def affine_requests(rng, W, H, n):
+    """com_mc_cu_affine calls: CUs 16..64, 2 or 3 control points, one or both lists, 4x4 or 8x8
+    sub-blocks, control-point MVs (1/16 samples) with zooms and rotations up to about +-1/4 and
+    translations reaching past the picture edges; returns (requests, output bytes)"""
+    import pyoracle
+    r = np.zeros(n, dtype=pyoracle.AFFINE_REQ)
+    off = 0
+    for i in range(n):
+        w, h = (16, 32, 64)[int(rng.integers(3))], (16, 32, 64)[int(rng.integers(3))]
+        r[i]["x"] = int(rng.integers(0, (W - w) // 8 + 1)) * 8
+        r[i]["y"] = int(rng.integers(0, (H - h) // 8 + 1)) * 8
+        r[i]["w"], r[i]["h"] = w, h
+        use = int(rng.integers(1, 4))
+        r[i]["slot"] = [int(rng.integers(0, 2)) if use & 1 else -1, int(rng.integers(0, 2)) if use & 2 else -1]
+        r[i]["cp_num"] = int(rng.integers(2, 4))
+        r[i]["sub8"] = int(rng.integers(0, 2))
+        for l in range(2):
+            t = rng.integers(-1200, 1201, 2)                        # translation, 1/16 samples
+            a = rng.uniform(-0.25, 0.25, 4)                         # affine parameters
+            r[i]["cpmv"][l][0] = t
+            r[i]["cpmv"][l][1] = t + np.rint(16 * w * np.array([a[0], a[1]])).astype(int)
+            r[i]["cpmv"][l][2] = t + np.rint(16 * h * np.array([a[2], a[3]])).astype(int)
+        r[i]["out_offset"] = off
+        off += w * h * 3 // 2
+    return r, off
+
+
+def run_affine(B, p, seed):
+    (keep, addrs, stride), (chroma, caddrs, sc), _, _ = mc_inputs(B, dict(p, n=1), seed)
+    reqs, nbytes = affine_requests(np.random.default_rng(seed + 1), p["w"], p["h"], p["n"])
+    return digest(B.mc_affine(p["w"], p["h"], addrs, stride, caddrs, sc, reqs, nbytes))
+
+
 RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -574,6 +607,8 @@ def all_cases():
         add("tz", **p)
     for p in MC_CASES:
         add("mc", **p)
+    for p in MC_CASES:
+        add("affine", **p)
     return cases
 
 

@@ -71,6 +71,8 @@ def _declare(L):
     L.uavs3e_cuda_me_chroma_stride.argtypes = [P]
     L.uavs3e_cuda_mc_cu.argtypes = [P, P, I, P, C.c_size_t]
     L.uavs3e_cuda_mc_cu_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
+    L.uavs3e_cuda_mc_affine.argtypes = [P, P, I, P, C.c_size_t]
+    L.uavs3e_cuda_mc_affine_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
 
 
 def check(rc, what="uavs3e_cuda"):
@@ -339,6 +341,31 @@ class MotionSearch:
         out = np.zeros(max(1, out_bytes), dtype=np.uint8)
         check(lib().uavs3e_cuda_mc_cu(self.h, reqs.ctypes.data, len(reqs), out.ctypes.data, out_bytes), "mc_cu")
         return out[:out_bytes]
+
+
+    def mc_affine(self, reqs, out_bytes):
+        """com_mc_cu_affine for every AFFINE_REQ against the session's references"""
+        reqs = np.ascontiguousarray(reqs, dtype=AFFINE_REQ)
+        out = np.zeros(max(1, out_bytes), dtype=np.uint8)
+        check(lib().uavs3e_cuda_mc_affine(self.h, reqs.ctypes.data, len(reqs), out.ctypes.data, out_bytes),
+              "mc_affine")
+        return out[:out_bytes]
+
+
+AFFINE_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)), ("cp_num", "u1"),
+                       ("sub8", "u1"), ("pad", "u1", (2,)), ("cpmv", "<i4", (2, 3, 2)), ("out_offset", "<u4")])
+
+
+def mc_affine_device(width, height, d_planes, i_ref, pad, d_chroma, i_c, pad_c, d_reqs, n, d_out, out_bytes,
+                     stream=None):
+    """device form of com_mc_cu_affine over a list of CUs"""
+    a = (C.c_void_p * len(d_planes))(*d_planes)
+    c = (C.c_void_p * len(d_chroma))(*d_chroma)
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_mc_affine_device(width, height, a, len(d_planes) // 16, i_ref, pad, c, i_c, pad_c, d_reqs,
+                                             n, d_out, out_bytes, stream), "mc_affine_device")
 
 
 MC_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)),

@@ -405,14 +405,15 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_set_ref_chroma(uavs3e_cuda_me *m, int slot, c
     return UC_OK;
 }
 
-UAVS3E_CUDA_API int uavs3e_cuda_mc_cu(uavs3e_cuda_me *m, const uavs3e_cuda_mc_req_t *reqs, int n, uint8_t *out,
-                                      size_t out_bytes)
+// the host entries of CU and affine motion compensation: requests up, predictions down
+static int me_mc_host(uavs3e_cuda_me *m, bool affine, const void *reqs, size_t req_size, int n, uint8_t *out,
+                      size_t out_bytes)
 {
-    if (!m || n < 0 || (n > 0 && (!reqs || !out))) return set_status(UC_ERR_ARG, "mc_cu: bad argument");
-    if (!m->chroma_buf) return set_status(UC_ERR_ARG, "mc_cu: no chroma planes (uavs3e_cuda_me_set_ref_chroma)");
+    if (!m || n < 0 || (n > 0 && (!reqs || !out))) return set_status(UC_ERR_ARG, "mc: bad argument");
+    if (!m->chroma_buf) return set_status(UC_ERR_ARG, "mc: no chroma planes (uavs3e_cuda_me_set_ref_chroma)");
     if (ensure_init()) return uavs3e_cuda_status();
     if (n == 0) return UC_OK;
-    const size_t rb = ((size_t)n * sizeof(uavs3e_cuda_mc_req_t) + 255) & ~(size_t)255;
+    const size_t rb = ((size_t)n * req_size + 255) & ~(size_t)255;
     if (m->mc_cap < rb + out_bytes) {
         if (m->mc_buf) UC_CHECK(cudaFree(m->mc_buf));
         m->mc_buf = nullptr;
@@ -427,13 +428,27 @@ UAVS3E_CUDA_API int uavs3e_cuda_mc_cu(uavs3e_cuda_me *m, const uavs3e_cuda_mc_re
         for (int c = 0; c < 2; c++) chroma[s * 2 + c] = me_chroma_ptr(m, s, c);
     }
     pel *d_out = (pel *)m->mc_buf + rb;
-    UC_CHECK(cudaMemcpyAsync(m->mc_buf, reqs, (size_t)n * sizeof(*reqs), cudaMemcpyHostToDevice, m->st));
-    int r = launch_mc_cu(m->W, m->H, planes, slots, m->stride, m->pad, chroma, m->stride_c, kPadC, m->mc_buf, n,
-                         d_out, (unsigned long long)out_bytes, m->st);
+    UC_CHECK(cudaMemcpyAsync(m->mc_buf, reqs, (size_t)n * req_size, cudaMemcpyHostToDevice, m->st));
+    int r = affine ? launch_mc_affine(m->W, m->H, planes, slots, m->stride, m->pad, chroma, m->stride_c, kPadC,
+                                      m->mc_buf, n, d_out, (unsigned long long)out_bytes, m->st)
+                   : launch_mc_cu(m->W, m->H, planes, slots, m->stride, m->pad, chroma, m->stride_c, kPadC,
+                                  m->mc_buf, n, d_out, (unsigned long long)out_bytes, m->st);
     if (r) return r;
     UC_CHECK(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, m->st));
     UC_CHECK(cudaStreamSynchronize(m->st));
     return UC_OK;
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_mc_affine(uavs3e_cuda_me *m, const uavs3e_cuda_affine_req_t *reqs, int n,
+                                          uint8_t *out, size_t out_bytes)
+{
+    return me_mc_host(m, true, reqs, sizeof(*reqs), n, out, out_bytes);
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_mc_cu(uavs3e_cuda_me *m, const uavs3e_cuda_mc_req_t *reqs, int n, uint8_t *out,
+                                      size_t out_bytes)
+{
+    return me_mc_host(m, false, reqs, sizeof(*reqs), n, out, out_bytes);
 }
 
 UAVS3E_CUDA_API int uavs3e_cuda_me_tz(uavs3e_cuda_me *m, const uavs3e_cuda_tz_pic_t *pic, const uint8_t *org,

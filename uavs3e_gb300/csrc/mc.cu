@@ -3,6 +3,9 @@
 // 4-tap filters at 1/8-sample positions (com_mc_blk_chroma :103-138: copy, ipflt H_4 / V_4,
 // ipflt_ext EXT_4), the two lists averaged (pel_avrg) -- bit-exact with the reference.
 //
+// Affine CUs: com_mc_cu_affine (:361-422) -- sub-block MVs from the control points, luma by the
+// 16-phase 8-tap filters, chroma by the 32-phase 4-tap filters, 1/16-sample positions.
+//
 // One warp per CU; lanes walk the CU's samples in raster order, so every store of the warp is
 // one contiguous run of the output buffer.
 #include "common.cuh"
@@ -116,6 +119,199 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc_cu(const McParams P)
     }
 }
 
+// ------------------------------------------------------------------ affine CUs
+struct AffReq {
+    s16 x, y; u8 w, h; s8 slot[2]; u8 cp_num; u8 sub8; u8 pad[2]; s32 cpmv[2][3][2]; u32 out_offset;
+};
+static_assert(sizeof(AffReq) == sizeof(uavs3e_cuda_affine_req_t), "affine request layout");
+
+// 1/16-sample luma and 1/32-sample chroma filters (com_tbl_mc_l_coeff_hp, com_tbl_mc_c_coeff_hp,
+// src/com_tables.c:130-189)
+__device__ __constant__ static const s8 kMcLumaHp[16][8] = {
+    { 0, 0, 0, 64, 0, 0, 0, 0 },      { 0, 1, -3, 63, 4, -2, 1, 0 },     { -1, 2, -5, 62, 8, -3, 1, 0 },
+    { -1, 3, -8, 60, 13, -4, 1, 0 },   { -1, 4, -10, 58, 17, -5, 1, 0 },  { -1, 4, -11, 52, 26, -8, 3, -1 },
+    { -1, 3, -9, 47, 31, -10, 4, -1 }, { -1, 4, -11, 45, 34, -10, 4, -1 }, { -1, 4, -11, 40, 40, -11, 4, -1 },
+    { -1, 4, -10, 34, 45, -11, 4, -1 }, { -1, 4, -10, 31, 47, -9, 3, -1 }, { -1, 3, -8, 26, 52, -11, 4, -1 },
+    { 0, 1, -5, 17, 58, -10, 4, -1 },  { 0, 1, -4, 13, 60, -8, 3, -1 },   { 0, 1, -3, 8, 62, -5, 2, -1 },
+    { 0, 1, -2, 4, 63, -3, 1, 0 },
+};
+__device__ __constant__ static const s8 kMcChromaHp[32][4] = {
+    { 0, 64, 0, 0 },    { -1, 63, 2, 0 },   { -2, 62, 4, 0 },   { -2, 60, 7, -1 },  { -2, 58, 10, -2 },
+    { -3, 57, 12, -2 }, { -4, 56, 14, -2 }, { -4, 55, 15, -2 }, { -4, 54, 16, -2 }, { -5, 53, 18, -2 },
+    { -6, 52, 20, -2 }, { -6, 49, 24, -3 }, { -6, 46, 28, -4 }, { -5, 44, 29, -4 }, { -4, 42, 30, -4 },
+    { -4, 39, 33, -4 }, { -4, 36, 36, -4 }, { -4, 33, 39, -4 }, { -4, 30, 42, -4 }, { -4, 29, 44, -5 },
+    { -4, 28, 46, -6 }, { -3, 24, 49, -6 }, { -2, 20, 52, -6 }, { -2, 18, 53, -5 }, { -2, 16, 54, -4 },
+    { -2, 15, 55, -4 }, { -2, 14, 56, -4 }, { -2, 12, 57, -3 }, { -2, 10, 58, -2 }, { -1, 7, 60, -2 },
+    { 0, 4, 62, -2 },   { 0, 2, 63, -1 },
+};
+
+// one luma sample of com_mc_blk_luma with hp_flag 1: always filtered from the integer plane
+// (the reference's plane shortcut tests dy == 0 and dy == 8 together and never applies)
+__device__ __forceinline__ int aff_luma_sample(const pel *s, int is, int dx, int dy)
+{
+    if (!dx && !dy) return s[0];
+    if (!dy) {
+        int v = 0;
+#pragma unroll
+        for (int t = 0; t < 8; t++) v += s[t - 3] * kMcLumaHp[dx][t];
+        return min(255, max(0, (v + 32) >> 6));
+    }
+    if (!dx) {
+        int v = 0;
+#pragma unroll
+        for (int t = 0; t < 8; t++) v += s[(t - 3) * is] * kMcLumaHp[dy][t];
+        return min(255, max(0, (v + 32) >> 6));
+    }
+    int v = 0;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const pel *r = s + (t - 3) * is;
+        int hs = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) hs += r[k - 3] * kMcLumaHp[dx][k];
+        v += (int)(s16)hs * kMcLumaHp[dy][t];
+    }
+    return min(255, max(0, (v + 2048) >> 12));
+}
+
+__device__ __forceinline__ int aff_chroma_sample(const pel *s, int ic, int dx, int dy)
+{
+    if (!dx && !dy) return s[0];
+    if (!dy) {
+        const int v = s[-1] * kMcChromaHp[dx][0] + s[0] * kMcChromaHp[dx][1] + s[1] * kMcChromaHp[dx][2] +
+                      s[2] * kMcChromaHp[dx][3];
+        return min(255, max(0, (v + 32) >> 6));
+    }
+    if (!dx) {
+        const int v = s[-ic] * kMcChromaHp[dy][0] + s[0] * kMcChromaHp[dy][1] + s[ic] * kMcChromaHp[dy][2] +
+                      s[2 * ic] * kMcChromaHp[dy][3];
+        return min(255, max(0, (v + 32) >> 6));
+    }
+    int v = 0;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const pel *r = s + (t - 1) * ic;
+        const int hs = r[-1] * kMcChromaHp[dx][0] + r[0] * kMcChromaHp[dx][1] + r[1] * kMcChromaHp[dx][2] +
+                       r[2] * kMcChromaHp[dx][3];
+        v += (int)(s16)hs * kMcChromaHp[dy][t];
+    }
+    return min(255, max(0, (v + 2048) >> 12));
+}
+
+// com_mv_rounding_s32 with right shift 7: magnitude rounded to 1/16 sample
+__device__ __forceinline__ s32 aff_round7(s32 v) { return v >= 0 ? (v + 64) >> 7 : -((-v + 64) >> 7); }
+
+// the sub-block MVs of one list (com_mc_blk_affine, src/com_mc.c:256-330) into mv[16][16] per
+// 4x4 unit (8x8 sub-blocks fill their four units)
+__device__ void aff_subblock_mvs(const AffReq &q, int l, int sub, s32 (*mv)[16][2], int lane)
+{
+    const int cw = q.w, ch = q.h, lw = 31 - __clz(cw), lh = 31 - __clz(ch), half = sub >> 1;
+    const s32 *a0 = q.cpmv[l][0], *a1 = q.cpmv[l][1], *a2 = q.cpmv[l][2];
+    const s32 dhx = ((a1[0] - a0[0]) * 128) >> lw, dhy = ((a1[1] - a0[1]) * 128) >> lw;
+    s32 dvx = -dhy, dvy = dhx;
+    if (q.cp_num == 3) { dvx = ((a2[0] - a0[0]) * 128) >> lh; dvy = ((a2[1] - a0[1]) * 128) >> lh; }
+    const int nx = cw / sub, n = nx * (ch / sub);
+    for (int b = lane; b < n; b += 32) {
+        const int w = (b % nx) * sub, h = (b / nx) * sub;
+        int px = w + half, py = h + half;
+        if (w == 0 && h == 0) { px = 0; py = 0; }
+        else if (w + sub == cw && h == 0) { px = cw; py = 0; }
+        else if (w == 0 && h + sub == ch && q.cp_num == 3) { px = 0; py = ch; }
+        const s32 mx = min(max(aff_round7(a0[0] * 128 + dhx * px + dvx * py), -131072), 131071);
+        const s32 my = min(max(aff_round7(a0[1] * 128 + dhy * px + dvy * py), -131072), 131071);
+        for (int j = 0; j < sub / 4; j++)
+            for (int i = 0; i < sub / 4; i++) { mv[(w >> 2) + i][(h >> 2) + j][0] = mx; mv[(w >> 2) + i][(h >> 2) + j][1] = my; }
+    }
+}
+
+constexpr int AFF_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * AFF_WARPS) k_mc_affine(const McParams P, const AffReq *reqs)
+{
+    __shared__ s32 s_mv[AFF_WARPS][2][16][16][2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * AFF_WARPS + warp;
+    if (r >= P.n) return;
+    const AffReq q = reqs[r];
+    const int w = q.w, h = q.h, nl = (q.slot[0] >= 0) + (q.slot[1] >= 0);
+    if ((w != 16 && w != 32 && w != 64) || (h != 16 && h != 32 && h != 64) || q.x < 0 || q.y < 0 ||
+        q.x + w > P.W || q.y + h > P.H || (q.cp_num != 2 && q.cp_num != 3) || nl == 0 || q.slot[0] >= P.n_slots ||
+        q.slot[1] >= P.n_slots || (unsigned long long)q.out_offset + (unsigned long long)(w * h * 3 / 2) > P.out_bytes)
+        return;
+    const int sub = (q.sub8 == 1 || nl == 2) ? 8 : 4;
+    int ls[2], k = 0;
+    for (int l = 0; l < 2; l++)
+        if (q.slot[l] >= 0) { aff_subblock_mvs(q, l, sub, s_mv[warp][k], lane); ls[k++] = l; }
+    __syncwarp();
+    pel *o = P.out + q.out_offset;
+    // luma: 16-phase filters per sub-block MV
+    for (int i = lane; i < w * h; i += 32) {
+        const int j = i / w, c = i - j * w;
+        int v = 0;
+        for (int t = 0; t < k; t++) {
+            const s32 *m = s_mv[warp][t][c >> 2][j >> 2];
+            const int bx = c & ~(sub - 1), by = j & ~(sub - 1);
+            const int qx = ((q.x + bx) << 4) + m[0], qy = ((q.y + by) << 4) + m[1];
+            const int px = min(max(qx >> 4, -128 - 4), P.W + 4), py = min(max(qy >> 4, -128 - 4), P.H + 4);
+            const pel *s = P.planes[q.slot[ls[t]] * 16] + (long long)(py + j - by) * P.i_ref + px + c - bx;
+            const int sv = aff_luma_sample(s, P.i_ref, qx & 15, qy & 15);
+            v = t ? (v + sv + 1) >> 1 : sv;
+        }
+        o[i] = (pel)v;
+    }
+    o += w * h;
+    // chroma: 4x4 blocks per 8x8 luma with the rounded mean of their four 4x4 MVs
+    const int wc = w >> 1, hc = h >> 1;
+    for (int pl = 0; pl < 2; pl++, o += wc * hc)
+        for (int i = lane; i < wc * hc; i += 32) {
+            const int j = i / wc, c = i - j * wc;
+            const int lx = (c >> 2) << 3, ly = (j >> 2) << 3, us = lx >> 2, vs = ly >> 2;
+            int v = 0;
+            for (int t = 0; t < k; t++) {
+                const s32 (*m)[16][2] = s_mv[warp][t];
+                const s32 mx = (m[us][vs][0] + m[us + 1][vs][0] + m[us][vs + 1][0] + m[us + 1][vs + 1][0] + 2) >> 2;
+                const s32 my = (m[us][vs][1] + m[us + 1][vs][1] + m[us][vs + 1][1] + m[us + 1][vs + 1][1] + 2) >> 2;
+                const int qx = ((q.x + lx) << 4) + mx, qy = ((q.y + ly) << 4) + my;
+                const int cx = min(max(qx >> 5, -64 - 2), (P.W + 4) >> 1), cy = min(max(qy >> 5, -64 - 2), (P.H + 4) >> 1);
+                const pel *s = P.chroma[q.slot[ls[t]] * 2 + pl] + (long long)(cy + (j & 3)) * P.i_c + cx + (c & 3);
+                const int sv = aff_chroma_sample(s, P.i_c, qx & 31, qy & 31);
+                v = t ? (v + sv + 1) >> 1 : sv;
+            }
+            o[i] = (pel)v;
+        }
+}
+
+int launch_mc_affine(int W, int H, const pel *const *planes, int n_slots, int i_ref, int pad,
+                     const pel *const *chroma, int i_c, int pad_c, const void *reqs, int n, pel *out,
+                     unsigned long long out_bytes, cudaStream_t st)
+{
+    if (!planes || !chroma || !reqs || !out || n < 0) return set_status(UC_ERR_ARG, "mc_affine: null argument");
+    if (n_slots < 1 || n_slots > UAVS3E_CUDA_TZ_MAX_SLOTS || W < 16 || H < 16)
+        return set_status(UC_ERR_ARG, "mc_affine: slots / picture size");
+    // luma taps reach 132 + 3 samples before the picture, chroma 66 + 1
+    if (pad < 144 || pad_c < 72 || i_ref < W + 2 * pad || i_c < (W >> 1) + 2 * pad_c)
+        return set_status(UC_ERR_ARG, "mc_affine: padding (luma >= 144, chroma >= 72) / strides");
+    if (n == 0) return UC_OK;
+    McParams P;
+    memset(&P, 0, sizeof(P));
+    for (int i = 0; i < n_slots * 16; i++) {
+        if (!planes[i]) return set_status(UC_ERR_ARG, "mc_affine: null plane");
+        P.planes[i] = planes[i];
+    }
+    for (int i = 0; i < n_slots * 2; i++) {
+        if (!chroma[i]) return set_status(UC_ERR_ARG, "mc_affine: null chroma plane");
+        P.chroma[i] = chroma[i];
+    }
+    P.i_ref = i_ref; P.i_c = i_c; P.n_slots = n_slots; P.W = W; P.H = H;
+    P.n = n; P.out = out; P.out_bytes = out_bytes;
+    prof_begin(PROF_MC, st);
+    k_mc_affine<<<(unsigned)((n + AFF_WARPS - 1) / AFF_WARPS), 32 * AFF_WARPS, 0, st>>>(P, (const AffReq *)reqs);
+    UC_CHECK(cudaGetLastError());
+    count_launch(1);
+    prof_end(PROF_MC, st);
+    return UC_OK;
+}
+
 int launch_mc_cu(int W, int H, const pel *const *planes, int n_slots, int i_ref, int pad, const pel *const *chroma,
                  int i_c, int pad_c, const void *reqs, int n, pel *out, unsigned long long out_bytes, cudaStream_t st)
 {
@@ -150,6 +346,18 @@ int launch_mc_cu(int W, int H, const pel *const *planes, int n_slots, int i_ref,
 }  // namespace uc
 
 using namespace uc;
+
+extern "C" UAVS3E_CUDA_API int uavs3e_cuda_mc_affine_device(int width, int height, const uint8_t *const *d_planes,
+                                                            int n_slots, int i_ref, int pad,
+                                                            const uint8_t *const *d_chroma, int i_c, int pad_c,
+                                                            const uavs3e_cuda_affine_req_t *d_reqs, int n,
+                                                            uint8_t *d_out, size_t out_bytes, void *stream)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    return launch_mc_affine(width, height, d_planes, n_slots, i_ref, pad, d_chroma, i_c, pad_c, d_reqs, n, d_out,
+                            (unsigned long long)out_bytes, (cudaStream_t)stream);
+}
 
 extern "C" UAVS3E_CUDA_API int uavs3e_cuda_mc_cu_device(int width, int height, const uint8_t *const *d_planes,
                                                         int n_slots, int i_ref, int pad,

@@ -41,6 +41,9 @@ int ensure_init();   // selects the library's device (initialising device 0 on f
 int launch_mc_cu(int W, int H, const uint8_t *const *planes, int n_slots, int i_ref, int pad,
                  const uint8_t *const *chroma, int i_c, int pad_c, const void *reqs, int n, uint8_t *out,
                  unsigned long long out_bytes, cudaStream_t st);
+int launch_mc_affine(int W, int H, const uint8_t *const *planes, int n_slots, int i_ref, int pad,
+                     const uint8_t *const *chroma, int i_c, int pad_c, const void *reqs, int n, uint8_t *out,
+                     unsigned long long out_bytes, cudaStream_t st);
 int launch_me_tz(const uavs3e_cuda_tz_pic_t *pic, const uint8_t *org, int i_org, const uint8_t *const *planes,
                  int n_slots, int i_ref, int pad, const void *reqs, int n, void *out, cudaStream_t st);
 void prof_begin(int k, cudaStream_t st);
