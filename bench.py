@@ -37,8 +37,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="me,lattice,pruning,lookahead,tz",
-                    help="comma list of legs: me (the headline line), lattice, pruning, lookahead, tz")
+    ap.add_argument("--legs", default="me,lattice,pruning,lookahead,tz,rdoq",
+                    help="comma list of legs: me (the headline line), lattice, pruning, lookahead, tz, rdoq")
     ap.add_argument("--pruning-steps", type=int, default=3000, help="training steps of the pruning leg")
     return ap.parse_args()
 
@@ -579,6 +579,65 @@ def tz_leg(u, torch, stream, flush, with_cpu, hbm_peak, reps=10):
     return out
 
 
+def rdoq_leg(u, torch, stream, flush, with_cpu, reps=10):
+    """RDOQ (quant_non_zero -> rdoq_quant_block) of 60,000 transform blocks of every shape
+    4x4..64x64 (DCT2 coefficients of Laplacian residuals, steps 10..60, intra / inter, luma /
+    chroma, 8 estimate sets)"""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cases
+    import pyoracle
+    o = pyoracle.Oracle()
+    reqs, ests, coefs = cases.rdoq_inputs(o, dict(n=60000, k=8), 77)
+    sp = stream.cuda_stream
+    d_req = torch.from_numpy(reqs.view(np.uint8).copy()).cuda()
+    d_est = torch.from_numpy(ests.view(np.uint8).copy()).cuda()
+    d_src = torch.from_numpy(coefs.copy()).cuda()
+    d_coef = torch.empty_like(d_src)
+    d_nz = torch.empty(len(reqs), dtype=torch.int32, device="cuda")
+
+    def run():
+        d_coef.copy_(d_src)
+        u.rdoq_device(d_req.data_ptr(), len(reqs), d_est.data_ptr(), len(ests), d_coef.data_ptr(), coefs.size,
+                      d_nz.data_ptr(), sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / reps
+    nz = d_nz.cpu().numpy()
+    c = coefs.copy()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        c[:] = coefs
+        u.rdoq(reqs, ests, c)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / 3
+    out = {"workload": "RDOQ of 60,000 transform blocks 4x4..64x64 (21 shapes), steps 10..60, intra/inter, "
+                       "luma/chroma, 8 bin-cost estimate sets", "blocks": len(reqs), "coefficients": int(coefs.size),
+           "ms_per_batch": ms, "blocks_per_s": len(reqs) / (ms / 1000.0),
+           "coded_blocks": int((nz > 0).sum()),
+           "note": "the device time includes a device copy of the input coefficients before each call",
+           "e2e": {"ms_per_batch": e2e_ms, "blocks_per_s": len(reqs) / (e2e_ms / 1000.0),
+                   "h2d_bytes": int(coefs.nbytes + reqs.nbytes + ests.nbytes), "d2h_bytes": int(coefs.nbytes + 4 * len(reqs)),
+                   "path": "uavs3e_cuda_rdoq (host coefficients in, levels out)"}}
+    if with_cpu:
+        c[:] = coefs
+        t0 = time.perf_counter()
+        o.rdoq(reqs, ests, c)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(reqs) / dt, "unit": "blocks/s", "cores": 1, "kind": "port",
+                               "sample": f"the whole batch through the oracle restatement (one core), {dt:.2f} s"}
+    return out
+
+
 def pruning_leg(steps=3000):
     """the learned CU pruning beside the lattice: trained on the plain path's decisions over 16
     synthetic 1080p I-frames, evaluated on a held-out frame (RD-cost increase of the pruned
@@ -727,6 +786,7 @@ def run_ours(args):
     lookahead = (lookahead_leg(u, torch, stream, flush, sm_count, sm_mhz, not args.no_cpu)
                  if "lookahead" in legs else None)
     tz = tz_leg(u, torch, stream, flush, not args.no_cpu, hbm_peak) if "tz" in legs else None
+    rdoq = rdoq_leg(u, torch, stream, flush, not args.no_cpu) if "rdoq" in legs else None
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -747,6 +807,7 @@ def run_ours(args):
         "pruning": pruning,
         "lookahead": lookahead,
         "tz": tz,
+        "rdoq": rdoq,
         "clocks": clk,
     }
     if not args.no_cpu:
@@ -784,6 +845,8 @@ def run_legs(args):
     if "tz" in legs:
         out["tz"] = tz_leg(u, torch, torch.cuda.current_stream(), flush, not args.no_cpu,
                            float(peaks.get("hbm_gbs", 6800.0)))
+    if "rdoq" in legs:
+        out["rdoq"] = rdoq_leg(u, torch, torch.cuda.current_stream(), flush, not args.no_cpu)
     print(json.dumps(out))
 
 

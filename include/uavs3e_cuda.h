@@ -60,8 +60,8 @@ UAVS3E_CUDA_API const char *uavs3e_cuda_version(void);
 /* Kernel timing (observability; the reference has none): while enabled, every launch of the
  * batched kernels is bracketed by CUDA events on its stream.  collect() waits for them and
  * returns, per kernel id (0 pad, 1 frame interpolation, 2 integer search, 3 fractional
- * refinement, 4 intra lattice, 5 lookahead estimate, 6 TZ requests, 7 CU motion compensation), the summed
- * milliseconds and launch counts,
+ * refinement, 4 intra lattice, 5 lookahead estimate, 6 TZ requests, 7 CU motion compensation,
+ * 8 RDOQ), the summed milliseconds and launch counts,
  * then forgets them. */
 UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
 /* Measured issue rate of the 4-sample SAD instruction (vabsdiff4 with accumulate) on the current
@@ -427,6 +427,44 @@ UAVS3E_CUDA_API int uavs3e_cuda_loka_units_device(const uavs3e_cuda_loka_cfg_t *
 UAVS3E_CUDA_API double uavs3e_cuda_loka_finish(const uavs3e_cuda_loka_cfg_t *cfg, const uint64_t totals[4],
                                                const uint64_t *energy, double *icost, double icost_uv[2],
                                                float *map_dqp);
+
+/* ------------------------------------------------------------ RDOQ of transform blocks */
+
+/*
+ * quant_non_zero with flat quantisation (src/quant.c:315-383, declared inc/modules.h:62) ->
+ * rdoq_quant_block (:196-313) for a list of transform blocks: coefficients past 32 columns / rows
+ * zeroed, quant_check, the first pass (quant_rdoq) and the rate-distortion decision of each level
+ * and of the last position with the bin costs the encoder derived from its entropy-coder state
+ * (core_t rdoq_bin_est_*, inc/define.h:335-339, rdoq_init_cu_est_bits :139).  The levels are
+ * written over each block's coefficients as the reference writes them (blocks whose coefficients
+ * stay below the quant_check threshold keep them), num_nz[i] is the call's return value.
+ */
+typedef struct {
+    int32_t ctp[2];
+    int32_t cbf[3][2];
+    int32_t run[24][2];
+    int32_t lvl[24][2];
+    int32_t lst[2][6][12][2];
+} uavs3e_cuda_rdoq_est_t;
+
+typedef struct {
+    uint32_t coef_offset;    /* first coefficient of the w x h block (raster)                  */
+    uint8_t  log2w, log2h;   /* 2..6                                                           */
+    uint8_t  qp;             /* quantisation step index 0..79                                  */
+    uint8_t  is_intra;
+    uint8_t  ch_type;        /* 0 Y, 1 U, 2 V                                                  */
+    uint8_t  slice_type;     /* SLICE_I = 1 selects the intra dead zone                        */
+    uint16_t est;            /* index of the estimate set                                      */
+    uint32_t pad;
+    int64_t  lambda;         /* (int64_t)(d_lambda * 32768 + 0.5), as rdoq_quant_block forms it */
+} uavs3e_cuda_rdoq_req_t;
+
+/* host buffers, synchronous; num_nz[i] = -1 marks a request outside the domain (untouched) */
+UAVS3E_CUDA_API int uavs3e_cuda_rdoq(const uavs3e_cuda_rdoq_req_t *reqs, int n, const uavs3e_cuda_rdoq_est_t *ests,
+                                     int n_est, int16_t *coefs, size_t n_coefs, int32_t *num_nz);
+UAVS3E_CUDA_API int uavs3e_cuda_rdoq_device(const uavs3e_cuda_rdoq_req_t *d_reqs, int n,
+                                            const uavs3e_cuda_rdoq_est_t *d_ests, int n_est, int16_t *d_coefs,
+                                            size_t n_coefs, int32_t *d_num_nz, void *stream);
 
 /* ---------------------------------------------------------------------------------------
  * Learned CU-partition / intra-mode pruning network (no counterpart in the reference: the

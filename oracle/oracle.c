@@ -1857,3 +1857,93 @@ void orc_mc_affine(int width, int height, const pel *const *planes, int i_ref, c
         }
     }
 }
+
+/* ============================================================ RDOQ of a transform block */
+
+/* rdoq_one_coef (src/quant.c:158-194): the cheaper of keeping the coefficient at its level, one
+ * below, or (implicitly) zero; u32 arithmetic of the level difference as in the reference */
+static u32 rdoq_coef(s64 uncoded, s64 *coded, u32 level_double, u32 abs_level, const s32 *est_run,
+                     const s32 (*est_level)[2], int q_bits, s32 err_scale, s64 lambda, int last_pos)
+{
+    u32 best = 0;
+    *coded = uncoded + (s64)est_run[0] * lambda;
+    for (int checks = 2; abs_level && checks; checks--, abs_level--) {
+        s32 diff = (s32)(level_double - (abs_level << q_bits));
+        s64 err = ((s64)diff * err_scale) >> 20;
+        s32 rate = 32768;
+        if (!last_pos) rate += est_run[1];
+        if (abs_level == 1) rate += est_level[0][1];
+        else if (abs_level < 9) rate += est_level[0][0] + est_level[1][0] * (s32)(abs_level - 2) + est_level[1][1];
+        else rate += est_level[0][0] + est_level[1][0] * 7 + ((ilog2((int)abs_level - 8) << 1) + 1) * 32768;
+        s64 cost = err * err + (s64)rate * lambda;
+        if (cost < *coded) { best = abs_level; *coded = cost; }
+    }
+    return best;
+}
+
+static int rdoq_block(const orc_rdoq_req_t *r, const orc_rdoq_est_t *E, s16 *coef)
+{
+    const int lw = r->log2w, lh = r->log2h, w = 1 << lw, h = 1 << lh, qp = r->qp, ch = r->ch_type;
+    /* quant_non_zero (src/quant.c:315-336): coefficients past 32 columns / rows are zeroed */
+    if (w > 32)
+        for (int y = 0; y < h; y++) memset(coef + y * w + 32, 0, 32 * sizeof(s16));
+    if (h > 32) memset(coef + w * h / 2, 0, (size_t)w * h / 2 * sizeof(s16));
+    /* rdoq_quant_block (src/quant.c:196-313) */
+    const int odd = (lw + lh) & 1, log2_size = (lw + lh) >> 1;
+    const int q_bits = 14 + (15 - 8 - log2_size);
+    const int q_value = odd ? (Q_SCALE[qp] * 181 + 64) >> 7 : Q_SCALE[qp];
+    const int max_num = 1 << (lw + lh), max_used = 1 << (lw + MIN(5, lh));
+    const int offset = (r->slice_type == 1 ? 201 : 153) << (q_bits - 9);
+    const int nz_thr = ((((1 << q_bits) - offset) << 10) / q_value - 1) >> 10;
+    if (orc_quant_check(coef, max_used, nz_thr)) return 0;
+    static s16 c1[64 * 64], lev[64 * 64];
+    static u32 absc[64 * 64];
+    static s64 zerr[64 * 64];
+    const s32 err_scale = RDOQ_ERR_SCALE[qp][log2_size - 1];
+    const u16 *scan = SCAN[lw][lh];
+    for (int i = 0; i < max_num; i++) c1[i] = coef[scan[i]];
+    const int last_nz = orc_quant_rdoq(c1, max_num, q_value, q_bits, err_scale, 20, absc, lev, zerr);
+    const s64 lambda = r->lambda;
+    s64 best_delta, curr_delta;
+    if (!r->is_intra && ch == 0) { best_delta = (s64)E->ctp[1] * lambda; curr_delta = (s64)E->ctp[0] * lambda; }
+    else { best_delta = (s64)E->cbf[ch][0] * lambda; curr_delta = (s64)E->cbf[ch][1] * lambda; }
+    const int base = ch == 0 ? 0 : 12;
+    const s32 (*lst)[2] = E->lst[ch != 0][5];
+    const s32 (*est_run)[2] = E->run + 10 + base, (*est_lvl)[2] = E->lvl + 10 + base;
+    u32 last_b_zero = 0, end_pos = 0;
+    int last_checked = 0, tmp_nz = 0, num_nz = 0, zero_bins = 0;
+    memset(coef, 0, (size_t)max_num * sizeof(s16));
+    for (int i = 0; i <= last_nz; i++) {
+        if (!lev[i]) { zero_bins += est_run[last_b_zero][0]; last_b_zero = 1; continue; }
+        if (zero_bins) { curr_delta += (s64)zero_bins * lambda; zero_bins = 0; }
+        s64 cc;
+        u32 level = rdoq_coef(zerr[i], &cc, absc[i], (u32)lev[i], est_run[last_b_zero], est_lvl, q_bits, err_scale,
+                              lambda, i == max_num - 1);
+        curr_delta += cc - zerr[i];
+        if (level) {
+            last_checked = i;
+            coef[scan[i]] = (s16)(c1[i] < 0 ? -(int)level : (int)level);
+            s64 f0 = (s64)lst[ilog2(i + 1)][0] * lambda, f1 = (s64)lst[ilog2(i + 1)][1] * lambda;
+            s64 end_cost = curr_delta + f1;
+            curr_delta += f0;
+            tmp_nz++;
+            if (end_cost < best_delta) { best_delta = end_cost; end_pos = (u32)i; num_nz += tmp_nz; tmp_nz = 0; }
+            last_b_zero = 0;
+            int off = (MIN((int)level - 1, 5) << 1) + base;
+            est_lvl = E->lvl + off;
+            est_run = E->run + off;
+            lst = E->lst[ch != 0][MIN((int)level - 1, 5)];
+        } else {
+            last_b_zero = 1;
+        }
+    }
+    if (num_nz)
+        for (int i = (int)end_pos + 1; i <= last_checked; i++) coef[scan[i]] = 0;
+    return num_nz;
+}
+
+void orc_rdoq(const orc_rdoq_req_t *reqs, int n, const orc_rdoq_est_t *ests, s16 *coefs, s32 *num_nz)
+{
+    orc_init();
+    for (int i = 0; i < n; i++) num_nz[i] = rdoq_block(&reqs[i], &ests[reqs[i].est], coefs + reqs[i].coef_offset);
+}

@@ -220,6 +220,34 @@ typedef struct {
     u32 out_offset;     /* byte offset of the CU's prediction: Y (w x h), then U and V (w/2 x h/2) */
 } orc_mc_req_t;
 
+/* ------------- RDOQ of a transform block (quant_non_zero + rdoq_quant_block, src/quant.c:196-383) ------------- */
+
+/* the bin-cost estimates rdoq_init_cu_est_bits (src/quant.c:139-156) derives from the entropy
+ * coder's context state (core_t rdoq_bin_est_*, inc/define.h:335-339) */
+typedef struct {
+    s32 ctp[2];
+    s32 cbf[3][2];
+    s32 run[24][2];
+    s32 lvl[24][2];
+    s32 lst[2][6][12][2];
+} orc_rdoq_est_t;
+
+typedef struct {
+    u32 coef_offset;    /* first coefficient (s16 index) of the w x h block (raster)            */
+    u8  log2w, log2h;   /* 2..6                                                                 */
+    u8  qp;             /* 0..79 (quantisation step index)                                      */
+    u8  is_intra;
+    u8  ch_type;        /* 0 Y, 1 U, 2 V                                                        */
+    u8  slice_type;     /* 1 = SLICE_I                                                          */
+    u16 est;            /* index of the estimate set                                            */
+    u32 pad;
+    s64 lambda;         /* (s64)(d_lambda * 2^15 + 0.5), as rdoq_quant_block forms it           */
+} orc_rdoq_req_t;
+
+/* quant_non_zero with flat quantisation for every block: levels written over the coefficients
+ * (unchanged when quant_check finds no coefficient above the threshold), num_nz[i] returned */
+void orc_rdoq(const orc_rdoq_req_t *reqs, int n, const orc_rdoq_est_t *ests, s16 *coefs, s32 *num_nz);
+
 /* one affine CU (com_mc_cu_affine, src/com_mc.c:361-422) */
 typedef struct {
     s16 x, y;           /* CU position                                                            */

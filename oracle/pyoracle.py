@@ -223,6 +223,14 @@ class Oracle(_Common):
         self.L.orc_mc_affine(W, H, arr, i_ref, carr, i_c, ptr(reqs), len(reqs), ptr(out))
         return out[:out_bytes]
 
+    def rdoq(self, reqs, ests, coefs):
+        """quant_non_zero (flat) for every RDOQ_REQ; coefs (int16) is updated in place; returns num_nz"""
+        reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
+        ests = np.ascontiguousarray(ests, dtype=RDOQ_EST)
+        nz = np.zeros(len(reqs), dtype=np.int32)
+        self.L.orc_rdoq(ptr(reqs), len(reqs), ptr(ests), ptr(coefs), ptr(nz))
+        return nz
+
     def loka_finish(self, cfg, units):
         """(picture cost, icost, icost_uv[2], map_dqp) from the unit records"""
         cfg = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)
@@ -390,6 +398,25 @@ class RefLib(_Common):
                                   C.c_void_p(reqs.ctypes.data + i * AFFINE_REQ.itemsize), ptr(out))
         return out[:out_bytes]
 
+    def rdoq(self, reqs, ests, coefs):
+        """quant_non_zero itself, one call per request (same arguments as Oracle.rdoq)"""
+        reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
+        ests = np.ascontiguousarray(ests, dtype=RDOQ_EST)
+        nz = np.zeros(len(reqs), dtype=np.int32)
+        for i in range(len(reqs)):
+            nz[i] = self.L.refk_rdoq(C.c_void_p(reqs.ctypes.data + i * RDOQ_REQ.itemsize),
+                                     C.c_void_p(ests.ctypes.data + int(reqs[i]["est"]) * RDOQ_EST.itemsize),
+                                     ptr(coefs))
+        return nz
+
+    def rdoq_est_from_ctx(self, ctx):
+        """rdoq_init_cu_est_bits of 86 context models (ctp, cbf[3], run[24], level[24], last1[12],
+        last2[22])"""
+        ctx = np.ascontiguousarray(ctx, dtype=np.uint16)
+        e = np.zeros(1, dtype=RDOQ_EST)
+        self.L.refk_rdoq_est_from_ctx(ptr(ctx), ptr(e))
+        return e[0]
+
     def loka_search(self, cfg, org_y, i_org, ref, i_ref, ref_ptr, refi, num_refp, x, y):
         """me_search_tz of one 16x16 unit with the lookahead's settings: (mv_x, mv_y, cost)"""
         c = np.ascontiguousarray(cfg, dtype=LOKA_CFG).reshape(1)[0]
@@ -422,6 +449,10 @@ MC_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot"
                    ("mv", "<i2", (2, 2)), ("channel", "u1"), ("pad", "u1", (3,)), ("out_offset", "<u4")])
 AFFINE_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)), ("cp_num", "u1"),
                        ("sub8", "u1"), ("pad", "u1", (2,)), ("cpmv", "<i4", (2, 3, 2)), ("out_offset", "<u4")])
+RDOQ_EST = np.dtype([("ctp", "<i4", (2,)), ("cbf", "<i4", (3, 2)), ("run", "<i4", (24, 2)), ("lvl", "<i4", (24, 2)),
+                     ("lst", "<i4", (2, 6, 12, 2))])
+RDOQ_REQ = np.dtype([("coef_offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), ("qp", "u1"), ("is_intra", "u1"),
+                     ("ch_type", "u1"), ("slice_type", "u1"), ("est", "<u2"), ("pad", "<u4"), ("lambda_", "<i8")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
 
 MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],

@@ -416,3 +416,61 @@ void refk_mc_affine(int W, int H, pel **planes, int n_slots, int i_ref, pel **ch
     memcpy(o + n, pred[U_C], (size_t)n / 4);
     memcpy(o + n + n / 4, pred[V_C], (size_t)n / 4);
 }
+
+/* ---- 7. RDOQ of a transform block ------------------------------------------------------------
+ * quant_non_zero (src/quant.c:315) with flat quantisation, on a core_t whose bin-cost estimates
+ * (rdoq_bin_est_*) are the request's; layouts orc_rdoq_req_t / orc_rdoq_est_t (oracle.h).  The
+ * request's integer lambda L is passed as the double L / 2^15, which rdoq_quant_block turns back
+ * into L exactly. */
+typedef struct {
+    s32 ctp[2]; s32 cbf[3][2]; s32 run[24][2]; s32 lvl[24][2]; s32 lst[2][6][12][2];
+} glue_rdoq_est_t;
+typedef struct {
+    u32 coef_offset; u8 log2w, log2h; u8 qp, is_intra, ch_type, slice_type; u16 est; u32 pad; s64 lambda;
+} glue_rdoq_req_t;
+
+int refk_rdoq(const glue_rdoq_req_t *rq, const glue_rdoq_est_t *E, s16 *coef)
+{
+    refk_init();
+    static core_t *core = NULL;
+    static com_info_t info;
+    static com_pic_header_t pichdr;
+    if (!core) core = (core_t *)calloc(1, sizeof(core_t));
+    memset(&info, 0, sizeof(info));
+    memset(&pichdr, 0, sizeof(pichdr));
+    info.bit_depth_internal = 8;
+    pichdr.pic_wq_enable = 0;
+    core->info = &info;
+    core->pichdr = &pichdr;
+    memcpy(core->rdoq_bin_est_ctp, E->ctp, sizeof(E->ctp));
+    memcpy(core->rdoq_bin_est_cbf, E->cbf, sizeof(E->cbf));
+    memcpy(core->rdoq_bin_est_run, E->run, sizeof(E->run));
+    memcpy(core->rdoq_bin_est_lvl, E->lvl, sizeof(E->lvl));
+    memcpy(core->rdoq_bin_est_lst, E->lst, sizeof(E->lst));
+    return quant_non_zero(core, rq->qp, (double)rq->lambda / 32768.0, rq->is_intra, coef + rq->coef_offset,
+                          rq->log2w, rq->log2h, rq->ch_type, rq->slice_type);
+}
+
+/* rdoq_init_cu_est_bits (src/quant.c:139) from raw context models, for realistic estimate sets:
+ * ctx holds ctp_zero_flag, cbf[3], run_rdoq[24], level[24], last1[12], last2[22] (u16 models) */
+void refk_rdoq_est_from_ctx(const u16 *ctx, glue_rdoq_est_t *E)
+{
+    refk_init();
+    static core_t *core = NULL;
+    static lbac_t lbac;
+    if (!core) core = (core_t *)calloc(1, sizeof(core_t));
+    memset(&lbac, 0, sizeof(lbac));
+    int k = 0;
+    lbac.h.ctp_zero_flag[0] = ctx[k++];
+    for (int i = 0; i < LBAC_CTX_CBF; i++) lbac.h.cbf[i] = ctx[k++];
+    for (int i = 0; i < LBAC_CTX_RUN_RDOQ; i++) lbac.h.run_rdoq[i] = ctx[k++];
+    for (int i = 0; i < LBAC_CTX_LEVEL; i++) lbac.h.level[i] = ctx[k++];
+    for (int i = 0; i < LBAC_CTX_LAST1 * 2; i++) lbac.h.last1[i] = ctx[k++];
+    for (int i = 0; i < LBAC_CTX_LAST2 * 2 - 2; i++) lbac.h.last2[i] = ctx[k++];
+    rdoq_init_cu_est_bits(core, &lbac);
+    memcpy(E->ctp, core->rdoq_bin_est_ctp, sizeof(E->ctp));
+    memcpy(E->cbf, core->rdoq_bin_est_cbf, sizeof(E->cbf));
+    memcpy(E->run, core->rdoq_bin_est_run, sizeof(E->run));
+    memcpy(E->lvl, core->rdoq_bin_est_lvl, sizeof(E->lvl));
+    memcpy(E->lst, core->rdoq_bin_est_lst, sizeof(E->lst));
+}

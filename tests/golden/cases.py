@@ -511,11 +511,59 @@ def run_affine(B, p, seed):
     return digest(B.mc_affine(p["w"], p["h"], addrs, stride, caddrs, sc, reqs, nbytes))
 
 
+# ------------------------------------------------------------------ RDOQ of transform blocks
+RDOQ_SIZES = [(2, 2), (3, 3), (4, 4), (5, 5), (6, 6), (2, 3), (3, 2), (2, 4), (4, 2), (3, 4), (4, 3), (3, 5), (5, 3),
+              (4, 5), (5, 4), (4, 6), (6, 4), (5, 6), (6, 5), (3, 6), (6, 3)]
+
+
+def rdoq_ests(rng, k):
+    """k sets of bin-cost estimates: pairs of costs (1/32768 bit units) between ~0.01 and ~6 bits"""
+    import pyoracle
+    e = np.zeros(k, dtype=pyoracle.RDOQ_EST)
+    for f in ("ctp", "cbf", "run", "lvl", "lst"):
+        e[f] = rng.integers(300, 200000, e[f].shape)
+    return e
+
+
+def rdoq_inputs(B, p, seed):
+    """forward DCT2 coefficients of Laplacian residual blocks of every TB shape, quantisation
+    steps 10..60, intra / inter, luma / chroma"""
+    import pyoracle
+    rng = np.random.default_rng(seed)
+    n = p["n"]
+    reqs = np.zeros(n, dtype=pyoracle.RDOQ_REQ)
+    parts, off = [], 0
+    for i in range(n):
+        lw, lh = RDOQ_SIZES[int(rng.integers(len(RDOQ_SIZES)))]
+        w, h = 1 << lw, 1 << lh
+        scale = float(rng.choice([2.0, 6.0, 20.0, 60.0]))
+        resi = np.clip(np.rint(rng.laplace(0, scale, (h, w))), -255, 255).astype(np.int16)
+        coef = np.zeros(w * h, np.int16)
+        B.trans_dct2(lw, lh, resi, coef)
+        parts.append(coef)
+        qp = int(rng.integers(10, 61))
+        reqs[i]["coef_offset"] = off
+        reqs[i]["log2w"], reqs[i]["log2h"], reqs[i]["qp"] = lw, lh, qp
+        reqs[i]["is_intra"] = int(rng.integers(0, 2))
+        reqs[i]["ch_type"] = 0 if (lw > 5 or lh > 5) else int(rng.integers(0, 3))
+        reqs[i]["slice_type"] = int(rng.integers(1, 4))
+        reqs[i]["est"] = int(rng.integers(0, p["k"]))
+        reqs[i]["lambda_"] = int(round(1.43631 * 2.0 ** ((qp - 16) / 4.0) * 32768))
+        off += w * h
+    return reqs, rdoq_ests(rng, p["k"]), np.concatenate(parts)
+
+
+def run_rdoq(B, p, seed):
+    reqs, ests, coefs = rdoq_inputs(B, p, seed)
+    nz = B.rdoq(reqs, ests, coefs)
+    return digest(coefs, nz)
+
+
 RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "rdoq": run_rdoq,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -531,6 +579,9 @@ MC_CASES = [
     dict(w=192, h=128, vel=(2.5, -1.25), n=160),
     dict(w=96, h=64, vel=(-6.0, 3.5), n=96),
 ]
+
+# RDOQ cases (transform blocks of every shape, several estimate sets)
+RDOQ_CASES = [dict(n=200, k=4), dict(n=120, k=1)]
 
 # lookahead cases: encoder picture level (padded references, random access with both lists or
 # low delay with 4 references) and the scene-cut estimate (1 reference, no padding)
@@ -609,6 +660,8 @@ def all_cases():
         add("mc", **p)
     for p in MC_CASES:
         add("affine", **p)
+    for p in RDOQ_CASES:
+        add("rdoq", **p)
     return cases
 
 

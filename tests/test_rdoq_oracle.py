@@ -1,0 +1,22 @@
+"""CPU: the RDOQ restatement (orc_rdoq) against the reference's quant_non_zero on blocks whose bin-cost
+estimates come from the reference's own rdoq_init_cu_est_bits over random entropy-coder contexts."""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import cases  # noqa: E402
+
+
+def test_rdoq_with_estimates_from_contexts(oracle, ref):
+    rng = np.random.default_rng(12)
+    for seed in range(8):
+        reqs, _, coefs = cases.rdoq_inputs(oracle, dict(n=150, k=3), 4000 + seed)
+        # context models: 10-bit LPS probability << 1 | MPS
+        ests = np.stack([ref.rdoq_est_from_ctx((rng.integers(8, 1016, 86) << 1) | rng.integers(0, 2, 86))
+                         for _ in range(3)])
+        a, b = coefs.copy(), coefs.copy()
+        assert np.array_equal(oracle.rdoq(reqs, ests, a), ref.rdoq(reqs, ests, b))
+        assert np.array_equal(a, b)

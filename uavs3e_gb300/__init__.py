@@ -73,6 +73,8 @@ def _declare(L):
     L.uavs3e_cuda_mc_cu_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_mc_affine.argtypes = [P, P, I, P, C.c_size_t]
     L.uavs3e_cuda_mc_affine_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
+    L.uavs3e_cuda_rdoq.argtypes = [P, I, P, I, P, C.c_size_t, P]
+    L.uavs3e_cuda_rdoq_device.argtypes = [P, I, P, I, P, C.c_size_t, P, P]
 
 
 def check(rc, what="uavs3e_cuda"):
@@ -88,7 +90,7 @@ def init(device=0):
     check(lib().uavs3e_cuda_init(device), "uavs3e_cuda_init")
 
 
-PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz", "mc")
+PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz", "mc", "rdoq")
 
 CU = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
@@ -240,9 +242,9 @@ def launch_count():
 
 def profile_collect():
     """{kernel: (total_ms, launches)} since the last collect"""
-    ms = (C.c_double * 8)()
-    cnt = (C.c_int * 8)()
-    check(lib().uavs3e_cuda_profile_collect(ms, cnt, 8), "profile_collect")
+    ms = (C.c_double * 12)()
+    cnt = (C.c_int * 12)()
+    check(lib().uavs3e_cuda_profile_collect(ms, cnt, 12), "profile_collect")
     return {k: (ms[i], cnt[i]) for i, k in enumerate(PROF_KERNELS)}
 
 
@@ -382,6 +384,32 @@ def mc_cu_device(width, height, d_planes, i_ref, pad, d_chroma, i_c, pad_c, d_re
         stream = torch.cuda.current_stream().cuda_stream
     check(lib().uavs3e_cuda_mc_cu_device(width, height, a, len(d_planes) // 16, i_ref, pad, c, i_c, pad_c, d_reqs, n,
                                          d_out, out_bytes, stream), "mc_cu_device")
+
+
+# ------------------------------------------------------------------ RDOQ of transform blocks
+RDOQ_EST = np.dtype([("ctp", "<i4", (2,)), ("cbf", "<i4", (3, 2)), ("run", "<i4", (24, 2)), ("lvl", "<i4", (24, 2)),
+                     ("lst", "<i4", (2, 6, 12, 2))])
+RDOQ_REQ = np.dtype([("coef_offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), ("qp", "u1"), ("is_intra", "u1"),
+                     ("ch_type", "u1"), ("slice_type", "u1"), ("est", "<u2"), ("pad", "<u4"), ("lambda_", "<i8")])
+
+
+def rdoq(reqs, ests, coefs):
+    """quant_non_zero (flat) for every RDOQ_REQ on host arrays: coefs (int16) updated in place;
+    returns num_nz"""
+    reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
+    ests = np.ascontiguousarray(ests, dtype=RDOQ_EST)
+    assert coefs.dtype == np.int16 and coefs.flags["C_CONTIGUOUS"]
+    nz = np.zeros(max(1, len(reqs)), dtype=np.int32)
+    check(lib().uavs3e_cuda_rdoq(reqs.ctypes.data, len(reqs), ests.ctypes.data, len(ests), coefs.ctypes.data,
+                                 coefs.size, nz.ctypes.data), "rdoq")
+    return nz[:len(reqs)]
+
+
+def rdoq_device(d_reqs, n, d_ests, n_est, d_coefs, n_coefs, d_num_nz, stream=None):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_rdoq_device(d_reqs, n, d_ests, n_est, d_coefs, n_coefs, d_num_nz, stream), "rdoq_device")
 
 
 # ------------------------------------------------------------------ per-call TZ motion search
