@@ -3,12 +3,13 @@
 // the encoder derived from its entropy-coder state (rdoq_init_cu_est_bits, :139-156) -- the
 // levels and the count of coded coefficients bit-exact with the reference's call.
 //
-// One warp per block.  The warp zeroes the coefficients past 32 columns / rows, runs quant_check,
-// gathers the block into scan order in shared memory and marks, in a bitmask, the scan positions
-// whose first-pass level (quant_rdoq) is not zero.  The decision pass is a chain (each coded
-// level selects the contexts of the next), so one lane walks it, visiting only the marked
-// positions: a run of z zero levels adds est_run[last_b_zero][0] + (z - 1) est_run[1][0] bits at
-// once, as the reference's per-position loop accumulates them.
+// One warp per 32 blocks.  First the warp takes its blocks one by one: zeroes the coefficients
+// past 32 columns / rows, runs quant_check, and lists in scan order the positions whose
+// first-pass level (quant_rdoq) is not zero (ballot + prefix count).  The decision pass is a
+// chain (each coded level selects the contexts of the next), so then every lane walks the chain
+// of one block over its listed positions: a run of z zero levels adds
+// est_run[last_b_zero][0] + (z - 1) est_run[1][0] bits at once, as the reference's per-position
+// loop accumulates them.
 #include "common.cuh"
 #include "quant_tables.cuh"
 #include "tables.h"
@@ -39,6 +40,7 @@ struct RdoqParams {
     s16 *coefs;
     unsigned long long n_coefs;
     s32 *num_nz;
+    u32 *scratch;             // per coefficient: the listed positions of each block
     const u16 *scan[7][7];
     const u16 *scanpos[7][7];
     s32 err_scale[80][6];     // tbl_rdoq_err_scale (rdoq_init_err_scale, src/quant.c:69-83), 8-bit
@@ -66,59 +68,77 @@ __device__ __forceinline__ u32 rq_coef(s64 uncoded, s64 *coded, u32 level_double
 
 __global__ void __launch_bounds__(32 * RQ_WARPS) k_rdoq(const RdoqParams P)
 {
-    __shared__ s16 s_c1[RQ_WARPS][64 * 64];
-    __shared__ u32 s_mask[RQ_WARPS][64 * 64 / 32];
+    __shared__ int s_cnt[RQ_WARPS][32];        // marked positions of each of the warp's blocks, -1: done
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = blockIdx.x * RQ_WARPS + warp;
-    if (r >= P.n) return;
-    const RdoqReq q = P.reqs[r];
-    const int lw = q.log2w, lh = q.log2h, w = 1 << lw, h = 1 << lh, ch = q.ch_type;
-    // blocks outside the supported domain are left untouched, with num_nz = -1
-    if (lw < 2 || lw > 6 || lh < 2 || lh > 6 || q.qp > 79 || ch > 2 || q.est >= P.n_est ||
-        (unsigned long long)q.coef_offset + (unsigned long long)(w * h) > P.n_coefs) {
-        if (lane == 0) P.num_nz[r] = -1;
-        return;
+    const int r0 = (blockIdx.x * RQ_WARPS + warp) * 32;
+    if (r0 >= P.n) return;
+    // phase 1, the warp over each of its 32 blocks in turn
+    for (int b = 0; b < 32; b++) {
+        const int r = r0 + b;
+        if (r >= P.n) break;
+        const RdoqReq q = P.reqs[r];
+        const int lw = q.log2w, lh = q.log2h, w = 1 << lw, h = 1 << lh;
+        // blocks outside the supported domain are left untouched, with num_nz = -1
+        if (lw < 2 || lw > 6 || lh < 2 || lh > 6 || q.qp > 79 || q.ch_type > 2 || q.est >= P.n_est ||
+            (unsigned long long)q.coef_offset + (unsigned long long)(w * h) > P.n_coefs) {
+            if (lane == 0) { P.num_nz[r] = -1; s_cnt[warp][b] = -1; }
+            continue;
+        }
+        s16 *coef = P.coefs + q.coef_offset;
+        const int max_num = w * h, max_used = 1 << (lw + min(5, lh));
+        // quant_non_zero: coefficients past 32 columns / rows are zeroed
+        if (w > 32 || h > 32)
+            for (int p = lane; p < max_num; p += 32)
+                if ((p & (w - 1)) >= 32 || (p >> lw) >= 32) coef[p] = 0;
+        __syncwarp();
+        // rdoq_quant_block: quant_check over the first max_used coefficients (raster order)
+        const int odd = (lw + lh) & 1, log2_size = (lw + lh) >> 1;
+        const int q_bits = 14 + (15 - 8 - log2_size);
+        const int q_value = odd ? ((int)kQScale[q.qp] * 181 + 64) >> 7 : (int)kQScale[q.qp];
+        const int offset = (q.slice_type == 1 ? 201 : 153) << (q_bits - 9);
+        const int nz_thr = ((((1 << q_bits) - offset) << 10) / q_value - 1) >> 10;
+        bool above = false;
+        for (int p = lane; p < max_used; p += 32) {
+            const int c = coef[p];
+            above |= c > nz_thr || c < -nz_thr;
+        }
+        if (!__any_sync(0xffffffffu, above)) {
+            if (lane == 0) { P.num_nz[r] = 0; s_cnt[warp][b] = -1; }
+            continue;
+        }
+        // scan order; the positions whose first-pass level (quant_rdoq) is not zero -- exactly
+        // those with |c| >= thr -- are listed in order as (position << 16 | coefficient)
+        const u16 *scan = P.scan[lw][lh];
+        const int thr = ((1 << (q_bits - 1)) - 1) / q_value + 1;
+        u32 *list = P.scratch + q.coef_offset;
+        int cnt = 0;
+        for (int base = 0; base < max_num; base += 32) {
+            const int i = base + lane;
+            const int c = i < max_num ? coef[scan[i]] : 0;
+            const bool mark = abs(c) >= thr;
+            const u32 m = __ballot_sync(0xffffffffu, mark);
+            if (mark) list[cnt + __popc(m & ((1u << lane) - 1))] = ((u32)i << 16) | (u16)c;
+            cnt += __popc(m);
+        }
+        __syncwarp();
+        for (int p = lane; p < max_num; p += 32) coef[p] = 0;   // levels are written over the block
+        if (lane == 0) s_cnt[warp][b] = cnt;
+        __syncwarp();
     }
-    s16 *coef = P.coefs + q.coef_offset;
-    const int max_num = w * h, max_used = 1 << (lw + min(5, lh));
-    // quant_non_zero: coefficients past 32 columns / rows are zeroed
-    if (w > 32 || h > 32)
-        for (int p = lane; p < max_num; p += 32)
-            if ((p & (w - 1)) >= 32 || (p >> lw) >= 32) coef[p] = 0;
     __syncwarp();
-    // rdoq_quant_block: quant_check over the first max_used coefficients (raster order)
+    // phase 2: lane b walks the decision chain of block b
+    const int r = r0 + lane;
+    if (r >= P.n) return;
+    const int cnt = s_cnt[warp][lane];
+    if (cnt < 0) return;
+    const RdoqReq q = P.reqs[r];
+    const int lw = q.log2w, lh = q.log2h, ch = q.ch_type, max_num = 1 << (lw + lh);
     const int odd = (lw + lh) & 1, log2_size = (lw + lh) >> 1;
     const int q_bits = 14 + (15 - 8 - log2_size);
     const int q_value = odd ? ((int)kQScale[q.qp] * 181 + 64) >> 7 : (int)kQScale[q.qp];
-    const int offset = (q.slice_type == 1 ? 201 : 153) << (q_bits - 9);
-    const int nz_thr = ((((1 << q_bits) - offset) << 10) / q_value - 1) >> 10;
-    bool above = false;
-    for (int p = lane; p < max_used; p += 32) {
-        const int c = coef[p];
-        above |= c > nz_thr || c < -nz_thr;
-    }
-    if (!__any_sync(0xffffffffu, above)) {
-        if (lane == 0) P.num_nz[r] = 0;
-        return;
-    }
-    // scan order, first-pass level marks (quant_rdoq: level >= 1 exactly when |c| >= thr)
-    s16 *c1 = s_c1[warp];
-    u32 *mask = s_mask[warp];
-    const u16 *scanpos = P.scanpos[lw][lh], *scan = P.scan[lw][lh];
-    for (int p = lane; p < max_num; p += 32) c1[scanpos[p]] = coef[p];
-    __syncwarp();
-    const int thr = ((1 << (q_bits - 1)) - 1) / q_value + 1;
-    int last_nz = -1;
-    for (int base = 0; base < max_num; base += 32) {
-        const int i = base + lane;
-        const u32 m = __ballot_sync(0xffffffffu, i < max_num && abs((int)c1[i]) >= thr);
-        if (lane == 0) mask[base >> 5] = m;
-        if (m) last_nz = base + 31 - __clz(m);
-    }
-    for (int p = lane; p < max_num; p += 32) coef[p] = 0;   // levels are written over the block
-    __syncwarp();
-    if (lane != 0) return;
-    // the decision chain
+    s16 *coef = P.coefs + q.coef_offset;
+    const u16 *scan = P.scan[lw][lh];
+    const u32 *list = P.scratch + q.coef_offset;
     const RdoqEst &E = P.ests[q.est];
     const s32 err_scale = P.err_scale[q.qp][log2_size - 1];
     const s64 lambda = q.lambda;
@@ -131,47 +151,46 @@ __global__ void __launch_bounds__(32 * RQ_WARPS) k_rdoq(const RdoqParams P)
     const s32 (*est_run)[2] = E.run + 10 + base, (*est_lvl)[2] = E.lvl + 10 + base;
     u32 last_b_zero = 0;
     int end_pos = 0, last_checked = 0, tmp_nz = 0, num_nz = 0, zero_bins = 0, prev = -1;
-    for (int word = 0; word <= (last_nz >> 5); word++) {
-        u32 m = mask[word];
-        while (m) {
-            const int i = (word << 5) + __ffs(m) - 1;
-            m &= m - 1;
-            const int z = i - prev - 1;            // zero levels since the previous mark
-            if (z > 0) {
-                zero_bins += est_run[last_b_zero][0] + (z - 1) * est_run[1][0];
-                last_b_zero = 1;
-            }
-            prev = i;
-            if (zero_bins) { curr_delta += (s64)zero_bins * lambda; zero_bins = 0; }
-            const u32 a = (u32)abs((int)c1[i]);
-            const u32 ld = a * (u32)q_value;
-            const s64 e = ((s64)ld * err_scale) >> 20;
-            const s64 zerr = e * e;
-            const u32 abs_level = (u32)(s16)(u32)(((u64)ld + add) >> q_bits);
-            s64 cc;
-            const u32 level = rq_coef(zerr, &cc, ld, abs_level, est_run[last_b_zero], est_lvl, q_bits, err_scale,
-                                      lambda, i == max_num - 1);
-            curr_delta += cc - zerr;
-            if (level) {
-                last_checked = i;
-                coef[scan[i]] = (s16)(c1[i] < 0 ? -(int)level : (int)level);
-                const int lg = 31 - __clz(i + 1);
-                const s64 end_cost = curr_delta + (s64)lst[lg][1] * lambda;
-                curr_delta += (s64)lst[lg][0] * lambda;
-                tmp_nz++;
-                if (end_cost < best_delta) { best_delta = end_cost; end_pos = i; num_nz += tmp_nz; tmp_nz = 0; }
-                last_b_zero = 0;
-                const int cls = min((int)level - 1, 5);
-                est_lvl = E.lvl + (cls << 1) + base;
-                est_run = E.run + (cls << 1) + base;
-                lst = E.lst[ch != 0][cls];
-            } else {
-                last_b_zero = 1;
-            }
+    for (int k = 0; k < cnt; k++) {
+        const u32 ent = list[k];
+        const int i = (int)(ent >> 16), c = (s16)(ent & 0xffffu);
+        const int z = i - prev - 1;                // zero levels since the previous listed position
+        if (z > 0) {
+            zero_bins += est_run[last_b_zero][0] + (z - 1) * est_run[1][0];
+            last_b_zero = 1;
+        }
+        prev = i;
+        if (zero_bins) { curr_delta += (s64)zero_bins * lambda; zero_bins = 0; }
+        const u32 ld = (u32)abs(c) * (u32)q_value;
+        const s64 e = ((s64)ld * err_scale) >> 20;
+        const s64 zerr = e * e;
+        const u32 abs_level = (u32)(s16)(u32)(((u64)ld + add) >> q_bits);
+        s64 cc;
+        const u32 level = rq_coef(zerr, &cc, ld, abs_level, est_run[last_b_zero], est_lvl, q_bits, err_scale, lambda,
+                                  i == max_num - 1);
+        curr_delta += cc - zerr;
+        if (level) {
+            last_checked = i;
+            coef[scan[i]] = (s16)(c < 0 ? -(int)level : (int)level);
+            const int lg = 31 - __clz(i + 1);
+            const s64 end_cost = curr_delta + (s64)lst[lg][1] * lambda;
+            curr_delta += (s64)lst[lg][0] * lambda;
+            tmp_nz++;
+            if (end_cost < best_delta) { best_delta = end_cost; end_pos = i; num_nz += tmp_nz; tmp_nz = 0; }
+            last_b_zero = 0;
+            const int cls = min((int)level - 1, 5);
+            est_lvl = E.lvl + (cls << 1) + base;
+            est_run = E.run + (cls << 1) + base;
+            lst = E.lst[ch != 0][cls];
+        } else {
+            last_b_zero = 1;
         }
     }
     if (num_nz)
-        for (int i = end_pos + 1; i <= last_checked; i++) coef[scan[i]] = 0;
+        for (int k = 0; k < cnt; k++) {            // positions after the chosen last one, back to zero
+            const int i = (int)(list[k] >> 16);
+            if (i > end_pos && i <= last_checked) coef[scan[i]] = 0;
+        }
     P.num_nz[r] = num_nz;
 }
 
@@ -182,6 +201,7 @@ int launch_rdoq(const void *reqs, int n, const void *ests, int n_est, s16 *coefs
     if (n == 0) return UC_OK;
     int dev = 0;
     UC_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "rdoq: device index");
     const DevTables *tab = device_tables(dev);
     if (!tab) return set_status(UC_ERR_MEMORY, "rdoq: table upload failed");
     RdoqParams P;
@@ -205,8 +225,24 @@ int launch_rdoq(const void *reqs, int n, const void *ests, int n_est, s16 *coefs
             es = es / qs[qp] / 1;
             P.err_scale[qp][i] = (s32)(es * (double)(1 << 20));
         }
+    // the position lists: one word per coefficient, kept per device and grown on demand
+    {
+        static u32 *scratch[64] = { nullptr };
+        static unsigned long long cap[64] = { 0 };
+        static std::mutex mu;
+        std::lock_guard<std::mutex> lk(mu);
+        if (cap[dev] < n_coefs) {
+            if (scratch[dev]) UC_CHECK(cudaFree(scratch[dev]));
+            scratch[dev] = nullptr;
+            cap[dev] = 0;
+            UC_CHECK(cudaMalloc(&scratch[dev], n_coefs * sizeof(u32)));
+            cap[dev] = n_coefs;
+        }
+        P.scratch = scratch[dev];
+    }
     prof_begin(PROF_RDOQ, st);
-    k_rdoq<<<(unsigned)((n + RQ_WARPS - 1) / RQ_WARPS), 32 * RQ_WARPS, 0, st>>>(P);
+    const int warps = (n + 31) / 32;
+    k_rdoq<<<(unsigned)((warps + RQ_WARPS - 1) / RQ_WARPS), 32 * RQ_WARPS, 0, st>>>(P);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     prof_end(PROF_RDOQ, st);

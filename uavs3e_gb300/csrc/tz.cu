@@ -10,8 +10,9 @@
 // (cost << 20 | visit position) and moves the running best only when that minimum is strictly
 // smaller, as the reference's sequence of strict updates does.  The fractional refinement
 // (me_sub_pel_search :366-500) costs its centre and 8 half-sample points in one batch, then 8
-// quarter-sample points, with com_had tiles spread over the lanes (or per-lane SADs for
-// subpel_cost_type 1), and compares them in the reference's order.
+// quarter-sample points, with the rows of the com_had tiles spread over the lanes (columns
+// transformed through shuffles; per-lane SADs for subpel_cost_type 1), and compares them in the
+// reference's order.
 #include "common.cuh"
 #include "uavs3e_cuda_internal.h"
 #include "../../include/uavs3e_cuda.h"
@@ -218,27 +219,109 @@ __device__ __forceinline__ const pel *tz_mc_ptr(const TzParams &P, int slot, int
     return P.planes[slot * 16 + (qy & 3) * 4 + (qx & 3)] + (long long)py * P.i_ref + px;
 }
 
-// costs (com_had, or SAD when sad) of nc <= 9 candidates at the quarter-sample MVs (vx[k], vy[k])
-// of the block into sum[k]; every lane returns with sum[] complete
-__device__ void tz_sub_costs(const TzS &S, const TzParams &P, int slot, int bx, int by, const int *vx, const int *vy,
+// candidate k of a refinement batch: pattern 0 = centre + the 8 half-sample points, 1 = the 8
+// quarter-sample points, 2 = the centre alone
+__device__ __forceinline__ void tz_sub_mv(int pattern, int k, int cx, int cy, int &vx, int &vy)
+{
+    if (pattern == 1) { vx = cx + kTzQuar[k][0]; vy = cy + kTzQuar[k][1]; }
+    else if (pattern == 0 && k > 0) { vx = cx + kTzHalf[k - 1][0]; vy = cy + kTzHalf[k - 1][1]; }
+    else { vx = cx; vy = cy; }
+}
+
+// One pass of com_had tile rows over the warp: lanes in groups of TH hold one row each of a TW x TH
+// tile (row = lane % TH), rows transformed in registers, columns by butterflies across the group.
+// Tiles of 2:1 shape combine their two square halves as |a + b| + |a - b| = 2 max(|a|, |b|)
+// (com_had_16x8 / _8x16 / _8x4 / _4x8, src/com_cost.c:344-710).  Returns the tile's SATD in
+// every lane of the group (0 for inactive groups).
+template <int TW, int TH>
+__device__ __forceinline__ u32 tz_tile_rows(const pel *o, int io, const pel *p, int ip, bool active, int lane,
+                                            double sq32, double sq128)
+{
+    constexpr bool WIDE = TW > TH, TALL = TW < TH;
+    constexpr int N = WIDE ? TW / 2 : TW;            // points of each row transform
+    constexpr int V = TALL ? TH / 2 : TH;            // points of the column transform
+    int a[N], b[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        a[i] = active ? (int)o[i] - (int)p[i] : 0;
+        b[i] = (WIDE && active) ? (int)o[N + i] - (int)p[N + i] : 0;
+    }
+    wht<N>(a);
+    if (WIDE) wht<N>(b);
+#pragma unroll
+    for (int m = 1; m < V; m <<= 1) {
+        const bool hi = lane & m;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const int pa = __shfl_xor_sync(0xffffffffu, a[i], m);
+            a[i] = hi ? pa - a[i] : a[i] + pa;
+            if (WIDE) {
+                const int pb = __shfl_xor_sync(0xffffffffu, b[i], m);
+                b[i] = hi ? pb - b[i] : b[i] + pb;
+            }
+        }
+    }
+    int s = 0;
+    if (TALL) {                                       // the other half of the 16 (8) rows
+        const bool top = !(lane & V);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const int e = __shfl_xor_sync(0xffffffffu, a[i], V);
+            s += top ? 2 * max(abs(a[i]), abs(e)) : 0;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) s += WIDE ? 2 * max(abs(a[i]), abs(b[i])) : abs(a[i]);
+    }
+#pragma unroll
+    for (int m = 1; m < TH; m <<= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    if (TW == TH) return (u32)(TW == 8 ? (s + 2) >> 2 : (s + 1) >> 1);
+    return (u32)(int)((double)s / (TW * TH == 128 ? sq128 : sq32) * 2.0);
+}
+
+// com_had of nc refinement candidates, tiles spread over the warp as (candidate, tile, row) tasks
+template <int TW, int TH>
+__device__ void tz_had_batch(const TzS &S, const TzParams &P, int slot, int bx, int by, int pattern, int cx, int cy,
+                             int nc, u32 *sum, int lane)
+{
+    const int ntx = S.w / TW, nt = ntx * (S.h / TH), total = nc * nt * TH;
+    const pel *ob = (const pel *)S.so;
+    for (int base = 0; base < total; base += 32) {
+        const int t = base + lane;
+        const bool active = t < total;
+        const int tt = active ? t : 0;
+        const int k = tt / (nt * TH), rem = tt - k * nt * TH, tile = rem / TH, row = rem - tile * TH;
+        const int ox = (tile % ntx) * TW, oy = (tile / ntx) * TH + row;
+        int vx, vy;
+        tz_sub_mv(pattern, k, cx, cy, vx, vy);
+        const pel *p = tz_mc_ptr(P, slot, bx + vx, by + vy) + oy * P.i_ref + ox;
+        const u32 v = tz_tile_rows<TW, TH>(ob + oy * S.w + ox, S.w, p, P.i_ref, active, lane, P.sq32, P.sq128);
+        if (active && row == 0) atomicAdd(&sum[k], v);
+    }
+}
+
+// costs (com_had, or SAD when sad) of the nc candidates of a refinement batch into sum[k]; every
+// lane returns with sum[] complete
+__device__ void tz_sub_costs(const TzS &S, const TzParams &P, int slot, int bx, int by, int pattern, int cx, int cy,
                              int nc, bool sad, u32 *sum, int lane)
 {
     if (lane < 9) sum[lane] = 0;
     __syncwarp();
     if (sad) {
-        if (lane < nc) sum[lane] = tz_sad(S, tz_mc_ptr(P, slot, bx + vx[lane], by + vy[lane]));
+        if (lane < nc) {
+            int vx, vy;
+            tz_sub_mv(pattern, lane, cx, cy, vx, vy);
+            sum[lane] = tz_sad(S, tz_mc_ptr(P, slot, bx + vx, by + vy));
+        }
     } else {
         int tw, th;
         had_tile_shape(S.w, S.h, &tw, &th);
-        const int ntx = S.w / tw, nt = ntx * (S.h / th);
-        const pel *ob = (const pel *)S.so;
-        for (int t = lane; t < nt * nc; t += 32) {
-            const int k = t / nt, tile = t - k * nt;
-            const int ox = (tile % ntx) * tw, oy = (tile / ntx) * th;
-            const pel *p = tz_mc_ptr(P, slot, bx + vx[k], by + vy[k]);
-            const u32 v = satd_tile(tw, th, ob + oy * S.w + ox, S.w, p + oy * P.i_ref + ox, P.i_ref, P.sq32, P.sq128);
-            atomicAdd(&sum[k], v);
-        }
+        if (tw == 8 && th == 8) tz_had_batch<8, 8>(S, P, slot, bx, by, pattern, cx, cy, nc, sum, lane);
+        else if (tw == 4 && th == 4) tz_had_batch<4, 4>(S, P, slot, bx, by, pattern, cx, cy, nc, sum, lane);
+        else if (tw == 16) tz_had_batch<16, 8>(S, P, slot, bx, by, pattern, cx, cy, nc, sum, lane);
+        else if (th == 16) tz_had_batch<8, 16>(S, P, slot, bx, by, pattern, cx, cy, nc, sum, lane);
+        else if (tw == 8) tz_had_batch<8, 4>(S, P, slot, bx, by, pattern, cx, cy, nc, sum, lane);
+        else tz_had_batch<4, 8>(S, P, slot, bx, by, pattern, cx, cy, nc, sum, lane);
     }
     __syncwarp();
 }
@@ -329,33 +412,32 @@ __global__ void __launch_bounds__(32 * TZ_WARPS) k_me_tz(const TzParams P)
         const bool sad = q.flags & 1;
         const int bx = x << 2, by = y << 2;
         u32 *sum = s_sum[warp];
-        int vx[9], vy[9];
-        vx[0] = qx; vy[0] = qy;
-#pragma unroll
-        for (int i = 0; i < 8; i++) { vx[i + 1] = qx + kTzHalf[i][0]; vy[i + 1] = qy + kTzHalf[i][1]; }
-        tz_sub_costs(S, P, q.ref_slot, bx, by, vx, vy, 9, sad, sum, lane);
+        const int cx0 = qx, cy0 = qy;
+        tz_sub_costs(S, P, q.ref_slot, bx, by, 0, cx0, cy0, 9, sad, sum, lane);
         u64 best = (u64)(S.lambda * (tz_bits((qx >> mvr) - S.bpx) + tz_bits((qy >> mvr) - S.bpy))) +
                    ((u64)sum[0] << S.shift);
         for (int i = 1; i < 9; i++) {
-            const u64 c = (u64)(S.lambda * (tz_bits((vx[i] >> mvr) - S.bpx) + tz_bits((vy[i] >> mvr) - S.bpy))) +
+            int vx, vy;
+            tz_sub_mv(0, i, cx0, cy0, vx, vy);
+            const u64 c = (u64)(S.lambda * (tz_bits((vx >> mvr) - S.bpx) + tz_bits((vy >> mvr) - S.bpy))) +
                           ((u64)sum[i] << S.shift);
-            if (c < best) { best = c; qx = vx[i]; qy = vy[i]; }
+            if (c < best) { best = c; qx = vx; qy = vy; }
         }
         if (mvr == 0) {
-#pragma unroll
-            for (int i = 0; i < 8; i++) { vx[i] = qx + kTzQuar[i][0]; vy[i] = qy + kTzQuar[i][1]; }
+            const int cx1 = qx, cy1 = qy;
             __syncwarp();
-            tz_sub_costs(S, P, q.ref_slot, bx, by, vx, vy, 8, sad, sum, lane);
+            tz_sub_costs(S, P, q.ref_slot, bx, by, 1, cx1, cy1, 8, sad, sum, lane);
             for (int i = 0; i < 8; i++) {
-                const u64 c = (u64)(S.lambda * (tz_bits((vx[i] >> mvr) - S.bpx) + tz_bits((vy[i] >> mvr) - S.bpy))) +
+                int vx, vy;
+                tz_sub_mv(1, i, cx1, cy1, vx, vy);
+                const u64 c = (u64)(S.lambda * (tz_bits((vx >> mvr) - S.bpx) + tz_bits((vy >> mvr) - S.bpy))) +
                               ((u64)sum[i] << S.shift);
-                if (c < best) { best = c; qx = vx[i]; qy = vy[i]; }
+                if (c < best) { best = c; qx = vx; qy = vy; }
             }
         }
         if (sad) {   // SAD search, SATD at the winner
-            vx[0] = qx; vy[0] = qy;
             __syncwarp();
-            tz_sub_costs(S, P, q.ref_slot, bx, by, vx, vy, 1, false, sum, lane);
+            tz_sub_costs(S, P, q.ref_slot, bx, by, 2, qx, qy, 1, false, sum, lane);
             best = (u64)(S.lambda * (tz_bits((qx >> mvr) - S.bpx) + tz_bits((qy >> mvr) - S.bpy))) +
                    ((u64)sum[0] << (16 - bi));
         }
