@@ -150,6 +150,16 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_run(uavs3e_cuda_me *me, const uint8_t *org, i
 UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *me, const uint8_t *d_org, int i_org,
                                               uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);
 
+/* One frame as a CUDA graph: refresh reference `slot` from the device picture d_ref (stride
+ * i_src; padding and the 15 quarter-sample planes) and search d_org into d_out -- the launches of
+ * uavs3e_cuda_me_set_ref_device + uavs3e_cuda_me_run_device, captured once per distinct set of
+ * arguments (up to 32 kept, least recently used dropped; all dropped when lambda_mv changes the
+ * search tables) and replayed with one graph launch on `stream`.  The first call with a new set
+ * synchronises the session's stream to capture. */
+UAVS3E_CUDA_API int uavs3e_cuda_me_frame_graph(uavs3e_cuda_me *me, int slot, const uint8_t *d_ref, int i_src,
+                                               const uint8_t *d_org, int i_org, uint32_t lambda_mv,
+                                               uavs3e_cuda_me_result_t *d_out, void *stream);
+
 /*
  * The same search without any allocation -- no cudaMalloc/cudaFree, no allocating library call,
  * no host heap.  It has no counterpart in the reference; it exists for callers that cannot

@@ -91,3 +91,31 @@ def test_me_frame_repeatable_and_device_path(gpu):
     assert np.array_equal(a, b)
     c = ms.run(frames[2], lam)
     assert np.array_equal(a, c)
+
+
+def test_me_frame_graph_matches_plain_launches(gpu):
+    """the frame replayed as a captured CUDA graph gives the plain launches' results, across cached
+    graphs, new argument sets and a lambda change"""
+    import torch
+    W, H = 256, 192
+    frames = motion_sequence(W, H, 6, seed=21)
+    d_frames = [torch.from_numpy(f).cuda() for f in frames]
+    n = gpu.MotionSearch(W, H, n_refs=2, search_range=32, pad=144).n_results
+    plain = gpu.MotionSearch(W, H, n_refs=2, search_range=32, pad=144)
+    graph = gpu.MotionSearch(W, H, n_refs=2, search_range=32, pad=144)
+    sp = torch.cuda.current_stream().cuda_stream
+    d_a = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
+    d_b = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
+    schedule = [(1, 32), (2, 32), (3, 32), (1, 32), (2, 27), (4, 27), (5, 27), (2, 27)]
+    for t, qp in schedule:
+        lam = lambda_mv_for_qp(qp)
+        slot = (t - 1) % 2
+        for ms in (plain, graph):                # the other slot: the same picture in both sessions
+            ms.set_ref_device(1 - slot, d_frames[max(0, t - 2)].data_ptr(), W, sp)
+        plain.set_ref_device(slot, d_frames[t - 1].data_ptr(), W, sp)
+        plain.run_device(d_frames[t].data_ptr(), W, lam, d_a.data_ptr(), sp)
+        graph.frame_graph(slot, d_frames[t - 1].data_ptr(), W, d_frames[t].data_ptr(), W, lam, d_b.data_ptr(), sp)
+        torch.cuda.synchronize()
+        assert torch.equal(d_a, d_b), f"frame {t} (qp {qp}) differs"
+    plain.close()
+    graph.close()

@@ -50,6 +50,7 @@ def _declare(L):
     L.uavs3e_cuda_me_set_ref_device.argtypes = [P, I, P, I, P]
     L.uavs3e_cuda_me_run.argtypes = [P, P, I, U32, P]
     L.uavs3e_cuda_me_run_device.argtypes = [P, P, I, U32, P, P]
+    L.uavs3e_cuda_me_frame_graph.argtypes = [P, I, P, I, P, I, U32, P, P]
     L.uavs3e_cuda_me_plane.restype = P
     L.uavs3e_cuda_me_plane.argtypes = [P, I, I]
     L.uavs3e_cuda_me_plane_stride.argtypes = [P]
@@ -309,6 +310,11 @@ class MotionSearch:
 
     def run_device(self, d_org, i_org, lambda_mv, d_out, stream=None):
         check(lib().uavs3e_cuda_me_run_device(self.h, d_org, i_org, lambda_mv, d_out, stream), "me_run_device")
+
+    def frame_graph(self, slot, d_ref, i_src, d_org, i_org, lambda_mv, d_out, stream=None):
+        """set_ref_device(slot, d_ref) + run_device(d_org) replayed as a captured CUDA graph"""
+        check(lib().uavs3e_cuda_me_frame_graph(self.h, slot, d_ref, i_src, d_org, i_org, lambda_mv, d_out, stream),
+              "me_frame_graph")
 
     def plane_ptr(self, slot, phase):
         return lib().uavs3e_cuda_me_plane(self.h, slot, phase)

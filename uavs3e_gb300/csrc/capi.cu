@@ -76,9 +76,16 @@ static cudaEvent_t prof_event()
     return e;
 }
 
+// a stream being captured into a graph records no timing events
+static bool capturing(cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
 void prof_begin(int k, cudaStream_t st)
 {
-    if (!g_prof) return;
+    if (!g_prof || capturing(st)) return;
     std::lock_guard<std::mutex> lk(g_mu);
     cudaEvent_t e = prof_event();
     cudaEventRecord(e, st);
@@ -87,7 +94,7 @@ void prof_begin(int k, cudaStream_t st)
 
 void prof_end(int k, cudaStream_t st)
 {
-    if (!g_prof) return;
+    if (!g_prof || capturing(st)) return;
     std::lock_guard<std::mutex> lk(g_mu);
     if (g_prof_open[k].empty()) return;
     cudaEvent_t b = g_prof_open[k].back();
@@ -225,6 +232,16 @@ struct uavs3e_cuda_me {
     std::vector<u16> h_r2m;
     void *tz_buf = nullptr;           // TZ requests and results of host runs
     size_t tz_cap = 0;
+    struct Graph {                    // captured frames (uavs3e_cuda_me_frame_graph)
+        int slot, i_src, i_org;
+        const void *ref, *org;
+        void *out;
+        u32 lambda;
+        cudaGraphExec_t exec;
+        unsigned long long launches, used;
+    };
+    std::vector<Graph> graphs;
+    unsigned long long graph_tick = 0;
     pel *chroma_buf = nullptr;        // [n_refs][2][rows_c * stride_c], padded by 72
     int stride_c = 0, rows_c = 0;
     void *mc_buf = nullptr;           // CU MC requests and predictions of host runs
@@ -304,6 +321,7 @@ UAVS3E_CUDA_API void uavs3e_cuda_me_close(uavs3e_cuda_me *m)
     cudaFree(m->planes_buf); cudaFree(m->org_buf); cudaFree(m->out_buf);
     cudaFree(m->keys); cudaFree(m->sub); cudaFree(m->q2); cudaFree(m->r2m); cudaFree(m->tz_buf);
     cudaFree(m->chroma_buf); cudaFree(m->mc_buf);
+    for (auto &g : m->graphs) cudaGraphExecDestroy(g.exec);
     if (m->st) cudaStreamDestroy(m->st);
     delete m;
 }
@@ -482,6 +500,68 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_tz(uavs3e_cuda_me *m, const uavs3e_cuda_tz_pi
     if (r) return r;
     UC_CHECK(cudaMemcpyAsync(out, d_out, (size_t)n * sizeof(*out), cudaMemcpyDeviceToHost, m->st));
     UC_CHECK(cudaStreamSynchronize(m->st));
+    return UC_OK;
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_me_frame_graph(uavs3e_cuda_me *m, int slot, const uint8_t *d_ref, int i_src,
+                                               const uint8_t *d_org, int i_org, uint32_t lambda_mv,
+                                               uavs3e_cuda_me_result_t *d_out, void *stream)
+{
+    if (!m || !d_ref || !d_org || !d_out || slot < 0 || slot >= m->n_refs || i_src < m->W || i_org < m->W)
+        return set_status(UC_ERR_ARG, "me_frame_graph: bad argument");
+    if ((uint64_t)lambda_mv * 36u >= (1ull << 32)) return set_status(UC_ERR_ARG, "me_frame_graph: lambda_mv too large");
+    if (ensure_init()) return uavs3e_cuda_status();
+    // the search tables follow lambda: graphs captured with other tables are dropped
+    const bool new_tables = !(m->tab_ok && m->tab.lambda_mv == lambda_mv);
+    int r = me_prepare_tables(m, lambda_mv, m->st);
+    if (r) return r;
+    if (new_tables) {
+        for (auto &g : m->graphs) cudaGraphExecDestroy(g.exec);
+        m->graphs.clear();
+    }
+    r = me_frame_once();
+    if (r) return r;
+    uavs3e_cuda_me::Graph *hit = nullptr;
+    for (auto &g : m->graphs)
+        if (g.slot == slot && g.ref == d_ref && g.i_src == i_src && g.org == d_org && g.i_org == i_org &&
+            g.lambda == lambda_mv && g.out == d_out) { hit = &g; break; }
+    if (!hit) {
+        if (m->graphs.size() >= 32) {    // evict the least recently used
+            auto lru = m->graphs.begin();
+            for (auto it = m->graphs.begin(); it != m->graphs.end(); ++it) if (it->used < lru->used) lru = it;
+            cudaGraphExecDestroy(lru->exec);
+            m->graphs.erase(lru);
+        }
+        // capture on the session's stream the launches of set_ref_device + run_device
+        UC_CHECK(cudaStreamSynchronize(m->st));
+        UC_CHECK(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
+        const unsigned long long l0 = uavs3e_cuda_launch_count();
+        cudaError_t ce = cudaMemcpy2DAsync(me_plane_ptr(m, slot, 0), m->stride, d_ref, i_src, m->W, m->H,
+                                           cudaMemcpyDeviceToDevice, m->st);
+        int rr = ce == cudaSuccess ? me_interp_slot(m, slot, m->st) : UC_ERR_CUDA;
+        if (!rr) rr = me_launch(m, d_org, i_org, lambda_mv, (MeResult *)d_out, m->st);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(m->st, &graph);
+        if (rr || ce != cudaSuccess || ee != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            if (rr) return rr;
+            return check_cuda(ce != cudaSuccess ? ce : ee, "me_frame_graph: capture");
+        }
+        uavs3e_cuda_me::Graph g;
+        g.slot = slot; g.ref = d_ref; g.i_src = i_src; g.org = d_org; g.i_org = i_org; g.lambda = lambda_mv;
+        g.out = d_out;
+        g.launches = uavs3e_cuda_launch_count() - l0;
+        const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return check_cuda(ie, "me_frame_graph: instantiate");
+        m->graphs.push_back(g);
+        hit = &m->graphs.back();
+        // the capture counted its kernels once; replays count them below
+        count_launch(-(int)hit->launches);
+    }
+    hit->used = ++m->graph_tick;
+    UC_CHECK(cudaGraphLaunch(hit->exec, (cudaStream_t)stream));
+    count_launch((int)hit->launches);
     return UC_OK;
 }
 

@@ -794,16 +794,32 @@ __global__ void __launch_bounds__(256) k_me_sub_final(MeSubParams P)
 
 static bool g_ctu_tab_uploaded[64];
 
-int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStream_t st)
+// one-time per-device setup of the frame search (block table upload, shared-memory limits);
+// synchronous, so it runs before a frame is captured into a graph
+int me_frame_once()
 {
     int dev = 0;
     UC_CHECK(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !g_ctu_tab_uploaded[dev]) {
+    if (dev < 0 || dev >= 64) return UC_OK;
+    if (!g_ctu_tab_uploaded[dev]) {
         CtuBlock tab[ME_BLOCKS_PER_CTU];
         ctu_block_table(tab);
         UC_CHECK(cudaMemcpyToSymbol(kCtuBlocks, tab, sizeof(tab)));
         g_ctu_tab_uploaded[dev] = true;
     }
+    static bool attr_set[64];
+    if (!attr_set[dev]) {
+        UC_CHECK(cudaFuncSetAttribute(k_me_int<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        UC_CHECK(cudaFuncSetAttribute(k_me_int<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        attr_set[dev] = true;
+    }
+    return UC_OK;
+}
+
+int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStream_t st)
+{
+    int rc = me_frame_once();
+    if (rc) return rc;
     const int ctus_w = (a.W + 63) / 64, ctus_h = (a.H + 63) / 64;
     MeIntParams P;
     P.org = a.org; P.i_org = a.i_org;
@@ -824,12 +840,6 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     P.win_cols = ((15 + 64 + t.ndx + 4 + 15) / 16) * 16;
     if ((P.win_cols >> 2) + 18 + 2 > ME_WIN_WW) return set_status(UC_ERR_ARG, "me: window too wide");
     const size_t smem = (size_t)P.win_h * ME_WIN_WW * 4;
-    static bool attr_set[64];
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        UC_CHECK(cudaFuncSetAttribute(k_me_int<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-        UC_CHECK(cudaFuncSetAttribute(k_me_int<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-        attr_set[dev] = true;
-    }
     if (smem > 100 * 1024) return set_status(UC_ERR_ARG, "me: window too large");
     // interior CTUs: every 8x8 tile satisfies pos + 8 + hi <= pic - 1 in both directions
     int nx = a.W - 57 - t.hi_x >= 0 ? (a.W - 57 - t.hi_x) / 64 + 1 : 0;
