@@ -290,6 +290,8 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
     out = {"workload": "intra lattice of a 1080p I-frame: all 468,750 CUs of the 23 shapes 4x4..64x64 (aspect <= 8), "
                        "33 modes, SATD + DCT2 + quant/dequant/inverse/recon/SSD at QP 27/32/37/42",
            "ms_per_frame": ms, "frames_per_s": 1000.0 / ms, "cus": n,
+           "tuned_budgets_kb": {f"{4 << (c // 5)}x{4 << (c % 5)}": b // 1024
+                                for c, b in enumerate(u.lattice_budgets(33)) if b},
            "predicted_samples_per_s": samples / (ms / 1000.0),
            "roofline": {"bound": "int", "kernel": "k_intra_lattice (all shape instances of a frame)",
                         "achieved": macs / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GMAC/s",

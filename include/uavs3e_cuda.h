@@ -343,6 +343,14 @@ typedef struct {
     uint32_t sum_abs;     /* sum of |level|                                            */
 } uavs3e_cuda_lat_q_t;
 
+/* Layout autotuning (on by default): the first call per device and mode count with at least 512
+ * CUs of a shape times the CTA layouts (how many CUs, or which chunk of one CU's modes, a CTA
+ * takes) given by shared-memory budgets of 16..96 KB and keeps the fastest; records are the same
+ * for every layout.  budgets: per shape (log2 w - 2) * 5 + (log2 h - 2), in bytes, 0 = the
+ * default 48 KB (not tuned). */
+UAVS3E_CUDA_API void uavs3e_cuda_lattice_autotune(int on);
+UAVS3E_CUDA_API int uavs3e_cuda_lattice_budgets(int n_modes, int out[25]);
+
 /* The 23-shape lattice (w, h in 4..64, aspect <= 8, largest first) of a picture: writes up to
  * cap records to out (may be NULL) and returns the total count. */
 UAVS3E_CUDA_API int uavs3e_cuda_lattice_cus(int width, int height, uavs3e_cuda_cu_t *out, int cap);

@@ -110,3 +110,21 @@ def test_intra_lattice_mode_subset(gpu):
     assert np.array_equal(qq[sel], q_all.reshape(n, 33, len(qps))[sel])
     assert (satd[~sel] == 0xFFFFFFFF).all()
     assert (qq[~sel].view(np.uint8) == 0xAB).all()
+
+
+def test_lattice_autotuned_layouts_give_the_same_records(gpu):
+    """records do not depend on the CTA layout the autotuner picks"""
+    from uavs3e_gb300.synth import intra_frame
+    W, H = 384, 256
+    org = intra_frame(W, H, seed=41)
+    rec = np.clip(org.astype(int) + np.random.default_rng(42).integers(-4, 5, org.shape), 0, 255).astype(np.uint8)
+    cus = gpu.lattice_cus(W, H)
+    gpu.lattice_autotune(False)
+    want_s, want_q = gpu.intra_lattice(org, rec, cus)
+    gpu.lattice_autotune(True)
+    got_s, got_q = gpu.intra_lattice(org, rec, cus)       # tunes the shapes with >= 512 CUs
+    again_s, again_q = gpu.intra_lattice(org, rec, cus)   # runs the tuned layouts
+    assert np.array_equal(want_s, got_s) and np.array_equal(want_q.view(np.uint8), got_q.view(np.uint8))
+    assert np.array_equal(want_s, again_s) and np.array_equal(want_q.view(np.uint8), again_q.view(np.uint8))
+    tuned = gpu.lattice_budgets(33)
+    assert any(tuned)

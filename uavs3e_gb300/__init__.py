@@ -55,6 +55,9 @@ def _declare(L):
     L.uavs3e_cuda_me_plane.argtypes = [P, I, I]
     L.uavs3e_cuda_me_plane_stride.argtypes = [P]
     L.uavs3e_cuda_lattice_cus.argtypes = [I, I, P, I]
+    L.uavs3e_cuda_lattice_autotune.argtypes = [I]
+    L.uavs3e_cuda_lattice_autotune.restype = None
+    L.uavs3e_cuda_lattice_budgets.argtypes = [I, P]
     L.uavs3e_cuda_intra_lattice_device.argtypes = [P, I, P, I, I, I, P, I, I, P, I, I, P, P, P]
     L.uavs3e_cuda_profile_enable.argtypes = [I]
     L.uavs3e_cuda_launch_count.restype = C.c_ulonglong
@@ -103,6 +106,18 @@ def lattice_cus(width, height):
     out = np.zeros(n, dtype=CU)
     lib().uavs3e_cuda_lattice_cus(width, height, out.ctypes.data, n)
     return out
+
+
+def lattice_autotune(on=True):
+    """switch the lattice's CTA-layout autotuning on (default) or off"""
+    lib().uavs3e_cuda_lattice_autotune(1 if on else 0)
+
+
+def lattice_budgets(n_modes=33):
+    """tuned shared-memory budget (bytes) per shape (log2 w - 2) * 5 + (log2 h - 2); 0 = default"""
+    out = (C.c_int * 25)()
+    check(lib().uavs3e_cuda_lattice_budgets(n_modes, out), "lattice_budgets")
+    return list(out)
 
 
 def intra_lattice(org, rec, cus, qps=(27, 32, 37, 42), ipf=0, is_intra=1, stream=None):

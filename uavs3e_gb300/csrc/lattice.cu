@@ -19,6 +19,8 @@
 // the CU's org part (computed once per CU) minus a dp4a product with the u8 prediction; the
 // column pass and both inverse passes are dp2a products of s16 pairs with s8 matrix rows.
 #include "lattice_kernel.cuh"
+
+#include <mutex>
 #include "../../include/uavs3e_cuda.h"
 
 #include <algorithm>
@@ -96,8 +98,72 @@ size_t lattice_smem_bytes(int w, int h, int nm)
     while ((1 << lw) < w) lw++;
     while ((1 << lh) < h) lh++;
     LatLayout L;
-    lat_layout(lw, lh, nm, L);
+    lat_layout(lw, lh, nm, LAT_BUDGET, L);
     return (size_t)L.smem;
+}
+
+// Autotuning of the CTA layout: per device, mode count and shape, the first call with at least
+// LAT_TUNE_MIN_CUS CUs of the shape times each distinct layout the candidate budgets give (every
+// run writes the same records) and keeps the fastest for the later calls.
+constexpr int LAT_TUNE_MIN_CUS = 512;
+static const int kLatBudgets[] = { 16 * 1024, 24 * 1024, 32 * 1024, 40 * 1024, 48 * 1024, 56 * 1024,
+                                   72 * 1024, 96 * 1024 };
+struct LatTune {
+    std::mutex mu;
+    int budget[34][LAT_SHAPES] = {};
+};
+static LatTune g_tune[64];
+static bool g_tune_on = true;
+
+static int lat_launch(int lw, int lh, unsigned grid, int smem, cudaStream_t st, const LatParams &P)
+{
+    switch (lw) {
+    case 2: return lat_launch_w<2>(lh, grid, smem, st, P);
+    case 3: return lat_launch_w<3>(lh, grid, smem, st, P);
+    case 4: return lat_launch_w<4>(lh, grid, smem, st, P);
+    case 5: return lat_launch_w<5>(lh, grid, smem, st, P);
+    default: return lat_launch_w<6>(lh, grid, smem, st, P);
+    }
+}
+
+// times the distinct layouts of one shape on this call's CUs; returns the best budget (and the
+// launches it made in *launches)
+static int lat_tune_shape(int lw, int lh, int n, LatParams P, cudaStream_t st, int *launches, int *best_out)
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    UC_CHECK(cudaEventCreate(&e0));
+    UC_CHECK(cudaEventCreate(&e1));
+    float best_ms = 3.0e38f;
+    int best = LAT_BUDGET, seen = 0;
+    int seen_g[8], seen_mc[8];
+    for (int b : kLatBudgets) {
+        LatLayout L;
+        lat_layout(lw, lh, P.n_modes, b, L);
+        if (L.smem > LAT_SMEM_MAX || L.G < 1) continue;
+        bool dup = false;
+        for (int k = 0; k < seen; k++) dup |= seen_g[k] == L.G && seen_mc[k] == L.MC;
+        if (dup) continue;
+        seen_g[seen] = L.G; seen_mc[seen] = L.MC; seen++;
+        P.budget = b;
+        const unsigned grid = (unsigned)((long long)((n + L.G - 1) / L.G) * L.nchunk);
+        float ms = 3.0e38f;
+        for (int rep = 0; rep < 2; rep++) {
+            UC_CHECK(cudaEventRecord(e0, st));
+            int r = lat_launch(lw, lh, grid, L.smem, st, P);
+            if (r) { cudaEventDestroy(e0); cudaEventDestroy(e1); return r; }
+            UC_CHECK(cudaEventRecord(e1, st));
+            UC_CHECK(cudaEventSynchronize(e1));
+            float t = 0;
+            UC_CHECK(cudaEventElapsedTime(&t, e0, e1));
+            ms = t < ms ? t : ms;
+            (*launches)++;
+        }
+        if (ms < best_ms) { best_ms = ms; best = b; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *best_out = best;
+    return UC_OK;
 }
 
 // per device: the CU permutation and the per-shape counters
@@ -162,21 +228,29 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
             const int c = (lw - 2) * 5 + (lh - 2);
             const int n = S.h_counts[c];
             if (!n) continue;
-            LatLayout L;
-            lat_layout(lw, lh, n_modes, L);
             P.perm = S.perm + offs[c];
             P.n_shape = n;
             P.fold_w = tab->fold[lw]; P.fold_h = tab->fold[lh];
             P.scanpos = tab->scanpos[lw][lh];
-            const long long grid = (long long)((n + L.G - 1) / L.G) * L.nchunk;
-            int r = 0;
-            switch (lw) {
-            case 2: r = lat_launch_w<2>(lh, (unsigned)grid, L.smem, st, P); break;
-            case 3: r = lat_launch_w<3>(lh, (unsigned)grid, L.smem, st, P); break;
-            case 4: r = lat_launch_w<4>(lh, (unsigned)grid, L.smem, st, P); break;
-            case 5: r = lat_launch_w<5>(lh, (unsigned)grid, L.smem, st, P); break;
-            default: r = lat_launch_w<6>(lh, (unsigned)grid, L.smem, st, P); break;
+            int budget = LAT_BUDGET;
+            {
+                LatTune &T = g_tune[dev];
+                std::lock_guard<std::mutex> lk(T.mu);
+                if (T.budget[n_modes][c]) {
+                    budget = T.budget[n_modes][c];
+                } else if (g_tune_on && n >= LAT_TUNE_MIN_CUS) {
+                    int best = LAT_BUDGET;
+                    int r = lat_tune_shape(lw, lh, n, P, st, &launches, &best);
+                    if (r) return r;
+                    T.budget[n_modes][c] = budget = best;
+                    continue;   // the tuning runs wrote this shape's records
+                }
             }
+            LatLayout L;
+            lat_layout(lw, lh, n_modes, budget, L);
+            P.budget = budget;
+            const long long grid = (long long)((n + L.G - 1) / L.G) * L.nchunk;
+            int r = lat_launch(lw, lh, (unsigned)grid, L.smem, st, P);
             if (r) return r;
             launches++;
         }
@@ -193,6 +267,20 @@ static_assert(sizeof(LatCu) == sizeof(uavs3e_cuda_cu_t), "cu record layout");
 static_assert(sizeof(LatQ) == sizeof(uavs3e_cuda_lat_q_t), "lattice record layout");
 
 extern "C" {
+
+UAVS3E_CUDA_API void uavs3e_cuda_lattice_autotune(int on) { g_tune_on = on != 0; }
+
+UAVS3E_CUDA_API int uavs3e_cuda_lattice_budgets(int n_modes, int out[25])
+{
+    if (!out || n_modes < 1 || n_modes > 33) return set_status(UC_ERR_ARG, "lattice_budgets: bad argument");
+    int dev = 0;
+    UC_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "lattice_budgets: device index");
+    LatTune &T = g_tune[dev];
+    std::lock_guard<std::mutex> lk(T.mu);
+    for (int c = 0; c < 25; c++) out[c] = T.budget[n_modes][c];
+    return UC_OK;
+}
 
 UAVS3E_CUDA_API int uavs3e_cuda_lattice_cus(int width, int height, uavs3e_cuda_cu_t *out, int cap)
 {

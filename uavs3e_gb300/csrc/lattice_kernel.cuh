@@ -53,7 +53,7 @@ struct LatCu { s16 x, y; u8 w, h; u16 pad; };
 struct LatQ { u32 ssd; u32 coef_hash; u16 num_nz; s16 last_nz; u32 sum_abs; };
 
 constexpr int LAT_THREADS = 256;
-constexpr int LAT_BUDGET = 48 * 1024;   // dynamic shared bytes per CTA (4 CTAs per SM with the static part)
+constexpr int LAT_BUDGET = 48 * 1024;   // default dynamic shared bytes per CTA (4 CTAs per SM with the static part)
 constexpr int LAT_MAX_QP = 4;
 constexpr int LAT_SMEM_MAX = 96 * 1024;   // dynamic shared memory admitted by the kernel attribute
 constexpr int LAT_MAX_G = 8;            // CUs per CTA
@@ -82,7 +82,9 @@ struct LatLayout {
 
 __host__ __device__ __forceinline__ int lat_up16(int v) { return (v + 15) & ~15; }
 
-__host__ __device__ inline void lat_layout(int lw, int lh, int nm, LatLayout &L)
+// the layout of a CTA for (2^lw) x (2^lh) CUs and nm modes within `budget` bytes of dynamic
+// shared memory: how many CUs (or which chunk of one CU's modes) a CTA takes
+__host__ __device__ inline void lat_layout(int lw, int lh, int nm, int budget, LatLayout &L)
 {
     L.lw = lw; L.lh = lh; L.w = 1 << lw; L.h = 1 << lh;
     L.kw = L.w < 32 ? L.w : 32; L.kh = L.h < 32 ? L.h : 32;
@@ -114,7 +116,7 @@ __host__ __device__ inline void lat_layout(int lw, int lh, int nm, LatLayout &L)
     L.j_dqt = j; j += lat_up16(L.kw * L.ds * 2);
     L.j_t2 = j; j += lat_up16(L.h * L.t2s * 2);
     L.job_bytes = j;
-    const int avail = LAT_BUDGET - o;
+    const int avail = budget - o;
     // several whole CUs when nm jobs of the shape fit, else one CU and a chunk of its modes
     int G = avail / (nm * L.job_bytes + L.cu_bytes);
     if (G >= 1) {
@@ -146,6 +148,7 @@ struct LatParams {
     const u16 *scanpos;
     const u8 *modes;          // [CU][n_modes] modes to evaluate, or null for all 33 in order
     int n_modes;
+    int budget;               // dynamic shared bytes of the layout (lat_layout)
     double sq32, sq128;
 };
 
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     __shared__ int s_last[LAT_MAX_JOBS];
 
     LatLayout L;
-    lat_layout(LW, LH, P.n_modes, L);   // compile-time shape: the indices and trip counts below are constants
+    lat_layout(LW, LH, P.n_modes, P.budget, L);   // compile-time shape: the indices and trip counts below are constants
     const int w = L.w, h = L.h, lw = L.lw, lh = L.lh, kw = L.kw, kh = L.kh, lkw = L.lkw, lkh = L.lkh;
     const int N = w * h, lN = lw + lh;
     constexpr int W_ = 1 << LW, H_ = 1 << LH, KW_ = W_ < 32 ? W_ : 32, KH_ = H_ < 32 ? H_ : 32;
