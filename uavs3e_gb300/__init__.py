@@ -59,6 +59,7 @@ def _declare(L):
     L.uavs3e_cuda_lattice_autotune.restype = None
     L.uavs3e_cuda_lattice_budgets.argtypes = [I, P]
     L.uavs3e_cuda_intra_lattice_device.argtypes = [P, I, P, I, I, I, P, I, I, P, I, I, P, P, P]
+    L.uavs3e_cuda_intra_lattice_modes_device.argtypes = [P, I, P, I, I, I, P, I, P, I, I, P, I, I, P, P, P]
     L.uavs3e_cuda_profile_enable.argtypes = [I]
     L.uavs3e_cuda_launch_count.restype = C.c_ulonglong
     L.uavs3e_cuda_profile_collect.argtypes = [P, P, I]

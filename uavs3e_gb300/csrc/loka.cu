@@ -114,11 +114,65 @@ __device__ __forceinline__ u64 lk_cost(LkSearch &S, int mx, int my)
     return ((u64)sad << 16) + (u64)((lk_bits(mx) + lk_bits(my)) * S.lambda);
 }
 
-// search_diamond with bi = 0 (src/me.c:199-334) around the current MV; n_ring 28 for max_step 32,
-// 4 for max_step 8.  Returns the reference's best_step.
-__device__ int lk_diamond(LkSearch &S, int n_ring, int lane)
+// The reference rows every candidate of one diamond reads, staged in shared memory: rows
+// [wy0, wy1 + 15] and, per row, the words from the aligned start of column wx0 to the 5th word of
+// the last candidate (the span the global loads of lk_sad16 cover, nothing beyond it)
+struct LkWin {
+    const u32 *w;
+    int nw, wx0, wy0, sh0;
+};
+
+constexpr int LK_WIN_WORDS = 48 * 13;    // radius 16: 48 rows of (32 + 3) / 4 + 5 words
+
+__device__ __forceinline__ LkWin lk_stage(const LkSearch &S, int cx, int cy, int radius, u32 *buf, int lane)
+{
+    LkWin W;
+    W.wx0 = max(cx - radius, S.minx);
+    W.wy0 = max(cy - radius, S.miny);
+    const int wx1 = min(cx + radius, S.maxx), wy1 = min(cy + radius, S.maxy);
+    const uintptr_t base = (uintptr_t)(S.ref + W.wy0 * S.stride + W.wx0);
+    W.sh0 = (int)(base & 3);
+    W.nw = (wx1 - W.wx0 + W.sh0) / 4 + 5;
+    const int rows = wy1 - W.wy0 + 16;
+    const u32 *a0 = (const u32 *)(base & ~(uintptr_t)3);
+    const int ws = S.stride >> 2;
+    for (int i = lane; i < rows * W.nw; i += 32) {
+        const int r = i / W.nw, k = i - r * W.nw;
+        buf[i] = __ldg(a0 + r * ws + k);
+    }
+    __syncwarp();
+    W.w = buf;
+    return W;
+}
+
+// lk_cost with the SAD read from a staged window
+__device__ __forceinline__ u64 lk_cost_win(LkSearch &S, const LkWin &W, int mx, int my)
+{
+    S.evals++;
+    const int b = mx - W.wx0 + W.sh0;
+    const u32 *q = W.w + (my - W.wy0) * W.nw + (b >> 2);
+    const u32 sh = (u32)(b & 3) * 8;
+    u32 sad = 0;
+#pragma unroll 4
+    for (int r = 0; r < 16; r++, q += W.nw) {
+        const u32 w0 = q[0], w1 = q[1], w2 = q[2], w3 = q[3], w4 = q[4];
+        const uint4 o = *(const uint4 *)(S.so + r * 4);
+        sad = sad4(o.x, __funnelshift_r(w0, w1, sh), sad);
+        sad = sad4(o.y, __funnelshift_r(w1, w2, sh), sad);
+        sad = sad4(o.z, __funnelshift_r(w2, w3, sh), sad);
+        sad = sad4(o.w, __funnelshift_r(w3, w4, sh), sad);
+    }
+    return ((u64)sad << 16) + (u64)((lk_bits(mx) + lk_bits(my)) * S.lambda);
+}
+
+// search_diamond with bi = 0 (src/me.c:199-334) around the current MV; n_ring 28 for max_step 32
+// (candidates within 16 of the centre), 4 for max_step 8 (within 4).  Returns the reference's
+// best_step.
+__device__ int lk_diamond(LkSearch &S, int n_ring, u32 *buf, int lane)
 {
     const int cx = S.mvx, cy = S.mvy;
+    __syncwarp();                            // the previous stage's reads of buf are done
+    const LkWin W = lk_stage(S, cx, cy, n_ring > 4 ? 16 : 4, buf, lane);
     // core square with its edges strictly inside the MV range (src/me.c:240-243)
     const int x0 = max(cx - 2, S.minx + 1), x1 = min(cx + 2, S.maxx - 1);
     const int y0 = max(cy - 2, S.miny + 1), y1 = min(cy + 2, S.maxy - 1);
@@ -136,7 +190,7 @@ __device__ int lk_diamond(LkSearch &S, int n_ring, int lane)
             mx = cx + kRing[j][0]; my = cy + kRing[j][1];
             if (mx < S.minx || mx > S.maxx || my < S.miny || my > S.maxy) continue;
         }
-        const u64 key = (lk_cost(S, mx, my) << LK_LIST_BITS) | (u64)k;
+        const u64 key = (lk_cost_win(S, W, mx, my) << LK_LIST_BITS) | (u64)k;
         kmin = key < kmin ? key : kmin;
     }
     kmin = warp_min_u64(kmin);
@@ -307,6 +361,7 @@ __device__ __forceinline__ u32 lk_had16(const pel *o, const pel *p, int ip, int 
 __global__ void __launch_bounds__(32 * LK_WARPS) k_loka_search(const LokaParams P)
 {
     __shared__ __align__(16) u32 s_org[LK_WARPS][64];
+    __shared__ u32 s_win[LK_WARPS][LK_WIN_WORDS];
     __shared__ unsigned long long s_evals;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int u = blockIdx.x * LK_WARPS + warp;
@@ -336,10 +391,10 @@ __global__ void __launch_bounds__(32 * LK_WARPS) k_loka_search(const LokaParams 
         S.mvx = min(max(0, S.minx), S.maxx);
         S.mvy = min(max(0, S.miny), S.maxy);
         S.best = ~0ull;
-        const int best_step = lk_diamond(S, 28, lane);
+        const int best_step = lk_diamond(S, 28, s_win[warp], lane);
         if (S.mvx != 0 || S.mvy != 0) {
             if (best_step > 5) lk_raster(S, r, P.range[l][r], lane);
-            lk_diamond(S, 4, lane);
+            lk_diamond(S, 4, s_win[warp], lane);
         }
         const pel *blk = S.ref + S.mvy * P.i_ref + S.mvx;
         const u32 satd = lk_had16((const pel *)s_org[warp], blk, P.i_ref, lane);

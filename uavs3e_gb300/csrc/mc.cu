@@ -90,11 +90,22 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc_cu(const McParams P)
             const int px = min(max(qx >> 2, -128 - 4), P.W + 4), py = min(max(qy >> 2, -128 - 4), P.H + 4);
             src[k++] = P.planes[q.slot[l] * 16 + (qy & 3) * 4 + (qx & 3)] + (long long)py * P.i_ref + px;
         }
-        for (int i = lane; i < w * h; i += 32) {
-            const int j = i / w, c = i - j * w;
-            int v = src[0][j * P.i_ref + c];
-            if (k == 2) v = (v + src[1][j * P.i_ref + c] + 1) >> 1;
-            o[i] = (pel)v;
+        // 4 samples a lane: word loads from the (any-alignment) source rows, byte-wise rounded
+        // average of the two lists (pel_avrg), word stores where the output is 4-byte aligned
+        const int lq = 31 - __clz(w >> 2);           // log2 of the words per row
+        const bool aligned = ((uintptr_t)o & 3) == 0;
+        for (int i = lane; i < (w * h) >> 2; i += 32) {
+            const int j = i >> lq, c = (i - (j << lq)) << 2;
+            u32 v = 0;
+            for (int t = 0; t < k; t++) {
+                const uintptr_t a = (uintptr_t)(src[t] + j * P.i_ref + c);
+                const u32 *wp = (const u32 *)(a & ~(uintptr_t)3);
+                const u32 sv = __funnelshift_r(__ldg(wp), __ldg(wp + 1), (u32)(a & 3) * 8);
+                v = t ? __vavgu4(v, sv) : sv;
+            }
+            pel *d = o + (i << 2);
+            if (aligned) *(u32 *)d = v;
+            else { d[0] = (pel)v; d[1] = (pel)(v >> 8); d[2] = (pel)(v >> 16); d[3] = (pel)(v >> 24); }
         }
         o += w * h;
     }
@@ -109,8 +120,9 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc_cu(const McParams P)
                 dx[k] = qx & 7; dy[k] = qy & 7;
                 src[k++] = P.chroma[q.slot[l] * 2 + pl] + (long long)cy * P.i_c + cx;
             }
+            const int lwc = 31 - __clz(wc);
             for (int i = lane; i < wc * hc; i += 32) {
-                const int j = i / wc, c = i - j * wc;
+                const int j = i >> lwc, c = i - (j << lwc);
                 int v = mc_chroma_sample(src[0] + j * P.i_c + c, P.i_c, dx[0], dy[0]);
                 if (k == 2) v = (v + mc_chroma_sample(src[1] + j * P.i_c + c, P.i_c, dx[1], dy[1]) + 1) >> 1;
                 o[i] = (pel)v;
