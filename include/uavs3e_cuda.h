@@ -61,7 +61,7 @@ UAVS3E_CUDA_API const char *uavs3e_cuda_version(void);
  * batched kernels is bracketed by CUDA events on its stream.  collect() waits for them and
  * returns, per kernel id (0 pad, 1 frame interpolation, 2 integer search, 3 fractional
  * refinement, 4 intra lattice, 5 lookahead estimate, 6 TZ requests, 7 CU motion compensation,
- * 8 RDOQ), the summed milliseconds and launch counts,
+ * 8 RDOQ, 9 affine motion search), the summed milliseconds and launch counts,
  * then forgets them. */
 UAVS3E_CUDA_API void uavs3e_cuda_profile_enable(int on);
 /* Measured issue rate of the 4-sample SAD instruction (vabsdiff4 with accumulate) on the current
@@ -308,6 +308,64 @@ UAVS3E_CUDA_API int uavs3e_cuda_mc_affine_device(int width, int height, const ui
                                                  int i_ref, int pad, const uint8_t *const *d_chroma, int i_c,
                                                  int pad_c, const uavs3e_cuda_affine_req_t *d_reqs, int n,
                                                  uint8_t *d_out, size_t out_bytes, void *stream);
+
+/* ------------------------------------------------------------ affine motion search */
+
+/*
+ * affine_me_gradient (src/inter.c:1339-1470, file-local in the reference) for a list of
+ * independent calls: up to 7 (uni) / 5 (bi) gradient steps of the 4-parameter affine model from
+ * the start CPMVs, each step's CPMV change from the normal equations of the residual and the
+ * Sobel gradients of the prediction (affine_sobel_flt_hor / _ver, affine_coef_computer,
+ * solve_equal in double precision), rounded to the AMVR step, kept when SATD + MV cost drops.
+ * Flags add what the callers do around the call:
+ *   UAVS3E_CUDA_AFFME_UNI_START: the start CPMVs of analyze_affine_uni (:1607-1647), the cheaper
+ *     of the MVP and pi->best_mv_uni (req mv[0], quarter samples) clipped by mv_clip and scaled;
+ *   UAVS3E_CUDA_AFFME_BI: the org of analyze_affine_bi (:1730-1790), 2 org - the other list's
+ *     prediction (8x8 sub-blocks), the call with bi = 1 and 8x8 sub-blocks;
+ *   UAVS3E_CUDA_AFFME_SUB8: pichdr->affine_subblk_size_idx > 0 (8x8 sub-blocks in uni calls).
+ * Results equal the reference's: the CPMVs left in mv, the return value, and the callers' cost
+ * (return value + MV_COST of affine_mv_bits, + pi->mot_bits of the other list for bi).
+ * The reference asserts that mvp and the start CPMVs lie on the AMVR step's grid.
+ */
+#define UAVS3E_CUDA_AFFME_BI        1
+#define UAVS3E_CUDA_AFFME_UNI_START 2
+#define UAVS3E_CUDA_AFFME_SUB8      4
+
+typedef struct {
+    int16_t  x, y;            /* CU position (luma samples), CU inside the picture             */
+    uint8_t  w, h;            /* 16..64, powers of two                                         */
+    uint8_t  ref_slot;        /* planes of pi->ref_pic (only the integer plane is read)        */
+    int8_t   refi;            /* reference index, < num_refp (reference bits)                  */
+    uint8_t  num_refp;        /* pi->num_refp                                                  */
+    uint8_t  mvr;             /* pi->curr_mvr 0..2: CPMV step 1/4, 1, 1/16 sample              */
+    uint8_t  flags;           /* UAVS3E_CUDA_AFFME_*                                           */
+    uint8_t  other_slot;      /* bi: planes of the other list's reference                      */
+    uint32_t lambda_mv;       /* pi->lambda_mv                                                 */
+    int32_t  mot_bits_other;  /* bi: pi->mot_bits of the other list                            */
+    int32_t  pad;
+    int32_t  mvp[2][2];       /* affine MVP of the two control points, 1/16 samples            */
+    int32_t  mv[2][2];        /* start CPMVs; UNI_START: mv[0] = pi->best_mv_uni (1/4 samples) */
+    int32_t  other_mv[2][2];  /* bi: the other list's CPMVs                                    */
+} uavs3e_cuda_affme_req_t;
+
+typedef struct {
+    int32_t  mv[2][2];        /* the CPMVs the call leaves in mv                               */
+    uint32_t satd;            /* return value (com_had of the best prediction, >> bi)          */
+    int32_t  bits;            /* affine_mv_bits of the result (+ mot_bits_other for bi)        */
+    uint64_t cost;            /* satd + MV_COST(bits); UINT64_MAX for a request outside the    */
+                              /* supported domain (sides 16..64, CU inside the picture,        */
+                              /* CPMVs within 18 bits), mv = the start CPMVs                   */
+} uavs3e_cuda_affme_out_t;
+
+/* Requests against a motion-search session's references (slot = session slot), host buffers,
+ * synchronous: org is the current picture (row stride i_org). */
+UAVS3E_CUDA_API int uavs3e_cuda_me_affine(uavs3e_cuda_me *me, const uint8_t *org, int i_org,
+                                          const uavs3e_cuda_affme_req_t *reqs, int n, uavs3e_cuda_affme_out_t *out);
+/* Device form: d_planes as uavs3e_cuda_me_tz_device (n_slots * 16 pointers, padded by >= 144). */
+UAVS3E_CUDA_API int uavs3e_cuda_me_affine_device(int width, int height, const uint8_t *d_org, int i_org,
+                                                 const uint8_t *const *d_planes, int n_slots, int i_ref, int pad,
+                                                 const uavs3e_cuda_affme_req_t *d_reqs, int n,
+                                                 uavs3e_cuda_affme_out_t *d_out, void *stream);
 
 /* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
  * session's plane stride; for inspection by tests. */

@@ -1858,6 +1858,269 @@ void orc_mc_affine(int width, int height, const pel *const *planes, int i_ref, c
     }
 }
 
+/* ============================================================ affine motion search */
+
+#define CPMV_MIN (-131072)
+#define CPMV_MAX 131071
+
+/* Tab_Affine_AMVR (inc/com_define.h:203): CPMV step of the affine AMVR index */
+static int affme_shift(int mvr) { return mvr == 0 ? 2 : (mvr == 1 ? 4 : 0); }
+
+/* MV_COST (src/inter.c:41): unsigned 32-bit product, rounded */
+static u32 affme_mv_cost(u32 lambda_mv, int bits) { return (u32)(lambda_mv * (u32)bits + 32768u) >> 16; }
+
+/* affine_mv_bits (src/inter.c:1317-1337) */
+static int affme_bits(const s32 (*mv)[2], const s32 (*mvp)[2], int num_refp, int refi, int mvr)
+{
+    int bits = num_refp <= 1 ? 0 : MIN(refi + 1, num_refp - 1);     /* tbl_refi_bits, src/tables.c:52 */
+    const int sh = affme_shift(mvr);
+    for (int v = 0; v < 2; v++) {
+        int dx = ABSI((mv[v][0] - mvp[v][0]) >> sh), dy = ABSI((mv[v][1] - mvp[v][1]) >> sh);
+        bits += ((ilog2(dx + 1) + ilog2(dy + 1)) << 1) + 2 + !!dx + !!dy;
+    }
+    return bits;
+}
+
+/* com_mc_blk_affine_luma (src/com_mc.c:202-250): two control points, sub x sub blocks, each
+ * filtered from the integer plane at its 1/16-sample MV */
+static void affme_pred(int W, int H, int x, int y, int cw, int ch, const s32 (*ac)[2], int sub, const pel *plane,
+                       int i_ref, pel *pred)
+{
+    const int lw = ilog2(cw), half = sub >> 1;
+    const s32 dhx = ((ac[1][0] - ac[0][0]) * 128) >> lw, dhy = ((ac[1][1] - ac[0][1]) * 128) >> lw;
+    const s32 dvx = -dhy, dvy = dhx;
+    for (int h = 0; h < ch; h += sub)
+        for (int w = 0; w < cw; w += sub) {
+            int px = w + half, py = h + half;
+            if (w == 0 && h == 0) { px = 0; py = 0; }
+            else if (w + sub == cw && h == 0) { px = cw; py = 0; }
+            s32 mx = CLIP3(CPMV_MIN, CPMV_MAX, affine_round7(ac[0][0] * 128 + dhx * px + dvx * py));
+            s32 my = CLIP3(CPMV_MIN, CPMV_MAX, affine_round7(ac[0][1] * 128 + dhy * px + dvy * py));
+            affine_luma_blk(plane, i_ref, pred + h * cw + w, cw, ((x + w) << 4) + mx, ((y + h) << 4) + my, sub, sub,
+                            W + 4, H + 4);
+        }
+}
+
+/* (s16) of a double the way x86-64 code converts it (cvttsd2si to 32 bits, then the low 16
+ * bits): NaN and values outside the 32-bit range become INT_MIN, whose low half is 0 */
+static s16 affme_to_s16(double v)
+{
+    int i = (v > -2147483649.0 && v < 2147483648.0) ? (int)v : (int)0x80000000u;
+    return (s16)i;
+}
+
+/* solve_equal (src/inter.c:1280-1315): Gaussian elimination with partial pivoting over the
+ * rows 1..order of a (row 0 is the swap buffer), then back substitution.  Bit-exact doubles
+ * need the reference's operation order, which this follows term by term. */
+static void affme_solve(double (*a)[5], int order, double *x)
+{
+    for (int i = 1; i < order; i++) {
+        double best = fabs(a[i][i - 1]);
+        int bi = i;
+        for (int j = i + 1; j < order + 1; j++)
+            if (fabs(a[j][i - 1]) > best) { best = fabs(a[j][i - 1]); bi = j; }
+        if (bi != i)
+            for (int j = 0; j < order + 1; j++) { a[0][j] = a[i][j]; a[i][j] = a[bi][j]; a[bi][j] = a[0][j]; }
+        for (int j = i + 1; j < order + 1; j++)
+            for (int k = i; k < order + 1; k++) {
+                double t = a[i][k] * a[j][i - 1];
+                t = t / a[i][i - 1];
+                a[j][k] = a[j][k] - t;
+            }
+    }
+    x[order - 1] = a[order][order] / a[order][order - 1];
+    for (int i = order - 2; i >= 0; i--) {
+        double t = 0;
+        for (int j = i + 1; j < order; j++) {
+            double m = a[i + 1][j] * x[j];
+            t = t + m;
+        }
+        x[i] = (a[i + 1][order] - t) / a[i + 1][i];
+    }
+}
+
+/* the normal equations of one gradient step: residual, Sobel gradients of the prediction
+ * (affine_sobel_flt_hor / _ver, src/com_util.c:2966-3018: interior 3x3 Sobel, border samples
+ * copy their nearest interior neighbour) and their products (affine_coef_computer, :3020) */
+static void affme_equations(const pel *org, int i_org, const pel *pred, int w, int h, s64 (*coef)[5])
+{
+    memset(coef, 0, sizeof(s64) * 25);
+    for (int j = 0; j < h; j++)
+        for (int k = 0; k < w; k++) {
+            const int jj = CLIP3(1, h - 2, j), kk = CLIP3(1, w - 2, k);
+            const pel *p = pred + jj * w + kk;
+            const int gx = p[1 - w] - p[-1 - w] + 2 * p[1] - 2 * p[-1] + p[1 + w] - p[-1 + w];
+            const int gy = p[w - 1] - p[-w - 1] + 2 * p[w] - 2 * p[-w] + p[w + 1] - p[-w + 1];
+            const int resi = org[j * i_org + k] - pred[j * w + k];
+            const int c[4] = { gx, k * gx + j * gy, gy, j * gx - k * gy };
+            for (int col = 0; col < 4; col++) {
+                for (int row = 0; row < 4; row++) coef[col + 1][row] += (s64)c[col] * c[row];
+                coef[col + 1][4] += (s64)c[col] * resi * 8;
+            }
+        }
+}
+
+typedef struct {
+    int W, H, x, y, w, h, sub, bi, mvr, num_refp, refi, other_bits;
+    u32 lambda;
+    const pel *org, *plane;
+    int i_org, i_ref;
+} affme_ctx_t;
+
+static u64 affme_cost(const affme_ctx_t *c, const s32 (*mv)[2], const s32 (*mvp)[2], pel *pred, int *bits)
+{
+    affme_pred(c->W, c->H, c->x, c->y, c->w, c->h, mv, c->sub, c->plane, c->i_ref, pred);
+    *bits = affme_bits(mv, mvp, c->num_refp, c->refi, c->mvr) + (c->bi ? c->other_bits : 0);
+    return (u64)affme_mv_cost(c->lambda, *bits) + (orc_had(c->w, c->h, c->org, c->i_org, pred, c->w, 8) >> c->bi);
+}
+
+/* affine_me_gradient (src/inter.c:1339-1470): up to 7 (uni) / 5 (bi) Gauss-Newton steps on the
+ * 4-parameter model; each step's CPMV change rounded to the AMVR step, kept only when the
+ * SATD + MV cost drops.  mv in/out; returns the SATD part of the best cost. */
+static u64 affme_gradient(const affme_ctx_t *c, const s32 (*mvp)[2], s32 (*mv)[2], int *best_bits_out)
+{
+    pel pred[64 * 64];
+    s32 mvt[2][2] = { { mv[0][0], mv[0][1] }, { mv[1][0], mv[1][1] } };
+    int best_bits, bits;
+    u64 best = affme_cost(c, (const s32 (*)[2])mvt, mvp, pred, &best_bits);
+    const int sh = affme_shift(c->mvr);
+    for (int iter = 0; iter < (c->bi ? 5 : 7); iter++) {
+        s64 coef[5][5];
+        double a[5][5], para[4], d[4];
+        affme_equations(c->org, c->i_org, pred, c->w, c->h, coef);
+        for (int r = 0; r < 5; r++)
+            for (int k = 0; k < 5; k++) a[r][k] = (double)coef[r][k];
+        affme_solve(a, 4, para);
+        d[0] = para[0];
+        d[2] = para[2];
+        d[1] = para[1] * c->w + para[0];
+        d[3] = -para[3] * c->w + para[2];
+        s16 mvd[4];                        /* x0, y0, x1, y1 */
+        const int order[4] = { 0, 2, 1, 3 };
+        for (int v = 0; v < 4; v++) {
+            const double dv = d[order[v]];
+            if (sh == 0) mvd[v] = affme_to_s16(dv * 16 + (dv >= 0 ? 0.5 : -0.5));
+            else {
+                mvd[v] = affme_to_s16(dv * 4 + (dv >= 0 ? 0.5 : -0.5));
+                mvd[v] = (s16)(mvd[v] << 2);
+                mvd[v] = (s16)(((mvd[v] + (1 << (sh - 1))) >> sh) << sh);   /* com_mv_rounding_s16 */
+            }
+        }
+        if (!mvd[0] && !mvd[1] && !mvd[2] && !mvd[3]) break;
+        for (int v = 0; v < 2; v++)
+            for (int k = 0; k < 2; k++) {
+                s32 m = CLIP3(CPMV_MIN, CPMV_MAX, mvt[v][k] + mvd[v * 2 + k]);
+                if (m == CPMV_MAX) m = m >> sh << sh;
+                mvt[v][k] = m;
+            }
+        u64 cost = affme_cost(c, (const s32 (*)[2])mvt, mvp, pred, &bits);
+        if (cost < best) {
+            best = cost;
+            best_bits = bits;
+            memcpy(mv, mvt, sizeof(mvt));
+        }
+    }
+    *best_bits_out = best_bits;
+    return best - affme_mv_cost(c->lambda, best_bits);
+}
+
+/* the start CPMVs of analyze_affine_uni (src/inter.c:1607-1647): the better (SATD + MV cost) of
+ * the MVP and the uni-prediction MV clipped as mv_clip does (:1472), scaled to 1/16 samples and,
+ * at AMVR index 1, rounded to whole samples */
+static void affme_uni_start(const affme_ctx_t *c, const s32 (*mvp)[2], s32 um_x, s32 um_y, s32 (*start)[2])
+{
+    pel pred[64 * 64];
+    int bits;
+    const u64 c_mvp = affme_cost(c, mvp, mvp, pred, &bits);
+    const int x = c->x << 2, y = c->y << 2, w = c->w << 2, h = c->h << 2;
+    const int min_x = (-128 - 4) << 2, min_y = (-128 - 4) << 2;
+    const int max_x = (c->W - 1 + 128 + 4) << 2, max_y = (c->H - 1 + 128 + 4) << 2;
+    s16 mx = (s16)um_x, my = (s16)um_y;
+    if (x + mx < min_x) mx = (s16)(min_x - x);
+    if (y + my < min_y) my = (s16)(min_y - y);
+    if (x + mx + w - 4 > max_x) mx = (s16)(max_x - x - w + 4);
+    if (y + my + h - 4 > max_y) my = (s16)(max_y - y - h + 4);
+    s32 tx = (s32)mx << 2, ty = (s32)my << 2;
+    if (c->mvr == 1) {
+        tx = tx >= 0 ? ((tx + 8) >> 4) << 4 : -(((-tx + 8) >> 4) << 4);
+        ty = ty >= 0 ? ((ty + 8) >> 4) << 4 : -(((-ty + 8) >> 4) << 4);
+    }
+    tx = CLIP3(CPMV_MIN, CPMV_MAX, tx);
+    ty = CLIP3(CPMV_MIN, CPMV_MAX, ty);
+    const s32 tmp[2][2] = { { tx, ty }, { tx, ty } };
+    const u64 c_tmp = affme_cost(c, tmp, mvp, pred, &bits);
+    memcpy(start, c_tmp < c_mvp ? tmp : mvp, sizeof(tmp));
+}
+
+static void affme_one(int W, int H, const pel *org, int i_org, const pel *const *planes, int i_ref,
+                      const orc_affme_req_t *r, orc_affme_out_t *o)
+{
+    pel org_bi[64 * 64];
+    affme_ctx_t c;
+    c.W = W; c.H = H; c.x = r->x; c.y = r->y; c.w = r->w; c.h = r->h;
+    c.bi = r->flags & ORC_AFFME_BI;
+    c.sub = (c.bi || (r->flags & ORC_AFFME_SUB8)) ? 8 : 4;
+    c.mvr = r->mvr; c.num_refp = r->num_refp; c.refi = r->refi; c.other_bits = r->mot_bits_other;
+    c.lambda = r->lambda_mv;
+    c.plane = planes[r->ref_slot * 16];
+    c.i_ref = i_ref;
+    c.org = org + r->y * i_org + r->x;
+    c.i_org = i_org;
+    if (c.bi) {                           /* create_bi_org (src/inter.c:55) over an 8x8 prediction */
+        pel pred[64 * 64];
+        affme_pred(W, H, r->x, r->y, r->w, r->h, r->other_mv, 8, planes[r->other_slot * 16], i_ref, pred);
+        for (int j = 0; j < r->h; j++)
+            for (int i = 0; i < r->w; i++)
+                org_bi[j * r->w + i] = (pel)CLIP3(0, 255, (c.org[j * i_org + i] << 1) - pred[j * r->w + i]);
+        c.org = org_bi;
+        c.i_org = r->w;
+    }
+    s32 mv[2][2];
+    if (!c.bi && (r->flags & ORC_AFFME_UNI_START)) affme_uni_start(&c, r->mvp, r->mv[0][0], r->mv[0][1], mv);
+    else memcpy(mv, r->mv, sizeof(mv));
+    int bits;
+    const u64 satd = affme_gradient(&c, r->mvp, mv, &bits);
+    memcpy(o->mv, mv, sizeof(mv));
+    o->satd = (u32)satd;
+    o->bits = bits;
+    o->cost = satd + affme_mv_cost(c.lambda, bits);
+}
+
+static int affme_valid(int W, int H, const orc_affme_req_t *r)
+{
+    const int w = r->w, h = r->h;
+    if ((w != 16 && w != 32 && w != 64) || (h != 16 && h != 32 && h != 64)) return 0;
+    if (r->x < 0 || r->y < 0 || r->x + w > W || r->y + h > H || r->mvr > 2 || r->refi < 0 || r->refi >= r->num_refp)
+        return 0;
+    for (int v = 0; v < 2; v++)
+        for (int k = 0; k < 2; k++) {
+            if (r->mvp[v][k] < CPMV_MIN || r->mvp[v][k] > CPMV_MAX) return 0;
+            if (!(r->flags & ORC_AFFME_UNI_START) && (r->mv[v][k] < CPMV_MIN || r->mv[v][k] > CPMV_MAX)) return 0;
+            if ((r->flags & ORC_AFFME_BI) && (r->other_mv[v][k] < CPMV_MIN || r->other_mv[v][k] > CPMV_MAX)) return 0;
+        }
+    return 1;
+}
+
+void orc_me_affine(int width, int height, const pel *org, int i_org, const pel *const *planes, int i_ref,
+                   const orc_affme_req_t *reqs, int n, orc_affme_out_t *out, int threads)
+{
+    orc_init();
+#ifdef _OPENMP
+    if (threads < 1) threads = 1;
+    #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+#endif
+    for (int i = 0; i < n; i++) {
+        if (affme_valid(width, height, &reqs[i])) affme_one(width, height, org, i_org, planes, i_ref, &reqs[i], &out[i]);
+        else {
+            memcpy(out[i].mv, reqs[i].mv, sizeof(out[i].mv));
+            out[i].satd = 0;
+            out[i].bits = 0;
+            out[i].cost = ~0ull;
+        }
+    }
+    (void)threads;
+}
+
 /* ============================================================ RDOQ of a transform block */
 
 /* rdoq_one_coef (src/quant.c:158-194): the cheaper of keeping the coefficient at its level, one

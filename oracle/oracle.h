@@ -275,6 +275,41 @@ void orc_mc_cu(int width, int height, const pel *const *planes, int i_ref, const
 void orc_me_tz(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *const *planes, int i_ref,
                const orc_tz_req_t *reqs, int n, orc_tz_out_t *out, int threads);
 
+/* ------------- affine motion search (affine_me_gradient, src/inter.c:1339-1470) ------------- */
+
+#define ORC_AFFME_BI        1   /* bi argument: org = 2 org - the other list's prediction (8x8 sub-blocks) */
+#define ORC_AFFME_UNI_START 2   /* start CPMVs chosen as analyze_affine_uni does (src/inter.c:1607-1647)  */
+#define ORC_AFFME_SUB8      4   /* affine_subblk_size_idx > 0: 8x8 sub-blocks in uni calls                */
+
+typedef struct {
+    s16 x, y;           /* CU position (luma samples), CU inside the picture                        */
+    u8  w, h;           /* 16..64, powers of two                                                    */
+    u8  ref_slot;       /* integer plane planes[ref_slot * 16] of pi->ref_pic                       */
+    s8  refi;           /* reference index (reference bits), < num_refp                            */
+    u8  num_refp;       /* pi->num_refp                                                             */
+    u8  mvr;            /* pi->curr_mvr 0..2: CPMV step 1/4, 1, 1/16 sample (Tab_Affine_AMVR)       */
+    u8  flags;          /* ORC_AFFME_*                                                              */
+    u8  other_slot;     /* bi: integer plane of the other list's reference                          */
+    u32 lambda_mv;      /* pi->lambda_mv                                                            */
+    s32 mot_bits_other; /* bi: pi->mot_bits of the other list                                       */
+    s32 pad;
+    s32 mvp[2][2];      /* affine MVP of the two control points, 1/16 samples                      */
+    s32 mv[2][2];       /* start CPMVs; with ORC_AFFME_UNI_START mv[0] is pi->best_mv_uni (1/4)     */
+    s32 other_mv[2][2]; /* bi: the other list's CPMVs                                               */
+} orc_affme_req_t;
+
+typedef struct {
+    s32 mv[2][2];       /* the CPMVs the call leaves in mv                                          */
+    u32 satd;           /* affine_me_gradient's return value (com_had of the best, >> bi)          */
+    s32 bits;           /* affine_mv_bits of the result (+ mot_bits_other for bi)                   */
+    u64 cost;           /* satd + MV_COST(bits); UINT64_MAX for a request outside the domain        */
+} orc_affme_out_t;
+
+/* planes[slot * 16]: integer luma planes padded by >= 144 (stride i_ref); OpenMP over requests
+ * when threads > 1 */
+void orc_me_affine(int width, int height, const pel *org, int i_org, const pel *const *planes, int i_ref,
+                   const orc_affme_req_t *reqs, int n, orc_affme_out_t *out, int threads);
+
 /* the picture-level results from the records (src/lookahead.c:255-292): returns the picture
  * SATD cost; icost, icost_uv[2], map_dqp[units] are filled when non-NULL */
 double orc_loka_finish(const orc_loka_cfg_t *cfg, const orc_loka_unit_t *units, double *icost, double *icost_uv,

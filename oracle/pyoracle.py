@@ -223,6 +223,15 @@ class Oracle(_Common):
         self.L.orc_mc_affine(W, H, arr, i_ref, carr, i_c, ptr(reqs), len(reqs), ptr(out))
         return out[:out_bytes]
 
+    def me_affine(self, W, H, org, i_org, plane_ptrs, i_ref, reqs, threads=1):
+        """affine gradient searches (affine_me_gradient, with the uni start / bi org of its callers)
+        for every AFFME_REQ; plane_ptrs as me_tz (only each slot's integer plane is read)"""
+        arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFME_REQ)
+        out = np.zeros(len(reqs), dtype=AFFME_OUT)
+        self.L.orc_me_affine(W, H, ptr(org), i_org, arr, i_ref, ptr(reqs), len(reqs), ptr(out), threads)
+        return out
+
     def rdoq(self, reqs, ests, coefs):
         """quant_non_zero (flat) for every RDOQ_REQ; coefs (int16) is updated in place; returns num_nz"""
         reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
@@ -398,6 +407,17 @@ class RefLib(_Common):
                                   C.c_void_p(reqs.ctypes.data + i * AFFINE_REQ.itemsize), ptr(out))
         return out[:out_bytes]
 
+    def me_affine(self, W, H, org, i_org, plane_ptrs, i_ref, reqs, threads=1):
+        """the reference's affine_me_gradient, one call per request (same arguments as Oracle.me_affine)"""
+        arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFME_REQ)
+        out = np.zeros(len(reqs), dtype=AFFME_OUT)
+        for i in range(len(reqs)):
+            self.L.refk_affine_me(W, H, ptr(org), i_org, arr, i_ref,
+                                  C.c_void_p(reqs.ctypes.data + i * AFFME_REQ.itemsize),
+                                  C.c_void_p(out.ctypes.data + i * AFFME_OUT.itemsize))
+        return out
+
     def rdoq(self, reqs, ests, coefs):
         """quant_non_zero itself, one call per request (same arguments as Oracle.rdoq)"""
         reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
@@ -449,6 +469,12 @@ MC_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot"
                    ("mv", "<i2", (2, 2)), ("channel", "u1"), ("pad", "u1", (3,)), ("out_offset", "<u4")])
 AFFINE_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)), ("cp_num", "u1"),
                        ("sub8", "u1"), ("pad", "u1", (2,)), ("cpmv", "<i4", (2, 3, 2)), ("out_offset", "<u4")])
+AFFME_BI, AFFME_UNI_START, AFFME_SUB8 = 1, 2, 4
+AFFME_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("ref_slot", "u1"), ("refi", "i1"),
+                      ("num_refp", "u1"), ("mvr", "u1"), ("flags", "u1"), ("other_slot", "u1"), ("lambda_mv", "<u4"),
+                      ("mot_bits_other", "<i4"), ("pad", "<i4"), ("mvp", "<i4", (2, 2)), ("mv", "<i4", (2, 2)),
+                      ("other_mv", "<i4", (2, 2))])
+AFFME_OUT = np.dtype([("mv", "<i4", (2, 2)), ("satd", "<u4"), ("bits", "<i4"), ("cost", "<u8")])
 RDOQ_EST = np.dtype([("ctp", "<i4", (2,)), ("cbf", "<i4", (3, 2)), ("run", "<i4", (24, 2)), ("lvl", "<i4", (24, 2)),
                      ("lst", "<i4", (2, 6, 12, 2))])
 RDOQ_REQ = np.dtype([("coef_offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), ("qp", "u1"), ("is_intra", "u1"),

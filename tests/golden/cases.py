@@ -511,6 +511,88 @@ def run_affine(B, p, seed):
     return digest(B.mc_affine(p["w"], p["h"], addrs, stride, caddrs, sc, reqs, nbytes))
 
 
+# ------------------------------------------------------------------ affine motion search
+def affme_paint(rng, frames, W, H, n=6):
+    """flat, one-directional (stripe) and nearly one-directional patches at the same place in
+    every frame: blocks over them give singular or nearly singular normal equations"""
+    for _ in range(n):
+        s = int(rng.integers(24, 72))
+        y0, x0 = int(rng.integers(0, H - s)), int(rng.integers(0, W - s))
+        kind = int(rng.integers(4))
+        val = int(rng.integers(30, 220))
+        xx = np.arange(s)
+        speck = (rng.random((s, s)) < 0.004).astype(np.uint8)
+        for t in frames:
+            y = frames[t][0]
+            if kind == 0:
+                y[y0:y0 + s, x0:x0 + s] = val
+            elif kind == 1:
+                y[y0:y0 + s, x0:x0 + s] = np.clip(val + 40 * np.sin(xx / 3.0), 0, 255).astype(np.uint8)[None, :]
+            elif kind == 2:
+                y[y0:y0 + s, x0:x0 + s] = np.clip(val + 40 * np.sin(xx / 4.0), 0, 255).astype(np.uint8)[:, None]
+            else:                       # nearly one-directional: a stripe pattern with sparse specks
+                y[y0:y0 + s, x0:x0 + s] = np.clip(val + 40 * np.sin(xx / 5.0), 0, 254).astype(np.uint8)[None, :] + speck
+
+
+def affme_requests(rng, W, H, n, n_slots, bi_share=0.3):
+    """affine_me_gradient calls as analyze_affine_uni / _bi make them: CUs 16..64, AMVR index
+    0..2 with MVPs and start CPMVs on that step's grid, uni calls that pick their start from a
+    quarter-sample uni MV (some far outside the picture, so mv_clip acts), bi calls against the
+    other list's prediction, a few CPMVs at the 18-bit limits"""
+    import pyoracle
+    r = np.zeros(n, dtype=pyoracle.AFFME_REQ)
+    for i in range(n):
+        w, h = (16, 32, 64)[int(rng.integers(3))], (16, 32, 64)[int(rng.integers(3))]
+        mvr = int(rng.integers(0, 3))
+        unit = 1 << (2, 4, 0)[mvr]
+        q = int(rng.integers(22, 46))
+        r[i]["x"] = int(rng.integers(0, (W - w) // 8 + 1)) * 8
+        r[i]["y"] = int(rng.integers(0, (H - h) // 8 + 1)) * 8
+        r[i]["w"], r[i]["h"] = w, h
+        r[i]["ref_slot"] = int(rng.integers(0, n_slots))
+        r[i]["num_refp"] = int(rng.integers(1, 5))
+        r[i]["refi"] = int(rng.integers(0, r[i]["num_refp"]))
+        r[i]["mvr"] = mvr
+        bi = rng.random() < bi_share
+        r[i]["flags"] = (pyoracle.AFFME_BI if bi else (pyoracle.AFFME_UNI_START if rng.random() < 0.6 else 0)) | \
+            (pyoracle.AFFME_SUB8 if rng.random() < 0.3 else 0)
+        r[i]["other_slot"] = int(rng.integers(0, n_slots))
+        r[i]["lambda_mv"] = int(np.floor(65536.0 * np.sqrt(1.43631 * 2.0 ** ((q - 16) / 4.0))))
+        r[i]["mot_bits_other"] = int(rng.integers(2, 24))
+        t = rng.integers(-700, 701, 2)
+        if rng.random() < 0.05:
+            t = np.array([131071 - int(rng.integers(0, 64)), -131072 + int(rng.integers(0, 64))])[rng.permutation(2)]
+        a = rng.uniform(-0.06, 0.06, 2)
+        mvp = np.array([t, t + np.rint(16 * w * a).astype(int)])
+        r[i]["mvp"] = np.clip((mvp // unit) * unit, -131072, 131071 // unit * unit)
+        start = r[i]["mvp"] + (rng.integers(-64, 65, (2, 2)) // unit) * unit
+        r[i]["mv"] = np.clip(start, -131072, 131071 // unit * unit)
+        if r[i]["flags"] & pyoracle.AFFME_UNI_START:
+            um = rng.integers(-300, 301, 2) if rng.random() < 0.85 else rng.integers(-2500, 2501, 2)
+            r[i]["mv"] = 0
+            r[i]["mv"][0] = um
+        ot = rng.integers(-500, 501, 2)
+        r[i]["other_mv"] = [ot, ot + rng.integers(-40, 41, 2)]
+    return r
+
+
+def affme_inputs(B, p, seed):
+    rng = np.random.default_rng(seed)
+    W, H = p["w"], p["h"]
+    frames = loka_frames(rng, W, H, [0, 4, 8], p["vel"])
+    if p.get("paint"):
+        affme_paint(rng, frames, W, H)
+    keep, addrs, stride = tz_planes(B, frames, [4, 0], W, H)
+    reqs = affme_requests(rng, W, H, p["n"], 2)
+    return frames[8][0], keep, addrs, stride, reqs
+
+
+def run_affme(B, p, seed):
+    org, keep, addrs, stride, reqs = affme_inputs(B, p, seed)
+    out = B.me_affine(p["w"], p["h"], org, p["w"], addrs, stride, reqs)
+    return digest(out.view(np.uint8))
+
+
 # ------------------------------------------------------------------ RDOQ of transform blocks
 RDOQ_SIZES = [(2, 2), (3, 3), (4, 4), (5, 5), (6, 6), (2, 3), (3, 2), (2, 4), (4, 2), (3, 4), (4, 3), (3, 5), (5, 3),
               (4, 5), (5, 4), (4, 6), (6, 4), (5, 6), (6, 5), (3, 6), (6, 3)]
@@ -563,7 +645,7 @@ RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "rdoq": run_rdoq,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rdoq": run_rdoq,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -578,6 +660,12 @@ TZ_CASES = [
 MC_CASES = [
     dict(w=192, h=128, vel=(2.5, -1.25), n=160),
     dict(w=96, h=64, vel=(-6.0, 3.5), n=96),
+]
+
+# affine motion search cases: panning content, and the same with flat and stripe patches
+AFFME_CASES = [
+    dict(w=192, h=128, vel=(2.5, -1.25), n=96),
+    dict(w=160, h=96, vel=(-3.0, 2.0), n=96, paint=1),
 ]
 
 # RDOQ cases (transform blocks of every shape, several estimate sets)
@@ -662,6 +750,8 @@ def all_cases():
         add("affine", **p)
     for p in RDOQ_CASES:
         add("rdoq", **p)
+    for p in AFFME_CASES:
+        add("affme", **p)
     return cases
 
 

@@ -79,6 +79,8 @@ def _declare(L):
     L.uavs3e_cuda_mc_affine.argtypes = [P, P, I, P, C.c_size_t]
     L.uavs3e_cuda_mc_affine_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_rdoq.argtypes = [P, I, P, I, P, C.c_size_t, P]
+    L.uavs3e_cuda_me_affine.argtypes = [P, P, I, P, I, P]
+    L.uavs3e_cuda_me_affine_device.argtypes = [I, I, P, I, P, I, I, I, P, I, P, P]
     L.uavs3e_cuda_rdoq_device.argtypes = [P, I, P, I, P, C.c_size_t, P, P]
 
 
@@ -95,7 +97,7 @@ def init(device=0):
     check(lib().uavs3e_cuda_init(device), "uavs3e_cuda_init")
 
 
-PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz", "mc", "rdoq")
+PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz", "mc", "rdoq", "affme")
 
 CU = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
@@ -345,6 +347,15 @@ class MotionSearch:
                                       len(reqs), out.ctypes.data), "me_tz")
         return out[:len(reqs)]
 
+    def affine(self, org, reqs):
+        """affine_me_gradient calls (AFFME_REQ array) against the session's references; returns
+        AFFME_OUT"""
+        org = np.ascontiguousarray(org, dtype=np.uint8)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFME_REQ)
+        out = np.zeros(max(1, len(reqs)), dtype=AFFME_OUT)
+        check(lib().uavs3e_cuda_me_affine(self.h, org.ctypes.data, org.strides[0], reqs.ctypes.data, len(reqs),
+                                          out.ctypes.data), "me_affine")
+        return out[:len(reqs)]
 
     def set_ref_chroma(self, slot, u, v):
         u = np.ascontiguousarray(u, dtype=np.uint8)
@@ -453,3 +464,23 @@ def me_tz_device(pic, d_org, i_org, d_planes, i_ref, pad, d_reqs, n, d_out, stre
         stream = torch.cuda.current_stream().cuda_stream
     check(lib().uavs3e_cuda_me_tz_device(p.ctypes.data, d_org, i_org, arr, len(d_planes) // 16, i_ref, pad, d_reqs,
                                          n, d_out, stream), "me_tz_device")
+
+
+# ------------------------------------------------------------------ affine motion search
+AFFME_BI, AFFME_UNI_START, AFFME_SUB8 = 1, 2, 4
+AFFME_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("ref_slot", "u1"), ("refi", "i1"),
+                      ("num_refp", "u1"), ("mvr", "u1"), ("flags", "u1"), ("other_slot", "u1"), ("lambda_mv", "<u4"),
+                      ("mot_bits_other", "<i4"), ("pad", "<i4"), ("mvp", "<i4", (2, 2)), ("mv", "<i4", (2, 2)),
+                      ("other_mv", "<i4", (2, 2))])
+AFFME_OUT = np.dtype([("mv", "<i4", (2, 2)), ("satd", "<u4"), ("bits", "<i4"), ("cost", "<u8")])
+
+
+def me_affine_device(width, height, d_org, i_org, d_planes, i_ref, pad, d_reqs, n, d_out, stream=None):
+    """device form of the affine search: d_planes = slot-major list of 16 device addresses per
+    reference (only each slot's integer plane is read)"""
+    arr = (C.c_void_p * len(d_planes))(*d_planes)
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_me_affine_device(width, height, d_org, i_org, arr, len(d_planes) // 16, i_ref, pad, d_reqs,
+                                             n, d_out, stream), "me_affine_device")

@@ -1,0 +1,370 @@
+// Affine motion search for lists of calls: affine_me_gradient (src/inter.c:1339-1470) -- up to 7
+// (uni) / 5 (bi) Gauss-Newton steps of the 4-parameter affine model, each from the normal
+// equations of the residual and the Sobel gradients of the current prediction, its CPMV change
+// rounded to the AMVR step and kept when the SATD + MV cost drops -- with the start CPMVs of
+// analyze_affine_uni (:1607-1647) or the bi org of analyze_affine_bi (:1730-1790) on request.
+// Bit-exact with the reference, including its double-precision solve.
+//
+// One warp per call.  The CU's org (or bi org) and the current prediction sit in shared memory;
+// the prediction (com_mc_blk_affine_luma, src/com_mc.c:202-250) is rebuilt there after every
+// step, the lanes walk its samples for the SATD tiles and the equation sums, which reduce across
+// the warp in 64-bit integers.  The 4x4 solve runs on lane 0 in IEEE double with every operation
+// rounded on its own (no fused multiply-add), in the reference's order.
+#include "common.cuh"
+#include "affine.cuh"
+#include "uavs3e_cuda_internal.h"
+#include "../../include/uavs3e_cuda.h"
+
+#include <math.h>
+#include <string.h>
+
+namespace uc {
+
+constexpr int AME_WARPS = 4;
+constexpr s32 CPMV_MIN = -131072, CPMV_MAX = 131071;
+
+struct AffMeReq {
+    s16 x, y; u8 w, h; u8 ref_slot; s8 refi; u8 num_refp; u8 mvr; u8 flags; u8 other_slot;
+    u32 lambda_mv; s32 mot_bits_other; s32 pad;
+    s32 mvp[2][2]; s32 mv[2][2]; s32 other_mv[2][2];
+};
+struct AffMeOut { s32 mv[2][2]; u32 satd; s32 bits; u64 cost; };
+static_assert(sizeof(AffMeReq) == sizeof(uavs3e_cuda_affme_req_t), "affine search request layout");
+static_assert(sizeof(AffMeOut) == sizeof(uavs3e_cuda_affme_out_t), "affine search result layout");
+
+struct AffMeParams {
+    const pel *planes[UAVS3E_CUDA_TZ_MAX_SLOTS];   // integer plane of each slot
+    const pel *org;
+    int i_org, i_ref, n_slots, W, H, n;
+    double sq32, sq128;
+    const AffMeReq *reqs;
+    AffMeOut *out;
+};
+
+// Tab_Affine_AMVR (inc/com_define.h:203)
+__device__ __forceinline__ int ame_shift(int mvr) { return mvr == 0 ? 2 : (mvr == 1 ? 4 : 0); }
+
+// MV_COST (src/inter.c:41): unsigned 32-bit product, rounded
+__device__ __forceinline__ u32 ame_mv_cost(u32 lambda, int bits) { return (lambda * (u32)bits + 32768u) >> 16; }
+
+__device__ __forceinline__ int ame_log2(int v) { return 31 - __clz(v); }
+
+// affine_mv_bits (src/inter.c:1317-1337), tbl_refi_bits (src/tables.c:52) in closed form
+__device__ __forceinline__ int ame_bits(const s32 *mv, const s32 *mvp, int num_refp, int refi, int sh)
+{
+    int bits = num_refp <= 1 ? 0 : min(refi + 1, num_refp - 1);
+#pragma unroll
+    for (int v = 0; v < 2; v++) {
+        const int dx = abs((mv[2 * v] - mvp[2 * v]) >> sh), dy = abs((mv[2 * v + 1] - mvp[2 * v + 1]) >> sh);
+        bits += ((ame_log2(dx + 1) + ame_log2(dy + 1)) << 1) + 2 + (dx != 0) + (dy != 0);
+    }
+    return bits;
+}
+
+// com_mc_blk_affine_luma (src/com_mc.c:202-250) into dst (w x h, stride w): each sample takes the
+// MV of its sub x sub block (centre, or the control point for the two top corner blocks), rounded
+// to 1/16 and clipped to 18 bits, and is filtered from the integer plane (com_mc_blk_luma, hp)
+__device__ void ame_pred(const AffMeParams &P, const pel *plane, int x, int y, int w, int h, int lw, const s32 *mv,
+                         int sub, pel *dst, int lane)
+{
+    const s32 dhx = ((mv[2] - mv[0]) * 128) >> lw, dhy = ((mv[3] - mv[1]) * 128) >> lw;
+    const s32 dvx = -dhy, dvy = dhx;
+    const int half = sub >> 1;
+    for (int i = lane; i < w * h; i += 32) {
+        const int j = i >> lw, c = i & (w - 1);
+        const int bx = c & ~(sub - 1), by = j & ~(sub - 1);
+        int px = bx + half, py = by + half;
+        if (bx == 0 && by == 0) { px = 0; py = 0; }
+        else if (bx + sub == w && by == 0) { px = w; py = 0; }
+        const s32 mx = min(max(aff_round7(mv[0] * 128 + dhx * px + dvx * py), CPMV_MIN), CPMV_MAX);
+        const s32 my = min(max(aff_round7(mv[1] * 128 + dhy * px + dvy * py), CPMV_MIN), CPMV_MAX);
+        const int qx = ((x + bx) << 4) + mx, qy = ((y + by) << 4) + my;
+        const int sx = min(max(qx >> 4, -128 - 4), P.W + 4), sy = min(max(qy >> 4, -128 - 4), P.H + 4);
+        const pel *s = plane + (long long)(sy + j - by) * P.i_ref + sx + c - bx;
+        dst[i] = (pel)aff_luma_sample(s, P.i_ref, qx & 15, qy & 15);
+    }
+}
+
+// com_had (src/com_cost.c:712-812) of the w x h block o - p (both stride w) with TW x TH tiles
+template <int TW, int TH>
+__device__ u32 ame_had_tiles(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128)
+{
+    const int ntx = w / TW, total = ntx * (h / TH) * TH;
+    u32 acc = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int t = base + lane;
+        const bool active = t < total;
+        const int tt = active ? t : 0, tile = tt / TH, row = tt - tile * TH;
+        const int off = ((tile / ntx) * TH + row) * w + (tile % ntx) * TW;
+        const u32 v = had_tile_rows<TW, TH>(o + off, w, p + off, w, active, lane, sq32, sq128);
+        if (active && row == 0) acc += v;
+    }
+#pragma unroll
+    for (int m = 16; m; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+    return acc;
+}
+
+__device__ __forceinline__ u32 ame_had(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128)
+{
+    if (w == h) return ame_had_tiles<8, 8>(o, p, w, h, lane, sq32, sq128);
+    if (w > h) return ame_had_tiles<16, 8>(o, p, w, h, lane, sq32, sq128);
+    return ame_had_tiles<8, 16>(o, p, w, h, lane, sq32, sq128);
+}
+
+// the sums of one gradient step (affine_sobel_flt_hor / _ver and affine_coef_computer,
+// src/com_util.c:2966-3045): per sample the Sobel gradients of the prediction at the nearest
+// interior position, the four model columns c0..c3 and the residual; e[0..9] = the products
+// c_i c_j (i <= j), e[10..13] = c_i * residual, summed over the block and the warp
+__device__ void ame_equations(const pel *o, const pel *p, int w, int h, int lw, int lane, s64 *e)
+{
+#pragma unroll
+    for (int i = 0; i < 14; i++) e[i] = 0;
+    for (int i = lane; i < w * h; i += 32) {
+        const int j = i >> lw, k = i & (w - 1);
+        const int jj = min(max(j, 1), h - 2), kk = min(max(k, 1), w - 2);
+        const pel *q = p + jj * w + kk;
+        const int gx = q[1 - w] - q[-1 - w] + 2 * (q[1] - q[-1]) + q[1 + w] - q[-1 + w];
+        const int gy = q[w - 1] - q[-w - 1] + 2 * (q[w] - q[-w]) + q[w + 1] - q[-w + 1];
+        const int r = (int)o[i] - (int)p[i];
+        const int c0 = gx, c1 = k * gx + j * gy, c2 = gy, c3 = j * gx - k * gy;
+        e[0] += (s64)c0 * c0; e[1] += (s64)c0 * c1; e[2] += (s64)c0 * c2; e[3] += (s64)c0 * c3;
+        e[4] += (s64)c1 * c1; e[5] += (s64)c1 * c2; e[6] += (s64)c1 * c3;
+        e[7] += (s64)c2 * c2; e[8] += (s64)c2 * c3; e[9] += (s64)c3 * c3;
+        e[10] += (s64)c0 * r; e[11] += (s64)c1 * r; e[12] += (s64)c2 * r; e[13] += (s64)c3 * r;
+    }
+#pragma unroll
+    for (int i = 0; i < 14; i++)
+#pragma unroll
+        for (int m = 16; m; m >>= 1) e[i] += __shfl_xor_sync(0xffffffffu, e[i], m);
+}
+
+// (s16) of a double as x86-64 code converts it (the reference's platform): truncation to 32 bits
+// by cvttsd2si -- NaN and values outside the 32-bit range give INT_MIN -- then the low 16 bits
+__device__ __forceinline__ s16 ame_to_s16(double v)
+{
+    const int i = (v > -2147483649.0 && v < 2147483648.0) ? __double2int_rz(v) : (int)0x80000000u;
+    return (s16)(u16)(u32)i;
+}
+
+// solve_equal (src/inter.c:1280-1315) on the rows 1..4 of a (row 0 is the swap buffer) and the
+// conversion of the solution to the four CPMV changes (x0, y0, x1, y1) at AMVR shift sh
+__device__ void ame_solve(double (*a)[5], int w, int sh, s16 *mvd)
+{
+    constexpr int order = 4;
+    double x[4];
+    for (int i = 1; i < order; i++) {
+        double best = fabs(a[i][i - 1]);
+        int bi = i;
+        for (int j = i + 1; j < order + 1; j++)
+            if (fabs(a[j][i - 1]) > best) { best = fabs(a[j][i - 1]); bi = j; }
+        if (bi != i)
+            for (int j = 0; j < order + 1; j++) { a[0][j] = a[i][j]; a[i][j] = a[bi][j]; a[bi][j] = a[0][j]; }
+        for (int j = i + 1; j < order + 1; j++)
+            for (int k = i; k < order + 1; k++)
+                a[j][k] = __dsub_rn(a[j][k], __ddiv_rn(__dmul_rn(a[i][k], a[j][i - 1]), a[i][i - 1]));
+    }
+    x[order - 1] = __ddiv_rn(a[order][order], a[order][order - 1]);
+    for (int i = order - 2; i >= 0; i--) {
+        double t = 0;
+        for (int j = i + 1; j < order; j++) t = __dadd_rn(t, __dmul_rn(a[i + 1][j], x[j]));
+        x[i] = __ddiv_rn(__dsub_rn(a[i + 1][order], t), a[i + 1][i]);
+    }
+    const double wd = (double)w;
+    const double d[4] = { x[0], x[2], __dadd_rn(__dmul_rn(x[1], wd), x[0]), __dadd_rn(__dmul_rn(-x[3], wd), x[2]) };
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+        const double half = d[v] >= 0 ? 0.5 : -0.5;
+        if (sh == 0) mvd[v] = ame_to_s16(__dadd_rn(__dmul_rn(d[v], 16.0), half));
+        else {
+            s16 m = ame_to_s16(__dadd_rn(__dmul_rn(d[v], 4.0), half));
+            m = (s16)(m << 2);
+            mvd[v] = (s16)(((m + (1 << (sh - 1))) >> sh) << sh);   // com_mv_rounding_s16
+        }
+    }
+}
+
+__device__ __forceinline__ bool ame_cpmv_ok(const s32 (*m)[2])
+{
+    return m[0][0] >= CPMV_MIN && m[0][0] <= CPMV_MAX && m[0][1] >= CPMV_MIN && m[0][1] <= CPMV_MAX &&
+           m[1][0] >= CPMV_MIN && m[1][0] <= CPMV_MAX && m[1][1] >= CPMV_MIN && m[1][1] <= CPMV_MAX;
+}
+
+__global__ void __launch_bounds__(32 * AME_WARPS) k_me_affine(const AffMeParams P)
+{
+    __shared__ __align__(16) pel s_org[AME_WARPS][64 * 64];
+    __shared__ __align__(16) pel s_pred[AME_WARPS][64 * 64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * AME_WARPS + warp;
+    if (r >= P.n) return;
+    const AffMeReq q = P.reqs[r];
+    AffMeOut *out = P.out + r;
+    const int w = q.w, h = q.h, bi = q.flags & UAVS3E_CUDA_AFFME_BI;
+    // calls outside the supported domain (CU inside the picture, sides 16..64, slots, AMVR index,
+    // reference index, CPMVs within 18 bits) return cost ~0 with the start CPMVs
+    if ((w != 16 && w != 32 && w != 64) || (h != 16 && h != 32 && h != 64) || q.x < 0 || q.y < 0 ||
+        q.x + w > P.W || q.y + h > P.H || q.ref_slot >= P.n_slots || (bi && q.other_slot >= P.n_slots) ||
+        q.mvr > 2 || q.refi < 0 || q.refi >= q.num_refp || !ame_cpmv_ok(q.mvp) ||
+        (!(q.flags & UAVS3E_CUDA_AFFME_UNI_START) && !ame_cpmv_ok(q.mv)) || (bi && !ame_cpmv_ok(q.other_mv))) {
+        if (lane == 0) {
+            for (int v = 0; v < 2; v++) { out->mv[v][0] = q.mv[v][0]; out->mv[v][1] = q.mv[v][1]; }
+            out->satd = 0;
+            out->bits = 0;
+            out->cost = ~0ull;
+        }
+        return;
+    }
+    pel *so = s_org[warp], *sp = s_pred[warp];
+    const int lw = 31 - __clz(w), n = w * h;
+    const pel *plane = P.planes[q.ref_slot];
+    const pel *org = P.org + (long long)q.y * P.i_org + q.x;
+    for (int i = lane; i < n; i += 32) so[i] = org[(i >> lw) * P.i_org + (i & (w - 1))];
+    if (bi) {                                      // create_bi_org (src/inter.c:55), 8x8 prediction
+        const s32 om[4] = { q.other_mv[0][0], q.other_mv[0][1], q.other_mv[1][0], q.other_mv[1][1] };
+        ame_pred(P, P.planes[q.other_slot], q.x, q.y, w, h, lw, om, 8, sp, lane);
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) so[i] = (pel)min(255, max(0, 2 * (int)so[i] - (int)sp[i]));
+    }
+    __syncwarp();
+    const int sh = ame_shift(q.mvr), sub = (bi || (q.flags & UAVS3E_CUDA_AFFME_SUB8)) ? 8 : 4;
+    const int other = bi ? q.mot_bits_other : 0;
+    const s32 mvp[4] = { q.mvp[0][0], q.mvp[0][1], q.mvp[1][0], q.mvp[1][1] };
+    s32 mv[4] = { q.mv[0][0], q.mv[0][1], q.mv[1][0], q.mv[1][1] };
+    bool have_pred = false;
+    u32 had = 0;
+    if (!bi && (q.flags & UAVS3E_CUDA_AFFME_UNI_START)) {
+        // analyze_affine_uni's start: the MVP, or the uni MV clipped (mv_clip, src/inter.c:1472) and
+        // scaled to 1/16 sample (rounded to whole samples at AMVR index 1), whichever costs less
+        ame_pred(P, plane, q.x, q.y, w, h, lw, mvp, sub, sp, lane);
+        __syncwarp();
+        const u64 c_mvp = (u64)ame_had(so, sp, w, h, lane, P.sq32, P.sq128) +
+                          ame_mv_cost(q.lambda_mv, ame_bits(mvp, mvp, q.num_refp, q.refi, sh));
+        const int x4 = q.x << 2, y4 = q.y << 2, w4 = w << 2, h4 = h << 2;
+        const int min_c = (-128 - 4) << 2, max_x = (P.W - 1 + 128 + 4) << 2, max_y = (P.H - 1 + 128 + 4) << 2;
+        s16 mx = (s16)q.mv[0][0], my = (s16)q.mv[0][1];
+        if (x4 + mx < min_c) mx = (s16)(min_c - x4);
+        if (y4 + my < min_c) my = (s16)(min_c - y4);
+        if (x4 + mx + w4 - 4 > max_x) mx = (s16)(max_x - x4 - w4 + 4);
+        if (y4 + my + h4 - 4 > max_y) my = (s16)(max_y - y4 - h4 + 4);
+        s32 tx = (s32)mx * 4, ty = (s32)my * 4;
+        if (q.mvr == 1) {
+            tx = tx >= 0 ? ((tx + 8) >> 4) << 4 : -(((-tx + 8) >> 4) << 4);
+            ty = ty >= 0 ? ((ty + 8) >> 4) << 4 : -(((-ty + 8) >> 4) << 4);
+        }
+        tx = min(max(tx, CPMV_MIN), CPMV_MAX);
+        ty = min(max(ty, CPMV_MIN), CPMV_MAX);
+        const s32 tmp[4] = { tx, ty, tx, ty };
+        __syncwarp();
+        ame_pred(P, plane, q.x, q.y, w, h, lw, tmp, sub, sp, lane);
+        __syncwarp();
+        const u32 had_tmp = ame_had(so, sp, w, h, lane, P.sq32, P.sq128);
+        const u64 c_tmp = (u64)had_tmp + ame_mv_cost(q.lambda_mv, ame_bits(tmp, mvp, q.num_refp, q.refi, sh));
+        if (c_tmp < c_mvp) {
+#pragma unroll
+            for (int v = 0; v < 4; v++) mv[v] = tmp[v];
+            have_pred = true;
+            had = had_tmp;
+        } else {
+#pragma unroll
+            for (int v = 0; v < 4; v++) mv[v] = mvp[v];
+        }
+    }
+    if (!have_pred) {
+        __syncwarp();
+        ame_pred(P, plane, q.x, q.y, w, h, lw, mv, sub, sp, lane);
+        __syncwarp();
+        had = ame_had(so, sp, w, h, lane, P.sq32, P.sq128);
+    }
+    // affine_me_gradient
+    int best_bits = ame_bits(mv, mvp, q.num_refp, q.refi, sh) + other;
+    u64 best = (u64)ame_mv_cost(q.lambda_mv, best_bits) + (had >> bi);
+    s32 mvt[4] = { mv[0], mv[1], mv[2], mv[3] };
+    for (int iter = 0; iter < (bi ? 5 : 7); iter++) {
+        s64 e[14];
+        ame_equations(so, sp, w, h, lw, lane, e);
+        u32 packed[2] = { 0, 0 };
+        if (lane == 0) {
+            const int ix[4][4] = { { 0, 1, 2, 3 }, { 1, 4, 5, 6 }, { 2, 5, 7, 8 }, { 3, 6, 8, 9 } };
+            double a[5][5];
+            for (int k = 0; k < 5; k++) a[0][k] = 0.0;
+            for (int c = 0; c < 4; c++) {
+                for (int k = 0; k < 4; k++) a[c + 1][k] = __ll2double_rn(e[ix[c][k]]);
+                a[c + 1][4] = __ll2double_rn(e[10 + c] * 8);
+            }
+            s16 mvd[4];
+            ame_solve(a, w, sh, mvd);
+            packed[0] = (u32)(u16)mvd[0] | ((u32)(u16)mvd[1] << 16);
+            packed[1] = (u32)(u16)mvd[2] | ((u32)(u16)mvd[3] << 16);
+        }
+        packed[0] = __shfl_sync(0xffffffffu, packed[0], 0);
+        packed[1] = __shfl_sync(0xffffffffu, packed[1], 0);
+        if (!packed[0] && !packed[1]) break;
+        const s16 mvd[4] = { (s16)(u16)packed[0], (s16)(u16)(packed[0] >> 16), (s16)(u16)packed[1],
+                             (s16)(u16)(packed[1] >> 16) };
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            s32 m = min(max(mvt[v] + (s32)mvd[v], CPMV_MIN), CPMV_MAX);
+            if (m == CPMV_MAX) m = m >> sh << sh;
+            mvt[v] = m;
+        }
+        __syncwarp();
+        ame_pred(P, plane, q.x, q.y, w, h, lw, mvt, sub, sp, lane);
+        __syncwarp();
+        const int bits = ame_bits(mvt, mvp, q.num_refp, q.refi, sh) + other;
+        const u64 cost = (u64)ame_mv_cost(q.lambda_mv, bits) + (ame_had(so, sp, w, h, lane, P.sq32, P.sq128) >> bi);
+        if (cost < best) {
+            best = cost;
+            best_bits = bits;
+#pragma unroll
+            for (int v = 0; v < 4; v++) mv[v] = mvt[v];
+        }
+    }
+    if (lane == 0) {
+        const u64 satd = best - ame_mv_cost(q.lambda_mv, best_bits);
+        for (int v = 0; v < 2; v++) { out->mv[v][0] = mv[2 * v]; out->mv[v][1] = mv[2 * v + 1]; }
+        out->satd = (u32)satd;
+        out->bits = best_bits;
+        out->cost = satd + ame_mv_cost(q.lambda_mv, best_bits);
+    }
+}
+
+int launch_me_affine(int W, int H, const pel *org, int i_org, const pel *const *planes, int n_slots, int i_ref,
+                     int pad, const void *reqs, int n, void *out, cudaStream_t st)
+{
+    if (!org || !planes || (n > 0 && (!reqs || !out)) || n < 0) return set_status(UC_ERR_ARG, "me_affine: null argument");
+    if (n_slots < 1 || n_slots > UAVS3E_CUDA_TZ_MAX_SLOTS || W < 16 || H < 16 || i_org < W)
+        return set_status(UC_ERR_ARG, "me_affine: slots / picture size / org stride");
+    // 8-tap windows reach 132 + 3 samples before the picture and W + 4 + 7 + 4 after it
+    if (pad < 144 || i_ref < W + 2 * pad) return set_status(UC_ERR_ARG, "me_affine: padding (>= 144) / stride");
+    if (n == 0) return UC_OK;
+    AffMeParams P;
+    memset(&P, 0, sizeof(P));
+    for (int s = 0; s < n_slots; s++) {
+        if (!planes[s * 16]) return set_status(UC_ERR_ARG, "me_affine: null plane");
+        P.planes[s] = planes[s * 16];
+    }
+    P.org = org; P.i_org = i_org; P.i_ref = i_ref; P.n_slots = n_slots; P.W = W; P.H = H; P.n = n;
+    P.sq32 = sqrt(32.0);
+    P.sq128 = sqrt(128.0);
+    P.reqs = (const AffMeReq *)reqs;
+    P.out = (AffMeOut *)out;
+    prof_begin(PROF_AFFME, st);
+    k_me_affine<<<(unsigned)((n + AME_WARPS - 1) / AME_WARPS), 32 * AME_WARPS, 0, st>>>(P);
+    UC_CHECK(cudaGetLastError());
+    count_launch(1);
+    prof_end(PROF_AFFME, st);
+    return UC_OK;
+}
+
+}  // namespace uc
+
+using namespace uc;
+
+UAVS3E_CUDA_API int uavs3e_cuda_me_affine_device(int width, int height, const uint8_t *d_org, int i_org,
+                                                 const uint8_t *const *d_planes, int n_slots, int i_ref, int pad,
+                                                 const uavs3e_cuda_affme_req_t *d_reqs, int n,
+                                                 uavs3e_cuda_affme_out_t *d_out, void *stream)
+{
+    if (ensure_init()) return uavs3e_cuda_status();
+    return launch_me_affine(width, height, d_org, i_org, d_planes, n_slots, i_ref, pad, d_reqs, n, d_out,
+                            (cudaStream_t)stream);
+}

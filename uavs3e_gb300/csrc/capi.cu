@@ -230,7 +230,7 @@ struct uavs3e_cuda_me {
     cudaStream_t st = nullptr;
     std::vector<u32> h_q2;
     std::vector<u16> h_r2m;
-    void *tz_buf = nullptr;           // TZ requests and results of host runs
+    void *tz_buf = nullptr;           // TZ / affine-search requests and results of host runs
     size_t tz_cap = 0;
     struct Graph {                    // captured frames (uavs3e_cuda_me_frame_graph)
         int slot, i_src, i_org;
@@ -497,6 +497,39 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_tz(uavs3e_cuda_me *m, const uavs3e_cuda_tz_pi
     UC_CHECK(cudaMemcpy2DAsync(m->org_buf, m->W, org, i_org, m->W, m->H, cudaMemcpyHostToDevice, m->st));
     UC_CHECK(cudaMemcpyAsync(d_req, reqs, (size_t)n * sizeof(*reqs), cudaMemcpyHostToDevice, m->st));
     int r = launch_me_tz(pic, m->org_buf, m->W, planes, slots, m->stride, m->pad, d_req, n, d_out, m->st);
+    if (r) return r;
+    UC_CHECK(cudaMemcpyAsync(out, d_out, (size_t)n * sizeof(*out), cudaMemcpyDeviceToHost, m->st));
+    UC_CHECK(cudaStreamSynchronize(m->st));
+    return UC_OK;
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_me_affine(uavs3e_cuda_me *m, const uint8_t *org, int i_org,
+                                          const uavs3e_cuda_affme_req_t *reqs, int n, uavs3e_cuda_affme_out_t *out)
+{
+    if (!m || !org || (n > 0 && (!reqs || !out)) || n < 0 || i_org < m->W)
+        return set_status(UC_ERR_ARG, "me_affine: bad argument");
+    if (ensure_init()) return uavs3e_cuda_status();
+    if (n == 0) return UC_OK;
+    const size_t need = (size_t)n * (sizeof(uavs3e_cuda_affme_req_t) + sizeof(uavs3e_cuda_affme_out_t));
+    if (m->tz_cap < need) {
+        if (m->tz_buf) UC_CHECK(cudaFree(m->tz_buf));
+        m->tz_buf = nullptr;
+        m->tz_cap = 0;
+        UC_CHECK(cudaMalloc(&m->tz_buf, need));
+        m->tz_cap = need;
+    }
+    uavs3e_cuda_affme_req_t *d_req = (uavs3e_cuda_affme_req_t *)m->tz_buf;
+    uavs3e_cuda_affme_out_t *d_out = (uavs3e_cuda_affme_out_t *)(d_req + n);
+    const pel *planes[UAVS3E_CUDA_TZ_MAX_SLOTS * 16];
+    const int slots = std::min(m->n_refs, UAVS3E_CUDA_TZ_MAX_SLOTS);
+    for (int s = 0; s < slots; s++)
+        for (int ph = 0; ph < 16; ph++) planes[s * 16 + ph] = me_plane_ptr(m, s, ph);
+    for (int i = 0; i < n; i++)
+        if (reqs[i].ref_slot >= slots || ((reqs[i].flags & UAVS3E_CUDA_AFFME_BI) && reqs[i].other_slot >= slots))
+            return set_status(UC_ERR_ARG, "me_affine: reference slot");
+    UC_CHECK(cudaMemcpy2DAsync(m->org_buf, m->W, org, i_org, m->W, m->H, cudaMemcpyHostToDevice, m->st));
+    UC_CHECK(cudaMemcpyAsync(d_req, reqs, (size_t)n * sizeof(*reqs), cudaMemcpyHostToDevice, m->st));
+    int r = launch_me_affine(m->W, m->H, m->org_buf, m->W, planes, slots, m->stride, m->pad, d_req, n, d_out, m->st);
     if (r) return r;
     UC_CHECK(cudaMemcpyAsync(out, d_out, (size_t)n * sizeof(*out), cudaMemcpyDeviceToHost, m->st));
     UC_CHECK(cudaStreamSynchronize(m->st));

@@ -171,4 +171,56 @@ __host__ __device__ __forceinline__ void had_tile_shape(int w, int h, int *tw, i
     else { if (w == 4 || (w & 7)) { *tw = 4; *th = 8; } else { *tw = 8; *th = 16; } }
 }
 
+// One pass of com_had tile rows over the warp: lanes in groups of TH hold one row each of a TW x TH
+// tile (row = lane % TH), rows transformed in registers, columns by butterflies across the group.
+// Tiles of 2:1 shape combine their two square halves as |a + b| + |a - b| = 2 max(|a|, |b|)
+// (com_had_16x8 / _8x16 / _8x4 / _4x8, src/com_cost.c:344-710).  Returns the tile's SATD in
+// every lane of the group (0 for inactive groups).
+template <int TW, int TH>
+__device__ __forceinline__ u32 had_tile_rows(const pel *o, int io, const pel *p, int ip, bool active, int lane,
+                                            double sq32, double sq128)
+{
+    constexpr bool WIDE = TW > TH, TALL = TW < TH;
+    constexpr int N = WIDE ? TW / 2 : TW;            // points of each row transform
+    constexpr int V = TALL ? TH / 2 : TH;            // points of the column transform
+    int a[N], b[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        a[i] = active ? (int)o[i] - (int)p[i] : 0;
+        b[i] = (WIDE && active) ? (int)o[N + i] - (int)p[N + i] : 0;
+    }
+    wht<N>(a);
+    if (WIDE) wht<N>(b);
+#pragma unroll
+    for (int m = 1; m < V; m <<= 1) {
+        const bool hi = lane & m;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const int pa = __shfl_xor_sync(0xffffffffu, a[i], m);
+            a[i] = hi ? pa - a[i] : a[i] + pa;
+            if (WIDE) {
+                const int pb = __shfl_xor_sync(0xffffffffu, b[i], m);
+                b[i] = hi ? pb - b[i] : b[i] + pb;
+            }
+        }
+    }
+    int s = 0;
+    if (TALL) {                                       // the other half of the 16 (8) rows
+        const bool top = !(lane & V);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const int e = __shfl_xor_sync(0xffffffffu, a[i], V);
+            s += top ? 2 * max(abs(a[i]), abs(e)) : 0;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++) s += WIDE ? 2 * max(abs(a[i]), abs(b[i])) : abs(a[i]);
+    }
+#pragma unroll
+    for (int m = 1; m < TH; m <<= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    if (TW == TH) return (u32)(TW == 8 ? (s + 2) >> 2 : (s + 1) >> 1);
+    return (u32)(int)((double)s / (TW * TH == 128 ? sq128 : sq32) * 2.0);
+}
+
+
 }  // namespace uc

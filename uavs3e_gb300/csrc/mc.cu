@@ -9,6 +9,7 @@
 // One warp per CU; lanes walk the CU's samples in raster order, so every store of the warp is
 // one contiguous run of the output buffer.
 #include "common.cuh"
+#include "affine.cuh"
 #include "uavs3e_cuda_internal.h"
 #include "../../include/uavs3e_cuda.h"
 
@@ -137,16 +138,7 @@ struct AffReq {
 };
 static_assert(sizeof(AffReq) == sizeof(uavs3e_cuda_affine_req_t), "affine request layout");
 
-// 1/16-sample luma and 1/32-sample chroma filters (com_tbl_mc_l_coeff_hp, com_tbl_mc_c_coeff_hp,
-// src/com_tables.c:130-189)
-__device__ __constant__ static const s8 kMcLumaHp[16][8] = {
-    { 0, 0, 0, 64, 0, 0, 0, 0 },      { 0, 1, -3, 63, 4, -2, 1, 0 },     { -1, 2, -5, 62, 8, -3, 1, 0 },
-    { -1, 3, -8, 60, 13, -4, 1, 0 },   { -1, 4, -10, 58, 17, -5, 1, 0 },  { -1, 4, -11, 52, 26, -8, 3, -1 },
-    { -1, 3, -9, 47, 31, -10, 4, -1 }, { -1, 4, -11, 45, 34, -10, 4, -1 }, { -1, 4, -11, 40, 40, -11, 4, -1 },
-    { -1, 4, -10, 34, 45, -11, 4, -1 }, { -1, 4, -10, 31, 47, -9, 3, -1 }, { -1, 3, -8, 26, 52, -11, 4, -1 },
-    { 0, 1, -5, 17, 58, -10, 4, -1 },  { 0, 1, -4, 13, 60, -8, 3, -1 },   { 0, 1, -3, 8, 62, -5, 2, -1 },
-    { 0, 1, -2, 4, 63, -3, 1, 0 },
-};
+// 1/32-sample chroma filters (com_tbl_mc_c_coeff_hp, src/com_tables.c:156-189)
 __device__ __constant__ static const s8 kMcChromaHp[32][4] = {
     { 0, 64, 0, 0 },    { -1, 63, 2, 0 },   { -2, 62, 4, 0 },   { -2, 60, 7, -1 },  { -2, 58, 10, -2 },
     { -3, 57, 12, -2 }, { -4, 56, 14, -2 }, { -4, 55, 15, -2 }, { -4, 54, 16, -2 }, { -5, 53, 18, -2 },
@@ -156,35 +148,6 @@ __device__ __constant__ static const s8 kMcChromaHp[32][4] = {
     { -2, 15, 55, -4 }, { -2, 14, 56, -4 }, { -2, 12, 57, -3 }, { -2, 10, 58, -2 }, { -1, 7, 60, -2 },
     { 0, 4, 62, -2 },   { 0, 2, 63, -1 },
 };
-
-// one luma sample of com_mc_blk_luma with hp_flag 1: always filtered from the integer plane
-// (the reference's plane shortcut tests dy == 0 and dy == 8 together and never applies)
-__device__ __forceinline__ int aff_luma_sample(const pel *s, int is, int dx, int dy)
-{
-    if (!dx && !dy) return s[0];
-    if (!dy) {
-        int v = 0;
-#pragma unroll
-        for (int t = 0; t < 8; t++) v += s[t - 3] * kMcLumaHp[dx][t];
-        return min(255, max(0, (v + 32) >> 6));
-    }
-    if (!dx) {
-        int v = 0;
-#pragma unroll
-        for (int t = 0; t < 8; t++) v += s[(t - 3) * is] * kMcLumaHp[dy][t];
-        return min(255, max(0, (v + 32) >> 6));
-    }
-    int v = 0;
-#pragma unroll
-    for (int t = 0; t < 8; t++) {
-        const pel *r = s + (t - 3) * is;
-        int hs = 0;
-#pragma unroll
-        for (int k = 0; k < 8; k++) hs += r[k - 3] * kMcLumaHp[dx][k];
-        v += (int)(s16)hs * kMcLumaHp[dy][t];
-    }
-    return min(255, max(0, (v + 2048) >> 12));
-}
 
 __device__ __forceinline__ int aff_chroma_sample(const pel *s, int ic, int dx, int dy)
 {
@@ -210,8 +173,6 @@ __device__ __forceinline__ int aff_chroma_sample(const pel *s, int ic, int dx, i
     return min(255, max(0, (v + 2048) >> 12));
 }
 
-// com_mv_rounding_s32 with right shift 7: magnitude rounded to 1/16 sample
-__device__ __forceinline__ s32 aff_round7(s32 v) { return v >= 0 ? (v + 64) >> 7 : -((-v + 64) >> 7); }
 
 // the sub-block MVs of one list (com_mc_blk_affine, src/com_mc.c:256-330) into mv[16][16] per
 // 4x4 unit (8x8 sub-blocks fill their four units)

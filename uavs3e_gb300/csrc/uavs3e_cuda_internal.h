@@ -34,7 +34,7 @@ struct MeResult {
 };
 
 // optional per-kernel timing with CUDA events on the launching stream
-enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_LOKA = 5, PROF_TZ = 6, PROF_MC = 7, PROF_RDOQ = 8, PROF_N = 12 };
+enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_LOKA = 5, PROF_TZ = 6, PROF_MC = 7, PROF_RDOQ = 8, PROF_AFFME = 9, PROF_N = 12 };
 int ensure_init();   // selects the library's device (initialising device 0 on first use)
 int me_frame_once(); // one-time per-device setup of the frame search (me.cu)
 // per-call TZ motion searches (tz.cu); planes: n_slots * 16 sample-(0,0) pointers
@@ -45,6 +45,8 @@ int launch_mc_cu(int W, int H, const uint8_t *const *planes, int n_slots, int i_
 int launch_mc_affine(int W, int H, const uint8_t *const *planes, int n_slots, int i_ref, int pad,
                      const uint8_t *const *chroma, int i_c, int pad_c, const void *reqs, int n, uint8_t *out,
                      unsigned long long out_bytes, cudaStream_t st);
+int launch_me_affine(int W, int H, const uint8_t *org, int i_org, const uint8_t *const *planes, int n_slots,
+                     int i_ref, int pad, const void *reqs, int n, void *out, cudaStream_t st);
 int launch_me_tz(const uavs3e_cuda_tz_pic_t *pic, const uint8_t *org, int i_org, const uint8_t *const *planes,
                  int n_slots, int i_ref, int pad, const void *reqs, int n, void *out, cudaStream_t st);
 void prof_begin(int k, cudaStream_t st);
