@@ -37,8 +37,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="me,lattice,pruning,lookahead,tz,rdoq",
-                    help="comma list of legs: me (the headline line), lattice, pruning, lookahead, tz, rdoq")
+    ap.add_argument("--legs", default="me,lattice,pruning,lookahead,tz,rdoq,affme",
+                    help="comma list of legs: me (the headline line), lattice, pruning, lookahead, tz, rdoq, affme")
     ap.add_argument("--pruning-steps", type=int, default=3000, help="training steps of the pruning leg")
     return ap.parse_args()
 
@@ -581,6 +581,77 @@ def tz_leg(u, torch, stream, flush, with_cpu, hbm_peak, reps=10):
     return out
 
 
+def affme_leg(u, torch, stream, flush, with_cpu, reps=10):
+    """affine motion searches (affine_me_gradient) of a 1080p frame: every block of 16x16 and
+    larger on the CTU grid against 2 references, AMVR indices 0..2, 70 % uni calls (60 % of them
+    with analyze_affine_uni's start selection), 30 % bi calls against the other list's prediction"""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cases
+    from uavs3e_gb300.synth import motion_sequence
+    seq = motion_sequence(W, H, 3, seed=33)
+    ms = u.MotionSearch(W, H, n_refs=2, search_range=RANGE, pad=PAD)
+    sp = stream.cuda_stream
+    d_seq = [torch.from_numpy(f).cuda() for f in seq]
+    ms.set_ref_device(0, d_seq[1].data_ptr(), W, sp)
+    ms.set_ref_device(1, d_seq[0].data_ptr(), W, sp)
+    b = u.me_blocks(W, H)
+    blocks = b[(b[:, 0] + b[:, 2] <= W) & (b[:, 1] + b[:, 3] <= H) & (b[:, 2] >= 16) & (b[:, 3] >= 16)]
+    reqs = cases.affme_requests(np.random.default_rng(19), W, H, 2 * len(blocks), 2)
+    for i, f in enumerate(("x", "y", "w", "h")):
+        reqs[f] = np.repeat(blocks[:, i], 2)
+    reqs["ref_slot"] = np.tile([0, 1], len(blocks))
+    reqs["other_slot"] = 1 - reqs["ref_slot"]
+    n = len(reqs)
+    planes = [ms.plane_ptr(s, ph) for s in range(2) for ph in range(16)]
+    d_req = torch.from_numpy(reqs.view(np.uint8).copy()).cuda()
+    d_out = torch.empty(n * u.AFFME_OUT.itemsize, dtype=torch.uint8, device="cuda")
+
+    def run():
+        u.me_affine_device(W, H, d_seq[2].data_ptr(), W, planes, ms.stride, PAD, d_req.data_ptr(), n,
+                           d_out.data_ptr(), sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms_gpu = sum(a.elapsed_time(b) for a, b in evs) / reps
+    org_pin = torch.from_numpy(seq[2]).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        got = ms.affine(org_pin.numpy(), reqs)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / reps
+    moved = int((got["mv"] != reqs["mv"]).any(axis=(1, 2)).sum())
+    out = {"workload": f"affine_me_gradient calls of a 1080p frame: {len(blocks)} blocks of 16x16..64x64 on the CTU "
+                       "grid x 2 references, AMVR indices 0..2, 30 % bi, uni calls with and without the "
+                       "analyze_affine_uni start selection, 4x4 / 8x8 sub-blocks",
+           "calls": n, "ms_per_batch": ms_gpu, "calls_per_s": n / (ms_gpu / 1000.0),
+           "bi_calls": int((reqs["flags"] & u.AFFME_BI != 0).sum()), "calls_that_moved": moved,
+           "predicted_samples": int((reqs["w"].astype(np.int64) * reqs["h"]).sum()),
+           "e2e": {"ms_per_batch": e2e_ms, "calls_per_s": n / (e2e_ms / 1000.0),
+                   "h2d_bytes": int(W * H + reqs.nbytes), "d2h_bytes": int(got.nbytes),
+                   "path": "uavs3e_cuda_me_affine (host org and requests, session references)"}}
+    if with_cpu:
+        import pyoracle
+        o = pyoracle.Oracle()
+        keep, addrs, stride = cases.tz_planes(o, {t: (seq[t],) for t in range(3)}, [1, 0], W, H)
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        o.me_affine(W, H, seq[2], W, addrs, stride, reqs, threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "calls/s", "cores": threads, "kind": "port",
+                               "sample": f"the whole batch through the oracle restatement, {dt:.2f} s"}
+    ms.close()
+    return out
+
+
 def rdoq_leg(u, torch, stream, flush, with_cpu, reps=10):
     """RDOQ (quant_non_zero -> rdoq_quant_block) of 60,000 transform blocks of every shape
     4x4..64x64 (DCT2 coefficients of Laplacian residuals, steps 10..60, intra / inter, luma /
@@ -800,6 +871,7 @@ def run_ours(args):
                  if "lookahead" in legs else None)
     tz = tz_leg(u, torch, stream, flush, not args.no_cpu, hbm_peak) if "tz" in legs else None
     rdoq = rdoq_leg(u, torch, stream, flush, not args.no_cpu) if "rdoq" in legs else None
+    affme = affme_leg(u, torch, stream, flush, not args.no_cpu) if "affme" in legs else None
     h2d = 2 * W * H
     d2h = ms.n_results * 32
     out = {
@@ -822,6 +894,7 @@ def run_ours(args):
         "lookahead": lookahead,
         "tz": tz,
         "rdoq": rdoq,
+        "affme": affme,
         "clocks": clk,
     }
     if not args.no_cpu:
@@ -861,6 +934,8 @@ def run_legs(args):
                            float(peaks.get("hbm_gbs", 6800.0)))
     if "rdoq" in legs:
         out["rdoq"] = rdoq_leg(u, torch, torch.cuda.current_stream(), flush, not args.no_cpu)
+    if "affme" in legs:
+        out["affme"] = affme_leg(u, torch, torch.cuda.current_stream(), flush, not args.no_cpu)
     print(json.dumps(out))
 
 

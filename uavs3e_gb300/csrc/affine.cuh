@@ -15,6 +15,23 @@ __device__ __constant__ static const s8 kMcLumaHp[16][8] = {
     { 0, 1, -2, 4, 63, -3, 1, 0 },
 };
 
+// the same rows packed 4 signed taps per word (taps 0..3, taps 4..7), for dp4a, in global memory
+// so that lanes reading different phases do not serialise as they would on the constant cache
+__device__ static const u32 kMcLumaHpPacked[16][2] = {
+    { 0x40000000u, 0x00000000u }, { 0x3ffd0100u, 0x0001fe04u }, { 0x3efb02ffu, 0x0001fd08u }, { 0x3cf803ffu, 0x0001fc0du },
+    { 0x3af604ffu, 0x0001fb11u }, { 0x34f504ffu, 0xff03f81au }, { 0x2ff703ffu, 0xff04f61fu }, { 0x2df504ffu, 0xff04f622u },
+    { 0x28f504ffu, 0xff04f528u }, { 0x22f604ffu, 0xff04f52du }, { 0x1ff604ffu, 0xff03f72fu }, { 0x1af803ffu, 0xff04f534u },
+    { 0x11fb0100u, 0xff04f63au }, { 0x0dfc0100u, 0xff03f83cu }, { 0x08fd0100u, 0xff02fb3eu }, { 0x04fe0100u, 0x0001fd3fu },
+};
+
+// sum of 4 unsigned bytes of a times 4 signed bytes of b, plus c
+__device__ __forceinline__ int dp4a_us(u32 a, u32 b, int c)
+{
+    int d;
+    asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 // one luma sample of com_mc_blk_luma with hp_flag 1: always filtered from the integer plane
 // (the reference's plane shortcut tests dy == 0 and dy == 8 together and never applies)
 __device__ __forceinline__ int aff_luma_sample(const pel *s, int is, int dx, int dy)

@@ -8,8 +8,8 @@
 // One warp per call.  The CU's org (or bi org) and the current prediction sit in shared memory;
 // the prediction (com_mc_blk_affine_luma, src/com_mc.c:202-250) is rebuilt there after every
 // step, the lanes walk its samples for the SATD tiles and the equation sums, which reduce across
-// the warp in 64-bit integers.  The 4x4 solve runs on lane 0 in IEEE double with every operation
-// rounded on its own (no fused multiply-add), in the reference's order.
+// the warp in 64-bit integers.  The 4x4 solve runs over the warp's lanes in IEEE double with every
+// operation rounded on its own (no fused multiply-add), in the reference's order.
 #include "common.cuh"
 #include "affine.cuh"
 #include "uavs3e_cuda_internal.h"
@@ -62,27 +62,61 @@ __device__ __forceinline__ int ame_bits(const s32 *mv, const s32 *mvp, int num_r
 }
 
 // com_mc_blk_affine_luma (src/com_mc.c:202-250) into dst (w x h, stride w): each sample takes the
-// MV of its sub x sub block (centre, or the control point for the two top corner blocks), rounded
-// to 1/16 and clipped to 18 bits, and is filtered from the integer plane (com_mc_blk_luma, hp)
-__device__ void ame_pred(const AffMeParams &P, const pel *plane, int x, int y, int w, int h, int lw, const s32 *mv,
-                         int sub, pel *dst, int lane)
+// MV of its SUB x SUB block (centre, or the control point for the two top corner blocks), rounded
+// to 1/16 and clipped to 18 bits, and is filtered from the integer plane (com_mc_blk_luma, hp).
+// A lane takes one column of one band of sub-blocks: the 8-tap horizontal filter of its SUB + 7
+// rows (two dp4a per row on the row's 8 bytes), then the vertical filter of those sums.  The
+// reference's copy and 1-D cases are the 2-D formula with the phase-0 taps {0,0,0,64,0,0,0,0}:
+// 64 s through (v + 2048) >> 12 gives (s * 64 + 32) >> 6 exactly, so one path serves all four.
+template <int SUB>
+__device__ void ame_pred_t(const AffMeParams &P, const pel *plane, int x, int y, int w, int h, int lw, const s32 *mv,
+                           pel *dst, int lane)
 {
     const s32 dhx = ((mv[2] - mv[0]) * 128) >> lw, dhy = ((mv[3] - mv[1]) * 128) >> lw;
     const s32 dvx = -dhy, dvy = dhx;
-    const int half = sub >> 1;
-    for (int i = lane; i < w * h; i += 32) {
-        const int j = i >> lw, c = i & (w - 1);
-        const int bx = c & ~(sub - 1), by = j & ~(sub - 1);
-        int px = bx + half, py = by + half;
+    const int tasks = w * (h / SUB);
+    for (int t = lane; t < tasks; t += 32) {
+        const int c = t & (w - 1), by = (t >> lw) * SUB, bx = c & ~(SUB - 1);
+        int px = bx + SUB / 2, py = by + SUB / 2;
         if (bx == 0 && by == 0) { px = 0; py = 0; }
-        else if (bx + sub == w && by == 0) { px = w; py = 0; }
+        else if (bx + SUB == w && by == 0) { px = w; py = 0; }
         const s32 mx = min(max(aff_round7(mv[0] * 128 + dhx * px + dvx * py), CPMV_MIN), CPMV_MAX);
         const s32 my = min(max(aff_round7(mv[1] * 128 + dhy * px + dvy * py), CPMV_MIN), CPMV_MAX);
         const int qx = ((x + bx) << 4) + mx, qy = ((y + by) << 4) + my;
         const int sx = min(max(qx >> 4, -128 - 4), P.W + 4), sy = min(max(qy >> 4, -128 - 4), P.H + 4);
-        const pel *s = plane + (long long)(sy + j - by) * P.i_ref + sx + c - bx;
-        dst[i] = (pel)aff_luma_sample(s, P.i_ref, qx & 15, qy & 15);
+        const u32 hlo = kMcLumaHpPacked[qx & 15][0], hhi = kMcLumaHpPacked[qx & 15][1];
+        const u32 vlo = kMcLumaHpPacked[qy & 15][0], vhi = kMcLumaHpPacked[qy & 15][1];
+        int cv[8];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            cv[k] = (int)(s8)(u8)(vlo >> (8 * k));
+            cv[k + 4] = (int)(s8)(u8)(vhi >> (8 * k));
+        }
+        const pel *s = plane + (long long)(sy - 3) * P.i_ref + sx + (c - bx) - 3;
+        int hs[SUB + 7];
+#pragma unroll
+        for (int r = 0; r < SUB + 7; r++) {
+            const unsigned long long a = (unsigned long long)(s + (long long)r * P.i_ref);
+            const u32 *aw = (const u32 *)(a & ~3ull);
+            const u32 sh = (u32)(a & 3) * 8;
+            const u32 w0 = aw[0], w1 = aw[1], w2 = aw[2];
+            hs[r] = dp4a_us(__funnelshift_r(w1, w2, sh), hhi, dp4a_us(__funnelshift_r(w0, w1, sh), hlo, 0));
+        }
+#pragma unroll
+        for (int o = 0; o < SUB; o++) {
+            int v = 0;
+#pragma unroll
+            for (int k = 0; k < 8; k++) v += hs[o + k] * cv[k];
+            dst[(by + o) * w + c] = (pel)min(255, max(0, (v + 2048) >> 12));
+        }
     }
+}
+
+__device__ __noinline__ void ame_pred(const AffMeParams &P, const pel *plane, int x, int y, int w, int h, int lw,
+                                      const s32 *mv, int sub, pel *dst, int lane)
+{
+    if (sub == 8) ame_pred_t<8>(P, plane, x, y, w, h, lw, mv, dst, lane);
+    else ame_pred_t<4>(P, plane, x, y, w, h, lw, mv, dst, lane);
 }
 
 // com_had (src/com_cost.c:712-812) of the w x h block o - p (both stride w) with TW x TH tiles
@@ -104,7 +138,7 @@ __device__ u32 ame_had_tiles(const pel *o, const pel *p, int w, int h, int lane,
     return acc;
 }
 
-__device__ __forceinline__ u32 ame_had(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128)
+__device__ __noinline__ u32 ame_had(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128)
 {
     if (w == h) return ame_had_tiles<8, 8>(o, p, w, h, lane, sq32, sq128);
     if (w > h) return ame_had_tiles<16, 8>(o, p, w, h, lane, sq32, sq128);
@@ -146,41 +180,79 @@ __device__ __forceinline__ s16 ame_to_s16(double v)
     return (s16)(u16)(u32)i;
 }
 
-// solve_equal (src/inter.c:1280-1315) on the rows 1..4 of a (row 0 is the swap buffer) and the
-// conversion of the solution to the four CPMV changes (x0, y0, x1, y1) at AMVR shift sh
-__device__ void ame_solve(double (*a)[5], int w, int sh, s16 *mvd)
+// solve_equal (src/inter.c:1280-1315) over the warp and the conversion of its solution to the four
+// CPMV changes (x0, y0, x1, y1) at AMVR shift sh.  Lane 5 r + k (< 25) holds element (r, k) of the
+// augmented matrix (rows 1..4, row 0 being the reference's swap buffer); in step i every element
+// (j > i, k >= i) of the elimination is one lane's a[j][k] - a[i][k] * a[j][i-1] / a[i][i-1], each
+// operation rounded on its own, so the values are the reference's; the back substitution runs on
+// lane 0 in the reference's order.  e[] = the equation sums (identical in every lane).
+__device__ __noinline__ void ame_solve(const s64 *e, int w, int sh, int lane, s16 *mvd)
 {
-    constexpr int order = 4;
-    double x[4];
-    for (int i = 1; i < order; i++) {
-        double best = fabs(a[i][i - 1]);
-        int bi = i;
-        for (int j = i + 1; j < order + 1; j++)
-            if (fabs(a[j][i - 1]) > best) { best = fabs(a[j][i - 1]); bi = j; }
-        if (bi != i)
-            for (int j = 0; j < order + 1; j++) { a[0][j] = a[i][j]; a[i][j] = a[bi][j]; a[bi][j] = a[0][j]; }
-        for (int j = i + 1; j < order + 1; j++)
-            for (int k = i; k < order + 1; k++)
-                a[j][k] = __dsub_rn(a[j][k], __ddiv_rn(__dmul_rn(a[i][k], a[j][i - 1]), a[i][i - 1]));
-    }
-    x[order - 1] = __ddiv_rn(a[order][order], a[order][order - 1]);
-    for (int i = order - 2; i >= 0; i--) {
-        double t = 0;
-        for (int j = i + 1; j < order; j++) t = __dadd_rn(t, __dmul_rn(a[i + 1][j], x[j]));
-        x[i] = __ddiv_rn(__dsub_rn(a[i + 1][order], t), a[i + 1][i]);
-    }
-    const double wd = (double)w;
-    const double d[4] = { x[0], x[2], __dadd_rn(__dmul_rn(x[1], wd), x[0]), __dadd_rn(__dmul_rn(-x[3], wd), x[2]) };
+    const bool mine = lane < 25;
+    const int r = mine ? lane / 5 : 0, col = mine ? lane - 5 * (lane / 5) : 0;
+    // coef[c + 1][k] = e[ix(c, k)] for k < 4 (the symmetric products), coef[c + 1][4] = 8 e[10 + c]
+    const int c = r - 1;
+    const int lo = min(c, col), hi = max(c, col);
+    const int idx = col == 4 ? 10 + c : (lo == 0 ? hi : (lo == 1 ? 3 + hi : (lo == 2 ? 5 + hi : 9)));
+    s64 val = 0;
 #pragma unroll
-    for (int v = 0; v < 4; v++) {
-        const double half = d[v] >= 0 ? 0.5 : -0.5;
-        if (sh == 0) mvd[v] = ame_to_s16(__dadd_rn(__dmul_rn(d[v], 16.0), half));
-        else {
-            s16 m = ame_to_s16(__dadd_rn(__dmul_rn(d[v], 4.0), half));
-            m = (s16)(m << 2);
-            mvd[v] = (s16)(((m + (1 << (sh - 1))) >> sh) << sh);   // com_mv_rounding_s16
+    for (int i = 0; i < 14; i++) val = (i == idx) ? e[i] : val;
+    if (col == 4) val *= 8;
+    double v = (mine && r >= 1) ? __ll2double_rn(val) : 0.0;
+    for (int i = 1; i < 4; i++) {
+        double best = fabs(__shfl_sync(0xffffffffu, v, i * 5 + i - 1));
+        int bi = i;
+        for (int j = i + 1; j < 5; j++) {
+            const double cand = fabs(__shfl_sync(0xffffffffu, v, j * 5 + i - 1));
+            if (cand > best) { best = cand; bi = j; }
         }
+        if (bi != i) {
+            const int src = (mine && r == i) ? bi * 5 + col : ((mine && r == bi) ? i * 5 + col : lane);
+            v = __shfl_sync(0xffffffffu, v, src);
+        }
+        const double aik = __shfl_sync(0xffffffffu, v, i * 5 + col);
+        const double aji = __shfl_sync(0xffffffffu, v, r * 5 + i - 1);
+        const double aii = __shfl_sync(0xffffffffu, v, i * 5 + i - 1);
+        if (mine && r > i && col >= i) v = __dsub_rn(v, __ddiv_rn(__dmul_rn(aik, aji), aii));
     }
+    double m[25];
+#pragma unroll
+    for (int k = 5; k < 25; k++) m[k] = __shfl_sync(0xffffffffu, v, k);
+    u32 packed[2] = { 0, 0 };
+    if (lane == 0) {
+#define A(i, j) m[(i) * 5 + (j)]
+        double x[4];
+        x[3] = __ddiv_rn(A(4, 4), A(4, 3));
+#pragma unroll
+        for (int i = 2; i >= 0; i--) {
+            double t = 0;
+#pragma unroll
+            for (int j = i + 1; j < 4; j++) t = __dadd_rn(t, __dmul_rn(A(i + 1, j), x[j]));
+            x[i] = __ddiv_rn(__dsub_rn(A(i + 1, 4), t), A(i + 1, i));
+        }
+#undef A
+        const double wd = (double)w;
+        const double d[4] = { x[0], x[2], __dadd_rn(__dmul_rn(x[1], wd), x[0]), __dadd_rn(__dmul_rn(-x[3], wd), x[2]) };
+        s16 o[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const double half = d[k] >= 0 ? 0.5 : -0.5;
+            if (sh == 0) o[k] = ame_to_s16(__dadd_rn(__dmul_rn(d[k], 16.0), half));
+            else {
+                s16 q = ame_to_s16(__dadd_rn(__dmul_rn(d[k], 4.0), half));
+                q = (s16)(q << 2);
+                o[k] = (s16)(((q + (1 << (sh - 1))) >> sh) << sh);   // com_mv_rounding_s16
+            }
+        }
+        packed[0] = (u32)(u16)o[0] | ((u32)(u16)o[1] << 16);
+        packed[1] = (u32)(u16)o[2] | ((u32)(u16)o[3] << 16);
+    }
+    packed[0] = __shfl_sync(0xffffffffu, packed[0], 0);
+    packed[1] = __shfl_sync(0xffffffffu, packed[1], 0);
+    mvd[0] = (s16)(u16)packed[0];
+    mvd[1] = (s16)(u16)(packed[0] >> 16);
+    mvd[2] = (s16)(u16)packed[1];
+    mvd[3] = (s16)(u16)(packed[1] >> 16);
 }
 
 __device__ __forceinline__ bool ame_cpmv_ok(const s32 (*m)[2])
@@ -281,25 +353,9 @@ __global__ void __launch_bounds__(32 * AME_WARPS) k_me_affine(const AffMeParams 
     for (int iter = 0; iter < (bi ? 5 : 7); iter++) {
         s64 e[14];
         ame_equations(so, sp, w, h, lw, lane, e);
-        u32 packed[2] = { 0, 0 };
-        if (lane == 0) {
-            const int ix[4][4] = { { 0, 1, 2, 3 }, { 1, 4, 5, 6 }, { 2, 5, 7, 8 }, { 3, 6, 8, 9 } };
-            double a[5][5];
-            for (int k = 0; k < 5; k++) a[0][k] = 0.0;
-            for (int c = 0; c < 4; c++) {
-                for (int k = 0; k < 4; k++) a[c + 1][k] = __ll2double_rn(e[ix[c][k]]);
-                a[c + 1][4] = __ll2double_rn(e[10 + c] * 8);
-            }
-            s16 mvd[4];
-            ame_solve(a, w, sh, mvd);
-            packed[0] = (u32)(u16)mvd[0] | ((u32)(u16)mvd[1] << 16);
-            packed[1] = (u32)(u16)mvd[2] | ((u32)(u16)mvd[3] << 16);
-        }
-        packed[0] = __shfl_sync(0xffffffffu, packed[0], 0);
-        packed[1] = __shfl_sync(0xffffffffu, packed[1], 0);
-        if (!packed[0] && !packed[1]) break;
-        const s16 mvd[4] = { (s16)(u16)packed[0], (s16)(u16)(packed[0] >> 16), (s16)(u16)packed[1],
-                             (s16)(u16)(packed[1] >> 16) };
+        s16 mvd[4];
+        ame_solve(e, w, sh, lane, mvd);
+        if (!mvd[0] && !mvd[1] && !mvd[2] && !mvd[3]) break;
 #pragma unroll
         for (int v = 0; v < 4; v++) {
             s32 m = min(max(mvt[v] + (s32)mvd[v], CPMV_MIN), CPMV_MAX);
