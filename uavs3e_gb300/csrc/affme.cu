@@ -64,10 +64,7 @@ __device__ __forceinline__ int ame_bits(const s32 *mv, const s32 *mvp, int num_r
 // com_mc_blk_affine_luma (src/com_mc.c:202-250) into dst (w x h, stride w): each sample takes the
 // MV of its SUB x SUB block (centre, or the control point for the two top corner blocks), rounded
 // to 1/16 and clipped to 18 bits, and is filtered from the integer plane (com_mc_blk_luma, hp).
-// A lane takes one column of one band of sub-blocks: the 8-tap horizontal filter of its SUB + 7
-// rows (two dp4a per row on the row's 8 bytes), then the vertical filter of those sums.  The
-// reference's copy and 1-D cases are the 2-D formula with the phase-0 taps {0,0,0,64,0,0,0,0}:
-// 64 s through (v + 2048) >> 12 gives (s * 64 + 32) >> 6 exactly, so one path serves all four.
+// A lane takes one column of one band of sub-blocks (aff_luma_column).
 template <int SUB>
 __device__ void ame_pred_t(const AffMeParams &P, const pel *plane, int x, int y, int w, int h, int lw, const s32 *mv,
                            pel *dst, int lane)
@@ -83,32 +80,10 @@ __device__ void ame_pred_t(const AffMeParams &P, const pel *plane, int x, int y,
         const s32 mx = min(max(aff_round7(mv[0] * 128 + dhx * px + dvx * py), CPMV_MIN), CPMV_MAX);
         const s32 my = min(max(aff_round7(mv[1] * 128 + dhy * px + dvy * py), CPMV_MIN), CPMV_MAX);
         const int qx = ((x + bx) << 4) + mx, qy = ((y + by) << 4) + my;
-        const int sx = min(max(qx >> 4, -128 - 4), P.W + 4), sy = min(max(qy >> 4, -128 - 4), P.H + 4);
-        const u32 hlo = kMcLumaHpPacked[qx & 15][0], hhi = kMcLumaHpPacked[qx & 15][1];
-        const u32 vlo = kMcLumaHpPacked[qy & 15][0], vhi = kMcLumaHpPacked[qy & 15][1];
-        int cv[8];
+        int v[SUB];
+        aff_luma_column<SUB>(plane, P.i_ref, P.W, P.H, qx, qy, c - bx, v);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            cv[k] = (int)(s8)(u8)(vlo >> (8 * k));
-            cv[k + 4] = (int)(s8)(u8)(vhi >> (8 * k));
-        }
-        const pel *s = plane + (long long)(sy - 3) * P.i_ref + sx + (c - bx) - 3;
-        int hs[SUB + 7];
-#pragma unroll
-        for (int r = 0; r < SUB + 7; r++) {
-            const unsigned long long a = (unsigned long long)(s + (long long)r * P.i_ref);
-            const u32 *aw = (const u32 *)(a & ~3ull);
-            const u32 sh = (u32)(a & 3) * 8;
-            const u32 w0 = aw[0], w1 = aw[1], w2 = aw[2];
-            hs[r] = dp4a_us(__funnelshift_r(w1, w2, sh), hhi, dp4a_us(__funnelshift_r(w0, w1, sh), hlo, 0));
-        }
-#pragma unroll
-        for (int o = 0; o < SUB; o++) {
-            int v = 0;
-#pragma unroll
-            for (int k = 0; k < 8; k++) v += hs[o + k] * cv[k];
-            dst[(by + o) * w + c] = (pel)min(255, max(0, (v + 2048) >> 12));
-        }
+        for (int o = 0; o < SUB; o++) dst[(by + o) * w + c] = (pel)v[o];
     }
 }
 
@@ -261,7 +236,7 @@ __device__ __forceinline__ bool ame_cpmv_ok(const s32 (*m)[2])
            m[1][0] >= CPMV_MIN && m[1][0] <= CPMV_MAX && m[1][1] >= CPMV_MIN && m[1][1] <= CPMV_MAX;
 }
 
-__global__ void __launch_bounds__(32 * AME_WARPS) k_me_affine(const AffMeParams P)
+__global__ void __launch_bounds__(32 * AME_WARPS, 5) k_me_affine(const AffMeParams P)
 {
     __shared__ __align__(16) pel s_org[AME_WARPS][64 * 64];
     __shared__ __align__(16) pel s_pred[AME_WARPS][64 * 64];

@@ -217,20 +217,22 @@ __global__ void __launch_bounds__(32 * AFF_WARPS) k_mc_affine(const McParams P, 
         if (q.slot[l] >= 0) { aff_subblock_mvs(q, l, sub, s_mv[warp][k], lane); ls[k++] = l; }
     __syncwarp();
     pel *o = P.out + q.out_offset;
-    // luma: 16-phase filters per sub-block MV
-    for (int i = lane; i < w * h; i += 32) {
-        const int j = i / w, c = i - j * w;
-        int v = 0;
-        for (int t = 0; t < k; t++) {
-            const s32 *m = s_mv[warp][t][c >> 2][j >> 2];
-            const int bx = c & ~(sub - 1), by = j & ~(sub - 1);
+    // luma: 16-phase filters per sub-block MV, a lane per column of a band of sub-blocks
+    const int tasks = w * (h / sub);
+    for (int t = lane; t < tasks; t += 32) {
+        const int c = t % w, by = (t / w) * sub, bx = c & ~(sub - 1);
+        int acc[8];
+        for (int u = 0; u < k; u++) {
+            const s32 *m = s_mv[warp][u][c >> 2][by >> 2];
             const int qx = ((q.x + bx) << 4) + m[0], qy = ((q.y + by) << 4) + m[1];
-            const int px = min(max(qx >> 4, -128 - 4), P.W + 4), py = min(max(qy >> 4, -128 - 4), P.H + 4);
-            const pel *s = P.planes[q.slot[ls[t]] * 16] + (long long)(py + j - by) * P.i_ref + px + c - bx;
-            const int sv = aff_luma_sample(s, P.i_ref, qx & 15, qy & 15);
-            v = t ? (v + sv + 1) >> 1 : sv;
+            const pel *plane = P.planes[q.slot[ls[u]] * 16];
+            int v[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+            if (sub == 8) aff_luma_column<8>(plane, P.i_ref, P.W, P.H, qx, qy, c - bx, v);
+            else aff_luma_column<4>(plane, P.i_ref, P.W, P.H, qx, qy, c - bx, v);
+#pragma unroll
+            for (int i = 0; i < 8; i++) acc[i] = u ? (acc[i] + v[i] + 1) >> 1 : v[i];
         }
-        o[i] = (pel)v;
+        for (int i = 0; i < sub; i++) o[(by + i) * w + c] = (pel)acc[i];
     }
     o += w * h;
     // chroma: 4x4 blocks per 8x8 luma with the rounded mean of their four 4x4 MVs
