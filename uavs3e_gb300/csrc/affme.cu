@@ -94,20 +94,30 @@ __device__ __noinline__ void ame_pred(const AffMeParams &P, const pel *plane, in
     else ame_pred_t<4>(P, plane, x, y, w, h, lw, mv, dst, lane);
 }
 
-// com_had (src/com_cost.c:712-812) of the w x h block o - p (both stride w) with TW x TH tiles
+// com_had (src/com_cost.c:712-812) of the w x h block o - p (both stride w) with TW x TH tiles.
+// 2:1 tiles: each pass's group sums move to one lane per tile, and the double normalisation runs
+// once for all (at most 16) tiles of the block instead of once per pass.
 template <int TW, int TH>
 __device__ u32 ame_had_tiles(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128)
 {
-    const int ntx = w / TW, total = ntx * (h / TH) * TH;
+    constexpr int G = 32 / TH;                      // tiles per pass
+    const int ntx = w / TW, ntiles = ntx * (h / TH), total = ntiles * TH;
     u32 acc = 0;
-    for (int base = 0; base < total; base += 32) {
+    int held = 0;
+    for (int base = 0, pass = 0; base < total; base += 32, pass++) {
         const int t = base + lane;
         const bool active = t < total;
         const int tt = active ? t : 0, tile = tt / TH, row = tt - tile * TH;
         const int off = ((tile / ntx) * TH + row) * w + (tile % ntx) * TW;
-        const u32 v = had_tile_rows<TW, TH>(o + off, w, p + off, w, active, lane, sq32, sq128);
-        if (active && row == 0) acc += v;
+        const int s = had_tile_sum<TW, TH>(o + off, p + off, active, lane);
+        if (TW == TH) {
+            if (active && row == 0) acc += had_tile_norm<TW, TH>(s, sq32, sq128);
+        } else {
+            const int got = __shfl_sync(0xffffffffu, s, ((lane - pass * G) * TH) & 31);
+            if (lane >= pass * G && lane < pass * G + G) held = got;
+        }
     }
+    if (TW != TH && lane < ntiles) acc = had_tile_norm<TW, TH>(held, sq32, sq128);
 #pragma unroll
     for (int m = 16; m; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
     return acc;
@@ -149,10 +159,20 @@ __device__ void ame_equations(const pel *o, const pel *p, int w, int h, int lw, 
 
 // (s16) of a double as x86-64 code converts it (the reference's platform): truncation to 32 bits
 // by cvttsd2si -- NaN and values outside the 32-bit range give INT_MIN -- then the low 16 bits
+// (the range test on the exponent bits: |v| >= 2^31, infinities and NaN all give INT_MIN, and
+// the values in (-2^31 - 1, -2^31] that truncate to INT_MIN give it too)
 __device__ __forceinline__ s16 ame_to_s16(double v)
 {
-    const int i = (v > -2147483649.0 && v < 2147483648.0) ? __double2int_rz(v) : (int)0x80000000u;
+    const int e = (int)((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff;
+    const int i = e < 1023 + 31 ? __double2int_rz(v) : (int)0x80000000u;
     return (s16)(u16)(u32)i;
+}
+
+// the bits of |v| as an unsigned integer: for non-NaN values |a| > |b| exactly when
+// ame_mag(a) > ame_mag(b); NaN maps above every finite value
+__device__ __forceinline__ unsigned long long ame_mag(double v)
+{
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
 // solve_equal (src/inter.c:1280-1315) over the warp and the conversion of its solution to the four
@@ -175,11 +195,12 @@ __device__ __noinline__ void ame_solve(const s64 *e, int w, int sh, int lane, s1
     if (col == 4) val *= 8;
     double v = (mine && r >= 1) ? __ll2double_rn(val) : 0.0;
     for (int i = 1; i < 4; i++) {
-        double best = fabs(__shfl_sync(0xffffffffu, v, i * 5 + i - 1));
+        // fabs(cand) > best in integers: false when cand is NaN, and nothing exceeds a NaN best
+        unsigned long long best = ame_mag(__shfl_sync(0xffffffffu, v, i * 5 + i - 1));
         int bi = i;
         for (int j = i + 1; j < 5; j++) {
-            const double cand = fabs(__shfl_sync(0xffffffffu, v, j * 5 + i - 1));
-            if (cand > best) { best = cand; bi = j; }
+            const unsigned long long cand = ame_mag(__shfl_sync(0xffffffffu, v, j * 5 + i - 1));
+            if (cand <= 0x7ff0000000000000ull && cand > best) { best = cand; bi = j; }
         }
         if (bi != i) {
             const int src = (mine && r == i) ? bi * 5 + col : ((mine && r == bi) ? i * 5 + col : lane);
@@ -193,10 +214,9 @@ __device__ __noinline__ void ame_solve(const s64 *e, int w, int sh, int lane, s1
     double m[25];
 #pragma unroll
     for (int k = 5; k < 25; k++) m[k] = __shfl_sync(0xffffffffu, v, k);
-    u32 packed[2] = { 0, 0 };
+    double x[4] = { 0, 0, 0, 0 };
     if (lane == 0) {
 #define A(i, j) m[(i) * 5 + (j)]
-        double x[4];
         x[3] = __ddiv_rn(A(4, 4), A(4, 3));
 #pragma unroll
         for (int i = 2; i >= 0; i--) {
@@ -206,24 +226,32 @@ __device__ __noinline__ void ame_solve(const s64 *e, int w, int sh, int lane, s1
             x[i] = __ddiv_rn(__dsub_rn(A(i + 1, 4), t), A(i + 1, i));
         }
 #undef A
-        const double wd = (double)w;
-        const double d[4] = { x[0], x[2], __dadd_rn(__dmul_rn(x[1], wd), x[0]), __dadd_rn(__dmul_rn(-x[3], wd), x[2]) };
-        s16 o[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const double half = d[k] >= 0 ? 0.5 : -0.5;
-            if (sh == 0) o[k] = ame_to_s16(__dadd_rn(__dmul_rn(d[k], 16.0), half));
-            else {
-                s16 q = ame_to_s16(__dadd_rn(__dmul_rn(d[k], 4.0), half));
-                q = (s16)(q << 2);
-                o[k] = (s16)(((q + (1 << (sh - 1))) >> sh) << sh);   // com_mv_rounding_s16
-            }
-        }
-        packed[0] = (u32)(u16)o[0] | ((u32)(u16)o[1] << 16);
-        packed[1] = (u32)(u16)o[2] | ((u32)(u16)o[3] << 16);
     }
-    packed[0] = __shfl_sync(0xffffffffu, packed[0], 0);
-    packed[1] = __shfl_sync(0xffffffffu, packed[1], 0);
+    // lanes 0..3 convert x0 -> mvd x0, x2 -> y0, x1 w + x0 -> x1, -x3 w + x2 -> y1
+    const double x0 = __shfl_sync(0xffffffffu, x[0], 0), x1 = __shfl_sync(0xffffffffu, x[1], 0);
+    const double x2 = __shfl_sync(0xffffffffu, x[2], 0), x3 = __shfl_sync(0xffffffffu, x[3], 0);
+    u32 o = 0;
+    if (lane < 4) {
+        const double wd = (double)w;
+        const double d = lane == 0 ? x0 : (lane == 1 ? x2 : (lane == 2 ? __dadd_rn(__dmul_rn(x1, wd), x0)
+                                                                        : __dadd_rn(__dmul_rn(-x3, wd), x2)));
+        // d >= 0: +0, -0 and positive values, not NaN
+        const long long db = __double_as_longlong(d);
+        const bool ge0 = db == (long long)0x8000000000000000ull ||
+                         (db >= 0 && (unsigned long long)db <= 0x7ff0000000000000ull);
+        const double half = ge0 ? 0.5 : -0.5;
+        s16 q;
+        if (sh == 0) q = ame_to_s16(__dadd_rn(__dmul_rn(d, 16.0), half));
+        else {
+            q = ame_to_s16(__dadd_rn(__dmul_rn(d, 4.0), half));
+            q = (s16)(q << 2);
+            q = (s16)(((q + (1 << (sh - 1))) >> sh) << sh);   // com_mv_rounding_s16
+        }
+        o = (u32)(u16)q;
+    }
+    u32 packed[2];
+    packed[0] = __shfl_sync(0xffffffffu, o, 0) | (__shfl_sync(0xffffffffu, o, 1) << 16);
+    packed[1] = __shfl_sync(0xffffffffu, o, 2) | (__shfl_sync(0xffffffffu, o, 3) << 16);
     mvd[0] = (s16)(u16)packed[0];
     mvd[1] = (s16)(u16)(packed[0] >> 16);
     mvd[2] = (s16)(u16)packed[1];

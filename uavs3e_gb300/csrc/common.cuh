@@ -174,11 +174,10 @@ __host__ __device__ __forceinline__ void had_tile_shape(int w, int h, int *tw, i
 // One pass of com_had tile rows over the warp: lanes in groups of TH hold one row each of a TW x TH
 // tile (row = lane % TH), rows transformed in registers, columns by butterflies across the group.
 // Tiles of 2:1 shape combine their two square halves as |a + b| + |a - b| = 2 max(|a|, |b|)
-// (com_had_16x8 / _8x16 / _8x4 / _4x8, src/com_cost.c:344-710).  Returns the tile's SATD in
-// every lane of the group (0 for inactive groups).
+// (com_had_16x8 / _8x16 / _8x4 / _4x8, src/com_cost.c:344-710).  had_tile_sum returns the tile's
+// magnitude sum, had_tile_rows its SATD, in every lane of the group (0 for inactive groups).
 template <int TW, int TH>
-__device__ __forceinline__ u32 had_tile_rows(const pel *o, int io, const pel *p, int ip, bool active, int lane,
-                                            double sq32, double sq128)
+__device__ __forceinline__ int had_tile_sum(const pel *o, const pel *p, bool active, int lane)
 {
     constexpr bool WIDE = TW > TH, TALL = TW < TH;
     constexpr int N = WIDE ? TW / 2 : TW;            // points of each row transform
@@ -218,8 +217,23 @@ __device__ __forceinline__ u32 had_tile_rows(const pel *o, int io, const pel *p,
     }
 #pragma unroll
     for (int m = 1; m < TH; m <<= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    return s;
+}
+
+// com_had's normalisation of a tile's magnitude sum: 4x4 (s+1)>>1, 8x8 (s+2)>>2, 2:1 tiles
+// (int)(s / sqrt(w h) * 2.0) in double
+template <int TW, int TH>
+__device__ __forceinline__ u32 had_tile_norm(int s, double sq32, double sq128)
+{
     if (TW == TH) return (u32)(TW == 8 ? (s + 2) >> 2 : (s + 1) >> 1);
     return (u32)(int)((double)s / (TW * TH == 128 ? sq128 : sq32) * 2.0);
+}
+
+template <int TW, int TH>
+__device__ __forceinline__ u32 had_tile_rows(const pel *o, int io, const pel *p, int ip, bool active, int lane,
+                                            double sq32, double sq128)
+{
+    return had_tile_norm<TW, TH>(had_tile_sum<TW, TH>(o, p, active, lane), sq32, sq128);
 }
 
 
