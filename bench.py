@@ -300,8 +300,73 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
                         "peak_source": f"2 x dp2a issue rate max(measured {dp_clk:.1f}, 64) per clk per SM x "
                                        f"{sm_count} SMs x {sm_mhz:.0f} MHz; matrix-form transform multiply-adds only "
                                        f"(prediction, SATD, quantisation not counted)"}}
+    out["rmd"] = rmd_part(u, torch, stream, flush, d_satd, cus, with_cpu)
     if with_cpu:
         out["cpu_baseline"] = lattice_cpu_baseline(org, rec, cus)
+    return out
+
+
+def rmd_part(u, torch, stream, flush, d_satd, cus, with_cpu, reps=10):
+    """make_ipred_list of every CU of the lattice from the lattice's own SATD records (random MPM
+    pairs, coder states, fast / full searches, inter-SATD cuts)"""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cases
+    n = len(cus)
+    reqs, _, _, _, _ = cases.rmd_inputs(np.random.default_rng(29), 1)
+    reqs = np.repeat(reqs, n)
+    base = np.random.default_rng(31)
+    reqs["satd_row"] = np.arange(n)
+    reqs["pb_w"], reqs["pb_h"] = cus["w"], cus["h"]
+    m = np.sort(base.integers(0, 34, (n, 2)), axis=1)
+    reqs["mpm"] = m
+    reqs["skip_ipd"] = base.random(n) < 0.3
+    reqs["fast"] = base.random(n) < 0.7
+    reqs["range"] = base.integers(256, 512, n)
+    reqs["ctx"] = cases.rmd_ctx(base, 7 * n).reshape(n, 7)
+    reqs["sqrt_lambda"] = base.uniform(4.0, 60.0, n)
+    cut = base.random(n) < 0.5
+    reqs["inter_satd"] = np.where(cut, (base.integers(1, 40, n) * cus["w"].astype(np.int64) * cus["h"]).astype(np.uint64),
+                                  np.uint64(np.iinfo(np.uint64).max))
+    reqs["satd_threshold"] = base.uniform(0.9, 1.6, n)
+    d_req = torch.from_numpy(reqs.view(np.uint8).copy()).cuda()
+    d_out = torch.empty(n * u.RMD_OUT.itemsize, dtype=torch.uint8, device="cuda")
+    sp = stream.cuda_stream
+
+    def run():
+        u.intra_rmd_device(d_satd.data_ptr(), n, d_req.data_ptr(), n, d_out.data_ptr(), sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / reps
+    satd = d_satd.cpu().numpy().view(np.uint32).reshape(n, 33)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        got = u.intra_rmd(satd, reqs)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / reps
+    out = {"workload": f"make_ipred_list of the {n} lattice CUs from its SATD records (70 % fast search, 30 % "
+                       "DC/planar/bilinear skipped, MPM pairs, LBAC states for the mode bits, 50 % inter-SATD cuts)",
+           "blocks": n, "ms_per_batch": ms, "blocks_per_s": n / (ms / 1000.0),
+           "mean_candidates": float(got["count"].mean()),
+           "e2e": {"ms_per_batch": e2e_ms, "blocks_per_s": n / (e2e_ms / 1000.0),
+                   "h2d_bytes": int(satd.nbytes + reqs.nbytes), "d2h_bytes": int(got.nbytes),
+                   "path": "uavs3e_cuda_intra_rmd (host SATD records and requests)"}}
+    if with_cpu:
+        import pyoracle
+        t0 = time.perf_counter()
+        pyoracle.Oracle().intra_rmd(satd, reqs)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "blocks/s", "cores": 1, "kind": "port",
+                               "sample": f"the whole batch through the oracle restatement (one core), {dt:.2f} s"}
     return out
 
 

@@ -409,6 +409,42 @@ typedef struct {
 UAVS3E_CUDA_API void uavs3e_cuda_lattice_autotune(int on);
 UAVS3E_CUDA_API int uavs3e_cuda_lattice_budgets(int n_modes, int out[25]);
 
+/*
+ * Intra mode candidates: make_ipred_list (src/intra.c:226-367, file-local) for a list of
+ * prediction blocks, each with the SATD of its 33 modes taken from row satd_row of an array laid
+ * out as the lattice's satd records (satd[row * 33 + mode], e.g. uavs3e_cuda_intra_lattice's
+ * satd output with row = CU index) and with the coder state the encoder holds in
+ * core->lbac_bakup: the bits of each mode are lbac_enc_intra_dir (src/entropy.c:2118) in
+ * counting mode from that range and those intra_dir context models.  Output: ipred_list[0..4] and
+ * the return value (the number of candidates the RDO takes), as the reference leaves them.
+ */
+typedef struct {
+    uint32_t satd_row;        /* row of the SATD array                                         */
+    uint8_t  pb_w, pb_h;      /* prediction block, 4..64 (powers of two)                       */
+    uint8_t  mpm[2];          /* cur_info->mpm[part_idx], 0..33 (33 = IPD_IPCM)                */
+    uint8_t  skip_ipd;        /* the skip_ipd argument (no DC / planar / bilinear)             */
+    uint8_t  fast;            /* info->intra_fast_rmd                                          */
+    uint16_t range;           /* core->lbac_bakup.range, 256..511                              */
+    int16_t  ctx[7];          /* core->lbac_bakup.h.intra_dir[0..6] (non-zero LPS probability) */
+    uint8_t  pad[6];
+    double   sqrt_lambda;     /* core->sqrt_lambda[0], >= 0                                    */
+    uint64_t inter_satd;      /* core->inter_satd (UINT64_MAX: none)                           */
+    double   satd_threshold;  /* core->satd_threshold                                          */
+} uavs3e_cuda_rmd_req_t;
+
+typedef struct {
+    int8_t   list[5];         /* ipred_list[0..4] (-1: empty)                                  */
+    uint8_t  count;           /* return value; 255 for a request outside the supported domain  */
+    uint8_t  pad[2];
+} uavs3e_cuda_rmd_out_t;
+
+/* Host buffers, synchronous: satd has n_rows * 33 entries. */
+UAVS3E_CUDA_API int uavs3e_cuda_intra_rmd(const uint32_t *satd, size_t n_rows, const uavs3e_cuda_rmd_req_t *reqs,
+                                          int n, uavs3e_cuda_rmd_out_t *out);
+UAVS3E_CUDA_API int uavs3e_cuda_intra_rmd_device(const uint32_t *d_satd, size_t n_rows,
+                                                 const uavs3e_cuda_rmd_req_t *d_reqs, int n,
+                                                 uavs3e_cuda_rmd_out_t *d_out, void *stream);
+
 /* The 23-shape lattice (w, h in 4..64, aspect <= 8, largest first) of a picture: writes up to
  * cap records to out (may be NULL) and returns the total count. */
 UAVS3E_CUDA_API int uavs3e_cuda_lattice_cus(int width, int height, uavs3e_cuda_cu_t *out, int cap);

@@ -1858,6 +1858,156 @@ void orc_mc_affine(int width, int height, const pel *const *planes, int i_ref, c
     }
 }
 
+/* ============================================================ intra mode candidates */
+
+/* one bin of lbac_encode_bin in counting mode (src/entropy.c:1168-1187): the range after it and
+ * the bits it adds.  Each intra_dir context model is used once per syntax element, so its
+ * update does not change the count. */
+static void rmd_bin(u32 *range, int *bits, int bin, int model)
+{
+    const u32 lps = (u32)(model & 2047) >> 3;
+    u32 mps = *range - lps;
+    const int s = mps < 256;
+    mps |= 0x100;
+    if (bin == (model & 1)) {
+        *bits += s;
+        *range = mps;
+    } else {
+        const u32 l = (*range << s) - mps;          /* 1..510 */
+        const int sh = 8 - ilog2((int)l);            /* get_shift */
+        *range = l << sh;
+        *bits += sh + s;
+    }
+}
+
+/* lbac_enc_intra_dir (src/entropy.c:2118-2130): an MPM as flag 1 + its index, any other mode as
+ * flag 0 + its 5-bit rank among the non-MPM modes (msb first, contexts 1..5) */
+int orc_intra_dir_bits(int range, const s16 *ctx, int ipm, const u8 *mpm)
+{
+    const int code = ipm == mpm[0] ? -2 : (ipm == mpm[1] ? -1 : (ipm < mpm[0] ? ipm : (ipm < mpm[1] ? ipm - 1 : ipm - 2)));
+    u32 r = (u32)range;
+    int bits = 0;
+    if (code < 0) {
+        rmd_bin(&r, &bits, 1, ctx[0]);
+        rmd_bin(&r, &bits, code + 2, ctx[6]);
+    } else {
+        rmd_bin(&r, &bits, 0, ctx[0]);
+        for (int i = 4; i >= 0; i--) rmd_bin(&r, &bits, (code >> i) & 1, ctx[1 + (4 - i)]);
+    }
+    return bits;
+}
+
+/* com_update_cand_list (src/intra.c:187-207): the mode's cost is recorded, and the mode enters
+ * the first len entries of the cost-ordered list before the first entry it does not beat
+ * strictly (empty entries count as beaten), the entries below it moving down one */
+static void rmd_update(int ipm, double cost, int len, int *list, double *cost_of)
+{
+    cost_of[ipm] = cost;
+    int shift = 0, p = len - 1;
+    while (shift < len && (list[p] < 0 || cost < cost_of[list[p]])) { p--; shift++; }
+    if (shift) {
+        int q = len - 1;
+        for (shift--; shift; shift--, q--) list[q] = list[q - 1];
+        list[q] = ipm;
+    }
+}
+
+typedef struct {
+    const u32 *satd;
+    const orc_rmd_req_t *r;
+    int *list;
+    double *cost_of;
+} rmd_ctx_t;
+
+/* check_one_mode (src/intra.c:209-224) with the mode's SATD given: cost = SATD + bits x
+ * sqrt_lambda in double, then the list update */
+static void rmd_check(const rmd_ctx_t *c, int ipm, int len)
+{
+    const int bits = orc_intra_dir_bits(c->r->range, c->r->ctx, ipm, c->r->mpm);
+    const double cost = (double)c->satd[ipm] + (double)bits * c->r->sqrt_lambda;
+    rmd_update(ipm, cost, len, c->list, c->cost_of);
+}
+
+/* make_ipred_list (src/intra.c:226-367): with intra_fast_rmd the 10 coarse modes, then +-2 of the
+ * best 7, +-1 of the first 3 angular entries, and the MPMs not yet tried; otherwise every mode.
+ * Then the MPMs the list lacks replace its last entries, and entries costlier than the inter
+ * SATD x threshold are cut from the end.  Reproduces the reference's stale entries: the list
+ * keeps 10 positions from the coarse stage while later stages insert into 4 or 5. */
+static int rmd_one(const u32 *satd, const orc_rmd_req_t *r, int *list)
+{
+    const int w = r->pb_w, h = r->pb_h;
+    int cnt = (w >= h * 4 || h >= w * 4) ? 4 : 5;
+    double cost_of[33];
+    for (int i = 0; i < 33; i++) { list[i] = -1; cost_of[i] = 1.7e+308; }
+    rmd_ctx_t c = { satd, r, list, cost_of };
+    if (r->fast) {
+        static const int r4[10] = { 0, 1, 2, 6, 10, 14, 18, 22, 26, 30 };
+        int map[35] = { 0 };
+        for (int i = 0; i < 10; i++) map[r4[i]] = 1;
+        for (int i = r->skip_ipd ? 3 : 0; i < 10; i++) rmd_check(&c, r4[i], i + 1);
+        int r2[12], n2 = 0;
+        for (int k = 0; k < 7; k++) {
+            const int ipm = list[k];
+            if (ipm >= 6) {
+                if (!map[ipm - 2]) { r2[n2++] = ipm - 2; map[ipm - 2] = 1; }
+                if (!map[ipm + 2]) { r2[n2++] = ipm + 2; map[ipm + 2] = 1; }
+            }
+        }
+        for (int i = 0; i < n2; i++) rmd_check(&c, r2[i], MAX(cnt, 3));
+        int r1[8], n1 = 0;
+        for (int k = 0, i = 0; k < 3 && i < 10;) {
+            const int ipm = list[i++];
+            if (ipm >= 4) {
+                k++;
+                if (!map[ipm - 1]) { r1[n1++] = ipm - 1; map[ipm - 1] = 1; }
+                if (ipm + 1 < 33 && !map[ipm + 1]) { r1[n1++] = ipm + 1; map[ipm + 1] = 1; }
+            }
+        }
+        for (int i = 0; i < n1; i++) rmd_check(&c, r1[i], MIN(cnt, 5));
+        for (int k = 0; k < 2; k++) {
+            const int m = r->mpm[k];
+            if (m < 33) {
+                if (r->skip_ipd && m <= 2) continue;
+                if (!map[m]) rmd_check(&c, m, MIN(cnt, 5));
+            }
+        }
+    } else {
+        for (int i = r->skip_ipd ? 3 : 0; i < 33; i++) rmd_check(&c, i, cnt);
+    }
+    int need[2] = { 0, 0 };
+    for (int k = 0; k < 2; k++)
+        if (r->mpm[k] != 33 && !(r->skip_ipd && r->mpm[k] <= 2)) need[k] = 1;
+    for (int i = 0; i < cnt; i++) {
+        if (need[0] && list[i] == r->mpm[0]) need[0] = 0;
+        if (need[1] && list[i] == r->mpm[1]) need[1] = 0;
+    }
+    if (need[0] + need[1] == 2) {
+        const int first = cost_of[r->mpm[0]] <= cost_of[r->mpm[1]];
+        list[cnt - 2] = first ? r->mpm[0] : r->mpm[1];
+        list[cnt - 1] = first ? r->mpm[1] : r->mpm[0];
+    } else if (need[0] + need[1]) {
+        const int add = need[0] ? 0 : 1;
+        if (list[cnt - 1] == r->mpm[1 - add]) list[cnt - 2] = list[cnt - 1];
+        list[cnt - 1] = r->mpm[add];
+    }
+    for (int i = cnt - 1; i >= 0; i--) {
+        if (r->inter_satd != ~0ull && cost_of[list[i]] > (double)r->inter_satd * r->satd_threshold) cnt--;
+        else break;
+    }
+    return cnt;
+}
+
+void orc_intra_rmd(const u32 *satd, const orc_rmd_req_t *reqs, int n, orc_rmd_out_t *out)
+{
+    for (int i = 0; i < n; i++) {
+        int list[33];
+        const int cnt = rmd_one(satd + (size_t)reqs[i].satd_row * 33, &reqs[i], list);
+        for (int k = 0; k < 5; k++) out[i].list[k] = (s8)list[k];
+        out[i].count = (u8)cnt;
+        out[i].pad[0] = out[i].pad[1] = 0;
+    }
+}
+
 /* ============================================================ affine motion search */
 
 #define CPMV_MIN (-131072)

@@ -275,6 +275,36 @@ void orc_mc_cu(int width, int height, const pel *const *planes, int i_ref, const
 void orc_me_tz(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *const *planes, int i_ref,
                const orc_tz_req_t *reqs, int n, orc_tz_out_t *out, int threads);
 
+/* ------------- intra mode candidates (make_ipred_list, src/intra.c:236-367) ------------- */
+
+/* one prediction block's candidate search: the SATD of each of its 33 modes comes from a
+ * satd[satd_row * 33 + mode] array (the lattice's records), the rate of each mode from the
+ * counting-mode LBAC coding of intra_dir (lbac_enc_intra_dir, src/entropy.c:2118) from the state
+ * core->lbac_bakup holds: its range and the 7 intra_dir context models */
+typedef struct {
+    u32 satd_row;
+    u8  pb_w, pb_h;     /* prediction block size                                                  */
+    u8  mpm[2];         /* cur_info->mpm[part_idx] (33 = IPD_IPCM)                                */
+    u8  skip_ipd;       /* skip DC, planar, bilinear                                              */
+    u8  fast;           /* info->intra_fast_rmd                                                   */
+    u16 range;          /* lbac_bakup.range, 256..511                                             */
+    s16 ctx[7];         /* lbac_bakup.h.intra_dir[0..6]                                           */
+    u8  pad[6];
+    double sqrt_lambda; /* core->sqrt_lambda[0]                                                   */
+    u64 inter_satd;     /* core->inter_satd (UINT64_MAX: no inter candidate yet)                  */
+    double satd_threshold;
+} orc_rmd_req_t;
+
+typedef struct {
+    s8 list[5];         /* ipred_list[0..4] as make_ipred_list leaves them                        */
+    u8 count;           /* its return value (the candidates the RDO takes)                        */
+    u8 pad[2];
+} orc_rmd_out_t;
+
+void orc_intra_rmd(const u32 *satd, const orc_rmd_req_t *reqs, int n, orc_rmd_out_t *out);
+/* bits of intra prediction mode ipm (lbac_enc_intra_dir in counting mode) */
+int orc_intra_dir_bits(int range, const s16 *ctx, int ipm, const u8 *mpm);
+
 /* ------------- affine motion search (affine_me_gradient, src/inter.c:1339-1470) ------------- */
 
 #define ORC_AFFME_BI        1   /* bi argument: org = 2 org - the other list's prediction (8x8 sub-blocks) */

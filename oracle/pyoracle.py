@@ -223,6 +223,14 @@ class Oracle(_Common):
         self.L.orc_mc_affine(W, H, arr, i_ref, carr, i_c, ptr(reqs), len(reqs), ptr(out))
         return out[:out_bytes]
 
+    def intra_rmd(self, satd, reqs):
+        """make_ipred_list for every RMD_REQ from the 33 SATDs of row satd_row of satd"""
+        satd = np.ascontiguousarray(satd, dtype=np.uint32)
+        reqs = np.ascontiguousarray(reqs, dtype=RMD_REQ)
+        out = np.zeros(len(reqs), dtype=RMD_OUT)
+        self.L.orc_intra_rmd(ptr(satd), ptr(reqs), len(reqs), ptr(out))
+        return out
+
     def me_affine(self, W, H, org, i_org, plane_ptrs, i_ref, reqs, threads=1):
         """affine gradient searches (affine_me_gradient, with the uni start / bi org of its callers)
         for every AFFME_REQ; plane_ptrs as me_tz (only each slot's integer plane is read)"""
@@ -407,6 +415,14 @@ class RefLib(_Common):
                                   C.c_void_p(reqs.ctypes.data + i * AFFINE_REQ.itemsize), ptr(out))
         return out[:out_bytes]
 
+    def make_ipred_list(self, nb, org, s_org, avail, ipf, req):
+        """the reference's make_ipred_list for one block; returns (RMD_OUT record, satd[33])"""
+        req = np.ascontiguousarray(np.asarray(req).reshape(1), dtype=RMD_REQ)
+        out = np.zeros(1, dtype=RMD_OUT)
+        satd = np.zeros(33, dtype=np.uint32)
+        self.L.refk_make_ipred_list(ptr(nb), C.c_void_p(org), s_org, avail, ipf, ptr(req), ptr(out), ptr(satd))
+        return out[0], satd
+
     def me_affine(self, W, H, org, i_org, plane_ptrs, i_ref, reqs, threads=1):
         """the reference's affine_me_gradient, one call per request (same arguments as Oracle.me_affine)"""
         arr = (C.c_void_p * len(plane_ptrs))(*plane_ptrs)
@@ -469,6 +485,10 @@ MC_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot"
                    ("mv", "<i2", (2, 2)), ("channel", "u1"), ("pad", "u1", (3,)), ("out_offset", "<u4")])
 AFFINE_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)), ("cp_num", "u1"),
                        ("sub8", "u1"), ("pad", "u1", (2,)), ("cpmv", "<i4", (2, 3, 2)), ("out_offset", "<u4")])
+RMD_REQ = np.dtype([("satd_row", "<u4"), ("pb_w", "u1"), ("pb_h", "u1"), ("mpm", "u1", (2,)), ("skip_ipd", "u1"),
+                    ("fast", "u1"), ("range", "<u2"), ("ctx", "<i2", (7,)), ("pad", "u1", (6,)),
+                    ("sqrt_lambda", "<f8"), ("inter_satd", "<u8"), ("satd_threshold", "<f8")])
+RMD_OUT = np.dtype([("list", "i1", (5,)), ("count", "u1"), ("pad", "u1", (2,))])
 AFFME_BI, AFFME_UNI_START, AFFME_SUB8 = 1, 2, 4
 AFFME_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("ref_slot", "u1"), ("refi", "i1"),
                       ("num_refp", "u1"), ("mvr", "u1"), ("flags", "u1"), ("other_slot", "u1"), ("lambda_mv", "<u4"),

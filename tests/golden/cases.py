@@ -511,6 +511,75 @@ def run_affine(B, p, seed):
     return digest(B.mc_affine(p["w"], p["h"], addrs, stride, caddrs, sc, reqs, nbytes))
 
 
+# ------------------------------------------------------------------ intra mode candidates (RMD)
+RMD_SHAPES = [(4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (8, 4), (4, 8), (16, 8), (8, 16), (32, 16), (16, 32),
+              (16, 4), (4, 16), (32, 8), (8, 32), (64, 16), (16, 64), (32, 4), (4, 32), (64, 8), (8, 64)]
+
+
+def rmd_ctx(rng, k):
+    """k intra_dir context models: 10-bit LPS probabilities (not 0) and an MPS bit"""
+    return (rng.integers(8, 1016, k) << 1) | rng.integers(0, 2, k)
+
+
+def rmd_inputs(rng, n):
+    """make_ipred_list calls: block shapes of every aspect (4:1 ones take 4 candidates), fast and
+    full searches, DC / planar / bilinear skipped or not, MPM pairs (equal, IPCM, unsorted), LBAC
+    states, inter SATDs that cut candidates or none; returns (requests, neighbour arrays, org
+    blocks, avail, ipf)"""
+    import pyoracle
+    r = np.zeros(n, dtype=pyoracle.RMD_REQ)
+    nbs, orgs, avails, ipfs = [], [], [], []
+    for i in range(n):
+        w, h = RMD_SHAPES[int(rng.integers(len(RMD_SHAPES)))]
+        r[i]["satd_row"] = i
+        r[i]["pb_w"], r[i]["pb_h"] = w, h
+        m = rng.integers(0, 34, 2)
+        u = rng.random()
+        if u < 0.1:
+            m[1] = m[0]
+        elif u < 0.7:
+            m = np.sort(m)
+        r[i]["mpm"] = m
+        r[i]["skip_ipd"] = int(rng.random() < 0.3)
+        r[i]["fast"] = int(rng.random() < 0.7)
+        r[i]["range"] = int(rng.integers(256, 512))
+        r[i]["ctx"] = rmd_ctx(rng, 7)
+        r[i]["sqrt_lambda"] = float(rng.uniform(4.0, 60.0))
+        r[i]["inter_satd"] = np.iinfo(np.uint64).max if rng.random() < 0.5 else int(rng.integers(1, 40) * w * h)
+        r[i]["satd_threshold"] = float(rng.uniform(0.9, 1.6))
+        nbs.append(nb_array(rng, int(rng.integers(3))))
+        orgs.append(pic(rng, h, w, int(rng.integers(3))))
+        avails.append(int(rng.integers(0, 8)))
+        ipfs.append(int(rng.integers(0, 2)))
+    return r, nbs, orgs, avails, ipfs
+
+
+def rmd_satd(B, reqs, nbs, orgs, avails, ipfs):
+    """the 33 SATDs per block (com_intra_pred + calc_satd_intra) by backend B"""
+    satd = np.zeros((len(reqs), 33), np.uint32)
+    for i in range(len(reqs)):
+        w, h = int(reqs[i]["pb_w"]), int(reqs[i]["pb_h"])
+        d = np.zeros(w * h, np.uint8)
+        for mode in range(33):
+            B.intra_pred(nbs[i], d, mode, w, h, avails[i], ipfs[i])
+            satd[i, mode] = B.satd_intra(w, h, orgs[i].ctypes.data, d.ctypes.data, w, w)
+    return satd
+
+
+def run_rmd(B, p, seed):
+    rng = np.random.default_rng(seed)
+    reqs, nbs, orgs, avails, ipfs = rmd_inputs(rng, p["n"])
+    if hasattr(B, "make_ipred_list"):            # the reference itself, block by block
+        import pyoracle
+        out = np.zeros(len(reqs), dtype=pyoracle.RMD_OUT)
+        for i in range(len(reqs)):
+            out[i], _ = B.make_ipred_list(nbs[i], orgs[i].ctypes.data, int(reqs[i]["pb_w"]), avails[i], ipfs[i],
+                                          reqs[i])
+    else:
+        out = B.intra_rmd(rmd_satd(B, reqs, nbs, orgs, avails, ipfs), reqs)
+    return digest(out.view(np.uint8))
+
+
 # ------------------------------------------------------------------ affine motion search
 def affme_paint(rng, frames, W, H, n=6):
     """flat, one-directional (stripe) and nearly one-directional patches at the same place in
@@ -645,7 +714,7 @@ RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rdoq": run_rdoq,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "rdoq": run_rdoq,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -667,6 +736,9 @@ AFFME_CASES = [
     dict(w=192, h=128, vel=(2.5, -1.25), n=96),
     dict(w=160, h=96, vel=(-3.0, 2.0), n=96, paint=1),
 ]
+
+# intra mode candidate cases (make_ipred_list)
+RMD_CASES = [dict(n=200), dict(n=120)]
 
 # RDOQ cases (transform blocks of every shape, several estimate sets)
 RDOQ_CASES = [dict(n=200, k=4), dict(n=120, k=1)]
@@ -752,6 +824,8 @@ def all_cases():
         add("rdoq", **p)
     for p in AFFME_CASES:
         add("affme", **p)
+    for p in RMD_CASES:
+        add("rmd", **p)
     return cases
 
 

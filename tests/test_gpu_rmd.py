@@ -1,0 +1,90 @@
+"""GPU: intra mode candidates (uavs3e_cuda_intra_rmd*, make_ipred_list src/intra.c:226) bit-exact
+against the reference's golden digests and the oracle restatement, alone and on the intra
+lattice's own SATD records."""
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import cases  # noqa: E402
+
+GOLDEN = [c for c in json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"] if c["kernel"] == "rmd"]
+
+
+def _gpu_rmd_device(gpu, satd, reqs):
+    import torch
+    d_satd = torch.from_numpy(np.ascontiguousarray(satd, dtype=np.uint32).view(np.int32).reshape(-1).copy()).cuda()
+    d_req = torch.from_numpy(np.ascontiguousarray(reqs).view(np.uint8).copy()).cuda()
+    d_out = torch.zeros(max(1, len(reqs)) * gpu.RMD_OUT.itemsize, dtype=torch.uint8, device="cuda")
+    gpu.intra_rmd_device(d_satd.data_ptr(), satd.size // 33, d_req.data_ptr(), len(reqs), d_out.data_ptr())
+    torch.cuda.synchronize()
+    return d_out.cpu().numpy().view(gpu.RMD_OUT)[:len(reqs)]
+
+
+def _assert_same(reqs, want, got):
+    bad = [i for i in range(len(want)) if want[i].tobytes() != got[i].tobytes()]
+    assert not bad, f"{len(bad)} of {len(want)} differ; first: req {reqs[bad[0]]} want {want[bad[0]]} got {got[bad[0]]}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", GOLDEN, ids=[str(c["params"]["n"]) for c in GOLDEN])
+def test_rmd_matches_reference_golden(gpu, oracle, case):
+    reqs, nbs, orgs, avails, ipfs = cases.rmd_inputs(np.random.default_rng(case["seed"]), case["params"]["n"])
+    satd = cases.rmd_satd(oracle, reqs, nbs, orgs, avails, ipfs)
+    assert cases.digest(_gpu_rmd_device(gpu, satd, reqs).view(np.uint8)) == case["md5"]
+    assert cases.digest(gpu.intra_rmd(satd, reqs).view(np.uint8)) == case["md5"]     # host entry
+
+
+@pytest.mark.gpu
+def test_rmd_matches_oracle_many_requests(gpu, oracle):
+    """random SATD rows (ties included) and requests, 40,000 blocks"""
+    rng = np.random.default_rng(88)
+    n = 40000
+    reqs, _, _, _, _ = cases.rmd_inputs(rng, 1)
+    reqs = np.repeat(reqs, n)
+    base, _, _, _, _ = cases.rmd_inputs(np.random.default_rng(89), n)
+    for f in ("pb_w", "pb_h", "mpm", "skip_ipd", "fast", "range", "ctx", "sqrt_lambda", "inter_satd", "satd_threshold"):
+        reqs[f] = base[f]
+    reqs["satd_row"] = rng.integers(0, 5000, n)
+    satd = rng.integers(0, 3000, (5000, 33)).astype(np.uint32)
+    satd[::7] //= 64                      # coarse values: equal costs
+    want = oracle.intra_rmd(satd, reqs)
+    _assert_same(reqs, want, _gpu_rmd_device(gpu, satd, reqs))
+
+
+@pytest.mark.gpu
+def test_rmd_on_lattice_records(gpu, oracle):
+    """the lattice's SATD records of a picture feed the candidate search directly"""
+    from uavs3e_gb300.synth import intra_frame
+    W, H = 256, 128
+    org = intra_frame(W, H, seed=5)
+    rec = intra_frame(W, H, seed=6)
+    cus = gpu.lattice_cus(W, H)
+    satd, _ = gpu.intra_lattice(org, rec, cus, [32], ipf=1)
+    satd = np.asarray(satd, dtype=np.uint32).reshape(-1, 33)
+    reqs, _, _, _, _ = cases.rmd_inputs(np.random.default_rng(90), len(cus))
+    reqs["satd_row"] = np.arange(len(cus))
+    reqs["pb_w"], reqs["pb_h"] = cus["w"], cus["h"]
+    want = oracle.intra_rmd(satd, reqs)
+    _assert_same(reqs, want, _gpu_rmd_device(gpu, satd, reqs))
+
+
+@pytest.mark.gpu
+def test_rmd_out_of_domain_requests(gpu, oracle):
+    reqs, nbs, orgs, avails, ipfs = cases.rmd_inputs(np.random.default_rng(91), 12)
+    satd = cases.rmd_satd(oracle, reqs, nbs, orgs, avails, ipfs)
+    want = oracle.intra_rmd(satd, reqs)
+    bad = reqs.copy()
+    bad[0]["satd_row"] = 12               # past the array
+    bad[1]["pb_w"] = 12                   # not a power of two
+    bad[2]["mpm"][0] = 40                 # no such mode
+    bad[3]["range"] = 200                 # not a coder range
+    bad[4]["ctx"][2] = 3                  # zero LPS range
+    bad[5]["sqrt_lambda"] = -1.0
+    got = _gpu_rmd_device(gpu, satd, bad)
+    assert (got["count"][:6] == 255).all() and (got["list"][:6] == -1).all()
+    _assert_same(reqs[6:], want[6:], got[6:])

@@ -80,6 +80,8 @@ def _declare(L):
     L.uavs3e_cuda_mc_affine_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_rdoq.argtypes = [P, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_me_affine.argtypes = [P, P, I, P, I, P]
+    L.uavs3e_cuda_intra_rmd.argtypes = [P, C.c_size_t, P, I, P]
+    L.uavs3e_cuda_intra_rmd_device.argtypes = [P, C.c_size_t, P, I, P, P]
     L.uavs3e_cuda_me_affine_device.argtypes = [I, I, P, I, P, I, I, I, P, I, P, P]
     L.uavs3e_cuda_rdoq_device.argtypes = [P, I, P, I, P, C.c_size_t, P, P]
 
@@ -484,3 +486,27 @@ def me_affine_device(width, height, d_org, i_org, d_planes, i_ref, pad, d_reqs, 
         stream = torch.cuda.current_stream().cuda_stream
     check(lib().uavs3e_cuda_me_affine_device(width, height, d_org, i_org, arr, len(d_planes) // 16, i_ref, pad, d_reqs,
                                              n, d_out, stream), "me_affine_device")
+
+
+# ------------------------------------------------------------------ intra mode candidates
+RMD_REQ = np.dtype([("satd_row", "<u4"), ("pb_w", "u1"), ("pb_h", "u1"), ("mpm", "u1", (2,)), ("skip_ipd", "u1"),
+                    ("fast", "u1"), ("range", "<u2"), ("ctx", "<i2", (7,)), ("pad", "u1", (6,)),
+                    ("sqrt_lambda", "<f8"), ("inter_satd", "<u8"), ("satd_threshold", "<f8")])
+RMD_OUT = np.dtype([("list", "i1", (5,)), ("count", "u1"), ("pad", "u1", (2,))])
+
+
+def intra_rmd(satd, reqs):
+    """make_ipred_list for every RMD_REQ on host arrays: satd (rows x 33, uint32); returns RMD_OUT"""
+    satd = np.ascontiguousarray(satd, dtype=np.uint32)
+    reqs = np.ascontiguousarray(reqs, dtype=RMD_REQ)
+    out = np.zeros(max(1, len(reqs)), dtype=RMD_OUT)
+    check(lib().uavs3e_cuda_intra_rmd(satd.ctypes.data, satd.size // 33, reqs.ctypes.data, len(reqs),
+                                      out.ctypes.data), "intra_rmd")
+    return out[:len(reqs)]
+
+
+def intra_rmd_device(d_satd, n_rows, d_reqs, n, d_out, stream=None):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_intra_rmd_device(d_satd, n_rows, d_reqs, n, d_out, stream), "intra_rmd_device")

@@ -264,7 +264,7 @@ __device__ __forceinline__ bool ame_cpmv_ok(const s32 (*m)[2])
            m[1][0] >= CPMV_MIN && m[1][0] <= CPMV_MAX && m[1][1] >= CPMV_MIN && m[1][1] <= CPMV_MAX;
 }
 
-__global__ void __launch_bounds__(32 * AME_WARPS, 5) k_me_affine(const AffMeParams P)
+__global__ void __launch_bounds__(32 * AME_WARPS, 20 / AME_WARPS) k_me_affine(const AffMeParams P)
 {
     __shared__ __align__(16) pel s_org[AME_WARPS][64 * 64];
     __shared__ __align__(16) pel s_pred[AME_WARPS][64 * 64];

@@ -23,7 +23,7 @@
 
 namespace uc {
 
-constexpr int TZ_WARPS = 4;
+constexpr int TZ_WARPS = 1;
 constexpr int TZ_KEY_BITS = 20;
 
 struct TzReq {
