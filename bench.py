@@ -717,6 +717,54 @@ def affme_leg(u, torch, stream, flush, with_cpu, reps=10):
     return out
 
 
+def coef_rate_part(u, torch, stream, flush, rreqs, nz, d_levels, levels, with_cpu, reps=10):
+    """the coefficient rate (lbac_enc_run_length_cc_rdo) of every block RDOQ coded, each from a
+    random coder state, on the GPU's RDOQ output"""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import cases
+    rng = np.random.default_rng(41)
+    sel = np.nonzero(nz > 0)[0]
+    r = np.zeros(len(sel), dtype=u.COEF_RATE_REQ)
+    r["coef_offset"] = rreqs["coef_offset"][sel]
+    r["log2w"], r["log2h"] = rreqs["log2w"][sel], rreqs["log2h"][sel]
+    r["ch_type"] = (rreqs["ch_type"][sel] != 0).astype(np.uint8)
+    r["num_sig"] = nz[sel]
+    r["range"] = rng.integers(256, 512, len(r))
+    for f, k in (("run", 12), ("run_rdoq", 12), ("level", 12), ("last1", 6), ("last2", 12)):
+        r[f] = cases.coef_models(rng, k * len(r)).reshape(len(r), k)
+    d_req = torch.from_numpy(r.view(np.uint8).copy()).cuda()
+    d_out = torch.empty(len(r) * u.COEF_RATE_OUT.itemsize, dtype=torch.uint8, device="cuda")
+    sp = stream.cuda_stream
+
+    def run():
+        u.coef_rate_device(d_req.data_ptr(), len(r), d_levels.data_ptr(), levels.size, d_out.data_ptr(), sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / reps
+    got = d_out.cpu().numpy().view(u.COEF_RATE_OUT)
+    out = {"workload": f"lbac_enc_run_length_cc_rdo of the {len(r)} blocks RDOQ coded (their levels, random coder "
+                       "states)", "blocks": len(r), "levels": int(r["num_sig"].sum()), "ms_per_batch": ms,
+           "blocks_per_s": len(r) / (ms / 1000.0), "mean_bits": float(got["bits"].mean())}
+    if with_cpu:
+        import pyoracle
+        t0 = time.perf_counter()
+        pyoracle.Oracle().coef_rate(levels, r)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(r) / dt, "unit": "blocks/s", "cores": 1, "kind": "port",
+                               "sample": f"the whole batch through the oracle restatement (one core), {dt:.2f} s"}
+    return out
+
+
 def rdoq_leg(u, torch, stream, flush, with_cpu, reps=10):
     """RDOQ (quant_non_zero -> rdoq_quant_block) of 60,000 transform blocks of every shape
     4x4..64x64 (DCT2 coefficients of Laplacian residuals, steps 10..60, intra / inter, luma /
@@ -773,6 +821,7 @@ def rdoq_leg(u, torch, stream, flush, with_cpu, reps=10):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": len(reqs) / dt, "unit": "blocks/s", "cores": 1, "kind": "port",
                                "sample": f"the whole batch through the oracle restatement (one core), {dt:.2f} s"}
+    out["rate"] = coef_rate_part(u, torch, stream, flush, reqs, nz, d_coef, c, with_cpu)
     return out
 
 

@@ -309,6 +309,43 @@ UAVS3E_CUDA_API int uavs3e_cuda_mc_affine_device(int width, int height, const ui
                                                  int pad_c, const uavs3e_cuda_affine_req_t *d_reqs, int n,
                                                  uint8_t *d_out, size_t out_bytes, void *stream);
 
+/* ------------------------------------------------------------ coefficient rate */
+
+/*
+ * lbac_enc_run_length_cc_rdo (src/entropy.c:1688-1950): the bits the encoder's RDO counts for a
+ * transform block's levels, for a list of blocks each with the coder state it starts from -- the
+ * range and its channel's context models (the luma or chroma half of lbac->h.run, run_rdoq,
+ * level, last1, last2).  Each result holds the bits counted (the bitcounter increase), the range
+ * and the models after the block, so the caller can go on from that state.  Levels are int16 in
+ * raster order (w x h from coef_offset), e.g. the output of uavs3e_cuda_rdoq.
+ */
+typedef struct {
+    int16_t run[12], run_rdoq[12], level[12], last1[6], last2[12];   /* chroma: last2[0..9] */
+} uavs3e_cuda_coef_ctx_t;
+
+typedef struct {
+    uint32_t coef_offset;     /* first level of the block                                      */
+    uint8_t  log2w, log2h;    /* 2..6 luma, 2..5 chroma                                        */
+    uint8_t  ch_type;         /* 0 luma, 1 chroma                                              */
+    uint8_t  pad;
+    uint16_t num_sig;         /* non-zero levels of the block (>= 1)                           */
+    uint16_t range;           /* coder range, 256..511                                         */
+    uavs3e_cuda_coef_ctx_t ctx;
+} uavs3e_cuda_coef_rate_req_t;
+
+typedef struct {
+    uint32_t bits;            /* bits counted; UINT32_MAX for a request outside the domain     */
+    uint16_t range;           /* (invalid: num_sig above the block's non-zero levels, shapes,  */
+    uint16_t pad;             /* ranges, models with a zero LPS range); state unchanged then   */
+    uavs3e_cuda_coef_ctx_t ctx;
+} uavs3e_cuda_coef_rate_out_t;
+
+UAVS3E_CUDA_API int uavs3e_cuda_coef_rate(const uavs3e_cuda_coef_rate_req_t *reqs, int n, const int16_t *levels,
+                                          size_t n_levels, uavs3e_cuda_coef_rate_out_t *out);
+UAVS3E_CUDA_API int uavs3e_cuda_coef_rate_device(const uavs3e_cuda_coef_rate_req_t *d_reqs, int n,
+                                                 const int16_t *d_levels, size_t n_levels,
+                                                 uavs3e_cuda_coef_rate_out_t *d_out, void *stream);
+
 /* ------------------------------------------------------------ affine motion search */
 
 /*

@@ -1858,6 +1858,127 @@ void orc_mc_affine(int width, int height, const pel *const *planes, int i_ref, c
     }
 }
 
+/* ============================================================ coefficient rate */
+
+/* The context-model update the reference tabulates in tbl_plps / tbl_plps_ext (src/entropy.c:41,
+ * 16,384 entries): a model is (window state c in bits 11-12) | (LPS probability p, 10 bits, in
+ * bits 1-10) | MPS.  The window is 3, 3, 4, 5 for states 0..3.  After an MPS p loses
+ * p >> w + p >> (w + 2) and state 0 becomes 1; after an LPS p gains 197, 95 or 46 (w = 3, 4, 5),
+ * reflected about 1023 with the MPS flipped when it passes it, and the state steps up to 3.
+ * (The rule reproduces all 16,384 entries of the reference's table.) */
+int orc_lbac_next(int model, int mps)
+{
+    const int c = (model >> 11) & 3, w = c < 2 ? 3 : c + 2;
+    int p = (model >> 1) & 1023, m = model & 1;
+    if (mps) {
+        p -= (p >> w) + (p >> (w + 2));
+        return ((c == 0 ? 1 : c) << 11) | (p << 1) | m;
+    }
+    p += w == 3 ? 197 : (w == 4 ? 95 : 46);
+    if (p > 1023) { p = 2047 - p; m ^= 1; }
+    return (MIN(c + 1, 3) << 11) | (p << 1) | m;
+}
+
+/* counting-mode coding of one bin with model *mdl: range, bits, model updated */
+static void crate_bin(u32 *range, u32 *bits, s16 *mdl, int bin)
+{
+    const u32 lps = (u32)(*mdl & 2047) >> 3;
+    u32 mps = *range - lps;
+    const int s = mps < 256;
+    mps |= 0x100;
+    if (bin == (*mdl & 1)) {
+        *bits += s;
+        *range = mps;
+        *mdl = (s16)orc_lbac_next(*mdl, 1);
+    } else {
+        const u32 l = (*range << s) - mps;
+        const int sh = 8 - ilog2((int)l);
+        *range = l << sh;
+        *bits += sh + s;
+        *mdl = (s16)orc_lbac_next(*mdl, 0);
+    }
+}
+
+/* a truncated unary symbol of the run / level coding: the first bin on m[0] ('1' for 0), the
+ * rest on m[1] ('0' per unit, the closing '1' omitted at the cap), as the reference's
+ * counting-mode run and level coders do (src/entropy.c:1715-1782, :1800-1866) */
+static void crate_unary(u32 *range, u32 *bits, s16 *m, int sym, int cap)
+{
+    crate_bin(range, bits, &m[0], sym == 0);
+    if (sym == 0) return;
+    for (int k = 1; k <= sym && k < cap; k++) crate_bin(range, bits, &m[1], k == sym);
+}
+
+/* bits of the exp-Golomb escape of value v (order 0 code of v, with the reference's loop) */
+static u32 crate_egk(int v)
+{
+    int order = 1;
+    for (int s = v; s >= 0; order++) s -= 1 << order;
+    return (u32)((order << 1) - 1);
+}
+
+/* lbac_enc_run_length_cc_rdo (src/entropy.c:1688-1950): for each non-zero level in scan order,
+ * its run of zeros (truncated unary capped at 16 + escape; the run_rdoq models follow the same
+ * run without the cap), its level - 1 (capped at 8 + escape), the sign, and the last flag on the
+ * averaged pair (last1 by the previous level, last2 by log2 of the scan position) */
+static void crate_one(const s16 *coef, const orc_coef_rate_req_t *r, orc_coef_rate_out_t *o)
+{
+    o->ctx = r->ctx;
+    orc_coef_ctx_t *c = &o->ctx;
+    const u16 *scan = orc_scan(r->log2w, r->log2h);
+    const int n = 1 << (r->log2w + r->log2h);
+    u32 range = r->range, bits = 0;
+    int t0 = 10, num_sig = r->num_sig, last = -1, pos = 0;
+    do {
+        while (!coef[scan[pos]]) pos++;
+        const int run = pos - last - 1;
+        last = pos;
+        crate_unary(&range, &bits, &c->run[t0], MIN(run, 16), 16);
+        if (run >= 16) bits += crate_egk(run - 17);
+        /* run_rdoq: the uncapped unary run's model updates, no bits */
+        c->run_rdoq[t0] = (s16)orc_lbac_next(c->run_rdoq[t0], (run == 0) == (c->run_rdoq[t0] & 1));
+        for (int k = 1; k <= run; k++)
+            c->run_rdoq[t0 + 1] = (s16)orc_lbac_next(c->run_rdoq[t0 + 1], (k == run) == (c->run_rdoq[t0 + 1] & 1));
+        const int level = ABSI(coef[scan[pos]]);
+        crate_unary(&range, &bits, &c->level[t0], MIN(level - 1, 8), 8);
+        if (level >= 9) bits += crate_egk(level - 10);
+        bits++;                                                   /* sign */
+        if (pos == n - 1) break;
+        num_sig--;
+        /* last flag on the pair (lbac_encode_binW): the common MPS, or the likelier one */
+        s16 *m1 = &c->last1[t0 >> 1], *m2 = &c->last2[ilog2(pos + 1)];
+        t0 = MIN(level - 1, 5) << 1;
+        const int p1 = (*m1 & 2047) >> 1, p2 = (*m2 & 2047) >> 1, c1 = *m1 & 1, c2 = *m2 & 1;
+        int cm, pl;
+        if (c1 == c2) { cm = c1; pl = (p1 + p2) >> 1; }
+        else if (p1 < p2) { cm = c1; pl = (256 << 2) - 1 - ((p2 - p1) >> 1); }
+        else { cm = c2; pl = (256 << 2) - 1 - ((p1 - p2) >> 1); }
+        const int flag = num_sig == 0;
+        u32 mps = range - ((u32)pl >> 2);
+        const int s = mps < 256;
+        mps |= 0x100;
+        if (flag == cm) { bits += s; range = mps; }
+        else {
+            const u32 l = (range << s) - mps;
+            const int sh = 8 - ilog2((int)l);
+            range = l << sh;
+            bits += sh + s;
+        }
+        *m1 = (s16)orc_lbac_next(*m1, flag == c1);
+        *m2 = (s16)orc_lbac_next(*m2, flag == c2);
+        pos++;
+    } while (num_sig);
+    o->bits = bits;
+    o->range = (u16)range;
+    o->pad = 0;
+}
+
+void orc_coef_rate(const s16 *levels, const orc_coef_rate_req_t *reqs, int n, orc_coef_rate_out_t *out)
+{
+    orc_init();
+    for (int i = 0; i < n; i++) crate_one(levels + reqs[i].coef_offset, &reqs[i], &out[i]);
+}
+
 /* ============================================================ intra mode candidates */
 
 /* one bin of lbac_encode_bin in counting mode (src/entropy.c:1168-1187): the range after it and

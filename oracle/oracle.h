@@ -275,6 +275,35 @@ void orc_mc_cu(int width, int height, const pel *const *planes, int i_ref, const
 void orc_me_tz(const orc_tz_pic_t *pic, const pel *org, int i_org, const pel *const *planes, int i_ref,
                const orc_tz_req_t *reqs, int n, orc_tz_out_t *out, int threads);
 
+/* ------------- coefficient rate (lbac_enc_run_length_cc_rdo, src/entropy.c:1688-1950) ------------- */
+
+/* one transform block's levels coded in counting mode from a coder state: the context models of
+ * its channel (luma or chroma half of run, run_rdoq, level, last1, last2) and the range */
+typedef struct {
+    s16 run[12], run_rdoq[12], level[12], last1[6], last2[12];
+} orc_coef_ctx_t;
+
+typedef struct {
+    u32 coef_offset;    /* first level (s16 index) of the w x h block, raster order                */
+    u8  log2w, log2h;   /* 2..6 (luma) / 2..5 (chroma)                                             */
+    u8  ch_type;        /* 0 luma, 1 chroma                                                        */
+    u8  pad;
+    u16 num_sig;        /* non-zero levels of the block (>= 1)                                     */
+    u16 range;          /* coder range before the block, 256..511                                  */
+    orc_coef_ctx_t ctx; /* context models before the block                                         */
+} orc_coef_rate_req_t;
+
+typedef struct {
+    u32 bits;           /* the bits the block adds (lbac bitcounter)                               */
+    u16 range;          /* range after it                                                          */
+    u16 pad;
+    orc_coef_ctx_t ctx; /* context models after it                                                 */
+} orc_coef_rate_out_t;
+
+void orc_coef_rate(const s16 *levels, const orc_coef_rate_req_t *reqs, int n, orc_coef_rate_out_t *out);
+/* one context-model update of the coder (the reference's tbl_plps / tbl_plps_ext, src/entropy.c:41) */
+int orc_lbac_next(int model, int mps);
+
 /* ------------- intra mode candidates (make_ipred_list, src/intra.c:236-367) ------------- */
 
 /* one prediction block's candidate search: the SATD of each of its 33 modes comes from a

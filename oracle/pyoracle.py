@@ -223,6 +223,17 @@ class Oracle(_Common):
         self.L.orc_mc_affine(W, H, arr, i_ref, carr, i_c, ptr(reqs), len(reqs), ptr(out))
         return out[:out_bytes]
 
+    def coef_rate(self, levels, reqs):
+        """lbac_enc_run_length_cc_rdo for every COEF_RATE_REQ on levels (int16)"""
+        levels = np.ascontiguousarray(levels, dtype=np.int16)
+        reqs = np.ascontiguousarray(reqs, dtype=COEF_RATE_REQ)
+        out = np.zeros(len(reqs), dtype=COEF_RATE_OUT)
+        self.L.orc_coef_rate(ptr(levels), ptr(reqs), len(reqs), ptr(out))
+        return out
+
+    def lbac_next(self, model, mps):
+        return self.L.orc_lbac_next(int(model), int(mps))
+
     def intra_rmd(self, satd, reqs):
         """make_ipred_list for every RMD_REQ from the 33 SATDs of row satd_row of satd"""
         satd = np.ascontiguousarray(satd, dtype=np.uint32)
@@ -415,6 +426,19 @@ class RefLib(_Common):
                                   C.c_void_p(reqs.ctypes.data + i * AFFINE_REQ.itemsize), ptr(out))
         return out[:out_bytes]
 
+    def coef_rate(self, levels, reqs):
+        """the reference's lbac_enc_run_length_cc_rdo, one block per request"""
+        levels = np.ascontiguousarray(levels, dtype=np.int16)
+        reqs = np.ascontiguousarray(reqs, dtype=COEF_RATE_REQ)
+        out = np.zeros(len(reqs), dtype=COEF_RATE_OUT)
+        for i in range(len(reqs)):
+            self.L.refk_coef_rate(ptr(levels), C.c_void_p(reqs.ctypes.data + i * COEF_RATE_REQ.itemsize),
+                                  C.c_void_p(out.ctypes.data + i * COEF_RATE_OUT.itemsize))
+        return out
+
+    def lbac_next(self, model, mps):
+        return self.L.refk_lbac_next(int(model), int(mps))
+
     def make_ipred_list(self, nb, org, s_org, avail, ipf, req):
         """the reference's make_ipred_list for one block; returns (RMD_OUT record, satd[33])"""
         req = np.ascontiguousarray(np.asarray(req).reshape(1), dtype=RMD_REQ)
@@ -485,6 +509,11 @@ MC_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot"
                    ("mv", "<i2", (2, 2)), ("channel", "u1"), ("pad", "u1", (3,)), ("out_offset", "<u4")])
 AFFINE_REQ = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("slot", "i1", (2,)), ("cp_num", "u1"),
                        ("sub8", "u1"), ("pad", "u1", (2,)), ("cpmv", "<i4", (2, 3, 2)), ("out_offset", "<u4")])
+COEF_CTX = [("run", "<i2", (12,)), ("run_rdoq", "<i2", (12,)), ("level", "<i2", (12,)), ("last1", "<i2", (6,)),
+            ("last2", "<i2", (12,))]
+COEF_RATE_REQ = np.dtype([("coef_offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), ("ch_type", "u1"), ("pad", "u1"),
+                          ("num_sig", "<u2"), ("range", "<u2")] + COEF_CTX)
+COEF_RATE_OUT = np.dtype([("bits", "<u4"), ("range", "<u2"), ("pad", "<u2")] + COEF_CTX)
 RMD_REQ = np.dtype([("satd_row", "<u4"), ("pb_w", "u1"), ("pb_h", "u1"), ("mpm", "u1", (2,)), ("skip_ipd", "u1"),
                     ("fast", "u1"), ("range", "<u2"), ("ctx", "<i2", (7,)), ("pad", "u1", (6,)),
                     ("sqrt_lambda", "<f8"), ("inter_satd", "<u8"), ("satd_threshold", "<f8")])

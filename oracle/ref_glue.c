@@ -474,3 +474,52 @@ void refk_rdoq_est_from_ctx(const u16 *ctx, glue_rdoq_est_t *E)
     memcpy(E->lvl, core->rdoq_bin_est_lvl, sizeof(E->lvl));
     memcpy(E->lst, core->rdoq_bin_est_lst, sizeof(E->lst));
 }
+
+/* ---- 8. coefficient rate ------------------------------------------------------------------
+ * lbac_enc_run_length_cc_rdo (src/entropy.c:1688) for one block: a reset coder (lbac_reset,
+ * every context at PROB_INIT) takes the request's range and its channel's context models, codes
+ * the block's levels, and the bits it counted, its range and those models come back.  Layout of
+ * req / out: orc_coef_rate_req_t / orc_coef_rate_out_t (oracle.h). */
+typedef struct { s16 run[12], run_rdoq[12], level[12], last1[6], last2[12]; } glue_coef_ctx_t;
+typedef struct { u32 coef_offset; u8 log2w, log2h, ch_type, pad; u16 num_sig, range; glue_coef_ctx_t ctx; } glue_coef_rate_req_t;
+typedef struct { u32 bits; u16 range, pad; glue_coef_ctx_t ctx; } glue_coef_rate_out_t;
+
+void lbac_enc_run_length_cc_rdo(lbac_t *lbac, s16 *coef, int log2_w, int log2_h, int num_sig, int ch_type);
+void lbac_encode_bin_for_rdoq(u32 bin, lbac_ctx_model_t *model);
+
+void refk_coef_rate(s16 *levels, const glue_coef_rate_req_t *rq, glue_coef_rate_out_t *out)
+{
+    refk_init();
+    static lbac_t lb;
+    memset(&lb, 0, sizeof(lb));
+    lbac_ctx_init(&lb.h);
+    lbac_reset(&lb);
+    lb.range = rq->range;
+    const int c = rq->ch_type ? 1 : 0;
+    for (int i = 0; i < 12; i++) {
+        lb.h.run[c * 12 + i] = rq->ctx.run[i];
+        lb.h.run_rdoq[c * 12 + i] = rq->ctx.run_rdoq[i];
+        lb.h.level[c * 12 + i] = rq->ctx.level[i];
+    }
+    for (int i = 0; i < 6; i++) lb.h.last1[c * 6 + i] = rq->ctx.last1[i];
+    for (int i = 0; i < (c ? 10 : 12); i++) lb.h.last2[c * 12 + i] = rq->ctx.last2[i];
+    lbac_enc_run_length_cc_rdo(&lb, levels + rq->coef_offset, rq->log2w, rq->log2h, rq->num_sig, c);
+    out->bits = lb.bitcounter;
+    out->range = (u16)lb.range;
+    out->pad = 0;
+    for (int i = 0; i < 12; i++) {
+        out->ctx.run[i] = lb.h.run[c * 12 + i];
+        out->ctx.run_rdoq[i] = lb.h.run_rdoq[c * 12 + i];
+        out->ctx.level[i] = lb.h.level[c * 12 + i];
+    }
+    for (int i = 0; i < 6; i++) out->ctx.last1[i] = lb.h.last1[c * 6 + i];
+    for (int i = 0; i < 12; i++) out->ctx.last2[i] = (c && i >= 10) ? rq->ctx.last2[i] : lb.h.last2[c * 12 + i];
+}
+
+/* one entry of the reference's context-model transition table: MPS (mps = 1) or LPS */
+int refk_lbac_next(int model, int mps)
+{
+    s16 m = (s16)model;
+    lbac_encode_bin_for_rdoq(mps ? (u32)(m & 1) : (u32)!(m & 1), &m);
+    return m;
+}

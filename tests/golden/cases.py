@@ -511,6 +511,55 @@ def run_affine(B, p, seed):
     return digest(B.mc_affine(p["w"], p["h"], addrs, stride, caddrs, sc, reqs, nbytes))
 
 
+# ------------------------------------------------------------------ coefficient rate
+def coef_models(rng, k):
+    """k context models: window state 0..3, LPS probability 4..1023, MPS bit"""
+    return ((rng.integers(0, 4, k) << 11) | (rng.integers(4, 1024, k) << 1) | rng.integers(0, 2, k)).astype(np.int16)
+
+
+def coef_rate_inputs(rng, n):
+    """blocks of levels for lbac_enc_run_length_cc_rdo: luma 4x4..64x64 and chroma 4x4..32x32,
+    sparse low-frequency levels (long runs, escapes of runs >= 16 and levels >= 9, a level alone
+    at the last scan position), random coder states; returns (levels, requests)"""
+    import pyoracle
+    r = np.zeros(n, dtype=pyoracle.COEF_RATE_REQ)
+    blocks, off = [], 0
+    for i in range(n):
+        ch = int(rng.random() < 0.3)
+        top = 5 if ch else 6
+        lw, lh = int(rng.integers(2, top + 1)), int(rng.integers(2, top + 1))
+        w, h = 1 << lw, 1 << lh
+        kind = rng.random()
+        lev = np.zeros((h, w), np.int64)
+        if kind < 0.1:                                # only the last scan position
+            scan = np.frombuffer(np.ctypeslib.as_array(pyoracle.Oracle().L.orc_scan(lw, lh), (w * h,)).tobytes(),
+                                 np.uint16)
+            lev.flat[scan[-1]] = int(rng.integers(1, 40)) * (1 if rng.random() < 0.5 else -1)
+        else:
+            dens = rng.uniform(0.02, 0.5)
+            yy, xx = np.mgrid[0:h, 0:w]
+            p = dens * np.exp(-(xx + yy) / max(2.0, rng.uniform(1.0, 0.5 * (w + h))))
+            mask = rng.random((h, w)) < p
+            if not mask.any():
+                mask[0, 0] = True
+            mag = np.where(rng.random((h, w)) < 0.1, rng.integers(9, 600, (h, w)), rng.integers(1, 9, (h, w)))
+            lev = np.where(mask, mag * np.where(rng.random((h, w)) < 0.5, 1, -1), 0)
+        blocks.append(lev.astype(np.int16).ravel())
+        r[i]["coef_offset"] = off
+        off += w * h
+        r[i]["log2w"], r[i]["log2h"], r[i]["ch_type"] = lw, lh, ch
+        r[i]["num_sig"] = int(np.count_nonzero(lev))
+        r[i]["range"] = int(rng.integers(256, 512))
+        for f, k in (("run", 12), ("run_rdoq", 12), ("level", 12), ("last1", 6), ("last2", 12)):
+            r[i][f] = coef_models(rng, k)
+    return np.concatenate(blocks), r
+
+
+def run_coef_rate(B, p, seed):
+    levels, reqs = coef_rate_inputs(np.random.default_rng(seed), p["n"])
+    return digest(B.coef_rate(levels, reqs).view(np.uint8))
+
+
 # ------------------------------------------------------------------ intra mode candidates (RMD)
 RMD_SHAPES = [(4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (8, 4), (4, 8), (16, 8), (8, 16), (32, 16), (16, 32),
               (16, 4), (4, 16), (32, 8), (8, 32), (64, 16), (16, 64), (32, 4), (4, 32), (64, 8), (8, 64)]
@@ -714,7 +763,7 @@ RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "rdoq": run_rdoq,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "coef_rate": run_coef_rate, "rdoq": run_rdoq,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -736,6 +785,9 @@ AFFME_CASES = [
     dict(w=192, h=128, vel=(2.5, -1.25), n=96),
     dict(w=160, h=96, vel=(-3.0, 2.0), n=96, paint=1),
 ]
+
+# coefficient rate cases (lbac_enc_run_length_cc_rdo)
+COEF_RATE_CASES = [dict(n=200), dict(n=150)]
 
 # intra mode candidate cases (make_ipred_list)
 RMD_CASES = [dict(n=200), dict(n=120)]
@@ -826,6 +878,8 @@ def all_cases():
         add("affme", **p)
     for p in RMD_CASES:
         add("rmd", **p)
+    for p in COEF_RATE_CASES:
+        add("coef_rate", **p)
     return cases
 
 

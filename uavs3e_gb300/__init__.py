@@ -81,6 +81,8 @@ def _declare(L):
     L.uavs3e_cuda_rdoq.argtypes = [P, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_me_affine.argtypes = [P, P, I, P, I, P]
     L.uavs3e_cuda_intra_rmd.argtypes = [P, C.c_size_t, P, I, P]
+    L.uavs3e_cuda_coef_rate.argtypes = [P, I, P, C.c_size_t, P]
+    L.uavs3e_cuda_coef_rate_device.argtypes = [P, I, P, C.c_size_t, P, P]
     L.uavs3e_cuda_intra_rmd_device.argtypes = [P, C.c_size_t, P, I, P, P]
     L.uavs3e_cuda_me_affine_device.argtypes = [I, I, P, I, P, I, I, I, P, I, P, P]
     L.uavs3e_cuda_rdoq_device.argtypes = [P, I, P, I, P, C.c_size_t, P, P]
@@ -510,3 +512,28 @@ def intra_rmd_device(d_satd, n_rows, d_reqs, n, d_out, stream=None):
         import torch
         stream = torch.cuda.current_stream().cuda_stream
     check(lib().uavs3e_cuda_intra_rmd_device(d_satd, n_rows, d_reqs, n, d_out, stream), "intra_rmd_device")
+
+
+# ------------------------------------------------------------------ coefficient rate
+COEF_CTX = [("run", "<i2", (12,)), ("run_rdoq", "<i2", (12,)), ("level", "<i2", (12,)), ("last1", "<i2", (6,)),
+            ("last2", "<i2", (12,))]
+COEF_RATE_REQ = np.dtype([("coef_offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), ("ch_type", "u1"), ("pad", "u1"),
+                          ("num_sig", "<u2"), ("range", "<u2")] + COEF_CTX)
+COEF_RATE_OUT = np.dtype([("bits", "<u4"), ("range", "<u2"), ("pad", "<u2")] + COEF_CTX)
+
+
+def coef_rate(levels, reqs):
+    """lbac_enc_run_length_cc_rdo for every COEF_RATE_REQ on host levels (int16); returns COEF_RATE_OUT"""
+    levels = np.ascontiguousarray(levels, dtype=np.int16)
+    reqs = np.ascontiguousarray(reqs, dtype=COEF_RATE_REQ)
+    out = np.zeros(max(1, len(reqs)), dtype=COEF_RATE_OUT)
+    check(lib().uavs3e_cuda_coef_rate(reqs.ctypes.data, len(reqs), levels.ctypes.data, levels.size, out.ctypes.data),
+          "coef_rate")
+    return out[:len(reqs)]
+
+
+def coef_rate_device(d_reqs, n, d_levels, n_levels, d_out, stream=None):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    check(lib().uavs3e_cuda_coef_rate_device(d_reqs, n, d_levels, n_levels, d_out, stream), "coef_rate_device")

@@ -45,6 +45,8 @@ int launch_mc_cu(int W, int H, const uint8_t *const *planes, int n_slots, int i_
 int launch_mc_affine(int W, int H, const uint8_t *const *planes, int n_slots, int i_ref, int pad,
                      const uint8_t *const *chroma, int i_c, int pad_c, const void *reqs, int n, uint8_t *out,
                      unsigned long long out_bytes, cudaStream_t st);
+int launch_coef_rate(const void *reqs, int n, const int16_t *levels, unsigned long long n_levels, void *out,
+                     cudaStream_t st);
 int launch_intra_rmd(const uint32_t *satd, unsigned long long n_rows, const void *reqs, int n, void *out,
                      cudaStream_t st);
 int launch_me_affine(int W, int H, const uint8_t *org, int i_org, const uint8_t *const *planes, int n_slots,
