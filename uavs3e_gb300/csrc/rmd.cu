@@ -7,8 +7,9 @@
 // src/entropy.c:2118; lbac_encode_bin :1168) from the block's coder state (range and the 7
 // intra_dir context models), which is the part of the rate estimation this decision needs.
 //
-// One thread per block: the decision is a short sequential chain over at most 33 candidates.
-// Costs are non-negative doubles, so the list's comparisons run on their bit patterns.
+// One thread per block: the decision is a short sequential chain over at most 33 candidates; its
+// list and per-mode costs live in shared memory.  Costs are non-negative doubles, so the list's
+// comparisons run on their bit patterns.
 #include "common.cuh"
 #include "uavs3e_cuda_internal.h"
 #include "../../include/uavs3e_cuda.h"
@@ -64,9 +65,17 @@ __device__ __forceinline__ int rmd_bits(const RmdReq &q, int ipm)
     return bits;
 }
 
+constexpr int RMD_THREADS = 128;
+
+// a thread's candidate list and per-mode costs (bit patterns of the non-negative double costs),
+// in shared memory, mode-major so that the threads of a warp touch consecutive words
 struct RmdState {
-    int list[33];
-    unsigned long long cost[33];     // bit patterns of the (non-negative) double costs
+    unsigned long long (*cost)[RMD_THREADS];
+    s8 (*list)[RMD_THREADS];
+    int t;
+    __device__ int l(int k) const { return list[k][t]; }
+    __device__ void set_l(int k, int v) { list[k][t] = (s8)v; }
+    __device__ unsigned long long c(int m) const { return cost[m][t]; }
 };
 
 // check_one_mode + com_update_cand_list (src/intra.c:187-224)
@@ -74,19 +83,21 @@ __device__ void rmd_check(RmdState &S, const RmdReq &q, const u32 *satd, int ipm
 {
     const double c = __dadd_rn((double)satd[ipm], __dmul_rn((double)rmd_bits(q, ipm), q.sqrt_lambda));
     const unsigned long long cb = (unsigned long long)__double_as_longlong(c);
-    S.cost[ipm] = cb;
+    S.cost[ipm][S.t] = cb;
     int shift = 0, p = len - 1;
-    while (shift < len && (S.list[p] < 0 || cb < S.cost[S.list[p]])) { p--; shift++; }
+    while (shift < len && (S.l(p) < 0 || cb < S.c(S.l(p)))) { p--; shift++; }
     if (shift) {
         int k = len - 1;
-        for (shift--; shift; shift--, k--) S.list[k] = S.list[k - 1];
-        S.list[k] = ipm;
+        for (shift--; shift; shift--, k--) S.set_l(k, S.l(k - 1));
+        S.set_l(k, ipm);
     }
 }
 
-__global__ void __launch_bounds__(128) k_intra_rmd(const u32 *satd_all, unsigned long long n_rows, const RmdReq *reqs,
-                                                   int n, RmdOut *out)
+__global__ void __launch_bounds__(RMD_THREADS) k_intra_rmd(const u32 *satd_all, unsigned long long n_rows,
+                                                           const RmdReq *reqs, int n, RmdOut *out)
 {
+    __shared__ unsigned long long s_cost[33][RMD_THREADS];
+    __shared__ s8 s_list[33][RMD_THREADS];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const RmdReq q = reqs[i];
@@ -106,7 +117,10 @@ __global__ void __launch_bounds__(128) k_intra_rmd(const u32 *satd_all, unsigned
     }
     const u32 *satd = satd_all + (size_t)q.satd_row * 33;
     RmdState S;
-    for (int k = 0; k < 33; k++) { S.list[k] = -1; S.cost[k] = RMD_MAX_COST; }
+    S.cost = s_cost;
+    S.list = s_list;
+    S.t = threadIdx.x;
+    for (int k = 0; k < 33; k++) { S.set_l(k, -1); s_cost[k][S.t] = RMD_MAX_COST; }
     int cnt = (w >= h * 4 || h >= w * 4) ? 4 : 5;
     if (q.fast) {
         const int r4[10] = { 0, 1, 2, 6, 10, 14, 18, 22, 26, 30 };
@@ -115,7 +129,7 @@ __global__ void __launch_bounds__(128) k_intra_rmd(const u32 *satd_all, unsigned
         for (int k = q.skip_ipd ? 3 : 0; k < 10; k++) rmd_check(S, q, satd, r4[k], k + 1);
         int r2[12], n2 = 0;
         for (int k = 0; k < 7; k++) {
-            const int ipm = S.list[k];
+            const int ipm = S.l(k);
             if (ipm >= 6) {
                 if (!(map >> (ipm - 2) & 1)) { r2[n2++] = ipm - 2; map |= 1ull << (ipm - 2); }
                 if (!(map >> (ipm + 2) & 1)) { r2[n2++] = ipm + 2; map |= 1ull << (ipm + 2); }
@@ -124,7 +138,7 @@ __global__ void __launch_bounds__(128) k_intra_rmd(const u32 *satd_all, unsigned
         for (int k = 0; k < n2; k++) rmd_check(S, q, satd, r2[k], max(cnt, 3));
         int r1[8], n1 = 0;
         for (int k = 0, j = 0; k < 3 && j < 10;) {
-            const int ipm = S.list[j++];
+            const int ipm = S.l(j++);
             if (ipm >= 4) {
                 k++;
                 if (!(map >> (ipm - 1) & 1)) { r1[n1++] = ipm - 1; map |= 1ull << (ipm - 1); }
@@ -143,24 +157,24 @@ __global__ void __launch_bounds__(128) k_intra_rmd(const u32 *satd_all, unsigned
     int need0 = q.mpm[0] != 33 && !(q.skip_ipd && q.mpm[0] <= 2);
     int need1 = q.mpm[1] != 33 && !(q.skip_ipd && q.mpm[1] <= 2);
     for (int k = 0; k < cnt; k++) {
-        if (need0 && S.list[k] == q.mpm[0]) need0 = 0;
-        if (need1 && S.list[k] == q.mpm[1]) need1 = 0;
+        if (need0 && S.l(k) == q.mpm[0]) need0 = 0;
+        if (need1 && S.l(k) == q.mpm[1]) need1 = 0;
     }
     if (need0 && need1) {
-        const bool first = S.cost[q.mpm[0]] <= S.cost[q.mpm[1]];
-        S.list[cnt - 2] = first ? q.mpm[0] : q.mpm[1];
-        S.list[cnt - 1] = first ? q.mpm[1] : q.mpm[0];
+        const bool first = S.c(q.mpm[0]) <= S.c(q.mpm[1]);
+        S.set_l(cnt - 2, first ? q.mpm[0] : q.mpm[1]);
+        S.set_l(cnt - 1, first ? q.mpm[1] : q.mpm[0]);
     } else if (need0 || need1) {
         const int add = need0 ? 0 : 1;
-        if (S.list[cnt - 1] == q.mpm[1 - add]) S.list[cnt - 2] = S.list[cnt - 1];
-        S.list[cnt - 1] = q.mpm[add];
+        if (S.l(cnt - 1) == q.mpm[1 - add]) S.set_l(cnt - 2, S.l(cnt - 1));
+        S.set_l(cnt - 1, q.mpm[add]);
     }
     // candidates costlier than the inter SATD x threshold leave from the end
     if (q.inter_satd != ~0ull) {
         const double lim = __dmul_rn((double)q.inter_satd, q.satd_threshold);
-        while (cnt > 0 && S.list[cnt - 1] >= 0 && __longlong_as_double((long long)S.cost[S.list[cnt - 1]]) > lim) cnt--;
+        while (cnt > 0 && S.l(cnt - 1) >= 0 && __longlong_as_double((long long)S.c(S.l(cnt - 1))) > lim) cnt--;
     }
-    for (int k = 0; k < 5; k++) o.list[k] = (s8)S.list[k];
+    for (int k = 0; k < 5; k++) o.list[k] = (s8)S.l(k);
     o.count = (u8)cnt;
     out[i] = o;
 }
@@ -169,7 +183,9 @@ int launch_intra_rmd(const u32 *satd, unsigned long long n_rows, const void *req
 {
     if (!satd || n < 0 || (n > 0 && (!reqs || !out))) return set_status(UC_ERR_ARG, "intra_rmd: null argument");
     if (n == 0) return UC_OK;
-    k_intra_rmd<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(satd, n_rows, (const RmdReq *)reqs, n, (RmdOut *)out);
+    k_intra_rmd<<<(unsigned)((n + RMD_THREADS - 1) / RMD_THREADS), RMD_THREADS, 0, st>>>(satd, n_rows,
+                                                                                       (const RmdReq *)reqs, n,
+                                                                                       (RmdOut *)out);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     return UC_OK;
