@@ -301,9 +301,66 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
                                        f"{sm_count} SMs x {sm_mhz:.0f} MHz; matrix-form transform multiply-adds only "
                                        f"(prediction, SATD, quantisation not counted)"}}
     out["rmd"] = rmd_part(u, torch, stream, flush, d_satd, cus, with_cpu)
+    out["intra_decision"] = intra_decision_part(u, torch, stream, flush, d_org, d_rec, d_cus, cus, qps)
     if with_cpu:
         out["cpu_baseline"] = lattice_cpu_baseline(org, rec, cus)
     return out
+
+
+def intra_decision_part(u, torch, stream, flush, d_org, d_rec, d_cus, cus, qps, reps=5):
+    """the encoder's order on the lattice: SATD of every mode (no transforms), make_ipred_list per
+    CU (I-slice: no inter cut), then the transform / quantisation records of each CU's listed
+    modes only"""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import cases
+    n = len(cus)
+    lib = u.lib()
+    sp = stream.cuda_stream
+    reqs, _, _, _, _ = cases.rmd_inputs(np.random.default_rng(37), 1)
+    reqs = np.repeat(reqs, n)
+    rng = np.random.default_rng(38)
+    reqs["satd_row"] = np.arange(n)
+    reqs["pb_w"], reqs["pb_h"] = cus["w"], cus["h"]
+    reqs["mpm"] = np.sort(rng.integers(0, 33, (n, 2)), axis=1)
+    reqs["skip_ipd"] = 0
+    reqs["fast"] = 1
+    reqs["range"] = rng.integers(256, 512, n)
+    reqs["ctx"] = cases.rmd_ctx(rng, 7 * n).reshape(n, 7)
+    reqs["sqrt_lambda"] = 30.0
+    reqs["inter_satd"] = np.iinfo(np.uint64).max
+    d_req = torch.from_numpy(reqs.view(np.uint8).copy()).cuda()
+    d_satd = torch.empty(n * 33, dtype=torch.int32, device="cuda")
+    d_lists = torch.empty(n * u.RMD_OUT.itemsize, dtype=torch.uint8, device="cuda")
+    d_satd5 = torch.empty(n * 33, dtype=torch.int32, device="cuda")
+    d_q5 = torch.empty(n * 33 * len(qps) * 16, dtype=torch.uint8, device="cuda")
+    fn = lib.uavs3e_cuda_intra_lattice_modes_device
+
+    def run():
+        u.check(fn(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H, d_cus.data_ptr(), n, None, 33, 1, None, 0, 1,
+                   d_satd.data_ptr(), None, sp), "intra_lattice (SATD)")
+        u.intra_rmd_device(d_satd.data_ptr(), n, d_req.data_ptr(), n, d_lists.data_ptr(), sp)
+        lists = d_lists.view(torch.int8).view(n, u.RMD_OUT.itemsize)[:, :5].to(torch.int16)
+        modes = torch.where(lists < 0, lists[:, :1], lists).to(torch.uint8).contiguous()
+        u.check(fn(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H, d_cus.data_ptr(), n, modes.data_ptr(), 5, 1,
+                   qps.ctypes.data, len(qps), 1, d_satd5.data_ptr(), d_q5.data_ptr(), sp), "intra_lattice (lists)")
+
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            run()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            run()
+            e1.record(stream)
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / reps
+    counts = d_lists.view(n, u.RMD_OUT.itemsize)[:, 5].cpu().numpy()
+    return {"workload": "1080p intra decision in the encoder's order: SATD of the 33 modes of every lattice CU, "
+                        "make_ipred_list (fast RMD), then transform + 4-QP quantisation records of the listed modes",
+            "ms_per_frame": ms, "frames_per_s": 1000.0 / ms, "mean_candidates": float(counts.mean())}
 
 
 def rmd_part(u, torch, stream, flush, d_satd, cus, with_cpu, reps=10):

@@ -486,7 +486,8 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_rmd_device(const uint32_t *d_satd, size_t 
  * cap records to out (may be NULL) and returns the total count. */
 UAVS3E_CUDA_API int uavs3e_cuda_lattice_cus(int width, int height, uavs3e_cuda_cu_t *out, int cap);
 
-/* device buffers in and out, enqueued on `stream`; qps is a host array */
+/* device buffers in and out, enqueued on `stream`; qps is a host array.  n_qp = 0 writes the SATD
+ * records only (no transform stage; d_q may be NULL): the input of uavs3e_cuda_intra_rmd. */
 UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i_org, const uint8_t *d_rec, int i_rec,
                                                      int width, int height, const uavs3e_cuda_cu_t *d_cus, int n_cus,
                                                      int ipf, const int *qps, int n_qp, int is_intra_slice,

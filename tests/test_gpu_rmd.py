@@ -88,3 +88,55 @@ def test_rmd_out_of_domain_requests(gpu, oracle):
     got = _gpu_rmd_device(gpu, satd, bad)
     assert (got["count"][:6] == 255).all() and (got["list"][:6] == -1).all()
     _assert_same(reqs[6:], want[6:], got[6:])
+
+
+@pytest.mark.gpu
+def test_intra_decision_pipeline(gpu, oracle):
+    """SATD-only lattice -> candidate lists -> lattice over each CU's list: the SATD records equal
+    the full lattice's, the lists the oracle's, and the list modes' records the full lattice's"""
+    import ctypes as C
+
+    import torch
+    from uavs3e_gb300.synth import intra_frame
+    W, H = 160, 96
+    org = intra_frame(W, H, seed=11)
+    rec = np.clip(org.astype(int) + np.random.default_rng(11).integers(-4, 5, org.shape), 0, 255).astype(np.uint8)
+    cus = gpu.lattice_cus(W, H)
+    n = len(cus)
+    qps = [27, 37]
+    satd_all, q_all = gpu.intra_lattice(org, rec, cus, qps, ipf=1)
+    L = gpu.lib()
+    P, I = C.c_void_p, C.c_int
+    L.uavs3e_cuda_intra_lattice_modes_device.argtypes = [P, I, P, I, I, I, P, I, P, I, I, P, I, I, P, P, P]
+    d_org = torch.from_numpy(org).cuda()
+    d_rec = torch.from_numpy(rec).cuda()
+    d_cus = torch.from_numpy(cus.view(np.uint8).copy()).cuda()
+    d_satd = torch.zeros(n * 33, dtype=torch.int32, device="cuda")
+    sp = torch.cuda.current_stream().cuda_stream
+    assert L.uavs3e_cuda_intra_lattice_modes_device(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H, d_cus.data_ptr(),
+                                                    n, None, 33, 1, None, 0, 1, d_satd.data_ptr(), None, sp) == 0
+    torch.cuda.synchronize()
+    satd0 = d_satd.cpu().numpy().view(np.uint32).reshape(n, 33)
+    assert np.array_equal(satd0, satd_all.reshape(n, 33).view(np.uint32))
+    reqs, _, _, _, _ = cases.rmd_inputs(np.random.default_rng(12), n)
+    reqs["satd_row"] = np.arange(n)
+    reqs["pb_w"], reqs["pb_h"] = cus["w"], cus["h"]
+    reqs["inter_satd"] = np.iinfo(np.uint64).max
+    lists = gpu.intra_rmd(satd0, reqs)
+    assert lists.tobytes() == oracle.intra_rmd(satd0, reqs).tobytes()
+    modes = lists["list"].astype(np.int16).copy()
+    for k in range(1, 5):
+        modes[:, k] = np.where(modes[:, k] < 0, modes[:, 0], modes[:, k])
+    modes = modes.astype(np.uint8)
+    d_modes = torch.from_numpy(modes.copy()).cuda()
+    d_satd5 = torch.full((n * 33,), -1, dtype=torch.int32, device="cuda")
+    d_q5 = torch.zeros(n * 33 * len(qps) * gpu.LAT_Q.itemsize, dtype=torch.uint8, device="cuda")
+    q = np.array(qps, np.int32)
+    assert L.uavs3e_cuda_intra_lattice_modes_device(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H, d_cus.data_ptr(),
+                                                    n, d_modes.data_ptr(), 5, 1, q.ctypes.data, len(qps), 1,
+                                                    d_satd5.data_ptr(), d_q5.data_ptr(), sp) == 0
+    torch.cuda.synchronize()
+    q5 = d_q5.cpu().numpy().view(gpu.LAT_Q).reshape(n, 33, len(qps))
+    sel = np.zeros((n, 33), bool)
+    np.put_along_axis(sel, modes.astype(int), True, 1)
+    assert np.array_equal(q5[sel], q_all.reshape(n, 33, len(qps))[sel])

@@ -184,7 +184,8 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "intra_lattice: device index");
     const DevTables *tab = device_tables(dev);
     if (!tab) return set_status(UC_ERR_MEMORY, "intra_lattice: table upload failed");
-    if (n_qp < 1 || n_qp > LAT_MAX_QP || n_cus < 0) return set_status(UC_ERR_ARG, "intra_lattice: bad qp count");
+    if (n_qp < 0 || n_qp > LAT_MAX_QP || n_cus < 0 || (n_qp > 0 && !q_out))
+        return set_status(UC_ERR_ARG, "intra_lattice: bad qp count");
     if (n_modes < 1 || n_modes > 33 || (!modes && n_modes != 33))
         return set_status(UC_ERR_ARG, "intra_lattice: mode list");
     for (int i = 0; i < n_qp; i++)
@@ -238,7 +239,7 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
                 std::lock_guard<std::mutex> lk(T.mu);
                 if (T.budget[n_modes][c]) {
                     budget = T.budget[n_modes][c];
-                } else if (g_tune_on && n >= LAT_TUNE_MIN_CUS) {
+                } else if (g_tune_on && n >= LAT_TUNE_MIN_CUS && n_qp > 0) {   // SATD-only runs keep the default
                     int best = LAT_BUDGET;
                     int r = lat_tune_shape(lw, lh, n, P, st, &launches, &best);
                     if (r) return r;
@@ -309,7 +310,8 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_modes_device(const uint8_t *d_org,
 {
     int r = ensure_init();
     if (r) return r;
-    if (!d_org || !d_rec || !d_cus || !d_satd || !d_q || !qps) return set_status(UC_ERR_ARG, "intra_lattice: null pointer");
+    if (!d_org || !d_rec || !d_cus || !d_satd || (n_qp > 0 && (!d_q || !qps)))
+        return set_status(UC_ERR_ARG, "intra_lattice: null pointer");
     if (width % 4 || height % 4) return set_status(UC_ERR_ARG, "intra_lattice: picture size must be a multiple of 4");
     return launch_intra_lattice(d_org, i_org, d_rec, i_rec, width, height, (const LatCu *)d_cus, n_cus, d_modes, n_modes,
                                 ipf, qps, n_qp, is_intra_slice, d_satd, (LatQ *)d_q, (cudaStream_t)stream);

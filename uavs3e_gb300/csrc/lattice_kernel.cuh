@@ -383,8 +383,9 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
         const int avail = (cu.y > 0 ? 1 : 0) | (cu.x > 0 ? 2 : 0) | ((cu.x > 0 && cu.y > 0) ? 4 : 0);
         ipred_block_setup(cub + tid * L.cu_bytes + L.c_nb + 288, w, h, avail, 8, sB[tid]);
     }
-    // org part of the forward row pass: Torg[y][u] = sum_x Fw[u][x] org[y][x]
-    for (int i = tid; i < Gv * kw * h; i += LAT_THREADS) {
+    // org part of the forward row pass: Torg[y][u] = sum_x Fw[u][x] org[y][x] (no transform
+    // stage runs when no QP is asked: SATD records only)
+    for (int i = tid; i < (P.n_qp > 0 ? Gv * kw * h : 0); i += LAT_THREADS) {
         const int u = i & (kw - 1), y = (i >> lkw) & (h - 1), g = i >> (lkw + lh);
         const u8 *c = cub + g * L.cu_bytes;
         const u32 *o = (const u32 *)(c + L.c_org + y * L.ps), *f = fw + u * L.fw_ws;
@@ -422,7 +423,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     }
     {
         const int sh1 = lw - 2, rnd1 = sh1 > 0 ? 1 << (sh1 - 1) : 0;
-        for (int i = tid; i < J * NYC * KW_; i += LAT_THREADS) {
+        for (int i = tid; i < (P.n_qp > 0 ? J * NYC * KW_ : 0); i += LAT_THREADS) {
             const int u = i & (KW_ - 1), yc = (i >> LKW_) % NYC, j = i / (KW_ * NYC);
             u32 f[W_ / 4];
 #pragma unroll
@@ -460,7 +461,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
             nz_thr[q] = ((((1 << q_bits) - offset) << 10) / q_value - 1) >> 10;
         }
         const int sh2 = lh + 5, rnd2 = 1 << (sh2 - 1);
-        for (int i = tid; i < J * NUC * KH_; i += LAT_THREADS) {
+        for (int i = tid; i < (P.n_qp > 0 ? J * NUC * KH_ : 0); i += LAT_THREADS) {
             const int v = i & (KH_ - 1), uc = (i >> LKH_) % NUC, j = i / (KH_ * NUC);
             u32 f[H_ / 4];
 #pragma unroll
