@@ -317,7 +317,9 @@ UAVS3E_CUDA_API int uavs3e_cuda_mc_affine_device(int width, int height, const ui
  * range and its channel's context models (the luma or chroma half of lbac->h.run, run_rdoq,
  * level, last1, last2).  Each result holds the bits counted (the bitcounter increase), the range
  * and the models after the block, so the caller can go on from that state.  Levels are int16 in
- * raster order (w x h from coef_offset), e.g. the output of uavs3e_cuda_rdoq.
+ * raster order (w x h from coef_offset), e.g. the output of uavs3e_cuda_rdoq.  The blocks of one
+ * call may repeat a level range (the same block from several coder states) but not overlap one
+ * partially.
  */
 typedef struct {
     int16_t run[12], run_rdoq[12], level[12], last1[6], last2[12];   /* chroma: last2[0..9] */

@@ -6,8 +6,9 @@
 // (range and the channel's run, run_rdoq, level, last1, last2 models).  Results: the bits
 // counted, the range and the models after the block, bit-exact with the reference.
 //
-// One thread per block (the bins of a block form one chain: each updates the model and range the
-// next one reads); the models sit in registers / local memory.  The model update is the rule the
+// The scan of each block runs over the warp's lanes; the coding is one chain per block (each bin
+// updates the model and range the next one reads), one lane per block, the models in registers /
+// local memory.  The model update is the rule the
 // reference tabulates in tbl_plps / tbl_plps_ext (src/entropy.c:41), computed.
 #include "common.cuh"
 #include "tables.h"
@@ -85,52 +86,89 @@ __device__ __forceinline__ u32 cr_egk(int v)
     return (u32)((order << 1) - 1);
 }
 
-__global__ void __launch_bounds__(128) k_coef_rate(const CrParams P)
+__device__ __forceinline__ bool cr_valid(const CrReq &q, unsigned long long n_levels)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const CrReq q = P.reqs[i];
-    CrOut o;
-    o.ctx = q.ctx;
-    o.pad = 0;
     const int lw = q.log2w, lh = q.log2h, top = q.ch_type ? 5 : 6;
     const unsigned long long nc = 1ull << (lw + lh);
     bool ok = lw >= 2 && lw <= top && lh >= 2 && lh <= top && q.num_sig >= 1 && q.num_sig <= nc &&
-              q.range >= 256 && q.range <= 511 && (unsigned long long)q.coef_offset + nc <= P.n_levels;
+              q.range >= 256 && q.range <= 511 && (unsigned long long)q.coef_offset + nc <= n_levels;
     const s16 *mdl = &q.ctx.run[0];
     const int nchk = q.ch_type ? 52 : 54;             // chroma codes no last2 context past 9
 #pragma unroll
     for (int k = 0; k < 54; k++)
         ok = ok && (k >= nchk || (((mdl[k] >> 1) & 1023) >= 4 && mdl[k] >= 0 && mdl[k] < 8192));
-    if (!ok) {                        // outside the supported domain: bits ~0, state unchanged
-        o.bits = ~0u;
-        o.range = q.range;
+    return ok;
+}
+
+// Warp per 32 blocks.  First the warp takes its blocks one by one and lists, in scan order, the
+// positions and values of their first num_sig non-zero levels (a ballot and a prefix count per 32
+// positions) in list[] at the block's own level offset; then each lane codes its block's chain
+// from that list.  A run of zeros steps the run_rdoq model once per zero; the steps stop changing
+// the model once its probability is too small to move (p >> w == 0 after an MPS), so the walk ends
+// there.
+__global__ void __launch_bounds__(128) k_coef_rate(const CrParams P, u32 *list_all)
+{
+    __shared__ int s_cnt[4][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r0 = (blockIdx.x * 4 + warp) * 32;
+    if (r0 >= P.n) return;
+    for (int r = 0; r < 32 && r0 + r < P.n; r++) {
+        const CrReq q = P.reqs[r0 + r];
+        int cnt = 0;
+        if (cr_valid(q, P.n_levels)) {
+            const int n = 1 << (q.log2w + q.log2h);
+            const s16 *coef = P.levels + q.coef_offset;
+            const u16 *scan = P.scan[q.log2w][q.log2h];
+            u32 *list = list_all + q.coef_offset;
+            for (int base = 0; base < n && cnt < q.num_sig; base += 32) {
+                const int i = base + lane;
+                const int c = i < n ? coef[scan[i]] : 0;
+                const u32 m = __ballot_sync(0xffffffffu, c != 0);
+                const int at = cnt + __popc(m & ((1u << lane) - 1));
+                if (c != 0 && at < q.num_sig) list[at] = ((u32)i << 16) | (u16)(s16)c;
+                cnt += __popc(m);
+            }
+        }
+        if (lane == 0) s_cnt[warp][r] = min(cnt, 65535);
+    }
+    __syncwarp();
+    const int i = r0 + lane;
+    if (i >= P.n) return;
+    const CrReq q = P.reqs[i];
+    CrOut o;
+    o.ctx = q.ctx;
+    o.pad = 0;
+    o.bits = ~0u;                     // outside the domain, or fewer levels than num_sig: state unchanged
+    o.range = q.range;
+    if (!cr_valid(q, P.n_levels) || s_cnt[warp][lane] < q.num_sig) {
         P.out[i] = o;
         return;
     }
     CoefCtx &c = o.ctx;
-    const s16 *coef = P.levels + q.coef_offset;
-    const u16 *scan = P.scan[lw][lh];
-    const int n = (int)nc;
+    const u32 *list = list_all + q.coef_offset;
+    const int n = 1 << (q.log2w + q.log2h);
     u32 range = q.range, bits = 0;
-    int t0 = 10, num_sig = q.num_sig, last = -1, pos = 0;
-    bool good = true;
-    do {
-        while (pos < n && !coef[scan[pos]]) pos++;
-        if (pos >= n) { good = false; break; }        // fewer levels than num_sig
+    int t0 = 10, last = -1;
+    for (int k = 0; k < q.num_sig; k++) {
+        const u32 e = list[k];
+        const int pos = (int)(e >> 16), level = abs((int)(s16)(e & 0xFFFF));
         const int run = pos - last - 1;
         last = pos;
         cr_unary(range, bits, c.run[t0], c.run[t0 + 1], min(run, 16), 16);
         if (run >= 16) bits += cr_egk(run - 17);
         c.run_rdoq[t0] = cr_next(c.run_rdoq[t0], (run == 0) == (c.run_rdoq[t0] & 1));
-        for (int k = 1; k <= run; k++)
-            c.run_rdoq[t0 + 1] = cr_next(c.run_rdoq[t0 + 1], (k == run) == (c.run_rdoq[t0 + 1] & 1));
-        const int level = abs((int)coef[scan[pos]]);
+        s16 m = c.run_rdoq[t0 + 1];
+        for (int z = 1; z < run; z++) {                // zeros: bin 0
+            const s16 nm = cr_next(m, (m & 1) == 0);
+            if (nm == m) break;                        // a fixed point: the remaining zeros keep it
+            m = nm;
+        }
+        if (run > 0) m = cr_next(m, (m & 1) == 1);     // the closing '1'
+        c.run_rdoq[t0 + 1] = m;
         cr_unary(range, bits, c.level[t0], c.level[t0 + 1], min(level - 1, 8), 8);
         if (level >= 9) bits += cr_egk(level - 10);
         bits++;                                       // sign
         if (pos == n - 1) break;
-        num_sig--;
         s16 &m1 = c.last1[t0 >> 1];
         s16 &m2 = c.last2[31 - __clz(pos + 1)];
         t0 = min(level - 1, 5) << 1;
@@ -139,7 +177,7 @@ __global__ void __launch_bounds__(128) k_coef_rate(const CrParams P)
         if (c1 == c2) { cm = c1; pl = (p1 + p2) >> 1; }
         else if (p1 < p2) { cm = c1; pl = 1023 - ((p2 - p1) >> 1); }
         else { cm = c2; pl = 1023 - ((p1 - p2) >> 1); }
-        const int flag = num_sig == 0;
+        const int flag = k == q.num_sig - 1;
         u32 mps = range - ((u32)pl >> 2);
         const int s = mps < 256;
         mps |= 0x100;
@@ -152,16 +190,9 @@ __global__ void __launch_bounds__(128) k_coef_rate(const CrParams P)
         }
         m1 = cr_next(m1, flag == c1);
         m2 = cr_next(m2, flag == c2);
-        pos++;
-    } while (num_sig);
-    if (!good) {
-        o.ctx = q.ctx;
-        o.bits = ~0u;
-        o.range = q.range;
-    } else {
-        o.bits = bits;
-        o.range = (u16)range;
     }
+    o.bits = bits;
+    o.range = (u16)range;
     P.out[i] = o;
 }
 
@@ -179,8 +210,11 @@ int launch_coef_rate(const void *reqs, int n, const s16 *levels, unsigned long l
     P.reqs = (const CrReq *)reqs; P.n = n; P.levels = levels; P.n_levels = n_levels; P.out = (CrOut *)out;
     for (int a = 0; a < 7; a++)
         for (int b = 0; b < 7; b++) P.scan[a][b] = tab->scan[a][b];
-    k_coef_rate<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(P);
+    u32 *list = nullptr;                              // one word per level, at the levels' offsets
+    UC_CHECK(cudaMallocAsync((void **)&list, (size_t)n_levels * sizeof(u32), st));
+    k_coef_rate<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(P, list);
     UC_CHECK(cudaGetLastError());
+    UC_CHECK(cudaFreeAsync(list, st));
     count_launch(1);
     return UC_OK;
 }
