@@ -20,7 +20,7 @@
 
 namespace uc {
 
-constexpr int AME_WARPS = 4;
+constexpr int AME_WARPS = 2;
 constexpr s32 CPMV_MIN = -131072, CPMV_MAX = 131071;
 
 struct AffMeReq {
