@@ -618,6 +618,16 @@ UAVS3E_CUDA_API int uavs3e_cuda_rdoq_device(const uavs3e_cuda_rdoq_req_t *d_reqs
                                             const uavs3e_cuda_rdoq_est_t *d_ests, int n_est, int16_t *d_coefs,
                                             size_t n_coefs, int32_t *d_num_nz, void *stream);
 
+/* quant_non_zero's weighted branch (pichdr->pic_wq_enable, src/quant.c:335-380) for the same
+ * requests (lambda and est not used): the zero-out past 32, then plain quantisation with the
+ * weights of core->wq[0] (wq4, 16, for 4x4 blocks) and core->wq[1] (wq8, 64, the others; weights
+ * >= 1).  Levels over the coefficients, num_nz[i] per block (-1 outside the domain). */
+UAVS3E_CUDA_API int uavs3e_cuda_quant_wq(const uavs3e_cuda_rdoq_req_t *reqs, int n, const uint8_t *wq4,
+                                         const uint8_t *wq8, int16_t *coefs, size_t n_coefs, int32_t *num_nz);
+UAVS3E_CUDA_API int uavs3e_cuda_quant_wq_device(const uavs3e_cuda_rdoq_req_t *d_reqs, int n, const uint8_t *d_wq4,
+                                                const uint8_t *d_wq8, int16_t *d_coefs, size_t n_coefs,
+                                                int32_t *d_num_nz, void *stream);
+
 /* ---------------------------------------------------------------------------------------
  * Learned CU-partition / intra-mode pruning network (no counterpart in the reference: the
  * learned part stands beside the bit-exact path and never changes it).  bf16 tensor-core

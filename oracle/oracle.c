@@ -2129,6 +2129,47 @@ void orc_intra_rmd(const u32 *satd, const orc_rmd_req_t *reqs, int n, orc_rmd_ou
     }
 }
 
+/* ============================================================ weighted quantisation */
+
+/* quant_non_zero's pic_wq_enable branch (src/quant.c:335-380): each level is
+ * (s16)((|c| scale ns_scale 64 / weight + offset) >> shift) in 64-bit arithmetic, shift = 14 +
+ * 7 - (log2_size - ns_shift) with ns_shift 7 (and ns_scale 181) for blocks whose log2 w + log2 h
+ * is odd, offset (171 intra slice / 85) << (shift - 9); the weight of sample (i, j) is
+ * wq[(i / step) * width + (j >> idx_shift)] of the 4x4 matrix for 4x4 blocks, else of the 8x8
+ * one with idx_shift = max(log2 w, log2 h) - 3 and step = 1 << idx_shift */
+static int quant_wq_block(const orc_rdoq_req_t *r, const u8 *wq4, const u8 *wq8, s16 *coef)
+{
+    const int lw = r->log2w, lh = r->log2h, w = 1 << lw, h = 1 << lh;
+    if (w > 32)
+        for (int i = 0; i < h; i++) memset(coef + i * w + 32, 0, sizeof(s16) * (w - 32));
+    if (h > 32) memset(coef + w * h / 2, 0, sizeof(s16) * (w * h / 2));
+    const int scale = Q_SCALE[r->qp];
+    const int log2_size = (lw + lh) >> 1, odd = (lw + lh) & 1;
+    const int ns_shift = odd ? 7 : 0, ns_scale = odd ? 181 : 1;
+    const int tr_shift = 15 - 8 - (log2_size - ns_shift);
+    const int shift = 14 + tr_shift;
+    const s64 offset = (s64)(r->slice_type == 1 ? 171 : 85) << (shift - 9);
+    const u8 *wq = (lw == 2 && lh == 2) ? wq4 : wq8;
+    const int idx_shift = (lw == 2 && lh == 2) ? 0 : MAX(lw, lh) - 3;
+    const int width = (lw == 2 && lh == 2) ? 4 : 8;
+    int nz = 0;
+    for (int i = 0; i < h; i++)
+        for (int j = 0; j < w; j++) {
+            const int c = coef[i * w + j];
+            const int weight = wq[(i >> idx_shift) * width + (j >> idx_shift)];
+            const int lev = (s16)(((s64)ABSI(c) * scale * ns_scale * 64 / weight + offset) >> shift);
+            coef[i * w + j] = (s16)(c < 0 ? -lev : lev);
+            nz += coef[i * w + j] != 0;
+        }
+    return nz;
+}
+
+void orc_quant_wq(const orc_rdoq_req_t *reqs, int n, const u8 *wq4, const u8 *wq8, s16 *coefs, s32 *num_nz)
+{
+    orc_init();
+    for (int i = 0; i < n; i++) num_nz[i] = quant_wq_block(&reqs[i], wq4, wq8, coefs + reqs[i].coef_offset);
+}
+
 /* ============================================================ affine motion search */
 
 #define CPMV_MIN (-131072)

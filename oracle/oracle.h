@@ -248,6 +248,11 @@ typedef struct {
  * (unchanged when quant_check finds no coefficient above the threshold), num_nz[i] returned */
 void orc_rdoq(const orc_rdoq_req_t *reqs, int n, const orc_rdoq_est_t *ests, s16 *coefs, s32 *num_nz);
 
+/* quant_non_zero with pic_wq_enable (src/quant.c:315-383): the zero-out past 32, then plain
+ * quantisation with the weights of wq4 (4x4 blocks, 16) or wq8 (the others, 64; one weight per
+ * block of samples); lambda and est of the requests are not used */
+void orc_quant_wq(const orc_rdoq_req_t *reqs, int n, const u8 *wq4, const u8 *wq8, s16 *coefs, s32 *num_nz);
+
 /* one affine CU (com_mc_cu_affine, src/com_mc.c:361-422) */
 typedef struct {
     s16 x, y;           /* CU position                                                            */

@@ -223,6 +223,15 @@ class Oracle(_Common):
         self.L.orc_mc_affine(W, H, arr, i_ref, carr, i_c, ptr(reqs), len(reqs), ptr(out))
         return out[:out_bytes]
 
+    def quant_wq(self, reqs, wq4, wq8, coefs):
+        """quant_non_zero with weighted quantisation for every RDOQ_REQ; coefs updated, num_nz returned"""
+        reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
+        wq4 = np.ascontiguousarray(wq4, dtype=np.uint8)
+        wq8 = np.ascontiguousarray(wq8, dtype=np.uint8)
+        nz = np.zeros(len(reqs), dtype=np.int32)
+        self.L.orc_quant_wq(ptr(reqs), len(reqs), ptr(wq4), ptr(wq8), ptr(coefs), ptr(nz))
+        return nz
+
     def coef_rate(self, levels, reqs):
         """lbac_enc_run_length_cc_rdo for every COEF_RATE_REQ on levels (int16)"""
         levels = np.ascontiguousarray(levels, dtype=np.int16)
@@ -425,6 +434,17 @@ class RefLib(_Common):
             self.L.refk_mc_affine(W, H, arr, len(plane_ptrs) // 16, i_ref, carr, i_c,
                                   C.c_void_p(reqs.ctypes.data + i * AFFINE_REQ.itemsize), ptr(out))
         return out[:out_bytes]
+
+    def quant_wq(self, reqs, wq4, wq8, coefs):
+        """the reference's quant_non_zero with pic_wq_enable, one block per request"""
+        reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
+        wq4 = np.ascontiguousarray(wq4, dtype=np.uint8)
+        wq8 = np.ascontiguousarray(wq8, dtype=np.uint8)
+        nz = np.zeros(len(reqs), dtype=np.int32)
+        for i in range(len(reqs)):
+            nz[i] = self.L.refk_quant_wq(C.c_void_p(reqs.ctypes.data + i * RDOQ_REQ.itemsize), ptr(wq4), ptr(wq8),
+                                         ptr(coefs))
+        return nz
 
     def coef_rate(self, levels, reqs):
         """the reference's lbac_enc_run_length_cc_rdo, one block per request"""

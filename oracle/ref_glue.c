@@ -523,3 +523,25 @@ int refk_lbac_next(int model, int mps)
     lbac_encode_bin_for_rdoq(mps ? (u32)(m & 1) : (u32)!(m & 1), &m);
     return m;
 }
+
+/* ---- 9. weighted quantisation ----------------------------------------------------------------
+ * quant_non_zero (src/quant.c:315) with pichdr->pic_wq_enable set: core->wq[0] = wq4 (4x4),
+ * core->wq[1] = wq8 (8x8); the request as for refk_rdoq (lambda and estimates unused). */
+int refk_quant_wq(const glue_rdoq_req_t *rq, u8 *wq4, u8 *wq8, s16 *coef)
+{
+    refk_init();
+    static core_t *core = NULL;
+    static com_info_t info;
+    static com_pic_header_t pichdr;
+    if (!core) core = (core_t *)calloc(1, sizeof(core_t));
+    memset(&info, 0, sizeof(info));
+    memset(&pichdr, 0, sizeof(pichdr));
+    info.bit_depth_internal = 8;
+    pichdr.pic_wq_enable = 1;
+    core->info = &info;
+    core->pichdr = &pichdr;
+    core->wq[0] = wq4;
+    core->wq[1] = wq8;
+    return quant_non_zero(core, rq->qp, (double)rq->lambda / 32768.0, rq->is_intra, coef + rq->coef_offset,
+                          rq->log2w, rq->log2h, rq->ch_type, rq->slice_type);
+}

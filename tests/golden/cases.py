@@ -753,6 +753,18 @@ def rdoq_inputs(B, p, seed):
     return reqs, rdoq_ests(rng, p["k"]), np.concatenate(parts)
 
 
+def wq_matrices(rng):
+    """weighting matrices: 4x4 and 8x8, weights 8..255 (64 = flat)"""
+    return rng.integers(8, 256, 16).astype(np.uint8), rng.integers(8, 256, 64).astype(np.uint8)
+
+
+def run_quant_wq(B, p, seed):
+    reqs, _, coefs = rdoq_inputs(B, dict(p, k=1), seed)
+    wq4, wq8 = wq_matrices(np.random.default_rng(seed + 1))
+    nz = B.quant_wq(reqs, wq4, wq8, coefs)
+    return digest(nz, coefs)
+
+
 def run_rdoq(B, p, seed):
     reqs, ests, coefs = rdoq_inputs(B, p, seed)
     nz = B.rdoq(reqs, ests, coefs)
@@ -763,7 +775,7 @@ RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "coef_rate": run_coef_rate, "rdoq": run_rdoq,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "coef_rate": run_coef_rate, "quant_wq": run_quant_wq, "rdoq": run_rdoq,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -785,6 +797,9 @@ AFFME_CASES = [
     dict(w=192, h=128, vel=(2.5, -1.25), n=96),
     dict(w=160, h=96, vel=(-3.0, 2.0), n=96, paint=1),
 ]
+
+# weighted quantisation cases (quant_non_zero with pic_wq_enable)
+QUANT_WQ_CASES = [dict(n=200), dict(n=120)]
 
 # coefficient rate cases (lbac_enc_run_length_cc_rdo)
 COEF_RATE_CASES = [dict(n=200), dict(n=150)]
@@ -880,6 +895,8 @@ def all_cases():
         add("rmd", **p)
     for p in COEF_RATE_CASES:
         add("coef_rate", **p)
+    for p in QUANT_WQ_CASES:
+        add("quant_wq", **p)
     return cases
 
 

@@ -13,6 +13,7 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 import cases  # noqa: E402
 
 GOLDEN = [c for c in json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"] if c["kernel"] == "rdoq"]
+WQ_GOLDEN = [c for c in json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"] if c["kernel"] == "quant_wq"]
 
 
 class GpuRdoq:
@@ -80,3 +81,22 @@ def test_rdoq_skips_requests_outside_the_domain(gpu, oracle):
         o, n = int(reqs[i]["coef_offset"]), (1 << int(reqs[i]["log2w"])) * (1 << int(reqs[i]["log2h"]))
         assert np.array_equal(got_c[o:o + n], coefs[o:o + n])
     assert gpu.lib().uavs3e_cuda_status() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", WQ_GOLDEN, ids=[str(c["params"]["n"]) for c in WQ_GOLDEN])
+def test_quant_wq_matches_reference_golden(gpu, oracle, case):
+    """quant_non_zero's weighted branch (pic_wq_enable) against the reference's digests"""
+    reqs, _, coefs = cases.rdoq_inputs(oracle, dict(case["params"], k=1), case["seed"])
+    wq4, wq8 = cases.wq_matrices(np.random.default_rng(case["seed"] + 1))
+    nz = gpu.quant_wq(reqs, wq4, wq8, coefs)
+    assert cases.digest(nz, coefs) == case["md5"]
+
+
+@pytest.mark.gpu
+def test_quant_wq_matches_oracle_many_blocks(gpu, oracle):
+    reqs, _, coefs = cases.rdoq_inputs(oracle, dict(n=4000, k=1), 8400)
+    wq4, wq8 = cases.wq_matrices(np.random.default_rng(8401))
+    a, b = coefs.copy(), coefs.copy()
+    assert np.array_equal(gpu.quant_wq(reqs, wq4, wq8, a), oracle.quant_wq(reqs, wq4, wq8, b))
+    assert np.array_equal(a, b)

@@ -20,3 +20,13 @@ def test_rdoq_with_estimates_from_contexts(oracle, ref):
         a, b = coefs.copy(), coefs.copy()
         assert np.array_equal(oracle.rdoq(reqs, ests, a), ref.rdoq(reqs, ests, b))
         assert np.array_equal(a, b)
+
+
+def test_weighted_quant_oracle_matches_reference(oracle, ref):
+    """quant_non_zero with pic_wq_enable: the restatement equals the reference on every shape"""
+    for seed in range(3):
+        reqs, _, coefs = cases.rdoq_inputs(oracle, dict(n=200, k=1), 8200 + seed)
+        wq4, wq8 = cases.wq_matrices(np.random.default_rng(8300 + seed))
+        a, b = coefs.copy(), coefs.copy()
+        assert np.array_equal(oracle.quant_wq(reqs, wq4, wq8, a), ref.quant_wq(reqs, wq4, wq8, b))
+        assert np.array_equal(a, b)

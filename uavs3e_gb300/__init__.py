@@ -82,6 +82,8 @@ def _declare(L):
     L.uavs3e_cuda_me_affine.argtypes = [P, P, I, P, I, P]
     L.uavs3e_cuda_intra_rmd.argtypes = [P, C.c_size_t, P, I, P]
     L.uavs3e_cuda_coef_rate.argtypes = [P, I, P, C.c_size_t, P]
+    L.uavs3e_cuda_quant_wq.argtypes = [P, I, P, P, P, C.c_size_t, P]
+    L.uavs3e_cuda_quant_wq_device.argtypes = [P, I, P, P, P, C.c_size_t, P, P]
     L.uavs3e_cuda_coef_rate_device.argtypes = [P, I, P, C.c_size_t, P, P]
     L.uavs3e_cuda_intra_rmd_device.argtypes = [P, C.c_size_t, P, I, P, P]
     L.uavs3e_cuda_me_affine_device.argtypes = [I, I, P, I, P, I, I, I, P, I, P, P]
@@ -439,6 +441,19 @@ def rdoq(reqs, ests, coefs):
     nz = np.zeros(max(1, len(reqs)), dtype=np.int32)
     check(lib().uavs3e_cuda_rdoq(reqs.ctypes.data, len(reqs), ests.ctypes.data, len(ests), coefs.ctypes.data,
                                  coefs.size, nz.ctypes.data), "rdoq")
+    return nz[:len(reqs)]
+
+
+def quant_wq(reqs, wq4, wq8, coefs):
+    """quant_non_zero with weighted quantisation for every RDOQ_REQ on host arrays: coefs (int16)
+    updated in place; returns num_nz"""
+    reqs = np.ascontiguousarray(reqs, dtype=RDOQ_REQ)
+    wq4 = np.ascontiguousarray(wq4, dtype=np.uint8)
+    wq8 = np.ascontiguousarray(wq8, dtype=np.uint8)
+    assert coefs.dtype == np.int16 and coefs.flags["C_CONTIGUOUS"]
+    nz = np.zeros(max(1, len(reqs)), dtype=np.int32)
+    check(lib().uavs3e_cuda_quant_wq(reqs.ctypes.data, len(reqs), wq4.ctypes.data, wq8.ctypes.data, coefs.ctypes.data,
+                                     coefs.size, nz.ctypes.data), "quant_wq")
     return nz[:len(reqs)]
 
 

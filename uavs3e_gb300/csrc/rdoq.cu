@@ -254,6 +254,61 @@ int launch_rdoq(const void *reqs, int n, const void *ests, int n_est, s16 *coefs
 using namespace uc;
 
 // per device: buffers of the host-memory entry point
+// quant_non_zero's weighted branch (pic_wq_enable, src/quant.c:335-380) for lists of blocks: the
+// zero-out past 32 columns / rows, then every level (s16)((|c| scale ns_scale 64 / weight + offset)
+// >> shift) in 64-bit arithmetic with the weight of the sample's cell of the 4x4 (4x4 blocks) or
+// 8x8 matrix (one cell per 2^(max(log2 w, log2 h) - 3) samples each way).  A warp per block.
+__global__ void __launch_bounds__(128) k_quant_wq(const RdoqReq *reqs, int n, const u8 *wq4, const u8 *wq8,
+                                                  s16 *coefs, unsigned long long n_coefs, s32 *num_nz)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 4 + warp;
+    if (r >= n) return;
+    const RdoqReq q = reqs[r];
+    const int lw = q.log2w, lh = q.log2h, w = 1 << lw, h = 1 << lh;
+    if (lw < 2 || lw > 6 || lh < 2 || lh > 6 || q.qp > 79 || q.ch_type > 2 ||
+        (unsigned long long)q.coef_offset + (unsigned long long)(w * h) > n_coefs) {
+        if (lane == 0) num_nz[r] = -1;       // outside the supported domain: block untouched
+        return;
+    }
+    s16 *coef = coefs + q.coef_offset;
+    const int log2_size = (lw + lh) >> 1, odd = (lw + lh) & 1;
+    const int ns_shift = odd ? 7 : 0, ns_scale = odd ? 181 : 1;
+    const int shift = 14 + 15 - 8 - (log2_size - ns_shift);
+    const long long offset = (long long)(q.slice_type == 1 ? 171 : 85) << (shift - 9);
+    const long long scale = (long long)kQScale[q.qp] * ns_scale * 64;
+    const bool small = lw == 2 && lh == 2;
+    const u8 *wq = small ? wq4 : wq8;
+    const int idx_shift = small ? 0 : max(lw, lh) - 3, width = small ? 4 : 8;
+    int nz = 0;
+    for (int p = lane; p < w * h; p += 32) {
+        const int i = p >> lw, j = p & (w - 1);
+        const int c = (i >= 32 || j >= 32) ? 0 : coef[p];
+        const int weight = wq[(i >> idx_shift) * width + (j >> idx_shift)];
+        const int lev = (s16)(u16)(unsigned long long)((((long long)abs(c) * scale) / weight + offset) >> shift);
+        const s16 v = (s16)(c < 0 ? -lev : lev);
+        coef[p] = v;
+        nz += v != 0;
+    }
+#pragma unroll
+    for (int m = 16; m; m >>= 1) nz += __shfl_xor_sync(0xffffffffu, nz, m);
+    if (lane == 0) num_nz[r] = nz;
+}
+
+int launch_quant_wq(const void *reqs, int n, const u8 *wq4, const u8 *wq8, s16 *coefs, unsigned long long n_coefs,
+                    s32 *num_nz, cudaStream_t st)
+{
+    if (n < 0 || (n > 0 && (!reqs || !wq4 || !wq8 || !coefs || !num_nz)))
+        return set_status(UC_ERR_ARG, "quant_wq: null argument");
+    if (n == 0) return UC_OK;
+    prof_begin(PROF_RDOQ, st);
+    k_quant_wq<<<(unsigned)((n + 3) / 4), 128, 0, st>>>((const RdoqReq *)reqs, n, wq4, wq8, coefs, n_coefs, num_nz);
+    UC_CHECK(cudaGetLastError());
+    count_launch(1);
+    prof_end(PROF_RDOQ, st);
+    return UC_OK;
+}
+
 struct RdoqScratch {
     std::mutex mu;
     cudaStream_t st = nullptr;
@@ -311,4 +366,58 @@ extern "C" UAVS3E_CUDA_API int uavs3e_cuda_rdoq_device(const uavs3e_cuda_rdoq_re
     int rc = ensure_init();
     if (rc) return rc;
     return launch_rdoq(d_reqs, n, d_ests, n_est, d_coefs, (unsigned long long)n_coefs, d_num_nz, (cudaStream_t)stream);
+}
+
+extern "C" UAVS3E_CUDA_API int uavs3e_cuda_quant_wq(const uavs3e_cuda_rdoq_req_t *reqs, int n, const uint8_t *wq4,
+                                                   const uint8_t *wq8, int16_t *coefs, size_t n_coefs,
+                                                   int32_t *num_nz)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && (!reqs || !wq4 || !wq8 || !coefs || !num_nz)))
+        return set_status(UC_ERR_ARG, "quant_wq: bad argument");
+    if (n == 0) return UC_OK;
+    int dev = 0;
+    UC_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "quant_wq: device index");
+    RdoqScratch &S = g_rdoq[dev];
+    std::lock_guard<std::mutex> lk(S.mu);
+    if (!S.st) UC_CHECK(cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking));
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t b_req = up((size_t)n * sizeof(*reqs)), b_wq = 256;
+    const size_t b_coef = up(n_coefs * sizeof(int16_t)), b_nz = up((size_t)n * sizeof(int32_t));
+    const size_t need = b_req + b_wq + b_coef + b_nz;
+    if (S.cap < need) {
+        if (S.buf) UC_CHECK(cudaFree(S.buf));
+        S.buf = nullptr;
+        S.cap = 0;
+        UC_CHECK(cudaMalloc(&S.buf, need));
+        S.cap = need;
+    }
+    char *b = (char *)S.buf;
+    void *d_req = b;
+    u8 *d_wq = (u8 *)(b + b_req);
+    int16_t *d_coef = (int16_t *)(b + b_req + b_wq);
+    int32_t *d_nz = (int32_t *)(b + b_req + b_wq + b_coef);
+    UC_CHECK(cudaMemcpyAsync(d_req, reqs, (size_t)n * sizeof(*reqs), cudaMemcpyHostToDevice, S.st));
+    UC_CHECK(cudaMemcpyAsync(d_wq, wq4, 16, cudaMemcpyHostToDevice, S.st));
+    UC_CHECK(cudaMemcpyAsync(d_wq + 16, wq8, 64, cudaMemcpyHostToDevice, S.st));
+    UC_CHECK(cudaMemcpyAsync(d_coef, coefs, n_coefs * sizeof(int16_t), cudaMemcpyHostToDevice, S.st));
+    rc = launch_quant_wq(d_req, n, d_wq, d_wq + 16, d_coef, (unsigned long long)n_coefs, d_nz, S.st);
+    if (rc) return rc;
+    UC_CHECK(cudaMemcpyAsync(coefs, d_coef, n_coefs * sizeof(int16_t), cudaMemcpyDeviceToHost, S.st));
+    UC_CHECK(cudaMemcpyAsync(num_nz, d_nz, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, S.st));
+    UC_CHECK(cudaStreamSynchronize(S.st));
+    return UC_OK;
+}
+
+extern "C" UAVS3E_CUDA_API int uavs3e_cuda_quant_wq_device(const uavs3e_cuda_rdoq_req_t *d_reqs, int n,
+                                                          const uint8_t *d_wq4, const uint8_t *d_wq8,
+                                                          int16_t *d_coefs, size_t n_coefs, int32_t *d_num_nz,
+                                                          void *stream)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    return launch_quant_wq(d_reqs, n, d_wq4, d_wq8, d_coefs, (unsigned long long)n_coefs, d_num_nz,
+                           (cudaStream_t)stream);
 }
