@@ -968,11 +968,11 @@ def run_ours(args):
     h_out = torch.empty(ms.n_results * 32, dtype=torch.uint8).pin_memory()
     torch.cuda.synchronize()
     e2e_steps = max(5, args.steps // 2)
-    lib = u.lib()
 
     def e2e_step(t):
-        u.check(lib.uavs3e_cuda_me_set_ref(ms.h, (t - 1) % N_REFS, pin[(t - 1) % RING].data_ptr(), W), "me_set_ref")
-        ms.run_ptr(pin[t % RING].data_ptr(), W, lam, h_out.data_ptr())
+        # one call: the new reference and the frame up, the captured frame graph, the results down
+        ms.frame_ptr((t - 1) % N_REFS, pin[(t - 1) % RING].data_ptr(), W, pin[t % RING].data_ptr(), W, lam,
+                     h_out.data_ptr())
 
     for k in range(2):
         e2e_step(2 + k)
@@ -1055,7 +1055,7 @@ def run_ours(args):
         "gcandidates_per_s": gcand * value / 1e9,
         "e2e": {"value": world * e2e_steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "path": "uavs3e_cuda_me_set_ref + uavs3e_cuda_me_run with pinned host buffers"},
+                "path": "uavs3e_cuda_me_frame (reference and frame up, graph replay, results down) with pinned host buffers"},
         "gpu_launches": launches,
         "gpu_launches_per_step": launches / args.steps,
         "roofline": roofline,

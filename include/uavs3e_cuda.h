@@ -150,6 +150,12 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_run(uavs3e_cuda_me *me, const uint8_t *org, i
 UAVS3E_CUDA_API int uavs3e_cuda_me_run_device(uavs3e_cuda_me *me, const uint8_t *d_org, int i_org,
                                               uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);
 
+/* One call per frame from host buffers: reference `slot` becomes `ref` (as uavs3e_cuda_me_set_ref)
+ * and the frame `org` is searched (as uavs3e_cuda_me_run), the work replayed as the session's
+ * captured graph (uavs3e_cuda_me_frame_graph) with one synchronisation at the end. */
+UAVS3E_CUDA_API int uavs3e_cuda_me_frame(uavs3e_cuda_me *me, int slot, const uint8_t *ref, int i_ref,
+                                         const uint8_t *org, int i_org, uint32_t lambda_mv,
+                                         uavs3e_cuda_me_result_t *out);
 /* One frame as a CUDA graph: refresh reference `slot` from the device picture d_ref (stride
  * i_src; padding and the 15 quarter-sample planes) and search d_org into d_out -- the launches of
  * uavs3e_cuda_me_set_ref_device + uavs3e_cuda_me_run_device, captured once per distinct set of

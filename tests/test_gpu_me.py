@@ -119,3 +119,28 @@ def test_me_frame_graph_matches_plain_launches(gpu):
         assert torch.equal(d_a, d_b), f"frame {t} (qp {qp}) differs"
     plain.close()
     graph.close()
+
+
+def test_me_frame_host_matches_set_ref_run(gpu):
+    """uavs3e_cuda_me_frame (host reference + host frame, one graph replay) gives what
+    uavs3e_cuda_me_set_ref followed by uavs3e_cuda_me_run gives, over alternating slots, reused
+    cached graphs and a lambda change"""
+    W, H = 200, 136
+    frames = motion_sequence(W, H, 6, seed=23)
+    plain = gpu.MotionSearch(W, H, n_refs=2, search_range=32, pad=144)
+    onecall = gpu.MotionSearch(W, H, n_refs=2, search_range=32, pad=144)
+    out = np.zeros(onecall.n_results, dtype=gpu.ME_RESULT)
+    schedule = [(1, 32), (2, 32), (3, 32), (4, 32), (5, 27), (2, 27)]
+    for t, qp in schedule:
+        lam = lambda_mv_for_qp(qp)
+        slot = (t - 1) % 2
+        for ms in (plain, onecall):
+            ms.set_ref(1 - slot, frames[max(0, t - 2)])
+        plain.set_ref(slot, frames[t - 1])
+        want = plain.run(frames[t], lam)
+        ref = np.ascontiguousarray(frames[t - 1])
+        org = np.ascontiguousarray(frames[t])
+        onecall.frame_ptr(slot, ref.ctypes.data, W, org.ctypes.data, W, lam, out.ctypes.data)
+        assert np.array_equal(want, out), f"frame {t} (qp {qp}) differs"
+    plain.close()
+    onecall.close()

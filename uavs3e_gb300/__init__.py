@@ -80,6 +80,7 @@ def _declare(L):
     L.uavs3e_cuda_mc_affine_device.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_rdoq.argtypes = [P, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_me_affine.argtypes = [P, P, I, P, I, P]
+    L.uavs3e_cuda_me_frame.argtypes = [P, I, P, I, P, I, C.c_uint32, P]
     L.uavs3e_cuda_intra_rmd.argtypes = [P, C.c_size_t, P, I, P]
     L.uavs3e_cuda_coef_rate.argtypes = [P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_quant_wq.argtypes = [P, I, P, P, P, C.c_size_t, P]
@@ -339,6 +340,11 @@ class MotionSearch:
         """set_ref_device(slot, d_ref) + run_device(d_org) replayed as a captured CUDA graph"""
         check(lib().uavs3e_cuda_me_frame_graph(self.h, slot, d_ref, i_src, d_org, i_org, lambda_mv, d_out, stream),
               "me_frame_graph")
+
+    def frame_ptr(self, slot, ref_ptr, i_ref, org_ptr, i_org, lambda_mv, out_ptr):
+        """host pointers: set_ref(slot, ref) + run(org) as one graph replay and one synchronisation"""
+        check(lib().uavs3e_cuda_me_frame(self.h, slot, ref_ptr, i_ref, org_ptr, i_org, lambda_mv, out_ptr),
+              "me_frame")
 
     def plane_ptr(self, slot, phase):
         return lib().uavs3e_cuda_me_plane(self.h, slot, phase)

@@ -219,6 +219,7 @@ struct uavs3e_cuda_me {
     size_t plane_bytes;
     pel *planes_buf = nullptr;        // [n_refs][16][rows*stride]
     pel *org_buf = nullptr;           // W x H for host runs
+    pel *ref_stage = nullptr;         // W x H: a new reference's host samples (one-call frames)
     MeResult *out_buf = nullptr;      // device results for host runs
     u64 *keys = nullptr;              // per-block integer winners
     u32 *sub = nullptr;               // per-candidate SATD sums of the refinement
@@ -318,7 +319,7 @@ UAVS3E_CUDA_API void uavs3e_cuda_me_close(uavs3e_cuda_me *m)
 {
     if (!m) return;
     if (m->st) cudaStreamSynchronize(m->st);
-    cudaFree(m->planes_buf); cudaFree(m->org_buf); cudaFree(m->out_buf);
+    cudaFree(m->planes_buf); cudaFree(m->org_buf); cudaFree(m->out_buf); cudaFree(m->ref_stage);
     cudaFree(m->keys); cudaFree(m->sub); cudaFree(m->q2); cudaFree(m->r2m); cudaFree(m->tz_buf);
     cudaFree(m->chroma_buf); cudaFree(m->mc_buf);
     for (auto &g : m->graphs) cudaGraphExecDestroy(g.exec);
@@ -595,6 +596,25 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_frame_graph(uavs3e_cuda_me *m, int slot, cons
     hit->used = ++m->graph_tick;
     UC_CHECK(cudaGraphLaunch(hit->exec, (cudaStream_t)stream));
     count_launch((int)hit->launches);
+    return UC_OK;
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_me_frame(uavs3e_cuda_me *m, int slot, const uint8_t *ref, int i_ref,
+                                         const uint8_t *org, int i_org, uint32_t lambda_mv,
+                                         uavs3e_cuda_me_result_t *out)
+{
+    if (!m || !ref || !org || !out || slot < 0 || slot >= m->n_refs || i_ref < m->W || i_org < m->W)
+        return set_status(UC_ERR_ARG, "me_frame: bad argument");
+    if (ensure_init()) return uavs3e_cuda_status();
+    if (!m->ref_stage) UC_CHECK(cudaMalloc(&m->ref_stage, (size_t)m->W * m->H));
+    UC_CHECK(cudaMemcpy2DAsync(m->ref_stage, m->W, ref, i_ref, m->W, m->H, cudaMemcpyHostToDevice, m->st));
+    UC_CHECK(cudaMemcpy2DAsync(m->org_buf, m->W, org, i_org, m->W, m->H, cudaMemcpyHostToDevice, m->st));
+    int r = uavs3e_cuda_me_frame_graph(m, slot, m->ref_stage, m->W, m->org_buf, m->W, lambda_mv,
+                                       (uavs3e_cuda_me_result_t *)m->out_buf, m->st);
+    if (r) return r;
+    UC_CHECK(cudaMemcpyAsync(out, m->out_buf, (size_t)uavs3e_cuda_me_num_results(m) * sizeof(MeResult),
+                             cudaMemcpyDeviceToHost, m->st));
+    UC_CHECK(cudaStreamSynchronize(m->st));
     return UC_OK;
 }
 
