@@ -703,6 +703,60 @@ def tz_leg(u, torch, stream, flush, with_cpu, hbm_peak, reps=10):
     return out
 
 
+def affmvp_part(u, torch, stream, flush, with_cpu, reps=10):
+    """com_get_affine_mvp_scaling for every 8x8..128x128 CU position of a 1080p motion field, both
+    lists (uavs3e_cuda_affine_mvp_device, one thread per CU)"""
+    import cases
+    p = dict(w=480, h=270, nref=4, n=0, big=1)
+    ptr_cur, ref_ptr, mv, refi, i_scu, _ = cases.affmvp_inputs(p, 91)
+    rng = np.random.default_rng(92)
+    n = 1 << 20
+    reqs = np.zeros(n, dtype=u.AFFMVP_REQ)
+    cw = rng.choice([8, 16, 32, 64, 128], n)
+    x = (rng.random(n) * (481 - cw // 4)).astype(np.int64)
+    y = rng.integers(0, 270, n)
+    reqs["scup"] = y * i_scu + x
+    reqs["cu_width"] = cw
+    reqs["lidx"] = rng.integers(0, 2, n)
+    reqs["cur_refi"] = rng.integers(0, 4, n)
+    reqs["mvr"] = rng.integers(0, 3, n)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).cuda()  # noqa: E731
+    d_ref, d_mv, d_refi, d_req = d(ref_ptr), d(mv), d(refi), d(reqs)
+    d_out = torch.zeros(n * 16, dtype=torch.uint8, device="cuda")
+    rows = len(refi) // i_scu
+    sp = stream.cuda_stream
+
+    def run():
+        u.affine_mvp_device(ptr_cur, d_ref.data_ptr(), len(ref_ptr), d_mv.data_ptr(), d_refi.data_ptr(), i_scu, rows,
+                            d_req.data_ptr(), n, d_out.data_ptr(), None, sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms_gpu = sum(a.elapsed_time(b) for a, b in evs) / reps
+    moved = n * (12 + 16)
+    out = {"workload": "affine control-point MVP of 1,048,576 CUs (8x8..128x128, both lists, 4 references, AMVR "
+                       "0..2) on a 1080p motion field (480 x 270 SCUs)", "cus": n, "ms_per_batch": ms_gpu,
+           "cus_per_s": n / (ms_gpu / 1000.0),
+           "request_result_gb_s": moved / (ms_gpu / 1000.0) / 1e9}
+    if with_cpu:
+        import pyoracle
+        o = pyoracle.Oracle()
+        t0 = time.perf_counter()
+        o.affine_mvp(ptr_cur, ref_ptr, mv, refi, i_scu, reqs)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "CUs/s", "cores": 1, "kind": "port",
+                               "sample": f"the whole batch through the oracle restatement, {dt:.2f} s"}
+    return out
+
+
 def affme_leg(u, torch, stream, flush, with_cpu, reps=10):
     """affine motion searches (affine_me_gradient) of a 1080p frame: every block of 16x16 and
     larger on the CTU grid against 2 references, AMVR indices 0..2, 70 % uni calls (60 % of them
@@ -771,6 +825,7 @@ def affme_leg(u, torch, stream, flush, with_cpu, reps=10):
         out["cpu_baseline"] = {"value": n / dt, "unit": "calls/s", "cores": threads, "kind": "port",
                                "sample": f"the whole batch through the oracle restatement, {dt:.2f} s"}
     ms.close()
+    out["mvp"] = affmvp_part(u, torch, stream, flush, with_cpu, reps)
     return out
 
 

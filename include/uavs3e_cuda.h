@@ -412,6 +412,42 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_affine_device(int width, int height, const ui
                                                  const uavs3e_cuda_affme_req_t *d_reqs, int n,
                                                  uavs3e_cuda_affme_out_t *d_out, void *stream);
 
+/* Affine control-point MVP (com_get_affine_mvp_scaling, src/com_util.c:1983-2058, with
+ * scaling_mv1 src/com_util.c:322 and com_mv_rounding_s32 inc/com_util.h:189) for lists of CUs:
+ * the top-left predictor from neighbours A, B, D and the top-right one from G, C (the first with
+ * a valid reference index in list lidx, its MV scaled by the POC distances; zero when none),
+ * taken to 1/16 sample, rounded to the affine AMVR resolution and clipped to 18 bits.
+ * The motion field has the encoder's layout: map_mv s16 [rows * i_scu][2 lists][2], map_refi s8
+ * [rows * i_scu][2], stride i_scu = pic_width_in_scu + 2, the picture's SCU (0, 0) at index
+ * i_scu + 1 (one border row above, one border column on each side).  ref_ptr[n_ref][2] holds the
+ * POC of refp[i][list]. */
+typedef struct {
+    int32_t scup;       /* y_scu * i_scu + x_scu of the CU's top-left SCU */
+    int16_t cu_width;   /* luma samples */
+    int8_t lidx;        /* list 0 / 1 */
+    int8_t cur_refi;    /* the CU's reference index in list lidx */
+    int8_t mvr;         /* affine AMVR index: 0, 1, 2 (1/4, 1, 1/16 sample) */
+    int8_t pad[3];
+} uavs3e_cuda_affmvp_req_t;
+
+typedef struct {
+    int32_t mvp[2][2];  /* (x, y) of the top-left and top-right control points, 1/16 samples */
+} uavs3e_cuda_affmvp_out_t;
+
+/* Host buffers, synchronous.  Requests outside the domain (a neighbour outside the field, a
+ * reference index >= n_ref, a zero POC distance, mvr > 2, lidx > 1) get zero predictors and make
+ * the call return UAVS3E_CUDA_ERR_ARG after all results are written. */
+UAVS3E_CUDA_API int uavs3e_cuda_affine_mvp(int64_t ptr, const int64_t *ref_ptr, int n_ref, const int16_t *map_mv,
+                                           const int8_t *map_refi, int i_scu, int rows,
+                                           const uavs3e_cuda_affmvp_req_t *reqs, int n,
+                                           uavs3e_cuda_affmvp_out_t *out);
+/* Device buffers on `stream`; d_err (optional, device int32) gains the number of requests outside
+ * the domain. */
+UAVS3E_CUDA_API int uavs3e_cuda_affine_mvp_device(int64_t ptr, const int64_t *d_ref_ptr, int n_ref,
+                                                  const int16_t *d_map_mv, const int8_t *d_map_refi, int i_scu,
+                                                  int rows, const uavs3e_cuda_affmvp_req_t *d_reqs, int n,
+                                                  uavs3e_cuda_affmvp_out_t *d_out, int32_t *d_err, void *stream);
+
 /* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
  * session's plane stride; for inspection by tests. */
 UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *me, int slot, int phase);

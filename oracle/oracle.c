@@ -2522,3 +2522,84 @@ void orc_rdoq(const orc_rdoq_req_t *reqs, int n, const orc_rdoq_est_t *ests, s16
     orc_init();
     for (int i = 0; i < n; i++) num_nz[i] = rdoq_block(&reqs[i], &ests[reqs[i].est], coefs + reqs[i].coef_offset);
 }
+
+/* ======================================================================================
+ * Affine control-point MVP -- com_get_affine_mvp_scaling, src/com_util.c:1983-2058, with
+ * scaling_mv1 (src/com_util.c:322-341) and com_mv_rounding_s32 (inc/com_util.h:189-194)
+ * ====================================================================================== */
+
+/* the neighbour's MV scaled by the ratio of POC distances (both from the current picture):
+ * ratio = (2^14 / t_neb) * t_cur with C's truncating division first, then a symmetric rounding
+ * shift and an s16 clip */
+static s16 affmvp_scale(s16 mv, int ratio)
+{
+    const s64 t = (s64)mv * ratio;
+    s64 r = t == 0 ? 0 : t > 0 ? (t + 8192) >> 14 : -((-t + 8192) >> 14);
+    if (r < -32768) r = -32768;
+    if (r > 32767) r = 32767;
+    return (s16)r;
+}
+
+/* 1/4 -> 1/16 sample, rounded to the AMVR resolution (the magnitude rounded, the sign kept),
+ * clipped to the 18-bit CPMV range */
+static s32 affmvp_round(s16 v, int shift)
+{
+    const s32 x = (s32)v * 4;
+    const s32 add = shift > 0 ? 1 << (shift - 1) : 0;
+    s32 r = x >= 0 ? ((x + add) >> shift) << shift : -(((-x + add) >> shift) << shift);
+    if (r < -131072) r = -131072;
+    if (r > 131071) r = 131071;
+    return r;
+}
+
+static int affmvp_one(s64 ptr, const s64 *ref_ptr, int n_ref, const s16 *map_mv, const s8 *map_refi,
+                      long long n_field, int i_scu, const orc_affmvp_req_t *q, orc_affmvp_out_t *o)
+{
+    const int lidx = q->lidx;
+    if (lidx < 0 || lidx > 1 || q->cur_refi < 0 || q->cur_refi >= n_ref || q->mvr < 0 || q->mvr > 2 ||
+        q->cu_width < 4)
+        return 1;
+    const int t_cur = (int)(ptr * 2 - ref_ptr[q->cur_refi * 2 + lidx] * 2);
+    if (t_cur == 0) return 1;
+    const long long origin = i_scu + 1;
+    const int wsc = q->cu_width >> 2;
+    /* top-left: A (left), B (above), D (above-left); top-right: G (above the last column), C
+     * (above-right); the first neighbour with a valid reference index in list lidx */
+    const long long nb[5] = { q->scup - 1, q->scup - i_scu, q->scup - i_scu - 1,
+                              q->scup - i_scu + wsc - 1, q->scup - i_scu + wsc };
+    s16 mv[2][2] = { { 0, 0 }, { 0, 0 } };
+    for (int g = 0; g < 2; g++) {
+        const int k0 = g == 0 ? 0 : 3, k1 = g == 0 ? 3 : 5;
+        for (int k = k0; k < k1; k++) {
+            const long long a = origin + nb[k];
+            if (a < 0 || a >= n_field) return 1;
+            const int refi = map_refi[a * 2 + lidx];
+            if (refi < 0) continue;
+            if (refi >= n_ref) return 1;
+            const int t_neb = (int)(ptr * 2 - ref_ptr[refi * 2 + lidx] * 2);
+            if (t_neb == 0) return 1;
+            const int ratio = (1 << 14) / t_neb * t_cur;
+            mv[g][0] = affmvp_scale(map_mv[(a * 2 + lidx) * 2 + 0], ratio);
+            mv[g][1] = affmvp_scale(map_mv[(a * 2 + lidx) * 2 + 1], ratio);
+            break;
+        }
+    }
+    const int shift = q->mvr == 0 ? 2 : q->mvr == 1 ? 4 : 0;
+    for (int g = 0; g < 2; g++)
+        for (int d = 0; d < 2; d++) o->mvp[g][d] = affmvp_round(mv[g][d], shift);
+    return 0;
+}
+
+int orc_affine_mvp(s64 ptr, const s64 *ref_ptr, int n_ref, const s16 *map_mv, const s8 *map_refi, int i_scu,
+                   int rows, const orc_affmvp_req_t *reqs, int n, orc_affmvp_out_t *out)
+{
+    int bad = 0;
+    for (int i = 0; i < n; i++) {
+        memset(&out[i], 0, sizeof(out[i]));
+        if (affmvp_one(ptr, ref_ptr, n_ref, map_mv, map_refi, (long long)rows * i_scu, i_scu, &reqs[i], &out[i])) {
+            memset(&out[i], 0, sizeof(out[i]));
+            bad++;
+        }
+    }
+    return bad;
+}

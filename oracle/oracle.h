@@ -374,6 +374,29 @@ typedef struct {
 void orc_me_affine(int width, int height, const pel *org, int i_org, const pel *const *planes, int i_ref,
                    const orc_affme_req_t *reqs, int n, orc_affme_out_t *out, int threads);
 
+/* one CU's affine MVP request (com_get_affine_mvp_scaling, src/com_util.c:1983-2058); the
+ * motion field has the reference's layout: stride i_scu = pic_width_in_scu + 2, SCU (0, 0) at
+ * index i_scu + 1 (one border row above, one border column on each side) */
+typedef struct {
+    s32 scup;           /* y_scu * i_scu + x_scu of the CU's top-left SCU                         */
+    s16 cu_width;       /* luma samples                                                            */
+    s8 lidx;            /* list 0 / 1                                                              */
+    s8 cur_refi;        /* the CU's reference index in list lidx                                   */
+    s8 mvr;             /* affine AMVR index (Tab_Affine_AMVR: 0 -> 2, 1 -> 4, 2 -> 0 bits)         */
+    s8 pad[3];
+} orc_affmvp_req_t;
+
+typedef struct {
+    s32 mvp[2][2];      /* (x, y) of the top-left and top-right control points, 1/16 samples       */
+} orc_affmvp_out_t;
+
+/* map_mv: s16 [rows * i_scu][2 lists][2]; map_refi: s8 [rows * i_scu][2]; ref_ptr: [n_ref][2]
+ * (the POC of refp[i][lidx]).  Returns the number of requests outside the domain (a neighbour
+ * outside the field, a reference index >= n_ref, a zero POC distance, mvr > 2); their output is
+ * zero. */
+int orc_affine_mvp(s64 ptr, const s64 *ref_ptr, int n_ref, const s16 *map_mv, const s8 *map_refi, int i_scu,
+                   int rows, const orc_affmvp_req_t *reqs, int n, orc_affmvp_out_t *out);
+
 /* the picture-level results from the records (src/lookahead.c:255-292): returns the picture
  * SATD cost; icost, icost_uv[2], map_dqp[units] are filled when non-NULL */
 double orc_loka_finish(const orc_loka_cfg_t *cfg, const orc_loka_unit_t *units, double *icost, double *icost_uv,

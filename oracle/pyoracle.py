@@ -232,6 +232,20 @@ class Oracle(_Common):
         self.L.orc_quant_wq(ptr(reqs), len(reqs), ptr(wq4), ptr(wq8), ptr(coefs), ptr(nz))
         return nz
 
+    def affine_mvp(self, ptr_cur, ref_ptr, map_mv, map_refi, i_scu, reqs):
+        """com_get_affine_mvp_scaling for every AFFMVP_REQ; map_mv int16 [rows * i_scu, 2, 2], map_refi
+        int8 [rows * i_scu, 2] (SCU (0, 0) at index i_scu + 1), ref_ptr int64 [n_ref, 2].
+        Returns (out, number of requests outside the domain)"""
+        ref_ptr = np.ascontiguousarray(ref_ptr, dtype=np.int64)
+        map_mv = np.ascontiguousarray(map_mv, dtype=np.int16)
+        map_refi = np.ascontiguousarray(map_refi, dtype=np.int8)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFMVP_REQ)
+        out = np.zeros(len(reqs), dtype=AFFMVP_OUT)
+        rows = len(map_refi) // i_scu
+        bad = self.L.orc_affine_mvp(C.c_int64(ptr_cur), ptr(ref_ptr), len(ref_ptr), ptr(map_mv), ptr(map_refi),
+                                    i_scu, rows, ptr(reqs), len(reqs), ptr(out))
+        return out, bad
+
     def coef_rate(self, levels, reqs):
         """lbac_enc_run_length_cc_rdo for every COEF_RATE_REQ on levels (int16)"""
         levels = np.ascontiguousarray(levels, dtype=np.int16)
@@ -446,6 +460,22 @@ class RefLib(_Common):
                                          ptr(coefs))
         return nz
 
+    def affine_mvp(self, ptr_cur, ref_ptr, map_mv, map_refi, i_scu, reqs):
+        """the reference's com_get_affine_mvp_scaling, one CU per request (requests in the domain)"""
+        ref_ptr = np.ascontiguousarray(ref_ptr, dtype=np.int64)
+        map_mv = np.ascontiguousarray(map_mv, dtype=np.int16)
+        map_refi = np.ascontiguousarray(map_refi, dtype=np.int8)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFMVP_REQ)
+        out = np.zeros(len(reqs), dtype=AFFMVP_OUT)
+        org = i_scu + 1
+        mv0 = C.c_void_p(map_mv.ctypes.data + org * 8)
+        refi0 = C.c_void_p(map_refi.ctypes.data + org * 2)
+        for i, q in enumerate(reqs):
+            self.L.refk_affine_mvp(C.c_int64(ptr_cur), ptr(ref_ptr), len(ref_ptr), mv0, refi0, i_scu, int(q["scup"]),
+                                   int(q["lidx"]), int(q["cur_refi"]), int(q["cu_width"]), int(q["mvr"]),
+                                   C.c_void_p(out.ctypes.data + i * AFFMVP_OUT.itemsize))
+        return out
+
     def coef_rate(self, levels, reqs):
         """the reference's lbac_enc_run_length_cc_rdo, one block per request"""
         levels = np.ascontiguousarray(levels, dtype=np.int16)
@@ -548,6 +578,9 @@ RDOQ_EST = np.dtype([("ctp", "<i4", (2,)), ("cbf", "<i4", (3, 2)), ("run", "<i4"
                      ("lst", "<i4", (2, 6, 12, 2))])
 RDOQ_REQ = np.dtype([("coef_offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), ("qp", "u1"), ("is_intra", "u1"),
                      ("ch_type", "u1"), ("slice_type", "u1"), ("est", "<u2"), ("pad", "<u4"), ("lambda_", "<i8")])
+AFFMVP_REQ = np.dtype([("scup", "<i4"), ("cu_width", "<i2"), ("lidx", "i1"), ("cur_refi", "i1"), ("mvr", "i1"),
+                       ("pad", "i1", (3,))])
+AFFMVP_OUT = np.dtype([("mvp", "<i4", (2, 2))])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
 
 MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],

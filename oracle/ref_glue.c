@@ -545,3 +545,22 @@ int refk_quant_wq(const glue_rdoq_req_t *rq, u8 *wq4, u8 *wq8, s16 *coef)
     return quant_non_zero(core, rq->qp, (double)rq->lambda / 32768.0, rq->is_intra, coef + rq->coef_offset,
                           rq->log2w, rq->log2h, rq->ch_type, rq->slice_type);
 }
+
+/* com_get_affine_mvp_scaling (src/com_util.c:1983) for one CU; map_mv / map_refi point at the
+ * field's SCU (0, 0) (the border before it readable), ref_ptr[n_ref][2] the reference POCs */
+void refk_affine_mvp(s64 ptr, const s64 *ref_ptr, int n_ref, s16 *map_mv, s8 *map_refi, int i_scu, int scup,
+                     int lidx, int cur_refi, int cu_width, int mvr, s32 *mvp_out)
+{
+    static com_ref_pic_t refp[MAX_REFS][REFP_NUM];
+    memset(refp, 0, sizeof(refp));
+    for (int i = 0; i < n_ref && i < MAX_REFS; i++) {
+        refp[i][0].ptr = ref_ptr[i * 2 + 0];
+        refp[i][1].ptr = ref_ptr[i * 2 + 1];
+    }
+    CPMV mvp[VER_NUM][MV_D];
+    com_get_affine_mvp_scaling(ptr, scup, lidx, (s8)cur_refi, (s16(*)[REFP_NUM][MV_D])map_mv,
+                               (s8(*)[REFP_NUM])map_refi, refp, cu_width, cu_width, i_scu, mvp, NULL, NULL,
+                               (u8)mvr);
+    for (int g = 0; g < 2; g++)
+        for (int d = 0; d < 2; d++) mvp_out[g * 2 + d] = mvp[g][d];
+}

@@ -765,6 +765,46 @@ def run_quant_wq(B, p, seed):
     return digest(nz, coefs)
 
 
+def affmvp_inputs(p, seed):
+    """a motion field in the reference's layout (stride w + 2, one border row / column of invalid
+    reference indices), reference POCs on both sides of the current picture and CU requests of
+    every width, list, reference index and AMVR index"""
+    import pyoracle
+    rng = np.random.default_rng(seed)
+    w, h, nref = p["w"], p["h"], p["nref"]
+    i_scu, rows = w + 2, h + 2
+    refi = np.full((rows, i_scu, 2), -1, dtype=np.int8)
+    inner = rng.integers(0, nref, (h, w, 2))
+    inner[rng.random((h, w, 2)) < 0.35] = -1
+    refi[1:h + 1, 1:w + 1] = inner
+    mv = rng.integers(-300, 301, (rows, i_scu, 2, 2))
+    if p.get("big"):
+        wide = rng.random((rows, i_scu, 2, 2)) < 0.3
+        mv[wide] = rng.integers(-32768, 32768, int(wide.sum()))
+    ptr_cur = 40
+    ref_ptr = np.zeros((nref, 2), dtype=np.int64)
+    for i in range(nref):
+        ref_ptr[i, 0] = ptr_cur - (1 << i) if i % 2 == 0 else ptr_cur - 3 * i
+        ref_ptr[i, 1] = ptr_cur + (1 << i) if i % 3 else ptr_cur - 5 - i
+    n = p["n"]
+    reqs = np.zeros(n, dtype=pyoracle.AFFMVP_REQ)
+    widths = [c for c in (8, 16, 32, 64, 128) if c // 4 <= w]
+    for k in range(n):
+        cw = int(rng.choice(widths))
+        x = int(rng.integers(0, w - cw // 4 + 1))
+        y = int(rng.integers(0, h))
+        reqs[k] = (y * i_scu + x, cw, int(rng.integers(0, 2)), int(rng.integers(0, nref)), int(rng.integers(0, 3)),
+                   (0, 0, 0))
+    return ptr_cur, ref_ptr, mv.astype(np.int16).reshape(-1, 2, 2), refi.reshape(-1, 2), i_scu, reqs
+
+
+def run_affmvp(B, p, seed):
+    ptr_cur, ref_ptr, mv, refi, i_scu, reqs = affmvp_inputs(p, seed)
+    res = B.affine_mvp(ptr_cur, ref_ptr, mv, refi, i_scu, reqs)
+    out = res[0] if isinstance(res, tuple) else res
+    return digest(out)
+
+
 def run_rdoq(B, p, seed):
     reqs, ests, coefs = rdoq_inputs(B, p, seed)
     nz = B.rdoq(reqs, ests, coefs)
@@ -775,7 +815,7 @@ RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "coef_rate": run_coef_rate, "quant_wq": run_quant_wq, "rdoq": run_rdoq,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "coef_rate": run_coef_rate, "quant_wq": run_quant_wq, "affmvp": run_affmvp, "rdoq": run_rdoq,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -800,6 +840,10 @@ AFFME_CASES = [
 
 # weighted quantisation cases (quant_non_zero with pic_wq_enable)
 QUANT_WQ_CASES = [dict(n=200), dict(n=120)]
+
+# affine control-point MVP cases (com_get_affine_mvp_scaling): a 4-reference field with small
+# MVs, and a narrow 2-reference field with full-range MVs (the s16 and CPMV clips)
+AFFMVP_CASES = [dict(w=48, h=32, nref=4, n=200), dict(w=30, h=17, nref=2, n=160, big=1)]
 
 # coefficient rate cases (lbac_enc_run_length_cc_rdo)
 COEF_RATE_CASES = [dict(n=200), dict(n=150)]
@@ -897,6 +941,8 @@ def all_cases():
         add("coef_rate", **p)
     for p in QUANT_WQ_CASES:
         add("quant_wq", **p)
+    for p in AFFMVP_CASES:
+        add("affmvp", **p)
     return cases
 
 

@@ -81,6 +81,8 @@ def _declare(L):
     L.uavs3e_cuda_rdoq.argtypes = [P, I, P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_me_affine.argtypes = [P, P, I, P, I, P]
     L.uavs3e_cuda_me_frame.argtypes = [P, I, P, I, P, I, C.c_uint32, P]
+    L.uavs3e_cuda_affine_mvp.argtypes = [C.c_int64, P, I, P, P, I, I, P, I, P]
+    L.uavs3e_cuda_affine_mvp_device.argtypes = [C.c_int64, P, I, P, P, I, I, P, I, P, P, P]
     L.uavs3e_cuda_intra_rmd.argtypes = [P, C.c_size_t, P, I, P]
     L.uavs3e_cuda_coef_rate.argtypes = [P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_quant_wq.argtypes = [P, I, P, P, P, C.c_size_t, P]
@@ -558,3 +560,29 @@ def coef_rate_device(d_reqs, n, d_levels, n_levels, d_out, stream=None):
         import torch
         stream = torch.cuda.current_stream().cuda_stream
     check(lib().uavs3e_cuda_coef_rate_device(d_reqs, n, d_levels, n_levels, d_out, stream), "coef_rate_device")
+
+
+AFFMVP_REQ = np.dtype([("scup", "<i4"), ("cu_width", "<i2"), ("lidx", "i1"), ("cur_refi", "i1"), ("mvr", "i1"),
+                       ("pad", "i1", (3,))])
+AFFMVP_OUT = np.dtype([("mvp", "<i4", (2, 2))])
+
+
+def affine_mvp(ptr_cur, ref_ptr, map_mv, map_refi, i_scu, reqs):
+    """uavs3e_cuda_affine_mvp: com_get_affine_mvp_scaling for every AFFMVP_REQ against the motion
+    field map_mv int16 [rows * i_scu, 2, 2] / map_refi int8 [rows * i_scu, 2] (the encoder's layout:
+    SCU (0, 0) at index i_scu + 1), ref_ptr int64 [n_ref, 2]; returns AFFMVP_OUT"""
+    ref_ptr = np.ascontiguousarray(ref_ptr, dtype=np.int64)
+    map_mv = np.ascontiguousarray(map_mv, dtype=np.int16)
+    map_refi = np.ascontiguousarray(map_refi, dtype=np.int8)
+    reqs = np.ascontiguousarray(reqs, dtype=AFFMVP_REQ)
+    out = np.zeros(max(1, len(reqs)), dtype=AFFMVP_OUT)
+    check(lib().uavs3e_cuda_affine_mvp(int(ptr_cur), ref_ptr.ctypes.data, len(ref_ptr), map_mv.ctypes.data,
+                                       map_refi.ctypes.data, i_scu, len(map_refi) // i_scu, reqs.ctypes.data,
+                                       len(reqs), out.ctypes.data), "affine_mvp")
+    return out[:len(reqs)]
+
+
+def affine_mvp_device(ptr_cur, d_ref_ptr, n_ref, d_map_mv, d_map_refi, i_scu, rows, d_reqs, n, d_out, d_err=None,
+                      stream=None):
+    check(lib().uavs3e_cuda_affine_mvp_device(int(ptr_cur), d_ref_ptr, n_ref, d_map_mv, d_map_refi, i_scu, rows,
+                                              d_reqs, n, d_out, d_err, stream), "affine_mvp_device")

@@ -427,3 +427,152 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_affine_device(int width, int height, const ui
     return launch_me_affine(width, height, d_org, i_org, d_planes, n_slots, i_ref, pad, d_reqs, n, d_out,
                             (cudaStream_t)stream);
 }
+
+// ---------------------------------------------------------------------------------------------
+// Affine control-point MVP: one thread per CU.  The neighbour walk, the POC-distance scaling
+// (ratio = (2^14 / t_neb) * t_cur, C's truncating division first; symmetric rounding shift by
+// 14; s16 clip) and the AMVR rounding of the 1/16-sample value (magnitude rounded, sign kept;
+// 18-bit clip) are integer and follow com_get_affine_mvp_scaling step for step.
+// ---------------------------------------------------------------------------------------------
+static_assert(sizeof(uavs3e_cuda_affmvp_req_t) == 12, "affine MVP request layout");
+static_assert(sizeof(uavs3e_cuda_affmvp_out_t) == 16, "affine MVP result layout");
+
+__device__ __forceinline__ int amvp_scale(int mv, int ratio)
+{
+    const long long t = (long long)mv * ratio;
+    const long long r = t == 0 ? 0 : t > 0 ? (t + 8192) >> 14 : -((-t + 8192) >> 14);
+    return (int)max(-32768ll, min(32767ll, r));
+}
+
+__device__ __forceinline__ int amvp_round(int v, int shift)
+{
+    const int x = v * 4, add = shift > 0 ? 1 << (shift - 1) : 0;
+    const int r = x >= 0 ? ((x + add) >> shift) << shift : -(((-x + add) >> shift) << shift);
+    return max(-131072, min(131071, r));
+}
+
+__global__ void __launch_bounds__(256) k_affine_mvp(long long ptr, const long long *ref_ptr, int n_ref,
+                                                    const short *map_mv, const signed char *map_refi, int i_scu,
+                                                    long long n_field, const uavs3e_cuda_affmvp_req_t *reqs, int n,
+                                                    uavs3e_cuda_affmvp_out_t *out, int *err)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uavs3e_cuda_affmvp_req_t q = reqs[i];
+    uavs3e_cuda_affmvp_out_t o = {};
+    bool bad = q.lidx < 0 || q.lidx > 1 || q.cur_refi < 0 || q.cur_refi >= n_ref || q.mvr < 0 || q.mvr > 2 ||
+               q.cu_width < 4;
+    int t_cur = 0;
+    if (!bad) {
+        t_cur = (int)(ptr * 2 - ref_ptr[q.cur_refi * 2 + q.lidx] * 2);
+        bad = t_cur == 0;
+    }
+    int mv[2][2] = { { 0, 0 }, { 0, 0 } };
+    if (!bad) {
+        const long long base = (long long)i_scu + 1 + q.scup - i_scu;   // the row above the CU
+        const int wsc = q.cu_width >> 2;
+        // A (left, same row), B (above), D (above-left); G (above the last column), C (above-right)
+        const long long nb[5] = { base + i_scu - 1, base, base - 1, base + wsc - 1, base + wsc };
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            bool found = false;
+#pragma unroll
+            for (int k = g == 0 ? 0 : 3; k < (g == 0 ? 3 : 5); k++) {
+                if (found || bad) continue;
+                const long long a = nb[k];
+                if (a < 0 || a >= n_field) { bad = true; continue; }
+                const int refi = map_refi[a * 2 + q.lidx];
+                if (refi < 0) continue;
+                if (refi >= n_ref) { bad = true; continue; }
+                const int t_neb = (int)(ptr * 2 - ref_ptr[refi * 2 + q.lidx] * 2);
+                if (t_neb == 0) { bad = true; continue; }
+                const int ratio = (1 << 14) / t_neb * t_cur;
+                const short2 v = *(const short2 *)(map_mv + (a * 2 + q.lidx) * 2);
+                mv[g][0] = amvp_scale(v.x, ratio);
+                mv[g][1] = amvp_scale(v.y, ratio);
+                found = true;
+            }
+        }
+    }
+    if (!bad) {
+        const int shift = q.mvr == 0 ? 2 : q.mvr == 1 ? 4 : 0;
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            o.mvp[g][0] = amvp_round(mv[g][0], shift);
+            o.mvp[g][1] = amvp_round(mv[g][1], shift);
+        }
+    } else if (err) {
+        atomicAdd(err, 1);
+    }
+    out[i] = o;
+}
+
+int launch_affine_mvp(long long ptr, const long long *d_ref_ptr, int n_ref, const short *d_map_mv,
+                      const signed char *d_map_refi, int i_scu, int rows, const void *d_reqs, int n, void *d_out,
+                      int *d_err, cudaStream_t st)
+{
+    if (n < 0 || n_ref < 1 || i_scu < 3 || rows < 2 || (n > 0 && (!d_ref_ptr || !d_map_mv || !d_map_refi || !d_reqs || !d_out)))
+        return set_status(UC_ERR_ARG, "affine_mvp: bad argument");
+    if (((uintptr_t)d_map_mv & 3) != 0) return set_status(UC_ERR_ARG, "affine_mvp: map_mv not 4-byte aligned");
+    if (n == 0) return UC_OK;
+    k_affine_mvp<<<(n + 255) / 256, 256, 0, st>>>(ptr, d_ref_ptr, n_ref, d_map_mv, d_map_refi, i_scu,
+                                                  (long long)rows * i_scu, (const uavs3e_cuda_affmvp_req_t *)d_reqs, n,
+                                                  (uavs3e_cuda_affmvp_out_t *)d_out, d_err);
+    UC_CHECK(cudaGetLastError());
+    count_launch(1);
+    return UC_OK;
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_affine_mvp_device(int64_t ptr, const int64_t *d_ref_ptr, int n_ref,
+                                                  const int16_t *d_map_mv, const int8_t *d_map_refi, int i_scu,
+                                                  int rows, const uavs3e_cuda_affmvp_req_t *d_reqs, int n,
+                                                  uavs3e_cuda_affmvp_out_t *d_out, int32_t *d_err, void *stream)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    return launch_affine_mvp(ptr, (const long long *)d_ref_ptr, n_ref, d_map_mv, (const signed char *)d_map_refi,
+                             i_scu, rows, d_reqs, n, d_out, (int *)d_err, (cudaStream_t)stream);
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_affine_mvp(int64_t ptr, const int64_t *ref_ptr, int n_ref, const int16_t *map_mv,
+                                           const int8_t *map_refi, int i_scu, int rows,
+                                           const uavs3e_cuda_affmvp_req_t *reqs, int n,
+                                           uavs3e_cuda_affmvp_out_t *out)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (n < 0 || n_ref < 1 || i_scu < 3 || rows < 2 || (n > 0 && (!ref_ptr || !map_mv || !map_refi || !reqs || !out)))
+        return set_status(UC_ERR_ARG, "affine_mvp: bad argument");
+    if (n == 0) return UC_OK;
+    cudaStream_t st = nullptr;
+    UC_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t field = (size_t)rows * i_scu;
+    const size_t b_ref = (size_t)n_ref * 16, b_mv = field * 8, b_refi = (field * 2 + 255) & ~(size_t)255;
+    const size_t b_req = (size_t)n * sizeof(uavs3e_cuda_affmvp_req_t), b_out = (size_t)n * sizeof(uavs3e_cuda_affmvp_out_t);
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    char *buf = nullptr;
+    cudaError_t ce = cudaMallocAsync((void **)&buf, up(b_ref) + up(b_mv) + b_refi + up(b_req) + up(b_out) + 256, st);
+    if (ce != cudaSuccess) { cudaStreamDestroy(st); return check_cuda(ce, "affine_mvp: allocate"); }
+    char *d_ref = buf, *d_mv = d_ref + up(b_ref), *d_refi = d_mv + up(b_mv), *d_req = d_refi + b_refi;
+    char *d_out = d_req + up(b_req), *d_err = d_out + up(b_out);
+    int bad = 0;
+    rc = UC_OK;
+    if ((ce = cudaMemcpyAsync(d_ref, ref_ptr, b_ref, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_mv, map_mv, b_mv, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_refi, map_refi, field * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_req, reqs, b_req, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemsetAsync(d_err, 0, 4, st)) != cudaSuccess)
+        rc = check_cuda(ce, "affine_mvp: upload");
+    if (!rc) rc = launch_affine_mvp(ptr, (const long long *)d_ref, n_ref, (const short *)d_mv,
+                                    (const signed char *)d_refi, i_scu, rows, d_req, n, d_out, (int *)d_err, st);
+    if (!rc && ((ce = cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (ce = cudaMemcpyAsync(&bad, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess))
+        rc = check_cuda(ce, "affine_mvp: download");
+    cudaFreeAsync(buf, st);
+    ce = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return check_cuda(ce, "affine_mvp: synchronise");
+    if (bad) return set_status(UC_ERR_ARG, "affine_mvp: requests outside the domain");
+    return UC_OK;
+}
