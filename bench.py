@@ -707,6 +707,7 @@ def affmvp_part(u, torch, stream, flush, with_cpu, reps=10):
     """com_get_affine_mvp_scaling for every 8x8..128x128 CU position of a 1080p motion field, both
     lists (uavs3e_cuda_affine_mvp_device, one thread per CU)"""
     import cases
+    import numpy as np
     p = dict(w=480, h=270, nref=4, n=0, big=1)
     ptr_cur, ref_ptr, mv, refi, i_scu, _ = cases.affmvp_inputs(p, 91)
     rng = np.random.default_rng(92)
