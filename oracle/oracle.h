@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU restatement of uavs3e's mode-decision kernels (8-bit luma).
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU path: the parity tests,
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle for the GPU path: the parity tests,
  * __graft_entry__.smoke() and bench.py's CPU-baseline leg call it; the product library
  * (libuavs3e_cuda) never links, loads or falls back to it.
  *

@@ -1,11 +1,11 @@
-"""ctypes bindings of the CPU checkers (test infrastructure only).
+"""ctypes bindings of the CPU oracles (test infrastructure only).
 
 ``Oracle``  wraps ``_build/liboracle.so`` (the C restatement, oracle.c); it builds on any host.
 ``RefLib``  wraps ``_ref/libuavs3e_ref.so`` (the reference encoder compiled from its own sources
             by ``make -C oracle ref``); it exists only where the reference sources are present.
 
 Both expose the same Python methods with numpy arguments, so a parity test can run one case
-through either checker and through the GPU library.  Nothing in the product imports this.
+through either oracle library and through the GPU library.  Nothing in the product imports this.
 """
 import ctypes as C
 import os

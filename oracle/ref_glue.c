@@ -1,5 +1,5 @@
 /*
- * ref_glue.c -- checker-side glue compiled together with the reference encoder's own C
+ * ref_glue.c -- test-side glue compiled together with the reference encoder's own C
  * sources (oracle/Makefile, target "ref").  TEST INFRASTRUCTURE ONLY: nothing in the
  * product library links or loads this.
  *
@@ -116,7 +116,7 @@ void refk_intra_pred(pel *nb, pel *dst, int ipm, int w, int h, int bd, int avail
     com_intra_pred(nb + INTRA_NEIB_MID, dst, ipm, w, h, bd, (u16)avail, (u8)ipf);
 }
 
-/* one angular table entry called directly: lets the checker compare the specialised
+/* one angular table entry called directly: lets the tests compare the specialised
  * entries (e.g. intra_pred_ang[4]) with the generic ones called for the same mode */
 void refk_intra_ang_entry(int entry, pel *nb, pel *dst, int i_dst, int mode, int w, int h)
 {

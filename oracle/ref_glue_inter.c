@@ -1,5 +1,5 @@
 /*
- * ref_glue_inter.c -- checker-side glue that compiles the reference's src/inter.c a second time
+ * ref_glue_inter.c -- test-side glue that compiles the reference's src/inter.c a second time
  * (oracle/Makefile, target "ref") to call its file-local affine motion search.  TEST
  * INFRASTRUCTURE ONLY: nothing in the product library links or loads this.
  *

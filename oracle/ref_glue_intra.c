@@ -1,5 +1,5 @@
 /*
- * ref_glue_intra.c -- checker-side glue that compiles the reference's src/intra.c a second time
+ * ref_glue_intra.c -- test-side glue that compiles the reference's src/intra.c a second time
  * (oracle/Makefile, target "ref") to call its file-local make_ipred_list.  TEST INFRASTRUCTURE
  * ONLY: nothing in the product library links or loads this.
  */
