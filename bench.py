@@ -27,7 +27,10 @@ sys.path.insert(0, ROOT)
 W, H, N_REFS, RANGE, QP, PAD = 1920, 1080, 2, 64, 32, 144
 RING = 8                      # distinct frames cycled through (working set > L2)
 CPU_SAMPLE_ROWS = 2           # CTU rows of one frame timed for the CPU baseline
-METRIC = "1080p ME frames/s (bit-exact batched integer+quarter-sample motion search, 2 refs)"
+METRIC = ("1080p full-search ME frames/s (batched motion-search kernel: +-64 integer full search + quarter-sample "
+          "SATD refinement of every 8x8..64x64 block, 2 refs, bit-exact per-candidate costs)")
+REF_SAMPLE_CTUS = 8           # CTUs of a frame searched per step by the reference arm
+REF_CTU_STRIDE = 67           # CTU k of step s: (s * REF_SAMPLE_CTUS + k) * 67 mod 510 (67 is prime to 510)
 
 
 def parse():
@@ -64,15 +67,23 @@ def replica_seed(rank):
 
 
 def workload_config():
+    """the workload of both arms (identical dicts: the GPU arm and the reference arm)"""
     from uavs3e_gb300.synth import lambda_mv_for_qp
     ctus = ((W + 63) // 64) * ((H + 63) // 64)
     return {
-        "workload": "batched integer (+-64 full search) + quarter-sample SATD motion search, 1920x1080 8-bit luma, "
-                    "2 references, blocks 8x8..64x64 incl. 2:1 on the 64x64 CTU grid",
+        "workload": "batched motion search of one 1920x1080 8-bit luma frame (the hot path's frame-level ME kernel, "
+                    "not a full encode): integer full search +-64 and quarter-sample SATD refinement of every block "
+                    "8x8..64x64 incl. 2:1 on the 64x64 CTU grid, against 2 references",
+        "search_rule": "full search of the +-64 window (candidate costs bit-exact with cost_sad / com_had / the "
+                       "me.c cost formula; the TZ search order of me_search_tz is the separate per-call kernel)",
         "width": W, "height": H, "refs": N_REFS, "search_range": RANGE, "qp": QP,
         "lambda_mv": lambda_mv_for_qp(QP), "ctus": ctus, "blocks_per_ctu": 169,
         "int_candidates_per_block": (2 * RANGE + 1) ** 2, "subpel_candidates_per_block": 17,
         "parallelism": "replicas",
+        "l2": "GPU arm: flushed (256 MiB write) before every timed step; per-step CUDA events",
+        "reference_arm_sample": f"each step searches {REF_SAMPLE_CTUS} CTUs spread over the frame (CTU "
+                                f"(step*{REF_SAMPLE_CTUS}+k)*{REF_CTU_STRIDE} mod {ctus}); frames/s = CTUs searched / "
+                                f"{ctus} / time",
     }
 
 
@@ -151,18 +162,24 @@ class CpuSearch:
         self.bl = u.me_blocks(W, H)
         self.org = np.ascontiguousarray(frames[2])
 
-    def time_rows(self, rows, first_row=4, col0=0, ncols=None):
+    def time_ctus(self, ctus):
+        """search every block of the listed CTUs (indices in raster order); returns (seconds, blocks)"""
         np, bl = self.np, self.bl
-        ncols = ncols if ncols is not None else (W + 63) // 64
-        sel = ((bl[:, 1] >= first_row * 64) & (bl[:, 1] < (first_row + rows) * 64) &
-               (bl[:, 0] >= col0 * 64) & (bl[:, 0] < (col0 + ncols) * 64) &
-               (bl[:, 0] + bl[:, 2] <= W) & (bl[:, 1] + bl[:, 3] <= H))
+        sel = np.isin(bl[:, 4], np.asarray(ctus)) & (bl[:, 0] + bl[:, 2] <= W) & (bl[:, 1] + bl[:, 3] <= H)
         blocks = np.zeros(int(sel.sum()), dtype=self.pyoracle.ME_BLOCK)
         blocks["x"], blocks["y"], blocks["w"], blocks["h"] = bl[sel, 0], bl[sel, 1], bl[sel, 2], bl[sel, 3]
         t0 = time.perf_counter()
         self.oracle.me_frame(self.org.ctypes.data, W, self.ptrs, self.stride, W, H, N_REFS, blocks, RANGE, self.lam,
                              threads=self.threads)
         return time.perf_counter() - t0, len(blocks)
+
+    def time_rows(self, rows, first_row=4):
+        cw = (W + 63) // 64
+        return self.time_ctus(list(range(first_row * cw, (first_row + rows) * cw)))
+
+
+def sample_ctus(step, n_ctu):
+    return [((step * REF_SAMPLE_CTUS + k) * REF_CTU_STRIDE) % n_ctu for k in range(REF_SAMPLE_CTUS)]
 
 
 def cpu_baseline(frames, lam, rows=CPU_SAMPLE_ROWS):
@@ -176,6 +193,9 @@ def cpu_baseline(frames, lam, rows=CPU_SAMPLE_ROWS):
 
 
 def run_reference(args):
+    """The CPU arm: the oracle restatement of the path (C, OpenMP over blocks, all host cores) on
+    the GPU arm's workload, a bounded sample of CTUs per step.  Loads only the oracle's library:
+    the block table and the frames are plain Python / numpy."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -183,25 +203,22 @@ def run_reference(args):
     frames = frames_ring()
     lam = lambda_mv_for_qp(QP)
     cs = CpuSearch(frames, lam)
-    ctu_rows, ctu_cols = (H + 63) // 64, (W + 63) // 64
-    n_ctu = ctu_rows * ctu_cols
-    SAMPLE = 8                      # CTUs searched per step (a bounded sample of the frame)
-
-    def step(k):
-        row, col = (k // (ctu_cols // SAMPLE)) % (ctu_rows - 1), (k % (ctu_cols // SAMPLE)) * SAMPLE
-        return cs.time_rows(1, first_row=row, col0=col, ncols=SAMPLE)[0]
-
+    n_ctu = ((H + 63) // 64) * ((W + 63) // 64)
     for k in range(args.warmup):
-        step(k)
-    tot = 0.0
+        cs.time_ctus(sample_ctus(k, n_ctu)[:1])
+    tot, blocks = 0.0, 0
     t0 = time.perf_counter()
     for k in range(args.steps):
-        tot += step(k)
+        dt, nb = cs.time_ctus(sample_ctus(k, n_ctu))
+        tot += dt
+        blocks += nb
     wall = time.perf_counter() - t0
-    v = args.steps * (SAMPLE / n_ctu) / tot
+    v = args.steps * (REF_SAMPLE_CTUS / n_ctu) / tot
     cb = {"value": v, "unit": "frames/s", "cores": cs.threads, "kind": "port",
-          "sample": f"each step: the search of {SAMPLE} of the {n_ctu} CTUs of a 1080p frame (2 refs, integer + "
-                    f"refinement), oracle restatement on all host cores; frames/s = CTUs searched / {n_ctu} / time"}
+          "sample": f"each step: every block of {REF_SAMPLE_CTUS} of the {n_ctu} CTUs of a 1080p frame, spread over "
+                    f"the frame (interior and edge CTUs), 2 refs, integer + refinement ({blocks} blocks in "
+                    f"{args.steps} steps); oracle restatement (the reference's own sources are not on the GPU host) "
+                    f"on all host cores; frames/s = CTUs searched / {n_ctu} / time"}
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
@@ -300,6 +317,27 @@ def lattice_leg(u, torch, stream, flush, peaks, sm_count, sm_mhz, with_cpu, reps
                         "peak_source": f"2 x dp2a issue rate max(measured {dp_clk:.1f}, 64) per clk per SM x "
                                        f"{sm_count} SMs x {sm_mhz:.0f} MHz; matrix-form transform multiply-adds only "
                                        f"(prediction, SATD, quantisation not counted)"}}
+    # end to end through the host-buffer entry uavs3e_cuda_intra_lattice: pinned picture, CUs and
+    # records, the copies inside each call
+    pin_org, pin_rec = (torch.from_numpy(a).pin_memory() for a in (org, rec))
+    pin_cus = torch.from_numpy(cus.view(np.uint8).copy()).pin_memory()
+    pin_satd = torch.empty(n * 33, dtype=torch.int32).pin_memory()
+    pin_q = torch.empty(n * 33 * len(LAT_QPS) * 16, dtype=torch.uint8).pin_memory()
+
+    def e2e():
+        u.check(lib.uavs3e_cuda_intra_lattice(pin_org.data_ptr(), W, pin_rec.data_ptr(), W, W, H, pin_cus.data_ptr(),
+                                              n, 0, qps.ctypes.data, len(qps), 1, pin_satd.data_ptr(),
+                                              pin_q.data_ptr()), "intra_lattice (host)")
+
+    e2e()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        e2e()
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / reps
+    out["e2e"] = {"ms_per_frame": e2e_ms, "frames_per_s": 1000.0 / e2e_ms,
+                  "h2d_bytes_per_step": int(2 * W * H + n * 8),
+                  "d2h_bytes_per_step": int(n * 33 * 4 + n * 33 * len(LAT_QPS) * 16),
+                  "path": "uavs3e_cuda_intra_lattice (pinned host picture, CUs and records; copies inside the call)"}
     out["rmd"] = rmd_part(u, torch, stream, flush, d_satd, cus, with_cpu)
     out["intra_decision"] = intra_decision_part(u, torch, stream, flush, d_org, d_rec, d_cus, cus, qps)
     if with_cpu:
@@ -1106,8 +1144,8 @@ def run_ours(args):
         "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": dict(cfg, l2="flushed (256 MiB write) before every timed step; per-step CUDA events",
-                       launch="each frame replayed as a captured CUDA graph (uavs3e_cuda_me_frame_graph)"),
+        "config": cfg,
+        "launch": "each frame replayed as a captured CUDA graph (uavs3e_cuda_me_frame_graph)",
         "gcandidates_per_s": gcand * value / 1e9,
         "e2e": {"value": world * e2e_steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,

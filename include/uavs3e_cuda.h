@@ -168,7 +168,7 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_frame_graph(uavs3e_cuda_me *me, int slot, con
 
 /*
  * The same search without any allocation -- no cudaMalloc/cudaFree, no allocating library call,
- * no host heap.  It has no counterpart in the reference; it exists for callers that cannot
+ * and no host heap while kernel timing (uavs3e_cuda_profile_enable) is off.  It has no counterpart in the reference; it exists for callers that cannot
  * allocate when they search a frame (an encoder thread working inside a fixed memory budget set
  * up at start-up, or code that must not call cudaMalloc/cudaFree because they synchronise the
  * device).  The caller passes every buffer: d_org (W x H, row stride i_org), d_planes
@@ -179,9 +179,13 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_frame_graph(uavs3e_cuda_me *me, int slot, con
  * array of UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
  * the process exits; frames beyond UAVS3E_CUDA_NOALLOC_MAX_CTUS CTUs (1920x1088), more than
  * UAVS3E_CUDA_NOALLOC_MAX_REFS references or a range above UAVS3E_CUDA_NOALLOC_MAX_RANGE are
- * rejected with UAVS3E_CUDA_ERR_ARG.  The first call on a device looks up the array's device
- * address (and every call with a new size or lambda uploads search tables and waits for that
- * upload), so make the first call on each device before any stream capture.  All calls share
+ * rejected with UAVS3E_CUDA_ERR_ARG.  The call runs on the device uavs3e_cuda_init selected
+ * (device 0 if none): the caller's current device must be that device and the buffers must live
+ * on it, else UAVS3E_CUDA_ERR_ARG.  The first call looks up the array's device address; with lazy
+ * module loading (the CUDA default) that lookup is also when the array is created on the device,
+ * so make the first call at start-up, inside the budget it is meant for, and before any stream
+ * capture.  Every call with a new size, range or lambda uploads search tables and waits for that
+ * upload.  All calls share
  * the one array and the call leaves its contents behind: calls whose GPU work overlaps (other
  * streams, other host threads) race and must be serialised by the caller.
  */
@@ -536,6 +540,14 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i
                                                      int width, int height, const uavs3e_cuda_cu_t *d_cus, int n_cus,
                                                      int ipf, const int *qps, int n_qp, int is_intra_slice,
                                                      uint32_t *d_satd, uavs3e_cuda_lat_q_t *d_q, void *stream);
+/* Host buffers in and out (org / rec with their own strides, cus, satd[n_cus * 33],
+ * q[n_cus * 33 * n_qp]), synchronous: the inputs are copied to device buffers the library keeps
+ * per device, the lattice runs on a stream of its own, the records are copied back.  Calls on
+ * one device are serialised. */
+UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice(const uint8_t *org, int i_org, const uint8_t *rec, int i_rec, int width,
+                                              int height, const uavs3e_cuda_cu_t *cus, int n_cus, int ipf,
+                                              const int *qps, int n_qp, int is_intra_slice, uint32_t *satd,
+                                              uavs3e_cuda_lat_q_t *q);
 /* The same over a subset of modes: d_modes holds n_modes mode indices (0..32) per CU
  * ([n_cus][n_modes], device); only those (CU, mode) records are written.  Used by the pruned
  * search, which evaluates a shortlist of modes per CU. */

@@ -30,8 +30,11 @@ def build_oracle():
     subprocess.run(["make", "-C", HERE, "-s"], check=True)
 
 
-def build_ref(ref_dir="/root/reference"):
-    if not os.path.isdir(ref_dir):
+def build_ref(ref_dir=None):
+    """builds oracle/_ref from the uavs3e source tree ref_dir (default: $UAVS3E_REF_TREE);
+    False when no tree is given or found"""
+    ref_dir = ref_dir or os.environ.get("UAVS3E_REF_TREE")
+    if not ref_dir or not os.path.isdir(os.path.join(ref_dir, "src")):
         return False
     subprocess.run(["make", "-C", HERE, "-s", "-j8", "ref", "REF=" + ref_dir], check=True)
     return True

@@ -2,7 +2,7 @@
 seeded cases of cases.py.
 
 Run where the uavs3e source tree is available (it builds oracle/_ref from it):
-    python tests/golden/make_golden.py [/path/to/uavs3e]
+    python tests/golden/make_golden.py /path/to/uavs3e      (or set UAVS3E_REF_TREE)
 """
 import json
 import os
@@ -18,7 +18,9 @@ import pyoracle  # noqa: E402
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("UAVS3E_REF_TREE")
+    if not ref_dir:
+        sys.exit("usage: make_golden.py <uavs3e source tree> (or set UAVS3E_REF_TREE)")
     if not pyoracle.build_ref(ref_dir):
         sys.exit(f"reference sources not found at {ref_dir}")
     R = pyoracle.RefLib()

@@ -77,3 +77,16 @@ def test_table_twin_has_reference_layout(ref):
     # reference's funs_handle_t; building it is the check, the size is read back here
     ref.L.refk_table_size.restype = C.c_size_t
     assert ref.L.refk_table_size() == 2072
+
+
+def test_block_table_matches_library(lib):
+    # the library's 169-block CTU table (a host query, no device needed) equals the package's
+    # plain-Python table used by the CPU baseline
+    import numpy as np
+    import uavs3e_gb300 as u
+    t = (C.c_int * (169 * 4))()
+    assert lib.uavs3e_cuda_me_block_table(t) == 0
+    assert np.array_equal(np.array(t, dtype=np.int32).reshape(169, 4), u.me_block_table())
+    b = u.me_blocks(200, 136)
+    assert b.shape == (4 * 3 * 169, 6)
+    assert tuple(b[169 * 5 + 3]) == (64 + 24, 64, 8, 8, 5, 3)

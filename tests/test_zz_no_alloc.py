@@ -46,27 +46,35 @@ class CallerPlanes:
             self.ptrs += p
 
 
-def run_both(gpu, torch, frames, org, lam):
-    L = gpu.lib()
-    _declare(L)
-    stream = torch.cuda.current_stream().cuda_stream
-    # the allocating session (existing entry point)
-    ms = gpu.MotionSearch(W, H, n_refs=REFS, search_range=RANGE, pad=PAD)
+def session_results(gpu, frames, org, lam, rng):
+    """the allocating session (the existing entry point) on the same inputs"""
+    ms = gpu.MotionSearch(W, H, n_refs=REFS, search_range=rng, pad=PAD)
     for r, f in enumerate(frames):
         ms.set_ref(r, f)
     want = ms.run(org, lam)
     ms.close()
-    # the no-allocation entry point on caller buffers
-    planes = CallerPlanes(torch, L, frames, stream)
-    d_org = torch.from_numpy(np.ascontiguousarray(org)).cuda()
-    d_out = torch.zeros(len(want) * 32, dtype=torch.uint8, device="cuda")
+    return want
+
+
+def noalloc_call(gpu, torch, planes, d_org, d_out, lam, rng):
+    L = gpu.lib()
+    stream = torch.cuda.current_stream().cuda_stream
     arr = (C.c_void_p * len(planes.ptrs))(*planes.ptrs)
-    rc = L.uavs3e_cuda_me_search_noalloc(d_org.data_ptr(), W, arr, planes.stride, PAD, W, H, REFS, RANGE, lam,
+    rc = L.uavs3e_cuda_me_search_noalloc(d_org.data_ptr(), W, arr, planes.stride, PAD, W, H, REFS, rng, lam,
                                          d_out.data_ptr(), stream)
     assert rc == 0, L.uavs3e_cuda_status_string()
     torch.cuda.synchronize()
-    got = d_out.cpu().numpy().view(gpu.ME_RESULT)
-    return got, want
+    return d_out.cpu().numpy().view(gpu.ME_RESULT).copy()
+
+
+def run_both(gpu, torch, frames, org, lam, rng=RANGE):
+    L = gpu.lib()
+    _declare(L)
+    want = session_results(gpu, frames, org, lam, rng)
+    planes = CallerPlanes(torch, L, frames, torch.cuda.current_stream().cuda_stream)
+    d_org = torch.from_numpy(np.ascontiguousarray(org)).cuda()
+    d_out = torch.zeros(len(want) * 32, dtype=torch.uint8, device="cuda")
+    return noalloc_call(gpu, torch, planes, d_org, d_out, lam, rng), want
 
 
 def test_noalloc_matches_session_twice_in_a_row(gpu):
@@ -78,6 +86,34 @@ def test_noalloc_matches_session_twice_in_a_row(gpu):
     # call 2 right after: other frames and another lambda (new tables, reused scratch)
     got, want = run_both(gpu, torch, [seq[2], seq[1]], seq[3], lambda_mv_for_qp(40))
     assert np.array_equal(got, want)
+    # call 3: the same size, range and lambda as call 2 with other frames (the tables already on
+    # the device are reused), call 4: a smaller range (a shorter table upload)
+    got, want = run_both(gpu, torch, [seq[1], seq[0]], seq[3], lambda_mv_for_qp(40))
+    assert np.array_equal(got, want)
+    got, want = run_both(gpu, torch, [seq[3], seq[2]], seq[1], lambda_mv_for_qp(40), rng=13)
+    assert np.array_equal(got, want)
+
+
+def test_noalloc_call_allocates_no_device_memory(gpu):
+    # with every caller buffer made beforehand, a call changes neither the device's free memory
+    # nor the caller's allocator: the scratch is the library's static array
+    import torch
+    L = gpu.lib()
+    _declare(L)
+    seq = motion_sequence(W, H, 3, seed=5, n_rects=3)
+    planes = CallerPlanes(torch, L, [seq[1], seq[0]], torch.cuda.current_stream().cuda_stream)
+    d_org = torch.from_numpy(np.ascontiguousarray(seq[2])).cuda()
+    n = ((W + 63) // 64) * ((H + 63) // 64) * 169 * REFS
+    d_out = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
+    lam = lambda_mv_for_qp(30)
+    first = noalloc_call(gpu, torch, planes, d_org, d_out, lam, RANGE)      # set-up call
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    for qp in (30, 33):                              # a table-cache hit, then a new lambda
+        noalloc_call(gpu, torch, planes, d_org, d_out, lambda_mv_for_qp(qp), RANGE)
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == alloc0
+    again = noalloc_call(gpu, torch, planes, d_org, d_out, lam, RANGE)
+    assert np.array_equal(first, again)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):

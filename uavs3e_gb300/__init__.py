@@ -59,6 +59,7 @@ def _declare(L):
     L.uavs3e_cuda_lattice_autotune.restype = None
     L.uavs3e_cuda_lattice_budgets.argtypes = [I, P]
     L.uavs3e_cuda_intra_lattice_device.argtypes = [P, I, P, I, I, I, P, I, I, P, I, I, P, P, P]
+    L.uavs3e_cuda_intra_lattice.argtypes = [P, I, P, I, I, I, P, I, I, P, I, I, P, P]
     L.uavs3e_cuda_intra_lattice_modes_device.argtypes = [P, I, P, I, I, I, P, I, P, I, I, P, I, I, P, P, P]
     L.uavs3e_cuda_profile_enable.argtypes = [I]
     L.uavs3e_cuda_launch_count.restype = C.c_ulonglong
@@ -150,6 +151,26 @@ def intra_lattice(org, rec, cus, qps=(27, 32, 37, 42), ipf=0, is_intra=1, stream
     torch.cuda.synchronize()
     return (d_satd.cpu().numpy().view(np.uint32)[:n * 33].copy(),
             d_q.cpu().numpy().view(LAT_Q)[:n * 33 * len(q)].copy())
+
+
+def intra_lattice_host(org, rec, cus, qps=(27, 32, 37, 42), ipf=0, is_intra=1, satd=None, q=None):
+    """Intra lattice through the host-buffer entry uavs3e_cuda_intra_lattice (copies inside the
+    call); returns (satd[n_cus*33], q[n_cus*33*n_qp]).  satd / q may be given (e.g. pinned)."""
+    H, W = org.shape
+    # rows must be contiguous; a row stride larger than the width is passed through
+    org = org if org.dtype == np.uint8 and org.strides[1] == 1 else np.ascontiguousarray(org, np.uint8)
+    rec = rec if rec.dtype == np.uint8 and rec.strides[1] == 1 else np.ascontiguousarray(rec, np.uint8)
+    cus = np.ascontiguousarray(cus)
+    n = len(cus)
+    qa = np.ascontiguousarray(qps, dtype=np.int32)
+    if satd is None:
+        satd = np.zeros(n * 33, np.uint32)
+    if q is None:
+        q = np.zeros(n * 33 * max(1, len(qa)), LAT_Q)
+    check(lib().uavs3e_cuda_intra_lattice(org.ctypes.data, org.strides[0], rec.ctypes.data, rec.strides[0], W, H,
+                                          cus.ctypes.data, n, ipf, qa.ctypes.data, len(qa), is_intra,
+                                          satd.ctypes.data, q.ctypes.data), "intra_lattice")
+    return satd, q
 
 
 # ------------------------------------------------------------------ lookahead cost estimation
@@ -276,22 +297,31 @@ def profile_collect():
     return {k: (ms[i], cnt[i]) for i, k in enumerate(PROF_KERNELS)}
 
 
+# the ten block shapes of the motion search, in result order
+ME_SHAPES = ((8, 8), (16, 8), (8, 16), (16, 16), (32, 16), (16, 32), (32, 32), (64, 32), (32, 64), (64, 64))
+
+
 def me_block_table():
-    t = (C.c_int * (169 * 4))()
-    lib().uavs3e_cuda_me_block_table(t)
-    return np.array(t, dtype=np.int32).reshape(169, 4)
+    """(x, y, w, h) of the 169 blocks of a 64x64 CTU in result order: the shapes of ME_SHAPES,
+    each in raster order.  Plain Python: the CPU baseline uses it without loading the library;
+    uavs3e_cuda_me_block_table returns the same table (tests/test_capi.py)."""
+    return np.array([(x, y, w, h) for w, h in ME_SHAPES for y in range(0, 64, h) for x in range(0, 64, w)],
+                    dtype=np.int32)
 
 
 def me_blocks(width, height):
     """(x, y, w, h, ctu, local) of every result slot in [ctu][block] order."""
     t = me_block_table()
     cw, ch = (width + 63) // 64, (height + 63) // 64
-    out = []
-    for cy in range(ch):
-        for cx in range(cw):
-            for i, (bx, by, bw, bh) in enumerate(t):
-                out.append((cx * 64 + bx, cy * 64 + by, bw, bh, cy * cw + cx, i))
-    return np.array(out, dtype=np.int32)
+    ctu = np.arange(cw * ch, dtype=np.int32)
+    out = np.zeros((cw * ch, len(t), 6), dtype=np.int32)
+    out[:, :, 0] = (ctu % cw)[:, None] * 64 + t[None, :, 0]
+    out[:, :, 1] = (ctu // cw)[:, None] * 64 + t[None, :, 1]
+    out[:, :, 2] = t[None, :, 2]
+    out[:, :, 3] = t[None, :, 3]
+    out[:, :, 4] = ctu[:, None]
+    out[:, :, 5] = np.arange(len(t), dtype=np.int32)[None, :]
+    return out.reshape(-1, 6)
 
 
 class MotionSearch:

@@ -38,7 +38,7 @@ def _stale(out, deps):
 def build(verbose=False, ptxas_info=False):
     os.makedirs(OBJ, exist_ok=True)
     nv = nvcc()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".inc"))]
     headers.append(os.path.join(HERE, "..", "include", "uavs3e_cuda.h"))
     headers += [os.path.join(HERE, "..", "include", f) for f in os.listdir(os.path.join(HERE, "..", "include"))]
     objs, jobs = [], []

@@ -260,6 +260,30 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     return UC_OK;
 }
 
+// host-buffer entry: per device, the device copies of the inputs and outputs (grown as needed)
+// and a stream of its own; calls on one device are serialised by its mutex
+struct LatHost {
+    std::mutex mu;
+    cudaStream_t st = nullptr;
+    u8 *org = nullptr, *rec = nullptr;
+    LatCu *cus = nullptr;
+    u32 *satd = nullptr;
+    LatQ *q = nullptr;
+    size_t org_cap = 0, rec_cap = 0, cu_cap = 0, satd_cap = 0, q_cap = 0;   // elements
+};
+static LatHost g_lat_host[64];
+
+template <typename T> static int grow(T **p, size_t *cap, size_t n)
+{
+    if (*cap >= n) return UC_OK;
+    if (*p) UC_CHECK(cudaFree(*p));
+    *p = nullptr;
+    *cap = 0;
+    UC_CHECK(cudaMalloc((void **)p, n * sizeof(T)));
+    *cap = n;
+    return UC_OK;
+}
+
 }  // namespace uc
 
 using namespace uc;
@@ -315,6 +339,44 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_modes_device(const uint8_t *d_org,
     if (width % 4 || height % 4) return set_status(UC_ERR_ARG, "intra_lattice: picture size must be a multiple of 4");
     return launch_intra_lattice(d_org, i_org, d_rec, i_rec, width, height, (const LatCu *)d_cus, n_cus, d_modes, n_modes,
                                 ipf, qps, n_qp, is_intra_slice, d_satd, (LatQ *)d_q, (cudaStream_t)stream);
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice(const uint8_t *org, int i_org, const uint8_t *rec, int i_rec, int width,
+                                              int height, const uavs3e_cuda_cu_t *cus, int n_cus, int ipf,
+                                              const int *qps, int n_qp, int is_intra_slice, uint32_t *satd,
+                                              uavs3e_cuda_lat_q_t *q)
+{
+    int r = ensure_init();
+    if (r) return r;
+    if (!org || !rec || !cus || !satd || (n_qp > 0 && (!q || !qps)) || n_cus < 0)
+        return set_status(UC_ERR_ARG, "intra_lattice: null pointer");
+    if (width <= 0 || height <= 0 || width % 4 || height % 4 || i_org < width || i_rec < width)
+        return set_status(UC_ERR_ARG, "intra_lattice: picture size must be a positive multiple of 4");
+    if (n_qp < 0 || n_qp > LAT_MAX_QP) return set_status(UC_ERR_ARG, "intra_lattice: bad qp count");
+    if (n_cus == 0) return UC_OK;
+    int dev = 0;
+    UC_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "intra_lattice: device index");
+    LatHost &S = g_lat_host[dev];
+    std::lock_guard<std::mutex> lk(S.mu);
+    if (!S.st) UC_CHECK(cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking));
+    const size_t pic = (size_t)width * height;
+    const size_t nq = (size_t)n_cus * 33 * (size_t)(n_qp > 0 ? n_qp : 1);
+    if ((r = grow(&S.org, &S.org_cap, pic)) || (r = grow(&S.rec, &S.rec_cap, pic)) ||
+        (r = grow(&S.cus, &S.cu_cap, (size_t)n_cus)) || (r = grow(&S.satd, &S.satd_cap, (size_t)n_cus * 33)) ||
+        (r = grow(&S.q, &S.q_cap, nq)))
+        return r;
+    UC_CHECK(cudaMemcpy2DAsync(S.org, width, org, i_org, width, height, cudaMemcpyHostToDevice, S.st));
+    UC_CHECK(cudaMemcpy2DAsync(S.rec, width, rec, i_rec, width, height, cudaMemcpyHostToDevice, S.st));
+    UC_CHECK(cudaMemcpyAsync(S.cus, cus, (size_t)n_cus * sizeof(LatCu), cudaMemcpyHostToDevice, S.st));
+    r = launch_intra_lattice(S.org, width, S.rec, width, width, height, S.cus, n_cus, nullptr, 33, ipf, qps, n_qp,
+                             is_intra_slice, S.satd, n_qp > 0 ? S.q : nullptr, S.st);
+    if (r) return r;
+    UC_CHECK(cudaMemcpyAsync(satd, S.satd, (size_t)n_cus * 33 * sizeof(u32), cudaMemcpyDeviceToHost, S.st));
+    if (n_qp > 0)
+        UC_CHECK(cudaMemcpyAsync(q, S.q, (size_t)n_cus * 33 * n_qp * sizeof(LatQ), cudaMemcpyDeviceToHost, S.st));
+    UC_CHECK(cudaStreamSynchronize(S.st));
+    return UC_OK;
 }
 
 UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i_org, const uint8_t *d_rec, int i_rec,

@@ -41,8 +41,9 @@ static_assert(NA_OFF_SUB % 256 == 0 && NA_OFF_Q2 % 16 == 0 && NA_OFF_R2M % 16 ==
 // the scratch every call of this entry point uses
 static __device__ __align__(256) unsigned char g_me_scratch[NA_BYTES];
 
-// per device: the scratch's device address (set-up on the first call with that device current)
-// and the parameters of the search tables it currently holds
+// the scratch's device address on the library's device (looked up by the first call, with that
+// device current) and the parameters of the search tables it currently holds; indexed by device
+// ordinal, though every call runs on the device uavs3e_cuda_init selected
 struct NaDevice {
     unsigned char *scratch = nullptr;
     bool tables = false;
@@ -78,16 +79,26 @@ extern "C" UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_or
     if ((uint64_t)lambda_mv * 36u >= (1ull << 32)) return set_status(UC_ERR_ARG, "me_search_noalloc: lambda_mv too large");
     for (int i = 0; i < n_refs * 16; i++)
         if (!d_planes[i]) return set_status(UC_ERR_ARG, "me_search_noalloc: null plane");
+    // the caller's buffers must live on the library's device: ensure_init makes that device
+    // current, so a caller on another device gets an argument error (and its device back)
+    int caller_dev = 0;
+    UC_CHECK(cudaGetDevice(&caller_dev));
     int r = ensure_init();
     if (r) return r;
     int dev = 0;
     UC_CHECK(cudaGetDevice(&dev));
+    if (dev != caller_dev) {
+        cudaSetDevice(caller_dev);
+        return set_status(UC_ERR_ARG, "me_search_noalloc: the current device is not the library's device "
+                                      "(uavs3e_cuda_init)");
+    }
     if (dev < 0 || dev >= 64) return set_status(UC_ERR_UNSUPPORTED, "me_search_noalloc: device index");
     NaDevice &D = g_na[dev];
     cudaStream_t st = (cudaStream_t)stream;
     if (!D.scratch) {
-        // once per device, with that device current: the array's device address (host code may
-        // not use the symbol itself)
+        // once, with the library's device current: the array's device address (host code may
+        // not use the symbol itself).  Under lazy module loading this lookup also loads this
+        // file's module, which is when the array is created on the device.
         void *p = nullptr;
         UC_CHECK(cudaGetSymbolAddress(&p, g_me_scratch));
         D.scratch = (unsigned char *)p;

@@ -1,8 +1,9 @@
 // Host-built transform and scan tables, uploaded once per device.
 //
-// The integer DCT2/DCT8/DST7 matrices are generated from the same closed forms as the
-// encoder (com_dct_coef_create, src/com_tables.c:222-278: sqrt(N)*32 times the orthonormal
-// basis, rounded half away from zero).  The DCT2 partial butterflies of the encoder
+// The integer DCT2/DCT8/DST7 matrices are the encoder's (com_dct_coef_create,
+// src/com_tables.c:222-278: sqrt(N)*32 times the orthonormal basis, rounded half away from
+// zero), frozen as constant data in dct_matrices.inc (gen_dct_matrices.py) rather than
+// recomputed with the host's cos() at start-up.  The DCT2 partial butterflies of the encoder
 // (src/transform.c:57-251, src/com_itdq.c:47-262) only read the first N/2^(l+1) entries of each
 // row and rebuild the rest by even/odd symmetry; fold_dct2() builds the matrix those
 // butterflies effectively apply, so the kernels can use plain matrix products with results
@@ -11,28 +12,12 @@
 #include "common.cuh"
 #include "tables.h"
 
-#include <math.h>
 #include <string.h>
 #include <vector>
 
 namespace uc {
 
-static void gen_dct(int L, s8 *T /* [3][N][N] */)
-{
-    const double PI = 3.14159265358979323846;
-    int c = 1 << L;
-    double s = sqrt((double)c) * 32;
-    for (int k = 0; k < c; k++)
-        for (int n = 0; n < c; n++) {
-            double w0 = k == 0 ? sqrt(0.5) : 1;
-            double v = cos(PI * (n + 0.5) * k / c) * w0 * sqrt(2.0 / c);
-            T[0 * c * c + k * c + n] = (s8)(s * v + (v > 0 ? 0.5 : -0.5));
-            v = cos(PI * (k + 0.5) * (n + 0.5) / (c + 0.5)) * sqrt(2.0 / (c + 0.5));
-            T[1 * c * c + k * c + n] = (s8)(s * v + (v > 0 ? 0.5 : -0.5));
-            v = sin(PI * (k + 0.5) * (n + 1) / (c + 0.5)) * sqrt(2.0 / (c + 0.5));
-            T[2 * c * c + k * c + n] = (s8)(s * v + (v > 0 ? 0.5 : -0.5));
-        }
-}
+#include "dct_matrices.inc"
 
 // even/odd decomposition run on unit vectors: row k uses the difference vector of level
 // ctz(k)+1, rows 0 and N/2 the final two-entry sum vector
@@ -101,7 +86,7 @@ static bool g_host_ok = false;
 const HostTables &host_tables()
 {
     if (!g_host_ok) {
-        for (int L = 1; L <= 6; L++) gen_dct(L, g_host.dct[L]);
+        for (int L = 1; L <= 6; L++) memcpy(g_host.dct[L], kDctMat[L], (size_t)3 << (2 * L));
         for (int L = 2; L <= 6; L++) {
             fold_dct2(L, g_host.dct[L], g_host.fold[L]);
             eff_dct87(L, g_host.dct[L], g_host.d87[0][L], g_host.d87[1][L]);
