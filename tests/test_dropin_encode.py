@@ -36,15 +36,15 @@ def write_yuv(path, n_frames=8):
             f.write(np.clip(d - 16, 0, 255).astype(np.uint8).tobytes())
 
 
-def encode(tmp, tag, env_extra=None):
+def encode(tmp, tag, env_extra=None, n_frames=8, timeout=600):
     env = dict(os.environ)
     env.update(env_extra or {})
     bs, rec = os.path.join(tmp, tag + ".bin"), os.path.join(tmp, tag + "_rec.yuv")
-    cmd = [ENC, "-i", os.path.join(tmp, "in.yuv"), "-w", "416", "-h", "240", "-d", "8", "-f", "8", "-q", "37",
+    cmd = [ENC, "-i", os.path.join(tmp, "in.yuv"), "-w", "416", "-h", "240", "-d", "8", "-f", str(n_frames), "-q", "37",
            "-p", "0", "-g", "0", "--ctu_size", "64", "--wpp_threads", "1", "--frm_threads", "1", "--fps_num", "30",
            "--fps_den", "1", "-v", "0", "-o", bs, "-r", rec]
     # the encoder writes psnr.txt into its working directory: run it inside the test's folder
-    r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=600, cwd=tmp)
+    r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=timeout, cwd=tmp)
     assert r.returncode == 0, r.stderr[-2000:]
     md5 = [hashlib.md5(open(p, "rb").read()).hexdigest() for p in (bs, rec)]
     return md5, r.stderr + r.stdout

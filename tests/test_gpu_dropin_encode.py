@@ -1,0 +1,48 @@
+"""GPU: the unchanged reference encoder on libuavs3e_cuda's kernel-table entries.
+
+The reference encoder application (oracle/_ref/uavs3enc, compiled from the uavs3e sources by
+`make -C oracle ref REF=<uavs3e source tree>`) encodes the seeded 416x240 8-bit 4:2:0 sequence of
+the CPU-runnable configuration (low delay, QP 37, 64x64 CTU, one thread) twice: with its own C
+kernel table, and with uavs3e_cuda_preload.so, which installs every hot-path member of the table
+as the GPU entries right after uavs3e_create.  The bitstream and the reconstruction must be
+identical, the library must report status 0 and must have launched kernels.
+
+Every call of the encoder's search loops is then one GPU round trip (the per-call entries; the
+batched entry points are the throughput path), so this is a boundary check, not a speed run.
+UAVS3E_DROPIN_FRAMES sets the frame count (default 2: one intra and one inter picture).
+Skipped where the encoder is not built (the uavs3e sources are not on every GPU host).
+"""
+import os
+import re
+import time
+
+import pytest
+
+from test_dropin_encode import ENC, encode, write_yuv
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not os.path.exists(ENC),
+                                 reason="reference encoder not built on this host (make -C oracle ref REF=<uavs3e "
+                                        "source tree>)")]
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PRELOAD = os.path.join(ROOT, "uavs3e_gb300", "libuavs3e_cuda_preload.so")
+
+
+def test_reference_encoder_on_gpu_entries_gives_the_reference_bitstream(gpu, tmp_path):
+    n = int(os.environ.get("UAVS3E_DROPIN_FRAMES", "2"))
+    tmp = str(tmp_path)
+    write_yuv(os.path.join(tmp, "in.yuv"), n)
+    t0 = time.perf_counter()
+    plain, _ = encode(tmp, "plain", n_frames=n)
+    t1 = time.perf_counter()
+    got, log = encode(tmp, "gpu", {"LD_PRELOAD": PRELOAD}, n_frames=n, timeout=5400)
+    t2 = time.perf_counter()
+    assert "kernel table installed (GPU entries)" in log
+    m = re.search(r"uavs3e_cuda_preload: status (-?\d+) \(([^)]*)\), (\d+) kernel launches", log)
+    assert m, log[-2000:]
+    assert int(m.group(1)) == 0, m.group(2)
+    assert int(m.group(3)) > 0
+    assert got == plain, f"md5 (bitstream, reconstruction) {got} != reference {plain}"
+    print(f"\ndrop-in encode, {n} frames: md5 {plain[0]} (both); reference C table {t1 - t0:.1f} s, "
+          f"GPU entries {t2 - t1:.1f} s, {m.group(3)} kernel launches")

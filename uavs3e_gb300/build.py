@@ -13,6 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libuavs3e_cuda.so")
+PRELOAD = os.path.join(HERE, "libuavs3e_cuda_preload.so")
+PRELOAD_SRC = os.path.join(HERE, "dropin", "preload.c")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr"]
 
@@ -62,6 +64,15 @@ def build(verbose=False, ptxas_info=False):
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    # the LD_PRELOAD wrapper that installs the entries into an unchanged encoder
+    if _stale(PRELOAD, [PRELOAD_SRC, LIB] + headers):
+        cc = os.environ.get("CC", "gcc")
+        cmd = [cc, "-O2", "-fPIC", "-shared", "-std=gnu11", "-Wall", "-o", PRELOAD, PRELOAD_SRC, "-L" + HERE,
+               "-luavs3e_cuda", "-Wl,-rpath,$ORIGIN", "-ldl"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("preload build failed")
     return LIB
 
 
