@@ -176,10 +176,11 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_frame_graph(uavs3e_cuda_me *me, int slot, con
  * ref*16 + dy*4 + dx, 0 = integer plane; padded by `pad` >= 144 with stride i_ref, e.g. filled
  * by uavs3e_cuda_pad_plane + uavs3e_cuda_subpel_planes) and d_out (uavs3e_cuda_me_block_table
  * order, (W+63)/64 * (H+63)/64 * 169 * n_refs records).  The scratch lives in one static device
- * array of UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
- * the process exits; frames beyond UAVS3E_CUDA_NOALLOC_MAX_CTUS CTUs (1920x1088), more than
- * UAVS3E_CUDA_NOALLOC_MAX_REFS references or a range above UAVS3E_CUDA_NOALLOC_MAX_RANGE are
- * rejected with UAVS3E_CUDA_ERR_ARG.  The call runs on the device uavs3e_cuda_init selected
+ * array of UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES (about 38 MB: the search's keys, refinement sums and
+ * tables, and the byte-shifted reference copies its windows are staged from) that every GPU
+ * loading this library holds until the process exits; frames beyond UAVS3E_CUDA_NOALLOC_MAX_CTUS
+ * CTUs or the padded area of 1920x1088, more than UAVS3E_CUDA_NOALLOC_MAX_REFS references or a
+ * range above UAVS3E_CUDA_NOALLOC_MAX_RANGE are rejected with UAVS3E_CUDA_ERR_ARG.  The call runs on the device uavs3e_cuda_init selected
  * (device 0 if none): the caller's current device must be that device and the buffers must live
  * on it, else UAVS3E_CUDA_ERR_ARG.  The first call looks up the array's device address; with lazy
  * module loading (the CUDA default) that lookup is also when the array is created on the device,
@@ -192,7 +193,7 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_frame_graph(uavs3e_cuda_me *me, int slot, con
 #define UAVS3E_CUDA_NOALLOC_MAX_CTUS      510
 #define UAVS3E_CUDA_NOALLOC_MAX_REFS      2
 #define UAVS3E_CUDA_NOALLOC_MAX_RANGE     64
-#define UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES 14143744u
+#define UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES 38449408u
 UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_org, int i_org, const uint8_t *const *d_planes,
                                                   int i_ref, int pad, int width, int height, int n_refs, int range,
                                                   uint32_t lambda_mv, uavs3e_cuda_me_result_t *d_out, void *stream);
@@ -684,11 +685,12 @@ UAVS3E_CUDA_API int uavs3e_cuda_quant_wq_device(const uavs3e_cuda_rdoq_req_t *d_
 
 /* ---------------------------------------------------------------------------------------
  * Learned CU-partition / intra-mode pruning network (no counterpart in the reference: the
- * learned part stands beside the bit-exact path and never changes it).  bf16 tensor-core
- * implicit-GEMM convolutions with FP32 accumulation; all pointers are device memory.
- * Activations NHWC bf16; weights [Cout][Kp] bf16 (k = (ky * ks + kx) * Cin + ci, Kp = ks*ks*Cin
- * rounded up to 16); biases, gradients and Adam state FP32.  Shapes: Cin even, Cout a multiple
- * of 8 (16 for wgrad), batch x output pixels a multiple of 16, ks 1 or 3 (padding ks/2). */
+ * learned part stands beside the bit-exact path and never changes it).  Implicit-GEMM
+ * convolutions on the 5th-generation tensor cores (tcgen05.mma, bf16 operands, FP32
+ * accumulation in tensor memory); all pointers are device memory.  Activations NHWC bf16;
+ * weights [Cout][Kp] bf16 (k = (ky * ks + kx) * Cin + ci, Kp = ks*ks*Cin rounded up to 16);
+ * biases, gradients and Adam state FP32.  Shapes: Cin even (a multiple of 16 for dgrad), Cout a
+ * multiple of 16 up to 64, batch x output pixels a multiple of 16, ks 1 or 3 (padding ks/2). */
 
 /* y = act(conv(x, w) + bias): y bf16, or FP32 when y_f32; relu 0/1. */
 UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int y_f32,
@@ -702,6 +704,9 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_dgrad(const void *dy, const void *w, co
 /* dw = dy^T x_col [cout][kp], db = sum dy (both overwritten). */
 UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_wgrad(const void *dy, const void *x, float *dw, float *db, int batch, int hin,
                                                int win, int cin, int cout, int ks, int stride, int kp, void *stream);
+/* Number of tensor-core convolution CTAs that gave up waiting for their MMAs (a bounded wait;
+ * their outputs were left unwritten) since the previous call; 0 in normal operation. */
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_timeouts(void);
 /* Network input of n CTUs at (ctu_xy[2i], ctu_xy[2i+1]) of a picture: [n][64][64][2] bf16. */
 UAVS3E_CUDA_API int uavs3e_cuda_cnn_input(const uint8_t *d_pic, int stride, int width, int height,
                                           const int *d_ctu_xy, int n, int qp, void *x0, void *stream);

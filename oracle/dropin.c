@@ -13,6 +13,9 @@
  * UAVS3E_DROPIN_SKIP (environment) lists member families to leave as the reference's:
  * "intra,mc,frame,recon,dquant,itx,tx,sad,ssd,satd,pel,quant".  UAVS3E_DROPIN_PLANT=satd adds
  * 1 to every 8x8 SATD (a planted mistake: the check must then see a different bitstream).
+ * UAVS3E_DROPIN_COSTLOG=1 records every cost call of the table as installed
+ * (uavs3e_gb300/dropin/costlog.h): with every family skipped, that is the reference's own
+ * functions, the record the GPU entries' record is compared with.
  */
 #define _GNU_SOURCE
 #include <dlfcn.h>
@@ -22,6 +25,7 @@
 
 #include "oracle.h"
 #include "../include/uavs3e_cuda_table.h"
+#include "../uavs3e_gb300/dropin/costlog.h"
 
 #define CLIP8(v) ((v) < 0 ? 0 : (v) > 255 ? 255 : (v))
 
@@ -205,6 +209,7 @@ void *uavs3e_create(void *cfg, int *err)
         exit(3);
     }
     install(t);
+    if (getenv("UAVS3E_DROPIN_COSTLOG") && getenv("UAVS3E_DROPIN_COSTLOG")[0] == '1') costlog_install(t);
     fprintf(stderr, "dropin: kernel table replaced by the oracle restatement\n");
     return h;
 }

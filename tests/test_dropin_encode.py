@@ -10,6 +10,7 @@ the bitstream.  Skipped where the reference is not built (the GPU host).
 """
 import hashlib
 import os
+import re
 import subprocess
 
 import numpy as np
@@ -60,3 +61,39 @@ def test_oracle_kernel_table_encodes_the_reference_bitstream(tmp_path):
     planted, log = encode(tmp, "planted", {"LD_PRELOAD": SHIM, "UAVS3E_DROPIN_PLANT": "satd"})
     assert "kernel table replaced" in log
     assert planted[0] != plain[0]
+
+
+ALL_FAMILIES = "intra,mc,frame,recon,dquant,itx,tx,sad,ssd,satd,pel,quant"
+
+
+def costlog(log):
+    """the 'costlog:' line of an encode's stderr (uavs3e_gb300/dropin/costlog.h) as a tuple"""
+    m = re.search(r"costlog: sad (\d+) sad_x3 (\d+) sad_x4 (\d+) ssd (\d+) satd (\d+) hash ([0-9a-f]{16})", log)
+    assert m, log[-2000:]
+    return tuple(int(v) for v in m.groups()[:5]) + (m.group(6),)
+
+
+def reference_costlog(tmp, n_frames):
+    """md5 and cost-call record of the reference's own kernel table (every family left in place,
+    its cost members wrapped by the record)"""
+    md5, log = encode(tmp, "refcost", {"LD_PRELOAD": SHIM, "UAVS3E_DROPIN_SKIP": ALL_FAMILIES,
+                                       "UAVS3E_DROPIN_COSTLOG": "1"}, n_frames=n_frames)
+    return md5, costlog(log)
+
+
+def test_cost_calls_of_the_oracle_table_match_the_reference(tmp_path):
+    # every SAD / SAD x3 / x4 / SSD / SATD call of a 2-frame encode returns the same value, in
+    # the same order, through the oracle restatement as through the reference's own functions
+    tmp = str(tmp_path)
+    write_yuv(os.path.join(tmp, "in.yuv"), 2)
+    plain, _ = encode(tmp, "plain", n_frames=2)
+    ref_md5, ref_log = reference_costlog(tmp, 2)
+    assert ref_md5 == plain
+    assert sum(ref_log[:5]) > 100000
+    md5, log = encode(tmp, "oracle", {"LD_PRELOAD": SHIM, "UAVS3E_DROPIN_COSTLOG": "1"}, n_frames=2)
+    assert md5 == plain
+    assert costlog(log) == ref_log
+    # a planted SATD mistake shows up in the record
+    _, log = encode(tmp, "planted", {"LD_PRELOAD": SHIM, "UAVS3E_DROPIN_COSTLOG": "1", "UAVS3E_DROPIN_PLANT": "satd"},
+                    n_frames=2)
+    assert costlog(log)[5] != ref_log[5]

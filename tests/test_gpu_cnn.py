@@ -50,6 +50,8 @@ def test_forward_backward_match_oracle(gpu, B, seed):
     for i, (dw, db) in enumerate(grads):
         assert rel(net.gw[i].cpu().numpy(), dw) < 2e-2, f"weight gradient {i}"
         assert rel(net.gb[i].cpu().numpy(), db) < 2e-2, f"bias gradient {i}"
+    # every tensor-core tile completed its MMAs within the bounded wait
+    assert gpu.lib().uavs3e_cuda_cnn_timeouts() == 0
 
 
 def test_adam_step_matches_formula(gpu):

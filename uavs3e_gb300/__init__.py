@@ -107,7 +107,8 @@ def init(device=0):
     check(lib().uavs3e_cuda_init(device), "uavs3e_cuda_init")
 
 
-PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz", "mc", "rdoq", "affme")
+PROF_KERNELS = ("pad", "subpel_planes", "me_int", "me_sub", "intra_lattice", "loka", "tz", "mc", "rdoq", "affme",
+                "shift_planes")
 
 CU = np.dtype([("x", "<i2"), ("y", "<i2"), ("w", "u1"), ("h", "u1"), ("pad", "<u2")])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])

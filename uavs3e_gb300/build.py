@@ -65,7 +65,7 @@ def build(verbose=False, ptxas_info=False):
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
     # the LD_PRELOAD wrapper that installs the entries into an unchanged encoder
-    if _stale(PRELOAD, [PRELOAD_SRC, LIB] + headers):
+    if _stale(PRELOAD, [PRELOAD_SRC, os.path.join(HERE, "dropin", "costlog.h"), LIB] + headers):
         cc = os.environ.get("CC", "gcc")
         cmd = [cc, "-O2", "-fPIC", "-shared", "-std=gnu11", "-Wall", "-o", PRELOAD, PRELOAD_SRC, "-L" + HERE,
                "-luavs3e_cuda", "-Wl,-rpath,$ORIGIN", "-ldl"]

@@ -1,9 +1,11 @@
 // C ABI of libuavs3e_cuda: library state, status, frame interpolation and the batched
 // motion-search session (include/uavs3e_cuda.h).
 #include "common.cuh"
+#include "tma.cuh"
 #include "uavs3e_cuda_internal.h"
 #include "../../include/uavs3e_cuda.h"
 
+#include <cudaTypedefs.h>
 #include <mutex>
 #include <stdio.h>
 #include <string.h>
@@ -102,6 +104,34 @@ void prof_end(int k, cudaStream_t st)
     cudaEvent_t e = prof_event();
     cudaEventRecord(e, st);
     g_prof_ev[k].push_back({ b, e });
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+static std::once_flag g_encode_once;
+
+int encode_tensor_map_u8(CUtensorMap *map, const void *base, uint64_t row_bytes, uint64_t rows, uint64_t pitch,
+                         uint32_t box_w, uint32_t box_h)
+{
+    std::call_once(g_encode_once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            g_encode_tiled = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    });
+    if (!g_encode_tiled) return set_status(UC_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    if (((uintptr_t)base & 15) || (pitch & 15) || (box_w & 15) || box_w > 256 || box_h > 256 || !box_w || !box_h)
+        return set_status(UC_ERR_ARG, "tensor map: alignment or box size");
+    const cuuint64_t dims[2] = { row_bytes, rows };
+    const cuuint64_t strides[1] = { pitch };
+    const cuuint32_t box[2] = { box_w, box_h };
+    const cuuint32_t elem[2] = { 1, 1 };
+    const CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void *>(base), dims, strides,
+                                      box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_status(UC_ERR_ARG, "cuTensorMapEncodeTiled failed");
+    return UC_OK;
 }
 
 int launch_pad_plane(pel *p, int W, int H, int pad, int stride, cudaStream_t st)
@@ -223,6 +253,7 @@ struct uavs3e_cuda_me {
     MeResult *out_buf = nullptr;      // device results for host runs
     u64 *keys = nullptr;              // per-block integer winners
     u32 *sub = nullptr;               // per-candidate SATD sums of the refinement
+    pel *shift = nullptr;             // byte-shifted reference copies of the integer search
     u32 *q2 = nullptr;                // device search tables
     u16 *r2m = nullptr;
     MeTables tab;
@@ -304,9 +335,11 @@ UAVS3E_CUDA_API uavs3e_cuda_me *uavs3e_cuda_me_open(int width, int height, int n
               cudaMalloc(&m->out_buf, nres * sizeof(MeResult)) == cudaSuccess &&
               cudaMalloc(&m->keys, me_key_scratch_bytes(width, height, n_refs)) == cudaSuccess &&
               cudaMalloc(&m->sub, me_sub_scratch_bytes(width, height, n_refs)) == cudaSuccess &&
+              cudaMalloc(&m->shift, me_shift_scratch_bytes(width, height, n_refs)) == cudaSuccess &&
               cudaMalloc(&m->q2, me_q2_entries(range, kNdy) * sizeof(u32)) == cudaSuccess &&
               cudaMalloc(&m->r2m, (size_t)ME_R2M_ENTRIES * sizeof(u16)) == cudaSuccess &&
-              cudaMemset(m->planes_buf, 0, m->plane_bytes * 16 * n_refs) == cudaSuccess;
+              cudaMemset(m->planes_buf, 0, m->plane_bytes * 16 * n_refs) == cudaSuccess &&
+              cudaMemset(m->shift, 0, me_shift_scratch_bytes(width, height, n_refs)) == cudaSuccess;
     if (!ok) {
         set_status(UC_ERR_MEMORY, "me_open: device allocation failed");
         uavs3e_cuda_me_close(m);
@@ -320,7 +353,7 @@ UAVS3E_CUDA_API void uavs3e_cuda_me_close(uavs3e_cuda_me *m)
     if (!m) return;
     if (m->st) cudaStreamSynchronize(m->st);
     cudaFree(m->planes_buf); cudaFree(m->org_buf); cudaFree(m->out_buf); cudaFree(m->ref_stage);
-    cudaFree(m->keys); cudaFree(m->sub); cudaFree(m->q2); cudaFree(m->r2m); cudaFree(m->tz_buf);
+    cudaFree(m->keys); cudaFree(m->sub); cudaFree(m->shift); cudaFree(m->q2); cudaFree(m->r2m); cudaFree(m->tz_buf);
     cudaFree(m->chroma_buf); cudaFree(m->mc_buf);
     for (auto &g : m->graphs) cudaGraphExecDestroy(g.exec);
     if (m->st) cudaStreamDestroy(m->st);
@@ -332,6 +365,8 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_num_results(const uavs3e_cuda_me *m)
     return m ? m->n_ctu * ME_BLOCKS_PER_CTU * m->n_refs : 0;
 }
 
+// a slot's new integer plane: padding, the 15 fractional planes and the byte-shifted copies the
+// integer search's windows are staged from
 static int me_interp_slot(uavs3e_cuda_me *m, int slot, cudaStream_t st)
 {
     pel *p0 = me_plane_ptr(m, slot, 0);
@@ -339,7 +374,11 @@ static int me_interp_slot(uavs3e_cuda_me *m, int slot, cudaStream_t st)
     if (r) return r;
     PlaneSet15 ps;
     for (int i = 0; i < 15; i++) ps.p[i] = me_plane_ptr(m, slot, i + 1);
-    return launch_subpel_planes(p0, m->stride, m->W, m->H, m->pad, ps, st);
+    r = launch_subpel_planes(p0, m->stride, m->W, m->H, m->pad, ps, st);
+    if (r) return r;
+    const pel *src[1] = { p0 };
+    return launch_shift_planes(src, 1, m->stride, m->W, m->H,
+                               m->shift + (size_t)slot * (me_shift_scratch_bytes(m->W, m->H, 1)), st);
 }
 
 UAVS3E_CUDA_API int uavs3e_cuda_me_set_ref(uavs3e_cuda_me *m, int slot, const uint8_t *plane, int stride)
@@ -374,7 +413,8 @@ static int me_launch(uavs3e_cuda_me *m, const pel *d_org, int i_org, u32 lambda,
         for (int q = 0; q < 16; q++) a.planes[s][q] = me_plane_ptr(m, s, q);
     a.i_ref = m->stride; a.pad = m->pad;
     a.W = m->W; a.H = m->H; a.n_refs = m->n_refs; a.range = m->range; a.lambda_mv = lambda;
-    a.out = d_out; a.q2tab = m->q2; a.rank2mv = m->r2m; a.sub_scratch = m->sub;
+    a.out = d_out; a.q2tab = m->q2; a.rank2mv = m->r2m; a.sub_scratch = m->sub; a.shift_scratch = m->shift;
+    a.shift_ready = true;             // kept current by me_interp_slot
     return launch_me_frame(a, m->tab, m->keys, st);
 }
 

@@ -5,17 +5,25 @@
 // (stride 2, ReLU; 2 -> 16 -> 32 -> 32 -> 64 channels, 64x64 -> 4x4) feed a 1x1 head with 48
 // outputs per cell: [split16, split32 part, split64 part, 33 mode logits, 12 unused].
 //
-// Convolutions are implicit GEMMs on the bf16 tensor cores with FP32 accumulation
-// (mma.sync m16n8k16): forward (rows = output pixels, K = taps x input channels), data gradient
-// (rows = input pixels, K = taps x output channels, with the previous layer's ReLU mask applied
-// on store) and weight gradient (rows = output channels, K = output pixels, split over CTAs with
-// FP32 atomics).  Activations are NHWC bf16, weights [Cout][K] bf16 with FP32 master copies
-// updated by Adam.
+// Convolutions are implicit GEMMs on the 5th-generation tensor cores (tcgen05.mma, bf16 x bf16
+// with FP32 accumulation in tensor memory): forward (rows = output pixels, K = taps x input
+// channels), data gradient (rows = input pixels, K = taps x output channels, with the previous
+// layer's ReLU mask applied on store) and weight gradient, computed transposed (rows = taps x
+// input channels, N = output channels, K = output pixels, split over CTAs with FP32 atomics).  A
+// CTA of 128 threads owns a 128-row tile: it gathers the operands chunk by chunk (64 columns of
+// K) into shared memory in the MMA's K-major layout, one thread issues the MMAs into a TMEM
+// accumulator of 128 lanes x N columns, and the four warps read their 32 lanes back for the
+// epilogue.  Activations are NHWC bf16, weights [Cout][K] bf16 with FP32 master copies updated
+// by Adam.
 #include "common.cuh"
+#include "tma.cuh"
+#include "umma.cuh"
 #include "uavs3e_cuda_internal.h"
 #include "../../include/uavs3e_cuda.h"
 
 #include <cuda_bf16.h>
+#include <string.h>
+#include <algorithm>
 
 namespace uc {
 
@@ -31,14 +39,6 @@ struct ConvShape {
 __device__ __forceinline__ u32 pack_bf16(bf16 lo, bf16 hi)
 {
     return (u32)__bfloat16_as_ushort(lo) | ((u32)__bfloat16_as_ushort(hi) << 16);
-}
-
-__device__ __forceinline__ void mma_bf16(float (&c)[4], const u32 (&a)[4], const u32 (&b)[2])
-{
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                 "{%0,%1,%2,%3};"
-                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
 // im2col element pair (k, k+1) of output pixel m (k even; the pair shares a tap because Cin is
@@ -70,78 +70,6 @@ __device__ __forceinline__ u32 dgrad_pair(const bf16 *dy, const ConvShape &S, in
     return *reinterpret_cast<const u32 *>(dy + (((size_t)b * S.Hout + oy) * S.Wout + ox) * S.Cout + co);
 }
 
-// one warp per 16 x 64 output tile (rows x columns); columns beyond N are skipped
-// MODE 0: forward, y = act(x (*) w + bias), rows = output pixels, N = Cout, y bf16 or f32
-// MODE 1: data gradient, dx = mask(x_in) * (dy (*) w^T), rows = input pixels, N = Cin
-template <int MODE>
-__global__ void __launch_bounds__(128) k_conv_gemm(ConvShape S, const bf16 *src, const bf16 *wmat, int wrow,
-                                                     const float *bias, void *dst, int dst_f32, int relu,
-                                                     const bf16 *mask)
-{
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int M = MODE == 0 ? S.B * S.Hout * S.Wout : S.B * S.Hin * S.Win;
-    const int N = MODE == 0 ? S.Cout : S.Cin;
-    const int K = MODE == 0 ? S.Kp : S.ks * S.ks * S.Cout;
-    const int m0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * 16;
-    const int n_base = blockIdx.y * 64;
-    if (m0 >= M) return;
-    float acc[8][4];
-#pragma unroll
-    for (int f = 0; f < 8; f++)
-#pragma unroll
-        for (int i = 0; i < 4; i++) acc[f][i] = 0.f;
-    for (int k0 = 0; k0 < K; k0 += 16) {
-        u32 a[4];
-        const int ka = k0 + 2 * t;
-        if (MODE == 0) {
-            a[0] = fwd_pair(src, S, m0 + g, ka);
-            a[1] = fwd_pair(src, S, m0 + g + 8, ka);
-            a[2] = fwd_pair(src, S, m0 + g, ka + 8);
-            a[3] = fwd_pair(src, S, m0 + g + 8, ka + 8);
-        } else {
-            a[0] = dgrad_pair(src, S, m0 + g, ka);
-            a[1] = dgrad_pair(src, S, m0 + g + 8, ka);
-            a[2] = dgrad_pair(src, S, m0 + g, ka + 8);
-            a[3] = dgrad_pair(src, S, m0 + g + 8, ka + 8);
-        }
-#pragma unroll
-        for (int f = 0; f < 8; f++) {
-            const int n = n_base + f * 8 + g;
-            if (n_base + f * 8 >= N) break;
-            u32 b[2];
-            const bf16 *wr = wmat + (size_t)n * wrow;
-            b[0] = *reinterpret_cast<const u32 *>(wr + ka);
-            b[1] = *reinterpret_cast<const u32 *>(wr + ka + 8);
-            mma_bf16(acc[f], a, b);
-        }
-    }
-#pragma unroll
-    for (int f = 0; f < 8; f++) {
-        if (n_base + f * 8 >= N) break;
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int m = m0 + g + 8 * h, n = n_base + f * 8 + 2 * t;
-            float v0 = acc[f][2 * h], v1 = acc[f][2 * h + 1];
-            if (MODE == 0) {
-                v0 += bias[n]; v1 += bias[n + 1];
-                if (relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
-            } else {
-                // the layer input is the previous layer's ReLU output: zero where it was clipped
-                const u32 xm = *reinterpret_cast<const u32 *>(mask + (size_t)m * N + n);
-                if (!(xm & 0x7FFFu)) v0 = 0.f;
-                if (!(xm & 0x7FFF0000u)) v1 = 0.f;
-            }
-            if (dst_f32) {
-                float *o = (float *)dst + (size_t)m * N + n;
-                o[0] = v0; o[1] = v1;
-            } else {
-                *reinterpret_cast<u32 *>((bf16 *)dst + (size_t)m * N + n) =
-                    pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
-            }
-        }
-    }
-}
-
 // im2col element of output pixel m, k (scalar)
 __device__ __forceinline__ bf16 fwd_elem(const bf16 *x, const ConvShape &S, int m, int k)
 {
@@ -155,37 +83,182 @@ __device__ __forceinline__ bf16 fwd_elem(const bf16 *x, const ConvShape &S, int 
     return x[(((size_t)b * S.Hin + iy) * S.Win + ix) * S.Cin + ci];
 }
 
-// weight gradient dw[co][k] += sum_m dy[m][co] x_col[m][k] over this CTA's chunk of rows m;
-// one warp per 16 (co) x 8 (k) tile, grid.z splits the output pixels
-constexpr int WG_CHUNK = 512;
+// ---------------------------------------------------------------- tensor-core GEMM tiles
 
-__global__ void __launch_bounds__(128) k_conv_wgrad(ConvShape S, const bf16 *dy, const bf16 *x, float *dw)
+constexpr int TC_M = 128;        // rows of a tile (the MMA's M)
+constexpr int TC_KC = 64;        // columns of K gathered per chunk
+constexpr int TC_THREADS = 128;
+constexpr int WG_CHUNK = 512;    // output pixels per CTA of the weight gradient
+constexpr uint32_t TC_POLLS = 1u << 22;
+// dynamic shared memory reserved (unused) by every launch so that at most 7 CTAs share an SM:
+// their TMEM accumulators (at most 64 columns each) then always fit the SM's 512 columns and
+// no CTA waits in its allocation
+constexpr int TC_SMEM_RESERVE = 8 * 1024;
+static __device__ unsigned int g_tc_timeouts;   // CTAs that gave up waiting for their MMAs
+
+struct TcArgs {
+    ConvShape S;
+    const bf16 *src;     // MODE 0: x; MODE 1: dy; MODE 2: x (the pixel rows' inputs)
+    const bf16 *wmat;    // MODE 0: w [Cout][Kp]; MODE 1: w^T [Cin][taps*Cout]; MODE 2: dy
+    int wrow;            // row length of wmat (MODE 0 / 1)
+    const float *bias;
+    void *dst; int dst_f32, relu;
+    const bf16 *mask;    // MODE 1: the layer input (ReLU output of the previous layer)
+    float *dw;           // MODE 2
+};
+
+// MODE 0: forward, y = act(x (*) w + bias), rows = output pixels, N = Cout
+// MODE 1: data gradient, dx = mask(x_in) * (dy (*) w^T), rows = input pixels, N = Cin
+// MODE 2: weight gradient, dw^T[k][co] += sum over this CTA's output pixels of x_col[m][k] dy[m][co]
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int M = S.B * S.Hout * S.Wout;
-    const int tile = blockIdx.x * 4 + (threadIdx.x >> 5);
-    const int n_tiles_k = S.Kp / 8;
-    const int co0 = (tile / n_tiles_k) * 16, k0 = (tile % n_tiles_k) * 8;
-    if (co0 >= S.Cout) return;
-    const int mb = blockIdx.z * WG_CHUNK, me = min(M, mb + WG_CHUNK);
-    float acc[4] = { 0.f, 0.f, 0.f, 0.f };
-    for (int m = mb; m < me; m += 16) {
-        u32 a[4], b[2];
-        const int r0 = m + 2 * t, r1 = r0 + 1, r2 = r0 + 8, r3 = r0 + 9;
-        const bf16 *d0 = dy + (size_t)r0 * S.Cout, *d1 = dy + (size_t)r1 * S.Cout;
-        const bf16 *d2 = dy + (size_t)r2 * S.Cout, *d3 = dy + (size_t)r3 * S.Cout;
-        a[0] = pack_bf16(d0[co0 + g], d1[co0 + g]);
-        a[1] = pack_bf16(d0[co0 + g + 8], d1[co0 + g + 8]);
-        a[2] = pack_bf16(d2[co0 + g], d3[co0 + g]);
-        a[3] = pack_bf16(d2[co0 + g + 8], d3[co0 + g + 8]);
-        b[0] = pack_bf16(fwd_elem(x, S, r0, k0 + g), fwd_elem(x, S, r1, k0 + g));
-        b[1] = pack_bf16(fwd_elem(x, S, r2, k0 + g), fwd_elem(x, S, r3, k0 + g));
-        mma_bf16(acc, a, b);
+    __shared__ __align__(128) unsigned char sa[TC_M * TC_KC * 2];
+    __shared__ __align__(128) unsigned char sb[64 * TC_KC * 2];
+    __shared__ __align__(8) u64 bar;
+    __shared__ u32 s_tmem;
+    const ConvShape &S = T.S;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = MODE == 0 ? S.Cout : MODE == 1 ? S.Cin : S.Cout;
+    const int ncols = N <= 32 ? 32 : 64;
+    // rows of the tile and the reduction range
+    int M, K, r0, kb = 0;
+    if (MODE == 0) { M = S.B * S.Hout * S.Wout; K = S.Kp; r0 = blockIdx.x * TC_M; }
+    else if (MODE == 1) { M = S.B * S.Hin * S.Win; K = S.ks * S.ks * S.Cout; r0 = blockIdx.x * TC_M; }
+    else { M = S.Kp; r0 = blockIdx.x * TC_M; kb = blockIdx.y * WG_CHUNK;
+           K = min(WG_CHUNK, S.B * S.Hout * S.Wout - kb); K = (K + 15) & ~15; }
+    const u32 bar_a = smem_u32(&bar);
+    if (warp == 0) tmem_alloc(smem_u32(&s_tmem), (u32)ncols);
+    if (tid == 0) {
+        mbar_init(bar_a, 1);
+        mbar_fence_init();
     }
-    float *o0 = dw + (size_t)(co0 + g) * S.Kp + k0 + 2 * t;
-    float *o1 = dw + (size_t)(co0 + g + 8) * S.Kp + k0 + 2 * t;
-    atomicAdd(o0, acc[0]); atomicAdd(o0 + 1, acc[1]);
-    atomicAdd(o1, acc[2]); atomicAdd(o1 + 1, acc[3]);
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    const u32 tmem = s_tmem;
+    const u32 idesc = umma_idesc_bf16(TC_M, N);
+    u32 phase = 0;
+    bool ok = true;
+    const int npix = MODE == 2 ? S.B * S.Hout * S.Wout : 0;
+
+    for (int k0 = 0; k0 < K && ok; k0 += TC_KC) {
+        const int kc = min(TC_KC, K - k0);         // a multiple of 16
+        const int kq = kc >> 3;                    // 16-byte units per row
+        // A: TC_M rows x kc columns; 8 consecutive threads write one 128-byte core matrix
+        for (int u = tid; u < TC_M * kq; u += TC_THREADS) {
+            const int r = (u & 7) + 8 * ((u >> 3) / kq), q = (u >> 3) % kq;
+            u32 v[4];
+            if (MODE == 0) {
+                const int m = r0 + r;
+#pragma unroll
+                for (int i = 0; i < 4; i++) v[i] = m < M ? fwd_pair(T.src, S, m, k0 + 8 * q + 2 * i) : 0u;
+            } else if (MODE == 1) {
+                const int m = r0 + r;
+#pragma unroll
+                for (int i = 0; i < 4; i++) v[i] = m < M ? dgrad_pair(T.src, S, m, k0 + 8 * q + 2 * i) : 0u;
+            } else {
+                // row r = input-column index kk of x_col, columns = output pixels kb + k0 + 8q + j
+                const int kk = r0 + r;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int m = kb + k0 + 8 * q + 2 * i;
+                    const bf16 z = __float2bfloat16(0.f);
+                    const bf16 e0 = (kk < S.Kp && m < npix) ? fwd_elem(T.src, S, m, kk) : z;
+                    const bf16 e1 = (kk < S.Kp && m + 1 < npix) ? fwd_elem(T.src, S, m + 1, kk) : z;
+                    v[i] = pack_bf16(e0, e1);
+                }
+            }
+            *reinterpret_cast<uint4 *>(sa + umma_tile_off(r, 8 * q, kc)) = make_uint4(v[0], v[1], v[2], v[3]);
+        }
+        // B: N rows x kc columns
+        for (int u = tid; u < N * kq; u += TC_THREADS) {
+            const int n = (u & 7) + 8 * ((u >> 3) / kq), q = (u >> 3) % kq;
+            uint4 v;
+            if (MODE != 2) {
+                v = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)n * T.wrow + k0 + 8 * q);
+            } else {
+                u32 w[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int m = kb + k0 + 8 * q + 2 * i;
+                    const bf16 z = __float2bfloat16(0.f);
+                    const bf16 e0 = m < npix ? T.wmat[(size_t)m * S.Cout + n] : z;
+                    const bf16 e1 = m + 1 < npix ? T.wmat[(size_t)(m + 1) * S.Cout + n] : z;
+                    w[i] = pack_bf16(e0, e1);
+                }
+                v = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+            *reinterpret_cast<uint4 *>(sb + umma_tile_off(n, 8 * q, kc)) = v;
+        }
+        // the operands written by the threads become visible to the tensor core
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after_sync();
+            const u32 a0 = smem_u32(sa), b0 = smem_u32(sb);
+            for (int s = 0; s < (kc >> 4); s++)
+                umma_bf16(tmem, umma_desc(a0 + 256 * s, 128, kc * 16), umma_desc(b0 + 256 * s, 128, kc * 16), idesc,
+                          (k0 | s) != 0);
+            umma_commit(bar_a);
+        }
+        // the chunk's MMAs must complete before the next chunk overwrites the operands
+        const bool done = mbar_wait_bounded(bar_a, phase, TC_POLLS);
+        phase ^= 1;
+        ok = !__syncthreads_or(!done);
+        if (!ok) {
+            if (tid == 0) atomicAdd(&g_tc_timeouts, 1u);
+            mbar_wait_bounded(bar_a, phase ^ 1, TC_POLLS);   // the commit may still arrive
+        }
+    }
+    tc_fence_after_sync();
+
+    if (ok) {
+        // epilogue: warp w holds rows 32w .. 32w + 31 of the tile in TMEM lanes of its quarter
+        const int r = 32 * warp + lane;
+        for (int c = 0; c < N; c += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((u32)(32 * warp) << 16) + (u32)c, v);
+            if (MODE == 0) {
+                const int m = r0 + r;
+                if (m < M) {
+#pragma unroll
+                    for (int i = 0; i < 16; i += 2) {
+                        float v0 = v[i] + T.bias[c + i], v1 = v[i + 1] + T.bias[c + i + 1];
+                        if (T.relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                        if (T.dst_f32) {
+                            float *o = (float *)T.dst + (size_t)m * N + c + i;
+                            o[0] = v0; o[1] = v1;
+                        } else {
+                            *reinterpret_cast<u32 *>((bf16 *)T.dst + (size_t)m * N + c + i) =
+                                pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
+                        }
+                    }
+                }
+            } else if (MODE == 1) {
+                const int m = r0 + r;
+                if (m < M) {
+#pragma unroll
+                    for (int i = 0; i < 16; i += 2) {
+                        // the layer input is the previous layer's ReLU output: zero where it was clipped
+                        const u32 xm = *reinterpret_cast<const u32 *>(T.mask + (size_t)m * N + c + i);
+                        const float v0 = (xm & 0x7FFFu) ? v[i] : 0.f, v1 = (xm & 0x7FFF0000u) ? v[i + 1] : 0.f;
+                        *reinterpret_cast<u32 *>((bf16 *)T.dst + (size_t)m * N + c + i) =
+                            pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
+                    }
+                }
+            } else {
+                const int kk = r0 + r;
+                if (kk < S.Kp) {
+#pragma unroll
+                    for (int i = 0; i < 16; i++) atomicAdd(T.dw + (size_t)(c + i) * S.Kp + kk, v[i]);
+                }
+            }
+        }
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, (u32)ncols);
 }
 
 // bias gradient db[co] += sum_m dy[m][co]
@@ -322,12 +395,14 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_fwd(const void *x, const void *w, const
     int r = ensure_init();
     if (r) return r;
     ConvShape S;
-    if (!x || !w || !bias || !y || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
+    if (!x || !w || !bias || !y || Cout % 16 || Cout > 64 || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
         return set_status(UC_ERR_ARG, "cnn_conv_fwd: shape");
     const int M = B * S.Hout * S.Wout;
-    dim3 grid((M / 16 + 3) / 4, (Cout + 63) / 64);
-    k_conv_gemm<0><<<grid, 128, 0, (cudaStream_t)stream>>>(S, (const bf16 *)x, (const bf16 *)w, Kp, bias, y, y_f32,
-                                                            relu, nullptr);
+    TcArgs T;
+    memset(&T, 0, sizeof(T));
+    T.S = S; T.src = (const bf16 *)x; T.wmat = (const bf16 *)w; T.wrow = Kp; T.bias = bias;
+    T.dst = y; T.dst_f32 = y_f32; T.relu = relu;
+    k_conv_tc<0><<<(M + TC_M - 1) / TC_M, TC_THREADS, TC_SMEM_RESERVE, (cudaStream_t)stream>>>(T);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     return UC_OK;
@@ -340,16 +415,19 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_dgrad(const void *dy, const void *w, co
     int r = ensure_init();
     if (r) return r;
     ConvShape S;
-    if (!dy || !w || !x || !dx || !wt_scratch || Cin % 8 || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
+    if (!dy || !w || !x || !dx || !wt_scratch || Cin % 16 || Cin > 64 ||
+        !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
         return set_status(UC_ERR_ARG, "cnn_conv_dgrad: shape");
     cudaStream_t st = (cudaStream_t)stream;
     const int taps = ks * ks, nw = Cout * Cin * taps;
     k_transpose_w<<<(nw + 255) / 256, 256, 0, st>>>((const bf16 *)w, Cout, Cin, taps, Kp, (bf16 *)wt_scratch);
     UC_CHECK(cudaGetLastError());
     const int M = B * Hin * Win;
-    dim3 grid((M / 16 + 3) / 4, (Cin + 63) / 64);
-    k_conv_gemm<1><<<grid, 128, 0, st>>>(S, (const bf16 *)dy, (const bf16 *)wt_scratch, taps * Cout, nullptr, dx, 0, 0,
-                                         (const bf16 *)x);
+    TcArgs T;
+    memset(&T, 0, sizeof(T));
+    T.S = S; T.src = (const bf16 *)dy; T.wmat = (const bf16 *)wt_scratch; T.wrow = taps * Cout;
+    T.dst = dx; T.mask = (const bf16 *)x;
+    k_conv_tc<1><<<(M + TC_M - 1) / TC_M, TC_THREADS, TC_SMEM_RESERVE, st>>>(T);
     UC_CHECK(cudaGetLastError());
     count_launch(2);
     return UC_OK;
@@ -361,21 +439,35 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_wgrad(const void *dy, const void *x, fl
     int r = ensure_init();
     if (r) return r;
     ConvShape S;
-    if (!dy || !x || !dw || !db || Cout % 16 || Cout > 256 || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
+    if (!dy || !x || !dw || !db || Cout % 16 || Cout > 64 || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
         return set_status(UC_ERR_ARG, "cnn_conv_wgrad: shape");
     cudaStream_t st = (cudaStream_t)stream;
     const int M = B * S.Hout * S.Wout;
     UC_CHECK(cudaMemsetAsync(dw, 0, (size_t)Cout * Kp * sizeof(float), st));
     UC_CHECK(cudaMemsetAsync(db, 0, (size_t)Cout * sizeof(float), st));
-    const int tiles = (Cout / 16) * (Kp / 8);
-    dim3 grid((tiles + 3) / 4, 1, (M + WG_CHUNK - 1) / WG_CHUNK);
-    k_conv_wgrad<<<grid, 128, 0, st>>>(S, (const bf16 *)dy, (const bf16 *)x, dw);
+    TcArgs T;
+    memset(&T, 0, sizeof(T));
+    T.S = S; T.src = (const bf16 *)x; T.wmat = (const bf16 *)dy; T.dw = dw;
+    dim3 grid((Kp + TC_M - 1) / TC_M, (M + WG_CHUNK - 1) / WG_CHUNK);
+    k_conv_tc<2><<<grid, TC_THREADS, TC_SMEM_RESERVE, st>>>(T);
     UC_CHECK(cudaGetLastError());
     const int rows = 256 / Cout;
     k_conv_bgrad<<<std::min(1024, (M + rows - 1) / rows), rows * Cout, 0, st>>>((const bf16 *)dy, M, Cout, db);
     UC_CHECK(cudaGetLastError());
     count_launch(2);
     return UC_OK;
+}
+
+// CTAs of the tensor-core convolutions that gave up waiting for their MMAs since the last call
+// (their outputs were not written)
+UAVS3E_CUDA_API int uavs3e_cuda_cnn_timeouts(void)
+{
+    int r = ensure_init();
+    if (r) return r;
+    unsigned int n = 0, zero = 0;
+    UC_CHECK(cudaMemcpyFromSymbol(&n, g_tc_timeouts, sizeof(n)));
+    UC_CHECK(cudaMemcpyToSymbol(g_tc_timeouts, &zero, sizeof(zero)));
+    return (int)n;
 }
 
 UAVS3E_CUDA_API int uavs3e_cuda_cnn_input(const uint8_t *d_pic, int stride, int width, int height, const int *d_ctu_xy,

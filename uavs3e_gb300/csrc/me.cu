@@ -20,6 +20,7 @@
 // IMNMX.  Per-group winners are merged into a 64-bit (cost << 15 | raster) key, first in
 // shared memory, then across the four class CTAs with global atomics.
 #include "common.cuh"
+#include "tma.cuh"
 #include "uavs3e_cuda_internal.h"
 #include <algorithm>
 
@@ -63,7 +64,13 @@ size_t me_sub_scratch_bytes(int W, int H, int n_refs)
 size_t me_key_scratch_bytes(int W, int H, int n_refs)
 {
     size_t nctu = (size_t)((W + 63) / 64) * ((H + 63) / 64);
-    return nctu * n_refs * ME_BLOCKS_PER_CTU * sizeof(u64);
+    return nctu * n_refs * ME_BLOCKS_PER_CTU * sizeof(u64) + 2 * sizeof(u32);
+}
+
+size_t me_shift_scratch_bytes(int W, int H, int n_refs)
+{
+    const size_t pitch = ((size_t)W + 2 * 144 + 15) & ~(size_t)15;
+    return (size_t)n_refs * 4 * pitch * (size_t)(H + 2 * 144);
 }
 
 // Search items.  Candidates of one alignment class c (dx index = c mod 4) are cut into main
@@ -108,14 +115,39 @@ int me_build_tables(int W, int H, int range, u32 lambda_mv, int ndy, MeTables *t
     }
     if (pos > q2cap) return UC_ERR_ARG;
     t->n_entries = (int)pos;
+    // Item order: the two lane groups of a warp run items it and it + 1 (it even) side by side,
+    // and their window words differ by their dx index difference k' - k.  The list therefore
+    // starts with every row's pairs (k, k + 16), k < 16, so such partners sit 16 words (16 banks)
+    // apart and the two half-warps' 16-bank sets do not overlap; the dx indices left unpaired
+    // (k >= 32, or all of them below 17 offsets) follow, row by row.
     for (int c = 0; c < ME_CLASSES; c++) {
+        const int n = t->n_dx[c];
+        const int pairs = n >= 17 ? std::min(16, n - 16) : 0;
+        int left[64], nl = 0;
+        if (n > 64) return UC_ERR_ARG;
+        for (int k = 0; k < n; k++)
+            if (!(k < pairs || (k >= 16 && k < 16 + pairs))) left[nl++] = k;
+        // (dx index, row) of entry ri of a list of `rows` rows
+        const auto entry = [&](int ri, int rows, int *k, int *row) {
+            if (ri < rows * 2 * pairs) {
+                const int j = ri % (2 * pairs);
+                *row = ri / (2 * pairs);
+                *k = (j >> 1) + ((j & 1) ? 16 : 0);
+            } else {
+                const int r2 = ri - rows * 2 * pairs;
+                *row = r2 / nl;
+                *k = left[r2 % nl];
+            }
+        };
         for (int it = 0; it < t->n_main[c]; it++) {
-            const int ri = it % nm_real[c];
-            q2tab[t->d_main[c] + it] = (u32)(ri % t->n_dx[c]) | (u32)(ndy * (ri / t->n_dx[c])) << 16;
+            int k, row;
+            entry(it % nm_real[c], t->nfull, &k, &row);
+            q2tab[t->d_main[c] + it] = (u32)k | (u32)(ndy * row) << 16;
         }
         for (int it = 0; it < t->n_tail[c]; it++) {
-            const int ri = it % nt_real[c];
-            q2tab[t->d_tail[c] + it] = (u32)(ri % t->n_dx[c]) | (u32)(ndy * t->nfull + ri / t->n_dx[c]) << 16;
+            int k, row;
+            entry(it % nt_real[c], t->rem, &k, &row);
+            q2tab[t->d_tail[c] + it] = (u32)k | (u32)(ndy * t->nfull + row) << 16;
         }
     }
     for (int c = 0; c < ME_CLASSES; c++)
@@ -150,15 +182,20 @@ int me_build_tables(int W, int H, int range, u32 lambda_mv, int ndy, MeTables *t
     return UC_OK;
 }
 
-// words per stored window row: data (at most 56 words at range 64), the largest skew (18)
-// and 2 spare; a multiple of 4, so rows 16 apart start on the same bank before the skew, and a
-// compile-time constant, so every row address of an item is an immediate offset
-constexpr int ME_WIN_WW = 76;
+// words per window row in shared memory: the TMA box is PITCH * 4 = 224 bytes wide, enough for
+// range 64 (the largest byte a lane reads is 15 + 48 + 128 + 3 + 12 < 224).  A compile-time
+// pitch keeps every row address of an item an immediate offset.
+constexpr int ME_WIN_PITCH = 56;
+constexpr int ME_WIN_BYTES_W = ME_WIN_PITCH * 4;
+// byte-shifted copies of a reference plane: fixed padding and geometry (see k_shift_planes)
+constexpr int ME_SHIFT_PAD = 144;
+// polls of a window's mbarrier before the search gives up (about a second)
+constexpr uint32_t ME_TMA_POLLS = 1u << 22;
 
 struct MeIntParams {
+    CUtensorMap maps[ME_MAX_REFS][4];   // per reference and byte shift s: the plane shifted left by s
     const pel *org; int i_org;
-    const pel *ref[ME_MAX_REFS]; int i_ref;
-    int W, H, ctus_w;
+    int W, H, ctus_w, ctus_h;
     int lo_x, hi_x, lo_y, hi_y, ndx;
     int n_main[ME_CLASSES], n_tail[ME_CLASSES];     // items per class (multiples of ME_GROUPS)
     int q2_main[ME_CLASSES], q2_tail[ME_CLASSES];   // offsets into q2tab
@@ -167,32 +204,22 @@ struct MeIntParams {
     u32 mul, one, minus1;  // 2^11, 1, 2^32-1 as run-time values: key arithmetic stays on IMAD
     const u32 *q2tab; const u16 *rank2mv;
     u64 *keys;             // [ctu][ref][169]
+    u32 *ctl;              // [1]: 0xFFFFFFFF, or 0 once a CTA gave up waiting for its window
     int n_refs;
-    int win_h;             // window rows (row pitch: ME_WIN_WW words)
-    int win_cols;          // window data bytes per row
-    int pad;               // reference padding (samples)
-    int edge, nx_int, ny_int, ctus_h;   // CTU subset of this launch (see ctu_of)
+    int win_h;             // window rows (row pitch: ME_WIN_PITCH words)
+    int nx_int, ny_int;    // interior CTU rectangle (no block can reach the right/bottom MV limit)
 };
 
-// CTU of this CTA: interior launches cover the nx_int x ny_int rectangle of CTUs whose blocks
-// can never reach the right/bottom MV limit; edge launches cover the rest (right strip, then
-// bottom strip)
-__device__ __forceinline__ void ctu_of(const MeIntParams &P, int i, int *col, int *row)
+// CTU of a CTA: interior launches cover the nx_int x ny_int rectangle of CTUs whose blocks can
+// never reach the right/bottom MV limit; edge launches cover the rest (right strip, then bottom
+// strip)
+__device__ __forceinline__ void ctu_of(const MeIntParams &P, int i, bool edge, int *col, int *row)
 {
-    if (!P.edge) { *col = i % P.nx_int; *row = i / P.nx_int; return; }
+    if (!edge) { *col = i % P.nx_int; *row = i / P.nx_int; return; }
     const int rw = P.ctus_w - P.nx_int;
     if (i < rw * P.ctus_h) { *col = P.nx_int + i % rw; *row = i / rw; return; }
     i -= rw * P.ctus_h;
     *col = i % P.nx_int; *row = P.ny_int + i / P.nx_int;
-}
-
-// word skew of window row r: rows 16 apart (the four sub-block rows of a half-warp) land on
-// bank offsets 0, 16, 2, 18, which with the 4-word column steps of the sub-block columns
-// gives 16 distinct even banks per half-warp
-__device__ __forceinline__ int win_skew(int r)
-{
-    int t = (r >> 4) & 3;
-    return ((t & 1) << 4) | ((t >> 1) << 1);
 }
 
 __device__ __forceinline__ void upd(u32 &b, u32 v, bool ok)
@@ -204,6 +231,10 @@ __device__ __forceinline__ void upd(u32 &b, u32 v, bool ok)
 struct MeLane {
     int sx, sy;
     u32 b0, b1, b2, b3, nb0, nb1, nb2, nb3;   // bits of the lane's sub-block index and complements
+    // word order of the lane: at its t-th word load the lane reads word (t ^ sy) of its four, so
+    // the 16 lanes of a half-warp (rows 16 apart in a dense window) hit 16 distinct banks; the
+    // lanes with sy >= 2 therefore accumulate their right 8x8 tile in the left tile's slot (A)
+    // and the left one in slot B
     // largest valid dx / dy of a block whose top-left corner is the lane's 16x16 sub-block (0),
     // its right or lower 8x8 half (1), the 32-aligned pair it belongs to (p), the CTU (c)
     int X0, X1, Xp, Xc, Y0, Y1, Yp, Yc;
@@ -220,15 +251,8 @@ __device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, co
     const int dyi0 = (int)(desc >> 16);
     const int dx = P.lo_x + dxi, dy0 = P.lo_y + dyi0;
     const int bx = off + 16 * L.sx + dxi;             // == the window's shift (mod 4)
-    // rows R0 .. R0+15+NDY-1 of the window; the skew changes once, at the same row for every
-    // lane of the half-warp (16*sy is a multiple of 16), so two base pointers cover the item
-    const int R0 = 16 * L.sy + dyi0;
-    const u32 *p0 = win + R0 * ME_WIN_WW + win_skew(R0) + (bx >> 2);
-    const u32 *p1 = p0 + (win_skew(R0 + 16) - win_skew(R0));
-    // main items start on a multiple of 8 rows: rows 0-7 are before the change, rows 16..
-    // after it, rows 8-15 on the side R0 & 8 selects
-    const u32 *pm = (R0 & 8) ? p1 : p0;
-    const int rr_c = 16 - (R0 & 15);
+    const u32 *pb = win + (16 * L.sy + dyi0) * ME_WIN_PITCH + (bx >> 2);
+    const u32 *w0 = pb + (0 ^ L.sy), *w1 = pb + (1 ^ L.sy), *w2 = pb + (2 ^ L.sy), *w3 = pb + (3 ^ L.sy);
 
     u32 acc[NDY][4];
 #pragma unroll
@@ -238,10 +262,8 @@ __device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, co
 
 #pragma unroll
     for (int rr = 0; rr < 16 + NDY - 1; rr++) {
-        const u32 *wp;
-        if (NDY == 8) wp = (rr < 8 ? p0 : rr < 16 ? pm : p1) + rr * ME_WIN_WW;
-        else wp = (rr < rr_c ? p0 : p1) + rr * ME_WIN_WW;
-        const u32 a0 = wp[0], a1 = wp[1], a2 = wp[2], a3 = wp[3];
+        const u32 a0 = w0[rr * ME_WIN_PITCH], a1 = w1[rr * ME_WIN_PITCH];
+        const u32 a2 = w2[rr * ME_WIN_PITCH], a3 = w3[rr * ME_WIN_PITCH];
 #pragma unroll
         for (int j = 0; j < NDY; j++) {
             const int r = rr - j;
@@ -259,6 +281,7 @@ __device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, co
     // pipe and leave the integer ALU pipe to the vabsdiff4s and the running minima
     const u32 mul = P.mul, one = P.one, m1 = P.minus1;
     const bool xa = dx <= L.X0, xb = dx <= L.X1, xp = dx <= L.Xp, xc = dx <= L.Xc;
+    const bool sw = L.sy >= 2, xA = sw ? xb : xa, xB = sw ? xa : xb;   // limits of slots A / B
     u32 s16[NDY], q2s[NDY];
 #pragma unroll
     for (int j = 0; j < NDY; j++) {
@@ -274,14 +297,14 @@ __device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, co
         const u32 vt = st * mul + q2, vb = sb * mul + q2;
         s16[j] = st * one + sb;
         const u32 v16 = s16[j] * mul + q2;
-        upd(best[0], v00, !EDGE || (xa && ya));
-        upd(best[1], v01, !EDGE || (xb && ya));
-        upd(best[2], v10, !EDGE || (xa && yb));
-        upd(best[3], v11, !EDGE || (xb && yb));
+        upd(best[0], v00, !EDGE || (xA && ya));    // 8x8, slot A top
+        upd(best[1], v01, !EDGE || (xB && ya));    // 8x8, slot B top
+        upd(best[2], v10, !EDGE || (xA && yb));
+        upd(best[3], v11, !EDGE || (xB && yb));
         upd(best[4], vt, !EDGE || (xa && ya));     // 16x8 top
         upd(best[5], vb, !EDGE || (xa && yb));     // 16x8 bottom
-        upd(best[6], vl, !EDGE || (xa && ya));     // 8x16 left
-        upd(best[7], vr, !EDGE || (xb && ya));     // 8x16 right
+        upd(best[6], vl, !EDGE || (xA && ya));     // 8x16, slot A
+        upd(best[7], vr, !EDGE || (xB && ya));     // 8x16, slot B
         upd(best[8], v16, !EDGE || (xa && ya));
     }
 
@@ -343,59 +366,61 @@ __device__ __forceinline__ void me_item(const MeIntParams &P, const u32 *win, co
     }
 }
 
+// all items of one class against the window in shared memory
 template <bool EDGE>
-__global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
+__device__ __forceinline__ void me_search_class(const MeIntParams &P, const u32 *win, const u32 (&o)[16][4],
+                                                u32 (&best)[15], int cls, int off, int g, const MeLane &L)
 {
-    extern __shared__ __align__(16) u32 win[];
-    __shared__ unsigned long long skey[ME_BLOCKS_PER_CTU];
+    // item counts are multiples of ME_GROUPS: the trip counts are warp-uniform
+    {
+        const u32 *dsc = P.q2tab + P.d_main[cls], *q2b = P.q2tab + P.q2_main[cls];
+        for (int it = g; it < P.n_main[cls]; it += ME_GROUPS)
+            me_item<ME_NDY, EDGE>(P, win, o, best, __ldg(dsc + it), q2b + it * ME_NDY, cls, off, L);
+    }
+    {
+        const u32 *dsc = P.q2tab + P.d_tail[cls], *q2b = P.q2tab + P.q2_tail[cls];
+        for (int it = g; it < P.n_tail[cls]; it += ME_GROUPS)
+            me_item<1, EDGE>(P, win, o, best, __ldg(dsc + it), q2b + it, cls, off, L);
+    }
+}
 
-    const int ref = blockIdx.y;
+// Integer search: one CTA per (CTU, reference, class of dx mod 4).  Its window (rows cy + lo_y
+// .., 224 bytes from a 16-byte boundary, of the reference plane shifted so that the class's
+// candidate words are word-aligned) is staged by one TMA tensor copy, issued first so that it
+// lands while the threads load their org sub-blocks; the two CTAs an SM holds overlap one's
+// window load with the other's search.
+template <bool EDGE>
+__global__ void __launch_bounds__(256, 2) k_me_int(const __grid_constant__ MeIntParams P)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ unsigned long long skey[ME_BLOCKS_PER_CTU];
+    __shared__ __align__(8) u64 bar;
+    // the window starts on a 128-byte boundary (TMA destination); the launch reserves 128 bytes
+    // of slack for this
+    const u32 *win = reinterpret_cast<const u32 *>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
+    const int tid = threadIdx.x;
+    const u32 bar_a = smem_u32(&bar);
+
+    const int ref = blockIdx.y, cls = blockIdx.z;
     int ccol, crow;
-    ctu_of(P, blockIdx.x, &ccol, &crow);
+    ctu_of(P, blockIdx.x, EDGE, &ccol, &crow);
     const int ctu = crow * P.ctus_w + ccol;
     const int cx = ccol * ME_CTU, cy = crow * ME_CTU;
-    const int tid = threadIdx.x;
-    const pel *rp = P.ref[ref];
-
-    // ---- stage the search window: rows cy+lo_y .., columns from a 16-byte boundary.
-    // This CTA only searches horizontal offsets of one residue class mod 4, so every lane's
-    // reference words start at the same byte offset `sh` within a word: the window is stored
-    // pre-shifted by sh bytes and the search reads whole words.  Row r is stored at word
-    // r*ME_WIN_WW + skew(r): the 16 lanes of a half-warp read rows 16 apart, and the skew spreads
-    // them over distinct banks.
-    const int cls = blockIdx.z;
-    const pel *g0 = rp + (long long)(cy + P.lo_y) * P.i_ref + (cx + P.lo_x);
-    const int off = (int)(((uintptr_t)g0) & 15);
-    const pel *gw = g0 - off;
-    const int sh = (off + cls) & 3;
-    const int wwords = P.win_cols >> 2;                 // words of window data per row
-    // columns past the right padding are never read by a valid candidate: filled with 0
-    const int gcol0 = cx + P.lo_x - off, gcol_end = P.W + P.pad;
-    {
-        const int nv = wwords >> 2;                     // 16-byte chunks per row
-        for (int i = tid; i < P.win_h * nv; i += blockDim.x) {
-            const int r = i / nv, c = i % nv;
-            const pel *grow = gw + (long long)r * P.i_ref;
-            u32 wv[5];
-            if ((P.i_ref & 15) == 0 && gcol0 + c * 16 + 19 < gcol_end) {
-                const uint4 v = __ldg(reinterpret_cast<const uint4 *>(grow) + c);
-                wv[0] = v.x; wv[1] = v.y; wv[2] = v.z; wv[3] = v.w;
-                wv[4] = __ldg(reinterpret_cast<const u32 *>(grow) + 4 * c + 4);
-            } else {
-                for (int q = 0; q < 5; q++) {
-                    wv[q] = 0;
-                    for (int b = 0; b < 4; b++) {
-                        const int col = c * 16 + q * 4 + b;
-                        if (gcol0 + col < gcol_end) wv[q] |= (u32)grow[col] << (8 * b);
-                    }
-                }
-            }
-            u32 *d = win + r * ME_WIN_WW + win_skew(r) + 4 * c;
-#pragma unroll
-            for (int q = 0; q < 4; q++) d[q] = __funnelshift_r(wv[q], wv[q + 1], 8 * sh);
-        }
+    const int gx = ME_SHIFT_PAD + cx + P.lo_x;            // first window column (padded coordinates)
+    const int off = gx & 15;
+    // the barrier is initialised and made visible to every thread before any thread polls it
+    // and before the copy is issued: a poll of an uninitialised barrier could pass early and let
+    // the CTA finish while its copy is still landing
+    if (tid == 0) {
+        mbar_init(bar_a, 1);
+        mbar_fence_init();
     }
     for (int i = tid; i < ME_BLOCKS_PER_CTU; i += blockDim.x) skey[i] = ~0ull;
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar_a, (u32)P.win_h * ME_WIN_BYTES_W);
+        tma_load_2d(smem_u32(win), &P.maps[ref][(off + cls) & 3], gx - off, ME_SHIFT_PAD + cy + P.lo_y, bar_a);
+    }
 
     const int lane = tid & 31, warp = tid >> 5;
     const int s = lane & 15, g = warp * 2 + (lane >> 4);
@@ -410,8 +435,10 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
     L.Xp = P.W - 1 - (cx + 16 * (L.sx & 2)); L.Xc = P.W - 1 - cx;
     L.Y0 = P.H - 1 - (cy + 16 * L.sy); L.Y1 = L.Y0 - 8;
     L.Yp = P.H - 1 - (cy + 16 * (L.sy & 2)); L.Yc = P.H - 1 - cy;
+    const bool swapped = L.sy >= 2;
 
-    // ---- org 16x16 sub-block in registers (reads clamped to the picture)
+    // org 16x16 sub-block in registers (reads clamped to the picture), words in the lane's
+    // order: o[r][t] = org word t ^ sy of row r
     u32 o[16][4];
     {
         const int ox = cx + 16 * L.sx, oy = cy + 16 * L.sy;
@@ -419,31 +446,29 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
         for (int r = 0; r < 16; r++) {
             const pel *orow = P.org + (long long)min(oy + r, P.H - 1) * P.i_org;
 #pragma unroll
-            for (int w = 0; w < 4; w++) {
+            for (int t = 0; t < 4; t++) {
+                const int c0 = ox + 4 * (t ^ L.sy);
                 u32 v = 0;
 #pragma unroll
-                for (int b = 0; b < 4; b++) v |= (u32)orow[min(ox + 4 * w + b, P.W - 1)] << (8 * b);
-                o[r][w] = v;
+                for (int b = 0; b < 4; b++) v |= (u32)orow[min(c0 + b, P.W - 1)] << (8 * b);
+                o[r][t] = v;
             }
         }
     }
-    __syncthreads();
+
+    // the window (bounded wait; a CTA that gives up records it, waits for its copy once more
+    // so that no copy lands in released shared memory, and leaves the keys untouched)
+    const bool landed = mbar_wait_bounded(bar_a, 0, ME_TMA_POLLS);
+    if (__syncthreads_or(!landed)) {
+        if (tid == 0) atomicAnd(P.ctl + 1, 0u);
+        mbar_wait_bounded(bar_a, 0, ME_TMA_POLLS);
+        return;
+    }
 
     u32 best[15];
 #pragma unroll
     for (int i = 0; i < 15; i++) best[i] = 0xFFFFFFFFu;
-
-    // item counts are multiples of ME_GROUPS: the trip counts are warp-uniform
-    {
-        const u32 *dsc = P.q2tab + P.d_main[cls], *q2b = P.q2tab + P.q2_main[cls];
-        for (int it = g; it < P.n_main[cls]; it += ME_GROUPS)
-            me_item<ME_NDY, EDGE>(P, win, o, best, __ldg(dsc + it), q2b + it * ME_NDY, cls, off, L);
-    }
-    {
-        const u32 *dsc = P.q2tab + P.d_tail[cls], *q2b = P.q2tab + P.q2_tail[cls];
-        for (int it = g; it < P.n_tail[cls]; it += ME_GROUPS)
-            me_item<1, EDGE>(P, win, o, best, __ldg(dsc + it), q2b + it, cls, off, L);
-    }
+    me_search_class<EDGE>(P, win, o, best, cls, off, g, L);
 
     // ---- decode the lane's winners and merge into the CTU's 64-bit keys.  The lanes that
     // share a block hold minima over disjoint (or repeated) candidates of the same lane group.
@@ -453,11 +478,11 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
 #pragma unroll
         for (int i = 0; i < 2; i++)
 #pragma unroll
-            for (int j = 0; j < 2; j++) ids[j * 2 + i] = (2 * sy + j) * 8 + 2 * sx + i;
+            for (int j = 0; j < 2; j++) ids[j * 2 + i] = (2 * sy + j) * 8 + 2 * sx + (swapped ? 1 - i : i);
         ids[4] = 64 + (2 * sy) * 4 + sx;
         ids[5] = 64 + (2 * sy + 1) * 4 + sx;
-        ids[6] = 96 + sy * 8 + 2 * sx;
-        ids[7] = 96 + sy * 8 + 2 * sx + 1;
+        ids[6] = 96 + sy * 8 + 2 * sx + (swapped ? 1 : 0);
+        ids[7] = 96 + sy * 8 + 2 * sx + (swapped ? 0 : 1);
         ids[8] = 128 + sy * 4 + sx;
         ids[9] = 144 + sy * 2 + (sx >> 1);
         ids[10] = 152 + (sy >> 1) * 4 + sx;
@@ -484,6 +509,72 @@ __global__ void __launch_bounds__(256, 2) k_me_int(MeIntParams P)
         if (skey[i] != ~0ull) atomicMin(reinterpret_cast<unsigned long long *>(dst + i), skey[i]);
 }
 
+// The four byte-shifted copies of each reference's integer plane that the integer search's TMA
+// windows read: copy s of reference r holds, at padded position (x, y), the sample at
+// (x - 144 + s, y - 144) of the reference's padded plane (0 beyond its right padding), with row
+// pitch `pitch` (a multiple of 16) and H + 288 rows.  The source needs padding >= 144.  A thread
+// writes one 16-byte chunk of every copy; sources on a 16-byte grid are read as two vectors.
+__global__ void __launch_bounds__(256) k_shift_planes(MeShiftSrc S, pel *dst, int W, int H, int pitch)
+{
+    const int rows = H + 2 * ME_SHIFT_PAD;
+    const int chunks = pitch >> 4;                   // 16-byte chunks per row
+    const long long per_ref = (long long)rows * chunks;
+    const long long total = per_ref * S.n_refs;
+    const int xmax = W + ME_SHIFT_PAD;               // first source column past the padding
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int ref = (int)(i / per_ref);
+        const long long rem = i - ref * per_ref;
+        const int y = (int)(rem / chunks), c = (int)(rem - (long long)y * chunks);
+        const pel *srow = S.plane[ref] + (long long)(y - ME_SHIFT_PAD) * S.stride;
+        const int x0 = c * 16 - ME_SHIFT_PAD;        // source column of the chunk's first byte
+        u32 b[5];                                    // source bytes x0 .. x0 + 19
+        const pel *sp = srow + x0;
+        if ((((uintptr_t)sp) & 15) == 0 && x0 + 32 <= xmax) {
+            const uint4 v0 = *reinterpret_cast<const uint4 *>(sp);
+            b[0] = v0.x; b[1] = v0.y; b[2] = v0.z; b[3] = v0.w;
+            b[4] = *reinterpret_cast<const u32 *>(sp + 16);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                u32 v = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int x = x0 + 4 * q + k;
+                    v |= (x < xmax ? (u32)sp[4 * q + k] : 0u) << (8 * k);
+                }
+                b[q] = v;
+            }
+        }
+        pel *d = dst + (size_t)ref * 4 * rows * pitch + (size_t)y * pitch + c * 16;
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            uint4 v;
+            v.x = __funnelshift_r(b[0], b[1], 8 * s); v.y = __funnelshift_r(b[1], b[2], 8 * s);
+            v.z = __funnelshift_r(b[2], b[3], 8 * s); v.w = __funnelshift_r(b[3], b[4], 8 * s);
+            *reinterpret_cast<uint4 *>(d + (size_t)s * rows * pitch) = v;
+        }
+    }
+}
+
+int launch_shift_planes(const pel *const *planes, int n_refs, int i_ref, int W, int H, pel *dst, cudaStream_t st)
+{
+    if (n_refs < 1 || n_refs > ME_MAX_REFS || !dst) return set_status(UC_ERR_ARG, "shift_planes: bad argument");
+    MeShiftSrc src;
+    memset(&src, 0, sizeof(src));
+    for (int r = 0; r < n_refs; r++) src.plane[r] = planes[r];
+    src.stride = i_ref; src.n_refs = n_refs;
+    const int pitch = (W + 2 * ME_SHIFT_PAD + 15) & ~15;
+    const long long chunks = (long long)n_refs * (H + 2 * ME_SHIFT_PAD) * (pitch >> 4);
+    prof_begin(PROF_SHIFT, st);
+    k_shift_planes<<<(unsigned)std::min<long long>((chunks + 255) / 256, 152LL * 16), 256, 0, st>>>(src, dst, W, H,
+                                                                                                   pitch);
+    UC_CHECK(cudaGetLastError());
+    count_launch(1);
+    prof_end(PROF_SHIFT, st);
+    return UC_OK;
+}
+
 // ---------------------------------------------------------------- fractional refinement
 //
 // Task grid: one thread per (block, reference, candidate, com_had tile).  Stage 1 evaluates
@@ -505,6 +596,7 @@ struct MeSubParams {
     u32 *satd2;          // [item][8]
     u32 *hpel;           // [item]: stage-1 winner (mx, my)
     int cls_base[4], cls_nx[3];   // refinement items per tile class (per reference), tiles per row
+    const u32 *ctl;      // the integer search's control words ([1] != 0xFFFFFFFF: it gave up)
     MeResult *out;
 };
 
@@ -762,7 +854,9 @@ __global__ void __launch_bounds__(256) k_me_sub_final(MeSubParams P)
         const CtuBlock cb = kCtuBlocks[b];
         const int x = (ctu % P.ctus_w) * ME_CTU + cb.x, y = (ctu / P.ctus_w) * ME_CTU + cb.y;
         MeResult r = {};
-        if (x + cb.w > P.W || y + cb.h > P.H) {
+        // a search that gave up waiting for a window leaves no result: every record is marked
+        // invalid rather than filled from incomplete keys
+        if (x + cb.w > P.W || y + cb.h > P.H || P.ctl[1] != 0xFFFFFFFFu) {
             r.cost_int = ~0ull; r.cost_sub = ~0ull;
             P.out[item] = r;
             continue;
@@ -822,9 +916,9 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     if (rc) return rc;
     const int ctus_w = (a.W + 63) / 64, ctus_h = (a.H + 63) / 64;
     MeIntParams P;
+    memset(&P, 0, sizeof(P));
     P.org = a.org; P.i_org = a.i_org;
-    for (int r = 0; r < ME_MAX_REFS; r++) P.ref[r] = r < a.n_refs ? a.planes[r][0] : nullptr;
-    P.i_ref = a.i_ref; P.W = a.W; P.H = a.H; P.ctus_w = ctus_w;
+    P.W = a.W; P.H = a.H; P.ctus_w = ctus_w; P.ctus_h = ctus_h;
     P.lo_x = t.lo_x; P.hi_x = t.hi_x; P.lo_y = t.lo_y; P.hi_y = t.hi_y;
     P.ndx = t.ndx; P.lambda_mv = a.lambda_mv;
     for (int c = 0; c < ME_CLASSES; c++) {
@@ -834,30 +928,48 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     }
     P.mul = 1u << ME_RANK_BITS; P.one = 1u; P.minus1 = 0xFFFFFFFFu;
     P.q2tab = a.q2tab; P.rank2mv = a.rank2mv; P.keys = keys; P.n_refs = a.n_refs;
+    const size_t n_keys = (size_t)ctus_w * ctus_h * a.n_refs * ME_BLOCKS_PER_CTU;
+    P.ctl = reinterpret_cast<u32 *>(keys + n_keys);
     if (t.ndy_per_item != ME_NDY) return set_status(UC_ERR_ARG, "me: table built for another NDY");
+    if (a.pad < ME_SHIFT_PAD || !a.shift_scratch) return set_status(UC_ERR_ARG, "me: padding below 144 or no scratch");
     // rows read: main items up to 48 + 8 (nfull - 1) + 22, tail items up to 48 + ndy - 1 + 15
     P.win_h = t.ndy + 63;
-    P.win_cols = ((15 + 64 + t.ndx + 4 + 15) / 16) * 16;
-    if ((P.win_cols >> 2) + 18 + 2 > ME_WIN_WW) return set_status(UC_ERR_ARG, "me: window too wide");
-    const size_t smem = (size_t)P.win_h * ME_WIN_WW * 4;
+    const int win_cols = ((15 + 64 + t.ndx + 4 + 15) / 16) * 16;
+    if (win_cols > ME_WIN_BYTES_W || P.win_h > 256) return set_status(UC_ERR_ARG, "me: window too large");
+    const size_t smem = (size_t)P.win_h * ME_WIN_BYTES_W + 128;
     if (smem > 100 * 1024) return set_status(UC_ERR_ARG, "me: window too large");
     // interior CTUs: every 8x8 tile satisfies pos + 8 + hi <= pic - 1 in both directions
     int nx = a.W - 57 - t.hi_x >= 0 ? (a.W - 57 - t.hi_x) / 64 + 1 : 0;
     int ny = a.H - 57 - t.hi_y >= 0 ? (a.H - 57 - t.hi_y) / 64 + 1 : 0;
     nx = std::min(nx, ctus_w); ny = std::min(ny, ctus_h);
-    if (t.nfull == 0) nx = ny = 0;   // the interior kernel has no row limit: short ranges go to the edge kernel
-    P.pad = a.pad; P.ctus_h = ctus_h; P.nx_int = nx; P.ny_int = ny;
+    if (t.nfull == 0) nx = ny = 0;   // the interior path has no row limit: short ranges go to the edge path
+    P.nx_int = nx; P.ny_int = ny;
+
+    // the byte-shifted reference copies the windows are read from (made here unless the caller
+    // keeps them current), and their tensor maps
+    const size_t pitch = ((size_t)a.W + 2 * ME_SHIFT_PAD + 15) & ~(size_t)15;
+    const size_t rows = (size_t)a.H + 2 * ME_SHIFT_PAD;
+    for (int r = 0; r < a.n_refs; r++)
+        for (int sft = 0; sft < 4; sft++) {
+            const pel *base = a.shift_scratch + ((size_t)r * 4 + sft) * rows * pitch;
+            int e = encode_tensor_map_u8(&P.maps[r][sft], base, pitch, rows, pitch, ME_WIN_BYTES_W, (u32)P.win_h);
+            if (e) return e;
+        }
+    if (!a.shift_ready) {
+        const pel *src[ME_MAX_REFS];
+        for (int r = 0; r < a.n_refs; r++) src[r] = a.planes[r][0];
+        int e = launch_shift_planes(src, a.n_refs, a.i_ref, a.W, a.H, a.shift_scratch, st);
+        if (e) return e;
+    }
     prof_begin(PROF_ME_INT, st);
-    UC_CHECK(cudaMemsetAsync(keys, 0xFF, (size_t)ctus_w * ctus_h * a.n_refs * ME_BLOCKS_PER_CTU * sizeof(u64), st));
+    UC_CHECK(cudaMemsetAsync(keys, 0xFF, n_keys * sizeof(u64) + 2 * sizeof(u32), st));
     if (nx * ny > 0) {
-        P.edge = 0;
         k_me_int<false><<<dim3(nx * ny, a.n_refs, ME_CLASSES), 256, smem, st>>>(P);
         UC_CHECK(cudaGetLastError());
         count_launch(1);
     }
     const int n_edge = ctus_w * ctus_h - nx * ny;
     if (n_edge > 0) {
-        P.edge = 1;
         k_me_int<true><<<dim3(n_edge, a.n_refs, ME_CLASSES), 256, smem, st>>>(P);
         UC_CHECK(cudaGetLastError());
         count_launch(1);
@@ -871,7 +983,7 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     S.i_ref = a.i_ref; S.W = a.W; S.H = a.H; S.ctus_w = ctus_w; S.n_ctu = ctus_w * ctus_h; S.n_refs = a.n_refs;
     S.lo_x = t.lo_x; S.lo_y = t.lo_y; S.ndx = t.ndx; S.lambda_mv = a.lambda_mv;
     S.sq32 = sqrt(32.0); S.sq128 = sqrt(128.0);
-    S.keys = keys; S.out = a.out;
+    S.keys = keys; S.out = a.out; S.ctl = P.ctl;
     const long long items = (long long)S.n_ctu * ME_BLOCKS_PER_CTU * a.n_refs;
     S.satd1 = a.sub_scratch;
     S.satd2 = a.sub_scratch + items * 9;

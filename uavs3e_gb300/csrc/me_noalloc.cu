@@ -6,8 +6,9 @@
 // hands this library only the buffers it owns.  This variant takes every input and output from
 // the caller (original picture, the 16 planes of each reference -- e.g. from
 // uavs3e_cuda_pad_plane + uavs3e_cuda_subpel_planes -- and the result array) and keeps its
-// scratch -- the per-block integer winners, the per-candidate SATD sums of the refinement and
-// the per-lambda search tables -- in one file-scope device array of fixed size, which every GPU
+// scratch -- the per-block integer winners, the per-candidate SATD sums of the refinement, the
+// per-lambda search tables and the byte-shifted reference copies the integer search stages its
+// windows from -- in one file-scope device array of fixed size, which every GPU
 // that loads the library holds until the process exits.  The host-side search tables are built
 // in static host arrays, so no heap allocation happens either.
 #include "common.cuh"
@@ -25,7 +26,11 @@ constexpr int NA_MAX_CTUS = UAVS3E_CUDA_NOALLOC_MAX_CTUS;
 constexpr int NA_MAX_REFS = UAVS3E_CUDA_NOALLOC_MAX_REFS;
 constexpr int NA_MAX_RANGE = UAVS3E_CUDA_NOALLOC_MAX_RANGE;
 constexpr int NA_NDY = ME_NDY;
-constexpr size_t NA_KEYS = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * sizeof(u64);
+constexpr size_t NA_KEYS = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * sizeof(u64) + 2 * sizeof(u32);
+// byte-shifted reference copies of the integer search: 4 per reference, each at most the
+// padded geometry of a 1920x1088 frame (row pitch 2208, 1376 rows)
+constexpr size_t NA_SHIFT_PLANE = (size_t)2208 * 1376;
+constexpr size_t NA_SHIFT = (size_t)NA_MAX_REFS * 4 * NA_SHIFT_PLANE;
 constexpr size_t NA_SUB = (size_t)NA_MAX_CTUS * NA_MAX_REFS * ME_BLOCKS_PER_CTU * 18 * sizeof(u32);
 constexpr size_t NA_Q2_ENTRIES = me_q2_entries(NA_MAX_RANGE, NA_NDY);
 constexpr size_t NA_Q2 = NA_Q2_ENTRIES * sizeof(u32);
@@ -34,9 +39,11 @@ constexpr size_t na_up(size_t v) { return (v + 255) & ~(size_t)255; }
 constexpr size_t NA_OFF_SUB = na_up(NA_KEYS);
 constexpr size_t NA_OFF_Q2 = na_up(NA_OFF_SUB + NA_SUB);
 constexpr size_t NA_OFF_R2M = na_up(NA_OFF_Q2 + NA_Q2);
-constexpr size_t NA_BYTES = NA_OFF_R2M + NA_R2M;
+constexpr size_t NA_OFF_SHIFT = na_up(NA_OFF_R2M + NA_R2M);
+constexpr size_t NA_BYTES = NA_OFF_SHIFT + NA_SHIFT;
 static_assert(NA_BYTES == UAVS3E_CUDA_NOALLOC_SCRATCH_BYTES, "scratch size in the header");
-static_assert(NA_OFF_SUB % 256 == 0 && NA_OFF_Q2 % 16 == 0 && NA_OFF_R2M % 16 == 0, "scratch alignment");
+static_assert(NA_OFF_SUB % 256 == 0 && NA_OFF_Q2 % 16 == 0 && NA_OFF_R2M % 16 == 0 && NA_OFF_SHIFT % 256 == 0,
+              "scratch alignment");
 
 // the scratch every call of this entry point uses
 static __device__ __align__(256) unsigned char g_me_scratch[NA_BYTES];
@@ -74,6 +81,9 @@ extern "C" UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_or
         range > NA_MAX_RANGE)
         return set_status(UC_ERR_ARG, "me_search_noalloc: frame, reference count or range exceeds the static scratch "
                                       "(at most 510 CTUs of 64x64, 2 references, range 64)");
+    if ((size_t)((width + 2 * 144 + 15) & ~15) * (size_t)(height + 2 * 144) > NA_SHIFT_PLANE)
+        return set_status(UC_ERR_ARG, "me_search_noalloc: frame exceeds the static scratch (the padded area of "
+                                      "1920x1088)");
     if (!d_org || !d_planes || !d_out || i_org < width || pad < 144 || i_ref < width + 2 * pad)
         return set_status(UC_ERR_ARG, "me_search_noalloc: bad pointer or geometry");
     if ((uint64_t)lambda_mv * 36u >= (1ull << 32)) return set_status(UC_ERR_ARG, "me_search_noalloc: lambda_mv too large");
@@ -126,5 +136,6 @@ extern "C" UAVS3E_CUDA_API int uavs3e_cuda_me_search_noalloc(const uint8_t *d_or
     a.q2tab = (const u32 *)(D.scratch + NA_OFF_Q2);
     a.rank2mv = (const u16 *)(D.scratch + NA_OFF_R2M);
     a.sub_scratch = (u32 *)(D.scratch + NA_OFF_SUB);      // zeroed by launch_me_frame before use
+    a.shift_scratch = D.scratch + NA_OFF_SHIFT;           // rewritten by launch_me_frame from d_planes
     return launch_me_frame(a, D.tab, (u64 *)D.scratch, st);
 }

@@ -1,9 +1,10 @@
 // Kernel-table entries with the exact signatures of funs_handle_t (include/uavs3e_cuda_table.h).
 //
 // Each entry evaluates one call on the GPU: the samples it reads are packed into a per-thread
-// pinned staging buffer, copied to the device in one transfer, one kernel computes the
-// outputs, they are copied back in one transfer and unpacked into the caller's memory with
-// the caller's strides.  Only outputs the reference function writes are written back.
+// pinned staging buffer that is mapped into the device's address space, one kernel reads them
+// there and writes its outputs there, and after the stream synchronises they are unpacked into
+// the caller's memory with the caller's strides (one launch and one synchronisation per call,
+// no copy calls).  Only outputs the reference function writes are written back.
 #include "common.cuh"
 #include "intra.cuh"
 #include "tables.h"
@@ -17,7 +18,8 @@ namespace uc {
 // ------------------------------------------------------------------ per-thread staging
 struct CallCtx {
     cudaStream_t st = nullptr;
-    u8 *h = nullptr, *d = nullptr;
+    u8 *h = nullptr;      // pinned, mapped staging buffer (host address)
+    u8 *d = nullptr;      // the same buffer's device address
     size_t cap = 0;
 };
 static thread_local CallCtx t_ctx;
@@ -56,17 +58,11 @@ public:
     template <class T> T *dev(size_t off) { return (T *)(t_ctx.d + off); }
     template <class T> T *host(size_t off) { return (T *)(t_ctx.h + off); }
 
-    bool upload()
-    {
-        return check(cudaMemcpyAsync(t_ctx.d, t_ctx.h, used, cudaMemcpyHostToDevice, t_ctx.st), "entry upload");
-    }
+    // the kernel reads the staged inputs in place (mapped host memory): nothing to copy
+    bool upload() { return true; }
     bool launched() { return check(cudaGetLastError(), "entry kernel"); }
-    bool download(size_t off, size_t bytes)
-    {
-        if (!check(cudaMemcpyAsync(t_ctx.h + off, t_ctx.d + off, bytes, cudaMemcpyDeviceToHost, t_ctx.st), "entry download"))
-            return false;
-        return check(cudaStreamSynchronize(t_ctx.st), "entry sync");
-    }
+    // the kernel wrote its outputs in place: wait for it
+    bool download(size_t, size_t) { return check(cudaStreamSynchronize(t_ctx.st), "entry sync"); }
 
 private:
     static bool check(cudaError_t e, const char *what)
@@ -85,10 +81,9 @@ private:
         if (x.cap >= need) return true;
         size_t cap = std::max(need, (size_t)4 << 20);
         if (x.h) cudaFreeHost(x.h);
-        if (x.d) cudaFree(x.d);
         x.h = nullptr; x.d = nullptr; x.cap = 0;
-        if (cudaHostAlloc((void **)&x.h, cap, cudaHostAllocDefault) != cudaSuccess ||
-            cudaMalloc((void **)&x.d, cap) != cudaSuccess) {
+        if (cudaHostAlloc((void **)&x.h, cap, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&x.d, x.h, 0) != cudaSuccess) {
             set_status(UC_ERR_MEMORY, "entry: staging allocation failed");
             return false;
         }

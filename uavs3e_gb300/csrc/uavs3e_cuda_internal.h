@@ -34,7 +34,7 @@ struct MeResult {
 };
 
 // optional per-kernel timing with CUDA events on the launching stream
-enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_LOKA = 5, PROF_TZ = 6, PROF_MC = 7, PROF_RDOQ = 8, PROF_AFFME = 9, PROF_N = 12 };
+enum ProfKernel { PROF_PAD = 0, PROF_SUBPEL = 1, PROF_ME_INT = 2, PROF_ME_SUB = 3, PROF_LATTICE = 4, PROF_LOKA = 5, PROF_TZ = 6, PROF_MC = 7, PROF_RDOQ = 8, PROF_AFFME = 9, PROF_SHIFT = 10, PROF_N = 12 };
 int ensure_init();   // selects the library's device (initialising device 0 on first use)
 int me_frame_once(); // one-time per-device setup of the frame search (me.cu)
 // per-call TZ motion searches (tz.cu); planes: n_slots * 16 sample-(0,0) pointers
@@ -69,8 +69,17 @@ struct MeFrameArgs {
     // device copies of the host-built search tables (me_build_tables)
     const u32 *q2tab; const u16 *rank2mv;
     u32 *sub_scratch;                   // me_sub_scratch_bytes(): per-candidate SATD sums
+    pel *shift_scratch;                 // me_shift_scratch_bytes(): byte-shifted reference copies
+    bool shift_ready;                   // the copies are current (else made from planes[r][0])
 };
 size_t me_sub_scratch_bytes(int W, int H, int n_refs);
+// the four byte-shifted copies of every reference's integer plane read by the integer search
+// (padding 144, row pitch a multiple of 16)
+size_t me_shift_scratch_bytes(int W, int H, int n_refs);
+struct MeShiftSrc { const pel *plane[ME_MAX_REFS]; int stride, n_refs; };
+// writes the four shifted copies of each listed integer plane (padded by >= 144, stride i_ref)
+// into dst, laid out [ref][shift] as me_shift_scratch_bytes() sizes them
+int launch_shift_planes(const pel *const *planes, int n_refs, int i_ref, int W, int H, pel *dst, cudaStream_t st);
 
 struct MeTables {
     int lo_x, hi_x, lo_y, hi_y, ndx, ndy, ndy_per_item;
@@ -98,6 +107,8 @@ constexpr size_t me_q2_entries(int range, int ndy_per_item)
                                                ME_GROUPS) +
                          2 * (((2 * (size_t)range + 1 + ME_CLASSES - 1) / ME_CLASSES) * (ndy_per_item - 1) + ME_GROUPS));
 }
+// per-block integer winners ([ctu][ref][169] u64) followed by two control words (the search's
+// status word is the second); all preset to 0xFF bytes by each frame's search
 size_t me_key_scratch_bytes(int W, int H, int n_refs);
 u32 me_mvbits(int v);   // MV bits of one quarter-sample component (host)
 int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStream_t st);

@@ -10,7 +10,8 @@
  * own code; the preload does it without rebuilding the encoder.
  *
  * At exit it prints one line to stderr: the library's status (0 = every call succeeded) and the
- * number of kernels it launched.
+ * number of kernels it launched.  With UAVS3E_CUDA_COSTLOG=1 in the environment it also records
+ * every cost call (costlog.h) and prints the record's counts and hash at exit.
  *
  *   LD_PRELOAD=.../libuavs3e_cuda_preload.so uavs3enc ...
  */
@@ -20,6 +21,7 @@
 #include <stdlib.h>
 
 #include "../../include/uavs3e_cuda_table.h"
+#include "costlog.h"
 
 static int g_installed;
 
@@ -50,6 +52,7 @@ void *uavs3e_create(void *cfg, int *err)
         fprintf(stderr, "uavs3e_cuda_preload: install failed (%d): %s\n", rc, uavs3e_cuda_status_string());
         exit(4);
     }
+    if (getenv("UAVS3E_CUDA_COSTLOG") && getenv("UAVS3E_CUDA_COSTLOG")[0] == '1') costlog_install(table);
     if (!g_installed) atexit(report);
     g_installed = 1;
     fprintf(stderr, "uavs3e_cuda_preload: kernel table installed (GPU entries)\n");
