@@ -982,8 +982,25 @@ def pruning_leg(steps=3000):
     search, share of the lattice's work it searches, GPU time of the pruned lattice)"""
     from uavs3e_gb300 import cnn
     r = cnn.experiment(steps=steps)
-    r["workload"] = ("CNN 2 -> 16/32/32/64 ch (3x3, stride 2) + 1x1 head, bf16 tensor cores (mma.sync), FP32 "
-                     "accumulation; labels: quad-tree + mode decisions from the lattice's RD costs at QP 32")
+    r["workload"] = ("CNN 2 -> 16/32/32/64 ch (3x3, stride 2) + 1x1 head, bf16 tcgen05 tensor cores with FP32 "
+                     "accumulation in TMEM; labels: quad-tree + mode decisions from the lattice's RD costs at QP 32")
+    # one training step at a batch of 1,024 CTUs against the measured bf16 tensor peak
+    ms, flops = cnn.step_time(1024)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    tf = flops / (ms / 1000.0) / 1e12
+    r["train_step_b1024"] = {"ms": ms, "ctus_per_s": 1024 / (ms / 1000.0), "tflops": tf,
+                             "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s",
+                                          "frac": tf / peak,
+                                          "peak_source": "bf16_tflops of MEASURED_PEAKS.json" if "bf16_tflops" in peaks
+                                          else "fallback 1.9 PFLOP/s"},
+                             "note": "forward + loss + backward + Adam of 1,024 CTUs; FLOPs = the convolutions' GEMMs "
+                                     "(real K); the layers' K (18..288) and N (16..64) are small, so the step is bound "
+                                     "by the operand gathers, not the tensor pipe"}
     return r
 
 

@@ -141,6 +141,49 @@ class PruneNet:
                                               self.step_no, st), "cnn_adam")
 
 
+def step_flops(B):
+    """tensor multiply-adds x 2 of one training step at batch B: every convolution's forward GEMM,
+    its weight-gradient GEMM, and the data-gradient GEMM of every layer but the first (real K,
+    without the padding to 16)"""
+    tot, h = 0, 64
+    for i, (cin, cout, ks, st) in enumerate(LAYERS + [HEAD]):
+        ho = (h + 2 * (ks // 2) - ks) // st + 1
+        gemm = 2.0 * B * ho * ho * cout * ks * ks * cin
+        tot += gemm * (3 if i > 0 else 2)
+        h = ho
+    return tot
+
+
+def step_time(B=1024, reps=20, seed=0):
+    """milliseconds of one training step (forward, head loss, backward, Adam) at batch B, CUDA
+    events on the launching stream over `reps` steps after two warm-up steps; returns (ms, flops)"""
+    import torch
+    rng = np.random.default_rng(seed)
+    net = PruneNet(B, seed=seed)
+    net.acts[0].copy_(torch.from_numpy(rng.normal(0, 1, (B, 64, 64, 2)).astype(np.float32)).to(torch.bfloat16))
+    labels = np.zeros((B, 40), np.uint8)
+    labels[:, :21] = rng.integers(0, 2, (B, 21))
+    labels[:, 21:37] = rng.integers(0, 33, (B, 16))
+    d_lab = torch.from_numpy(labels).cuda()
+
+    def step():
+        net.forward()
+        net.backward(d_lab)
+        net.adam()
+
+    for _ in range(2):
+        step()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, step_flops(B)
+
+
 # ----------------------------------------------------------------------------- labels
 
 def square_cus(W, H):
