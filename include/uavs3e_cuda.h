@@ -487,11 +487,15 @@ typedef struct {
     uint32_t sum_abs;     /* sum of |level|                                            */
 } uavs3e_cuda_lat_q_t;
 
-/* Layout autotuning (on by default): the first call per device and mode count with at least 512
- * CUs of a shape times the CTA layouts (how many CUs, or which chunk of one CU's modes, a CTA
- * takes) given by shared-memory budgets of 16..96 KB and keeps the fastest; records are the same
- * for every layout.  budgets: per shape (log2 w - 2) * 5 + (log2 h - 2), in bytes, 0 = the
- * default 48 KB (not tuned). */
+/* The lattice of a call is one persistent launch walking a device queue of tiles (a tile =
+ * several whole CUs of one shape, or one CU and a chunk of its modes), largest shapes first,
+ * with no wait on the host between its launches: once the layouts are tuned, a call can be
+ * captured into a CUDA graph.  Layout autotuning (on by default): the first call with QPs per
+ * device and mode count times, for every shape with at least 512 CUs, the tile layouts given by
+ * shared-memory budgets of 16..48 KB on the queue restricted to that shape and keeps the
+ * fastest (that call waits for the GPU; make it before any capture); records are the same for
+ * every layout.  budgets: per shape (log2 w - 2) * 5 + (log2 h - 2), in bytes, 0 = the default
+ * 48 KB (not tuned). */
 UAVS3E_CUDA_API void uavs3e_cuda_lattice_autotune(int on);
 UAVS3E_CUDA_API int uavs3e_cuda_lattice_budgets(int n_modes, int out[25]);
 

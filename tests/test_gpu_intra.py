@@ -128,3 +128,49 @@ def test_lattice_autotuned_layouts_give_the_same_records(gpu):
     assert np.array_equal(want_s, again_s) and np.array_equal(want_q.view(np.uint8), again_q.view(np.uint8))
     tuned = gpu.lattice_budgets(33)
     assert any(tuned)
+
+
+def test_intra_lattice_is_one_graph(gpu):
+    # after a first plain call (which tunes the layouts), the whole lattice of a frame -- classify,
+    # plan, scatter and the persistent tile kernel -- is captured into one CUDA graph; replays give
+    # the plain launches' records, also for new frame content copied into the same buffers
+    import torch
+    W, H = 256, 192
+    lib = gpu.lib()
+    cus = gpu.lattice_cus(W, H)
+    n = len(cus)
+    qps = np.array([22, 37], np.int32)
+    d_org = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    d_rec = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    d_cus = torch.from_numpy(cus.view(np.uint8).copy()).cuda()
+    d_satd = torch.zeros(n * 33, dtype=torch.int32, device="cuda")
+    d_q = torch.zeros(n * 33 * len(qps) * 16, dtype=torch.uint8, device="cuda")
+
+    def frame(seed):
+        org = intra_frame(W, H, seed=seed)
+        rec = np.clip(org.astype(int) + np.random.default_rng(seed).integers(-5, 6, org.shape), 0, 255)
+        d_org.copy_(torch.from_numpy(org))
+        d_rec.copy_(torch.from_numpy(rec.astype(np.uint8)))
+
+    def run():
+        gpu.check(lib.uavs3e_cuda_intra_lattice_device(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H,
+                                                       d_cus.data_ptr(), n, 1, qps.ctypes.data, len(qps), 1,
+                                                       d_satd.data_ptr(), d_q.data_ptr(),
+                                                       torch.cuda.current_stream().cuda_stream), "intra_lattice")
+
+    want = {}
+    for seed in (21, 22):
+        frame(seed)
+        run()
+        torch.cuda.synchronize()
+        want[seed] = (d_satd.clone(), d_q.clone())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        run()
+    for seed in (21, 22, 21):
+        frame(seed)
+        d_satd.zero_()
+        d_q.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(d_satd, want[seed][0]) and torch.equal(d_q, want[seed][1]), seed

@@ -6,13 +6,17 @@
 // rdoq_quant_block parameters src/quant.c:196-231, com_dquant src/com_itdq.c:807,
 // itrans_dct2 :264-423, com_recon src/com_util.c:3107).
 //
-// Work is grouped by CU shape: a classify kernel counts the CUs of each of the 25 power-of-two
-// shapes (4..64 per side), a scatter kernel lists them per shape, and one launch per shape
-// runs CTAs of 256 threads whose shared memory is sized for that shape.  A CTA takes a job
-// list of (CU, mode) pairs: several whole CUs (33 modes each) for small shapes, one CU and a
-// chunk of its modes for large ones, about 48 KB of per-job buffers either way.  Every stage is
-// a flat loop over (job, element), and per-job sums are reduced across the lanes of a warp
-// before one shared-memory atomic.
+// The whole lattice of a frame is one launch of a persistent kernel walking a device work queue.
+// A classify kernel counts the CUs of each of the 25 power-of-two shape classes (4..64 per side),
+// a planning kernel turns the counts into each class's run of tiles (a tile = several whole CUs,
+// or one CU and a chunk of its modes, per the class's shared-memory layout) in the order largest
+// CUs first, a scatter kernel lists the CUs per class, and the persistent CTAs then take tiles
+// from a global counter until the queue is empty, each running the compile-time body of the
+// tile's class.  Nothing waits on the host between the launches, so a frame's intra lattice can
+// be captured into one CUDA graph.  Within a tile every stage is a flat loop over (job,
+// element), and per-job sums are reduced across the lanes of a warp before one shared-memory
+// atomic.  An autotuner picks each class's layout (how many CUs or which mode chunk a tile
+// takes) under a common shared-memory size, by timing the queue restricted to that class.
 //
 // Transforms are products with the folded DCT2 matrices (identical results to the encoder's
 // partial butterflies) on the byte/halfword dot-product instructions: the forward row pass is
@@ -92,6 +96,58 @@ __global__ void __launch_bounds__(256) k_lat_scatter(const LatCu *cus, int n, in
     }
 }
 
+// plans the queue of one launch: exclusive offsets of the classes' CUs in perm, the classes'
+// tile runs in launch order (only the classes in the mask), the cursors and the tile counter reset
+struct LatPlan { int tiles_per_cu[LAT_SHAPES], nchunk[LAT_SHAPES]; u32 mask; };
+
+__global__ void k_lat_plan(int *counters, const LatPlan Q)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int *counts = counters, *cursor = counters + 32, *cu_off = counters + 64, *tile_off = counters + 96;
+    int o = 0;
+    for (int c = 0; c < LAT_SHAPES; c++) { cu_off[c] = o; o += counts[c]; cursor[c] = 0; }
+    int t = 0;
+    for (int r = 0; r < LAT_SHAPES; r++) {
+        const int c = lat_order(r);
+        tile_off[r] = t;
+        if ((Q.mask >> c) & 1) t += (counts[c] + Q.tiles_per_cu[c] - 1) / Q.tiles_per_cu[c] * Q.nchunk[c];
+    }
+    tile_off[LAT_SHAPES] = t;
+    counters[127] = 0;      // the tile counter
+}
+
+// the persistent lattice: tiles from the queue until it is empty.  Its static shared memory is
+// the tile's LatShared and one word: with a 48 KB layout, four CTAs then still fit an SM (the
+// queue's tile offsets are read from global memory, not copied to shared memory, for that)
+__global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(const __grid_constant__ LatParams P)
+{
+    extern __shared__ __align__(16) u8 sm[];
+    __shared__ LatShared S;
+    __shared__ int s_t;
+    const int tid = threadIdx.x;
+    const int total = __ldg(P.tile_off + LAT_SHAPES);
+    for (;;) {
+        if (tid == 0) s_t = atomicAdd(P.next, 1);
+        __syncthreads();
+        const int t = s_t;
+        __syncthreads();
+        if (t >= total) break;
+        int r = 0;
+        while (t >= __ldg(P.tile_off + r + 1)) r++;
+        const int c = lat_order(r), lt = t - __ldg(P.tile_off + r);
+        const int *perm = P.perm + P.cu_off[c];
+        const int n = P.counts[c];
+        switch (c) {
+#define LAT_CASE(lw, lh) case ((lw) - 2) * 5 + ((lh) - 2): lat_tile<lw, lh>(P, perm, n, lt, sm, S); break;
+#define LAT_ROW(lw) LAT_CASE(lw, 2) LAT_CASE(lw, 3) LAT_CASE(lw, 4) LAT_CASE(lw, 5) LAT_CASE(lw, 6)
+            LAT_ROW(2) LAT_ROW(3) LAT_ROW(4) LAT_ROW(5) LAT_ROW(6)
+#undef LAT_ROW
+#undef LAT_CASE
+        default: break;
+        }
+    }
+}
+
 size_t lattice_smem_bytes(int w, int h, int nm)
 {
     int lw = 0, lh = 0;
@@ -102,61 +158,86 @@ size_t lattice_smem_bytes(int w, int h, int nm)
     return (size_t)L.smem;
 }
 
-// Autotuning of the CTA layout: per device, mode count and shape, the first call with at least
-// LAT_TUNE_MIN_CUS CUs of the shape times each distinct layout the candidate budgets give (every
-// run writes the same records) and keeps the fastest for the later calls.
+// Autotuning of the tile layouts: per device and mode count, the first call with at least
+// LAT_TUNE_MIN_CUS CUs of a class times the queue restricted to that class for each distinct
+// layout the candidate budgets give (every run writes the same records) and keeps the fastest.
+// All budgets are at most LAT_BUDGET, the launch's shared-memory size, so four CTAs share an SM.
 constexpr int LAT_TUNE_MIN_CUS = 512;
-static const int kLatBudgets[] = { 16 * 1024, 24 * 1024, 32 * 1024, 40 * 1024, 48 * 1024, 56 * 1024,
-                                   72 * 1024, 96 * 1024 };
+static const int kLatBudgets[] = { 16 * 1024, 24 * 1024, 32 * 1024, 40 * 1024, 48 * 1024 };
 struct LatTune {
     std::mutex mu;
-    int budget[34][LAT_SHAPES] = {};
+    int budget[34][LAT_SHAPES] = {};   // 0: the default LAT_BUDGET (not tuned)
+    bool done[34] = {};                // the tuning pass of this mode count has run
 };
 static LatTune g_tune[64];
 static bool g_tune_on = true;
 
-static int lat_launch(int lw, int lh, unsigned grid, int smem, cudaStream_t st, const LatParams &P)
+// per device: the CU permutation and the queue's counters
+struct LatScratch {
+    int *perm = nullptr;
+    int *counters = nullptr;   // [0, 32) counts, [32, 64) cursors, [64, 96) CU offsets, [96, 122) tile
+                               // offsets, [127] tile counter
+    size_t cap = 0;
+    int sms = 0, occ = 0;      // SMs and resident CTAs per SM at LAT_BUDGET
+};
+static LatScratch g_lat[64];
+
+// one launch of the plan + scatter + persistent lattice for the classes in `mask`
+static int lat_run(LatParams P, const LatCu *cus, int n_cus, int W, int H, const int *budgets, u32 mask,
+                   LatScratch &S, cudaStream_t st, int *launches)
 {
-    switch (lw) {
-    case 2: return lat_launch_w<2>(lh, grid, smem, st, P);
-    case 3: return lat_launch_w<3>(lh, grid, smem, st, P);
-    case 4: return lat_launch_w<4>(lh, grid, smem, st, P);
-    case 5: return lat_launch_w<5>(lh, grid, smem, st, P);
-    default: return lat_launch_w<6>(lh, grid, smem, st, P);
+    LatPlan Q;
+    int smem = 0;
+    for (int c = 0; c < LAT_SHAPES; c++) {
+        LatLayout L;
+        lat_layout(c / 5 + 2, c % 5 + 2, P.n_modes, budgets[c], L);
+        Q.tiles_per_cu[c] = L.G; Q.nchunk[c] = L.nchunk;
+        if ((mask >> c) & 1) smem = std::max(smem, L.smem);
+        P.budget[c] = budgets[c];
     }
+    Q.mask = mask;
+    if (smem > LAT_SMEM_MAX) return set_status(UC_ERR_ARG, "intra_lattice: shared memory layout");
+    k_lat_plan<<<1, 32, 0, st>>>(S.counters, Q);
+    UC_CHECK(cudaGetLastError());
+    const int nb = (n_cus + 256 * LAT_GROUP_K - 1) / (256 * LAT_GROUP_K);
+    k_lat_scatter<<<nb, 256, 0, st>>>(cus, n_cus, W, H, S.counters + 64, S.counters + 32, S.perm);
+    UC_CHECK(cudaGetLastError());
+    k_intra_lattice<<<S.sms * S.occ, LAT_THREADS, smem, st>>>(P);
+    UC_CHECK(cudaGetLastError());
+    *launches += 3;
+    return UC_OK;
 }
 
-// times the distinct layouts of one shape on this call's CUs; returns the best budget (and the
-// launches it made in *launches)
-static int lat_tune_shape(int lw, int lh, int n, LatParams P, cudaStream_t st, int *launches, int *best_out)
+// times the lattice restricted to class c for each distinct layout of the candidate budgets
+static int lat_tune_class(int c, const LatParams &P, const LatCu *cus, int n_cus, int W, int H, const int *budgets,
+                          LatScratch &S, cudaStream_t st, int *launches, int *best_out)
 {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     UC_CHECK(cudaEventCreate(&e0));
     UC_CHECK(cudaEventCreate(&e1));
     float best_ms = 3.0e38f;
-    int best = LAT_BUDGET, seen = 0;
-    int seen_g[8], seen_mc[8];
+    int best = LAT_BUDGET, seen = 0, seen_g[8], seen_mc[8];
+    int bud[LAT_SHAPES];
+    for (int k = 0; k < LAT_SHAPES; k++) bud[k] = budgets[k];
     for (int b : kLatBudgets) {
         LatLayout L;
-        lat_layout(lw, lh, P.n_modes, b, L);
-        if (L.smem > LAT_SMEM_MAX || L.G < 1) continue;
+        lat_layout(c / 5 + 2, c % 5 + 2, P.n_modes, b, L);
+        if (L.smem > LAT_BUDGET || L.G < 1) continue;
         bool dup = false;
         for (int k = 0; k < seen; k++) dup |= seen_g[k] == L.G && seen_mc[k] == L.MC;
         if (dup) continue;
         seen_g[seen] = L.G; seen_mc[seen] = L.MC; seen++;
-        P.budget = b;
-        const unsigned grid = (unsigned)((long long)((n + L.G - 1) / L.G) * L.nchunk);
+        bud[c] = b;
         float ms = 3.0e38f;
         for (int rep = 0; rep < 2; rep++) {
             UC_CHECK(cudaEventRecord(e0, st));
-            int r = lat_launch(lw, lh, grid, L.smem, st, P);
+            int r = lat_run(P, cus, n_cus, W, H, bud, 1u << c, S, st, launches);
             if (r) { cudaEventDestroy(e0); cudaEventDestroy(e1); return r; }
             UC_CHECK(cudaEventRecord(e1, st));
             UC_CHECK(cudaEventSynchronize(e1));
             float t = 0;
             UC_CHECK(cudaEventElapsedTime(&t, e0, e1));
             ms = t < ms ? t : ms;
-            (*launches)++;
         }
         if (ms < best_ms) { best_ms = ms; best = b; }
     }
@@ -165,15 +246,6 @@ static int lat_tune_shape(int lw, int lh, int n, LatParams P, cudaStream_t st, i
     *best_out = best;
     return UC_OK;
 }
-
-// per device: the CU permutation and the per-shape counters
-struct LatScratch {
-    int *perm = nullptr;
-    int *counters = nullptr;   // [0, 32): counts, [32, 64): cursors, [64, 96): offsets
-    int *h_counts = nullptr;   // pinned
-    size_t cap = 0;
-};
-static LatScratch g_lat[64];
 
 int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, int W, int H, const LatCu *cus,
                          int n_cus, const u8 *modes, int n_modes, int ipf, const int *qps, int n_qp, int is_intra,
@@ -193,8 +265,11 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     if (n_cus == 0) return UC_OK;
     LatScratch &S = g_lat[dev];
     if (!S.counters) {
-        UC_CHECK(cudaMalloc(&S.counters, 96 * sizeof(int)));
-        UC_CHECK(cudaMallocHost(&S.h_counts, 96 * sizeof(int)));
+        UC_CHECK(cudaDeviceGetAttribute(&S.sms, cudaDevAttrMultiProcessorCount, dev));
+        UC_CHECK(cudaFuncSetAttribute(k_intra_lattice, cudaFuncAttributeMaxDynamicSharedMemorySize, LAT_SMEM_MAX));
+        UC_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&S.occ, k_intra_lattice, LAT_THREADS, LAT_BUDGET));
+        S.occ = std::max(S.occ, 1);      // 4 on GB300 (64 registers, 56 KB of shared memory per CTA)
+        UC_CHECK(cudaMalloc(&S.counters, 128 * sizeof(int)));
     }
     if (S.cap < (size_t)n_cus) {
         if (S.perm) UC_CHECK(cudaFree(S.perm));
@@ -203,58 +278,49 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
         S.cap = (size_t)n_cus;
     }
     prof_begin(PROF_LATTICE, st);
-    UC_CHECK(cudaMemsetAsync(S.counters, 0, 96 * sizeof(int), st));
+    UC_CHECK(cudaMemsetAsync(S.counters, 0, 128 * sizeof(int), st));
     const int nb = (n_cus + 256 * LAT_GROUP_K - 1) / (256 * LAT_GROUP_K);
     k_lat_count<<<nb, 256, 0, st>>>(cus, n_cus, W, H, n_qp, S.counters, satd_out, q_out);
     UC_CHECK(cudaGetLastError());
-    UC_CHECK(cudaMemcpyAsync(S.h_counts, S.counters, 32 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    UC_CHECK(cudaStreamSynchronize(st));
-    int offs[32], total = 0;
-    for (int c = 0; c < LAT_SHAPES; c++) { offs[c] = total; total += S.h_counts[c]; }
-    for (int c = 0; c < LAT_SHAPES; c++) S.h_counts[64 + c] = offs[c];
-    UC_CHECK(cudaMemcpyAsync(S.counters + 64, S.h_counts + 64, 32 * sizeof(int), cudaMemcpyHostToDevice, st));
-    k_lat_scatter<<<nb, 256, 0, st>>>(cus, n_cus, W, H, S.counters + 64, S.counters + 32, S.perm);
-    UC_CHECK(cudaGetLastError());
-    int launches = 2;
+    int launches = 1;
     LatParams P;
+    memset(&P, 0, sizeof(P));
     P.org = org; P.i_org = i_org; P.rec = rec; P.i_rec = i_rec; P.W = W; P.H = H;
     P.cus = cus; P.ipf = ipf; P.n_qp = n_qp; P.is_intra = is_intra;
     for (int i = 0; i < LAT_MAX_QP; i++) P.qp[i] = i < n_qp ? qps[i] : 0;
     P.satd_out = satd_out; P.q_out = q_out;
     P.modes = modes; P.n_modes = n_modes;
     P.sq32 = sqrt(32.0); P.sq128 = sqrt(128.0);
-    // largest shapes first: their CTAs are the longest
-    for (int lw = 6; lw >= 2; lw--)
-        for (int lh = 6; lh >= 2; lh--) {
-            const int c = (lw - 2) * 5 + (lh - 2);
-            const int n = S.h_counts[c];
-            if (!n) continue;
-            P.perm = S.perm + offs[c];
-            P.n_shape = n;
-            P.fold_w = tab->fold[lw]; P.fold_h = tab->fold[lh];
-            P.scanpos = tab->scanpos[lw][lh];
-            int budget = LAT_BUDGET;
-            {
-                LatTune &T = g_tune[dev];
-                std::lock_guard<std::mutex> lk(T.mu);
-                if (T.budget[n_modes][c]) {
-                    budget = T.budget[n_modes][c];
-                } else if (g_tune_on && n >= LAT_TUNE_MIN_CUS && n_qp > 0) {   // SATD-only runs keep the default
-                    int best = LAT_BUDGET;
-                    int r = lat_tune_shape(lw, lh, n, P, st, &launches, &best);
-                    if (r) return r;
-                    T.budget[n_modes][c] = budget = best;
-                    continue;   // the tuning runs wrote this shape's records
-                }
+    for (int l = 0; l < 7; l++) {
+        P.fold[l] = tab->fold[l];
+        for (int m = 0; m < 7; m++) P.scanpos[l][m] = tab->scanpos[l][m];
+    }
+    P.counts = S.counters; P.cu_off = S.counters + 64; P.tile_off = S.counters + 96; P.perm = S.perm;
+    P.next = S.counters + 127;
+    // the classes' layouts: tuned on the first call with QPs per device and mode count (that call
+    // waits for the CU counts and times the candidates of every class with enough CUs; later
+    // calls, and every SATD-only call, do not wait -- make the first call before any capture)
+    int budgets[LAT_SHAPES];
+    {
+        LatTune &T = g_tune[dev];
+        std::lock_guard<std::mutex> lk(T.mu);
+        for (int c = 0; c < LAT_SHAPES; c++) budgets[c] = T.budget[n_modes][c] ? T.budget[n_modes][c] : LAT_BUDGET;
+        if (g_tune_on && !T.done[n_modes] && n_qp > 0) {
+            T.done[n_modes] = true;   // one pass: classes with too few CUs keep the default
+            int counts[32];
+            UC_CHECK(cudaMemcpyAsync(counts, S.counters, 32 * sizeof(int), cudaMemcpyDeviceToHost, st));
+            UC_CHECK(cudaStreamSynchronize(st));
+            for (int c = 0; c < LAT_SHAPES; c++) {
+                if (T.budget[n_modes][c] || counts[c] < LAT_TUNE_MIN_CUS) continue;
+                int best = LAT_BUDGET;
+                int r = lat_tune_class(c, P, cus, n_cus, W, H, budgets, S, st, &launches, &best);
+                if (r) return r;
+                T.budget[n_modes][c] = budgets[c] = best;
             }
-            LatLayout L;
-            lat_layout(lw, lh, n_modes, budget, L);
-            P.budget = budget;
-            const long long grid = (long long)((n + L.G - 1) / L.G) * L.nchunk;
-            int r = lat_launch(lw, lh, (unsigned)grid, L.smem, st, P);
-            if (r) return r;
-            launches++;
         }
+    }
+    int r = lat_run(P, cus, n_cus, W, H, budgets, (1u << LAT_SHAPES) - 1, S, st, &launches);
+    if (r) return r;
     count_launch(launches);
     prof_end(PROF_LATTICE, st);
     return UC_OK;

@@ -139,17 +139,31 @@ struct LatParams {
     const pel *rec; int i_rec;
     int W, H;
     const LatCu *cus;
-    const int *perm;          // CU indices of this shape
-    int n_shape;              // CUs of this shape
     int ipf, n_qp, is_intra;
     int qp[LAT_MAX_QP];
     u32 *satd_out; LatQ *q_out;
-    const s8 *fold_w, *fold_h;
-    const u16 *scanpos;
+    const s8 *fold[7];        // folded DCT2 matrices per log2 size
+    const u16 *scanpos[7][7]; // raster -> scan index per (log2 w, log2 h)
     const u8 *modes;          // [CU][n_modes] modes to evaluate, or null for all 33 in order
     int n_modes;
-    int budget;               // dynamic shared bytes of the layout (lat_layout)
+    int budget[LAT_SHAPES];   // dynamic shared bytes of each shape class's layout (lat_layout)
     double sq32, sq128;
+    // the device work queue (written by k_lat_plan for each launch)
+    const int *counts;        // [LAT_SHAPES] CUs per shape class
+    const int *cu_off;        // [LAT_SHAPES] first entry of each class in perm
+    const int *tile_off;      // [LAT_SHAPES + 1] first tile of the class of each launch rank; [25] = total
+    const int *perm;          // CU indices grouped by class
+    int *next;                // the next tile to take
+};
+
+// per-CTA shared scalars of a tile (the static part of the tile's shared memory)
+struct LatShared {
+    IpredBlock B[LAT_MAX_G];
+    int cu[LAT_MAX_G];
+    u8 mode[LAT_MAX_JOBS];
+    u32 satd[LAT_MAX_JOBS], flag[LAT_MAX_JOBS];
+    u32 nz[LAT_MAX_JOBS], sum[LAT_MAX_JOBS], hash[LAT_MAX_JOBS], ssd[LAT_MAX_JOBS];
+    int last[LAT_MAX_JOBS];
 };
 
 // lanes [k*seg, (k+1)*seg) of a warp hold one job's elements (seg = 16 or 32): the sum, max
@@ -289,19 +303,22 @@ __device__ __forceinline__ void lat_satd_tiles(int n_tiles, int lnt, int ntx, co
     }
 }
 
+// One tile of shape class (LW, LH): a few whole CUs, or one CU and a chunk of its modes, as the
+// class's layout says.  Called by every thread of the CTA; the tile's data lives in `sm` (the
+// layout's dynamic shared memory) and `S`.
 template <int LW, int LH>
-__global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
+__device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, int n_shape, int tile, u8 *sm,
+                                         LatShared &S)
 {
-    extern __shared__ __align__(16) u8 sm[];
-    __shared__ IpredBlock sB[LAT_MAX_G];
-    __shared__ int s_cu[LAT_MAX_G];
-    __shared__ u8 s_mode[LAT_MAX_JOBS];
-    __shared__ u32 s_satd[LAT_MAX_JOBS], s_flag[LAT_MAX_JOBS];
-    __shared__ u32 s_nz[LAT_MAX_JOBS], s_sum[LAT_MAX_JOBS], s_hash[LAT_MAX_JOBS], s_ssd[LAT_MAX_JOBS];
-    __shared__ int s_last[LAT_MAX_JOBS];
+    IpredBlock *sB = S.B;
+    int *s_cu = S.cu;
+    u8 *s_mode = S.mode;
+    u32 *s_satd = S.satd, *s_flag = S.flag, *s_nz = S.nz, *s_sum = S.sum, *s_hash = S.hash, *s_ssd = S.ssd;
+    int *s_last = S.last;
 
     LatLayout L;
-    lat_layout(LW, LH, P.n_modes, P.budget, L);   // compile-time shape: the indices and trip counts below are constants
+    // compile-time shape: the indices and trip counts below are constants
+    lat_layout(LW, LH, P.n_modes, P.budget[(LW - 2) * 5 + (LH - 2)], L);
     const int w = L.w, h = L.h, lw = L.lw, lh = L.lh, kw = L.kw, kh = L.kh, lkw = L.lkw, lkh = L.lkh;
     const int N = w * h, lN = lw + lh;
     constexpr int W_ = 1 << LW, H_ = 1 << LH, KW_ = W_ < 32 ? W_ : 32, KH_ = H_ < 32 ? H_ : 32;
@@ -313,10 +330,10 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     constexpr int RU = KW_ < 8 ? KW_ : 8, NUC = KW_ / RU;
     const int tid = threadIdx.x, lane = tid & 31, wbase = tid & ~31;
 
-    // this CTA's CUs and modes
-    const int grp = blockIdx.x / L.nchunk, chunk = blockIdx.x % L.nchunk;
+    // this tile's CUs and modes
+    const int grp = tile / L.nchunk, chunk = tile % L.nchunk;
     const int cu0 = grp * L.G;
-    const int Gv = min(L.G, P.n_shape - cu0);
+    const int Gv = min(L.G, n_shape - cu0);
     const int m0 = chunk * L.MC;
     const int MCv = min(L.MC, P.n_modes - m0);
     const int J = Gv * MCv;
@@ -329,22 +346,22 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
     // ---- matrices: rows packed 4 bytes to a word
     for (int i = tid; i < kw * w; i += LAT_THREADS) {
         const int u = i >> lw, x = i & (w - 1);
-        const u8 v = (u8)P.fold_w[u * w + x];
+        const u8 v = (u8)P.fold[LW][u * w + x];
         ((u8 *)fw)[u * L.fw_ws * 4 + x] = v;        // Fw[u][x]
         ((u8 *)fwt)[x * L.fwt_ws * 4 + u] = v;      // Fw^T[x][u]
     }
     for (int i = tid; i < kh * h; i += LAT_THREADS) {
         const int v = i >> lh, y = i & (h - 1);
-        const u8 c = (u8)P.fold_h[v * h + y];
+        const u8 c = (u8)P.fold[LH][v * h + y];
         ((u8 *)fh)[v * L.fh_ws * 4 + y] = c;        // Fh[v][y]
         ((u8 *)fht)[y * L.fht_ws * 4 + v] = c;      // Fh^T[y][v]
     }
     u16 *s_scan = (u16 *)(sm + L.o_scan);
-    for (int i = tid; i < kw * kh; i += LAT_THREADS) s_scan[i] = P.scanpos[(i >> lkw) * w + (i & (kw - 1))];
-    if (tid < Gv) s_cu[tid] = P.perm[cu0 + tid];
+    for (int i = tid; i < kw * kh; i += LAT_THREADS) s_scan[i] = P.scanpos[LW][LH][(i >> lkw) * w + (i & (kw - 1))];
+    if (tid < Gv) s_cu[tid] = perm[cu0 + tid];
     for (int j = tid; j < J; j += LAT_THREADS) {
         const int g = j / MCv, mi = m0 + (j - g * MCv);
-        s_mode[j] = P.modes ? P.modes[(size_t)P.perm[cu0 + g] * P.n_modes + mi] : (u8)mi;
+        s_mode[j] = P.modes ? P.modes[(size_t)perm[cu0 + g] * P.n_modes + mi] : (u8)mi;
         s_satd[j] = 0; s_flag[j] = 0; s_nz[j] = 0; s_sum[j] = 0; s_hash[j] = 0; s_ssd[j] = 0; s_last[j] = -1;
     }
     __syncthreads();
@@ -637,8 +654,8 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(LatParams P)
 #undef CORG
 }
 
-// launches the instance for (2^LW) x (2^lh) CUs (lattice_w*.cu)
-template <int LW>
-int lat_launch_w(int lh, unsigned grid, int smem, cudaStream_t st, const LatParams &P);
+// the size classes in launch order, largest CUs first (their tiles are the longest): rank r
+// takes class (log2 w - 2) * 5 + (log2 h - 2) = lat_order(r)
+__host__ __device__ constexpr int lat_order(int r) { return (4 - r / 5) * 5 + (4 - r % 5); }
 
 }  // namespace uc
