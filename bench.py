@@ -374,7 +374,7 @@ def intra_decision_part(u, torch, stream, flush, d_org, d_rec, d_cus, cus, qps, 
     d_q5 = torch.empty(n * 33 * len(qps) * 16, dtype=torch.uint8, device="cuda")
     fn = lib.uavs3e_cuda_intra_lattice_modes_device
 
-    def run():
+    def run(sp=sp):
         u.check(fn(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H, d_cus.data_ptr(), n, None, 33, 1, None, 0, 1,
                    d_satd.data_ptr(), None, sp), "intra_lattice (SATD)")
         u.intra_rmd_device(d_satd.data_ptr(), n, d_req.data_ptr(), n, d_lists.data_ptr(), sp)
@@ -396,9 +396,30 @@ def intra_decision_part(u, torch, stream, flush, d_org, d_rec, d_cus, cus, qps, 
         torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in evs) / reps
     counts = d_lists.view(n, u.RMD_OUT.itemsize)[:, 5].cpu().numpy()
+    # the same frame as one captured CUDA graph (SATD lattice, candidate lists, mode gather,
+    # listed-mode lattice), replayed per frame
+    want = d_q5.clone()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        run(torch.cuda.current_stream().cuda_stream)
+    with torch.cuda.stream(stream):
+        d_q5.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        graph_equal = bool(torch.equal(d_q5, want))
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
+        torch.cuda.synchronize()
+    graph_ms = sum(a.elapsed_time(b) for a, b in evs) / reps
     return {"workload": "1080p intra decision in the encoder's order: SATD of the 33 modes of every lattice CU, "
                         "make_ipred_list (fast RMD), then transform + 4-QP quantisation records of the listed modes",
-            "ms_per_frame": ms, "frames_per_s": 1000.0 / ms, "mean_candidates": float(counts.mean())}
+            "ms_per_frame": ms, "frames_per_s": 1000.0 / ms, "mean_candidates": float(counts.mean()),
+            "graph": {"ms_per_frame": graph_ms, "records_equal_plain": graph_equal,
+                      "note": "the frame's launches captured once into a CUDA graph and replayed"}}
 
 
 def rmd_part(u, torch, stream, flush, d_satd, cus, with_cpu, reps=10):

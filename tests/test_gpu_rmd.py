@@ -140,3 +140,70 @@ def test_intra_decision_pipeline(gpu, oracle):
     sel = np.zeros((n, 33), bool)
     np.put_along_axis(sel, modes.astype(int), True, 1)
     assert np.array_equal(q5[sel], q_all.reshape(n, 33, len(qps))[sel])
+
+
+@pytest.mark.gpu
+def test_intra_decision_frame_is_one_graph(gpu):
+    """the intra decision of a frame in the encoder's order -- SATD lattice, candidate lists,
+    gather of each CU's listed modes, lattice over the lists -- captured once into a CUDA graph:
+    replays on new frame content give the plain launches' records"""
+    import ctypes as C
+
+    import torch
+    from uavs3e_gb300.synth import intra_frame
+    W, H = 192, 128
+    cus = gpu.lattice_cus(W, H)
+    n = len(cus)
+    L = gpu.lib()
+    P, I = C.c_void_p, C.c_int
+    L.uavs3e_cuda_intra_lattice_modes_device.argtypes = [P, I, P, I, I, I, P, I, P, I, I, P, I, I, P, P, P]
+    reqs, _, _, _, _ = cases.rmd_inputs(np.random.default_rng(13), n)
+    reqs["satd_row"] = np.arange(n)
+    reqs["pb_w"], reqs["pb_h"] = cus["w"], cus["h"]
+    reqs["inter_satd"] = np.iinfo(np.uint64).max
+    d_req = torch.from_numpy(reqs.view(np.uint8).copy()).cuda()
+    d_org = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    d_rec = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    d_cus = torch.from_numpy(cus.view(np.uint8).copy()).cuda()
+    d_satd = torch.zeros(n * 33, dtype=torch.int32, device="cuda")
+    d_lists = torch.zeros(n * gpu.RMD_OUT.itemsize, dtype=torch.uint8, device="cuda")
+    d_satd5 = torch.zeros(n * 33, dtype=torch.int32, device="cuda")
+    qps = np.array([27, 37], np.int32)
+    d_q5 = torch.zeros(n * 33 * len(qps) * gpu.LAT_Q.itemsize, dtype=torch.uint8, device="cuda")
+
+    def frame(seed):
+        org = intra_frame(W, H, seed=seed)
+        rec = np.clip(org.astype(int) + np.random.default_rng(seed).integers(-4, 5, org.shape), 0, 255)
+        d_org.copy_(torch.from_numpy(org))
+        d_rec.copy_(torch.from_numpy(rec.astype(np.uint8)))
+
+    def run():
+        sp = torch.cuda.current_stream().cuda_stream
+        assert L.uavs3e_cuda_intra_lattice_modes_device(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H,
+                                                        d_cus.data_ptr(), n, None, 33, 1, None, 0, 1,
+                                                        d_satd.data_ptr(), None, sp) == 0
+        gpu.intra_rmd_device(d_satd.data_ptr(), n, d_req.data_ptr(), n, d_lists.data_ptr(), sp)
+        lists = d_lists.view(torch.int8).view(n, gpu.RMD_OUT.itemsize)[:, :5].to(torch.int16)
+        modes = torch.where(lists < 0, lists[:, :1], lists).to(torch.uint8).contiguous()
+        assert L.uavs3e_cuda_intra_lattice_modes_device(d_org.data_ptr(), W, d_rec.data_ptr(), W, W, H,
+                                                        d_cus.data_ptr(), n, modes.data_ptr(), 5, 1, qps.ctypes.data,
+                                                        len(qps), 1, d_satd5.data_ptr(), d_q5.data_ptr(), sp) == 0
+
+    want = {}
+    for seed in (41, 42):
+        frame(seed)
+        d_lists.zero_()
+        d_q5.zero_()  # records of modes off a CU's list are left untouched
+        run()
+        torch.cuda.synchronize()
+        want[seed] = (d_lists.clone(), d_q5.clone())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        run()
+    for seed in (41, 42, 41):
+        frame(seed)
+        d_lists.zero_()
+        d_q5.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(d_lists, want[seed][0]) and torch.equal(d_q5, want[seed][1]), seed
