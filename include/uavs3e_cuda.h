@@ -481,7 +481,7 @@ typedef struct { int16_t x, y; uint8_t w, h; uint16_t pad; } uavs3e_cuda_cu_t;
 
 typedef struct {
     uint32_t ssd;         /* SSD(org, reconstruction)                                  */
-    uint32_t coef_hash;   /* sum over non-zero levels of fmix32(pos << 16 | (u16)level) */
+    uint32_t coef_hash;   /* sum of level * ((pos * 0x9E3779B1 + 0x7F4A7C15) | 1), mod 2^32 */
     uint16_t num_nz;      /* non-zero levels                                           */
     int16_t  last_nz;     /* last non-zero level in zig-zag scan order, -1 if none     */
     uint32_t sum_abs;     /* sum of |level|                                            */

@@ -1120,20 +1120,14 @@ void orc_me_frame(const pel *org, int i_org, const pel *const *planes, int i_ref
 
 /* ===================================================================== batched: intra */
 
-/* MurmurHash3's 32-bit finaliser */
-static u32 fmix32(u32 h)
-{
-    h ^= h >> 16; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16;
-    return h;
-}
-
-/* order-independent hash of a level block: sum over non-zero levels of
- * fmix32(raster_position << 16 | (u16)level) */
+/* hash of a level block: sum over positions of level * weight(raster position) mod 2^32, with
+ * the odd weight (i * 0x9E3779B1 + 0x7F4A7C15) | 1: any single changed level, sign flip or
+ * exchange of two different levels changes it */
 u32 orc_level_hash(const s16 *lev, int n)
 {
     u32 hsh = 0;
     for (int i = 0; i < n; i++)
-        if (lev[i]) hsh += fmix32(((u32)i << 16) | (u16)lev[i]);
+        hsh += (u32)(int)lev[i] * (((u32)i * 0x9E3779B1u + 0x7F4A7C15u) | 1u);
     return hsh;
 }
 

@@ -137,7 +137,8 @@ void orc_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, int
                        const orc_cu_t *cus, int n_cus, int ipf, const int *qps, int n_qp, int is_intra_slice,
                        u32 *satd_out, orc_lat_q_t *q_out, int threads);
 
-/* level hash used by the lattice: sum over non-zero levels of fmix32(pos << 16 | (u16)level) */
+/* level hash used by the lattice: sum over positions of level * ((pos * 0x9E3779B1 + 0x7F4A7C15) | 1),
+ * mod 2^32 (pos = raster index in the w x h block) */
 u32 orc_level_hash(const s16 *lev, int n);
 
 /* ------------- lookahead cost estimation (loka_estimate_coding_cost, src/lookahead.c:82) ------------- */

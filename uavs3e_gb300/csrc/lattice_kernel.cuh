@@ -22,11 +22,10 @@ __device__ __constant__ static const u8 kDqShift[80] = {
     9, 8, 8, 8, 8, 8, 8, 8, 7, 7, 7, 7, 7, 7, 7, 7, 6, 6, 6, 6, 6, 6, 6, 6, 5, 5, 5, 5, 5, 5, 5, 5,
 };
 
-__device__ __forceinline__ u32 fmix32(u32 h)
-{
-    h ^= h >> 16; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16;
-    return h;
-}
+// weight of raster position p in the level hash of a record: odd, spread over 32 bits, so the
+// hash sum_p level[p] * weight(p) (mod 2^32) changes with any single level, any sign and any
+// exchange of two different levels
+__host__ __device__ __forceinline__ constexpr u32 lat_pos_weight(u32 p) { return (p * 0x9E3779B1u + 0x7F4A7C15u) | 1u; }
 
 // sum of 4 (unsigned byte of a) x (signed byte of b) products + c
 __device__ __forceinline__ int dp4a_us(u32 a, u32 b, int c)
@@ -208,6 +207,23 @@ __device__ __forceinline__ void lat_row(const void *p, u32 (&r)[NW])
     }
 }
 
+// position of index k in a row of n entries stored in even/odd order (the even k first)
+__host__ __device__ __forceinline__ constexpr int lat_eo(int k, int n) { return (k & 1) ? (n >> 1) + (k >> 1) : (k >> 1); }
+
+// the even part E and the odd part O of sum_k F[k] D[k] over N entries, D as s16 pairs and F as
+// bytes, both in even/odd order (D: N/2 words, F: N/4 words)
+template <int N>
+__device__ __forceinline__ void lat_eo_sums(const u32 (&d)[N / 2], const u32 (&f)[N / 4], int &e, int &o)
+{
+#pragma unroll
+    for (int p = 0; p < N / 4; p++) {
+        constexpr int H = N / 2;
+        const int be = 2 * p, bo = H + 2 * p;   // byte of the pair's first entry in F
+        e = ((be >> 1) & 1) ? dp2a_hi(d[p], f[be >> 2], e) : dp2a_lo(d[p], f[be >> 2], e);
+        o = ((bo >> 1) & 1) ? dp2a_hi(d[N / 4 + p], f[bo >> 2], o) : dp2a_lo(d[N / 4 + p], f[bo >> 2], o);
+    }
+}
+
 // sum over aligned groups of SEG lanes (SEG a power of two <= 32)
 template <int SEG>
 __device__ __forceinline__ u32 lat_seg_sum(u32 v, int lane)
@@ -343,18 +359,23 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
     u32 *fht = (u32 *)(sm + L.o_fht), *fwt = (u32 *)(sm + L.o_fwt);
     u8 *cub = sm + L.o_cu, *jobb = sm + L.o_job;
 
-    // ---- matrices: rows packed 4 bytes to a word
+    // ---- matrices: rows packed 4 bytes to a word.  The inverse passes use the even/odd
+    // symmetry of the folded DCT2 (row k of an N-point matrix satisfies F[k][N-1-n] =
+    // (-1)^k F[k][n], as the encoder's butterflies build it): for the first half of the outputs
+    // n they keep column n with the even-k entries first and the odd-k entries after them
+    // (Fw^T, Fh^T in even/odd order), and each sum over k splits into an even part E and an odd
+    // part O with out[n] = E + O and out[N-1-n] = E - O.
     for (int i = tid; i < kw * w; i += LAT_THREADS) {
         const int u = i >> lw, x = i & (w - 1);
         const u8 v = (u8)P.fold[LW][u * w + x];
         ((u8 *)fw)[u * L.fw_ws * 4 + x] = v;        // Fw[u][x]
-        ((u8 *)fwt)[x * L.fwt_ws * 4 + u] = v;      // Fw^T[x][u]
+        if (x < (w >> 1)) ((u8 *)fwt)[x * L.fwt_ws * 4 + lat_eo(u, kw)] = v;
     }
     for (int i = tid; i < kh * h; i += LAT_THREADS) {
         const int v = i >> lh, y = i & (h - 1);
         const u8 c = (u8)P.fold[LH][v * h + y];
         ((u8 *)fh)[v * L.fh_ws * 4 + y] = c;        // Fh[v][y]
-        ((u8 *)fht)[y * L.fht_ws * 4 + v] = c;      // Fh^T[y][v]
+        if (y < (h >> 1)) ((u8 *)fht)[y * L.fht_ws * 4 + lat_eo(v, kh)] = c;
     }
     u16 *s_scan = (u16 *)(sm + L.o_scan);
     for (int i = tid; i < kw * kh; i += LAT_THREADS) s_scan[i] = P.scanpos[LW][LH][(i >> lkw) * w + (i & (kw - 1))];
@@ -516,7 +537,8 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         const int dq_scale = (int)kDqScale[qp];
         const int dq_shift = (int)kDqShift[qp] - (15 - 8 - log2_size) + 1;
         const int dq_off = dq_shift == 0 ? 0 : 1 << (dq_shift - 1);
-        // first-pass levels, statistics, dequantisation (stored transposed, DQ^T[u][v]).  The
+        // first-pass levels, statistics, dequantisation (stored transposed, DQ^T[u][v], each row
+        // in even/odd order of v).  The
         // level (|c| q_value + 2^(q_bits-1)) >> q_bits is exact in 32 bits: |c| <= 2^15 and
         // q_value < 2^15.
         // A task is one coefficient row v of a job over RU columns (lanes take consecutive v):
@@ -547,13 +569,13 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
                     if (lev) {
                         nz++;
                         sa += (u32)(lev < 0 ? -lev : lev);
-                        hs += fmix32(((u32)(v * w + u) << 16) | (u16)(s16)lev);
+                        hs += (u32)lev * lat_pos_weight((u32)(v * w + u));
                         last = max(last, (int)s_scan[v * KW_ + u]);
                         int d = (lev * dq_scale + dq_off) >> dq_shift;
                         d = min(32767, max(-32768, d));
                         dq = odd ? (d * 181 + 128) >> 8 : d;
                     }
-                    if (act) JDQT(j)[u * L.ds + v] = (s16)dq;
+                    if (act) JDQT(j)[u * L.ds + lat_eo(v, KH_)] = (s16)dq;
                 }
                 if (__any_sync(0xFFFFFFFFu, nz != 0)) {
                     nz = lat_seg_sum<SEG>(nz, lane);
@@ -571,60 +593,59 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         }
         __syncthreads();
         // inverse column pass T2[y][u] = clip16((sum_v Fh[v][y] DQ[v][u] + 16) >> 5), only
-        // for jobs with coded levels
-        for (int i = tid; i < J * NUC * H_; i += LAT_THREADS) {
-            const int y = i & (H_ - 1), uc = (i >> LH) % NUC, j = i / (H_ * NUC);
+        // for jobs with coded levels; a task forms rows y and H-1-y from the even-v and odd-v
+        // sums, and T2 rows are stored in even/odd order of u
+        for (int i = tid; i < J * NUC * (H_ / 2); i += LAT_THREADS) {
+            const int y = i & (H_ / 2 - 1), uc = (i >> (LH - 1)) % NUC, j = i / ((H_ / 2) * NUC);
             if (!s_nz[j]) continue;
             u32 f[KH_ / 4];
 #pragma unroll
             for (int k = 0; k < KH_ / 4; k++) f[k] = fht[y * L.fht_ws + k];
-#pragma unroll
+#pragma unroll 2   // two rows per step: a full unroll spills at the 64-register limit
             for (int r = 0; r < RU; r++) {
                 const int u = uc * RU + r;
                 u32 dw[KH_ / 2];
                 lat_row<KH_ / 2>(JDQT(j) + u * L.ds, dw);
-                int acc = 0;
-#pragma unroll
-                for (int k = 0; k < KH_ / 4; k++) {
-                    acc = dp2a_lo(dw[2 * k], f[k], acc);
-                    acc = dp2a_hi(dw[2 * k + 1], f[k], acc);
-                }
-                JT2(j)[y * L.t2s + u] = (s16)min(32767, max(-32768, (acc + 16) >> 5));
+                int e = 0, o = 0;
+                lat_eo_sums<KH_>(dw, f, e, o);
+                s16 *t2 = JT2(j) + lat_eo(u, KW_);
+                t2[y * L.t2s] = (s16)min(32767, max(-32768, (e + o + 16) >> 5));
+                t2[(H_ - 1 - y) * L.t2s] = (s16)min(32767, max(-32768, (e - o + 16) >> 5));
             }
         }
         __syncthreads();
-        // inverse row pass, reconstruction, SSD: a task is one column x over RY rows
+        // inverse row pass, reconstruction, SSD: a task is the column pair x, W-1-x over RY
+        // rows (the even-u and odd-u sums of the T2 row give both)
         {
-            constexpr int TPJ = W_ * NYC, SEG = TPJ < 32 ? TPJ : 32;
+            constexpr int TPJ = (W_ / 2) * NYC, SEG = TPJ < 32 ? TPJ : 32;
             for (int base = wbase; base < J * TPJ; base += LAT_THREADS) {
                 const int i = base + lane;
                 const bool act = i < J * TPJ;
                 const int ii = act ? i : base;
-                const int x = ii & (W_ - 1), yc = (ii >> LW) % NYC, j = ii / TPJ;
+                const int x = ii & (W_ / 2 - 1), yc = (ii >> (LW - 1)) % NYC, j = ii / TPJ;
                 const bool coded = s_nz[j] != 0;
                 u32 f[KW_ / 4];
 #pragma unroll
                 for (int k = 0; k < KW_ / 4; k++) f[k] = fwt[x * L.fwt_ws + k];
                 const pel *po = CORG(JG(j));
+                const pel *pp = JPRED(j);
                 u32 e = 0;
 #pragma unroll
                 for (int r = 0; r < RY; r++) {
                     const int y = yc * RY + r;
-                    int rv = JPRED(j)[y * L.ps + x];
+                    int rv0 = pp[y * L.ps + x], rv1 = pp[y * L.ps + W_ - 1 - x];
                     if (coded) {
                         u32 tw[KW_ / 2];
                         lat_row<KW_ / 2>(JT2(j) + y * L.t2s, tw);
-                        int acc = 0;
-#pragma unroll
-                        for (int k = 0; k < KW_ / 4; k++) {
-                            acc = dp2a_lo(tw[2 * k], f[k], acc);
-                            acc = dp2a_hi(tw[2 * k + 1], f[k], acc);
-                        }
-                        const int res = min(255, max(-256, (acc + 2048) >> 12));
-                        rv = min(255, max(0, rv + res));
+                        int se = 0, so = 0;
+                        lat_eo_sums<KW_>(tw, f, se, so);
+                        const int res0 = min(255, max(-256, (se + so + 2048) >> 12));
+                        const int res1 = min(255, max(-256, (se - so + 2048) >> 12));
+                        rv0 = min(255, max(0, rv0 + res0));
+                        rv1 = min(255, max(0, rv1 + res1));
                     }
-                    const int d = (int)po[y * L.ps + x] - rv;
-                    e += (u32)(d * d);
+                    const int d0 = (int)po[y * L.ps + x] - rv0, d1 = (int)po[y * L.ps + W_ - 1 - x] - rv1;
+                    e += (u32)(d0 * d0) + (u32)(d1 * d1);
                 }
                 if (!act) e = 0;
                 e = lat_seg_sum<SEG>(e, lane);
