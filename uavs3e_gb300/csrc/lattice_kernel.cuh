@@ -1,11 +1,13 @@
-// Device side of the batched intra lattice (one kernel instance per CU shape); the launcher,
-// the shape grouping and the C ABI are in lattice.cu, the instances in lattice_w*.cu.
+// Device side of the batched intra lattice: the tile body of every CU shape class; the
+// persistent kernel, the device work queue, the layout tuner and the C ABI are in lattice.cu.
 #pragma once
 #include "common.cuh"
 #include "intra.cuh"
 #include "tables.h"
 #include "uavs3e_cuda_internal.h"
 #include "quant_tables.cuh"
+
+#include <type_traits>
 
 namespace uc {
 
@@ -555,26 +557,20 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
                 int last = -1;
 #pragma unroll
                 for (int r = 0; r < RU; r++) {
+                    // branch-free: a zero level adds nothing to the statistics and dequantises
+                    // to zero ((0 * scale + 2^(shift-1)) >> shift)
                     const int u = uc * RU + r;
-                    int lev = 0;
-                    if (coded) {
-                        const int c = JC(j)[v * L.cs + u];
-                        const int a = c < 0 ? -c : c;
-                        if (a >= thr) {
-                            const int l = (int)(s16)(((u32)a * q_value + qadd) >> q_bits);
-                            lev = c < 0 ? -l : l;
-                        }
-                    }
-                    int dq = 0;
-                    if (lev) {
-                        nz++;
-                        sa += (u32)(lev < 0 ? -lev : lev);
-                        hs += (u32)lev * lat_pos_weight((u32)(v * w + u));
-                        last = max(last, (int)s_scan[v * KW_ + u]);
-                        int d = (lev * dq_scale + dq_off) >> dq_shift;
-                        d = min(32767, max(-32768, d));
-                        dq = odd ? (d * 181 + 128) >> 8 : d;
-                    }
+                    const int c = coded ? (int)JC(j)[v * L.cs + u] : 0;
+                    const int a = c < 0 ? -c : c;
+                    const int l = a >= thr ? (int)(s16)(((u32)a * q_value + qadd) >> q_bits) : 0;
+                    const int lev = c < 0 ? -l : l;
+                    nz += lev != 0 ? 1u : 0u;
+                    sa += (u32)(lev < 0 ? -lev : lev);
+                    hs += (u32)lev * lat_pos_weight((u32)(v * w + u));
+                    if (lev) last = max(last, (int)s_scan[v * KW_ + u]);
+                    int d = (lev * dq_scale + dq_off) >> dq_shift;
+                    d = min(32767, max(-32768, d));
+                    const int dq = odd ? (d * 181 + 128) >> 8 : d;
                     if (act) JDQT(j)[u * L.ds + lat_eo(v, KH_)] = (s16)dq;
                 }
                 if (__any_sync(0xFFFFFFFFu, nz != 0)) {
@@ -594,35 +590,43 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         __syncthreads();
         // inverse column pass T2[y][u] = clip16((sum_v Fh[v][y] DQ[v][u] + 16) >> 5), only
         // for jobs with coded levels; a task forms rows y and H-1-y from the even-v and odd-v
-        // sums, and T2 rows are stored in even/odd order of u
-        for (int i = tid; i < J * NUC * (H_ / 2); i += LAT_THREADS) {
-            const int y = i & (H_ / 2 - 1), uc = (i >> (LH - 1)) % NUC, j = i / ((H_ / 2) * NUC);
-            if (!s_nz[j]) continue;
-            u32 f[KH_ / 4];
+        // sums over CU columns u (T2 rows are stored in even/odd order of u).  Tiles with few
+        // jobs take CU/2 columns per task so that the CTA's threads still have a task each.
+        auto inv_col = [&](auto cu_tag) {
+            constexpr int CU = decltype(cu_tag)::value, NCU = KW_ / CU;
+            for (int i = tid; i < J * NCU * (H_ / 2); i += LAT_THREADS) {
+                const int y = i & (H_ / 2 - 1), uc = (i >> (LH - 1)) % NCU, j = i / ((H_ / 2) * NCU);
+                if (!s_nz[j]) continue;
+                u32 f[KH_ / 4];
 #pragma unroll
-            for (int k = 0; k < KH_ / 4; k++) f[k] = fht[y * L.fht_ws + k];
-#pragma unroll 2   // two rows per step: a full unroll spills at the 64-register limit
-            for (int r = 0; r < RU; r++) {
-                const int u = uc * RU + r;
-                u32 dw[KH_ / 2];
-                lat_row<KH_ / 2>(JDQT(j) + u * L.ds, dw);
-                int e = 0, o = 0;
-                lat_eo_sums<KH_>(dw, f, e, o);
-                s16 *t2 = JT2(j) + lat_eo(u, KW_);
-                t2[y * L.t2s] = (s16)min(32767, max(-32768, (e + o + 16) >> 5));
-                t2[(H_ - 1 - y) * L.t2s] = (s16)min(32767, max(-32768, (e - o + 16) >> 5));
+                for (int k = 0; k < KH_ / 4; k++) f[k] = fht[y * L.fht_ws + k];
+#pragma unroll 2   // two columns per step: a full unroll spills at the 64-register limit
+                for (int r = 0; r < CU; r++) {
+                    const int u = uc * CU + r;
+                    u32 dw[KH_ / 2];
+                    lat_row<KH_ / 2>(JDQT(j) + u * L.ds, dw);
+                    int e = 0, o = 0;
+                    lat_eo_sums<KH_>(dw, f, e, o);
+                    s16 *t2 = JT2(j) + lat_eo(u, KW_);
+                    t2[y * L.t2s] = (s16)min(32767, max(-32768, (e + o + 16) >> 5));
+                    t2[(H_ - 1 - y) * L.t2s] = (s16)min(32767, max(-32768, (e - o + 16) >> 5));
+                }
             }
-        }
+        };
+        if (RU > 2 && J * NUC * (H_ / 2) < LAT_THREADS) inv_col(std::integral_constant<int, (RU > 2 ? RU / 2 : RU)>{});
+        else inv_col(std::integral_constant<int, RU>{});
         __syncthreads();
-        // inverse row pass, reconstruction, SSD: a task is the column pair x, W-1-x over RY
-        // rows (the even-u and odd-u sums of the T2 row give both)
-        {
-            constexpr int TPJ = (W_ / 2) * NYC, SEG = TPJ < 32 ? TPJ : 32;
+        // inverse row pass, reconstruction, SSD: a task is the column pair x, W-1-x over CY
+        // rows (the even-u and odd-u sums of the T2 row give both); CY = RY / 2 for tiles with
+        // few jobs
+        auto inv_row = [&](auto cy_tag) {
+            constexpr int CY = decltype(cy_tag)::value, NCY = H_ / CY;
+            constexpr int TPJ = (W_ / 2) * NCY, SEG = TPJ < 32 ? TPJ : 32;
             for (int base = wbase; base < J * TPJ; base += LAT_THREADS) {
                 const int i = base + lane;
                 const bool act = i < J * TPJ;
                 const int ii = act ? i : base;
-                const int x = ii & (W_ / 2 - 1), yc = (ii >> (LW - 1)) % NYC, j = ii / TPJ;
+                const int x = ii & (W_ / 2 - 1), yc = (ii >> (LW - 1)) % NCY, j = ii / TPJ;
                 const bool coded = s_nz[j] != 0;
                 u32 f[KW_ / 4];
 #pragma unroll
@@ -631,8 +635,8 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
                 const pel *pp = JPRED(j);
                 u32 e = 0;
 #pragma unroll
-                for (int r = 0; r < RY; r++) {
-                    const int y = yc * RY + r;
+                for (int r = 0; r < CY; r++) {
+                    const int y = yc * CY + r;
                     int rv0 = pp[y * L.ps + x], rv1 = pp[y * L.ps + W_ - 1 - x];
                     if (coded) {
                         u32 tw[KW_ / 2];
@@ -651,7 +655,9 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
                 e = lat_seg_sum<SEG>(e, lane);
                 if (act && (lane & (SEG - 1)) == 0) atomicAdd(&s_ssd[j], e);
             }
-        }
+        };
+        if (RY > 2 && J * (W_ / 2) * NYC < LAT_THREADS) inv_row(std::integral_constant<int, (RY > 2 ? RY / 2 : RY)>{});
+        else inv_row(std::integral_constant<int, RY>{});
         __syncthreads();
         for (int j = tid; j < J; j += LAT_THREADS) {
             const int g = JG(j);
