@@ -133,21 +133,25 @@ __device__ __forceinline__ int ang_sample(const pel *s, int mode, int w, int h, 
     return f4tap(s[idx], s[idx - 1], s[idx - 2], s[idx - 3], off);
 }
 
-// final prediction sample of com_intra_pred(ipm, ipf) at (i, j)
+// final prediction sample of com_intra_pred(ipm, ipf) at (i, j); with CW, CH > 0 the block is
+// known at compile time to be CW x CH at 8 bits (B's size fields are then not read)
+template <int CW = 0, int CH = 0>
 __device__ __forceinline__ int ipred_sample(const pel *s, const IpredBlock &B, int ipm, int ipf, int i, int j)
 {
-    const int w = B.w, h = B.h, mx = (1 << B.bd) - 1;
+    constexpr bool K = CW > 0 && CH > 0;
+    const int w = K ? CW : B.w, h = K ? CH : B.h, mx = K ? 255 : (1 << B.bd) - 1;
+    const int blw = K ? ilog2d(CW) : B.lw, blh = K ? ilog2d(CH) : B.lh;
     int v;
     bool s16path = false;
     if (ipm == 1) {                                         // plane
         v = (B.pl_t + j * B.pl_c + i * B.pl_b) >> 5;
         s16path = true;
     } else if (ipm == 2) {                                  // bilinear
-        int lxy = B.lw + B.lh + 1, offs = 1 << (B.lw + B.lh);
+        int lxy = blw + blh + 1, offs = 1 << (blw + blh);
         int up = s[i + 1], le = s[-j - 1];
-        int predx = (le << B.lw) + (i + 1) * (B.bi_a - le);
-        int refup = (up << B.lh) + (j + 1) * (B.bi_b - up);
-        v = ((predx << B.lh) + (refup << B.lw) + i * j * B.bi_wt + offs) >> lxy;
+        int predx = (le << blw) + (i + 1) * (B.bi_a - le);
+        int refup = (up << blh) + (j + 1) * (B.bi_b - up);
+        v = ((predx << blh) + (refup << blw) + i * j * B.bi_wt + offs) >> lxy;
         s16path = true;
     } else if (ipm == 0) {
         v = B.dc;
@@ -161,7 +165,7 @@ __device__ __forceinline__ int ipred_sample(const pel *s, const IpredBlock &B, i
     if (s16path && !ipf) return min(mx, max(0, v));
     if (!ipf) return v;
     // IPF ranges (ipf_core / ipf_core_s16)
-    int ih = B.lw - 2, iv = B.lh - 2;
+    int ih = blw - 2, iv = blh - 2;
     int vr = min(h, 10), hr = min(w, 10);
     if (ih > 4) { ih = 4; hr = 0; }
     if (iv > 4) { iv = 4; vr = 0; }

@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(LAT_THREADS, 4) k_intra_lattice(const __grid_c
     __shared__ int s_t;
     const int tid = threadIdx.x;
     const int total = __ldg(P.tile_off + LAT_SHAPES);
+    if (tid == 0) S.tables = -1;
     for (;;) {
         if (tid == 0) s_t = atomicAdd(P.next, 1);
         __syncthreads();

@@ -165,6 +165,7 @@ struct LatShared {
     u32 satd[LAT_MAX_JOBS], flag[LAT_MAX_JOBS];
     u32 nz[LAT_MAX_JOBS], sum[LAT_MAX_JOBS], hash[LAT_MAX_JOBS], ssd[LAT_MAX_JOBS];
     int last[LAT_MAX_JOBS];
+    int tables;   // shape class whose matrices and scan table are in place (-1: none)
 };
 
 // lanes [k*seg, (k+1)*seg) of a warp hold one job's elements (seg = 16 or 32): the sum, max
@@ -356,6 +357,9 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
     const int MCv = min(L.MC, P.n_modes - m0);
     const int J = Gv * MCv;
     if (Gv <= 0 || MCv <= 0) return;
+    // j / MCv as a multiply: with m = ceil(2^16 / MCv), (j m) >> 16 = j / MCv for every
+    // j * MCv < 2^16 (here j < 8 * 33 and MCv <= 33)
+    const u32 mc_magic = (65536u + (u32)MCv - 1u) / (u32)MCv;
 
     u32 *fw = (u32 *)(sm + L.o_fw), *fh = (u32 *)(sm + L.o_fh);
     u32 *fht = (u32 *)(sm + L.o_fht), *fwt = (u32 *)(sm + L.o_fwt);
@@ -367,20 +371,26 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
     // n they keep column n with the even-k entries first and the odd-k entries after them
     // (Fw^T, Fh^T in even/odd order), and each sum over k splits into an even part E and an odd
     // part O with out[n] = E + O and out[N-1-n] = E - O.
-    for (int i = tid; i < kw * w; i += LAT_THREADS) {
+    // A CTA takes its tiles from the queue in class order, so consecutive tiles mostly share
+    // the class: the tables of the previous tile are kept (the layout of a class is fixed
+    // within a launch).
+    const int cls = (LW - 2) * 5 + (LH - 2);
+    const bool tables_in_place = S.tables == cls;
+    for (int i = tid; i < (tables_in_place ? 0 : kw * w); i += LAT_THREADS) {
         const int u = i >> lw, x = i & (w - 1);
         const u8 v = (u8)P.fold[LW][u * w + x];
         ((u8 *)fw)[u * L.fw_ws * 4 + x] = v;        // Fw[u][x]
         if (x < (w >> 1)) ((u8 *)fwt)[x * L.fwt_ws * 4 + lat_eo(u, kw)] = v;
     }
-    for (int i = tid; i < kh * h; i += LAT_THREADS) {
+    for (int i = tid; i < (tables_in_place ? 0 : kh * h); i += LAT_THREADS) {
         const int v = i >> lh, y = i & (h - 1);
         const u8 c = (u8)P.fold[LH][v * h + y];
         ((u8 *)fh)[v * L.fh_ws * 4 + y] = c;        // Fh[v][y]
         if (y < (h >> 1)) ((u8 *)fht)[y * L.fht_ws * 4 + lat_eo(v, kh)] = c;
     }
     u16 *s_scan = (u16 *)(sm + L.o_scan);
-    for (int i = tid; i < kw * kh; i += LAT_THREADS) s_scan[i] = P.scanpos[LW][LH][(i >> lkw) * w + (i & (kw - 1))];
+    for (int i = tid; i < (tables_in_place ? 0 : kw * kh); i += LAT_THREADS)
+        s_scan[i] = P.scanpos[LW][LH][(i >> lkw) * w + (i & (kw - 1))];
     if (tid < Gv) s_cu[tid] = perm[cu0 + tid];
     for (int j = tid; j < J; j += LAT_THREADS) {
         const int g = j / MCv, mi = m0 + (j - g * MCv);
@@ -388,6 +398,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         s_satd[j] = 0; s_flag[j] = 0; s_nz[j] = 0; s_sum[j] = 0; s_hash[j] = 0; s_ssd[j] = 0; s_last[j] = -1;
     }
     __syncthreads();
+    if (tid == 0) S.tables = cls;   // every thread has read S.tables above
 
     // ---- per CU: org block, neighbours (com_intra_get_nbr with every in-picture sample
     // reconstructed)
@@ -437,7 +448,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
     __syncthreads();
 
     // job j -> (CU g, mode m): j = g * MCv + (m - m0)
-#define JG(j) ((j) / MCv)
+#define JG(j) ((int)(((u32)(j) * mc_magic) >> 16))
 #define JPRED(j) (jobb + (j) * L.job_bytes + L.j_pred)
 #define JT(j) ((s16 *)(jobb + (j) * L.job_bytes + L.j_t))
 #define JC(j) ((s16 *)(jobb + (j) * L.job_bytes + L.j_c))
@@ -450,7 +461,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         const int j = i >> lN, p = i & (N - 1);
         const int g = JG(j), m = s_mode[j];
         const int x = p & (w - 1), y = p >> lw;
-        JPRED(j)[y * L.ps + x] = (pel)ipred_sample(cub + g * L.cu_bytes + L.c_nb + 288, sB[g], m, P.ipf, x, y);
+        JPRED(j)[y * L.ps + x] = (pel)ipred_sample<W_, H_>(cub + g * L.cu_bytes + L.c_nb + 288, sB[g], m, P.ipf, x, y);
     }
     __syncthreads();
 
