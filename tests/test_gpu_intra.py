@@ -73,6 +73,41 @@ def test_intra_lattice_unsorted_and_invalid_cus(gpu, oracle):
     assert np.array_equal(q[valid].ravel(), q_o)
 
 
+def test_intra_lattice_odd_pitch_and_unaligned_cus(gpu, oracle):
+    # the org block is read by words only where the picture pitch and the CU's x allow it: an odd
+    # row pitch, and CUs at x not a multiple of 4, take the byte path with the same records
+    import torch
+    W, H = 96, 64
+    org = intra_frame(W, H, seed=9)
+    rec = np.clip(org.astype(int) + np.random.default_rng(9).integers(-4, 5, org.shape), 0, 255).astype(np.uint8)
+    cus = gpu.lattice_cus(W, H)
+    odd = np.zeros(4, dtype=cus.dtype)
+    odd[0] = (1, 3, 8, 8, 0)
+    odd[1] = (5, 17, 16, 4, 0)
+    odd[2] = (30, 2, 4, 16, 0)
+    odd[3] = (61, 31, 32, 32, 0)
+    allc = np.concatenate([cus[::7], odd])
+    qps = [27, 42]
+    satd_o, q_o = oracle_lattice(oracle, org, rec, allc, 1, qps)
+    for pitch in (W, W + 1):
+        po = np.zeros((H, pitch), np.uint8)
+        po[:, :W] = org
+        d_org = torch.from_numpy(po).cuda()
+        d_rec = torch.from_numpy(rec).cuda()
+        d_cus = torch.from_numpy(np.ascontiguousarray(allc).view(np.uint8)).cuda()
+        n = len(allc)
+        q = np.array(qps, np.int32)
+        d_satd = torch.zeros(n * 33, dtype=torch.int32, device="cuda")
+        d_q = torch.zeros(n * 33 * len(q) * gpu.LAT_Q.itemsize, dtype=torch.uint8, device="cuda")
+        gpu.check(gpu.lib().uavs3e_cuda_intra_lattice_device(d_org.data_ptr(), pitch, d_rec.data_ptr(), W, W, H,
+                                                             d_cus.data_ptr(), n, 1, q.ctypes.data, len(q), 1,
+                                                             d_satd.data_ptr(), d_q.data_ptr(),
+                                                             torch.cuda.current_stream().cuda_stream), "intra_lattice")
+        torch.cuda.synchronize()
+        assert np.array_equal(d_satd.cpu().numpy().view(np.uint32), satd_o), pitch
+        assert np.array_equal(d_q.cpu().numpy().view(gpu.LAT_Q), q_o), pitch
+
+
 def test_intra_lattice_mode_subset(gpu):
     # a shortlist of modes per CU writes exactly those records, equal to the full lattice's
     import ctypes as C

@@ -287,6 +287,7 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     LatParams P;
     memset(&P, 0, sizeof(P));
     P.org = org; P.i_org = i_org; P.rec = rec; P.i_rec = i_rec; P.W = W; P.H = H;
+    P.org_words = ((uintptr_t)org % 4 == 0 && i_org % 4 == 0) ? 1 : 0;
     P.cus = cus; P.ipf = ipf; P.n_qp = n_qp; P.is_intra = is_intra;
     for (int i = 0; i < LAT_MAX_QP; i++) P.qp[i] = i < n_qp ? qps[i] : 0;
     P.satd_out = satd_out; P.q_out = q_out;

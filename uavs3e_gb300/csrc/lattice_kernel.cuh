@@ -137,6 +137,7 @@ __host__ __device__ inline void lat_layout(int lw, int lh, int nm, int budget, L
 
 struct LatParams {
     const pel *org; int i_org;
+    int org_words;            // org and i_org are multiples of 4 (word loads for word-aligned CUs)
     const pel *rec; int i_rec;
     int W, H;
     const LatCu *cus;
@@ -402,11 +403,15 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
 
     // ---- per CU: org block, neighbours (com_intra_get_nbr with every in-picture sample
     // reconstructed)
-    for (int i = tid; i < Gv * N; i += LAT_THREADS) {
-        const int g = i >> lN, p = i & (N - 1);
+    // four samples per thread: one word load where the picture and the CU's x are word-aligned
+    for (int i = tid; i < Gv * (N >> 2); i += LAT_THREADS) {
+        const int g = i >> (lN - 2), p = (i & ((N >> 2) - 1)) << 2;
         const LatCu cu = P.cus[s_cu[g]];
-        (cub + g * L.cu_bytes + L.c_org)[(p >> lw) * L.ps + (p & (w - 1))] =
-            P.org[(long long)(cu.y + (p >> lw)) * P.i_org + cu.x + (p & (w - 1))];
+        const pel *src = P.org + (long long)(cu.y + (p >> lw)) * P.i_org + cu.x + (p & (w - 1));
+        u32 v;
+        if (P.org_words && !(cu.x & 3)) v = __ldg(reinterpret_cast<const u32 *>(src));
+        else v = (u32)src[0] | (u32)src[1] << 8 | (u32)src[2] << 16 | (u32)src[3] << 24;
+        *reinterpret_cast<u32 *>(cub + g * L.cu_bytes + L.c_org + (p >> lw) * L.ps + (p & (w - 1))) = v;
     }
     const int range = max(w, h) * 4 + 4;
     for (int i = tid; i < Gv * range; i += LAT_THREADS) {
