@@ -475,7 +475,8 @@ UAVS3E_CUDA_API int uavs3e_cuda_me_chroma_stride(const uavs3e_cuda_me *me);
  * dependent second pass stays with the CPU), dequantisation (com_dquant :807), inverse DCT2
  * (itrans_dct2 :264-423) and reconstruction (com_recon src/com_util.c:3107).
  *   satd[cu*33 + mode]; q[(cu*33 + mode)*n_qp + qp_index]  (n_qp <= 4)
- * CU sides are powers of two in 4..64 inside the picture (others yield zeroed records).
+ * CU sides are powers of two in 4..64, positions multiples of 4 (the encoder's 4x4 grid), CUs
+ * inside the picture (others yield zeroed records).
  */
 typedef struct { int16_t x, y; uint8_t w, h; uint16_t pad; } uavs3e_cuda_cu_t;
 
@@ -498,6 +499,12 @@ typedef struct {
  * 48 KB (not tuned). */
 UAVS3E_CUDA_API void uavs3e_cuda_lattice_autotune(int on);
 UAVS3E_CUDA_API int uavs3e_cuda_lattice_budgets(int n_modes, int out[25]);
+
+/* Per-stage SM cycles of the lattice tiles since the last call with clear != 0, as
+ * out[25 shape classes][10 stages] (summed over CTAs; thread 0 of a CTA reads clock64 at each
+ * CTA barrier of a tile).  Only a library built with UAVS3E_LAT_STAGE_CLOCKS keeps them
+ * (python -m uavs3e_gb300.lattice_stages builds one); otherwise UAVS3E_CUDA_ERR_UNSUPPORTED. */
+UAVS3E_CUDA_API int uavs3e_cuda_lattice_stage_clocks(unsigned long long *out, int clear);
 
 /*
  * Intra mode candidates: make_ipred_list (src/intra.c:226-367, file-local) for a list of

@@ -74,38 +74,41 @@ def test_intra_lattice_unsorted_and_invalid_cus(gpu, oracle):
 
 
 def test_intra_lattice_odd_pitch_and_unaligned_cus(gpu, oracle):
-    # the org block is read by words only where the picture pitch and the CU's x allow it: an odd
-    # row pitch, and CUs at x not a multiple of 4, take the byte path with the same records
+    # the org blocks are read by words only where the picture and its pitch are word-aligned: an
+    # odd row pitch takes the byte path with the same records; CUs off the 4x4 grid are outside
+    # the supported set and come back zeroed
     import torch
     W, H = 96, 64
     org = intra_frame(W, H, seed=9)
     rec = np.clip(org.astype(int) + np.random.default_rng(9).integers(-4, 5, org.shape), 0, 255).astype(np.uint8)
-    cus = gpu.lattice_cus(W, H)
-    odd = np.zeros(4, dtype=cus.dtype)
-    odd[0] = (1, 3, 8, 8, 0)
-    odd[1] = (5, 17, 16, 4, 0)
+    cus = gpu.lattice_cus(W, H)[::5]
+    odd = np.zeros(3, dtype=cus.dtype)
+    odd[0] = (1, 4, 8, 8, 0)
+    odd[1] = (8, 18, 16, 4, 0)
     odd[2] = (30, 2, 4, 16, 0)
-    odd[3] = (61, 31, 32, 32, 0)
-    allc = np.concatenate([cus[::7], odd])
+    allc = np.concatenate([cus, odd])
     qps = [27, 42]
-    satd_o, q_o = oracle_lattice(oracle, org, rec, allc, 1, qps)
+    satd_o, q_o = oracle_lattice(oracle, org, rec, cus, 1, qps)
+    n, nv = len(allc), len(cus)
     for pitch in (W, W + 1):
         po = np.zeros((H, pitch), np.uint8)
         po[:, :W] = org
         d_org = torch.from_numpy(po).cuda()
         d_rec = torch.from_numpy(rec).cuda()
         d_cus = torch.from_numpy(np.ascontiguousarray(allc).view(np.uint8)).cuda()
-        n = len(allc)
         q = np.array(qps, np.int32)
-        d_satd = torch.zeros(n * 33, dtype=torch.int32, device="cuda")
-        d_q = torch.zeros(n * 33 * len(q) * gpu.LAT_Q.itemsize, dtype=torch.uint8, device="cuda")
+        d_satd = torch.full((n * 33,), -1, dtype=torch.int32, device="cuda")
+        d_q = torch.full((n * 33 * len(q) * gpu.LAT_Q.itemsize,), 255, dtype=torch.uint8, device="cuda")
         gpu.check(gpu.lib().uavs3e_cuda_intra_lattice_device(d_org.data_ptr(), pitch, d_rec.data_ptr(), W, W, H,
                                                              d_cus.data_ptr(), n, 1, q.ctypes.data, len(q), 1,
                                                              d_satd.data_ptr(), d_q.data_ptr(),
                                                              torch.cuda.current_stream().cuda_stream), "intra_lattice")
         torch.cuda.synchronize()
-        assert np.array_equal(d_satd.cpu().numpy().view(np.uint32), satd_o), pitch
-        assert np.array_equal(d_q.cpu().numpy().view(gpu.LAT_Q), q_o), pitch
+        satd = d_satd.cpu().numpy().view(np.uint32)
+        rq = d_q.cpu().numpy().view(gpu.LAT_Q)
+        assert np.array_equal(satd[:nv * 33], satd_o), pitch
+        assert np.array_equal(rq[:nv * 33 * len(q)], q_o), pitch
+        assert not satd[nv * 33:].any() and not rq[nv * 33 * len(q):].view(np.uint8).any(), pitch
 
 
 def test_intra_lattice_mode_subset(gpu):

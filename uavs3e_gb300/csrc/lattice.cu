@@ -32,12 +32,12 @@
 namespace uc {
 
 // shape class of a CU: (log2 w - 2) * 5 + (log2 h - 2), or -1 outside the supported set
-// (power-of-two sides 4..64 inside the picture)
+// (power-of-two sides 4..64 inside the picture, on the 4x4 grid the encoder's CUs lie on)
 __device__ __forceinline__ int lat_class(const LatCu &cu, int W, int H)
 {
     const int w = cu.w, h = cu.h;
     if (w < 4 || w > 64 || h < 4 || h > 64 || (w & (w - 1)) || (h & (h - 1)) || cu.x < 0 || cu.y < 0 ||
-        cu.x + w > W || cu.y + h > H)
+        (cu.x & 3) || (cu.y & 3) || cu.x + w > W || cu.y + h > H)
         return -1;
     return (ilog2d(w) - 2) * 5 + (ilog2d(h) - 2);
 }
@@ -457,3 +457,21 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice_device(const uint8_t *d_org, int i
 }
 
 }  // extern "C"
+
+// per-stage SM cycles of the lattice tiles since the last clear, [25 classes][10 stages] (a
+// library built with UAVS3E_LAT_STAGE_CLOCKS; otherwise UC_ERR_UNSUPPORTED, nothing written)
+UAVS3E_CUDA_API int uavs3e_cuda_lattice_stage_clocks(unsigned long long *out, int clear)
+{
+#ifdef UAVS3E_LAT_STAGE_CLOCKS
+    if (!out) return UC_ERR_ARG;
+    if (cudaMemcpyFromSymbol(out, uc::g_lat_stage_clk, sizeof(uc::g_lat_stage_clk)) != cudaSuccess) return UC_ERR_CUDA;
+    if (clear) {
+        static unsigned long long zero[uc::LAT_SHAPES][uc::LAT_STAGES];
+        if (cudaMemcpyToSymbol(uc::g_lat_stage_clk, zero, sizeof(zero)) != cudaSuccess) return UC_ERR_CUDA;
+    }
+    return UC_OK;
+#else
+    (void)out; (void)clear;
+    return UC_ERR_UNSUPPORTED;
+#endif
+}

@@ -137,7 +137,7 @@ __host__ __device__ inline void lat_layout(int lw, int lh, int nm, int budget, L
 
 struct LatParams {
     const pel *org; int i_org;
-    int org_words;            // org and i_org are multiples of 4 (word loads for word-aligned CUs)
+    int org_words;            // org and i_org are multiples of 4: org blocks are read by words
     const pel *rec; int i_rec;
     int W, H;
     const LatCu *cus;
@@ -323,6 +323,29 @@ __device__ __forceinline__ void lat_satd_tiles(int n_tiles, int lnt, int ntx, co
     }
 }
 
+// Optional per-stage clocks (built with UAVS3E_LAT_STAGE_CLOCKS, off in the library): thread 0
+// of each CTA adds the SM cycles between consecutive CTA barriers of a tile to
+// g_lat_stage_clk[class][stage].  Stages: 0 tables and job setup, 1 org block and neighbours,
+// 2 org row-pass sums and block setup, 3 prediction, 4 SATD and forward row pass, 5 forward
+// column pass, then per QP 6 quantisation, 7 inverse column pass, 8 inverse row pass,
+// reconstruction and SSD, 9 records.
+constexpr int LAT_STAGES = 10;
+#ifdef UAVS3E_LAT_STAGE_CLOCKS
+__device__ unsigned long long g_lat_stage_clk[LAT_SHAPES][LAT_STAGES];
+#define LAT_STAGE_BEGIN() long long lat_clk0 = clock64()
+#define LAT_STAGE(k)                                                                                       \
+    do {                                                                                                  \
+        if (threadIdx.x == 0) {                                                                           \
+            const long long t_ = clock64();                                                               \
+            atomicAdd(&g_lat_stage_clk[(LW - 2) * 5 + (LH - 2)][k], (unsigned long long)(t_ - lat_clk0)); \
+            lat_clk0 = t_;                                                                                \
+        }                                                                                                 \
+    } while (0)
+#else
+#define LAT_STAGE_BEGIN() do { } while (0)
+#define LAT_STAGE(k) do { } while (0)
+#endif
+
 // One tile of shape class (LW, LH): a few whole CUs, or one CU and a chunk of its modes, as the
 // class's layout says.  Called by every thread of the CTA; the tile's data lives in `sm` (the
 // layout's dynamic shared memory) and `S`.
@@ -337,6 +360,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
     int *s_last = S.last;
 
     LatLayout L;
+    LAT_STAGE_BEGIN();
     // compile-time shape: the indices and trip counts below are constants
     lat_layout(LW, LH, P.n_modes, P.budget[(LW - 2) * 5 + (LH - 2)], L);
     const int w = L.w, h = L.h, lw = L.lw, lh = L.lh, kw = L.kw, kh = L.kh, lkw = L.lkw, lkh = L.lkh;
@@ -398,18 +422,19 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         s_mode[j] = P.modes ? P.modes[(size_t)perm[cu0 + g] * P.n_modes + mi] : (u8)mi;
         s_satd[j] = 0; s_flag[j] = 0; s_nz[j] = 0; s_sum[j] = 0; s_hash[j] = 0; s_ssd[j] = 0; s_last[j] = -1;
     }
-    __syncthreads();
+    __syncthreads(); LAT_STAGE(0);
     if (tid == 0) S.tables = cls;   // every thread has read S.tables above
 
     // ---- per CU: org block, neighbours (com_intra_get_nbr with every in-picture sample
     // reconstructed)
-    // four samples per thread: one word load where the picture and the CU's x are word-aligned
+    // four samples per thread (CU x positions are multiples of 4): one word load where the
+    // picture and its pitch are word-aligned
     for (int i = tid; i < Gv * (N >> 2); i += LAT_THREADS) {
         const int g = i >> (lN - 2), p = (i & ((N >> 2) - 1)) << 2;
         const LatCu cu = P.cus[s_cu[g]];
         const pel *src = P.org + (long long)(cu.y + (p >> lw)) * P.i_org + cu.x + (p & (w - 1));
         u32 v;
-        if (P.org_words && !(cu.x & 3)) v = __ldg(reinterpret_cast<const u32 *>(src));
+        if (P.org_words) v = __ldg(reinterpret_cast<const u32 *>(src));
         else v = (u32)src[0] | (u32)src[1] << 8 | (u32)src[2] << 16 | (u32)src[3] << 24;
         *reinterpret_cast<u32 *>(cub + g * L.cu_bytes + L.c_org + (p >> lw) * L.ps + (p & (w - 1))) = v;
     }
@@ -433,7 +458,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
             nbm[0] = c;
         }
     }
-    __syncthreads();
+    __syncthreads(); LAT_STAGE(1);
     if (tid < Gv) {
         const LatCu cu = P.cus[s_cu[tid]];
         const int avail = (cu.y > 0 ? 1 : 0) | (cu.x > 0 ? 2 : 0) | ((cu.x > 0 && cu.y > 0) ? 4 : 0);
@@ -450,7 +475,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         for (int k = 0; k < (w >> 2); k++) acc = dp4a_us(o[k], f[k], acc);
         ((int *)(c + L.c_torg))[y * kw + u] = acc;
     }
-    __syncthreads();
+    __syncthreads(); LAT_STAGE(2);
 
     // job j -> (CU g, mode m): j = g * MCv + (m - m0)
 #define JG(j) ((int)(((u32)(j) * mc_magic) >> 16))
@@ -468,7 +493,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         const int x = p & (w - 1), y = p >> lw;
         JPRED(j)[y * L.ps + x] = (pel)ipred_sample<W_, H_>(cub + g * L.cu_bytes + L.c_nb + 288, sB[g], m, P.ipf, x, y);
     }
-    __syncthreads();
+    __syncthreads(); LAT_STAGE(3);
 
     // ---- SATD (com_had tiling) and forward row pass T[u][y] = (Torg - sum_x Fw pred + rnd) >> sh1
     {
@@ -498,7 +523,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
             }
         }
     }
-    __syncthreads();
+    __syncthreads(); LAT_STAGE(4);
 
     // quantisation parameters per QP
     const int odd = lN & 1, log2_size = lN >> 1;
@@ -544,7 +569,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
             if (fl) atomicOr(&s_flag[j], fl);
         }
     }
-    __syncthreads();
+    __syncthreads(); LAT_STAGE(5);
     for (int j = tid; j < J; j += LAT_THREADS)
         P.satd_out[(size_t)s_cu[JG(j)] * 33 + s_mode[j]] = s_satd[j];
 
@@ -603,7 +628,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
                 }
             }
         }
-        __syncthreads();
+        __syncthreads(); LAT_STAGE(6);
         // inverse column pass T2[y][u] = clip16((sum_v Fh[v][y] DQ[v][u] + 16) >> 5), only
         // for jobs with coded levels; a task forms rows y and H-1-y from the even-v and odd-v
         // sums over CU columns u (T2 rows are stored in even/odd order of u).  Tiles with few
@@ -631,7 +656,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         };
         if (RU > 2 && J * NUC * (H_ / 2) < LAT_THREADS) inv_col(std::integral_constant<int, (RU > 2 ? RU / 2 : RU)>{});
         else inv_col(std::integral_constant<int, RU>{});
-        __syncthreads();
+        __syncthreads(); LAT_STAGE(7);
         // inverse row pass, reconstruction, SSD: a task is the column pair x, W-1-x over CY
         // rows (the even-u and odd-u sums of the T2 row give both); CY = RY / 2 for tiles with
         // few jobs
@@ -674,7 +699,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         };
         if (RY > 2 && J * (W_ / 2) * NYC < LAT_THREADS) inv_row(std::integral_constant<int, (RY > 2 ? RY / 2 : RY)>{});
         else inv_row(std::integral_constant<int, RY>{});
-        __syncthreads();
+        __syncthreads(); LAT_STAGE(8);
         for (int j = tid; j < J; j += LAT_THREADS) {
             const int g = JG(j);
             LatQ o;
@@ -686,7 +711,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
             P.q_out[((size_t)s_cu[g] * 33 + s_mode[j]) * P.n_qp + q] = o;
             s_ssd[j] = 0; s_hash[j] = 0; s_nz[j] = 0; s_last[j] = -1; s_sum[j] = 0;
         }
-        __syncthreads();
+        __syncthreads(); LAT_STAGE(9);
     }
 #undef JG
 #undef JPRED
