@@ -682,33 +682,50 @@ __device__ __forceinline__ void diff_row8(const pel *o, const pel *p, const pel 
 
 // magnitude sum of the 2-D WHT of the 8x8 difference org - pred; with o2/p2 the second 8x8
 // half of a 16x8 / 8x16 tile is folded in as first + sgn * second (the first stage of the
-// 16-point transform).  Rows r and r + 4 travel packed in one register as d[r+4] * 2^16 + d[r]
-// (integer adds and subtracts keep both halves exact: every value stays below 2^15 in
-// magnitude), so the row transforms and the first two column stages run on packed pairs; the
-// last column stage pairs the two halves, where |lo + hi| + |lo - hi| = 2 max(|lo|, |hi|).
+// 16-point transform).  Columns c and c + 2 of a row travel packed in one register as
+// d[c+2] * 2^16 + d[c] (PRMT spreads the two bytes of a word into 16-bit lanes, and one 32-bit
+// subtract of the packed org and prediction gives both differences exactly; every value stays
+// below 2^15 in magnitude, so integer adds and subtracts keep both halves exact).  The WHT's
+// stages commute, so the row stages of distance 1 and 4 and all column stages run on the packed
+// pairs, and the row stage of distance 2 -- the one between the two halves -- is left to the
+// end, where |lo + hi| + |lo - hi| = 2 max(|lo|, |hi|).
 __device__ __noinline__ int satd8x8_raw(const pel *o, int io, const pel *p, int ip, const pel *o2, const pel *p2,
                                            int sgn)
 {
-    int P[4][8];
+    int Q[8][4];
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        int lo[8], hi[8];
-        diff_row8(o + r * io, p + r * ip, o2 ? o2 + r * io : nullptr, p2 ? p2 + r * ip : nullptr, sgn, lo);
-        diff_row8(o + (r + 4) * io, p + (r + 4) * ip, o2 ? o2 + (r + 4) * io : nullptr,
-                  p2 ? p2 + (r + 4) * ip : nullptr, sgn, hi);
-#pragma unroll
-        for (int c = 0; c < 8; c++) P[r][c] = hi[c] * 65536 + lo[c];
-        wht<8>(P[r]);
+    for (int r = 0; r < 8; r++) {
+        u32 ol, oh, pl, ph;
+        load8(o + r * io, ol, oh);
+        load8(p + r * ip, pl, ph);
+        int q0 = (int)(__byte_perm(ol, 0u, 0x4240) - __byte_perm(pl, 0u, 0x4240));   // columns 0, 2
+        int q1 = (int)(__byte_perm(ol, 0u, 0x4341) - __byte_perm(pl, 0u, 0x4341));   // columns 1, 3
+        int q2 = (int)(__byte_perm(oh, 0u, 0x4240) - __byte_perm(ph, 0u, 0x4240));   // columns 4, 6
+        int q3 = (int)(__byte_perm(oh, 0u, 0x4341) - __byte_perm(ph, 0u, 0x4341));   // columns 5, 7
+        if (o2) {
+            load8(o2 + r * io, ol, oh);
+            load8(p2 + r * ip, pl, ph);
+            const int e0 = (int)(__byte_perm(ol, 0u, 0x4240) - __byte_perm(pl, 0u, 0x4240));
+            const int e1 = (int)(__byte_perm(ol, 0u, 0x4341) - __byte_perm(pl, 0u, 0x4341));
+            const int e2 = (int)(__byte_perm(oh, 0u, 0x4240) - __byte_perm(ph, 0u, 0x4240));
+            const int e3 = (int)(__byte_perm(oh, 0u, 0x4341) - __byte_perm(ph, 0u, 0x4341));
+            if (sgn > 0) { q0 += e0; q1 += e1; q2 += e2; q3 += e3; }
+            else { q0 -= e0; q1 -= e1; q2 -= e2; q3 -= e3; }
+        }
+        // row stages of distance 1 (words 0/1, 2/3) and 4 (words 0/2, 1/3)
+        const int a = q0 + q1, b = q0 - q1, c = q2 + q3, d = q2 - q3;
+        Q[r][0] = a + c; Q[r][2] = a - c; Q[r][1] = b + d; Q[r][3] = b - d;
     }
     int s = 0;
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-        const int b0 = P[0][c] + P[1][c], b1 = P[0][c] - P[1][c];
-        const int b2 = P[2][c] + P[3][c], b3 = P[2][c] - P[3][c];
-        const int q[4] = { b0 + b2, b1 + b3, b0 - b2, b1 - b3 };
+    for (int k = 0; k < 4; k++) {
+        int v[8];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int lo = (int)(short)(q[k] & 0xFFFF), hi = (q[k] - lo) >> 16;
+        for (int r = 0; r < 8; r++) v[r] = Q[r][k];
+        wht<8>(v);
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            const int lo = (int)(short)(v[r] & 0xFFFF), hi = (v[r] - lo) >> 16;
             s += max(abs(lo), abs(hi));
         }
     }
