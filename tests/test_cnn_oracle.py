@@ -81,3 +81,48 @@ def test_plain_decisions_quad_tree():
     assert labels[0, 0] == 1 and labels[0, 1:5].all() and labels[0, 5:21].all()
     assert labels[1, 0] == 0
     assert (labels[1, 21:37] == 5).all()
+
+
+def test_bd_rate_of_known_curves():
+    rate = np.array([1000.0, 1800.0, 3100.0, 5200.0])
+    psnr = np.array([31.0, 33.5, 36.0, 38.4])
+    assert abs(cnn.bd_rate(rate, psnr, rate, psnr)) < 1e-9
+    # the same curve at 1.1x the rate everywhere: +10 %; at 0.95x: -5 %
+    assert abs(cnn.bd_rate(rate, psnr, 1.1 * rate, psnr) - 10.0) < 1e-6
+    assert abs(cnn.bd_rate(rate, psnr, 0.95 * rate, psnr) + 5.0) < 1e-6
+    # a curve that needs more PSNR-matched rate is worse (positive)
+    assert cnn.bd_rate(rate, psnr, rate, psnr - 0.5) > 0
+
+
+def test_search_rd_full_and_keep_everything_agree():
+    W, H = 128, 64
+    cus = cnn.square_cus(W, H)
+    rng = np.random.default_rng(3)
+    S = rng.uniform(100, 5000, (len(cus), 33)) * (cus["w"].astype(float)[:, None] / 8) ** 2
+    R = rng.uniform(1, 200, (len(cus), 33))
+    qp = 37
+    J = S + cnn.LAMBDA_QP(qp) * R
+    labels, xy = cnn.plain_decisions(J, cus, W, H, qp)
+    full = cnn.search_rd(J, S, R, cus, xy, None, 0.9, qp)
+    n = len(xy)
+    keep_all = (np.full(n, 0.5), np.full((n, 4), 0.5), np.full((n, 16), 0.5), np.tile(np.arange(8), (n, 16, 1)))
+    same = cnn.search_rd(J, S, R, cus, xy, keep_all, 0.9, qp, shortlist=False)
+    assert np.allclose(full, same)
+    assert abs(full[2] - 1.0) < 1e-12
+    # the chosen decisions' J equals the quad-tree minimum of plain_decisions' recursion
+    jf = full[0] + cnn.LAMBDA_QP(qp) * full[1]
+    idx = {(int(c["x"]), int(c["y"]), int(c["w"])): i for i, c in enumerate(cus)}
+    lam = cnn.LAMBDA_QP(qp)
+
+    def best(x, y, s):
+        own = J[idx[(x, y, s)]].min() + lam
+        if s == 8:
+            return own
+        h = s // 2
+        return min(own, sum(best(x + dx, y + dy, h) for dy in (0, h) for dx in (0, h)) + lam)
+    assert abs(jf - sum(best(int(x), int(y), 64) for x, y in xy)) < 1e-6 * jf
+    # a shortlist that misses the best modes cannot lower the rate-distortion cost
+    worst = (np.full(n, 0.5), np.full((n, 4), 0.5), np.full((n, 16), 0.5),
+             np.tile(np.argsort(-J.mean(0))[:8], (n, 16, 1)))
+    pr = cnn.search_rd(J, S, R, cus, xy, worst, 0.9, qp)
+    assert pr[0] + lam * pr[1] >= jf - 1e-6 * jf and pr[2] < 1.0

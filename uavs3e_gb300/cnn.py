@@ -200,16 +200,23 @@ def square_cus(W, H):
     return c
 
 
-def rd_costs(q, cus, qp, qi=0, n_qp=1):
-    """J = SSD + lambda * R per (CU, mode) from the lattice's first-pass statistics at one QP;
-    R = 1 bit for an all-zero block, else 4 + 1.5 bits per coded level + 1 bit per level unit"""
+def rd_terms(q, cus, qp, qi=0, n_qp=1):
+    """(J, SSD, R) per (CU, mode) from the lattice's first-pass statistics at one QP: J = SSD +
+    lambda R, R = 1 bit for an all-zero block, else 4 + 1.5 bits per coded level + 1 bit per
+    level unit"""
     rec = q.reshape(len(cus), N_MODES, n_qp)[:, :, qi]
     nz = rec["num_nz"].astype(np.float64)
     bits = np.where(nz > 0, 4.0 + 1.5 * nz + rec["sum_abs"].astype(np.float64), 1.0)
-    return rec["ssd"].astype(np.float64) + LAMBDA_QP(qp) * bits
+    ssd = rec["ssd"].astype(np.float64)
+    return ssd + LAMBDA_QP(qp) * bits, ssd, bits
 
 
-def plain_decisions(J, cus, W, H):
+def rd_costs(q, cus, qp, qi=0, n_qp=1):
+    """J = SSD + lambda * R per (CU, mode) (rd_terms)"""
+    return rd_terms(q, cus, qp, qi, n_qp)[0]
+
+
+def plain_decisions(J, cus, W, H, qp=32):
     """quad-tree decisions of the plain path for every full CTU: labels [n_ctu][40] (u8) with
     [0] split64, [1..4] split32 (quadrants raster), [5..20] split16 (cells raster), [21..36] the
     best mode of each 16x16 cell, and the CTU origins [n_ctu][2]"""
@@ -219,7 +226,7 @@ def plain_decisions(J, cus, W, H):
     cw, ch = W // 64, H // 64
     labels = np.zeros((cw * ch, 40), np.uint8)
     xy = np.zeros((cw * ch, 2), np.int32)
-    split_bits = LAMBDA_QP(32) * 1.0
+    split_bits = LAMBDA_QP(qp) * 1.0
 
     def node(x, y, s):
         own = best[idx[(x, y, s)]] + split_bits
@@ -249,33 +256,48 @@ def plain_decisions(J, cus, W, H):
 def frame_dataset(frame, qp=32):
     """labels of the plain path for every full CTU of a frame (GPU lattice on the square CUs,
     org as the reconstructed neighbours) -> (ctus [n][64][64] u8, labels, xy, J, cus)"""
+    d = frame_dataset_qps(frame, (qp,))[qp]
+    return d[0], d[1], d[2], d[3], d[6]
+
+
+def frame_dataset_qps(frame, qps):
+    """frame_dataset at several QPs from one lattice run: {qp: (ctus, labels, xy, J, SSD, R, cus)}"""
     from . import intra_lattice
     H, W = frame.shape
     cus = square_cus(W, H)
-    _, q = intra_lattice(frame, frame, cus, qps=(qp,), ipf=0)
-    J = rd_costs(q, cus, qp)
-    labels, xy = plain_decisions(J, cus, W, H)
-    ctus = np.stack([frame[y:y + 64, x:x + 64] for x, y in xy])
-    return ctus, labels, xy, J, cus
+    _, q = intra_lattice(frame, frame, cus, qps=tuple(qps), ipf=0)
+    out = {}
+    ctus = None
+    for qi, qp in enumerate(qps):
+        J, S, R = rd_terms(q, cus, qp, qi, len(qps))
+        labels, xy = plain_decisions(J, cus, W, H, qp)
+        if ctus is None:
+            ctus = np.stack([frame[y:y + 64, x:x + 64] for x, y in xy])
+        out[qp] = (ctus, labels, xy, J, S, R, cus)
+    return out
 
 
 def host_input(ctus, qp):
-    """network input of CTUs (host): [n][64][64][2] float32, rounded to bf16 on upload"""
+    """network input of CTUs (host): [n][64][64][2] float32, rounded to bf16 on upload; qp is one
+    QP or one per CTU"""
     x = np.empty(ctus.shape + (2,), np.float32)
     x[..., 0] = (ctus.astype(np.float32) - 128.0) / 64.0
-    x[..., 1] = (qp - 32.0) / 8.0
+    q = np.asarray(qp, np.float32)
+    x[..., 1] = ((q.reshape(-1, 1, 1) if q.ndim else q) - 32.0) / 8.0
     return x
 
 
 def train(net, ctus, labels, qp=32, steps=300, lr=2e-3, seed=0):
-    """Adam on random batches of net.B CTUs; returns the loss (sum of the 4 parts) per step"""
+    """Adam on random batches of net.B CTUs (qp: one QP or one per CTU); returns the loss (sum of
+    the 4 parts) per step"""
     import torch
     rng = np.random.default_rng(seed)
     hist = []
     d_lab = torch.empty((net.B, 40), dtype=torch.uint8, device="cuda")
+    qa = np.asarray(qp)
     for _ in range(steps):
         idx = rng.integers(0, len(ctus), net.B)
-        net.acts[0].copy_(torch.from_numpy(host_input(ctus[idx], qp)).to(torch.bfloat16))
+        net.acts[0].copy_(torch.from_numpy(host_input(ctus[idx], qa[idx] if qa.ndim else qa)).to(torch.bfloat16))
         d_lab.copy_(torch.from_numpy(labels[idx]))
         net.forward()
         hist.append(net.backward(d_lab).sum())
@@ -302,6 +324,64 @@ def predict(net, ctus, qp=32):
         p16.append(sig(lg[:, :, 0]))
         top.append(np.argsort(-lg[:, :, 3:36], axis=2)[:, :, :SHORTLIST])
     return np.concatenate(p64), np.concatenate(p32), np.concatenate(p16), np.concatenate(top)
+
+
+def search_rd(J, S, R, cus, xy, pred, tau, qp, shortlist=True):
+    """(total SSD, total bits, fraction of the lattice's work searched) of the quad-tree decisions
+    at one QP: the full search when pred is None, else the pruned search of pruned_search; a CU's
+    own cost counts one flag bit, a split one more"""
+    lam = LAMBDA_QP(qp)
+    idx = {(int(c["x"]), int(c["y"]), int(c["w"])): i for i, c in enumerate(cus)}
+    work = [0.0]
+
+    def own(x, y, s, modes):
+        i = idx[(x, y, s)]
+        row = J[i]
+        work[0] += s * s * (len(modes) if modes is not None else N_MODES)
+        m = int(np.argmin(row)) if modes is None else int(modes[int(np.argmin(row[modes]))])
+        return (row[m] + lam, S[i, m], R[i, m] + 1.0)
+
+    def add(parts):
+        return (sum(p[0] for p in parts) + lam, sum(p[1] for p in parts), sum(p[2] for p in parts) + 1.0)
+
+    def node(x, y, s, b, x0, y0):
+        if pred is None:
+            p, modes = 0.5, None
+        else:
+            p64, p32, p16, top = pred
+            p = (p64[b] if s == 64 else p32[b][((y - y0) // 32) * 2 + (x - x0) // 32] if s == 32
+                 else p16[b][((y - y0) // 16) * 4 + (x - x0) // 16] if s == 16 else 0.0)
+            cell = ((y - y0) // 16) * 4 + (x - x0) // 16
+            modes = top[b][cell] if (shortlist and s <= 16) else None
+        best = None
+        if not p > tau:
+            best = own(x, y, s, modes)
+        if s > 8 and not p < 1 - tau:
+            h = s // 2
+            kids = add([node(x + dx, y + dy, h, b, x0, y0) for dy in (0, h) for dx in (0, h)])
+            if best is None or kids[0] < best[0]:
+                best = kids
+        return best
+
+    ssd = bits = 0.0
+    for b, (x0, y0) in enumerate(xy):
+        r = node(int(x0), int(y0), 64, b, int(x0), int(y0))
+        ssd += r[1]
+        bits += r[2]
+    return ssd, bits, work[0] / (len(xy) * 4 * 64 * 64 * N_MODES)
+
+
+def bd_rate(rate_a, psnr_a, rate_b, psnr_b):
+    """Bjontegaard delta rate (VCEG-M33) of curve b against curve a, in percent: the log rate of
+    each curve as a cubic polynomial in PSNR, integrated over the PSNR interval both cover; the
+    mean log-rate difference d gives (e^d - 1) * 100"""
+    la, lb = np.log(np.asarray(rate_a, np.float64)), np.log(np.asarray(rate_b, np.float64))
+    pa, pb = np.asarray(psnr_a, np.float64), np.asarray(psnr_b, np.float64)
+    ca, cb = np.polyfit(pa, la, 3), np.polyfit(pb, lb, 3)
+    lo, hi = max(pa.min(), pb.min()), min(pa.max(), pb.max())
+    ia, ib = np.polyint(ca), np.polyint(cb)
+    d = ((np.polyval(ib, hi) - np.polyval(ib, lo)) - (np.polyval(ia, hi) - np.polyval(ia, lo))) / (hi - lo)
+    return float((np.exp(d) - 1.0) * 100.0)
 
 
 def pruned_search(J, cus, xy, pred, tau, shortlist=True):
@@ -443,36 +523,43 @@ def pruned_lattice_ms(frame, cus, xy, pred, tau, qp=32):
 
 
 def experiment(train_seeds=range(100, 116), test_seeds=(900,), qp=32, steps=3000, batch=128, taus=(0.8, 0.9),
-               seed=0, width=1920, height=1080):
-    """train on the plain path's decisions over synthetic 1080p I-frames, evaluate on held-out
-    frames against the method without the network; one dict of results"""
+               seed=0, width=1920, height=1080, qps=(27, 32, 37, 42)):
+    """train on the plain path's decisions over synthetic 1080p I-frames at every QP of qps,
+    evaluate on held-out frames against the method without the network: at QP qp (accuracy,
+    RD-cost increase, work), and over qps as a Bjontegaard delta rate of the pruned search
+    against the full one; one dict of results"""
     import time
     import torch
     from .synth import intra_frame
     t0 = time.perf_counter()
-    tr = [frame_dataset(intra_frame(width, height, seed=s), qp) for s in train_seeds]
+    tr = [frame_dataset_qps(intra_frame(width, height, seed=s), qps) for s in train_seeds]
     te_frames = [intra_frame(width, height, seed=s) for s in test_seeds]
-    te = [frame_dataset(f, qp) for f in te_frames]
+    te_all = [frame_dataset_qps(f, qps) for f in te_frames]
+    te = [d[qp] for d in te_all]
     t_label = time.perf_counter() - t0
-    ctus = np.concatenate([d[0] for d in tr])
-    labels = np.concatenate([d[1] for d in tr])
+    ctus = np.concatenate([d[q][0] for d in tr for q in qps])
+    labels = np.concatenate([d[q][1] for d in tr for q in qps])
+    qarr = np.concatenate([np.full(len(d[q][0]), q, np.int32) for d in tr for q in qps])
+    labels_at = {q: np.concatenate([d[q][1] for d in tr]) for q in qps}
     net = PruneNet(batch, seed=seed)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    hist = train(net, ctus, labels, qp=qp, steps=steps, seed=seed)
+    hist = train(net, ctus, labels, qp=qarr, steps=steps, seed=seed)
     e1.record()
     torch.cuda.synchronize()
     train_ms = e0.elapsed_time(e1) / steps
-    out = {"train_ctus": int(len(ctus)), "test_ctus": int(sum(len(d[0]) for d in te)), "steps": steps, "batch": batch,
-           "label_rates": {"split64": float(labels[:, 0].mean()), "split32": float(labels[:, 1:5].mean()),
-                           "split16": float(labels[:, 5:21].mean()),
-                           "mode_top8_share": float(np.sort(np.bincount(labels[:, 21:37].ravel(), minlength=N_MODES))[::-1][:SHORTLIST].sum() / labels[:, 21:37].size)},
+    lq = labels_at[qp]
+    out = {"train_ctus": int(len(ctus)), "train_qps": list(qps), "test_ctus": int(sum(len(d[0]) for d in te)),
+           "steps": steps, "batch": batch,
+           "label_rates": {"split64": float(lq[:, 0].mean()), "split32": float(lq[:, 1:5].mean()),
+                           "split16": float(lq[:, 5:21].mean()),
+                           "mode_top8_share": float(np.sort(np.bincount(lq[:, 21:37].ravel(), minlength=N_MODES))[::-1][:SHORTLIST].sum() / lq[:, 21:37].size)},
            "train_ms_per_step": train_ms, "label_s": t_label, "loss_first": hist[0], "loss_last": float(np.mean(hist[-20:]))}
-    # accuracy against the held-out plain decisions
+    # accuracy against the held-out plain decisions at QP qp
     te_ctus = np.concatenate([d[0] for d in te])
     te_labels = np.concatenate([d[1] for d in te])
     pred = predict(net, te_ctus, qp)
-    prior = prior_predictions(labels, len(te_ctus))
+    prior = prior_predictions(lq, len(te_ctus))
     for name, p in (("net", pred), ("prior", prior)):
         p64, p32, p16, top = p
         out[name] = {
@@ -481,17 +568,49 @@ def experiment(train_seeds=range(100, 116), test_seeds=(900,), qp=32, steps=3000
             "split16_acc": float(((p16 > 0.5) == te_labels[:, 5:21].astype(bool)).mean()),
             "mode_top8_recall": float((top == te_labels[:, 21:37, None]).any(2).mean()),
         }
-    # pruned search on the held-out frames: RD-cost increase and work kept, per threshold
+    # pruned search on the held-out frames at QP qp: RD-cost increase and work kept, per threshold
     for tau in taus:
         for name, p in (("net", pred), ("prior", prior)):
             dj, wk, off = [], [], 0
             for d in te:
                 n = len(d[0])
                 sub = tuple(a[off:off + n] for a in p)
-                r = pruned_search(d[3], d[4], d[2], sub, tau)
+                r = pruned_search(d[3], d[6], d[2], sub, tau)
                 dj.append(r[0]); wk.append(r[1])
                 off += n
             out[name][f"tau{tau}"] = {"rd_cost_increase": float(np.mean(dj)), "work_fraction": float(np.mean(wk))}
+    # over the QPs: rate (bits of the RD model) and PSNR-Y (SSD of the decisions) of the full and
+    # the pruned searches on the held-out frames, and the Bjontegaard delta rates
+    n_pix = float(sum(len(d[0]) for d in te)) * 64 * 64
+    curves = {"full": {"rate": [], "psnr": [], "work": []}}
+    for tau in taus:
+        curves[f"net_tau{tau}"] = {"rate": [], "psnr": [], "work": []}
+        curves[f"prior_tau{tau}"] = {"rate": [], "psnr": [], "work": []}
+    for q in qps:
+        preds = {"net": predict(net, np.concatenate([d[q][0] for d in te_all]), q),
+                 "prior": prior_predictions(labels_at[q], sum(len(d[q][0]) for d in te_all))}
+        runs = [("full", None, 0.9)] + [(f"{m}_tau{tau}", m, tau) for tau in taus for m in ("net", "prior")]
+        for key, m, tau in runs:
+            ssd = bits = work = 0.0
+            off = 0
+            for d in te_all:
+                c, _, xy, J, S, R, cus = d[q]
+                n = len(c)
+                p = None if m is None else tuple(a[off:off + n] for a in preds[m])
+                off += n
+                r = search_rd(J, S, R, cus, xy, p, tau, q)
+                ssd += r[0]; bits += r[1]; work += r[2] / len(te_all)
+            curves[key]["rate"].append(bits)
+            curves[key]["psnr"].append(10.0 * np.log10(255.0 ** 2 * n_pix / max(ssd, 1.0)))
+            curves[key]["work"].append(work)
+    out["bd_rate"] = {"qps": list(qps), "model": "rate = the RD model's bits (coded levels, all-zero and split "
+                                                  "flags), PSNR-Y of the CTUs' reconstruction by the chosen CUs/modes",
+                      "curves": curves}
+    for key in curves:
+        if key != "full":
+            out["bd_rate"][key] = {"bd_rate_pct": bd_rate(curves["full"]["rate"], curves["full"]["psnr"],
+                                                          curves[key]["rate"], curves[key]["psnr"]),
+                                   "mean_work_fraction": float(np.mean(curves[key]["work"]))}
     # GPU time: inference of a frame's CTUs, and the lattice over all square CUs vs the kept ones
     f0, d0 = te_frames[0], te[0]
     infer = PruneNet(len(d0[0]), params=net.params())
@@ -504,12 +623,12 @@ def experiment(train_seeds=range(100, 116), test_seeds=(900,), qp=32, steps=3000
     e1.record()
     torch.cuda.synchronize()
     out["inference_ms_per_frame"] = e0.elapsed_time(e1) / 5
-    full_ms = lattice_ms(f0, d0[4], qp)
+    full_ms = lattice_ms(f0, d0[6], qp)
     n0 = len(d0[0])
     out["lattice_square_cus_ms"] = full_ms
-    out["square_cus"] = int(len(d0[4]))
+    out["square_cus"] = int(len(d0[6]))
     for tau in taus:
-        ms, nk = pruned_lattice_ms(f0, d0[4], d0[2], tuple(a[:n0] for a in pred), tau, qp)
+        ms, nk = pruned_lattice_ms(f0, d0[6], d0[2], tuple(a[:n0] for a in pred), tau, qp)
         out[f"pruned_lattice_tau{tau}"] = {"ms": ms, "kept_cus": int(nk), "speedup": full_ms / ms if ms else None}
     return out
 
