@@ -1142,14 +1142,15 @@ def run_ours(args):
     avg_int_ms = ms_int / max(1, prof_steps)                   # both integer-search launches of a step
     alg_ops = N_REFS * W * H * n_cand / 4.0
     achieved = alg_ops / (avg_int_ms / 1000.0) / 1e9
-    # DRAM traffic of the two integer-search launches of one frame (interior 7.87 MB + edge
-    # 2.55 MB read, nothing written back), from the ncu capture summarised in
-    # profiles/me_kernels_1080p_full.md
-    traffic = 7.87e6 + 2.55e6
+    # DRAM traffic of the two integer-search launches of one frame: the ncu capture of the interior
+    # launch (3,480 CTAs) read 21.9 MB and wrote nothing; the edge launch (600 CTAs of the same
+    # window size) is counted in proportion to its CTAs
+    traffic = 21.9e6 * 4080.0 / 3480.0
     roofline = {"bound": "int", "kernel": "k_me_int (integer full search, both launches of a frame)",
                 "achieved": achieved, "peak": int_peak, "unit": "Gop/s", "frac": achieved / int_peak,
                 "traffic": traffic,
-                "traffic_note": "DRAM bytes per frame (both launches) from ncu; algorithmic ops, not bytes, bind",
+                "traffic_note": "DRAM bytes per frame (both launches): the interior launch's ncu capture scaled "
+                                "by CTAs to both; algorithmic ops, not bytes, bind",
                 "peak_source": f"vabsdiff4.add issue rate max(measured {per_clk_sm:.1f}, 64) ops/clk/SM x {sm_count} "
                                f"SMs x {sm_mhz:.0f} MHz max SM clock (MEASURED_PEAKS.json has no integer peak)",
                 "ops_per_launch": alg_ops, "avg_launch_ms": avg_int_ms,
