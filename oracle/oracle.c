@@ -2597,3 +2597,268 @@ int orc_affine_mvp(s64 ptr, const s64 *ref_ptr, int n_ref, const s16 *map_mv, co
     }
     return bad;
 }
+
+/* ======================================================================================
+ * Affine merge candidates -- com_get_affine_merge_candidate, src/com_util.c:1761-1981
+ * ====================================================================================== */
+
+/* com_mv_rounding_s32 with right shift 7, no left shift: the magnitude rounded, the sign kept */
+static s32 affmrg_round7(s32 v)
+{
+    return v >= 0 ? (s32)(((u32)v + 64u) >> 7) : -(s32)(((u32)(-(s64)v) + 64u) >> 7);
+}
+
+static s32 affmrg_clip18(s32 v)
+{
+    return v < -131072 ? -131072 : v > 131071 ? 131071 : v;
+}
+
+/* scaling_mv1: the MV scaled by (2^14 / t_neb) * t_cur with symmetric rounding and an s16 clip */
+static int affmrg_scale(s64 ptr_cur, s64 ptr_cur_ref, s64 ptr_neb, s64 ptr_neb_ref, const s16 mv[2], s16 out[2])
+{
+    const int t0 = (int)(ptr_neb * 2 - ptr_neb_ref * 2), t1 = (int)(ptr_cur * 2 - ptr_cur_ref * 2);
+    if (t0 == 0 || t1 == 0) return 1;
+    const int ratio = (1 << 14) / t0 * t1;
+    for (int d = 0; d < 2; d++) {
+        const s64 t = (s64)mv[d] * ratio;
+        s64 r = t == 0 ? 0 : t > 0 ? (t + 8192) >> 14 : -((-t + 8192) >> 14);
+        if (r < -32768) r = -32768;
+        if (r > 32767) r = 32767;
+        out[d] = (s16)r;
+    }
+    return 0;
+}
+
+/* the fields of one request, with bounds-checked reads (relative to SCU (0, 0)) */
+typedef struct {
+    const orc_affmrg_pic_t *P;
+    const s16 *mv; const s8 *refi; const u8 *scu; const u32 *pos; const s16 *col_mv; const s8 *col_refi;
+    long long origin, nf;
+    int bad;
+} affmrg_ctx_t;
+
+static int affmrg_in(affmrg_ctx_t *c, long long a)
+{
+    if (a + c->origin < 0 || a + c->origin >= c->nf) { c->bad = 1; return 0; }
+    return 1;
+}
+#define AM_SCU(c, a) (affmrg_in(c, a) ? (c)->scu[(a) + (c)->origin] : 0)
+#define AM_POS(c, a) (affmrg_in(c, a) ? (c)->pos[(a) + (c)->origin] : 0u)
+#define AM_REFI(c, a, l) (affmrg_in(c, a) ? (c)->refi[((a) + (c)->origin) * 2 + (l)] : -1)
+#define AM_MV(c, a, l, d) (affmrg_in(c, a) ? (c)->mv[(((a) + (c)->origin) * 2 + (l)) * 2 + (d)] : 0)
+
+/* com_derive_affine_model_mv: the CU's control points from the affine neighbour covering scun */
+static void affmrg_model_mv(affmrg_ctx_t *c, int scup, int scun, int lidx, int cw, int ch, s32 mvp[3][2], int *vn)
+{
+    const int i_scu = c->P->i_scu;
+    const u32 pos = AM_POS(c, scun);
+    const int lw = (int)(pos & 7), lh = (int)((pos >> 3) & 7), nw = 1 << lw, nh = 1 << lh;
+    const int diff_w = 7 - lw, diff_h = 7 - lh;
+    const int a0 = (int)(pos >> 6), a1 = a0 + ((nw >> 2) - 1), a2 = a0 + ((nh >> 2) - 1) * i_scu, a3 = a2 + ((nw >> 2) - 1);
+    int neb_x = (a0 % i_scu) << 2, neb_y = (a0 / i_scu) << 2;
+    const int cur_x = (scup % i_scu) << 2, cur_y = (scup / i_scu) << 2;
+    const int ad[4] = { a0, a1, a2, a3 };
+    s32 nm[4][2];
+    for (int i = 0; i < 4; i++)
+        for (int d = 0; d < 2; d++) nm[i][d] = AM_MV(c, ad[i], lidx, d);
+    int top = 0;
+    if ((neb_y + nh) % (1 << c->P->log2_max_cuwh) == 0 && neb_y + nh == cur_y) {
+        top = 1;
+        neb_y += nh;
+        nm[0][0] = nm[2][0]; nm[0][1] = nm[2][1];
+        nm[1][0] = nm[3][0]; nm[1][1] = nm[3][1];
+    }
+    const s32 dhx = (s32)((u32)(nm[1][0] - nm[0][0]) << diff_w), dhy = (s32)((u32)(nm[1][1] - nm[0][1]) << diff_w);
+    s32 dvx, dvy;
+    if (*vn == 3 && !top) {
+        dvx = (s32)((u32)(nm[2][0] - nm[0][0]) << diff_h);
+        dvy = (s32)((u32)(nm[2][1] - nm[0][1]) << diff_h);
+    } else {
+        dvx = -dhy;
+        dvy = dhx;
+        *vn = 2;
+    }
+    const s32 hb = (s32)((u32)nm[0][0] << 7), vb = (s32)((u32)nm[0][1] << 7);
+    for (int k = 0; k < *vn; k++) {
+        const int ox = cur_x - neb_x + (k == 1 ? cw : 0), oy = cur_y - neb_y + (k == 2 ? ch : 0);
+        const s32 th = (s32)((u32)dhx * (u32)ox + (u32)dvx * (u32)oy + (u32)hb);
+        const s32 tv = (s32)((u32)dhy * (u32)ox + (u32)dvy * (u32)oy + (u32)vb);
+        mvp[k][0] = affmrg_clip18((s32)((u32)affmrg_round7(th) << 2));
+        mvp[k][1] = affmrg_clip18((s32)((u32)affmrg_round7(tv) << 2));
+    }
+}
+
+/* com_derive_affine_constructed_candidate for one model (cp_idx[0..ver-1]) */
+static void affmrg_constructed(orc_affmrg_out_t *o, int *cnt, int cw, int ch, const int valid[4], const s16 cmv[2][4][2],
+                               const int crefi[2][4], const int *cp_idx, int model, int ver)
+{
+    if (*cnt >= 5) return;
+    for (int i = 0; i < ver; i++)
+        if (!valid[cp_idx[i]]) return;
+    int vm[2] = { 0, 0 };
+    for (int l = 0; l < 2; l++) {
+        int ok = 1;
+        for (int i = 0; i < ver; i++)
+            if (crefi[l][cp_idx[i]] < 0 || crefi[l][cp_idx[i]] != crefi[l][cp_idx[0]]) ok = 0;
+        vm[l] = ok;
+    }
+    if (!vm[0] && !vm[1]) return;
+    const int k = *cnt;
+    o->cp_num[k] = (s8)ver;
+    const int lw = cw == 16 ? 4 : cw == 32 ? 5 : cw == 64 ? 6 : 7, lh = ch == 16 ? 4 : ch == 32 ? 5 : ch == 64 ? 6 : 7;
+    const int sh = 7 + lw - lh;
+    for (int l = 0; l < 2; l++) {
+        if (!vm[l]) {
+            o->refi[k][l] = -1;
+            for (int i = 0; i < ver; i++) o->cpmv[k][l][i][0] = o->cpmv[k][l][i][1] = 0;
+            continue;
+        }
+        s32 t[4][2] = { { 0, 0 }, { 0, 0 }, { 0, 0 }, { 0, 0 } };
+        for (int i = 0; i < ver; i++) { t[cp_idx[i]][0] = cmv[l][cp_idx[i]][0]; t[cp_idx[i]][1] = cmv[l][cp_idx[i]][1]; }
+        for (int d = 0; d < 2; d++) {
+            if (model == 1) t[2][d] = t[3][d] + t[0][d] - t[1][d];
+            if (model == 2) t[1][d] = t[3][d] + t[0][d] - t[2][d];
+            if (model == 3) t[0][d] = t[1][d] + t[2][d] - t[3][d];
+        }
+        if (model == 5) {
+            const s32 th = (s32)(((u32)(t[2][1] - t[0][1]) << sh) + ((u32)t[0][0] << 7));
+            const s32 tv = (s32)((u32)(-(s32)((u32)(t[2][0] - t[0][0]) << sh)) + ((u32)t[0][1] << 7));
+            t[1][0] = affmrg_round7(th);
+            t[1][1] = affmrg_round7(tv);
+        }
+        o->refi[k][l] = (s8)crefi[l][cp_idx[0]];
+        for (int i = 0; i < ver; i++)
+            for (int d = 0; d < 2; d++) o->cpmv[k][l][i][d] = affmrg_clip18((s32)((u32)t[i][d] << 2));
+    }
+    (*cnt)++;
+}
+
+static int affmrg_one(const orc_affmrg_pic_t *P, affmrg_ctx_t *c, const orc_affmrg_req_t *q, orc_affmrg_out_t *o)
+{
+    const int cw = q->cu_width, ch = q->cu_height;
+    if ((cw != 16 && cw != 32 && cw != 64 && cw != 128) || (ch != 16 && ch != 32 && ch != 64 && ch != 128)) return 1;
+    const int i_scu = P->i_scu, scup = q->scup, wsc = cw >> 2, hsc = ch >> 2;
+    c->bad = 0;
+    int cnt = 0;
+    /* model-based: F, G, C, A, D; the first two affine neighbours of distinct CUs */
+    {
+        const int nb[5] = { scup + i_scu * (hsc - 1) - 1, scup - i_scu + wsc - 1, scup - i_scu + wsc, scup - 1,
+                            scup - i_scu - 1 };
+        int valid[5], tl[5] = { 0, 0, 0, 0, 0 };
+        for (int k = 0; k < 5; k++) {
+            valid[k] = (AM_SCU(c, nb[k]) >> 4) & 3;
+            if (valid[k]) tl[k] = (int)(AM_POS(c, nb[k]) >> 6);
+        }
+        if (valid[2] && valid[1] && tl[1] == tl[2]) valid[2] = 0;
+        const int v3 = valid[3];
+        if (valid[3] && valid[0] && tl[0] == tl[3]) valid[3] = 0;
+        if ((valid[4] && v3 && tl[4] == tl[3]) || (valid[4] && valid[1] && tl[4] == tl[1])) valid[4] = 0;
+        for (int k = 0; k < 5; k++) {
+            if (valid[k]) {
+                int vn = ((AM_SCU(c, nb[k]) >> 4) & 3) == 1 ? 2 : 3;
+                for (int l = 0; l < 2; l++) {
+                    const int r = AM_REFI(c, nb[k], l);
+                    if (r >= 0) {
+                        o->refi[cnt][l] = (s8)r;
+                        affmrg_model_mv(c, scup, nb[k], l, cw, ch, o->cpmv[cnt][l], &vn);
+                    } else {
+                        o->refi[cnt][l] = -1;
+                        memset(o->cpmv[cnt][l], 0, sizeof(o->cpmv[cnt][l]));
+                    }
+                }
+                o->cp_num[cnt] = (s8)vn;
+                cnt++;
+            }
+            if (cnt >= 2) break;
+        }
+    }
+    /* control points: LT from A, B, D; RT from G, C; LB from F (the first inter SCU); RB from
+     * the colocated picture at the bottom-right SCU's colocated position, scaled */
+    {
+        s16 cmv[2][4][2];
+        int crefi[2][4], valid[4] = { 0, 0, 0, 0 };
+        memset(cmv, 0, sizeof(cmv));
+        for (int l = 0; l < 2; l++)
+            for (int i = 0; i < 4; i++) crefi[l][i] = -1;
+        const int lt[3] = { scup - 1, scup - i_scu, scup - i_scu - 1 }, rt[2] = { scup - i_scu + wsc - 1, scup - i_scu + wsc };
+        const int lb = scup + i_scu * (hsc - 1) - 1;
+        for (int g = 0; g < 3; g++) {
+            const int n = g == 0 ? 3 : g == 1 ? 2 : 1;
+            for (int k = 0; k < n; k++) {
+                const int a = g == 0 ? lt[k] : g == 1 ? rt[k] : lb;
+                if ((AM_SCU(c, a) & 3) != 1) continue;
+                for (int l = 0; l < 2; l++) {
+                    crefi[l][g] = AM_REFI(c, a, l);
+                    cmv[l][g][0] = (s16)AM_MV(c, a, l, 0);
+                    cmv[l][g][1] = (s16)AM_MV(c, a, l, 1);
+                }
+                valid[g] = 1;
+                break;
+            }
+        }
+        const int rb = scup + i_scu * (hsc - 1) + (wsc - 1);
+        /* get_colocal_scup */
+        const int bx = rb % i_scu, by = rb / i_scu;
+        int xpos = (bx & ~3) + 2, ypos = (by & ~3) + 2;
+        if (ypos >= P->pic_height_in_scu) ypos = ((by & ~3) + P->pic_height_in_scu) >> 1;
+        if (xpos >= P->pic_width_in_scu) xpos = ((bx & ~3) + P->pic_width_in_scu) >> 1;
+        const long long co = (long long)ypos * i_scu + xpos;
+        if (co + c->origin < 0 || co + c->origin >= c->nf) return 1;
+        const int cr = c->col_refi[(co + c->origin) * 2 + 0];
+        const s16 cm[2] = { c->col_mv[((co + c->origin) * 2 + 0) * 2 + 0], c->col_mv[((co + c->origin) * 2 + 0) * 2 + 1] };
+        if (cr >= 17) return 1;
+        if (P->slice_type == 3) {
+            if (cr >= 0) {
+                s16 m[2];
+                for (int l = 0; l < 2; l++) {
+                    if (affmrg_scale(P->ptr, P->ref0_ptr[l], P->ref0_ptr[1], P->col_list_ptr[cr], cm, m)) return 1;
+                    crefi[l][3] = 0;
+                    cmv[l][3][0] = m[0]; cmv[l][3][1] = m[1];
+                }
+                valid[3] = 1;
+            }
+        } else if (cr >= 0) {
+            s16 m[2];
+            if (affmrg_scale(P->ptr, P->ref0_ptr[0], P->ref0_ptr[0], P->col_list_ptr[cr], cm, m)) return 1;
+            crefi[0][3] = 0;
+            cmv[0][3][0] = m[0]; cmv[0][3][1] = m[1];
+            crefi[1][3] = -1;
+            cmv[1][3][0] = cmv[1][3][1] = 0;
+            valid[3] = 1;
+        }
+        static const int models[6][3] = { { 0, 1, 2 }, { 0, 1, 3 }, { 0, 2, 3 }, { 1, 2, 3 }, { 0, 1, 0 }, { 0, 2, 0 } };
+        static const int vers[6] = { 3, 3, 3, 3, 2, 2 };
+        for (int m = 0; m < 6; m++) affmrg_constructed(o, &cnt, cw, ch, valid, cmv, crefi, models[m], m, vers[m]);
+    }
+    o->num = cnt;
+    for (int k = cnt; k < 5; k++) {
+        o->cp_num[k] = 2;
+        memset(o->cpmv[k], 0, sizeof(o->cpmv[k]));
+        o->refi[k][0] = 0;
+        o->refi[k][1] = -1;
+    }
+    /* vertices past a candidate's control-point count carry nothing */
+    for (int k = 0; k < 5; k++)
+        for (int l = 0; l < 2; l++)
+            for (int i = o->cp_num[k]; i < 3; i++) o->cpmv[k][l][i][0] = o->cpmv[k][l][i][1] = 0;
+    return c->bad;
+}
+
+int orc_affine_merge(const orc_affmrg_pic_t *pic, const s16 *map_mv, const s8 *map_refi, const u8 *map_scu,
+                     const u32 *map_pos, const s16 *col_mv, const s8 *col_refi, const orc_affmrg_req_t *reqs, int n,
+                     orc_affmrg_out_t *out)
+{
+    affmrg_ctx_t c;
+    c.P = pic; c.mv = map_mv; c.refi = map_refi; c.scu = map_scu; c.pos = map_pos; c.col_mv = col_mv; c.col_refi = col_refi;
+    c.origin = pic->i_scu + 1;
+    c.nf = (long long)pic->rows * pic->i_scu;
+    int bad = 0;
+    for (int i = 0; i < n; i++) {
+        memset(&out[i], 0, sizeof(out[i]));
+        if (affmrg_one(pic, &c, &reqs[i], &out[i])) {
+            memset(&out[i], 0, sizeof(out[i]));
+            bad++;
+        }
+    }
+    return bad;
+}

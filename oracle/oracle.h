@@ -398,6 +398,43 @@ typedef struct {
 int orc_affine_mvp(s64 ptr, const s64 *ref_ptr, int n_ref, const s16 *map_mv, const s8 *map_refi, int i_scu,
                    int rows, const orc_affmvp_req_t *reqs, int n, orc_affmvp_out_t *out);
 
+/* Affine merge candidates (com_get_affine_merge_candidate, src/com_util.c:1761-1981, with
+ * com_derive_affine_model_mv :1566-1654, com_derive_affine_constructed_candidate :1656-1758,
+ * get_colocal_scup :303, get_col_mv / get_col_mv_from_list0 :977-1000, scaling_mv1 :322).  The
+ * picture's maps have the reference's layout (stride i_scu = pic_width_in_scu + 2, SCU (0, 0) at
+ * index i_scu + 1): map_mv s16 [rows * i_scu][2][2], map_refi s8 [rows * i_scu][2], map_scu u8
+ * (com_scu_t: bit 0 coded, bit 1 intra, bits 4-5 affine), map_pos u32 (top-left SCU << 6 |
+ * log2 h << 3 | log2 w of the CU covering the SCU); col_mv / col_refi are the colocated picture's
+ * maps in the same layout (refp[0][REFP_1] in B slices, refp[0][REFP_0] otherwise). */
+typedef struct {
+    s64 ptr;                 /* POC of the current picture                                        */
+    s64 ref0_ptr[2];         /* POC of refp[0][REFP_0] and refp[0][REFP_1]                         */
+    s64 col_list_ptr[17];    /* the colocated picture's list_ptr (POC of its list-0 references)    */
+    s32 i_scu, pic_width_in_scu, pic_height_in_scu, rows;
+    s32 slice_type;          /* 3 = SLICE_B, else the P rule                                      */
+    s32 log2_max_cuwh;
+} orc_affmrg_pic_t;
+
+typedef struct {
+    s32 scup;                /* y_scu * i_scu + x_scu of the CU's top-left SCU                     */
+    s16 cu_width, cu_height; /* luma samples, powers of two 16..128                                */
+} orc_affmrg_req_t;
+
+typedef struct {
+    s32 num;                 /* candidates derived (the list is zero-padded to 5)                  */
+    s8 cp_num[5];            /* control points of each candidate (2 or 3)                          */
+    s8 refi[5][2];           /* reference index per list, -1 unused                                */
+    s8 pad;
+    s32 cpmv[5][2][3][2];    /* control-point MVs (1/16 samples); vertices past cp_num are 0       */
+} orc_affmrg_out_t;
+
+/* Returns the number of requests outside the domain (a map read outside the field, sizes not
+ * powers of two in 16..128, a colocated reference index outside col_list_ptr, a zero POC
+ * distance); their output is zero. */
+int orc_affine_merge(const orc_affmrg_pic_t *pic, const s16 *map_mv, const s8 *map_refi, const u8 *map_scu,
+                     const u32 *map_pos, const s16 *col_mv, const s8 *col_refi, const orc_affmrg_req_t *reqs, int n,
+                     orc_affmrg_out_t *out);
+
 /* the picture-level results from the records (src/lookahead.c:255-292): returns the picture
  * SATD cost; icost, icost_uv[2], map_dqp[units] are filled when non-NULL */
 double orc_loka_finish(const orc_loka_cfg_t *cfg, const orc_loka_unit_t *units, double *icost, double *icost_uv,

@@ -249,6 +249,20 @@ class Oracle(_Common):
                                     i_scu, rows, ptr(reqs), len(reqs), ptr(out))
         return out, bad
 
+    def affine_merge(self, pic, map_mv, map_refi, map_scu, map_pos, col_mv, col_refi, reqs):
+        """com_get_affine_merge_candidate for every AFFMRG_REQ: pic an AFFMRG_PIC record, the maps in
+        the reference's layout (SCU (0, 0) at index i_scu + 1): map_mv / col_mv int16 [rows * i_scu, 2,
+        2], map_refi / col_refi int8 [rows * i_scu, 2], map_scu uint8, map_pos uint32 [rows * i_scu].
+        Returns (out, number of requests outside the domain)"""
+        pic = np.ascontiguousarray(pic, dtype=AFFMRG_PIC).reshape(1)
+        arrs = [np.ascontiguousarray(a, dtype=t) for a, t in ((map_mv, np.int16), (map_refi, np.int8),
+                                                               (map_scu, np.uint8), (map_pos, np.uint32),
+                                                               (col_mv, np.int16), (col_refi, np.int8))]
+        reqs = np.ascontiguousarray(reqs, dtype=AFFMRG_REQ)
+        out = np.zeros(len(reqs), dtype=AFFMRG_OUT)
+        bad = self.L.orc_affine_merge(ptr(pic), *[ptr(a) for a in arrs], ptr(reqs), len(reqs), ptr(out))
+        return out, bad
+
     def coef_rate(self, levels, reqs):
         """lbac_enc_run_length_cc_rdo for every COEF_RATE_REQ on levels (int16)"""
         levels = np.ascontiguousarray(levels, dtype=np.int16)
@@ -479,6 +493,39 @@ class RefLib(_Common):
                                    C.c_void_p(out.ctypes.data + i * AFFMVP_OUT.itemsize))
         return out
 
+    def affine_merge(self, pic, map_mv, map_refi, map_scu, map_pos, col_mv, col_refi, reqs):
+        """the reference's com_get_affine_merge_candidate, one CU per request (requests in the domain)"""
+        pic = np.ascontiguousarray(pic, dtype=AFFMRG_PIC).reshape(1)[0]
+        i_scu = int(pic["i_scu"])
+        org = i_scu + 1
+        mv = np.ascontiguousarray(map_mv, dtype=np.int16)
+        refi = np.ascontiguousarray(map_refi, dtype=np.int8)
+        scu = np.ascontiguousarray(map_scu, dtype=np.uint8)
+        pos = np.ascontiguousarray(map_pos, dtype=np.uint32)
+        cmv = np.ascontiguousarray(col_mv, dtype=np.int16)
+        crefi = np.ascontiguousarray(col_refi, dtype=np.int8)
+        ref0 = np.ascontiguousarray(pic["ref0_ptr"], dtype=np.int64)
+        clist = np.ascontiguousarray(pic["col_list_ptr"], dtype=np.int64)
+        reqs = np.ascontiguousarray(reqs, dtype=AFFMRG_REQ)
+        out = np.zeros(len(reqs), dtype=AFFMRG_OUT)
+        at = lambda a, b: C.c_void_p(a.ctypes.data + org * b)  # noqa: E731
+        num = C.c_int32()
+        for i, q in enumerate(reqs):
+            o = out[i:i + 1]
+            cp = np.zeros(5, np.int8)
+            rf = np.zeros((5, 2), np.int8)
+            mvs = np.zeros((5, 2, 3, 2), np.int32)
+            self.L.refk_affine_merge(C.c_int64(int(pic["ptr"])), ptr(ref0), ptr(clist), at(mv, 8), at(refi, 2),
+                                     at(scu, 1), at(pos, 4), at(cmv, 8), at(crefi, 2), i_scu,
+                                     int(pic["pic_width_in_scu"]), int(pic["pic_height_in_scu"]),
+                                     int(pic["slice_type"]), int(pic["log2_max_cuwh"]), int(q["scup"]),
+                                     int(q["cu_width"]), int(q["cu_height"]), C.byref(num), ptr(cp), ptr(rf), ptr(mvs))
+            o["num"] = num.value
+            o["cp_num"] = cp
+            o["refi"] = rf
+            o["cpmv"] = mvs
+        return out
+
     def coef_rate(self, levels, reqs):
         """the reference's lbac_enc_run_length_cc_rdo, one block per request"""
         levels = np.ascontiguousarray(levels, dtype=np.int16)
@@ -584,6 +631,12 @@ RDOQ_REQ = np.dtype([("coef_offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), (
 AFFMVP_REQ = np.dtype([("scup", "<i4"), ("cu_width", "<i2"), ("lidx", "i1"), ("cur_refi", "i1"), ("mvr", "i1"),
                        ("pad", "i1", (3,))])
 AFFMVP_OUT = np.dtype([("mvp", "<i4", (2, 2))])
+AFFMRG_PIC = np.dtype([("ptr", "<i8"), ("ref0_ptr", "<i8", (2,)), ("col_list_ptr", "<i8", (17,)), ("i_scu", "<i4"),
+                       ("pic_width_in_scu", "<i4"), ("pic_height_in_scu", "<i4"), ("rows", "<i4"),
+                       ("slice_type", "<i4"), ("log2_max_cuwh", "<i4")])
+AFFMRG_REQ = np.dtype([("scup", "<i4"), ("cu_width", "<i2"), ("cu_height", "<i2")])
+AFFMRG_OUT = np.dtype([("num", "<i4"), ("cp_num", "i1", (5,)), ("refi", "i1", (5, 2)), ("pad", "i1"),
+                       ("cpmv", "<i4", (5, 2, 3, 2))])
 LAT_Q = np.dtype([("ssd", "<u4"), ("coef_hash", "<u4"), ("num_nz", "<u2"), ("last_nz", "<i2"), ("sum_abs", "<u4")])
 
 MC_LUMA = np.array([[0, 0, 0, 64, 0, 0, 0, 0], [-1, 4, -10, 57, 19, -7, 3, -1], [-1, 4, -11, 40, 40, -11, 4, -1],

@@ -564,3 +564,38 @@ void refk_affine_mvp(s64 ptr, const s64 *ref_ptr, int n_ref, s16 *map_mv, s8 *ma
     for (int g = 0; g < 2; g++)
         for (int d = 0; d < 2; d++) mvp_out[g * 2 + d] = mvp[g][d];
 }
+
+/* com_get_affine_merge_candidate (src/com_util.c:1761) for one CU.  The maps point at the
+ * field's SCU (0, 0) (the border before it readable); the colocated picture's maps, POC and
+ * list_ptr go into refp[0][REFP_1] for B slices and refp[0][REFP_0] otherwise, as the function
+ * reads them.  out: num, cp_num[5], refi[5][2], cpmv[5][2][3][2] (vertices past cp_num zeroed). */
+void refk_affine_merge(s64 ptr, const s64 *ref0_ptr, s64 *col_list_ptr, s16 *map_mv, s8 *map_refi, u8 *map_scu,
+                       u32 *map_pos, s16 *col_mv, s8 *col_refi, int i_scu, int pic_w_scu, int pic_h_scu,
+                       int slice_type, int log2_max_cuwh, int scup, int cu_width, int cu_height, s32 *num,
+                       s8 *cp_num, s8 *refi, s32 *cpmv)
+{
+    static com_ref_pic_t refp[MAX_REFS][REFP_NUM];
+    memset(refp, 0, sizeof(refp));
+    refp[0][REFP_0].ptr = ref0_ptr[0];
+    refp[0][REFP_1].ptr = ref0_ptr[1];
+    com_ref_pic_t *col = &refp[0][slice_type == SLICE_B ? REFP_1 : REFP_0];
+    col->map_mv = (s16(*)[REFP_NUM][MV_D])col_mv;
+    col->map_refi = (s8(*)[REFP_NUM])col_refi;
+    col->list_ptr = col_list_ptr;
+    s8 mrg_refi[AFF_MAX_NUM_MRG][REFP_NUM];
+    CPMV mrg_cpmv[AFF_MAX_NUM_MRG][REFP_NUM][VER_NUM][MV_D];
+    int mrg_cp_num[AFF_MAX_NUM_MRG];
+    memset(mrg_cpmv, 0, sizeof(mrg_cpmv));
+    *num = com_get_affine_merge_candidate(ptr, scup, (s8(*)[REFP_NUM])map_refi, (s16(*)[REFP_NUM][MV_D])map_mv,
+                                          (com_scu_t *)map_scu, map_pos, refp, cu_width, cu_height, i_scu, pic_w_scu,
+                                          pic_h_scu, slice_type, mrg_refi, mrg_cpmv, mrg_cp_num, log2_max_cuwh);
+    for (int k = 0; k < AFF_MAX_NUM_MRG; k++) {
+        cp_num[k] = (s8)mrg_cp_num[k];
+        for (int l = 0; l < REFP_NUM; l++) {
+            refi[k * 2 + l] = mrg_refi[k][l];
+            for (int i = 0; i < 3; i++)
+                for (int d = 0; d < MV_D; d++)
+                    cpmv[((k * 2 + l) * 3 + i) * 2 + d] = i < mrg_cp_num[k] ? mrg_cpmv[k][l][i][d] : 0;
+        }
+    }
+}

@@ -805,6 +805,95 @@ def run_affmvp(B, p, seed):
     return digest(out)
 
 
+def affmrg_inputs(p, seed):
+    """a picture's coded-CU maps in the reference's layout (stride w + 2, border of uncoded SCUs):
+    64x64 CTUs split into random CUs (8..64), each inter (some affine: 4- or 6-parameter, 16x16
+    and larger) or intra, with per-list reference indices and per-SCU MVs; the colocated picture's
+    list-0 maps; merge requests of every affine CU size at random positions"""
+    import pyoracle
+    rng = np.random.default_rng(seed)
+    w, h = p["w"], p["h"]
+    i_scu, rows = w + 2, h + 2
+    org = i_scu + 1
+    scu = np.zeros(rows * i_scu, np.uint8)
+    pos = np.zeros(rows * i_scu, np.uint32)
+    refi = np.full((rows * i_scu, 2), -1, np.int8)
+    mv = np.zeros((rows * i_scu, 2, 2), np.int16)
+
+    def cu(x, y, s):
+        if s > 2 and rng.random() < (0.6 if s > 4 else 0.4):
+            for dy in (0, s // 2):
+                for dx in (0, s // 2):
+                    cu(x + dx, y + dy, s // 2)
+            return
+        cw = ch = s
+        if s >= 4 and rng.random() < 0.3:   # a horizontal or vertical binary split
+            if rng.random() < 0.5:
+                ch = s // 2
+                cus = [(x, y, cw, ch), (x, y + ch, cw, ch)]
+            else:
+                cw = s // 2
+                cus = [(x, y, cw, ch), (x + cw, y, cw, ch)]
+        else:
+            cus = [(x, y, cw, ch)]
+        for (cx, cy, a, b) in cus:
+            if cx >= w or cy >= h:
+                continue
+            intra = rng.random() < 0.2
+            aff = 0 if intra or a < 4 or b < 4 or rng.random() < 0.55 else int(rng.integers(1, 3))
+            r = np.where(rng.random(2) < 0.65, 0, rng.integers(-1, p["nref"], 2))
+            if not intra and (r < 0).all():
+                r[rng.integers(0, 2)] = rng.integers(0, p["nref"])
+            base = rng.integers(-200, 201, (2, 2))
+            lw, lh = int(a * 4).bit_length() - 1, int(b * 4).bit_length() - 1
+            for yy in range(cy, min(cy + b, h)):
+                for xx in range(cx, min(cx + a, w)):
+                    k = org + yy * i_scu + xx
+                    scu[k] = 1 | (2 if intra else 0) | (aff << 4)
+                    pos[k] = ((cy * i_scu + cx) << 6) | (lh << 3) | lw
+                    if not intra:
+                        refi[k] = r
+                        mv[k] = base + rng.integers(-24, 25, (2, 2))
+
+    for cy in range(0, h, 16):
+        for cx in range(0, w, 16):
+            cu(cx, cy, 16)
+    col_refi = np.full((rows * i_scu, 2), -1, np.int8)
+    col_mv = np.zeros((rows * i_scu, 2, 2), np.int16)
+    inner = np.zeros((rows, i_scu), bool)
+    inner[1:h + 1, 1:w + 1] = True
+    inner = inner.ravel()
+    col_refi[inner, 0] = rng.integers(-1, 4, int(inner.sum()))
+    col_mv[inner, 0] = rng.integers(-300, 301, (int(inner.sum()), 2))
+    pic = np.zeros(1, dtype=pyoracle.AFFMRG_PIC)
+    pic["ptr"] = 40
+    b = p["slice"] == "B"
+    pic["ref0_ptr"] = (32, 48) if b else (36, 28)
+    pic["col_list_ptr"] = np.array([(16, 24, 8, 0)[i % 4] if b else (20, 12, 4, 34)[i % 4] for i in range(17)])
+    pic["i_scu"] = i_scu
+    pic["pic_width_in_scu"] = w
+    pic["pic_height_in_scu"] = h
+    pic["rows"] = rows
+    pic["slice_type"] = 3 if b else 2
+    pic["log2_max_cuwh"] = 6
+    n = p["n"]
+    reqs = np.zeros(n, dtype=pyoracle.AFFMRG_REQ)
+    sizes = [16, 32, 64]
+    for k in range(n):
+        cw, ch = int(rng.choice(sizes)), int(rng.choice(sizes))
+        x = int(rng.integers(0, w - cw // 4 + 1)) & ~(cw // 4 - 1)
+        y = int(rng.integers(0, h - ch // 4 + 1)) & ~(ch // 4 - 1)
+        reqs[k] = (y * i_scu + x, cw, ch)
+    return pic, mv.reshape(-1, 2, 2), refi, scu, pos, col_mv, col_refi, reqs
+
+
+def run_affmrg(B, p, seed):
+    pic, mv, refi, scu, pos, cmv, crefi, reqs = affmrg_inputs(p, seed)
+    res = B.affine_merge(pic, mv, refi, scu, pos, cmv, crefi, reqs)
+    out = res[0] if isinstance(res, tuple) else res
+    return digest(out)
+
+
 def run_rdoq(B, p, seed):
     reqs, ests, coefs = rdoq_inputs(B, p, seed)
     nz = B.rdoq(reqs, ests, coefs)
@@ -815,7 +904,7 @@ RUNNERS = {
     "sad": run_sad, "satd_tile": run_satd_tile, "had": run_had, "ipflt": run_ipflt, "ipflt_ext": run_ipflt_ext,
     "ipcpy": run_ipcpy, "if_luma_frame": run_if_luma_frame, "pel": run_pel, "intra": run_intra,
     "ang_entry": run_ang_entry, "nbr": run_nbr, "fdct2": run_fdct2, "dct87": run_dct87, "xform": run_xform,
-    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "coef_rate": run_coef_rate, "quant_wq": run_quant_wq, "affmvp": run_affmvp, "rdoq": run_rdoq,
+    "quant": run_quant, "dquant": run_dquant, "tables": run_tables, "loka": run_loka, "tz": run_tz, "mc": run_mc, "affine": run_affine, "affme": run_affme, "rmd": run_rmd, "coef_rate": run_coef_rate, "quant_wq": run_quant_wq, "affmvp": run_affmvp, "affmrg": run_affmrg, "rdoq": run_rdoq,
 }
 
 # TZ search cases: encoder core search (padded references, random-access and low-delay ranges)
@@ -844,6 +933,13 @@ QUANT_WQ_CASES = [dict(n=200), dict(n=120)]
 # affine control-point MVP cases (com_get_affine_mvp_scaling): a 4-reference field with small
 # MVs, and a narrow 2-reference field with full-range MVs (the s16 and CPMV clips)
 AFFMVP_CASES = [dict(w=48, h=32, nref=4, n=200), dict(w=30, h=17, nref=2, n=160, big=1)]
+
+# affine merge candidate cases: B and P slices (colocated list-1 / list-0 picture), two picture
+# sizes
+AFFMRG_CASES = [
+    dict(w=48, h=32, nref=3, slice="B", n=240),
+    dict(w=64, h=48, nref=2, slice="P", n=240),
+]
 
 # coefficient rate cases (lbac_enc_run_length_cc_rdo)
 COEF_RATE_CASES = [dict(n=200), dict(n=150)]
@@ -943,6 +1039,8 @@ def all_cases():
         add("quant_wq", **p)
     for p in AFFMVP_CASES:
         add("affmvp", **p)
+    for p in AFFMRG_CASES:
+        add("affmrg", **p)
     return cases
 
 
