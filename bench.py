@@ -817,6 +817,48 @@ def affmvp_part(u, torch, stream, flush, with_cpu, reps=10):
     return out
 
 
+def affmrg_part(u, torch, stream, flush, with_cpu, reps=10):
+    """com_get_affine_merge_candidate for 262,144 CUs (16x16..64x64, B slice) of a 1080p picture's
+    coded-CU maps (uavs3e_cuda_affine_merge_device, one thread per CU)"""
+    import cases
+    import numpy as np
+    n = 1 << 18
+    args = cases.affmrg_inputs(dict(w=480, h=270, nref=3, slice="B", n=n), 93)
+    pic, reqs = args[0], args[7]
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).cuda()  # noqa: E731
+    dm = [d(a) for a in args[1:8]]
+    d_out = torch.zeros(n * u.AFFMRG_OUT.itemsize, dtype=torch.uint8, device="cuda")
+    sp = stream.cuda_stream
+
+    def run():
+        u.affine_merge_device(pic, *[a.data_ptr() for a in dm], n, d_out.data_ptr(), None, sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms_gpu = sum(a.elapsed_time(b) for a, b in evs) / reps
+    moved = n * (8 + u.AFFMRG_OUT.itemsize)
+    out = {"workload": "affine merge candidates of 262,144 CUs (16x16..64x64, B slice, colocated scaling) on a "
+                       "1080p picture's coded-CU maps (480 x 270 SCUs)", "cus": n, "ms_per_batch": ms_gpu,
+           "cus_per_s": n / (ms_gpu / 1000.0), "request_result_gb_s": moved / (ms_gpu / 1000.0) / 1e9}
+    if with_cpu:
+        import pyoracle
+        o = pyoracle.Oracle()
+        t0 = time.perf_counter()
+        o.affine_merge(*args)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "CUs/s", "cores": 1, "kind": "port",
+                               "sample": f"the whole batch through the oracle restatement, {dt:.2f} s"}
+    return out
+
+
 def affme_leg(u, torch, stream, flush, with_cpu, reps=10):
     """affine motion searches (affine_me_gradient) of a 1080p frame: every block of 16x16 and
     larger on the CTU grid against 2 references, AMVR indices 0..2, 70 % uni calls (60 % of them
@@ -886,6 +928,7 @@ def affme_leg(u, torch, stream, flush, with_cpu, reps=10):
                                "sample": f"the whole batch through the oracle restatement, {dt:.2f} s"}
     ms.close()
     out["mvp"] = affmvp_part(u, torch, stream, flush, with_cpu, reps)
+    out["merge"] = affmrg_part(u, torch, stream, flush, with_cpu, reps)
     return out
 
 

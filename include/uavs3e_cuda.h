@@ -453,6 +453,57 @@ UAVS3E_CUDA_API int uavs3e_cuda_affine_mvp_device(int64_t ptr, const int64_t *d_
                                                   int rows, const uavs3e_cuda_affmvp_req_t *d_reqs, int n,
                                                   uavs3e_cuda_affmvp_out_t *d_out, int32_t *d_err, void *stream);
 
+/* Affine merge candidates (com_get_affine_merge_candidate, src/com_util.c:1761-1981, with
+ * com_derive_affine_model_mv :1566, com_derive_affine_constructed_candidate :1656,
+ * get_colocal_scup :303, get_col_mv / get_col_mv_from_list0 :977-1000, scaling_mv1 :322) for lists
+ * of CUs: up to 2 candidates inherited from affine neighbours (F, G, C, A, D; the neighbour CU's
+ * corner MVs extrapolated to the CU, 4-parameter across a CTU row boundary), then the
+ * constructed ones from the control points LT (A, B, D), RT (G, C), LB (F) and the colocated
+ * RB (scaled by POC distances) in the reference's 6 model orders, zero-padded to 5.  The maps
+ * have the motion field's layout of uavs3e_cuda_affine_mvp (stride i_scu, SCU (0, 0) at index
+ * i_scu + 1): map_mv s16 [rows * i_scu][2][2], map_refi s8 [rows * i_scu][2], map_scu u8 (the
+ * encoder's com_scu_t byte: bit 0 coded, bit 1 intra, bits 4-5 affine), map_pos u32 (the covering
+ * CU's top-left SCU << 6 | log2 height << 3 | log2 width); col_mv / col_refi are the colocated
+ * picture's (refp[0][REFP_1] in B slices, refp[0][REFP_0] otherwise) in the same layout. */
+typedef struct {
+    int64_t ptr;                /* POC of the current picture                                  */
+    int64_t ref0_ptr[2];        /* POC of refp[0][REFP_0] and refp[0][REFP_1]                   */
+    int64_t col_list_ptr[17];   /* the colocated picture's list_ptr (its list-0 reference POCs)  */
+    int32_t i_scu, pic_width_in_scu, pic_height_in_scu, rows;
+    int32_t slice_type;         /* 3 = SLICE_B (colocated in list 1, both lists scaled), else P */
+    int32_t log2_max_cuwh;
+} uavs3e_cuda_affmrg_pic_t;
+
+typedef struct {
+    int32_t scup;               /* y_scu * i_scu + x_scu of the CU's top-left SCU               */
+    int16_t cu_width, cu_height; /* luma samples, powers of two 16..128                          */
+} uavs3e_cuda_affmrg_req_t;
+
+typedef struct {
+    int32_t num;                /* candidates derived before the zero padding                   */
+    int8_t  cp_num[5];          /* control points of each candidate, 2 or 3                     */
+    int8_t  refi[5][2];         /* reference index per list, -1 unused                          */
+    int8_t  pad;
+    int32_t cpmv[5][2][3][2];   /* control-point MVs, 1/16 samples; vertices past cp_num are 0  */
+} uavs3e_cuda_affmrg_out_t;
+
+/* Host buffers, synchronous; returns UAVS3E_CUDA_ERR_ARG when a request falls outside the domain
+ * (a map read outside the field, sizes, a colocated reference index >= 17, a zero POC distance):
+ * its result is zeroed, the others are valid. */
+UAVS3E_CUDA_API int uavs3e_cuda_affine_merge(const uavs3e_cuda_affmrg_pic_t *pic, const int16_t *map_mv,
+                                             const int8_t *map_refi, const uint8_t *map_scu,
+                                             const uint32_t *map_pos, const int16_t *col_mv, const int8_t *col_refi,
+                                             const uavs3e_cuda_affmrg_req_t *reqs, int n,
+                                             uavs3e_cuda_affmrg_out_t *out);
+/* Device buffers on a stream, no synchronisation; d_err (optional) counts the requests outside
+ * the domain. */
+UAVS3E_CUDA_API int uavs3e_cuda_affine_merge_device(const uavs3e_cuda_affmrg_pic_t *pic, const int16_t *d_map_mv,
+                                                    const int8_t *d_map_refi, const uint8_t *d_map_scu,
+                                                    const uint32_t *d_map_pos, const int16_t *d_col_mv,
+                                                    const int8_t *d_col_refi, const uavs3e_cuda_affmrg_req_t *d_reqs,
+                                                    int n, uavs3e_cuda_affmrg_out_t *d_out, int32_t *d_err,
+                                                    void *stream);
+
 /* Device pointer to sample (0,0) of plane `phase` (dy*4 + dx, 0 = integer) of `slot`, and the
  * session's plane stride; for inspection by tests. */
 UAVS3E_CUDA_API const uint8_t *uavs3e_cuda_me_plane(uavs3e_cuda_me *me, int slot, int phase);

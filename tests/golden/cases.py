@@ -821,7 +821,8 @@ def affmrg_inputs(p, seed):
     mv = np.zeros((rows * i_scu, 2, 2), np.int16)
 
     def cu(x, y, s):
-        if s > 2 and rng.random() < (0.6 if s > 4 else 0.4):
+        # a CU crossing the picture's edge is split, as the encoder does
+        if s > 2 and (x + s > w or y + s > h or rng.random() < (0.6 if s > 4 else 0.4)):
             for dy in (0, s // 2):
                 for dx in (0, s // 2):
                     cu(x + dx, y + dy, s // 2)

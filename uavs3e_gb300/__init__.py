@@ -84,6 +84,8 @@ def _declare(L):
     L.uavs3e_cuda_me_frame.argtypes = [P, I, P, I, P, I, C.c_uint32, P]
     L.uavs3e_cuda_affine_mvp.argtypes = [C.c_int64, P, I, P, P, I, I, P, I, P]
     L.uavs3e_cuda_affine_mvp_device.argtypes = [C.c_int64, P, I, P, P, I, I, P, I, P, P, P]
+    L.uavs3e_cuda_affine_merge.argtypes = [P, P, P, P, P, P, P, P, I, P]
+    L.uavs3e_cuda_affine_merge_device.argtypes = [P, P, P, P, P, P, P, P, I, P, P, P]
     L.uavs3e_cuda_intra_rmd.argtypes = [P, C.c_size_t, P, I, P]
     L.uavs3e_cuda_coef_rate.argtypes = [P, I, P, C.c_size_t, P]
     L.uavs3e_cuda_quant_wq.argtypes = [P, I, P, P, P, C.c_size_t, P]
@@ -617,3 +619,34 @@ def affine_mvp_device(ptr_cur, d_ref_ptr, n_ref, d_map_mv, d_map_refi, i_scu, ro
                       stream=None):
     check(lib().uavs3e_cuda_affine_mvp_device(int(ptr_cur), d_ref_ptr, n_ref, d_map_mv, d_map_refi, i_scu, rows,
                                               d_reqs, n, d_out, d_err, stream), "affine_mvp_device")
+
+
+AFFMRG_PIC = np.dtype([("ptr", "<i8"), ("ref0_ptr", "<i8", (2,)), ("col_list_ptr", "<i8", (17,)), ("i_scu", "<i4"),
+                       ("pic_width_in_scu", "<i4"), ("pic_height_in_scu", "<i4"), ("rows", "<i4"),
+                       ("slice_type", "<i4"), ("log2_max_cuwh", "<i4")])
+AFFMRG_REQ = np.dtype([("scup", "<i4"), ("cu_width", "<i2"), ("cu_height", "<i2")])
+AFFMRG_OUT = np.dtype([("num", "<i4"), ("cp_num", "i1", (5,)), ("refi", "i1", (5, 2)), ("pad", "i1"),
+                       ("cpmv", "<i4", (5, 2, 3, 2))])
+
+
+def affine_merge(pic, map_mv, map_refi, map_scu, map_pos, col_mv, col_refi, reqs):
+    """uavs3e_cuda_affine_merge: com_get_affine_merge_candidate for every AFFMRG_REQ; pic an
+    AFFMRG_PIC record, the maps in the encoder's layout (SCU (0, 0) at index i_scu + 1): map_mv /
+    col_mv int16 [rows * i_scu, 2, 2], map_refi / col_refi int8 [rows * i_scu, 2], map_scu uint8 and
+    map_pos uint32 [rows * i_scu]; returns AFFMRG_OUT"""
+    pic = np.ascontiguousarray(pic, dtype=AFFMRG_PIC).reshape(1)
+    arrs = [np.ascontiguousarray(a, dtype=t) for a, t in ((map_mv, np.int16), (map_refi, np.int8), (map_scu, np.uint8),
+                                                           (map_pos, np.uint32), (col_mv, np.int16),
+                                                           (col_refi, np.int8))]
+    reqs = np.ascontiguousarray(reqs, dtype=AFFMRG_REQ)
+    out = np.zeros(max(1, len(reqs)), dtype=AFFMRG_OUT)
+    check(lib().uavs3e_cuda_affine_merge(pic.ctypes.data, *[a.ctypes.data for a in arrs], reqs.ctypes.data, len(reqs),
+                                         out.ctypes.data), "affine_merge")
+    return out[:len(reqs)]
+
+
+def affine_merge_device(pic, d_map_mv, d_map_refi, d_map_scu, d_map_pos, d_col_mv, d_col_refi, d_reqs, n, d_out,
+                        d_err=None, stream=None):
+    pic = np.ascontiguousarray(pic, dtype=AFFMRG_PIC).reshape(1)
+    check(lib().uavs3e_cuda_affine_merge_device(pic.ctypes.data, d_map_mv, d_map_refi, d_map_scu, d_map_pos, d_col_mv,
+                                                d_col_refi, d_reqs, n, d_out, d_err, stream), "affine_merge_device")

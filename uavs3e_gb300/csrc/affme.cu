@@ -576,3 +576,359 @@ UAVS3E_CUDA_API int uavs3e_cuda_affine_mvp(int64_t ptr, const int64_t *ref_ptr, 
     if (bad) return set_status(UC_ERR_ARG, "affine_mvp: requests outside the domain");
     return UC_OK;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Affine merge candidates: one thread per CU, the reference's derivation order.  Model-based
+// candidates: the first two affine neighbours among F, G, C, A, D (same-CU duplicates dropped),
+// each neighbour CU's corner MVs (found through its map_pos entry) extrapolated to the CU's
+// corners in 1/128 units with the magnitude-rounding shift, a 4-parameter model when the
+// neighbour's bottom edge is the CTU row boundary above the CU.  Constructed candidates: LT, RT,
+// LB from the first inter neighbour of each corner, RB from the colocated picture (scaled by POC
+// distances), combined in the 6 model orders while the list has room.  Every read of the maps is
+// bounds-checked; a request with an out-of-field read gets a zeroed result and is counted.
+// Records are assembled in shared memory and written out by the CTA as contiguous words.
+// ---------------------------------------------------------------------------------------------
+static_assert(sizeof(uavs3e_cuda_affmrg_req_t) == 8, "affine merge request layout");
+static_assert(sizeof(uavs3e_cuda_affmrg_out_t) == 260, "affine merge result layout");
+static_assert(sizeof(uavs3e_cuda_affmrg_pic_t) == 184, "affine merge picture layout");
+
+struct AmrgMaps {
+    const short *mv; const signed char *refi; const unsigned char *scu; const unsigned *pos;
+    const short *col_mv; const signed char *col_refi;
+    long long origin, nf;
+};
+
+struct AmrgReader {
+    const AmrgMaps &M;
+    bool bad;
+    __device__ bool in(long long a)
+    {
+        const long long k = a + M.origin;
+        if (k < 0 || k >= M.nf) { bad = true; return false; }
+        return true;
+    }
+    __device__ int scu(long long a) { return in(a) ? M.scu[a + M.origin] : 0; }
+    __device__ unsigned pos(long long a) { return in(a) ? M.pos[a + M.origin] : 0u; }
+    __device__ int refi(long long a, int l) { return in(a) ? M.refi[(a + M.origin) * 2 + l] : -1; }
+    __device__ int mv(long long a, int l, int d) { return in(a) ? M.mv[((a + M.origin) * 2 + l) * 2 + d] : 0; }
+};
+
+__device__ __forceinline__ int amrg_round7(int v)
+{
+    return v >= 0 ? (int)(((unsigned)v + 64u) >> 7) : -(int)(((unsigned)(-(long long)v) + 64u) >> 7);
+}
+
+__device__ __forceinline__ int amrg_clip18(int v) { return max(-131072, min(131071, v)); }
+
+__device__ __forceinline__ int amrg_shl(int v, int s) { return (int)((unsigned)v << s); }
+
+// scaling_mv1 of an MV (x, y): false on a zero POC distance
+__device__ __forceinline__ bool amrg_scale(long long cur, long long cur_ref, long long neb, long long neb_ref, int mx,
+                                           int my, int &ox, int &oy)
+{
+    const int t0 = (int)(neb * 2 - neb_ref * 2), t1 = (int)(cur * 2 - cur_ref * 2);
+    if (t0 == 0 || t1 == 0) return false;
+    const int ratio = (1 << 14) / t0 * t1;
+    ox = amvp_scale(mx, ratio);
+    oy = amvp_scale(my, ratio);
+    return true;
+}
+
+// com_derive_affine_model_mv: control points of the CU at scup from the affine CU covering scun
+__device__ void amrg_model(AmrgReader &R, const uavs3e_cuda_affmrg_pic_t &P, int scup, int scun, int l, int cw, int ch,
+                           int (*mvp)[2], int &vn)
+{
+    const int i_scu = P.i_scu;
+    const unsigned pos = R.pos(scun);
+    const int lw = (int)(pos & 7), lh = (int)((pos >> 3) & 7), nw = 1 << lw, nh = 1 << lh;
+    const int a0 = (int)(pos >> 6), a1 = a0 + ((nw >> 2) - 1), a2 = a0 + ((nh >> 2) - 1) * i_scu, a3 = a2 + ((nw >> 2) - 1);
+    const int neb_x = (a0 % i_scu) << 2;
+    int neb_y = (a0 / i_scu) << 2;
+    const int cur_x = (scup % i_scu) << 2, cur_y = (scup / i_scu) << 2;
+    int m0x = R.mv(a0, l, 0), m0y = R.mv(a0, l, 1), m1x = R.mv(a1, l, 0), m1y = R.mv(a1, l, 1);
+    const int m2x = R.mv(a2, l, 0), m2y = R.mv(a2, l, 1), m3x = R.mv(a3, l, 0), m3y = R.mv(a3, l, 1);
+    bool top = false;
+    if ((neb_y + nh) % (1 << P.log2_max_cuwh) == 0 && neb_y + nh == cur_y) {
+        top = true;
+        neb_y += nh;
+        m0x = m2x; m0y = m2y; m1x = m3x; m1y = m3y;
+    }
+    const int dhx = amrg_shl(m1x - m0x, 7 - lw), dhy = amrg_shl(m1y - m0y, 7 - lw);
+    int dvx, dvy;
+    if (vn == 3 && !top) {
+        dvx = amrg_shl(m2x - m0x, 7 - lh);
+        dvy = amrg_shl(m2y - m0y, 7 - lh);
+    } else {
+        dvx = -dhy;
+        dvy = dhx;
+        vn = 2;
+    }
+    const int hb = amrg_shl(m0x, 7), vb = amrg_shl(m0y, 7);
+    for (int k = 0; k < vn; k++) {
+        const int ox = cur_x - neb_x + (k == 1 ? cw : 0), oy = cur_y - neb_y + (k == 2 ? ch : 0);
+        const int th = (int)((unsigned)dhx * (unsigned)ox + (unsigned)dvx * (unsigned)oy + (unsigned)hb);
+        const int tv = (int)((unsigned)dhy * (unsigned)ox + (unsigned)dvy * (unsigned)oy + (unsigned)vb);
+        mvp[k][0] = amrg_clip18(amrg_shl(amrg_round7(th), 2));
+        mvp[k][1] = amrg_clip18(amrg_shl(amrg_round7(tv), 2));
+    }
+}
+
+// com_derive_affine_constructed_candidate for the control points c0, c1[, c2] of model m
+__device__ void amrg_construct(uavs3e_cuda_affmrg_out_t &o, int &cnt, int cw, int ch, const bool *valid,
+                               const int (*cmv)[4][2], const int (*crefi)[4], int c0, int c1, int c2, int m, int ver)
+{
+    if (cnt >= 5) return;
+    const int idx[3] = { c0, c1, c2 };
+    for (int i = 0; i < ver; i++)
+        if (!valid[idx[i]]) return;
+    bool vm[2];
+    for (int l = 0; l < 2; l++) {
+        bool ok = true;
+        for (int i = 0; i < ver; i++) ok = ok && crefi[l][idx[i]] >= 0 && crefi[l][idx[i]] == crefi[l][c0];
+        vm[l] = ok;
+    }
+    if (!vm[0] && !vm[1]) return;
+    o.cp_num[cnt] = (signed char)ver;
+    const int sh = 7 + (31 - __clz(cw)) - (31 - __clz(ch));
+    for (int l = 0; l < 2; l++) {
+        if (!vm[l]) {
+            o.refi[cnt][l] = -1;
+            for (int i = 0; i < ver; i++) o.cpmv[cnt][l][i][0] = o.cpmv[cnt][l][i][1] = 0;
+            continue;
+        }
+        int t[4][2] = { { 0, 0 }, { 0, 0 }, { 0, 0 }, { 0, 0 } };
+        for (int i = 0; i < ver; i++) { t[idx[i]][0] = cmv[l][idx[i]][0]; t[idx[i]][1] = cmv[l][idx[i]][1]; }
+        for (int d = 0; d < 2; d++) {
+            if (m == 1) t[2][d] = t[3][d] + t[0][d] - t[1][d];
+            if (m == 2) t[1][d] = t[3][d] + t[0][d] - t[2][d];
+            if (m == 3) t[0][d] = t[1][d] + t[2][d] - t[3][d];
+        }
+        if (m == 5) {
+            const int th = (int)((unsigned)amrg_shl(t[2][1] - t[0][1], sh) + (unsigned)amrg_shl(t[0][0], 7));
+            const int tv = (int)((unsigned)(-amrg_shl(t[2][0] - t[0][0], sh)) + (unsigned)amrg_shl(t[0][1], 7));
+            t[1][0] = amrg_round7(th);
+            t[1][1] = amrg_round7(tv);
+        }
+        o.refi[cnt][l] = (signed char)crefi[l][c0];
+        for (int i = 0; i < ver; i++)
+            for (int d = 0; d < 2; d++) o.cpmv[cnt][l][i][d] = amrg_clip18(amrg_shl(t[i][d], 2));
+    }
+    cnt++;
+}
+
+__device__ bool amrg_one(const uavs3e_cuda_affmrg_pic_t &P, const AmrgMaps &M, const uavs3e_cuda_affmrg_req_t q,
+                         uavs3e_cuda_affmrg_out_t &o)
+{
+    const int cw = q.cu_width, ch = q.cu_height;
+    if ((cw != 16 && cw != 32 && cw != 64 && cw != 128) || (ch != 16 && ch != 32 && ch != 64 && ch != 128)) return false;
+    AmrgReader R{ M, false };
+    const int i_scu = P.i_scu, scup = q.scup, wsc = cw >> 2, hsc = ch >> 2;
+    int cnt = 0;
+    {
+        const int nb[5] = { scup + i_scu * (hsc - 1) - 1, scup - i_scu + wsc - 1, scup - i_scu + wsc, scup - 1,
+                            scup - i_scu - 1 };
+        int aff[5], tl[5];
+        bool valid[5];
+        for (int k = 0; k < 5; k++) {
+            aff[k] = (R.scu(nb[k]) >> 4) & 3;
+            valid[k] = aff[k] != 0;
+            tl[k] = valid[k] ? (int)(R.pos(nb[k]) >> 6) : 0;
+        }
+        if (valid[2] && valid[1] && tl[1] == tl[2]) valid[2] = false;
+        const bool v3 = valid[3];
+        if (valid[3] && valid[0] && tl[0] == tl[3]) valid[3] = false;
+        if ((valid[4] && v3 && tl[4] == tl[3]) || (valid[4] && valid[1] && tl[4] == tl[1])) valid[4] = false;
+        for (int k = 0; k < 5 && cnt < 2; k++) {
+            if (!valid[k]) continue;
+            int vn = aff[k] == 1 ? 2 : 3;
+            for (int l = 0; l < 2; l++) {
+                const int r = R.refi(nb[k], l);
+                if (r >= 0) {
+                    o.refi[cnt][l] = (signed char)r;
+                    amrg_model(R, P, scup, nb[k], l, cw, ch, o.cpmv[cnt][l], vn);
+                } else {
+                    o.refi[cnt][l] = -1;
+                    for (int i = 0; i < 3; i++) o.cpmv[cnt][l][i][0] = o.cpmv[cnt][l][i][1] = 0;
+                }
+            }
+            o.cp_num[cnt] = (signed char)vn;
+            cnt++;
+        }
+    }
+    {
+        int cmv[2][4][2], crefi[2][4];
+        bool valid[4] = { false, false, false, false };
+        for (int l = 0; l < 2; l++)
+            for (int i = 0; i < 4; i++) { cmv[l][i][0] = cmv[l][i][1] = 0; crefi[l][i] = -1; }
+        const int corner[6] = { scup - 1, scup - i_scu, scup - i_scu - 1, scup - i_scu + wsc - 1, scup - i_scu + wsc,
+                                scup + i_scu * (hsc - 1) - 1 };
+        const int first[4] = { 0, 3, 5, 6 };
+        for (int g = 0; g < 3; g++) {
+            for (int k = first[g]; k < first[g + 1]; k++) {
+                const int a = corner[k];
+                if ((R.scu(a) & 3) != 1) continue;
+                for (int l = 0; l < 2; l++) {
+                    crefi[l][g] = R.refi(a, l);
+                    cmv[l][g][0] = R.mv(a, l, 0);
+                    cmv[l][g][1] = R.mv(a, l, 1);
+                }
+                valid[g] = true;
+                break;
+            }
+        }
+        const int rb = scup + i_scu * (hsc - 1) + (wsc - 1);
+        const int bx = rb % i_scu, by = rb / i_scu;
+        int xpos = (bx & ~3) + 2, ypos = (by & ~3) + 2;
+        if (ypos >= P.pic_height_in_scu) ypos = ((by & ~3) + P.pic_height_in_scu) >> 1;
+        if (xpos >= P.pic_width_in_scu) xpos = ((bx & ~3) + P.pic_width_in_scu) >> 1;
+        const long long co = (long long)ypos * i_scu + xpos + M.origin;
+        if (co < 0 || co >= M.nf) return false;
+        const int cr = M.col_refi[co * 2];
+        const int cx = M.col_mv[co * 4 + 0], cy = M.col_mv[co * 4 + 1];
+        if (cr >= 17) return false;
+        if (cr >= 0) {
+            if (P.slice_type == 3) {
+                for (int l = 0; l < 2; l++) {
+                    if (!amrg_scale(P.ptr, P.ref0_ptr[l], P.ref0_ptr[1], P.col_list_ptr[cr], cx, cy, cmv[l][3][0], cmv[l][3][1]))
+                        return false;
+                    crefi[l][3] = 0;
+                }
+            } else {
+                if (!amrg_scale(P.ptr, P.ref0_ptr[0], P.ref0_ptr[0], P.col_list_ptr[cr], cx, cy, cmv[0][3][0], cmv[0][3][1]))
+                    return false;
+                crefi[0][3] = 0;
+                crefi[1][3] = -1;
+            }
+            valid[3] = true;
+        }
+        amrg_construct(o, cnt, cw, ch, valid, cmv, crefi, 0, 1, 2, 0, 3);
+        amrg_construct(o, cnt, cw, ch, valid, cmv, crefi, 0, 1, 3, 1, 3);
+        amrg_construct(o, cnt, cw, ch, valid, cmv, crefi, 0, 2, 3, 2, 3);
+        amrg_construct(o, cnt, cw, ch, valid, cmv, crefi, 1, 2, 3, 3, 3);
+        amrg_construct(o, cnt, cw, ch, valid, cmv, crefi, 0, 1, 0, 4, 2);
+        amrg_construct(o, cnt, cw, ch, valid, cmv, crefi, 0, 2, 0, 5, 2);
+    }
+    o.num = cnt;
+    for (int k = cnt; k < 5; k++) {
+        o.cp_num[k] = 2;
+        o.refi[k][0] = 0;
+        o.refi[k][1] = -1;
+    }
+    for (int k = 0; k < 5; k++)
+        for (int l = 0; l < 2; l++)
+            for (int i = (k < cnt ? o.cp_num[k] : 0); i < 3; i++) o.cpmv[k][l][i][0] = o.cpmv[k][l][i][1] = 0;
+    return !R.bad;
+}
+
+constexpr int AMRG_THREADS = 128;
+
+__global__ void __launch_bounds__(AMRG_THREADS) k_affine_merge(const uavs3e_cuda_affmrg_pic_t P, AmrgMaps M,
+                                                              const uavs3e_cuda_affmrg_req_t *reqs, int n,
+                                                              uavs3e_cuda_affmrg_out_t *out, int *err)
+{
+    __shared__ uavs3e_cuda_affmrg_out_t s_out[AMRG_THREADS];
+    const int base = blockIdx.x * AMRG_THREADS, i = base + threadIdx.x;
+    if (i < n) {
+        uavs3e_cuda_affmrg_out_t o;
+        memset(&o, 0, sizeof(o));
+        if (!amrg_one(P, M, reqs[i], o)) {
+            memset(&o, 0, sizeof(o));
+            if (err) atomicAdd(err, 1);
+        }
+        s_out[threadIdx.x] = o;
+    }
+    __syncthreads();
+    // the CTA's records are contiguous: copy them out as words
+    const int nrec = min(AMRG_THREADS, n - base);
+    const unsigned *src = reinterpret_cast<const unsigned *>(s_out);
+    unsigned *dst = reinterpret_cast<unsigned *>(out + base);
+    const int words = nrec * (int)(sizeof(uavs3e_cuda_affmrg_out_t) / 4);
+    for (int w = threadIdx.x; w < words; w += AMRG_THREADS) dst[w] = src[w];
+}
+
+int launch_affine_merge(const uavs3e_cuda_affmrg_pic_t &pic, const short *d_mv, const signed char *d_refi,
+                        const unsigned char *d_scu, const unsigned *d_pos, const short *d_col_mv,
+                        const signed char *d_col_refi, const uavs3e_cuda_affmrg_req_t *d_reqs, int n,
+                        uavs3e_cuda_affmrg_out_t *d_out, int *d_err, cudaStream_t st)
+{
+    if (n < 0 || pic.i_scu < 3 || pic.rows < 2 || pic.pic_width_in_scu < 1 || pic.pic_height_in_scu < 1 ||
+        pic.log2_max_cuwh < 2 || pic.log2_max_cuwh > 7 ||
+        (n > 0 && (!d_mv || !d_refi || !d_scu || !d_pos || !d_col_mv || !d_col_refi || !d_reqs || !d_out)))
+        return set_status(UC_ERR_ARG, "affine_merge: bad argument");
+    if (((uintptr_t)d_mv & 3) || ((uintptr_t)d_col_mv & 3) || ((uintptr_t)d_pos & 3) || ((uintptr_t)d_out & 3))
+        return set_status(UC_ERR_ARG, "affine_merge: map_mv, col_mv, map_pos or out not 4-byte aligned");
+    if (n == 0) return UC_OK;
+    AmrgMaps M{ d_mv, d_refi, d_scu, d_pos, d_col_mv, d_col_refi, (long long)pic.i_scu + 1,
+                (long long)pic.rows * pic.i_scu };
+    k_affine_merge<<<(n + AMRG_THREADS - 1) / AMRG_THREADS, AMRG_THREADS, 0, st>>>(pic, M, d_reqs, n, d_out, d_err);
+    UC_CHECK(cudaGetLastError());
+    count_launch(1);
+    return UC_OK;
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_affine_merge_device(const uavs3e_cuda_affmrg_pic_t *pic, const int16_t *d_map_mv,
+                                                    const int8_t *d_map_refi, const uint8_t *d_map_scu,
+                                                    const uint32_t *d_map_pos, const int16_t *d_col_mv,
+                                                    const int8_t *d_col_refi, const uavs3e_cuda_affmrg_req_t *d_reqs,
+                                                    int n, uavs3e_cuda_affmrg_out_t *d_out, int32_t *d_err,
+                                                    void *stream)
+{
+    if (ensure_init()) return uavs3e_cuda_status();
+    if (!pic) return set_status(UC_ERR_ARG, "affine_merge: bad argument");
+    return launch_affine_merge(*pic, d_map_mv, (const signed char *)d_map_refi, d_map_scu, d_map_pos, d_col_mv,
+                               (const signed char *)d_col_refi, d_reqs, n, d_out, (int *)d_err, (cudaStream_t)stream);
+}
+
+UAVS3E_CUDA_API int uavs3e_cuda_affine_merge(const uavs3e_cuda_affmrg_pic_t *pic, const int16_t *map_mv,
+                                             const int8_t *map_refi, const uint8_t *map_scu,
+                                             const uint32_t *map_pos, const int16_t *col_mv, const int8_t *col_refi,
+                                             const uavs3e_cuda_affmrg_req_t *reqs, int n,
+                                             uavs3e_cuda_affmrg_out_t *out)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (!pic || n < 0 || pic->i_scu < 3 || pic->rows < 2 ||
+        (n > 0 && (!map_mv || !map_refi || !map_scu || !map_pos || !col_mv || !col_refi || !reqs || !out)))
+        return set_status(UC_ERR_ARG, "affine_merge: bad argument");
+    if (n == 0) return UC_OK;
+    const size_t field = (size_t)pic->rows * pic->i_scu;
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t b_mv = up(field * 8), b_refi = up(field * 2), b_scu = up(field), b_pos = up(field * 4);
+    const size_t b_req = up((size_t)n * sizeof(uavs3e_cuda_affmrg_req_t)), b_out = up((size_t)n * sizeof(uavs3e_cuda_affmrg_out_t));
+    cudaStream_t st = nullptr;
+    UC_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    char *buf = nullptr;
+    cudaError_t ce = cudaMallocAsync((void **)&buf, 2 * b_mv + 2 * b_refi + b_scu + b_pos + b_req + b_out + 256, st);
+    if (ce != cudaSuccess) { cudaStreamDestroy(st); return check_cuda(ce, "affine_merge: allocate"); }
+    char *d_mv = buf, *d_refi = d_mv + b_mv, *d_scu = d_refi + b_refi, *d_pos = d_scu + b_scu;
+    char *d_cmv = d_pos + b_pos, *d_crefi = d_cmv + b_mv, *d_req = d_crefi + b_refi, *d_out = d_req + b_req;
+    char *d_err = d_out + b_out;
+    int bad = 0;
+    rc = UC_OK;
+    if ((ce = cudaMemcpyAsync(d_mv, map_mv, field * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_refi, map_refi, field * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_scu, map_scu, field, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_pos, map_pos, field * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_cmv, col_mv, field * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_crefi, col_refi, field * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_req, reqs, (size_t)n * sizeof(uavs3e_cuda_affmrg_req_t), cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess ||
+        (ce = cudaMemsetAsync(d_err, 0, 4, st)) != cudaSuccess)
+        rc = check_cuda(ce, "affine_merge: upload");
+    if (!rc)
+        rc = launch_affine_merge(*pic, (const short *)d_mv, (const signed char *)d_refi, (const unsigned char *)d_scu,
+                                 (const unsigned *)d_pos, (const short *)d_cmv, (const signed char *)d_crefi,
+                                 (const uavs3e_cuda_affmrg_req_t *)d_req, n, (uavs3e_cuda_affmrg_out_t *)d_out,
+                                 (int *)d_err, st);
+    if (!rc && ((ce = cudaMemcpyAsync(out, d_out, (size_t)n * sizeof(uavs3e_cuda_affmrg_out_t), cudaMemcpyDeviceToHost,
+                                      st)) != cudaSuccess ||
+                (ce = cudaMemcpyAsync(&bad, d_err, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess))
+        rc = check_cuda(ce, "affine_merge: download");
+    cudaFreeAsync(buf, st);
+    ce = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return check_cuda(ce, "affine_merge: synchronise");
+    if (bad) return set_status(UC_ERR_ARG, "affine_merge: requests outside the domain");
+    return UC_OK;
+}
