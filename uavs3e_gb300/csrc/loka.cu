@@ -231,36 +231,57 @@ __device__ void lk_grid(LkSearch &S, int x0, int x1, int y0, int y1, int s, int 
 // the words w[2l .. 2l+4] of the row (from the common aligned base), so each lane loads its own
 // two words and takes the next three from lanes l+1 and l+2.  30 candidates per pass; the two
 // lanes after the last candidate only load, and only the words of the last candidate's span.
+// Vertically the candidates of consecutive grid rows are 8 rows apart and share 8 of their 16
+// reference rows, so a pass walks the reference rows once, top to bottom: each row feeds the
+// candidate it is row r of (r = 0..15) and, for r >= 8, also the next grid row's candidate (its
+// row r - 8); a candidate's SAD is complete at its row 15.
 __device__ void lk_grid8(LkSearch &S, int x0, int x1, int y0, int y1, int lane)
 {
     const int nx = (x1 - x0) / 8 + 1, ny = (y1 - y0) / 8 + 1;
     const u32 sh = (u32)(((uintptr_t)(S.ref + x0)) & 3) * 8;       // the same for every row and lane
     const int ws = S.stride >> 2;
     u64 kmin = ~0ull;
-    for (int gy = 0; gy < ny; gy++) {
-        const int my = y0 + 8 * gy;
-        for (int c0 = 0; c0 < nx; c0 += 30) {
-            const int nc = min(30, nx - c0);
-            const bool ld = lane < nc + 2;
-            const int mx = x0 + 8 * (c0 + lane);
-            const u32 *q = (const u32 *)(((uintptr_t)(S.ref + my * S.stride + mx)) & ~(uintptr_t)3);
-            u32 sad = 0;
-#pragma unroll 4
-            for (int r = 0; r < 16; r++, q += ws) {
-                const u32 w0 = ld ? __ldg(q) : 0u, w1 = lane < nc + 1 ? __ldg(q + 1) : 0u;
-                const u32 w2 = __shfl_down_sync(0xffffffffu, w0, 1), w3 = __shfl_down_sync(0xffffffffu, w1, 1);
-                const u32 w4 = __shfl_down_sync(0xffffffffu, w0, 2);
-                const uint4 o = *(const uint4 *)(S.so + r * 4);
-                sad = sad4(o.x, __funnelshift_r(w0, w1, sh), sad);
-                sad = sad4(o.y, __funnelshift_r(w1, w2, sh), sad);
-                sad = sad4(o.z, __funnelshift_r(w2, w3, sh), sad);
-                sad = sad4(o.w, __funnelshift_r(w3, w4, sh), sad);
+    for (int c0 = 0; c0 < nx; c0 += 30) {
+        const int nc = min(30, nx - c0);
+        const bool ld = lane < nc + 2, ld1 = lane < nc + 1;
+        const int mx = x0 + 8 * (c0 + lane);
+        const u32 *q = (const u32 *)(((uintptr_t)(S.ref + y0 * S.stride + mx)) & ~(uintptr_t)3);
+        u32 sa = 0, sb = 0;   // SADs of grid rows g and g + 1
+        int g = 0, ra = 0;    // ra: the current reference row's index within grid row g's candidate
+        const int rows = 8 * ny + 8;
+        for (int R = 0; R < rows; R++, q += ws) {
+            const u32 w0 = ld ? __ldg(q) : 0u, w1 = ld1 ? __ldg(q + 1) : 0u;
+            const u32 w2 = __shfl_down_sync(0xffffffffu, w0, 1), w3 = __shfl_down_sync(0xffffffffu, w1, 1);
+            const u32 w4 = __shfl_down_sync(0xffffffffu, w0, 2);
+            const u32 d0 = __funnelshift_r(w0, w1, sh), d1 = __funnelshift_r(w1, w2, sh);
+            const u32 d2 = __funnelshift_r(w2, w3, sh), d3 = __funnelshift_r(w3, w4, sh);
+            const uint4 o = *(const uint4 *)(S.so + ra * 4);
+            sa = sad4(o.x, d0, sa);
+            sa = sad4(o.y, d1, sa);
+            sa = sad4(o.z, d2, sa);
+            sa = sad4(o.w, d3, sa);
+            if (ra >= 8 && g + 1 < ny) {
+                const uint4 ob = *(const uint4 *)(S.so + (ra - 8) * 4);
+                sb = sad4(ob.x, d0, sb);
+                sb = sad4(ob.y, d1, sb);
+                sb = sad4(ob.z, d2, sb);
+                sb = sad4(ob.w, d3, sb);
             }
-            if (lane < nc) {
-                S.evals++;
-                const u64 cost = ((u64)sad << 16) + (u64)((lk_bits(mx) + lk_bits(my)) * S.lambda);
-                const u64 key = (cost << LK_LIST_BITS) | (u64)(gy * nx + c0 + lane);
-                kmin = key < kmin ? key : kmin;
+            if (ra == 15) {
+                if (lane < nc) {
+                    S.evals++;
+                    const int my = y0 + 8 * g;
+                    const u64 cost = ((u64)sa << 16) + (u64)((lk_bits(mx) + lk_bits(my)) * S.lambda);
+                    const u64 key = (cost << LK_LIST_BITS) | (u64)(g * nx + c0 + lane);
+                    kmin = key < kmin ? key : kmin;
+                }
+                sa = sb;
+                sb = 0;
+                g++;
+                ra = 8;
+                if (g >= ny) break;
+            } else {
+                ra++;
             }
         }
     }
