@@ -117,3 +117,17 @@ def test_intra_lattice_host_entry_matches_device_entry(gpu):
         got_satd, got_q = gpu.intra_lattice_host(big_org[:, 8:8 + Wp], rec, sub, qps, ipf=1)
         assert np.array_equal(got_satd, want_satd)
         assert np.array_equal(got_q, want_q)
+
+
+def test_intra_lattice_host_entry_in_ranges_at_1080p(gpu):
+    # a 1080p call (468,750 CUs) runs as four CU ranges whose record downloads overlap the next
+    # range's lattice; the records equal one device-entry launch over all CUs
+    org = intra_frame(W, H, seed=21)
+    rec = np.clip(org.astype(int) + np.random.default_rng(22).integers(-5, 6, org.shape), 0, 255).astype(np.uint8)
+    cus = gpu.lattice_cus(W, H)
+    assert len(cus) >= 4 * 65536
+    qps = [27, 32, 37, 42]
+    want_satd, want_q = gpu.intra_lattice(org, rec, cus, qps)
+    got_satd, got_q = gpu.intra_lattice_host(org, rec, cus, qps)
+    assert np.array_equal(got_satd, want_satd)
+    assert np.array_equal(got_q.view(np.uint8), want_q.view(np.uint8))

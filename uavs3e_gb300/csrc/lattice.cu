@@ -330,9 +330,14 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
 
 // host-buffer entry: per device, the device copies of the inputs and outputs (grown as needed)
 // and a stream of its own; calls on one device are serialised by its mutex
+constexpr int LAT_HOST_CHUNKS = 4;       // CU ranges whose record downloads overlap the next range's lattice
+constexpr int LAT_HOST_CHUNK_MIN = 65536; // CUs below which a call runs as one range
+
 struct LatHost {
     std::mutex mu;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr;               // the lattice launches
+    cudaStream_t cp = nullptr;               // the record downloads
+    cudaEvent_t ev[LAT_HOST_CHUNKS] = {};
     u8 *org = nullptr, *rec = nullptr;
     LatCu *cus = nullptr;
     u32 *satd = nullptr;
@@ -434,15 +439,36 @@ UAVS3E_CUDA_API int uavs3e_cuda_intra_lattice(const uint8_t *org, int i_org, con
         (r = grow(&S.cus, &S.cu_cap, (size_t)n_cus)) || (r = grow(&S.satd, &S.satd_cap, (size_t)n_cus * 33)) ||
         (r = grow(&S.q, &S.q_cap, nq)))
         return r;
+    if (!S.cp) {
+        UC_CHECK(cudaStreamCreateWithFlags(&S.cp, cudaStreamNonBlocking));
+        for (int c = 0; c < LAT_HOST_CHUNKS; c++) UC_CHECK(cudaEventCreateWithFlags(&S.ev[c], cudaEventDisableTiming));
+    }
     UC_CHECK(cudaMemcpy2DAsync(S.org, width, org, i_org, width, height, cudaMemcpyHostToDevice, S.st));
     UC_CHECK(cudaMemcpy2DAsync(S.rec, width, rec, i_rec, width, height, cudaMemcpyHostToDevice, S.st));
     UC_CHECK(cudaMemcpyAsync(S.cus, cus, (size_t)n_cus * sizeof(LatCu), cudaMemcpyHostToDevice, S.st));
-    r = launch_intra_lattice(S.org, width, S.rec, width, width, height, S.cus, n_cus, nullptr, 33, ipf, qps, n_qp,
-                             is_intra_slice, S.satd, n_qp > 0 ? S.q : nullptr, S.st);
-    if (r) return r;
-    UC_CHECK(cudaMemcpyAsync(satd, S.satd, (size_t)n_cus * 33 * sizeof(u32), cudaMemcpyDeviceToHost, S.st));
-    if (n_qp > 0)
-        UC_CHECK(cudaMemcpyAsync(q, S.q, (size_t)n_cus * 33 * n_qp * sizeof(LatQ), cudaMemcpyDeviceToHost, S.st));
+    // the records of a large call come back in CU ranges: range c's download (copy stream) overlaps
+    // range c + 1's lattice (compute stream); a range's records are contiguous because records go
+    // by CU index
+    const int nqp = n_qp > 0 ? n_qp : 0;
+    const int chunks = n_cus >= LAT_HOST_CHUNKS * LAT_HOST_CHUNK_MIN ? LAT_HOST_CHUNKS : 1;
+    for (int c = 0; c < chunks; c++) {
+        const int a = (int)((long long)n_cus * c / chunks), b = (int)((long long)n_cus * (c + 1) / chunks);
+        r = launch_intra_lattice(S.org, width, S.rec, width, width, height, S.cus + a, b - a, nullptr, 33, ipf, qps,
+                                 n_qp, is_intra_slice, S.satd + (size_t)a * 33,
+                                 nqp > 0 ? S.q + (size_t)a * 33 * nqp : nullptr, S.st);
+        if (r) {
+            cudaStreamSynchronize(S.cp);
+            return r;
+        }
+        UC_CHECK(cudaEventRecord(S.ev[c], S.st));
+        UC_CHECK(cudaStreamWaitEvent(S.cp, S.ev[c], 0));
+        UC_CHECK(cudaMemcpyAsync(satd + (size_t)a * 33, S.satd + (size_t)a * 33, (size_t)(b - a) * 33 * sizeof(u32),
+                                 cudaMemcpyDeviceToHost, S.cp));
+        if (nqp > 0)
+            UC_CHECK(cudaMemcpyAsync(q + (size_t)a * 33 * nqp, S.q + (size_t)a * 33 * nqp,
+                                     (size_t)(b - a) * 33 * nqp * sizeof(LatQ), cudaMemcpyDeviceToHost, S.cp));
+    }
+    UC_CHECK(cudaStreamSynchronize(S.cp));
     UC_CHECK(cudaStreamSynchronize(S.st));
     return UC_OK;
 }
