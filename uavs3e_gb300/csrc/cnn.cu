@@ -117,6 +117,13 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     __shared__ __align__(128) unsigned char sb[64 * TC_KC * 2];
     __shared__ __align__(8) u64 bar;
     __shared__ u32 s_tmem;
+    // index tables: the tile's rows (one per thread) and the chunk's columns, decomposed once
+    // instead of per gathered element (MODE 0: rows = output pixels {b Hin, oy s - pad, ox s - pad},
+    // column pairs = {ky, kx, ci}; MODE 1: rows = input pixels {b Hout, iy + pad, ix + pad},
+    // column pairs = {ky, kx, co}; MODE 2: rows = {ky, kx, ci}, columns = output pixels as MODE 0's
+    // rows); .w = 1 where the row / column exists
+    __shared__ int4 s_row[TC_M];
+    __shared__ int4 s_col[TC_KC];
     const ConvShape &S = T.S;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = MODE == 0 ? S.Cout : MODE == 1 ? S.Cin : S.Cout;
@@ -141,32 +148,95 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     u32 phase = 0;
     bool ok = true;
     const int npix = MODE == 2 ? S.B * S.Hout * S.Wout : 0;
+    // output pixel p -> {b Hin, oy s - pad, ox s - pad, exists}
+    auto out_pixel = [&](int p, int n) {
+        if (p >= n) return make_int4(0, 0, 0, 0);
+        const int hw = S.Hout * S.Wout, b = p / hw, rr = p - b * hw, oy = rr / S.Wout, ox = rr - oy * S.Wout;
+        return make_int4(b * S.Hin, oy * S.stride - S.pad, ox * S.stride - S.pad, 1);
+    };
+    {
+        const int row = r0 + tid;   // TC_THREADS == TC_M: one row per thread
+        if (MODE == 0) {
+            s_row[tid] = out_pixel(row, M);
+        } else if (MODE == 1) {
+            if (row < M) {
+                const int hw = S.Hin * S.Win, b = row / hw, rr = row - b * hw, iy = rr / S.Win, ix = rr - iy * S.Win;
+                s_row[tid] = make_int4(b * S.Hout, iy + S.pad, ix + S.pad, 1);
+            } else {
+                s_row[tid] = make_int4(0, 0, 0, 0);
+            }
+        } else {
+            if (row < S.K) {
+                const int tap = row / S.Cin, ci = row - tap * S.Cin, ky = tap / S.ks;
+                s_row[tid] = make_int4(ky, tap - ky * S.ks, ci, 1);
+            } else {
+                s_row[tid] = make_int4(0, 0, 0, 0);
+            }
+        }
+    }
+    const int sshift = S.stride == 2 ? 1 : 0;   // the network's strides are 1 and 2
 
     for (int k0 = 0; k0 < K && ok; k0 += TC_KC) {
         const int kc = min(TC_KC, K - k0);         // a multiple of 16
         const int kq = kc >> 3;                    // 16-byte units per row
+        // the chunk's column table (the previous chunk's MMAs have completed: see the wait below)
+        if (MODE == 2) {
+            for (int j = tid; j < kc; j += TC_THREADS) s_col[j] = out_pixel(kb + k0 + j, npix);
+        } else {
+            const int cdiv = MODE == 0 ? S.Cin : S.Cout, kmax = MODE == 0 ? S.K : K;
+            for (int j = tid; j < (kc >> 1); j += TC_THREADS) {
+                const int k = k0 + 2 * j;
+                if (k < kmax) {
+                    const int tap = k / cdiv, c = k - tap * cdiv, ky = tap / S.ks;
+                    s_col[j] = make_int4(ky, tap - ky * S.ks, c, 1);
+                } else {
+                    s_col[j] = make_int4(0, 0, 0, 0);
+                }
+            }
+        }
+        __syncthreads();
         // A: TC_M rows x kc columns; 8 consecutive threads write one 128-byte core matrix
         for (int u = tid; u < TC_M * kq; u += TC_THREADS) {
             const int r = (u & 7) + 8 * ((u >> 3) / kq), q = (u >> 3) % kq;
+            const int4 R = s_row[r];
             u32 v[4];
             if (MODE == 0) {
-                const int m = r0 + r;
-#pragma unroll
-                for (int i = 0; i < 4; i++) v[i] = m < M ? fwd_pair(T.src, S, m, k0 + 8 * q + 2 * i) : 0u;
-            } else if (MODE == 1) {
-                const int m = r0 + r;
-#pragma unroll
-                for (int i = 0; i < 4; i++) v[i] = m < M ? dgrad_pair(T.src, S, m, k0 + 8 * q + 2 * i) : 0u;
-            } else {
-                // row r = input-column index kk of x_col, columns = output pixels kb + k0 + 8q + j
-                const int kk = r0 + r;
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
-                    const int m = kb + k0 + 8 * q + 2 * i;
-                    const bf16 z = __float2bfloat16(0.f);
-                    const bf16 e0 = (kk < S.Kp && m < npix) ? fwd_elem(T.src, S, m, kk) : z;
-                    const bf16 e1 = (kk < S.Kp && m + 1 < npix) ? fwd_elem(T.src, S, m + 1, kk) : z;
-                    v[i] = pack_bf16(e0, e1);
+                    const int4 Cc = s_col[4 * q + i];
+                    const int iy = R.y + Cc.x, ix = R.z + Cc.y;
+                    v[i] = (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
+                               ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(R.x + iy) * S.Win + ix) * S.Cin + Cc.z)
+                               : 0u;
+                }
+            } else if (MODE == 1) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int4 Cc = s_col[4 * q + i];
+                    // the output pixel that read input pixel R through tap (ky, kx)
+                    const int ty = R.y - Cc.x, tx = R.z - Cc.y;
+                    const bool hit = (R.w & Cc.w) && ty >= 0 && tx >= 0 &&
+                                     (sshift ? !((ty | tx) & 1) : S.stride == 1 || (ty % S.stride == 0 && tx % S.stride == 0));
+                    const int oy = sshift ? ty >> 1 : S.stride == 1 ? ty : ty / S.stride;
+                    const int ox = sshift ? tx >> 1 : S.stride == 1 ? tx : tx / S.stride;
+                    v[i] = hit && oy < S.Hout && ox < S.Wout
+                               ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(R.x + oy) * S.Wout + ox) * S.Cout + Cc.z)
+                               : 0u;
+                }
+            } else {
+                // row r = input-column index (tap, ci) of x_col, columns = output pixels kb + k0 + 8q + j
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    bf16 e[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int4 Cc = s_col[8 * q + 2 * i + h];
+                        const int iy = Cc.y + R.x, ix = Cc.z + R.y;
+                        e[h] = (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
+                                   ? T.src[((size_t)(Cc.x + iy) * S.Win + ix) * S.Cin + R.z]
+                                   : __float2bfloat16(0.f);
+                    }
+                    v[i] = pack_bf16(e[0], e[1]);
                 }
             }
             *reinterpret_cast<uint4 *>(sa + umma_tile_off(r, 8 * q, kc)) = make_uint4(v[0], v[1], v[2], v[3]);
