@@ -331,14 +331,23 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     if (warp == 0) tmem_dealloc(tmem, (u32)ncols);
 }
 
-// bias gradient db[co] += sum_m dy[m][co]
-__global__ void k_conv_bgrad(const bf16 *dy, int M, int C, float *db)
+// bias gradient db[co] += sum_m dy[m][co]: a CTA of 256 threads walks rows m in steps of
+// rows = 256 / C (thread t < rows C takes channel t % C of row t / C), sums its channels in shared
+// memory and adds them to db with one atomic per channel
+__global__ void __launch_bounds__(256) k_conv_bgrad(const bf16 *dy, int M, int C, float *db)
 {
-    const int co = threadIdx.x % C, lane_rows = blockDim.x / C;
+    __shared__ float s_part[256];
+    const int co = threadIdx.x % C, rows = 256 / C, r0 = threadIdx.x / C;
     float s = 0.f;
-    for (int m = blockIdx.x * lane_rows + threadIdx.x / C; m < M; m += gridDim.x * lane_rows)
-        s += __bfloat162float(dy[(size_t)m * C + co]);
-    atomicAdd(&db[co], s);
+    if (r0 < rows)   // C = 48 leaves the last 16 threads idle
+        for (int m = blockIdx.x * rows + r0; m < M; m += gridDim.x * rows) s += __bfloat162float(dy[(size_t)m * C + co]);
+    s_part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float t = 0.f;
+        for (int r = 0; r < rows; r++) t += s_part[r * C + threadIdx.x];
+        atomicAdd(&db[threadIdx.x], t);
+    }
 }
 
 // wt[ci][tap * Cout + co] = w[co][tap * Cin + ci] (the data gradient's weight matrix)
@@ -370,58 +379,58 @@ __global__ void k_cnn_input(const pel *pic, int stride, int W, int H, const int 
 // Writes dlogits (bf16, scaled by 1/B) and adds the CTU's loss parts to loss[4].
 constexpr int HEAD_C = 48;
 
-__global__ void k_cnn_head_loss(const float *logits, const u8 *labels, int B, bf16 *dlog, float *loss)
+__global__ void __launch_bounds__(256) k_cnn_head_loss(const float *logits, const u8 *labels, int B, bf16 *dlog,
+                                                        float *loss)
 {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
-    const float *L = logits + (size_t)b * 16 * HEAD_C;
-    const u8 *lab = labels + (size_t)b * 40;    // [0] s64, [1..4] s32, [5..20] s16, [21..36] mode
-    bf16 *D = dlog + (size_t)b * 16 * HEAD_C;
+    // a half-warp per CTU, a lane per 4x4 cell c = cy * 4 + cx; the split sums over the CTU and
+    // over each 2x2-cell quadrant are shuffles within the half-warp (quadrant cells are lanes
+    // c, c ^ 1, c ^ 4, c ^ 5)
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, b = t >> 4, c = t & 15;
+    const bool act = b < B;
+    const float *L = logits + ((size_t)(act ? b : 0) * 16 + c) * HEAD_C;
+    const u8 *lab = labels + (size_t)(act ? b : 0) * 40;   // [0] s64, [1..4] s32, [5..20] s16, [21..36] mode
     const float inv = 1.f / B;
-    float l64 = 0.f, l32 = 0.f, l16 = 0.f, lm = 0.f;
-    float grad[16][HEAD_C];
-#pragma unroll 1
-    for (int c = 0; c < 16; c++)
-        for (int k = 0; k < HEAD_C; k++) grad[c][k] = 0.f;
-    {   // split64
-        float s = 0.f;
-        for (int c = 0; c < 16; c++) s += L[c * HEAD_C + 2];
-        s /= 16.f;
-        const float p = 1.f / (1.f + expf(-s)), y = (float)lab[0];
-        l64 = fmaxf(s, 0.f) - s * y + log1pf(expf(-fabsf(s)));
-        for (int c = 0; c < 16; c++) grad[c][2] = (p - y) / 16.f;
+    auto bce = [](float s, float y) { return fmaxf(s, 0.f) - s * y + log1pf(expf(-fabsf(s))); };
+    // split64: the mean of the 16 cells' part
+    float s64 = L[2];
+#pragma unroll
+    for (int d = 1; d < 16; d <<= 1) s64 += __shfl_xor_sync(0xffffffffu, s64, d);
+    s64 /= 16.f;
+    const float y64 = (float)lab[0];
+    // split32: the mean over the cell's quadrant
+    const int q = (c >> 3) * 2 + ((c & 3) >> 1);
+    float s32 = L[1];
+    s32 += __shfl_xor_sync(0xffffffffu, s32, 1);
+    s32 += __shfl_xor_sync(0xffffffffu, s32, 4);
+    s32 /= 4.f;
+    const float y32 = (float)lab[1 + q];
+    // split16 and the 33 mode logits of the cell
+    const float s16 = L[0], y16 = (float)lab[5 + c];
+    float mx = -1e30f;
+    for (int k = 0; k < 33; k++) mx = fmaxf(mx, L[3 + k]);
+    float z = 0.f;
+    for (int k = 0; k < 33; k++) z += expf(L[3 + k] - mx);
+    const int ym = lab[21 + c];
+    float part[4] = { c == 0 ? bce(s64, y64) : 0.f, (c == 0 || c == 2 || c == 8 || c == 10) ? bce(s32, y32) / 4.f : 0.f,
+                      bce(s16, y16) / 16.f, (logf(z) + mx - L[3 + ym]) / 16.f };
+    if (act) {
+        bf16 *D = dlog + ((size_t)b * 16 + c) * HEAD_C;
+        const float p16 = 1.f / (1.f + expf(-s16)), p32 = 1.f / (1.f + expf(-s32)), p64 = 1.f / (1.f + expf(-s64));
+        D[0] = __float2bfloat16((p16 - y16) / 16.f * inv);
+        D[1] = __float2bfloat16((p32 - y32) / 4.f / 4.f * inv);
+        D[2] = __float2bfloat16((p64 - y64) / 16.f * inv);
+        for (int k = 0; k < 33; k++)
+            D[3 + k] = __float2bfloat16((expf(L[3 + k] - mx) / z - (k == ym ? 1.f : 0.f)) / 16.f * inv);
+        for (int k = 36; k < HEAD_C; k++) D[k] = __float2bfloat16(0.f);
     }
-    for (int q = 0; q < 4; q++) {   // split32, quadrant q = (qy, qx) of 2x2 cells
-        const int qy = q >> 1, qx = q & 1;
-        float s = 0.f;
-        for (int dy = 0; dy < 2; dy++)
-            for (int dx = 0; dx < 2; dx++) s += L[((2 * qy + dy) * 4 + 2 * qx + dx) * HEAD_C + 1];
-        s /= 4.f;
-        const float p = 1.f / (1.f + expf(-s)), y = (float)lab[1 + q];
-        l32 += fmaxf(s, 0.f) - s * y + log1pf(expf(-fabsf(s)));
-        for (int dy = 0; dy < 2; dy++)
-            for (int dx = 0; dx < 2; dx++) grad[(2 * qy + dy) * 4 + 2 * qx + dx][1] = (p - y) / 4.f / 4.f;
+    // the loss parts summed over the warp (two CTUs), one atomic per part and warp
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float v = act ? part[i] * inv : 0.f;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&loss[i], v);
     }
-    for (int c = 0; c < 16; c++) {   // split16 and modes
-        const float s = L[c * HEAD_C + 0];
-        const float p = 1.f / (1.f + expf(-s)), y = (float)lab[5 + c];
-        l16 += fmaxf(s, 0.f) - s * y + log1pf(expf(-fabsf(s)));
-        grad[c][0] = (p - y) / 16.f;
-        float mx = -1e30f;
-        for (int k = 0; k < 33; k++) mx = fmaxf(mx, L[c * HEAD_C + 3 + k]);
-        float z = 0.f;
-        for (int k = 0; k < 33; k++) z += expf(L[c * HEAD_C + 3 + k] - mx);
-        const int ym = lab[21 + c];
-        lm += logf(z) + mx - L[c * HEAD_C + 3 + ym];
-        for (int k = 0; k < 33; k++) grad[c][3 + k] = (expf(L[c * HEAD_C + 3 + k] - mx) / z - (k == ym ? 1.f : 0.f)) / 16.f;
-    }
-    l32 /= 4.f; l16 /= 16.f; lm /= 16.f;
-    for (int c = 0; c < 16; c++)
-        for (int k = 0; k < HEAD_C; k++) D[c * HEAD_C + k] = __float2bfloat16(grad[c][k] * inv);
-    atomicAdd(&loss[0], l64 * inv);
-    atomicAdd(&loss[1], l32 * inv);
-    atomicAdd(&loss[2], l16 * inv);
-    atomicAdd(&loss[3], lm * inv);
 }
 
 // Adam on FP32 master weights; refreshes the bf16 copy.  Entries of a weight row beyond the
@@ -521,8 +530,7 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_wgrad(const void *dy, const void *x, fl
     dim3 grid((Kp + TC_M - 1) / TC_M, (M + WG_CHUNK - 1) / WG_CHUNK);
     k_conv_tc<2><<<grid, TC_THREADS, TC_SMEM_RESERVE, st>>>(T);
     UC_CHECK(cudaGetLastError());
-    const int rows = 256 / Cout;
-    k_conv_bgrad<<<std::min(1024, (M + rows - 1) / rows), rows * Cout, 0, st>>>((const bf16 *)dy, M, Cout, db);
+    k_conv_bgrad<<<std::min(256, (M + 255) / 256), 256, 0, st>>>((const bf16 *)dy, M, Cout, db);
     UC_CHECK(cudaGetLastError());
     count_launch(2);
     return UC_OK;
@@ -560,7 +568,7 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_head_loss(const float *logits, const uint8_t
     if (!logits || !labels || !dlogits || !loss || B <= 0) return set_status(UC_ERR_ARG, "cnn_head_loss");
     cudaStream_t st = (cudaStream_t)stream;
     UC_CHECK(cudaMemsetAsync(loss, 0, 4 * sizeof(float), st));
-    k_cnn_head_loss<<<(B + 63) / 64, 64, 0, st>>>(logits, labels, B, (bf16 *)dlogits, loss);
+    k_cnn_head_loss<<<(B * 16 + 255) / 256, 256, 0, st>>>(logits, labels, B, (bf16 *)dlogits, loss);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     return UC_OK;
