@@ -530,7 +530,7 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_wgrad(const void *dy, const void *x, fl
     dim3 grid((Kp + TC_M - 1) / TC_M, (M + WG_CHUNK - 1) / WG_CHUNK);
     k_conv_tc<2><<<grid, TC_THREADS, TC_SMEM_RESERVE, st>>>(T);
     UC_CHECK(cudaGetLastError());
-    k_conv_bgrad<<<std::min(256, (M + 255) / 256), 256, 0, st>>>((const bf16 *)dy, M, Cout, db);
+    k_conv_bgrad<<<std::min(1024, (M + 255) / 256), 256, 0, st>>>((const bf16 *)dy, M, Cout, db);
     UC_CHECK(cudaGetLastError());
     count_launch(2);
     return UC_OK;
