@@ -1046,6 +1046,8 @@ def pruning_leg(steps=3000):
     search, share of the lattice's work it searches, GPU time of the pruned lattice)"""
     from uavs3e_gb300 import cnn
     r = cnn.experiment(steps=steps)
+    # the same network trained on the reference encoder's own CU decisions (committed fixture)
+    r["encoder_labels"] = cnn.encoder_label_experiment(os.path.join(ROOT, "tests", "golden", "encoder_labels.npz"))
     r["workload"] = ("CNN 2 -> 16/32/32/64 ch (3x3, stride 2) + 1x1 head, bf16 tcgen05 tensor cores with FP32 "
                      "accumulation in TMEM; labels: quad-tree + mode decisions from the lattice's RD costs at QP 32")
     # one training step at a batch of 1,024 CTUs against the measured bf16 tensor peak

@@ -599,3 +599,31 @@ void refk_affine_merge(s64 ptr, const s64 *ref0_ptr, s64 *col_list_ptr, s16 *map
         }
     }
 }
+
+/* ---- the encoder's final CU decisions (labels for the pruning network) ----
+ * lbac_enc_unit (src/entropy.c:2461) codes each final CU of a picture into the bitstream; the
+ * library is linked with --wrap=lbac_enc_unit, so the CU tree's calls (src/uavs3e.c:646) come
+ * here first.  With UAVS3E_CU_LOG set, each call appends "x y w h intra ipm" (luma position and
+ * size, 1 for an intra CU, its first luma prediction mode) to that file. */
+int __real_lbac_enc_unit(lbac_t *lbac, bs_t *bs, core_t *core, enc_cu_t *cu_data, int x, int y, int cup, int cu_width,
+                         int cu_height);
+
+int __wrap_lbac_enc_unit(lbac_t *lbac, bs_t *bs, core_t *core, enc_cu_t *cu_data, int x, int y, int cup, int cu_width,
+                         int cu_height)
+{
+    static FILE *log_file;
+    static int log_init;
+    const int r = __real_lbac_enc_unit(lbac, bs, core, cu_data, x, y, cup, cu_width, cu_height);
+    if (!log_init) {
+        const char *path = getenv("UAVS3E_CU_LOG");
+        if (path) log_file = fopen(path, "a");
+        log_init = 1;
+    }
+    if (log_file) {
+        const com_mode_t *m = &core->mod_info_curr;
+        fprintf(log_file, "%d %d %d %d %d %d\n", x, y, cu_width, cu_height, m->cu_mode == MODE_INTRA,
+                (int)m->ipm[0][0]);
+        fflush(log_file);
+    }
+    return r;
+}

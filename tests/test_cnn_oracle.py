@@ -126,3 +126,35 @@ def test_search_rd_full_and_keep_everything_agree():
              np.tile(np.argsort(-J.mean(0))[:8], (n, 16, 1)))
     pr = cnn.search_rd(J, S, R, cus, xy, worst, 0.9, qp)
     assert pr[0] + lam * pr[1] >= jf - 1e-6 * jf and pr[2] < 1.0
+
+
+def test_encoder_label_fixture_and_derivation():
+    """the committed labels from the reference encoder's CU decisions: shapes, value ranges, and
+    the derivation on a hand-made CU list"""
+    import os
+    import sys
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, golden)
+    import make_encoder_labels as mel
+    d = np.load(os.path.join(golden, "encoder_labels.npz"))
+    lab = d["labels"]
+    assert lab.shape == (len(d["seeds"]), len(d["qps"]), (int(d["width"]) // 64) * (int(d["height"]) // 64), 40)
+    assert lab[..., :21].max() <= 1 and lab[..., 21:37].max() <= 32
+    # an unsplit CTU implies unsplit quadrants and cells
+    whole = lab[..., 0] == 0
+    assert not lab[whole][:, 1:21].any()
+    # a 128x64 picture: CTU 0 one 64x64 CU (mode 7); CTU 1 four 32x32 CUs, the first split into
+    # 16x16 CUs (modes 3), the others 32x32 (mode 12)
+    cus = [(0, 0, 64, 64, 1, 7)]
+    for q in range(4):
+        x, y = 64 + 32 * (q & 1), 32 * (q >> 1)
+        if q == 0:
+            cus += [(x + 16 * (k & 1), y + 16 * (k >> 1), 16, 16, 1, 3) for k in range(4)]
+        else:
+            cus.append((x, y, 32, 32, 1, 12))
+    labels, xy = mel.ctu_labels(np.array(cus), 128, 64)
+    assert xy.tolist() == [[0, 0], [64, 0]]
+    assert labels[0, 0] == 0 and not labels[0, 1:21].any() and (labels[0, 21:37] == 7).all()
+    assert labels[1, 0] == 1 and labels[1, 1:5].tolist() == [1, 0, 0, 0]
+    assert not labels[1, 5:21].any()
+    assert labels[1, 21] == 3 and labels[1, 23] == 12

@@ -133,3 +133,17 @@ def test_pruning_beats_the_method_without_the_network(gpu):
     assert net["rd_cost_increase"] < prior["rd_cost_increase"]
     assert net["work_fraction"] < 0.5
     assert r["pruned_lattice_tau0.9"]["speedup"] > 1.5
+
+
+def test_network_learns_the_reference_encoders_decisions(gpu):
+    # trained on the reference encoder's own final CUs (committed fixture of seeded 512x256
+    # I-frames at 4 QPs), evaluated on its held-out frames: a better mode shortlist and 64x64
+    # split decision than the method without the network
+    import os
+    from uavs3e_gb300 import cnn
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "encoder_labels.npz")
+    r = cnn.encoder_label_experiment(path, steps=800, batch=64)
+    assert r["loss_last"] < 0.6 * r["loss_first"]
+    assert r["net"]["mode_top8_recall"] > r["prior"]["mode_top8_recall"] + 0.1
+    assert r["net"]["split64_acc"] >= r["prior"]["split64_acc"]
+    assert 0.0 < r["rd_model_agreement"]["split64"] <= 1.0

@@ -633,6 +633,60 @@ def experiment(train_seeds=range(100, 116), test_seeds=(900,), qp=32, steps=3000
     return out
 
 
+def encoder_label_experiment(path, steps=2000, batch=128, seed=0):
+    """the network trained on the reference encoder's own CU decisions (the fixture written by
+    tests/golden/make_encoder_labels.py: seeded 512x256 I-frames coded at 4 QPs) and evaluated on
+    its held-out frames against the method without the network; also how often the lattice's RD
+    model (the labels of experiment()) agrees with the encoder's decisions on the same frames"""
+    import torch
+    from .synth import intra_frame
+    d = np.load(path)
+    seeds, qps, labels, xy = d["seeds"], d["qps"], d["labels"], d["xy"]
+    W, H, n_train = int(d["width"]), int(d["height"]), int(d["n_train"])
+    ctus = [np.stack([f[y:y + 64, x:x + 64] for x, y in xy]) for f in (intra_frame(W, H, seed=int(s)) for s in seeds)]
+    nf, nq = len(seeds), len(qps)
+    tr = [(f, qi) for f in range(n_train) for qi in range(nq)]
+    X = np.concatenate([ctus[f] for f, _ in tr])
+    Y = np.concatenate([labels[f, qi] for f, qi in tr])
+    Q = np.concatenate([np.full(len(xy), int(qps[qi]), np.int32) for _, qi in tr])
+    net = PruneNet(batch, seed=seed)
+    hist = train(net, X, Y, qp=Q, steps=steps, seed=seed)
+    out = {"frames": f"{nf} seeded {W}x{H} I-frames ({n_train} training, {nf - n_train} held out), QP "
+                     f"{', '.join(str(int(q)) for q in qps)}: the reference encoder's final CUs",
+           "train_samples": int(len(X)), "steps": steps, "loss_first": hist[0], "loss_last": float(np.mean(hist[-20:])),
+           "encoder_label_rates": {"split64": float(Y[:, 0].mean()), "split32": float(Y[:, 1:5].mean()),
+                                   "split16": float(Y[:, 5:21].mean())}}
+    prior = None
+    for name in ("net", "prior"):
+        acc = {"split64_acc": [], "split32_acc": [], "split16_acc": [], "mode_top8_recall": []}
+        for f in range(n_train, nf):
+            for qi in range(nq):
+                lab = labels[f, qi]
+                if name == "net":
+                    p64, p32, p16, top = predict(net, ctus[f], int(qps[qi]))
+                else:
+                    p64, p32, p16, top = prior_predictions(Y, len(lab))
+                acc["split64_acc"].append(((p64 > 0.5) == lab[:, 0].astype(bool)).mean())
+                acc["split32_acc"].append(((p32 > 0.5) == lab[:, 1:5].astype(bool)).mean())
+                acc["split16_acc"].append(((p16 > 0.5) == lab[:, 5:21].astype(bool)).mean())
+                acc["mode_top8_recall"].append((top == lab[:, 21:37, None]).any(2).mean())
+        out[name] = {k: float(np.mean(v)) for k, v in acc.items()}
+    # the lattice RD model's decisions on the same frames against the encoder's
+    agree = {"split64": [], "split32": [], "split16": [], "mode": []}
+    for f in range(nf):
+        frame = intra_frame(W, H, seed=int(seeds[f]))
+        dq = frame_dataset_qps(frame, tuple(int(q) for q in qps))
+        for qi, q in enumerate(qps):
+            pl = dq[int(q)][1]
+            el = labels[f, qi]
+            agree["split64"].append((pl[:, 0] == el[:, 0]).mean())
+            agree["split32"].append((pl[:, 1:5] == el[:, 1:5]).mean())
+            agree["split16"].append((pl[:, 5:21] == el[:, 5:21]).mean())
+            agree["mode"].append((pl[:, 21:37] == el[:, 21:37]).mean())
+    out["rd_model_agreement"] = {k: float(np.mean(v)) for k, v in agree.items()}
+    return out
+
+
 if __name__ == "__main__":
     import json
     from . import build, init
