@@ -800,8 +800,12 @@ template <int STAGE>
 __global__ void __launch_bounds__(256, 3) k_me_sub_eval(MeSubParams P, int n_threads)
 {
     constexpr int NC = STAGE == 1 ? 9 : 8;
+    // candidate-major order: consecutive threads take consecutive tiles with the same candidate,
+    // so the tiles of one block (sharing its winner, hence its plane and offset) read adjacent
+    // columns of the same rows
+    const int n_items = n_threads / NC;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_threads; t += gridDim.x * blockDim.x) {
-        const int it = t / NC, c = t - it * NC;
+        const int c = t / n_items, it = t - c * n_items;
         SubItem I;
         decode_sub_item(P, it, I);
         const pel *ptr[4];
