@@ -37,12 +37,13 @@ def write_yuv(path, n_frames=8):
             f.write(np.clip(d - 16, 0, 255).astype(np.uint8).tobytes())
 
 
-def encode(tmp, tag, env_extra=None, n_frames=8, timeout=600):
+def encode(tmp, tag, env_extra=None, n_frames=8, timeout=600, wpp_threads=1):
     env = dict(os.environ)
     env.update(env_extra or {})
     bs, rec = os.path.join(tmp, tag + ".bin"), os.path.join(tmp, tag + "_rec.yuv")
     cmd = [ENC, "-i", os.path.join(tmp, "in.yuv"), "-w", "416", "-h", "240", "-d", "8", "-f", str(n_frames), "-q", "37",
-           "-p", "0", "-g", "0", "--ctu_size", "64", "--wpp_threads", "1", "--frm_threads", "1", "--fps_num", "30",
+           "-p", "0", "-g", "0", "--ctu_size", "64", "--wpp_threads", str(wpp_threads), "--frm_threads", "1",
+           "--fps_num", "30",
            "--fps_den", "1", "-v", "0", "-o", bs, "-r", rec]
     # the encoder writes psnr.txt into its working directory: run it inside the test's folder
     r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=timeout, cwd=tmp)
@@ -97,3 +98,16 @@ def test_cost_calls_of_the_oracle_table_match_the_reference(tmp_path):
     _, log = encode(tmp, "planted", {"LD_PRELOAD": SHIM, "UAVS3E_DROPIN_COSTLOG": "1", "UAVS3E_DROPIN_PLANT": "satd"},
                     n_frames=2)
     assert costlog(log)[5] != ref_log[5]
+
+
+def test_oracle_kernel_table_under_wavefront_threads(tmp_path):
+    # 4 WPP threads share the kernel table: one frame through the oracle table gives the
+    # reference's 4-thread bitstream (the reference's own output is the same on every run)
+    tmp = str(tmp_path)
+    write_yuv(os.path.join(tmp, "in.yuv"), 1)
+    plain, _ = encode(tmp, "plain4", n_frames=1, wpp_threads=4)
+    again, _ = encode(tmp, "again4", n_frames=1, wpp_threads=4)
+    assert again == plain
+    dropin, log = encode(tmp, "dropin4", {"LD_PRELOAD": SHIM}, n_frames=1, wpp_threads=4)
+    assert "kernel table replaced by the oracle restatement" in log
+    assert dropin == plain

@@ -52,3 +52,17 @@ def test_reference_encoder_on_gpu_entries_gives_the_reference_bitstream(gpu, tmp
     print(f"\ndrop-in encode, {n} frames: md5 {plain[0]} (both); reference C table {t1 - t0:.1f} s, "
           f"GPU entries {t2 - t1:.1f} s, {m.group(3)} kernel launches; cost calls {sum(ref_costs[:5])} "
           f"(sad, x3, x4, ssd, satd = {ref_costs[:5]}), record hash {ref_costs[5]} (both)")
+
+
+def test_gpu_entries_under_wavefront_threads(gpu, tmp_path):
+    # the encoder's WPP threads call the shared kernel table concurrently; each thread stages its
+    # calls separately (per-thread buffers and stream), so one frame coded with 4 threads on the
+    # GPU entries gives the reference's 4-thread bitstream
+    tmp = str(tmp_path)
+    write_yuv(os.path.join(tmp, "in.yuv"), 1)
+    plain, _ = encode(tmp, "plain4", n_frames=1, wpp_threads=4)
+    got, log = encode(tmp, "gpu4", {"LD_PRELOAD": PRELOAD}, n_frames=1, timeout=3600, wpp_threads=4)
+    assert "kernel table installed (GPU entries)" in log
+    m = re.search(r"uavs3e_cuda_preload: status (-?\d+) \(([^)]*)\), (\d+) kernel launches", log)
+    assert m and int(m.group(1)) == 0, log[-2000:]
+    assert got == plain, f"md5 (bitstream, reconstruction) {got} != reference {plain}"
