@@ -776,10 +776,13 @@ __device__ __forceinline__ void decode_sub_item(const MeSubParams &P, int it, Su
         I.ok[j] = false; I.item[j] = 0; I.bx[j] = 0; I.by[j] = 0; I.ctu[j] = 0; I.b[j] = 0;
         if (j >= I.nb) continue;
         const int sh = kClassShapes[c][j];
+        // block sides are powers of two: positions within the CTU by shifts (a division by a
+        // table value would compile to a full integer division)
         const int w = kShapeWH[sh][0], h = kShapeWH[sh][1];
+        const int lw = 31 - __clz(w), lh = 31 - __clz(h);
         const int bx = I.px & ~(w - 1), by = I.py & ~(h - 1);
         const int ctu = (by >> 6) * P.ctus_w + (bx >> 6);
-        const int b = kShapeFirst[sh] + ((by & 63) / h) * (ME_CTU / w) + ((bx & 63) / w);
+        const int b = kShapeFirst[sh] + (((by & 63) >> lh) << (6 - lw)) + ((bx & 63) >> lw);
         I.bx[j] = bx; I.by[j] = by; I.ctu[j] = ctu; I.b[j] = b;
         I.item[j] = (ctu * ME_BLOCKS_PER_CTU + b) * P.n_refs + I.ref;
         I.ok[j] = bx + w <= P.W && by + h <= P.H;
