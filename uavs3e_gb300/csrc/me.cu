@@ -596,6 +596,7 @@ struct MeSubParams {
     u32 *satd2;          // [item][8]
     u32 *hpel;           // [item]: stage-1 winner (mx, my)
     int cls_base[4], cls_nx[3];   // refinement items per tile class (per reference), tiles per row
+    u32 cls_nx_inv[3];            // floor(2^32 / cls_nx) + 1 (nx > 1): r / nx = umulhi(r, inv) for r nx < 2^32
     const u32 *ctl;      // the integer search's control words ([1] != 0xFFFFFFFF: it gave up)
     MeResult *out;
 };
@@ -761,15 +762,17 @@ struct SubItem {
 
 __device__ __forceinline__ void decode_sub_item(const MeSubParams &P, int it, SubItem &I)
 {
-    I.ref = it % P.n_refs;
-    int rest = it / P.n_refs;
+    // two references (the usual case) by a shift
+    I.ref = P.n_refs == 2 ? (it & 1) : it % P.n_refs;
+    int rest = P.n_refs == 2 ? (it >> 1) : it / P.n_refs;
     int c = 0;
     while (c < 2 && rest >= P.cls_base[c + 1]) c++;
     rest -= P.cls_base[c];
     I.cls = c;
     I.tw = c == 1 ? 16 : 8; I.th = c == 2 ? 16 : 8;
     const int nx = P.cls_nx[c];
-    I.px = (rest % nx) * I.tw; I.py = (rest / nx) * I.th;
+    const int ry = nx > 1 ? (int)__umulhi((u32)rest, P.cls_nx_inv[c]) : rest;
+    I.px = (rest - ry * nx) * I.tw; I.py = ry * I.th;
     I.nb = c == 0 ? 4 : 3;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
@@ -1015,7 +1018,11 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     const int cnx[3] = { (a.W + 7) / 8, (a.W + 15) / 16, (a.W + 7) / 8 };
     const int cny[3] = { (a.H + 7) / 8, (a.H + 7) / 8, (a.H + 15) / 16 };
     S.cls_base[0] = 0;
-    for (int c = 0; c < 3; c++) { S.cls_nx[c] = cnx[c]; S.cls_base[c + 1] = S.cls_base[c] + cnx[c] * cny[c]; }
+    for (int c = 0; c < 3; c++) {
+        S.cls_nx[c] = cnx[c];
+        S.cls_nx_inv[c] = cnx[c] > 1 ? (u32)((1ull << 32) / (unsigned long long)cnx[c] + 1) : 0u;   // nx = 1: ry = r
+        S.cls_base[c + 1] = S.cls_base[c] + cnx[c] * cny[c];
+    }
     const long long n_items = (long long)S.cls_base[3] * a.n_refs;
     if (n_items * 9 >= (1ll << 31)) return set_status(UC_ERR_ARG, "me: frame too large for the refinement grid");
     S.hpel = a.sub_scratch + items * 17;
