@@ -758,8 +758,8 @@ UAVS3E_CUDA_API int uavs3e_cuda_quant_wq_device(const uavs3e_cuda_rdoq_req_t *d_
 UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int y_f32,
                                              int batch, int hin, int win, int cin, int cout, int ks, int stride,
                                              int kp, int relu, void *stream);
-/* dx = (x > 0) * conv^T(dy, w): the gradient at the previous layer's pre-activation, bf16;
- * wt_scratch holds cin * ks * ks * cout bf16. */
+/* dx = (x > 0) * conv^T(dy, w): the gradient at the previous layer's pre-activation, bf16.
+ * wt_scratch is not used (the weights are read in place) and may be NULL. */
 UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_dgrad(const void *dy, const void *w, const void *x, void *dx, void *wt_scratch,
                                                int batch, int hin, int win, int cin, int cout, int ks, int stride,
                                                int kp, void *stream);

@@ -147,3 +147,58 @@ def test_network_learns_the_reference_encoders_decisions(gpu):
     assert r["net"]["mode_top8_recall"] > r["prior"]["mode_top8_recall"] + 0.1
     assert r["net"]["split64_acc"] >= r["prior"]["split64_acc"]
     assert 0.0 < r["rd_model_agreement"]["split64"] <= 1.0
+
+
+# single convolutions through the C ABI: stride 1 and 2, odd picture sizes (the data gradient's
+# phase classes then differ in size), 8-channel groups and channel counts that are not a
+# multiple of 8 (the element-wise gathers)
+CONV_SHAPES = [  # B, H, Cin, Cout, ks, stride
+    (16, 9, 16, 32, 3, 2),
+    (4, 12, 32, 16, 3, 1),
+    (16, 8, 8, 16, 3, 2),
+    (16, 10, 6, 16, 3, 2),
+    (16, 7, 2, 16, 3, 1),
+    (4, 4, 64, 48, 1, 1),
+]
+
+
+@pytest.mark.parametrize("B,H,Cin,Cout,ks,stride", CONV_SHAPES)
+def test_conv_layer_matches_oracle(gpu, B, H, Cin, Cout, ks, stride):
+    import torch
+    from uavs3e_gb300 import cnn
+    L = gpu.lib()
+    cnn._declare(L)
+    rng = np.random.default_rng(B * 1000 + H * 10 + Cin + stride)
+    Kp = cnn.kpad(Cin, ks)
+    K = ks * ks * Cin
+    Ho = (H + 2 * (ks // 2) - ks) // stride + 1
+    # a ReLU output: about a third of the inputs are 0 (the data gradient's mask)
+    x = cnn_ref.bf16(np.maximum(rng.normal(0.2, 1, (B, H, H, Cin)), 0).astype(np.float32))
+    w = np.zeros((Cout, Kp), np.float32)
+    w[:, :K] = cnn_ref.bf16(rng.normal(0, 0.3, (Cout, K)).astype(np.float32))
+    b = rng.normal(0, 0.1, Cout).astype(np.float32)
+    dy = cnn_ref.bf16(rng.normal(0, 1, (B, Ho, Ho, Cout)).astype(np.float32))
+    dev = lambda a, dt=torch.bfloat16: torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()  # noqa: E731
+    d_x, d_w, d_b, d_dy = dev(x), dev(w), dev(b, torch.float32), dev(dy)
+    d_y = torch.zeros((B, Ho, Ho, Cout), dtype=torch.bfloat16, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    assert L.uavs3e_cuda_cnn_conv_fwd(d_x.data_ptr(), d_w.data_ptr(), d_b.data_ptr(), d_y.data_ptr(), 0, B, H, H,
+                                      Cin, Cout, ks, stride, Kp, 1, st) == 0
+    d_dw = torch.zeros((Cout, Kp), dtype=torch.float32, device="cuda")
+    d_db = torch.zeros(Cout, dtype=torch.float32, device="cuda")
+    assert L.uavs3e_cuda_cnn_conv_wgrad(d_dy.data_ptr(), d_x.data_ptr(), d_dw.data_ptr(), d_db.data_ptr(), B, H, H,
+                                        Cin, Cout, ks, stride, Kp, st) == 0
+    need_dx = Cin % 16 == 0
+    if need_dx:
+        d_dx = torch.zeros((B, H, H, Cin), dtype=torch.bfloat16, device="cuda")
+        assert L.uavs3e_cuda_cnn_conv_dgrad(d_dy.data_ptr(), d_w.data_ptr(), d_x.data_ptr(), d_dx.data_ptr(),
+                                            None, B, H, H, Cin, Cout, ks, stride, Kp, st) == 0
+    torch.cuda.synchronize()
+    y_ref = cnn_ref.conv_fwd(x, w, b, ks, stride, relu=True)
+    dw_ref, db_ref, dx_ref = cnn_ref.conv_bwd(dy, x, w, ks, stride, need_dx=need_dx)
+    assert rel(d_y.float().cpu().numpy(), y_ref) < 1e-2
+    assert rel(d_dw.cpu().numpy(), dw_ref) < 1e-4
+    assert rel(d_db.cpu().numpy(), db_ref) < 1e-4
+    if need_dx:
+        assert rel(d_dx.float().cpu().numpy(), dx_ref) < 1e-2
+    assert L.uavs3e_cuda_cnn_timeouts() == 0

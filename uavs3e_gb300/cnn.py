@@ -73,22 +73,41 @@ class PruneNet:
             ho = (h + 2 * (ks // 2) - ks) // st + 1
             self.shapes.append((h, cin, cout, ks, st, kpad(cin, ks), ho))
             h = ho
-        self.w32 = [torch.from_numpy(w.copy()).to(dev) for w, _ in params]
-        self.b32 = [torch.from_numpy(b.copy()).to(dev) for _, b in params]
-        self.wbf = [w.to(torch.bfloat16) for w in self.w32]
-        self.mw = [torch.zeros_like(w) for w in self.w32]
-        self.vw = [torch.zeros_like(w) for w in self.w32]
-        self.mb = [torch.zeros_like(b) for b in self.b32]
-        self.vb = [torch.zeros_like(b) for b in self.b32]
-        self.gw = [torch.zeros_like(w) for w in self.w32]
-        self.gb = [torch.zeros_like(b) for b in self.b32]
+        # every layer's weights and biases are views of one flat FP32 buffer (and its moments,
+        # gradients and bf16 copy), so one Adam launch updates them all; each view starts on a
+        # multiple of 16 elements (Cout * Kp and Cout are), as the 16-byte gathers need
+        sizes = []
+        for w, b in params:
+            sizes += [w.size, b.size]
+        n = sum(sizes)
+        self.flat32 = torch.zeros(n, dtype=torch.float32, device=dev)
+        self.flat_m = torch.zeros_like(self.flat32)
+        self.flat_v = torch.zeros_like(self.flat32)
+        self.flat_g = torch.zeros_like(self.flat32)
+        self.flat_bf = torch.zeros(n, dtype=torch.bfloat16, device=dev)
+
+        def views(flat):
+            out, off = [], 0
+            for w, b in params:
+                out.append(flat[off:off + w.size].view(w.shape))
+                off += w.size
+                out.append(flat[off:off + b.size].view(b.shape))
+                off += b.size
+            return out[0::2], out[1::2]
+
+        self.w32, self.b32 = views(self.flat32)
+        for (w, b), dw, db in zip(params, self.w32, self.b32):
+            dw.copy_(torch.from_numpy(np.ascontiguousarray(w, np.float32)))
+            db.copy_(torch.from_numpy(np.ascontiguousarray(b, np.float32)))
+        self.flat_bf.copy_(self.flat32.to(torch.bfloat16))
+        self.wbf, _ = views(self.flat_bf)
+        self.gw, self.gb = views(self.flat_g)
         self.acts = [torch.zeros((B, 64, 64, 2), dtype=torch.bfloat16, device=dev)]
         for (h_in, cin, cout, ks, st, kp, ho) in self.shapes[:-1]:
             self.acts.append(torch.zeros((B, ho, ho, cout), dtype=torch.bfloat16, device=dev))
         self.logits = torch.zeros((B, 16, HEAD[1]), dtype=torch.float32, device=dev)
         self.dlog = torch.zeros((B, 16, HEAD[1]), dtype=torch.bfloat16, device=dev)
         self.dx = [torch.zeros_like(a) for a in self.acts]
-        self.wt = torch.zeros(64 * 9 * 64, dtype=torch.bfloat16, device=dev)
         self.loss = torch.zeros(4, dtype=torch.float32, device=dev)
         self.step_no = 0
 
@@ -124,7 +143,7 @@ class PruneNet:
                   "cnn_conv_wgrad")
             if i > 0:
                 check(self.L.uavs3e_cuda_cnn_conv_dgrad(dy.data_ptr(), self.wbf[i].data_ptr(), self.acts[i].data_ptr(),
-                                                        self.dx[i].data_ptr(), self.wt.data_ptr(), self.B, h, h, cin,
+                                                        self.dx[i].data_ptr(), None, self.B, h, h, cin,
                                                         cout, ks, s, kp, st), "cnn_conv_dgrad")
                 dy = self.dx[i]
         return self.loss
@@ -132,13 +151,10 @@ class PruneNet:
     def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
         st = self._stream()
         self.step_no += 1
-        for i in range(len(self.shapes)):
-            check(self.L.uavs3e_cuda_cnn_adam(self.w32[i].data_ptr(), self.mw[i].data_ptr(), self.vw[i].data_ptr(),
-                                              self.gw[i].data_ptr(), self.wbf[i].data_ptr(), self.w32[i].numel(), lr,
-                                              b1, b2, eps, self.step_no, st), "cnn_adam")
-            check(self.L.uavs3e_cuda_cnn_adam(self.b32[i].data_ptr(), self.mb[i].data_ptr(), self.vb[i].data_ptr(),
-                                              self.gb[i].data_ptr(), None, self.b32[i].numel(), lr, b1, b2, eps,
-                                              self.step_no, st), "cnn_adam")
+        # every weight and bias in one launch (the biases' bf16 copies are written but not read)
+        check(self.L.uavs3e_cuda_cnn_adam(self.flat32.data_ptr(), self.flat_m.data_ptr(), self.flat_v.data_ptr(),
+                                          self.flat_g.data_ptr(), self.flat_bf.data_ptr(), self.flat32.numel(), lr,
+                                          b1, b2, eps, self.step_no, st), "cnn_adam")
 
 
 def step_flops(B):

@@ -7,14 +7,16 @@
 //
 // Convolutions are implicit GEMMs on the 5th-generation tensor cores (tcgen05.mma, bf16 x bf16
 // with FP32 accumulation in tensor memory): forward (rows = output pixels, K = taps x input
-// channels), data gradient (rows = input pixels, K = taps x output channels, with the previous
-// layer's ReLU mask applied on store) and weight gradient, computed transposed (rows = taps x
-// input channels, N = output channels, K = output pixels, split over CTAs with FP32 atomics).  A
+// channels), data gradient (rows = the input pixels of one stride phase class, K = the taps that
+// class reaches x output channels, with the previous layer's ReLU mask applied on store) and
+// weight gradient, computed transposed (rows = taps x input channels plus a row of ones for the
+// bias gradient, N = output channels, K = output pixels, split over CTAs with FP32 atomics).  A
 // CTA of 128 threads owns a 128-row tile: it gathers the operands chunk by chunk (64 columns of
-// K) into shared memory in the MMA's K-major layout, one thread issues the MMAs into a TMEM
-// accumulator of 128 lanes x N columns, and the four warps read their 32 lanes back for the
-// epilogue.  Activations are NHWC bf16, weights [Cout][K] bf16 with FP32 master copies updated
-// by Adam.
+// K) into shared memory in the MMA's no-swizzle layouts (K-major for the forward and data
+// gradient, MN-major for the weight gradient, whichever makes 8 channels of one pixel one
+// 16-byte load), one thread issues the MMAs into a TMEM accumulator of 128 lanes x N columns,
+// and the four warps read their 32 lanes back for the epilogue.  Activations are NHWC bf16,
+// weights [Cout][K] bf16 with FP32 master copies updated by Adam.
 #include "common.cuh"
 #include "tma.cuh"
 #include "umma.cuh"
@@ -41,75 +43,44 @@ __device__ __forceinline__ u32 pack_bf16(bf16 lo, bf16 hi)
     return (u32)__bfloat16_as_ushort(lo) | ((u32)__bfloat16_as_ushort(hi) << 16);
 }
 
-// im2col element pair (k, k+1) of output pixel m (k even; the pair shares a tap because Cin is
-// even): two input channels of one input pixel, or 0 outside the picture / beyond K
-__device__ __forceinline__ u32 fwd_pair(const bf16 *x, const ConvShape &S, int m, int k)
-{
-    if (k >= S.K) return 0u;
-    const int hw = S.Hout * S.Wout;
-    const int b = m / hw, r = m - b * hw, oy = r / S.Wout, ox = r - oy * S.Wout;
-    const int tap = k / S.Cin, ci = k - tap * S.Cin;
-    const int ky = tap / S.ks, kx = tap - ky * S.ks;
-    const int iy = oy * S.stride + ky - S.pad, ix = ox * S.stride + kx - S.pad;
-    if (iy < 0 || iy >= S.Hin || ix < 0 || ix >= S.Win) return 0u;
-    return *reinterpret_cast<const u32 *>(x + (((size_t)b * S.Hin + iy) * S.Win + ix) * S.Cin + ci);
-}
-
-// data-gradient gather: for input pixel m and k = tap * Cout + co (co even), the output
-// gradients (co, co+1) of the output pixel that read input pixel m through that tap
-__device__ __forceinline__ u32 dgrad_pair(const bf16 *dy, const ConvShape &S, int m, int k)
-{
-    const int hw = S.Hin * S.Win;
-    const int b = m / hw, r = m - b * hw, iy = r / S.Win, ix = r - iy * S.Win;
-    const int tap = k / S.Cout, co = k - tap * S.Cout;
-    const int ky = tap / S.ks, kx = tap - ky * S.ks;
-    const int ty = iy + S.pad - ky, tx = ix + S.pad - kx;
-    if (ty < 0 || tx < 0 || ty % S.stride || tx % S.stride) return 0u;
-    const int oy = ty / S.stride, ox = tx / S.stride;
-    if (oy >= S.Hout || ox >= S.Wout) return 0u;
-    return *reinterpret_cast<const u32 *>(dy + (((size_t)b * S.Hout + oy) * S.Wout + ox) * S.Cout + co);
-}
-
-// im2col element of output pixel m, k (scalar)
-__device__ __forceinline__ bf16 fwd_elem(const bf16 *x, const ConvShape &S, int m, int k)
-{
-    if (k >= S.K) return __float2bfloat16(0.f);
-    const int hw = S.Hout * S.Wout;
-    const int b = m / hw, r = m - b * hw, oy = r / S.Wout, ox = r - oy * S.Wout;
-    const int tap = k / S.Cin, ci = k - tap * S.Cin;
-    const int ky = tap / S.ks, kx = tap - ky * S.ks;
-    const int iy = oy * S.stride + ky - S.pad, ix = ox * S.stride + kx - S.pad;
-    if (iy < 0 || iy >= S.Hin || ix < 0 || ix >= S.Win) return __float2bfloat16(0.f);
-    return x[(((size_t)b * S.Hin + iy) * S.Win + ix) * S.Cin + ci];
-}
-
 // ---------------------------------------------------------------- tensor-core GEMM tiles
 
 constexpr int TC_M = 128;        // rows of a tile (the MMA's M)
 constexpr int TC_KC = 64;        // columns of K gathered per chunk
 constexpr int TC_THREADS = 128;
-constexpr int WG_CHUNK = 512;    // output pixels per CTA of the weight gradient
+constexpr int WG_CHUNK = 512;    // most output pixels per CTA of the weight gradient
 constexpr uint32_t TC_POLLS = 1u << 22;
-// dynamic shared memory reserved (unused) by every launch so that at most 7 CTAs share an SM:
-// their TMEM accumulators (at most 64 columns each) then always fit the SM's 512 columns and
-// no CTA waits in its allocation
-constexpr int TC_SMEM_RESERVE = 8 * 1024;
+// the static shared memory of a CTA (operand tiles and index tables, over 27 KB) lets at most 8
+// CTAs share an SM (228 KB, plus 1 KB per CTA for the system): their TMEM accumulators (at most
+// 64 columns each) then always fit the SM's 512 columns and no CTA waits in its allocation
+constexpr int TC_STATIC_SMEM = TC_M * TC_KC * 2 + 64 * TC_KC * 2 + (TC_M + TC_KC) * 16;
+static_assert(9 * (TC_STATIC_SMEM + 1024) > 228 * 1024, "more than 8 CTAs per SM would oversubscribe TMEM");
 static __device__ unsigned int g_tc_timeouts;   // CTAs that gave up waiting for their MMAs
 
 struct TcArgs {
     ConvShape S;
     const bf16 *src;     // MODE 0: x; MODE 1: dy; MODE 2: x (the pixel rows' inputs)
-    const bf16 *wmat;    // MODE 0: w [Cout][Kp]; MODE 1: w^T [Cin][taps*Cout]; MODE 2: dy
-    int wrow;            // row length of wmat (MODE 0 / 1)
+    const bf16 *wmat;    // MODE 0 / 1: w [Cout][Kp]; MODE 2: dy
+    int wrow;            // row length of wmat (MODE 0 / 1: Kp)
     const float *bias;
     void *dst; int dst_f32, relu;
     const bf16 *mask;    // MODE 1: the layer input (ReLU output of the previous layer)
-    float *dw;           // MODE 2
+    float *dw, *db;      // MODE 2
+    int ncls;            // MODE 1: phase classes (stride^2) and the first tile of each (+ the total)
+    int cls_tile0[5];
+    int wg_chunk;        // MODE 2: output pixels per CTA (a multiple of 64, at most WG_CHUNK)
 };
 
 // MODE 0: forward, y = act(x (*) w + bias), rows = output pixels, N = Cout
-// MODE 1: data gradient, dx = mask(x_in) * (dy (*) w^T), rows = input pixels, N = Cin
-// MODE 2: weight gradient, dw^T[k][co] += sum over this CTA's output pixels of x_col[m][k] dy[m][co]
+// MODE 1: data gradient, dx = mask(x_in) * (dy (*) w^T), N = Cin.  The input pixels are split into
+//         the stride x stride phase classes (iy % stride, ix % stride): a pixel of one class is
+//         read only through the taps (ky, kx) with (iy + pad - ky) and (ix + pad - kx) divisible by
+//         the stride, so each class is a dense GEMM with K = its taps x Cout (at stride 2 with 3x3
+//         taps: 1, 2, 2 or 4 taps instead of 9); a CTA takes 128 rows of one class
+// MODE 2: weight gradient, dw^T[k][co] += sum over this CTA's output pixels of x_col[m][k] dy[m][co];
+//         row K of x_col^T is a row of ones, so the same MMAs give the bias gradient
+//         db[co] = sum_m dy[m][co].  Both operands are stored MN-major (the 8 channels of one pixel
+//         are one 16-byte row of a core matrix), so each 16 bytes is one load from the NHWC tensors
 template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
 {
@@ -118,22 +89,37 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     __shared__ __align__(8) u64 bar;
     __shared__ u32 s_tmem;
     // index tables: the tile's rows (one per thread) and the chunk's columns, decomposed once
-    // instead of per gathered element (MODE 0: rows = output pixels {b Hin, oy s - pad, ox s - pad},
-    // column pairs = {ky, kx, ci}; MODE 1: rows = input pixels {b Hout, iy + pad, ix + pad},
-    // column pairs = {ky, kx, co}; MODE 2: rows = {ky, kx, ci}, columns = output pixels as MODE 0's
-    // rows); .w = 1 where the row / column exists
+    // instead of per gathered element.  Rows: MODE 0 output pixels {b Hin, oy s - pad, ox s - pad};
+    // MODE 1 input pixels {b Hout, iy + pad, ix + pad}; MODE 2 {ky, kx, ci}.  Columns: MODE 0 one
+    // entry per 8 columns {ky, kx, ci} (per column pair when Cin is not a multiple of 8); MODE 1 one
+    // per 8 columns {ky, kx, co, column of w^T}; MODE 2 one per output pixel as MODE 0's rows.
+    // .w = 1 where the row / column exists (MODE 0 / 2)
     __shared__ int4 s_row[TC_M];
     __shared__ int4 s_col[TC_KC];
+    __shared__ int s_pix[TC_M];   // MODE 1: the row's input pixel, -1 past the class's rows
     const ConvShape &S = T.S;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = MODE == 0 ? S.Cout : MODE == 1 ? S.Cin : S.Cout;
     const int ncols = N <= 32 ? 32 : 64;
+    const int sshift = S.stride == 2 ? 1 : 0;   // strides 1 and 2
     // rows of the tile and the reduction range
     int M, K, r0, kb = 0;
-    if (MODE == 0) { M = S.B * S.Hout * S.Wout; K = S.Kp; r0 = blockIdx.x * TC_M; }
-    else if (MODE == 1) { M = S.B * S.Hin * S.Win; K = S.ks * S.ks * S.Cout; r0 = blockIdx.x * TC_M; }
-    else { M = S.Kp; r0 = blockIdx.x * TC_M; kb = blockIdx.y * WG_CHUNK;
-           K = min(WG_CHUNK, S.B * S.Hout * S.Wout - kb); K = (K + 15) & ~15; }
+    int py = 0, px = 0, Hc = 0, Wc = 0, ky0 = 0, kx0 = 0, nkx = 1;
+    if (MODE == 0) {
+        M = S.B * S.Hout * S.Wout; K = S.Kp; r0 = blockIdx.x * TC_M;
+    } else if (MODE == 1) {
+        int cls = 0;
+        while (cls + 1 < T.ncls && (int)blockIdx.x >= T.cls_tile0[cls + 1]) cls++;
+        py = cls >> sshift; px = cls - (py << sshift);
+        Hc = (S.Hin - py + S.stride - 1) >> sshift; Wc = (S.Win - px + S.stride - 1) >> sshift;
+        ky0 = (py + S.pad) & sshift; kx0 = (px + S.pad) & sshift;
+        const int nky = (S.ks - ky0 + S.stride - 1) >> sshift;
+        nkx = (S.ks - kx0 + S.stride - 1) >> sshift;
+        M = S.B * Hc * Wc; K = nky * nkx * S.Cout; r0 = (blockIdx.x - T.cls_tile0[cls]) * TC_M;
+    } else {
+        M = S.K + 1; r0 = blockIdx.x * TC_M; kb = blockIdx.y * T.wg_chunk;
+        K = min(T.wg_chunk, S.B * S.Hout * S.Wout - kb); K = (K + 15) & ~15;
+    }
     const u32 bar_a = smem_u32(&bar);
     if (warp == 0) tmem_alloc(smem_u32(&s_tmem), (u32)ncols);
     if (tid == 0) {
@@ -144,10 +130,18 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     __syncthreads();
     tc_fence_after_sync();
     const u32 tmem = s_tmem;
-    const u32 idesc = umma_idesc_bf16(TC_M, N);
+    const u32 idesc = umma_idesc_bf16(TC_M, N, MODE == 2, MODE != 0);
     u32 phase = 0;
     bool ok = true;
     const int npix = MODE == 2 ? S.B * S.Hout * S.Wout : 0;
+    const bool vec = MODE == 1 || S.Cin % 8 == 0;   // 16-byte gathers of 8 channels
+    const int rowK = MODE == 2 ? S.K - r0 : -1;      // MODE 2: the tile row of the ones row (bias)
+    // MODE 2: 8-row groups of the tile that hold a (tap, channel) row or the ones row; the groups
+    // past them are zero in every chunk, so they are cleared once here and never gathered
+    const int ng = MODE == 2 ? min(TC_M / 8, (M - r0 + 7) >> 3) : TC_M / 8;
+    if (MODE == 2 && ng < TC_M / 8)
+        for (int i = tid; i < TC_M * TC_KC * 2 / 16; i += TC_THREADS)
+            reinterpret_cast<uint4 *>(sa)[i] = make_uint4(0u, 0u, 0u, 0u);
     // output pixel p -> {b Hin, oy s - pad, ox s - pad, exists}
     auto out_pixel = [&](int p, int n) {
         if (p >= n) return make_int4(0, 0, 0, 0);
@@ -160,10 +154,13 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
             s_row[tid] = out_pixel(row, M);
         } else if (MODE == 1) {
             if (row < M) {
-                const int hw = S.Hin * S.Win, b = row / hw, rr = row - b * hw, iy = rr / S.Win, ix = rr - iy * S.Win;
+                const int hw = Hc * Wc, b = row / hw, rr = row - b * hw, j = rr / Wc, i = rr - j * Wc;
+                const int iy = (j << sshift) + py, ix = (i << sshift) + px;
                 s_row[tid] = make_int4(b * S.Hout, iy + S.pad, ix + S.pad, 1);
+                s_pix[tid] = (b * S.Hin + iy) * S.Win + ix;
             } else {
                 s_row[tid] = make_int4(0, 0, 0, 0);
+                s_pix[tid] = -1;
             }
         } else {
             if (row < S.K) {
@@ -174,20 +171,25 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
             }
         }
     }
-    const int sshift = S.stride == 2 ? 1 : 0;   // the network's strides are 1 and 2
 
     for (int k0 = 0; k0 < K && ok; k0 += TC_KC) {
         const int kc = min(TC_KC, K - k0);         // a multiple of 16
-        const int kq = kc >> 3;                    // 16-byte units per row
+        const int kq = kc >> 3;                    // 8-column groups
         // the chunk's column table (the previous chunk's MMAs have completed: see the wait below)
         if (MODE == 2) {
             for (int j = tid; j < kc; j += TC_THREADS) s_col[j] = out_pixel(kb + k0 + j, npix);
+        } else if (MODE == 1) {
+            if (tid < kq) {
+                const int k = k0 + 8 * tid, t = k / S.Cout, co = k - t * S.Cout, tyi = t / nkx;
+                const int ky = ky0 + (tyi << sshift), kx = kx0 + ((t - tyi * nkx) << sshift);
+                s_col[tid] = make_int4(ky, kx, co, 0);
+            }
         } else {
-            const int cdiv = MODE == 0 ? S.Cin : S.Cout, kmax = MODE == 0 ? S.K : K;
-            for (int j = tid; j < (kc >> 1); j += TC_THREADS) {
-                const int k = k0 + 2 * j;
-                if (k < kmax) {
-                    const int tap = k / cdiv, c = k - tap * cdiv, ky = tap / S.ks;
+            const int per = vec ? 8 : 2;           // columns per table entry
+            for (int j = tid; j < kc / per; j += TC_THREADS) {
+                const int k = k0 + per * j;
+                if (k < S.K) {
+                    const int tap = k / S.Cin, c = k - tap * S.Cin, ky = tap / S.ks;
                     s_col[j] = make_int4(ky, tap - ky * S.ks, c, 1);
                 } else {
                     s_col[j] = make_int4(0, 0, 0, 0);
@@ -195,71 +197,125 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
             }
         }
         __syncthreads();
-        // A: TC_M rows x kc columns; 8 consecutive threads write one 128-byte core matrix
-        for (int u = tid; u < TC_M * kq; u += TC_THREADS) {
-            const int r = (u & 7) + 8 * ((u >> 3) / kq), q = (u >> 3) % kq;
-            const int4 R = s_row[r];
-            u32 v[4];
-            if (MODE == 0) {
+        // A: TC_M rows x kc columns, 16 bytes per unit, loaded for the thread's units first and
+        // stored after.  MODE 0 / 1 (K-major): unit u = 8 columns of one row, 8 consecutive threads
+        // fill one 128-byte core matrix.  MODE 2 (MN-major): unit u = 8 rows of one column.
+        {
+            const int nunits = MODE == 2 ? ng * kc : TC_M * kq;
+            uint4 va[8];
+            u32 off[8];
+            // MODE 0 / 1 with kq = 2, 4 or 8 (kq divides 16): unit u = tid + 128 i has the column group
+            // (tid / 8) % kq for every i and row (tid % 8) + 8 ((tid / 8) / kq) + i (128 / kq), so the
+            // column entry is read once
+            const bool qfix = MODE != 2 && vec && (kq & (kq - 1)) == 0;
+            const int lkq = 31 - __clz(kq);
+            const int qf = (tid >> 3) & (kq - 1);
+            const int4 Cq = s_col[qfix ? qf : 0];
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const int4 Cc = s_col[4 * q + i];
-                    const int iy = R.y + Cc.x, ix = R.z + Cc.y;
-                    v[i] = (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
-                               ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(R.x + iy) * S.Win + ix) * S.Cin + Cc.z)
-                               : 0u;
-                }
-            } else if (MODE == 1) {
+            for (int i = 0; i < 8; i++) {
+                const int u = tid + i * TC_THREADS;
+                va[i] = make_uint4(0, 0, 0, 0);
+                off[i] = 0;
+                if (u >= nunits) continue;
+                const int r = qfix ? (tid & 7) + 8 * ((tid >> 3) >> lkq) + (i << (7 - lkq)) : (u & 7) + 8 * ((u >> 3) / kq);
+                const int q = qfix ? qf : (u >> 3) % kq;
+                if (MODE == 0) {
+                    const int4 R = s_row[r];
+                    off[i] = umma_tile_off(r, 8 * q, kc);
+                    if (vec) {
+                        const int4 Cc = qfix ? Cq : s_col[q];
+                        const int iy = R.y + Cc.x, ix = R.z + Cc.y;
+                        if ((R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win)
+                            va[i] = *reinterpret_cast<const uint4 *>(T.src + ((size_t)(R.x + iy) * S.Win + ix) * S.Cin + Cc.z);
+                    } else {
+                        u32 v[4];
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const int4 Cc = s_col[4 * q + i];
-                    // the output pixel that read input pixel R through tap (ky, kx)
-                    const int ty = R.y - Cc.x, tx = R.z - Cc.y;
-                    const bool hit = (R.w & Cc.w) && ty >= 0 && tx >= 0 &&
-                                     (sshift ? !((ty | tx) & 1) : S.stride == 1 || (ty % S.stride == 0 && tx % S.stride == 0));
-                    const int oy = sshift ? ty >> 1 : S.stride == 1 ? ty : ty / S.stride;
-                    const int ox = sshift ? tx >> 1 : S.stride == 1 ? tx : tx / S.stride;
-                    v[i] = hit && oy < S.Hout && ox < S.Wout
-                               ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(R.x + oy) * S.Wout + ox) * S.Cout + Cc.z)
-                               : 0u;
-                }
-            } else {
-                // row r = input-column index (tap, ci) of x_col, columns = output pixels kb + k0 + 8q + j
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    bf16 e[2];
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const int4 Cc = s_col[8 * q + 2 * i + h];
-                        const int iy = Cc.y + R.x, ix = Cc.z + R.y;
-                        e[h] = (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
-                                   ? T.src[((size_t)(Cc.x + iy) * S.Win + ix) * S.Cin + R.z]
-                                   : __float2bfloat16(0.f);
+                        for (int e = 0; e < 4; e++) {
+                            const int4 Cc = s_col[4 * q + e];
+                            const int iy = R.y + Cc.x, ix = R.z + Cc.y;
+                            v[e] = (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
+                                       ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(R.x + iy) * S.Win + ix) * S.Cin + Cc.z)
+                                       : 0u;
+                        }
+                        va[i] = make_uint4(v[0], v[1], v[2], v[3]);
                     }
-                    v[i] = pack_bf16(e[0], e[1]);
-                }
-            }
-            *reinterpret_cast<uint4 *>(sa + umma_tile_off(r, 8 * q, kc)) = make_uint4(v[0], v[1], v[2], v[3]);
-        }
-        // B: N rows x kc columns
-        for (int u = tid; u < N * kq; u += TC_THREADS) {
-            const int n = (u & 7) + 8 * ((u >> 3) / kq), q = (u >> 3) % kq;
-            uint4 v;
-            if (MODE != 2) {
-                v = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)n * T.wrow + k0 + 8 * q);
-            } else {
-                u32 w[4];
+                } else if (MODE == 1) {
+                    const int4 R = s_row[r], Cc = qfix ? Cq : s_col[q];
+                    off[i] = umma_tile_off(r, 8 * q, kc);
+                    // the output pixel that read input pixel R through tap (ky, kx); the class
+                    // makes ty and tx multiples of the stride
+                    const int ty = R.y - Cc.x, tx = R.z - Cc.y;
+                    const int oy = ty >> sshift, ox = tx >> sshift;
+                    if (R.w && ty >= 0 && tx >= 0 && oy < S.Hout && ox < S.Wout)
+                        va[i] = *reinterpret_cast<const uint4 *>(T.src + ((size_t)(R.x + oy) * S.Wout + ox) * S.Cout + Cc.z);
+                } else {
+                    const int kk = u & 7, t8 = u >> 3, kg = t8 / ng, g = t8 - kg * ng, k = 8 * kg + kk;
+                    const int4 Cc = s_col[k];
+                    off[i] = (u32)((k >> 3) * (TC_M * 16) + g * 128 + kk * 16);
+                    if (vec && 8 * g == rowK) {
+                        // K is a multiple of 8 here: the ones row starts a group of 8 rows
+                        va[i] = make_uint4(Cc.w ? 0x3F80u : 0u, 0u, 0u, 0u);
+                    } else if (vec) {
+                        const int4 R = s_row[8 * g];
+                        const int iy = Cc.y + R.x, ix = Cc.z + R.y;
+                        if ((R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win)
+                            va[i] = *reinterpret_cast<const uint4 *>(T.src + ((size_t)(Cc.x + iy) * S.Win + ix) * S.Cin + R.z);
+                    } else {
+                        // row pairs (2e, 2e + 1) are channels (ci, ci + 1) of one tap (Cin and K
+                        // are even): one 4-byte load each; the ones row K is the low half of a pair
+                        u32 v[4];
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const int m = kb + k0 + 8 * q + 2 * i;
-                    const bf16 z = __float2bfloat16(0.f);
-                    const bf16 e0 = m < npix ? T.wmat[(size_t)m * S.Cout + n] : z;
-                    const bf16 e1 = m + 1 < npix ? T.wmat[(size_t)(m + 1) * S.Cout + n] : z;
-                    w[i] = pack_bf16(e0, e1);
+                        for (int e = 0; e < 4; e++) {
+                            const int rr = 8 * g + 2 * e;
+                            const int4 R = s_row[rr];
+                            const int iy = Cc.y + R.x, ix = Cc.z + R.y;
+                            v[e] = rr == rowK ? (Cc.w ? 0x3F80u : 0u)
+                                   : (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
+                                       ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(Cc.x + iy) * S.Win + ix) * S.Cin + R.z)
+                                       : 0u;
+                        }
+                        va[i] = make_uint4(v[0], v[1], v[2], v[3]);
+                    }
                 }
-                v = make_uint4(w[0], w[1], w[2], w[3]);
             }
-            *reinterpret_cast<uint4 *>(sb + umma_tile_off(n, 8 * q, kc)) = v;
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (tid + i * TC_THREADS < nunits) *reinterpret_cast<uint4 *>(sa + off[i]) = va[i];
+        }
+        // B: N rows x kc columns.  MODE 0: rows of the weight matrix (K-major).  MODE 1: the weights
+        // w[co][tap Cin + ci] as they are stored, MN-major (unit = 8 input channels of one (tap,
+        // co) column).  MODE 2: dy, MN-major (unit = 8 output channels of one pixel)
+        {
+            const int nh = N >> 3;
+            const int nunits = MODE != 0 ? nh * kc : N * kq;
+            uint4 vb[4];
+            u32 off[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int u = tid + i * TC_THREADS;
+                vb[i] = make_uint4(0, 0, 0, 0);
+                off[i] = 0;
+                if (u >= nunits) continue;
+                if (MODE == 0) {
+                    const int n = (u & 7) + 8 * ((u >> 3) / kq), q = (u >> 3) % kq;
+                    off[i] = umma_tile_off(n, 8 * q, kc);
+                    vb[i] = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)n * T.wrow + k0 + 8 * q);
+                } else {
+                    const int kk = u & 7, h = (u >> 3) % nh, k = 8 * ((u >> 3) / nh) + kk;
+                    off[i] = (u32)((k >> 3) * (N * 16) + h * 128 + kk * 16);
+                    if (MODE == 1) {
+                        const int4 Cc = s_col[k >> 3];
+                        vb[i] = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)(Cc.z + kk) * T.wrow +
+                                                                 (Cc.x * S.ks + Cc.y) * S.Cin + 8 * h);
+                    } else {
+                        const int m = kb + k0 + k;
+                        if (m < npix) vb[i] = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)m * S.Cout + 8 * h);
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                if (tid + i * TC_THREADS < nunits) *reinterpret_cast<uint4 *>(sb + off[i]) = vb[i];
         }
         // the operands written by the threads become visible to the tensor core
         fence_proxy_async_smem();
@@ -267,9 +323,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
         if (tid == 0) {
             tc_fence_after_sync();
             const u32 a0 = smem_u32(sa), b0 = smem_u32(sb);
-            for (int s = 0; s < (kc >> 4); s++)
-                umma_bf16(tmem, umma_desc(a0 + 256 * s, 128, kc * 16), umma_desc(b0 + 256 * s, 128, kc * 16), idesc,
-                          (k0 | s) != 0);
+            for (int s = 0; s < (kc >> 4); s++) {
+                // one MMA per 16 columns of K: two core matrices along K
+                const u64 ad = MODE == 2 ? umma_desc_mn(a0 + 2 * (TC_M * 16) * s, 128, TC_M * 16)
+                                         : umma_desc(a0 + 256 * s, 128, kc * 16);
+                const u64 bd = MODE != 0 ? umma_desc_mn(b0 + 2 * (N * 16) * s, 128, N * 16)
+                                         : umma_desc(b0 + 256 * s, 128, kc * 16);
+                umma_bf16(tmem, ad, bd, idesc, (k0 | s) != 0);
+            }
             umma_commit(bar_a);
         }
         // the chunk's MMAs must complete before the next chunk overwrites the operands
@@ -285,43 +346,64 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
 
     if (ok) {
         // epilogue: warp w holds rows 32w .. 32w + 31 of the tile in TMEM lanes of its quarter
+        // (a data-gradient class without taps, K = 0, has no accumulator: its rows are 0)
         const int r = 32 * warp + lane;
         for (int c = 0; c < N; c += 16) {
             float v[16];
-            tmem_ld16(tmem + ((u32)(32 * warp) << 16) + (u32)c, v);
+            if (K > 0) {
+                tmem_ld16(tmem + ((u32)(32 * warp) << 16) + (u32)c, v);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; i++) v[i] = 0.f;
+            }
+            // the row's 16 columns are 32 (bf16) or 64 (FP32) contiguous bytes, N a multiple of 16:
+            // 16-byte loads and stores
             if (MODE == 0) {
                 const int m = r0 + r;
                 if (m < M) {
 #pragma unroll
-                    for (int i = 0; i < 16; i += 2) {
-                        float v0 = v[i] + T.bias[c + i], v1 = v[i + 1] + T.bias[c + i + 1];
-                        if (T.relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
-                        if (T.dst_f32) {
-                            float *o = (float *)T.dst + (size_t)m * N + c + i;
-                            o[0] = v0; o[1] = v1;
-                        } else {
-                            *reinterpret_cast<u32 *>((bf16 *)T.dst + (size_t)m * N + c + i) =
-                                pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
-                        }
+                    for (int i = 0; i < 16; i++) {
+                        v[i] += T.bias[c + i];
+                        if (T.relu) v[i] = fmaxf(v[i], 0.f);
+                    }
+                    if (T.dst_f32) {
+                        float4 *o = reinterpret_cast<float4 *>((float *)T.dst + (size_t)m * N + c);
+#pragma unroll
+                        for (int j = 0; j < 4; j++) o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                    } else {
+                        u32 p[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) p[j] = pack_bf16(__float2bfloat16(v[2 * j]), __float2bfloat16(v[2 * j + 1]));
+                        uint4 *o = reinterpret_cast<uint4 *>((bf16 *)T.dst + (size_t)m * N + c);
+                        o[0] = make_uint4(p[0], p[1], p[2], p[3]);
+                        o[1] = make_uint4(p[4], p[5], p[6], p[7]);
                     }
                 }
             } else if (MODE == 1) {
-                const int m = r0 + r;
-                if (m < M) {
+                const int m = s_pix[r];
+                if (m >= 0) {
+                    // the layer input is the previous layer's ReLU output: zero where it was clipped
+                    const uint4 *xm4 = reinterpret_cast<const uint4 *>(T.mask + (size_t)m * N + c);
+                    const uint4 xa = xm4[0], xb = xm4[1];
+                    const u32 xm[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
+                    u32 p[8];
 #pragma unroll
-                    for (int i = 0; i < 16; i += 2) {
-                        // the layer input is the previous layer's ReLU output: zero where it was clipped
-                        const u32 xm = *reinterpret_cast<const u32 *>(T.mask + (size_t)m * N + c + i);
-                        const float v0 = (xm & 0x7FFFu) ? v[i] : 0.f, v1 = (xm & 0x7FFF0000u) ? v[i + 1] : 0.f;
-                        *reinterpret_cast<u32 *>((bf16 *)T.dst + (size_t)m * N + c + i) =
-                            pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
+                    for (int j = 0; j < 8; j++) {
+                        const float v0 = (xm[j] & 0x7FFFu) ? v[2 * j] : 0.f, v1 = (xm[j] & 0x7FFF0000u) ? v[2 * j + 1] : 0.f;
+                        p[j] = pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
                     }
+                    uint4 *o = reinterpret_cast<uint4 *>((bf16 *)T.dst + (size_t)m * N + c);
+                    o[0] = make_uint4(p[0], p[1], p[2], p[3]);
+                    o[1] = make_uint4(p[4], p[5], p[6], p[7]);
                 }
             } else {
                 const int kk = r0 + r;
-                if (kk < S.Kp) {
+                if (kk < S.K) {
 #pragma unroll
                     for (int i = 0; i < 16; i++) atomicAdd(T.dw + (size_t)(c + i) * S.Kp + kk, v[i]);
+                } else if (kk == S.K) {
+#pragma unroll
+                    for (int i = 0; i < 16; i++) atomicAdd(T.db + c + i, v[i]);
                 }
             }
         }
@@ -329,34 +411,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     tc_fence_before_sync();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, (u32)ncols);
-}
-
-// bias gradient db[co] += sum_m dy[m][co]: a CTA of 256 threads walks rows m in steps of
-// rows = 256 / C (thread t < rows C takes channel t % C of row t / C), sums its channels in shared
-// memory and adds them to db with one atomic per channel
-__global__ void __launch_bounds__(256) k_conv_bgrad(const bf16 *dy, int M, int C, float *db)
-{
-    __shared__ float s_part[256];
-    const int co = threadIdx.x % C, rows = 256 / C, r0 = threadIdx.x / C;
-    float s = 0.f;
-    if (r0 < rows)   // C = 48 leaves the last 16 threads idle
-        for (int m = blockIdx.x * rows + r0; m < M; m += gridDim.x * rows) s += __bfloat162float(dy[(size_t)m * C + co]);
-    s_part[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x < C) {
-        float t = 0.f;
-        for (int r = 0; r < rows; r++) t += s_part[r * C + threadIdx.x];
-        atomicAdd(&db[threadIdx.x], t);
-    }
-}
-
-// wt[ci][tap * Cout + co] = w[co][tap * Cin + ci] (the data gradient's weight matrix)
-__global__ void k_transpose_w(const bf16 *w, int Cout, int Cin, int taps, int Kp, bf16 *wt)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= Cout * Cin * taps) return;
-    const int co = i % Cout, r = i / Cout, tap = r % taps, ci = r / taps;
-    wt[(size_t)ci * taps * Cout + tap * Cout + co] = w[(size_t)co * Kp + tap * Cin + ci];
 }
 
 // network input: 64x64 luma of CTU (cx, cy) of the picture (edge samples repeated beyond the
@@ -448,6 +502,9 @@ __global__ void k_adam(float *w, float *m, float *v, const float *g, bf16 *wb, i
     if (wb) wb[i] = __float2bfloat16(wi);
 }
 
+// the 16-byte gathers and epilogue stores address 8 channels at a time from the tensors' bases
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
 static bool conv_shape(int B, int Hin, int Win, int Cin, int Cout, int ks, int stride, int Kp, ConvShape &S)
 {
     S.B = B; S.Hin = Hin; S.Win = Win; S.Cin = Cin; S.Cout = Cout; S.ks = ks; S.stride = stride;
@@ -458,7 +515,7 @@ static bool conv_shape(int B, int Hin, int Win, int Cin, int Cout, int ks, int s
     S.Kp = Kp;
     return B > 0 && Cin >= 2 && !(Cin & 1) && Cout >= 16 && !(Cout % 8) && Kp >= S.K && !(Kp % 16) &&
            (B * S.Hout * S.Wout) % 16 == 0 && (B * Hin * Win) % 16 == 0 && (ks == 1 || ks == 3) &&
-           (ks * ks * Cout) % 16 == 0;
+           (stride == 1 || stride == 2) && (ks * ks * Cout) % 16 == 0;
 }
 
 }  // namespace uc
@@ -476,12 +533,13 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_fwd(const void *x, const void *w, const
     ConvShape S;
     if (!x || !w || !bias || !y || Cout % 16 || Cout > 64 || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
         return set_status(UC_ERR_ARG, "cnn_conv_fwd: shape");
+    if (!aligned16(x) || !aligned16(w) || !aligned16(y)) return set_status(UC_ERR_ARG, "cnn_conv_fwd: alignment");
     const int M = B * S.Hout * S.Wout;
     TcArgs T;
     memset(&T, 0, sizeof(T));
     T.S = S; T.src = (const bf16 *)x; T.wmat = (const bf16 *)w; T.wrow = Kp; T.bias = bias;
     T.dst = y; T.dst_f32 = y_f32; T.relu = relu;
-    k_conv_tc<0><<<(M + TC_M - 1) / TC_M, TC_THREADS, TC_SMEM_RESERVE, (cudaStream_t)stream>>>(T);
+    k_conv_tc<0><<<(M + TC_M - 1) / TC_M, TC_THREADS, 0, (cudaStream_t)stream>>>(T);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     return UC_OK;
@@ -494,21 +552,28 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_dgrad(const void *dy, const void *w, co
     int r = ensure_init();
     if (r) return r;
     ConvShape S;
-    if (!dy || !w || !x || !dx || !wt_scratch || Cin % 16 || Cin > 64 ||
-        !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
+    (void)wt_scratch;   // the weights are read in place (MN-major); kept for the ABI
+    if (!dy || !w || !x || !dx || Cin % 16 || Cin > 64 || Cout % 16 || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
         return set_status(UC_ERR_ARG, "cnn_conv_dgrad: shape");
+    if (!aligned16(dy) || !aligned16(w) || !aligned16(x) || !aligned16(dx))
+        return set_status(UC_ERR_ARG, "cnn_conv_dgrad: alignment");
     cudaStream_t st = (cudaStream_t)stream;
-    const int taps = ks * ks, nw = Cout * Cin * taps;
-    k_transpose_w<<<(nw + 255) / 256, 256, 0, st>>>((const bf16 *)w, Cout, Cin, taps, Kp, (bf16 *)wt_scratch);
-    UC_CHECK(cudaGetLastError());
-    const int M = B * Hin * Win;
     TcArgs T;
     memset(&T, 0, sizeof(T));
-    T.S = S; T.src = (const bf16 *)dy; T.wmat = (const bf16 *)wt_scratch; T.wrow = taps * Cout;
+    T.S = S; T.src = (const bf16 *)dy; T.wmat = (const bf16 *)w; T.wrow = Kp;
     T.dst = dx; T.mask = (const bf16 *)x;
-    k_conv_tc<1><<<(M + TC_M - 1) / TC_M, TC_THREADS, TC_SMEM_RESERVE, st>>>(T);
+    // the input pixels' phase classes (iy % stride, ix % stride), each a run of 128-row tiles
+    T.ncls = stride * stride;
+    T.cls_tile0[0] = 0;
+    for (int c = 0; c < T.ncls; c++) {
+        const int py = c / stride, px = c % stride;
+        const int rows = B * ((Hin - py + stride - 1) / stride) * ((Win - px + stride - 1) / stride);
+        T.cls_tile0[c + 1] = T.cls_tile0[c] + (rows + TC_M - 1) / TC_M;
+    }
+    if (T.cls_tile0[T.ncls] == 0) return set_status(UC_ERR_ARG, "cnn_conv_dgrad: shape");
+    k_conv_tc<1><<<T.cls_tile0[T.ncls], TC_THREADS, 0, st>>>(T);
     UC_CHECK(cudaGetLastError());
-    count_launch(2);
+    count_launch(1);
     return UC_OK;
 }
 
@@ -520,19 +585,26 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_wgrad(const void *dy, const void *x, fl
     ConvShape S;
     if (!dy || !x || !dw || !db || Cout % 16 || Cout > 64 || !conv_shape(B, Hin, Win, Cin, Cout, ks, stride, Kp, S))
         return set_status(UC_ERR_ARG, "cnn_conv_wgrad: shape");
+    if (!aligned16(dy) || !aligned16(x)) return set_status(UC_ERR_ARG, "cnn_conv_wgrad: alignment");
     cudaStream_t st = (cudaStream_t)stream;
     const int M = B * S.Hout * S.Wout;
     UC_CHECK(cudaMemsetAsync(dw, 0, (size_t)Cout * Kp * sizeof(float), st));
     UC_CHECK(cudaMemsetAsync(db, 0, (size_t)Cout * sizeof(float), st));
     TcArgs T;
     memset(&T, 0, sizeof(T));
-    T.S = S; T.src = (const bf16 *)x; T.wmat = (const bf16 *)dy; T.dw = dw;
-    dim3 grid((Kp + TC_M - 1) / TC_M, (M + WG_CHUNK - 1) / WG_CHUNK);
-    k_conv_tc<2><<<grid, TC_THREADS, TC_SMEM_RESERVE, st>>>(T);
+    T.S = S; T.src = (const bf16 *)x; T.wmat = (const bf16 *)dy; T.dw = dw; T.db = db;
+    // rows: the K (tap, input channel) rows and the ones row of the bias gradient; the pixels are
+    // split into chunks small enough that the launch still has 4 CTAs per SM (down to 64 pixels)
+    const int rowtiles = (S.K + 1 + TC_M - 1) / TC_M;
+    int sms = 0, dev = 0;
+    UC_CHECK(cudaGetDevice(&dev));
+    UC_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    T.wg_chunk = WG_CHUNK;
+    while (T.wg_chunk > 64 && rowtiles * ((M + T.wg_chunk - 1) / T.wg_chunk) < 4 * sms) T.wg_chunk >>= 1;
+    dim3 grid(rowtiles, (M + T.wg_chunk - 1) / T.wg_chunk);
+    k_conv_tc<2><<<grid, TC_THREADS, 0, st>>>(T);
     UC_CHECK(cudaGetLastError());
-    k_conv_bgrad<<<std::min(1024, (M + 255) / 256), 256, 0, st>>>((const bf16 *)dy, M, Cout, db);
-    UC_CHECK(cudaGetLastError());
-    count_launch(2);
+    count_launch(1);
     return UC_OK;
 }
 

@@ -8,6 +8,11 @@
 // offset) and 8-row groups are K * 16 bytes apart (its stride byte offset):
 //     byte(r, k) = (r / 8) * (K * 16) + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2.
 // One MMA consumes 16 columns of K, i.e. the descriptor of step s starts s * 256 bytes in.
+//
+// "MN-major, no swizzle" (the operand transposed): a core matrix holds 8 MN-consecutive elements
+// (16 bytes) for each of 8 consecutive K (128 contiguous bytes); the descriptor's leading byte
+// offset is then the distance between core matrices adjacent along K and its stride byte offset
+// the distance between core matrices adjacent along MN.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -19,19 +24,27 @@ __host__ __device__ constexpr uint32_t umma_tile_off(int r, int k, int K)
     return (uint32_t)((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
-// shared-memory matrix descriptor: start address, leading byte offset (K direction), stride byte
-// offset (8-row groups), descriptor version 1, no swizzle
+// shared-memory matrix descriptor: start address, leading byte offset (K direction of a K-major
+// operand), stride byte offset (its 8-row groups), descriptor version 1, no swizzle
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
 {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-// instruction descriptor of kind::f16 with bf16 A and B (both the same type), f32 accumulator,
-// both operands K-major, M x N
-__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N)
+// descriptor of an MN-major, no-swizzle operand (layout above): mn_stride = bytes between core
+// matrices adjacent along M (or N), k_stride = bytes between core matrices adjacent along K
+__device__ __forceinline__ uint64_t umma_desc_mn(uint32_t saddr, uint32_t mn_stride, uint32_t k_stride)
 {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+    return umma_desc(saddr, k_stride, mn_stride);
+}
+
+// instruction descriptor of kind::f16 with bf16 A and B (both the same type), f32 accumulator,
+// M x N; A and B K-major unless a_mn / b_mn (bits 15 / 16: the operand is MN-major)
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N, bool a_mn = false, bool b_mn = false)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // TMEM allocation of ncols columns (a power of two >= 32) by one whole warp; the address is
