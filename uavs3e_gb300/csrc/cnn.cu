@@ -53,7 +53,7 @@ constexpr uint32_t TC_POLLS = 1u << 22;
 // the static shared memory of a CTA (operand tiles and index tables, over 27 KB) lets at most 8
 // CTAs share an SM (228 KB, plus 1 KB per CTA for the system): their TMEM accumulators (at most
 // 64 columns each) then always fit the SM's 512 columns and no CTA waits in its allocation
-constexpr int TC_STATIC_SMEM = TC_M * TC_KC * 2 + 64 * TC_KC * 2 + (TC_M + TC_KC) * 16;
+constexpr int TC_STATIC_SMEM = TC_M * TC_KC * 2 + 64 * TC_KC * 2 + TC_M * 8 + TC_KC * 16;
 static_assert(9 * (TC_STATIC_SMEM + 1024) > 228 * 1024, "more than 8 CTAs per SM would oversubscribe TMEM");
 static __device__ unsigned int g_tc_timeouts;   // CTAs that gave up waiting for their MMAs
 
@@ -81,20 +81,24 @@ struct TcArgs {
 //         row K of x_col^T is a row of ones, so the same MMAs give the bias gradient
 //         db[co] = sum_m dy[m][co].  Both operands are stored MN-major (the 8 channels of one pixel
 //         are one 16-byte row of a core matrix), so each 16 bytes is one load from the NHWC tensors
-template <int MODE>
-__global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
+// VEC: the 8 channels of a unit are contiguous (MODE 1, or Cin a multiple of 8) and gathered by
+// one 16-byte load; otherwise by 4-byte channel pairs
+template <int MODE, bool VEC>
+__global__ void __launch_bounds__(TC_THREADS, 7) k_conv_tc(const TcArgs T)
 {
     __shared__ __align__(128) unsigned char sa[TC_M * TC_KC * 2];
     __shared__ __align__(128) unsigned char sb[64 * TC_KC * 2];
     __shared__ __align__(8) u64 bar;
     __shared__ u32 s_tmem;
-    // index tables: the tile's rows (one per thread) and the chunk's columns, decomposed once
-    // instead of per gathered element.  Rows: MODE 0 output pixels {b Hin, oy s - pad, ox s - pad};
-    // MODE 1 input pixels {b Hout, iy + pad, ix + pad}; MODE 2 {ky, kx, ci}.  Columns: MODE 0 one
-    // entry per 8 columns {ky, kx, ci} (per column pair when Cin is not a multiple of 8); MODE 1 one
-    // per 8 columns {ky, kx, co, column of w^T}; MODE 2 one per output pixel as MODE 0's rows.
-    // .w = 1 where the row / column exists (MODE 0 / 2)
-    __shared__ int4 s_row[TC_M];
+    // index tables, decomposed once instead of per gathered element.  A gathered element is
+    // src[base + delta]: the pixel side of the product gives base and a mask of its taps (bit
+    // ky ks + kx) that lie inside the picture, the (tap, channel) side gives delta and its tap:
+    //   MODE 0: rows = output pixels {base, mask}; columns per 8 (per 2 when Cin is not a
+    //           multiple of 8) = {delta, tap};
+    //   MODE 1: rows = the class's input pixels {base, mask}; columns per 8 = {delta, tap, co};
+    //   MODE 2: rows = (tap, ci) {delta, tap}; columns = output pixels {base, mask}.
+    // Rows and columns that do not exist have mask 0 or tap 31 (never in a mask).
+    __shared__ int2 s_row[TC_M];
     __shared__ int4 s_col[TC_KC];
     __shared__ int s_pix[TC_M];   // MODE 1: the row's input pixel, -1 past the class's rows
     const ConvShape &S = T.S;
@@ -134,7 +138,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     u32 phase = 0;
     bool ok = true;
     const int npix = MODE == 2 ? S.B * S.Hout * S.Wout : 0;
-    const bool vec = MODE == 1 || S.Cin % 8 == 0;   // 16-byte gathers of 8 channels
+    constexpr bool vec = VEC;
     const int rowK = MODE == 2 ? S.K - r0 : -1;      // MODE 2: the tile row of the ones row (bias)
     // MODE 2: 8-row groups of the tile that hold a (tap, channel) row or the ones row; the groups
     // past them are zero in every chunk, so they are cleared once here and never gathered
@@ -142,11 +146,27 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
     if (MODE == 2 && ng < TC_M / 8)
         for (int i = tid; i < TC_M * TC_KC * 2 / 16; i += TC_THREADS)
             reinterpret_cast<uint4 *>(sa)[i] = make_uint4(0u, 0u, 0u, 0u);
-    // output pixel p -> {b Hin, oy s - pad, ox s - pad, exists}
+    // t / ng and t / (N / 8) for t < 8 ng and t < N as multiply-shifts (exact in those ranges)
+    const u32 ng_inv = (65536u + ng - 1) / ng, nh_inv = (65536u + (N >> 3) - 1) / (N >> 3);
+    // output pixel p -> {offset of its window's corner (oy s - pad, ox s - pad), mask of its taps
+    // inside the picture}; {0, 0} past n
     auto out_pixel = [&](int p, int n) {
-        if (p >= n) return make_int4(0, 0, 0, 0);
+        if (p >= n) return make_int2(0, 0);
         const int hw = S.Hout * S.Wout, b = p / hw, rr = p - b * hw, oy = rr / S.Wout, ox = rr - oy * S.Wout;
-        return make_int4(b * S.Hin, oy * S.stride - S.pad, ox * S.stride - S.pad, 1);
+        const int y0 = oy * S.stride - S.pad, x0 = ox * S.stride - S.pad;
+        // the taps inside are the rows ky in [ylo, yhi] x the columns kx in [xlo, xhi]
+        const int ylo = max(0, -y0), yhi = min(S.ks - 1, S.Hin - 1 - y0);
+        const int xlo = max(0, -x0), xhi = min(S.ks - 1, S.Win - 1 - x0);
+        const int cols = ((1 << (xhi + 1)) - 1) & ~((1 << xlo) - 1);
+        int mask = 0;
+        for (int ky = ylo; ky <= yhi; ky++) mask |= cols << (ky * S.ks);
+        return make_int2(((b * S.Hin + y0) * S.Win + x0) * S.Cin, xlo <= xhi ? mask : 0);
+    };
+    // column k of x_col (tap, input channel) -> {delta from the window's corner, tap}; tap 31 past K
+    auto tap_col = [&](int k) {
+        if (k >= S.K) return make_int2(0, 31);
+        const int tap = k / S.Cin, c = k - tap * S.Cin, ky = tap / S.ks, kx = tap - ky * S.ks;
+        return make_int2((ky * S.Win + kx) * S.Cin + c, tap);
     };
     {
         const int row = r0 + tid;   // TC_THREADS == TC_M: one row per thread
@@ -156,19 +176,22 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
             if (row < M) {
                 const int hw = Hc * Wc, b = row / hw, rr = row - b * hw, j = rr / Wc, i = rr - j * Wc;
                 const int iy = (j << sshift) + py, ix = (i << sshift) + px;
-                s_row[tid] = make_int4(b * S.Hout, iy + S.pad, ix + S.pad, 1);
+                // the class's taps reach output pixel (ay - ky / s, ax - kx / s), s = 1 or 2
+                const int ay = (iy + S.pad) >> sshift, ax = (ix + S.pad) >> sshift;
+                int mask = 0;
+                for (int ky = ky0; ky < S.ks; ky += S.stride)
+                    for (int kx = kx0; kx < S.ks; kx += S.stride) {
+                        const int oy = ay - (ky >> sshift), ox = ax - (kx >> sshift);
+                        if (oy >= 0 && oy < S.Hout && ox >= 0 && ox < S.Wout) mask |= 1 << (ky * S.ks + kx);
+                    }
+                s_row[tid] = make_int2(((b * S.Hout + ay) * S.Wout + ax) * S.Cout, mask);
                 s_pix[tid] = (b * S.Hin + iy) * S.Win + ix;
             } else {
-                s_row[tid] = make_int4(0, 0, 0, 0);
+                s_row[tid] = make_int2(0, 0);
                 s_pix[tid] = -1;
             }
         } else {
-            if (row < S.K) {
-                const int tap = row / S.Cin, ci = row - tap * S.Cin, ky = tap / S.ks;
-                s_row[tid] = make_int4(ky, tap - ky * S.ks, ci, 1);
-            } else {
-                s_row[tid] = make_int4(0, 0, 0, 0);
-            }
+            s_row[tid] = tap_col(row);
         }
     }
 
@@ -177,23 +200,21 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
         const int kq = kc >> 3;                    // 8-column groups
         // the chunk's column table (the previous chunk's MMAs have completed: see the wait below)
         if (MODE == 2) {
-            for (int j = tid; j < kc; j += TC_THREADS) s_col[j] = out_pixel(kb + k0 + j, npix);
+            for (int j = tid; j < kc; j += TC_THREADS) {
+                const int2 P = out_pixel(kb + k0 + j, npix);
+                s_col[j] = make_int4(P.x, P.y, 0, 0);
+            }
         } else if (MODE == 1) {
             if (tid < kq) {
                 const int k = k0 + 8 * tid, t = k / S.Cout, co = k - t * S.Cout, tyi = t / nkx;
                 const int ky = ky0 + (tyi << sshift), kx = kx0 + ((t - tyi * nkx) << sshift);
-                s_col[tid] = make_int4(ky, kx, co, 0);
+                s_col[tid] = make_int4(-((ky >> sshift) * S.Wout + (kx >> sshift)) * S.Cout + co, ky * S.ks + kx, co, 0);
             }
         } else {
             const int per = vec ? 8 : 2;           // columns per table entry
             for (int j = tid; j < kc / per; j += TC_THREADS) {
-                const int k = k0 + per * j;
-                if (k < S.K) {
-                    const int tap = k / S.Cin, c = k - tap * S.Cin, ky = tap / S.ks;
-                    s_col[j] = make_int4(ky, tap - ky * S.ks, c, 1);
-                } else {
-                    s_col[j] = make_int4(0, 0, 0, 0);
-                }
+                const int2 D = tap_col(k0 + per * j);
+                s_col[j] = make_int4(D.x, D.y, 0, 0);
             }
         }
         __syncthreads();
@@ -202,8 +223,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
         // fill one 128-byte core matrix.  MODE 2 (MN-major): unit u = 8 rows of one column.
         {
             const int nunits = MODE == 2 ? ng * kc : TC_M * kq;
-            uint4 va[8];
-            u32 off[8];
             // MODE 0 / 1 with kq = 2, 4 or 8 (kq divides 16): unit u = tid + 128 i has the column group
             // (tid / 8) % kq for every i and row (tid % 8) + 8 ((tid / 8) / kq) + i (128 / kq), so the
             // column entry is read once
@@ -211,76 +230,67 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
             const int lkq = 31 - __clz(kq);
             const int qf = (tid >> 3) & (kq - 1);
             const int4 Cq = s_col[qfix ? qf : 0];
+            // units are loaded in batches of UB before they are stored (the weight gradient's
+            // units hold more state: 4 keep it within the registers of 7 CTAs per SM)
+            constexpr int UB = MODE == 2 ? 4 : 8;
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const int u = tid + i * TC_THREADS;
-                va[i] = make_uint4(0, 0, 0, 0);
-                off[i] = 0;
-                if (u >= nunits) continue;
-                const int r = qfix ? (tid & 7) + 8 * ((tid >> 3) >> lkq) + (i << (7 - lkq)) : (u & 7) + 8 * ((u >> 3) / kq);
-                const int q = qfix ? qf : (u >> 3) % kq;
-                if (MODE == 0) {
-                    const int4 R = s_row[r];
-                    off[i] = umma_tile_off(r, 8 * q, kc);
-                    if (vec) {
-                        const int4 Cc = qfix ? Cq : s_col[q];
-                        const int iy = R.y + Cc.x, ix = R.z + Cc.y;
-                        if ((R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win)
-                            va[i] = *reinterpret_cast<const uint4 *>(T.src + ((size_t)(R.x + iy) * S.Win + ix) * S.Cin + Cc.z);
-                    } else {
-                        u32 v[4];
+            for (int i0 = 0; i0 < 8; i0 += UB) {
+                uint4 va[UB];
+                u32 off[UB];
 #pragma unroll
-                        for (int e = 0; e < 4; e++) {
-                            const int4 Cc = s_col[4 * q + e];
-                            const int iy = R.y + Cc.x, ix = R.z + Cc.y;
-                            v[e] = (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
-                                       ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(R.x + iy) * S.Win + ix) * S.Cin + Cc.z)
-                                       : 0u;
+                for (int j = 0; j < UB; j++) {
+                    const int i = i0 + j, u = tid + i * TC_THREADS;
+                    va[j] = make_uint4(0, 0, 0, 0);
+                    off[j] = 0;
+                    if (u >= nunits) continue;
+                    if (MODE != 2) {
+                        const int r = qfix ? (tid & 7) + 8 * ((tid >> 3) >> lkq) + (i << (7 - lkq)) : (u & 7) + 8 * ((u >> 3) / kq);
+                        const int q = qfix ? qf : (u >> 3) % kq;
+                        const int2 R = s_row[r];
+                        off[j] = umma_tile_off(r, 8 * q, kc);
+                        if (vec) {
+                            const int4 Cc = qfix ? Cq : s_col[q];
+                            if ((R.y >> Cc.y) & 1) va[j] = *reinterpret_cast<const uint4 *>(T.src + (R.x + Cc.x));
+                        } else {
+                            // MODE 0 with Cin not a multiple of 8: column pairs (two channels of one tap)
+                            u32 v[4];
+#pragma unroll
+                            for (int e = 0; e < 4; e++) {
+                                const int4 Cc = s_col[4 * q + e];
+                                v[e] = (R.y >> Cc.y) & 1 ? *reinterpret_cast<const u32 *>(T.src + (R.x + Cc.x)) : 0u;
+                            }
+                            va[j] = make_uint4(v[0], v[1], v[2], v[3]);
                         }
-                        va[i] = make_uint4(v[0], v[1], v[2], v[3]);
-                    }
-                } else if (MODE == 1) {
-                    const int4 R = s_row[r], Cc = qfix ? Cq : s_col[q];
-                    off[i] = umma_tile_off(r, 8 * q, kc);
-                    // the output pixel that read input pixel R through tap (ky, kx); the class
-                    // makes ty and tx multiples of the stride
-                    const int ty = R.y - Cc.x, tx = R.z - Cc.y;
-                    const int oy = ty >> sshift, ox = tx >> sshift;
-                    if (R.w && ty >= 0 && tx >= 0 && oy < S.Hout && ox < S.Wout)
-                        va[i] = *reinterpret_cast<const uint4 *>(T.src + ((size_t)(R.x + oy) * S.Wout + ox) * S.Cout + Cc.z);
-                } else {
-                    const int kk = u & 7, t8 = u >> 3, kg = t8 / ng, g = t8 - kg * ng, k = 8 * kg + kk;
-                    const int4 Cc = s_col[k];
-                    off[i] = (u32)((k >> 3) * (TC_M * 16) + g * 128 + kk * 16);
-                    if (vec && 8 * g == rowK) {
-                        // K is a multiple of 8 here: the ones row starts a group of 8 rows
-                        va[i] = make_uint4(Cc.w ? 0x3F80u : 0u, 0u, 0u, 0u);
-                    } else if (vec) {
-                        const int4 R = s_row[8 * g];
-                        const int iy = Cc.y + R.x, ix = Cc.z + R.y;
-                        if ((R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win)
-                            va[i] = *reinterpret_cast<const uint4 *>(T.src + ((size_t)(Cc.x + iy) * S.Win + ix) * S.Cin + R.z);
                     } else {
-                        // row pairs (2e, 2e + 1) are channels (ci, ci + 1) of one tap (Cin and K
-                        // are even): one 4-byte load each; the ones row K is the low half of a pair
-                        u32 v[4];
+                        const int kk = u & 7, t8 = u >> 3, kg = (int)(((u32)t8 * ng_inv) >> 16), g = t8 - kg * ng;
+                        const int k = 8 * kg + kk;
+                        const int4 Cc = s_col[k];
+                        off[j] = (u32)(kg * (TC_M * 16) + g * 128 + kk * 16);
+                        if (vec && 8 * g == rowK) {
+                            // K is a multiple of 8 here: the ones row starts a group of 8 rows
+                            va[j] = make_uint4(Cc.y ? 0x3F80u : 0u, 0u, 0u, 0u);
+                        } else if (vec) {
+                            const int2 R = s_row[8 * g];
+                            if ((Cc.y >> R.y) & 1) va[j] = *reinterpret_cast<const uint4 *>(T.src + (Cc.x + R.x));
+                        } else {
+                            // row pairs (2e, 2e + 1) are channels (ci, ci + 1) of one tap (Cin and K
+                            // are even): one 4-byte load each; the ones row K is the low half of a pair
+                            u32 v[4];
 #pragma unroll
-                        for (int e = 0; e < 4; e++) {
-                            const int rr = 8 * g + 2 * e;
-                            const int4 R = s_row[rr];
-                            const int iy = Cc.y + R.x, ix = Cc.z + R.y;
-                            v[e] = rr == rowK ? (Cc.w ? 0x3F80u : 0u)
-                                   : (R.w & Cc.w) && iy >= 0 && iy < S.Hin && ix >= 0 && ix < S.Win
-                                       ? *reinterpret_cast<const u32 *>(T.src + ((size_t)(Cc.x + iy) * S.Win + ix) * S.Cin + R.z)
-                                       : 0u;
+                            for (int e = 0; e < 4; e++) {
+                                const int rr = 8 * g + 2 * e;
+                                const int2 R = s_row[rr];
+                                v[e] = rr == rowK ? (Cc.y ? 0x3F80u : 0u)
+                                       : (Cc.y >> R.y) & 1 ? *reinterpret_cast<const u32 *>(T.src + (Cc.x + R.x)) : 0u;
+                            }
+                            va[j] = make_uint4(v[0], v[1], v[2], v[3]);
                         }
-                        va[i] = make_uint4(v[0], v[1], v[2], v[3]);
                     }
                 }
-            }
 #pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (tid + i * TC_THREADS < nunits) *reinterpret_cast<uint4 *>(sa + off[i]) = va[i];
+                for (int j = 0; j < UB; j++)
+                    if (tid + (i0 + j) * TC_THREADS < nunits) *reinterpret_cast<uint4 *>(sa + off[j]) = va[j];
+            }
         }
         // B: N rows x kc columns.  MODE 0: rows of the weight matrix (K-major).  MODE 1: the weights
         // w[co][tap Cin + ci] as they are stored, MN-major (unit = 8 input channels of one (tap,
@@ -301,12 +311,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const TcArgs T)
                     off[i] = umma_tile_off(n, 8 * q, kc);
                     vb[i] = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)n * T.wrow + k0 + 8 * q);
                 } else {
-                    const int kk = u & 7, h = (u >> 3) % nh, k = 8 * ((u >> 3) / nh) + kk;
-                    off[i] = (u32)((k >> 3) * (N * 16) + h * 128 + kk * 16);
+                    const int t8 = u >> 3, kg = (int)(((u32)t8 * nh_inv) >> 16), h = t8 - kg * nh, k = 8 * kg + (u & 7);
+                    off[i] = (u32)(kg * (N * 16) + h * 128 + (u & 7) * 16);
                     if (MODE == 1) {
-                        const int4 Cc = s_col[k >> 3];
-                        vb[i] = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)(Cc.z + kk) * T.wrow +
-                                                                 (Cc.x * S.ks + Cc.y) * S.Cin + 8 * h);
+                        const int4 Cc = s_col[kg];   // {delta, tap, co}
+                        vb[i] = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)(Cc.z + (u & 7)) * T.wrow +
+                                                                 Cc.y * S.Cin + 8 * h);
                     } else {
                         const int m = kb + k0 + k;
                         if (m < npix) vb[i] = *reinterpret_cast<const uint4 *>(T.wmat + (size_t)m * S.Cout + 8 * h);
@@ -515,7 +525,9 @@ static bool conv_shape(int B, int Hin, int Win, int Cin, int Cout, int ks, int s
     S.Kp = Kp;
     return B > 0 && Cin >= 2 && !(Cin & 1) && Cout >= 16 && !(Cout % 8) && Kp >= S.K && !(Kp % 16) &&
            (B * S.Hout * S.Wout) % 16 == 0 && (B * Hin * Win) % 16 == 0 && (ks == 1 || ks == 3) &&
-           (stride == 1 || stride == 2) && (ks * ks * Cout) % 16 == 0;
+           (stride == 1 || stride == 2) && (ks * ks * Cout) % 16 == 0 &&
+           // element offsets are 32-bit
+           (long long)B * Hin * Win * Cin < (1ll << 31) && (long long)B * S.Hout * S.Wout * Cout < (1ll << 31);
 }
 
 }  // namespace uc
@@ -539,7 +551,10 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_fwd(const void *x, const void *w, const
     memset(&T, 0, sizeof(T));
     T.S = S; T.src = (const bf16 *)x; T.wmat = (const bf16 *)w; T.wrow = Kp; T.bias = bias;
     T.dst = y; T.dst_f32 = y_f32; T.relu = relu;
-    k_conv_tc<0><<<(M + TC_M - 1) / TC_M, TC_THREADS, 0, (cudaStream_t)stream>>>(T);
+    if (Cin % 8 == 0)
+        k_conv_tc<0, true><<<(M + TC_M - 1) / TC_M, TC_THREADS, 0, (cudaStream_t)stream>>>(T);
+    else
+        k_conv_tc<0, false><<<(M + TC_M - 1) / TC_M, TC_THREADS, 0, (cudaStream_t)stream>>>(T);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     return UC_OK;
@@ -571,7 +586,7 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_dgrad(const void *dy, const void *w, co
         T.cls_tile0[c + 1] = T.cls_tile0[c] + (rows + TC_M - 1) / TC_M;
     }
     if (T.cls_tile0[T.ncls] == 0) return set_status(UC_ERR_ARG, "cnn_conv_dgrad: shape");
-    k_conv_tc<1><<<T.cls_tile0[T.ncls], TC_THREADS, 0, st>>>(T);
+    k_conv_tc<1, true><<<T.cls_tile0[T.ncls], TC_THREADS, 0, st>>>(T);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     return UC_OK;
@@ -602,7 +617,10 @@ UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_wgrad(const void *dy, const void *x, fl
     T.wg_chunk = WG_CHUNK;
     while (T.wg_chunk > 64 && rowtiles * ((M + T.wg_chunk - 1) / T.wg_chunk) < 4 * sms) T.wg_chunk >>= 1;
     dim3 grid(rowtiles, (M + T.wg_chunk - 1) / T.wg_chunk);
-    k_conv_tc<2><<<grid, TC_THREADS, 0, st>>>(T);
+    if (Cin % 8 == 0)
+        k_conv_tc<2, true><<<grid, TC_THREADS, 0, st>>>(T);
+    else
+        k_conv_tc<2, false><<<grid, TC_THREADS, 0, st>>>(T);
     UC_CHECK(cudaGetLastError());
     count_launch(1);
     return UC_OK;
