@@ -752,7 +752,10 @@ UAVS3E_CUDA_API int uavs3e_cuda_quant_wq_device(const uavs3e_cuda_rdoq_req_t *d_
  * accumulation in tensor memory); all pointers are device memory.  Activations NHWC bf16;
  * weights [Cout][Kp] bf16 (k = (ky * ks + kx) * Cin + ci, Kp = ks*ks*Cin rounded up to 16);
  * biases, gradients and Adam state FP32.  Shapes: Cin even (a multiple of 16 for dgrad), Cout a
- * multiple of 16 up to 64, batch x output pixels a multiple of 16, ks 1 or 3 (padding ks/2). */
+ * multiple of 16 up to 64, batch x output pixels a multiple of 16, ks 1 or 3 (padding ks/2),
+ * stride 1 or 2, fewer than 2^31 elements per activation tensor.  The activation, weight and
+ * output tensors start on 16-byte boundaries (they are read and written 8 channels at a time);
+ * UC_ERR_ARG otherwise. */
 
 /* y = act(conv(x, w) + bias): y bf16, or FP32 when y_f32; relu 0/1. */
 UAVS3E_CUDA_API int uavs3e_cuda_cnn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int y_f32,

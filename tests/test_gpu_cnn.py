@@ -202,3 +202,35 @@ def test_conv_layer_matches_oracle(gpu, B, H, Cin, Cout, ks, stride):
     if need_dx:
         assert rel(d_dx.float().cpu().numpy(), dx_ref) < 1e-2
     assert L.uavs3e_cuda_cnn_timeouts() == 0
+
+
+def test_conv_rejects_bad_shapes_and_alignment(gpu):
+    """shapes outside the kernels' rules and tensors off a 16-byte boundary are refused before
+    any launch"""
+    import torch
+    from uavs3e_gb300 import cnn
+    L = gpu.lib()
+    cnn._declare(L)
+    B, H, Cin, Cout, ks = 16, 8, 16, 32, 3
+    Kp = cnn.kpad(Cin, ks)
+    x = torch.zeros(B * H * H * Cin + 8, dtype=torch.bfloat16, device="cuda")
+    w = torch.zeros(Cout * Kp, dtype=torch.bfloat16, device="cuda")
+    b = torch.zeros(Cout, dtype=torch.float32, device="cuda")
+    y = torch.zeros(B * H * H * Cout, dtype=torch.bfloat16, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    ok = L.uavs3e_cuda_cnn_conv_fwd(x.data_ptr(), w.data_ptr(), b.data_ptr(), y.data_ptr(), 0, B, H, H, Cin, Cout,
+                                    ks, 2, Kp, 1, st)
+    assert ok == 0
+    # stride 3
+    assert L.uavs3e_cuda_cnn_conv_fwd(x.data_ptr(), w.data_ptr(), b.data_ptr(), y.data_ptr(), 0, B, H, H, Cin, Cout,
+                                      ks, 3, Kp, 1, st) != 0
+    # activations 2 bytes past a 16-byte boundary
+    assert L.uavs3e_cuda_cnn_conv_fwd(x.data_ptr() + 2, w.data_ptr(), b.data_ptr(), y.data_ptr(), 0, B, H, H, Cin,
+                                      Cout, ks, 2, Kp, 1, st) != 0
+    dw = torch.zeros(Cout * Kp, dtype=torch.float32, device="cuda")
+    assert L.uavs3e_cuda_cnn_conv_wgrad(y.data_ptr(), x.data_ptr() + 2, dw.data_ptr(), b.data_ptr(), B, H, H, Cin,
+                                        Cout, ks, 2, Kp, st) != 0
+    # data gradient: output channels not a multiple of 16
+    assert L.uavs3e_cuda_cnn_conv_dgrad(y.data_ptr(), w.data_ptr(), x.data_ptr(), x.data_ptr(), None, B, H, H, Cin,
+                                        24, ks, 2, Kp, st) != 0
+    torch.cuda.synchronize()
