@@ -37,6 +37,7 @@ struct AffMeParams {
     const pel *org;
     int i_org, i_ref, n_slots, W, H, n;
     double sq32, sq128;
+    u64 k32, k128;       // had_scale_k of sq32, sq128
     const AffMeReq *reqs;
     AffMeOut *out;
 };
@@ -98,7 +99,8 @@ __device__ __noinline__ void ame_pred(const AffMeParams &P, const pel *plane, in
 // 2:1 tiles: each pass's group sums move to one lane per tile, and the double normalisation runs
 // once for all (at most 16) tiles of the block instead of once per pass.
 template <int TW, int TH>
-__device__ u32 ame_had_tiles(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128)
+__device__ u32 ame_had_tiles(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128, u64 k32,
+                             u64 k128)
 {
     constexpr int G = 32 / TH;                      // tiles per pass
     const int ntx = w / TW, ntiles = ntx * (h / TH), total = ntiles * TH;
@@ -111,23 +113,23 @@ __device__ u32 ame_had_tiles(const pel *o, const pel *p, int w, int h, int lane,
         const int off = ((tile / ntx) * TH + row) * w + (tile % ntx) * TW;
         const int s = had_tile_sum<TW, TH>(o + off, p + off, active, lane);
         if (TW == TH) {
-            if (active && row == 0) acc += had_tile_norm<TW, TH>(s, sq32, sq128);
+            if (active && row == 0) acc += had_tile_norm<TW, TH>(s, sq32, sq128, k32, k128);
         } else {
             const int got = __shfl_sync(0xffffffffu, s, ((lane - pass * G) * TH) & 31);
             if (lane >= pass * G && lane < pass * G + G) held = got;
         }
     }
-    if (TW != TH && lane < ntiles) acc = had_tile_norm<TW, TH>(held, sq32, sq128);
+    if (TW != TH && lane < ntiles) acc = had_tile_norm<TW, TH>(held, sq32, sq128, k32, k128);
 #pragma unroll
     for (int m = 16; m; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
     return acc;
 }
 
-__device__ __noinline__ u32 ame_had(const pel *o, const pel *p, int w, int h, int lane, double sq32, double sq128)
+__device__ __noinline__ u32 ame_had(const pel *o, const pel *p, int w, int h, int lane, const AffMeParams &P)
 {
-    if (w == h) return ame_had_tiles<8, 8>(o, p, w, h, lane, sq32, sq128);
-    if (w > h) return ame_had_tiles<16, 8>(o, p, w, h, lane, sq32, sq128);
-    return ame_had_tiles<8, 16>(o, p, w, h, lane, sq32, sq128);
+    if (w == h) return ame_had_tiles<8, 8>(o, p, w, h, lane, P.sq32, P.sq128, P.k32, P.k128);
+    if (w > h) return ame_had_tiles<16, 8>(o, p, w, h, lane, P.sq32, P.sq128, P.k32, P.k128);
+    return ame_had_tiles<8, 16>(o, p, w, h, lane, P.sq32, P.sq128, P.k32, P.k128);
 }
 
 // the sums of one gradient step (affine_sobel_flt_hor / _ver and affine_coef_computer,
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(32 * AME_WARPS, 20 / AME_WARPS) k_me_affine(co
         // scaled to 1/16 sample (rounded to whole samples at AMVR index 1), whichever costs less
         ame_pred(P, plane, q.x, q.y, w, h, lw, mvp, sub, sp, lane);
         __syncwarp();
-        const u64 c_mvp = (u64)ame_had(so, sp, w, h, lane, P.sq32, P.sq128) +
+        const u64 c_mvp = (u64)ame_had(so, sp, w, h, lane, P) +
                           ame_mv_cost(q.lambda_mv, ame_bits(mvp, mvp, q.num_refp, q.refi, sh));
         const int x4 = q.x << 2, y4 = q.y << 2, w4 = w << 2, h4 = h << 2;
         const int min_c = (-128 - 4) << 2, max_x = (P.W - 1 + 128 + 4) << 2, max_y = (P.H - 1 + 128 + 4) << 2;
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(32 * AME_WARPS, 20 / AME_WARPS) k_me_affine(co
         __syncwarp();
         ame_pred(P, plane, q.x, q.y, w, h, lw, tmp, sub, sp, lane);
         __syncwarp();
-        const u32 had_tmp = ame_had(so, sp, w, h, lane, P.sq32, P.sq128);
+        const u32 had_tmp = ame_had(so, sp, w, h, lane, P);
         const u64 c_tmp = (u64)had_tmp + ame_mv_cost(q.lambda_mv, ame_bits(tmp, mvp, q.num_refp, q.refi, sh));
         if (c_tmp < c_mvp) {
 #pragma unroll
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(32 * AME_WARPS, 20 / AME_WARPS) k_me_affine(co
         __syncwarp();
         ame_pred(P, plane, q.x, q.y, w, h, lw, mv, sub, sp, lane);
         __syncwarp();
-        had = ame_had(so, sp, w, h, lane, P.sq32, P.sq128);
+        had = ame_had(so, sp, w, h, lane, P);
     }
     // affine_me_gradient
     int best_bits = ame_bits(mv, mvp, q.num_refp, q.refi, sh) + other;
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(32 * AME_WARPS, 20 / AME_WARPS) k_me_affine(co
         ame_pred(P, plane, q.x, q.y, w, h, lw, mvt, sub, sp, lane);
         __syncwarp();
         const int bits = ame_bits(mvt, mvp, q.num_refp, q.refi, sh) + other;
-        const u64 cost = (u64)ame_mv_cost(q.lambda_mv, bits) + (ame_had(so, sp, w, h, lane, P.sq32, P.sq128) >> bi);
+        const u64 cost = (u64)ame_mv_cost(q.lambda_mv, bits) + (ame_had(so, sp, w, h, lane, P) >> bi);
         if (cost < best) {
             best = cost;
             best_bits = bits;
@@ -404,6 +406,8 @@ int launch_me_affine(int W, int H, const pel *org, int i_org, const pel *const *
     P.org = org; P.i_org = i_org; P.i_ref = i_ref; P.n_slots = n_slots; P.W = W; P.H = H; P.n = n;
     P.sq32 = sqrt(32.0);
     P.sq128 = sqrt(128.0);
+    P.k32 = had_scale_k(P.sq32);
+    P.k128 = had_scale_k(P.sq128);
     P.reqs = (const AffMeReq *)reqs;
     P.out = (AffMeOut *)out;
     prof_begin(PROF_AFFME, st);

@@ -112,6 +112,23 @@ __device__ __forceinline__ void load_diff(int *d, const pel *o, int io, const pe
         for (int c = 0; c < N; c++) d[r * N + c] = (int)o[r * io + c] - (int)p[r * ip + c];
 }
 
+// com_had's normalisation of a 2:1 tile, (int)((double)s / sq * 2.0) for s >= 0 and sq = the
+// host's sqrt(128) (16x8 / 8x16 tiles) or sqrt(32) (8x4 / 4x8), src/com_cost.c:344-710.  With
+// k = had_scale_k(sq) = round(2^41 / sq), s k / 2^40 equals 2 s / sq to within 2^-17 for
+// s < 2^23, so wherever its fraction lies at least 2^-16 from an integer its integer part is the
+// double expression's value (a unit test checks every s < 2^23); the products nearer an integer
+// (about 3 in 10^5) and larger s take the double expression itself.  A double division costs far
+// more on this GPU than the 64-bit multiply.
+__host__ __device__ __forceinline__ u64 had_scale_k(double sq) { return (u64)(2199023255552.0 / sq + 0.5); }
+
+__device__ __forceinline__ u32 had_scale(int s, double sq, u64 k)
+{
+    const u64 prod = (u64)(u32)s * k;
+    const u64 frac = prod & ((1ull << 40) - 1);
+    if ((u32)s < (1u << 23) && frac >= (1ull << 24) && frac <= (1ull << 40) - (1ull << 24)) return (u32)(prod >> 40);
+    return (u32)(int)((double)s / sq * 2.0);
+}
+
 // Hadamard SATD of a tw x th tile (com_had_4x4/8x8/16x8/8x16/8x4/4x8, src/com_cost.c:176-710).
 // The 16-point (8-point) transform of a [left|right] row is [H(l)+H(r), H(l)-H(r)], so a
 // 16x8 tile's coefficient magnitudes are |A+B| and |A-B| for the 8x8 transforms A, B of its
@@ -223,17 +240,17 @@ __device__ __forceinline__ int had_tile_sum(const pel *o, const pel *p, bool act
 // com_had's normalisation of a tile's magnitude sum: 4x4 (s+1)>>1, 8x8 (s+2)>>2, 2:1 tiles
 // (int)(s / sqrt(w h) * 2.0) in double
 template <int TW, int TH>
-__device__ __forceinline__ u32 had_tile_norm(int s, double sq32, double sq128)
+__device__ __forceinline__ u32 had_tile_norm(int s, double sq32, double sq128, u64 k32, u64 k128)
 {
     if (TW == TH) return (u32)(TW == 8 ? (s + 2) >> 2 : (s + 1) >> 1);
-    return (u32)(int)((double)s / (TW * TH == 128 ? sq128 : sq32) * 2.0);
+    return TW * TH == 128 ? had_scale(s, sq128, k128) : had_scale(s, sq32, k32);
 }
 
 template <int TW, int TH>
 __device__ __forceinline__ u32 had_tile_rows(const pel *o, int io, const pel *p, int ip, bool active, int lane,
-                                            double sq32, double sq128)
+                                            double sq32, double sq128, u64 k32, u64 k128)
 {
-    return had_tile_norm<TW, TH>(had_tile_sum<TW, TH>(o, p, active, lane), sq32, sq128);
+    return had_tile_norm<TW, TH>(had_tile_sum<TW, TH>(o, p, active, lane), sq32, sq128, k32, k128);
 }
 
 

@@ -293,6 +293,7 @@ int launch_intra_lattice(const pel *org, int i_org, const pel *rec, int i_rec, i
     P.satd_out = satd_out; P.q_out = q_out;
     P.modes = modes; P.n_modes = n_modes;
     P.sq32 = sqrt(32.0); P.sq128 = sqrt(128.0);
+    P.k32 = had_scale_k(P.sq32); P.k128 = had_scale_k(P.sq128);
     for (int l = 0; l < 7; l++) {
         P.fold[l] = tab->fold[l];
         for (int m = 0; m < 7; m++) P.scanpos[l][m] = tab->scanpos[l][m];

@@ -150,6 +150,7 @@ struct LatParams {
     int n_modes;
     int budget[LAT_SHAPES];   // dynamic shared bytes of each shape class's layout (lat_layout)
     double sq32, sq128;
+    u64 k32, k128;       // had_scale_k of sq32, sq128
     // the device work queue (written by k_lat_plan for each launch)
     const int *counts;        // [LAT_SHAPES] CUs per shape class
     const int *cu_off;        // [LAT_SHAPES] first entry of each class in perm
@@ -272,7 +273,7 @@ constexpr int lat_th(int w, int h)
 template <int TW, int TH>
 __device__ __forceinline__ void lat_satd_tiles(int n_tiles, int lnt, int ntx, const u8 *cub, int cu_bytes, int c_org,
                                                const u8 *jobb, int job_bytes, int j_pred, int ps, int MCv,
-                                               u32 *s_satd, double sq32, double sq128)
+                                               u32 *s_satd, double sq32, double sq128, u64 k32, u64 k128)
 {
     constexpr int R = (TW == 4 || TH == 4) ? 4 : 8;
     constexpr bool PAIR = TW != TH, SIDE = TW > TH;
@@ -317,7 +318,7 @@ __device__ __forceinline__ void lat_satd_tiles(int n_tiles, int lnt, int ntx, co
         if (act && k == 0) {
             u32 v;
             if (!PAIR) v = R == 8 ? (u32)((sum + 2) >> 2) : (u32)((sum + 1) >> 1);
-            else v = (u32)(int)((double)sum / (R == 8 ? sq128 : sq32) * 2.0);
+            else v = R == 8 ? had_scale(sum, sq128, k128) : had_scale(sum, sq32, k32);
             atomicAdd(&s_satd[j], v);
         }
     }
@@ -500,7 +501,7 @@ __device__ __forceinline__ void lat_tile(const LatParams &P, const int *perm, in
         constexpr int TW = lat_tw(1 << LW, 1 << LH), TH = lat_th(1 << LW, 1 << LH);
         constexpr int lnt = LW + LH - (TW == 16 ? 4 : TW == 8 ? 3 : 2) - (TH == 16 ? 4 : TH == 8 ? 3 : 2);
         lat_satd_tiles<TW, TH>(J << lnt, lnt, (1 << LW) / TW, cub, L.cu_bytes, L.c_org, jobb, L.job_bytes, L.j_pred, L.ps,
-                               MCv, s_satd, P.sq32, P.sq128);
+                               MCv, s_satd, P.sq32, P.sq128, P.k32, P.k128);
     }
     {
         const int sh1 = lw - 2, rnd1 = sh1 > 0 ? 1 << (sh1 - 1) : 0;

@@ -591,6 +591,7 @@ struct MeSubParams {
     int lo_x, lo_y, ndx;
     u32 lambda_mv;
     double sq32, sq128;
+    u64 k32, k128;       // had_scale_k of sq32, sq128
     const u64 *keys;
     u32 *satd1;          // [item][9]
     u32 *satd2;          // [item][8]
@@ -733,18 +734,6 @@ __device__ __noinline__ int satd8x8_raw(const pel *o, int io, const pel *p, int 
     return 2 * s;
 }
 
-// com_had tile SATD for the ME tile shapes 8x8 / 16x8 / 8x16.  For 16x8 (8x16) the 16-point
-// transform's first stage forms left+right and left-right (top+bottom, top-bottom); the
-// magnitude sum is the sum of the two 8x8 transforms of those.
-__device__ __forceinline__ u32 me_tile_satd(int tw, int th, const pel *o, int io, const pel *p, int ip, double sq128)
-{
-    if (tw == 8 && th == 8) return (u32)((satd8x8_raw(o, io, p, ip, nullptr, nullptr, 0) + 2) >> 2);
-    const int bo = tw == 16 ? 8 : 8 * io, bp = tw == 16 ? 8 : 8 * ip;
-    int s = satd8x8_raw(o, io, p, ip, o + bo, p + bp, 1);
-    s += satd8x8_raw(o, io, p, ip, o + bo, p + bp, -1);
-    return (u32)(int)((double)s / sq128 * 2.0);
-}
-
 // Refinement work items: one per (reference, com_had tile position, tile class).  The tile
 // classes are 8x8 (tiles of the square blocks 8x8 .. 64x64), 16x8 (16x8, 32x16, 64x32) and 8x16
 // (8x16, 16x32, 32x64); a tile of a class lies in exactly one block of each of the class's
@@ -792,6 +781,9 @@ __device__ __forceinline__ void decode_sub_item(const MeSubParams &P, int it, Su
     }
 }
 
+// com_had tile SATD of the item's tile against prediction pb.  For 16x8 (8x16) the 16-point
+// transform's first stage forms left+right and left-right (top+bottom, top-bottom); the
+// magnitude sum is the sum of the two 8x8 transforms of those.
 __device__ __forceinline__ u32 sub_tile_satd(const MeSubParams &P, const SubItem &I, const pel *pb)
 {
     const pel *ob = P.org + (long long)I.py * P.i_org + I.px;
@@ -799,7 +791,7 @@ __device__ __forceinline__ u32 sub_tile_satd(const MeSubParams &P, const SubItem
     const int bo = I.cls == 1 ? 8 : 8 * P.i_org, bp = I.cls == 1 ? 8 : 8 * P.i_ref;
     int s = satd8x8_raw(ob, P.i_org, pb, P.i_ref, ob + bo, pb + bp, 1);
     s += satd8x8_raw(ob, P.i_org, pb, P.i_ref, ob + bo, pb + bp, -1);
-    return (u32)(int)((double)s / P.sq128 * 2.0);
+    return had_scale(s, P.sq128, P.k128);
 }
 
 template <int STAGE>
@@ -1010,6 +1002,7 @@ int launch_me_frame(const MeFrameArgs &a, const MeTables &t, u64 *keys, cudaStre
     S.i_ref = a.i_ref; S.W = a.W; S.H = a.H; S.ctus_w = ctus_w; S.n_ctu = ctus_w * ctus_h; S.n_refs = a.n_refs;
     S.lo_x = t.lo_x; S.lo_y = t.lo_y; S.ndx = t.ndx; S.lambda_mv = a.lambda_mv;
     S.sq32 = sqrt(32.0); S.sq128 = sqrt(128.0);
+    S.k32 = had_scale_k(S.sq32); S.k128 = had_scale_k(S.sq128);
     S.keys = keys; S.out = a.out; S.ctl = P.ctl;
     const long long items = (long long)S.n_ctu * ME_BLOCKS_PER_CTU * a.n_refs;
     S.satd1 = a.sub_scratch;

@@ -44,6 +44,7 @@ struct TzParams {
     int n;
     TzOut *out;
     double sq32, sq128;
+    u64 k32, k128;       // had_scale_k of sq32, sq128
 };
 
 // search_diamond's ring points (src/me.c:307-331) at MV resolution <= integer: step 4, 8, 16
@@ -244,7 +245,8 @@ __device__ void tz_had_batch(const TzS &S, const TzParams &P, int slot, int bx, 
         int vx, vy;
         tz_sub_mv(pattern, k, cx, cy, vx, vy);
         const pel *p = tz_mc_ptr(P, slot, bx + vx, by + vy) + oy * P.i_ref + ox;
-        const u32 v = had_tile_rows<TW, TH>(ob + oy * S.w + ox, S.w, p, P.i_ref, active, lane, P.sq32, P.sq128);
+        const u32 v = had_tile_rows<TW, TH>(ob + oy * S.w + ox, S.w, p, P.i_ref, active, lane, P.sq32, P.sq128,
+                                             P.k32, P.k128);
         if (active && row == 0) atomicAdd(&sum[k], v);
     }
 }
@@ -423,6 +425,7 @@ int launch_me_tz(const uavs3e_cuda_tz_pic_t *pic, const pel *org, int i_org, con
     P.mto = (std::max(pic->width, pic->height) << 2) + 3;
     P.reqs = (const TzReq *)reqs; P.n = n; P.out = (TzOut *)out;
     P.sq32 = sqrt(32.0); P.sq128 = sqrt(128.0);
+    P.k32 = had_scale_k(P.sq32); P.k128 = had_scale_k(P.sq128);
     prof_begin(PROF_TZ, st);
     k_me_tz<<<(unsigned)((n + TZ_WARPS - 1) / TZ_WARPS), 32 * TZ_WARPS, 0, st>>>(P);
     UC_CHECK(cudaGetLastError());
