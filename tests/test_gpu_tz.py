@@ -92,6 +92,17 @@ def test_tz_1080p_batch(gpu, oracle):
 
 
 @pytest.mark.gpu
+def test_tz_repeatable(gpu, oracle):
+    """the same calls three times give byte-identical results (each warp's search depends only on
+    its request: no cross-warp state, integer atomics only)"""
+    p = cases.TZ_CASES[0]
+    q = dict(p, n=512)
+    pic, org, keep, addrs, stride, reqs = cases.tz_inputs(oracle, q, 321)
+    runs = [_gpu_tz(gpu, pic, org, keep, stride, reqs).tobytes() for _ in range(3)]
+    assert runs[0] == runs[1] == runs[2]
+
+
+@pytest.mark.gpu
 def test_tz_rejects_bad_arguments(gpu):
     import torch
     d = torch.zeros(1 << 20, dtype=torch.uint8, device="cuda")
