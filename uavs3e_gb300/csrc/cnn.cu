@@ -50,7 +50,7 @@ constexpr int TC_KC = 64;        // columns of K gathered per chunk
 constexpr int TC_THREADS = 128;
 constexpr int WG_CHUNK = 512;    // most output pixels per CTA of the weight gradient
 constexpr uint32_t TC_POLLS = 1u << 22;
-// the static shared memory of a CTA (operand tiles and index tables, over 27 KB) lets at most 8
+// the static shared memory of a CTA (operand tiles and index tables, about 26 KB) lets at most 8
 // CTAs share an SM (228 KB, plus 1 KB per CTA for the system): their TMEM accumulators (at most
 // 64 columns each) then always fit the SM's 512 columns and no CTA waits in its allocation
 constexpr int TC_STATIC_SMEM = TC_M * TC_KC * 2 + 64 * TC_KC * 2 + TC_M * 8 + TC_KC * 16;
