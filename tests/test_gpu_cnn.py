@@ -159,6 +159,7 @@ CONV_SHAPES = [  # B, H, Cin, Cout, ks, stride
     (16, 10, 6, 16, 3, 2),
     (16, 7, 2, 16, 3, 1),
     (4, 4, 64, 48, 1, 1),
+    (4, 8, 16, 32, 1, 2),      # 1x1 at stride 2: three phase classes reach no tap (dx = 0 there)
 ]
 
 
